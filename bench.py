@@ -1,0 +1,314 @@
+#!/usr/bin/env python3
+"""Benchmark of the D3Q27 entropic LB level step on GB300.
+
+Workload (one GPU): the learned-alpha boundary-layer case, D3Q27, FP32
+deviation storage, 512x256x256 nodes, inlet u = 0.06, nu = 2e-5, seeded
++-5e-3 velocity noise; flat-plate faces (inlet x=0, outlet x=511, no-slip
+bounce-back wall z=0, freestream z=255, inviscid walls y=0 and y=255).
+A "step" is one fused level step (stream + boundaries + moments + alpha +
+collision) over all 33.5 M nodes.  The populations (7.2 GB) exceed L2
+(129 MB), so every step streams from HBM without an explicit flush.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the step (the reference solver
+is Fortran/AMReX and cannot be built here) on a bounded sample of the same
+workload, with all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "D3Q27 ELBM MLUPS: learned-α vs Newton-α at |ΔH|≤1e-10; % of HBM roofline"
+UNIT = "MLUPS"
+NX, NY, NZ = 512, 256, 256
+U_IN = (0.06, 0.0, 0.0)
+NU = 2e-5
+NOISE = 5e-3
+SEED = 1234 + 5
+BYTES_PER_NODE_FP32 = 216  # 27 x 4 B read + 27 x 4 B written
+BYTES_PER_NODE_FP64 = 432
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return 6800.0, "fallback"
+
+
+def build_workload(pkg):
+    geo = pkg.geometry
+    state = geo.box_state27(NX, NY, NZ, geo.flat_plate_faces())
+    f0 = geo.perturbed_equilibrium(NX, NY, NZ, U_IN, NOISE, seed=SEED)
+    bp = geo.d3q27_boundary_params(U_IN, NU)
+    return state, f0, bp
+
+
+def run_reference(args):
+    """CPU restatement of the step (oracle port) on a bounded sample of the workload."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    from oracle import oracle as orc
+
+    geo = pkg.geometry
+    sx, sy, sz = 128, 64, 64  # sample: a 128x64x64 box of the same boundary-layer case
+    state = geo.box_state27(sx, sy, sz, geo.flat_plate_faces())
+    f = geo.perturbed_equilibrium(sx, sy, sz, U_IN, NOISE, seed=SEED)
+    bp = geo.d3q27_boundary_params(U_IN, NU)
+    p = orc.params(bp["nu"], bp["fs_feq"], bp["inl_feq"], bp["outl_feq"], bp["outlet_type"])
+    for _ in range(args.warmup):
+        f, _, _, _ = orc.step27(state, f, p)
+    t0 = time.perf_counter()
+    nodes = 0
+    for _ in range(args.steps):
+        f, _, _, s = orc.step27(state, f, p)
+        nodes += s["fluid_nodes"]
+    dt = time.perf_counter() - t0
+    mlups = nodes / dt / 1e6
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": mlups, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"D3Q27 boundary layer {NX}x{NY}x{NZ} (sampled {sx}x{sy}x{sz})", "alpha": "newton",
+                   "storage": "fp64"},
+        "cpu_baseline": {"value": mlups, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{sx}x{sy}x{sz} sub-box of the workload, {args.steps} steps, OpenMP"},
+        "e2e": {"value": mlups, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_sample(pkg, budget_s=15.0):
+    """The oracle port timed on the host cores on a bounded sample (rank 0, N = 1)."""
+    from oracle import oracle as orc
+
+    geo = pkg.geometry
+    sx, sy, sz = 128, 64, 64
+    state = geo.box_state27(sx, sy, sz, geo.flat_plate_faces())
+    f = geo.perturbed_equilibrium(sx, sy, sz, U_IN, NOISE, seed=SEED)
+    bp = geo.d3q27_boundary_params(U_IN, NU)
+    p = orc.params(bp["nu"], bp["fs_feq"], bp["inl_feq"], bp["outl_feq"], bp["outlet_type"])
+    f, _, _, _ = orc.step27(state, f, p)  # warm-up
+    t0 = time.perf_counter()
+    steps = nodes = 0
+    while time.perf_counter() - t0 < budget_s and steps < 50:
+        f, _, _, s = orc.step27(state, f, p)
+        nodes += s["fluid_nodes"]
+        steps += 1
+    dt = time.perf_counter() - t0
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": nodes / dt / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{sx}x{sy}x{sz} sub-box of the workload, {steps} FP64 Newton-alpha steps, {dt:.1f} s"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    rank, world, local_rank = dist_env()
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        pg = dist
+    import __graft_entry__ as ge
+
+    ge.build() if rank == 0 or world == 1 else None
+    if pg:
+        pg.barrier()
+    pkg = ge.load_package()
+    cap = pkg.capi
+    state, f0, bp = build_workload(pkg)
+
+    ctx = cap.Context(local_rank)
+    box = [[0, 0, 0, NX - 1, NY - 1, NZ - 1]]
+    ctx.level_register(0, cap.ELBM_D3Q27, cap.ELBM_STORE_FP32_DEV, box)
+    ctx.set_d3q27_params(0, cap.make_d3q27_params(**bp))
+    ctx.set_links(0, 0, state)
+    ctx.upload(0, 0, f0)
+
+    # warm-up, then the timed region: K fused steps, events on the library's stream
+    ctx.step(0, args.warmup, want_stats=False)
+    ctx.sync()
+    if pg:
+        pg.barrier()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    t0 = time.perf_counter()
+    st = ctx.step(0, args.steps)  # synchronises; kernel_ms from CUDA events around the K launches
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    kernel_s = st["kernel_ms"] / 1e3
+    if pg:
+        import torch
+
+        t = torch.tensor([kernel_s], dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        kernel_s = float(t[0])
+    nodes_per_step = st["node_updates"] / args.steps
+    value = nodes_per_step * args.steps * world / kernel_s / 1e6
+    per_launch_s = kernel_s / args.steps
+    peak, peak_kind = measured_peak_hbm()
+    achieved = BYTES_PER_NODE_FP32 * nodes_per_step / per_launch_s / 1e9
+
+    # entropy condition and fallbacks over a validation window (check mode, not timed)
+    chk = cap.make_d3q27_params(**bp)
+    chk.check_dH = 1
+    ctx.set_d3q27_params(0, chk)
+    vst = ctx.step(0, 3)
+    ctx.set_d3q27_params(0, cap.make_d3q27_params(**bp))
+
+    # end to end through the C ABI with host buffers: upload, K steps, download
+    import torch
+
+    host_in = torch.from_numpy(f0).pin_memory()
+    host_out = torch.empty_like(host_in).pin_memory()
+    ctx.sync()
+    te = time.perf_counter()
+    ctx.upload(0, 0, host_in.numpy())
+    ctx.step(0, args.steps, want_stats=False)
+    ctx.download(0, 0, host_out.numpy())
+    e2e_s = time.perf_counter() - te
+    e2e = nodes_per_step * args.steps * world / e2e_s / 1e6
+    h2d = f0.nbytes / args.steps
+    d2h = f0.nbytes / args.steps
+    ctx.close()
+
+    # plain FP64 Newton-alpha path on the same workload (short window; FP64 is 1/60 of FP32 on GB300)
+    fp64 = None
+    if not args.no_fp64:
+        c64 = cap.Context(local_rank)
+        c64.level_register(0, cap.ELBM_D3Q27, cap.ELBM_STORE_FP64, box)
+        c64.set_d3q27_params(0, cap.make_d3q27_params(**bp))
+        c64.set_links(0, 0, state)
+        c64.upload(0, 0, f0)
+        c64.step(0, 1, want_stats=False)
+        s64 = c64.step(0, 2)
+        fp64 = s64["node_updates"] / (s64["kernel_ms"] / 1e3) / 1e6
+        c64.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_sample(pkg)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": per_launch_s * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"D3Q27 boundary layer {NX}x{NY}x{NZ}, FP32 deviation storage, Newton alpha",
+                       "alpha": "newton", "storage": "fp32_dev", "nu": NU, "u_in": U_IN[0], "noise": NOISE,
+                       "l2": "inputs (7.2 GB) larger than L2, no flush", "parallelism": f"replicas x{world}"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                         "bytes_per_node": BYTES_PER_NODE_FP32},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "note": "upload + K steps + download through the C ABI, pinned host FP64 FAB"},
+            "gpu_launches": args.steps,
+            "clocks": clk,
+            "wall_ms_per_step": wall / args.steps * 1e3,
+            "validation": {"max_abs_dH": vst["max_abs_dH"], "fallbacks": vst["fallbacks"],
+                           "exact_path_nodes": vst["exact_path_nodes"], "status": vst["status"],
+                           "newton_iters_per_node": vst["newton_iters"] / max(1, vst["node_updates"])},
+            "plain_fp64_newton_mlups": fp64,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.barrier()
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,132 @@
+/*
+ * elbm_gb300 — C ABI of the GB300 (sm_103a) entropic lattice Boltzmann level step.
+ *
+ * The reference solver (University of Cincinnati Lattice Boltzmann Solver,
+ * Fortran + AMReX) advances one AMR level per call chain
+ *   streaming(level_step,fine,lvl)              looping/timestepping/streaming.f95:1
+ *   calculate_flow_variables(level_step,fine,lvl) looping/timestepping/calculate_flow_variables.f95:1
+ *   collision(level_step,fine,lvl)              looping/timestepping/collision.f95:1
+ *   damp_it(level_step,fine,lvl)                looping/timestepping/damp_it.f95:1
+ * issued from loop (looping/timestepping/loop.f95:94-147) over the boxes of the
+ * level's MultiFabs (amr/modules/amr_info_holder.f95:70-76).  This library
+ * replaces that chain with one fused device pass per level step.  The Fortran
+ * driver keeps its subroutine signatures; their bodies call the functions
+ * below through ISO_C_BINDING (fortran/elbm_gb300_iface.f90).
+ *
+ * Conventions
+ *  - Plain pointers and sizes only.  Host arrays are AMReX FAB layouts: for a
+ *    box lo..hi (inclusive, 0-based or not) with `ngrow` ghost layers the FAB
+ *    spans (hi-lo+1+2*ngrow) nodes per axis, x fastest, then y, z, then the
+ *    component (population) index — exactly mf%dataptr(mfi) of the reference.
+ *  - Every call returns 0 on success or a negative ELBM_E_* code; it never
+ *    aborts (the reference prints and STOPs, general/background_calcs/error_out.f95:12-14).
+ *    elbm_last_error_string() describes the last failure.
+ *  - One CUDA stream per context; a context is not thread-safe.  Steps are
+ *    asynchronous; download and stats calls synchronise.
+ */
+#ifndef ELBM_GB300_H
+#define ELBM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct elbm_ctx elbm_ctx;
+
+/* return codes */
+#define ELBM_OK 0
+#define ELBM_E_ARG -1         /* bad argument (null pointer, size, ncomp) */
+#define ELBM_E_CUDA -2        /* CUDA runtime error */
+#define ELBM_E_UNSUPPORTED -3 /* unsupported link code / configuration */
+#define ELBM_E_STATE -4       /* call out of order (e.g. step before upload) */
+
+/* numerical health flags in elbm_stats.status */
+#define ELBM_ST_NAN 0x1u             /* a density or velocity became NaN/Inf */
+#define ELBM_ST_NEWTON_FALLBACK 0x2u /* some alpha solve fell back (count in .fallbacks) */
+#define ELBM_ST_NEG_POP 0x4u         /* a post-collision population was negative */
+#define ELBM_ST_DH_TOL 0x8u          /* check mode: some |dH| exceeded the tolerance */
+
+/* lattices */
+#define ELBM_D3Q27 27
+#define ELBM_D3Q39 39
+
+/* population storage in HBM */
+#define ELBM_STORE_FP64 0     /* f_i in FP64 */
+#define ELBM_STORE_FP32_DEV 1 /* FP32 deviations d_i = f_i - w_i*rho0, rho0 = 1 */
+
+/* entropic alpha */
+#define ELBM_ALPHA_FIXED2 0  /* alpha = 2 (LBGK limit; calculate_flow_variables.f95:306-311 when turbulent is false) */
+#define ELBM_ALPHA_NEWTON 1  /* Newton from alpha = 2 on H(f) = H(f + alpha*Delta) */
+#define ELBM_ALPHA_LEARNED 2 /* MLP initial guess + at most two Newton polish steps, Newton fallback */
+
+typedef struct {
+  double nu;          /* kinematic viscosity (lattice units); beta = 1/(2 nu/T0 + 1), T0 = 1/3 */
+  double tol_alpha;   /* Newton tolerance on alpha (FP64 path; 1e-12) */
+  double tol_dH;      /* |H(f+alpha Delta) - H(f)| accepted by check mode and by the cap rule (1e-10) */
+  int32_t max_newton; /* iteration cap */
+  int32_t alpha_mode; /* ELBM_ALPHA_* */
+  int32_t check_dH;   /* 1: evaluate |dH| per node in FP64 and report the maximum (validation runs) */
+  int32_t record_alpha; /* 1: keep the per-node alpha of the last step for elbm_download_alpha */
+  int32_t outlet_type[8]; /* per outlet number: 1,4 outlet eq; 2 inlet table; 3 freestream; 6 pure outflow */
+  /* Boundary equilibria, computed by the host like
+   * boundary_conditions/basic_calcs/freestream_basis_calcs.f90 and inlet_outlet_basis_calcs.f90 */
+  double fs_feq[27];
+  double inl_feq[8][27];
+  double outl_feq[8][27];
+} elbm_d3q27_params;
+
+typedef struct {
+  int64_t node_updates;     /* fluid nodes advanced, summed over steps */
+  int64_t newton_iters;     /* total Newton iterations (scalar or per-population) */
+  int64_t exact_path_nodes; /* FP32 path: nodes solved with per-population logarithms */
+  int64_t fallbacks;        /* alpha solves that fell back */
+  uint32_t status;          /* ELBM_ST_* flags */
+  uint32_t pad;
+  double max_abs_dH;        /* check mode only */
+  double kernel_ms;         /* device time of the step kernels (CUDA events) */
+} elbm_stats;
+
+/* Context on one CUDA device. */
+int elbm_create(int device, elbm_ctx** out);
+void elbm_destroy(elbm_ctx* ctx);
+const char* elbm_last_error_string(const elbm_ctx* ctx);
+
+/* Declare a level and its boxes.  Replaces the per-level MultiFab set-up of
+ * from_scratch (amr/modules/amr_processes.f95:383-476).  lo_hi holds 6 ints per
+ * box (lo x,y,z, hi x,y,z, inclusive).  ngrow is the ghost width of the
+ * population FABs the host will pass (nghosts_mid in the reference,
+ * general/background_calcs/directions_and_weights.f95:355-362). */
+int elbm_level_register(elbm_ctx* ctx, int lvl, int lattice, int storage, int nbox, const int32_t* lo_hi,
+                        int ngrow);
+
+/* D3Q27 physical parameters and boundary equilibria of a level. */
+int elbm_set_d3q27_params(elbm_ctx* ctx, int lvl, const elbm_d3q27_params* p);
+
+/* Node types and link codes of one box: the reference's integer `state` FAB
+ * (Q components, ghost width ngrow_state; encoding of looping/timestepping/loop.f95:71-89,
+ * case ranges of streaming.f95:365-481).  Decoded once into a node-type byte
+ * per node and a compact table of boundary links. */
+int elbm_set_links(elbm_ctx* ctx, int lvl, int box, const int32_t* state, int ngrow_state);
+
+/* Copy one box's post-collision populations (fout FAB, FP64, Q comps) to / from the device. */
+int elbm_upload_level(elbm_ctx* ctx, int lvl, int box, const double* fout);
+int elbm_download_level(elbm_ctx* ctx, int lvl, int box, double* fout);
+
+/* Per-node alpha of the last step (valid-box layout without ghosts, FP64). */
+int elbm_download_alpha(elbm_ctx* ctx, int lvl, int box, double* alpha);
+
+/* Advance the level by nsteps fused steps (stream + boundaries + moments +
+ * alpha + collision).  Replaces streaming/calculate_flow_variables/collision
+ * for one level (looping/timestepping/loop.f95:104-139).  stats may be NULL;
+ * when given, the call synchronises and fills it. */
+int elbm_level_step(elbm_ctx* ctx, int lvl, int nsteps, elbm_stats* stats);
+
+/* Wait for all work of the context. */
+int elbm_sync(elbm_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ELBM_GB300_H */

@@ -1,0 +1,55 @@
+"""The C ABI library loads without a GPU, exports every function include/*.h
+declares, and the ctypes structures match the header's layout."""
+import ctypes as ct
+import pathlib
+import re
+import subprocess
+
+ROOT = pathlib.Path(__file__).resolve().parents[1]
+
+
+def declared_functions():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(elbm_\w+)\s*\(", text, flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_header_declares_the_entry_points():
+    names = declared_functions()
+    assert {"elbm_create", "elbm_destroy", "elbm_level_register", "elbm_set_links", "elbm_level_step",
+            "elbm_upload_level", "elbm_download_level", "elbm_last_error_string"} <= names
+
+
+def test_library_exports_every_declared_symbol(pkg, built_lib):
+    lib = ct.CDLL(str(built_lib))
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+    # the ctypes binding covers every declared function
+    assert declared_functions() <= set(pkg.capi.SIGNATURES)
+
+
+def test_struct_layout_matches_header(pkg, tmp_path):
+    cap = pkg.capi
+    src = tmp_path / "layout.c"
+    src.write_text(f"""
+#include <stddef.h>
+#include <stdio.h>
+#include "{ROOT / 'include' / 'elbm_gb300.h'}"
+int main(void) {{
+  printf("%zu %zu %zu %zu %zu\\n", sizeof(elbm_d3q27_params), offsetof(elbm_d3q27_params, outlet_type),
+         offsetof(elbm_d3q27_params, fs_feq), offsetof(elbm_d3q27_params, outl_feq), sizeof(elbm_stats));
+  printf("%zu %zu\\n", offsetof(elbm_stats, status), offsetof(elbm_stats, kernel_ms));
+  return 0;
+}}
+""")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    P, S = cap.D3Q27Params, cap.Stats
+    expect = [ct.sizeof(P), P.outlet_type.offset, P.fs_feq.offset, P.outl_feq.offset, ct.sizeof(S), S.status.offset,
+              S.kernel_ms.offset]
+    assert list(map(int, out)) == expect

@@ -1,0 +1,218 @@
+"""ctypes binding of the C ABI declared in include/elbm_gb300.h.
+
+This is the Python face of the same entry points the Fortran driver binds
+through ISO_C_BINDING (fortran/elbm_gb300_iface.f90).  There is no fallback:
+if libelbm_gb300.so is missing or cannot be loaded, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import pathlib
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+LIB_PATH = HERE / "libelbm_gb300.so"
+
+ELBM_OK = 0
+ELBM_E_ARG = -1
+ELBM_E_CUDA = -2
+ELBM_E_UNSUPPORTED = -3
+ELBM_E_STATE = -4
+
+ELBM_ST_NAN = 0x1
+ELBM_ST_NEWTON_FALLBACK = 0x2
+ELBM_ST_NEG_POP = 0x4
+ELBM_ST_DH_TOL = 0x8
+
+ELBM_D3Q27 = 27
+ELBM_D3Q39 = 39
+ELBM_STORE_FP64 = 0
+ELBM_STORE_FP32_DEV = 1
+ELBM_ALPHA_FIXED2 = 0
+ELBM_ALPHA_NEWTON = 1
+ELBM_ALPHA_LEARNED = 2
+
+# every function the header declares, with its ctypes signature
+_c_int, _c_double, _vp = ct.c_int, ct.c_double, ct.c_void_p
+
+
+class D3Q27Params(ct.Structure):
+    _fields_ = [
+        ("nu", ct.c_double),
+        ("tol_alpha", ct.c_double),
+        ("tol_dH", ct.c_double),
+        ("max_newton", ct.c_int32),
+        ("alpha_mode", ct.c_int32),
+        ("check_dH", ct.c_int32),
+        ("record_alpha", ct.c_int32),
+        ("outlet_type", ct.c_int32 * 8),
+        ("fs_feq", ct.c_double * 27),
+        ("inl_feq", (ct.c_double * 27) * 8),
+        ("outl_feq", (ct.c_double * 27) * 8),
+    ]
+
+
+class Stats(ct.Structure):
+    _fields_ = [
+        ("node_updates", ct.c_int64),
+        ("newton_iters", ct.c_int64),
+        ("exact_path_nodes", ct.c_int64),
+        ("fallbacks", ct.c_int64),
+        ("status", ct.c_uint32),
+        ("pad", ct.c_uint32),
+        ("max_abs_dH", ct.c_double),
+        ("kernel_ms", ct.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad"}
+
+
+SIGNATURES = {
+    "elbm_create": (_c_int, [_c_int, ct.POINTER(_vp)]),
+    "elbm_destroy": (None, [_vp]),
+    "elbm_last_error_string": (ct.c_char_p, [_vp]),
+    "elbm_level_register": (_c_int, [_vp, _c_int, _c_int, _c_int, _c_int, _vp, _c_int]),
+    "elbm_set_d3q27_params": (_c_int, [_vp, _c_int, ct.POINTER(D3Q27Params)]),
+    "elbm_set_links": (_c_int, [_vp, _c_int, _c_int, _vp, _c_int]),
+    "elbm_upload_level": (_c_int, [_vp, _c_int, _c_int, _vp]),
+    "elbm_download_level": (_c_int, [_vp, _c_int, _c_int, _vp]),
+    "elbm_download_alpha": (_c_int, [_vp, _c_int, _c_int, _vp]),
+    "elbm_level_step": (_c_int, [_vp, _c_int, _c_int, ct.POINTER(Stats)]),
+    "elbm_sync": (_c_int, [_vp]),
+}
+
+_lib = None
+
+
+def load(path: pathlib.Path | str | None = None) -> ct.CDLL:
+    """Load libelbm_gb300.so (built in-tree by build.py).  Raises if absent."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = pathlib.Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p.name} is not built; run the package build (nvcc for sm_103a) first")
+    lib = ct.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class ElbmError(RuntimeError):
+    def __init__(self, rc: int, msg: str):
+        super().__init__(f"elbm error {rc}: {msg}")
+        self.rc = rc
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(_vp)
+
+
+def make_d3q27_params(nu, tol_alpha=1e-12, tol_dH=1e-10, max_newton=30, alpha_mode=ELBM_ALPHA_NEWTON, check_dH=0,
+                      record_alpha=0, outlet_type=(1,) * 8, fs_feq=None, inl_feq=None, outl_feq=None) -> D3Q27Params:
+    p = D3Q27Params()
+    p.nu = nu
+    p.tol_alpha = tol_alpha
+    p.tol_dH = tol_dH
+    p.max_newton = max_newton
+    p.alpha_mode = alpha_mode
+    p.check_dH = check_dH
+    p.record_alpha = record_alpha
+    for k in range(8):
+        p.outlet_type[k] = int(list(outlet_type)[k])
+    z = np.zeros(27)
+    fs = np.asarray(fs_feq if fs_feq is not None else z, np.float64)
+    inl = np.asarray(inl_feq if inl_feq is not None else np.zeros((8, 27)), np.float64)
+    outl = np.asarray(outl_feq if outl_feq is not None else np.zeros((8, 27)), np.float64)
+    for j in range(27):
+        p.fs_feq[j] = fs[j]
+        for k in range(8):
+            p.inl_feq[k][j] = inl[k, j]
+            p.outl_feq[k][j] = outl[k, j]
+    return p
+
+
+class Context:
+    """One elbm_ctx (one CUDA device, one stream)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = _vp()
+        rc = self.lib.elbm_create(device, ct.byref(h))
+        if rc != ELBM_OK:
+            raise ElbmError(rc, "elbm_create failed (no usable CUDA device?)")
+        self.h = h
+        self._boxes = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.elbm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc):
+        if rc != ELBM_OK:
+            raise ElbmError(rc, self.lib.elbm_last_error_string(self.h).decode())
+
+    def level_register(self, lvl, lattice, storage, boxes, ngrow=0):
+        lo_hi = np.ascontiguousarray(np.asarray(boxes, np.int32).reshape(-1, 6))
+        self._check(self.lib.elbm_level_register(self.h, lvl, lattice, storage, lo_hi.shape[0], _ptr(lo_hi), ngrow))
+        self._boxes[lvl] = (lo_hi.copy(), ngrow, lattice)
+
+    def box_shape(self, lvl, box=0, ghosts=True):
+        lo_hi, ngrow, _ = self._boxes[lvl]
+        g = ngrow if ghosts else 0
+        lo, hi = lo_hi[box, :3], lo_hi[box, 3:]
+        n = hi - lo + 1 + 2 * g
+        return int(n[2]), int(n[1]), int(n[0])
+
+    def set_d3q27_params(self, lvl, params: D3Q27Params):
+        self._check(self.lib.elbm_set_d3q27_params(self.h, lvl, ct.byref(params)))
+
+    def set_links(self, lvl, box, state: np.ndarray, ngrow_state=0):
+        st = np.ascontiguousarray(state, np.int32)
+        self._check(self.lib.elbm_set_links(self.h, lvl, box, _ptr(st), ngrow_state))
+
+    def upload(self, lvl, box, f: np.ndarray):
+        fa = np.ascontiguousarray(f, np.float64)
+        self._check(self.lib.elbm_upload_level(self.h, lvl, box, _ptr(fa)))
+
+    def download(self, lvl, box=0, out: np.ndarray | None = None) -> np.ndarray:
+        q = self._boxes[lvl][2]
+        if out is None:
+            out = np.zeros((q,) + self.box_shape(lvl, box), np.float64)
+        self._check(self.lib.elbm_download_level(self.h, lvl, box, _ptr(out)))
+        return out
+
+    def download_alpha(self, lvl, box=0) -> np.ndarray:
+        out = np.zeros(self.box_shape(lvl, box, ghosts=False), np.float64)
+        self._check(self.lib.elbm_download_alpha(self.h, lvl, box, _ptr(out)))
+        return out
+
+    def step(self, lvl, nsteps=1, want_stats=True) -> dict | None:
+        if want_stats:
+            st = Stats()
+            self._check(self.lib.elbm_level_step(self.h, lvl, nsteps, ct.byref(st)))
+            return st.as_dict()
+        self._check(self.lib.elbm_level_step(self.h, lvl, nsteps, None))
+        return None
+
+    def sync(self):
+        self._check(self.lib.elbm_sync(self.h))

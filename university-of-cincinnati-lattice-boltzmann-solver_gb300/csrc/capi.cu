@@ -1,0 +1,558 @@
+// C ABI of libelbm_gb300: level registry, link decoding, host<->device copies
+// and the per-level step driver.  Declarations and reference citations live in
+// include/elbm_gb300.h.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/elbm_gb300.h"
+#include "kernels.cuh"
+#include "lattice.cuh"
+
+using namespace elbm;
+
+namespace {
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) {
+      reset();
+      p = o.p;
+      n = o.n;
+      o.p = nullptr;
+      o.n = 0;
+    }
+    return *this;
+  }
+  ~DevBuf() { reset(); }
+  void reset() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t alloc(size_t count) {
+    reset();
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e == cudaSuccess) n = count;
+    else p = nullptr;
+    return e;
+  }
+};
+
+struct Box {
+  int lo[3], hi[3];
+  int nx, ny, nz;
+  int64_t N, plane;
+  DevBuf<uint8_t> buf[2];  // population ping-pong (bytes: FP64 or FP32)
+  int cur = 0;             // buffer holding the latest post-collision state
+  DevBuf<uint8_t> ntype;
+  DevBuf<int32_t> bidx;
+  DevBuf<uint16_t> words;
+  DevBuf<float> alpha;
+  DevBuf<double> staging;  // FP64 packed staging for FP32 conversion
+  int64_t fluid_nodes = 0, boundary_nodes = 0;
+  bool links_set = false, data_set = false;
+};
+
+struct Level {
+  bool registered = false;
+  int lattice = 0, storage = 0, ngrow = 0;
+  std::vector<std::unique_ptr<Box>> boxes;
+  elbm_d3q27_params p27{};
+  bool params_set = false;
+  DevBuf<uint8_t> eq;  // kEqTables x Q, FP64 or FP32 deviations
+};
+
+}  // namespace
+
+struct elbm_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err;
+  std::vector<Level> levels;
+  DevBuf<DevStats> stats;
+};
+
+namespace {
+
+int fail(elbm_ctx* c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+
+int cuda_fail(elbm_ctx* c, cudaError_t e, const char* what) {
+  return fail(c, ELBM_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CUDA_TRY(call, what)                          \
+  do {                                                \
+    cudaError_t e_ = (call);                          \
+    if (e_ != cudaSuccess) return cuda_fail(c, e_, what); \
+  } while (0)
+
+Level* get_level(elbm_ctx* c, int lvl) {
+  if (!c || lvl < 0 || lvl >= (int)c->levels.size() || !c->levels[lvl].registered) return nullptr;
+  return &c->levels[lvl];
+}
+
+Box* get_box(elbm_ctx* c, int lvl, int box, Level** lv_out = nullptr) {
+  Level* lv = get_level(c, lvl);
+  if (!lv || box < 0 || box >= (int)lv->boxes.size()) return nullptr;
+  if (lv_out) *lv_out = lv;
+  return lv->boxes[box].get();
+}
+
+bool node_is_fluid(int32_t s0) {
+  // collision.f95:157-159 skips state < 0, 1000 <= state < 51000, 200 <= state < 299
+  if (s0 < 0) return false;
+  if (s0 >= 1000 && s0 < 51000) return false;
+  if (s0 >= 200 && s0 < 299) return false;
+  return true;
+}
+
+size_t elem_size(int storage) { return storage == ELBM_STORE_FP64 ? sizeof(double) : sizeof(float); }
+
+// ---- conversion kernels between the FP64 host layout and FP32 deviations ----
+__global__ void to_dev32_kernel(const double* __restrict__ f, float* __restrict__ d, int64_t N, int64_t plane) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (n >= N) return;
+  d[(int64_t)j * plane + n] = (float)(f[(int64_t)j * N + n] - w27(j));
+}
+__global__ void from_dev32_kernel(const float* __restrict__ d, double* __restrict__ f, int64_t N, int64_t plane) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y;
+  if (n >= N) return;
+  f[(int64_t)j * N + n] = (double)d[(int64_t)j * plane + n] + w27(j);
+}
+
+// Copy the valid region of a host FAB (ngrow ghosts, ncomp comps) into a
+// packed device array with component stride `plane` (elements of size es).
+template <typename T>
+cudaError_t fab_to_packed(const T* host, T* dev, const Box& b, int ngrow, int ncomp, int64_t plane, cudaStream_t s) {
+  const int fx = b.nx + 2 * ngrow, fy = b.ny + 2 * ngrow, fz = b.nz + 2 * ngrow;
+  if (ngrow == 0) {
+    return cudaMemcpy2DAsync(dev, plane * sizeof(T), host, b.N * sizeof(T), b.N * sizeof(T), ncomp,
+                             cudaMemcpyHostToDevice, s);
+  }
+  for (int q = 0; q < ncomp; ++q) {
+    cudaMemcpy3DParms p{};
+    p.srcPtr = make_cudaPitchedPtr((void*)(host + (int64_t)q * fx * fy * fz), fx * sizeof(T), fx, fy);
+    p.srcPos = make_cudaPos(ngrow * sizeof(T), ngrow, ngrow);
+    p.dstPtr = make_cudaPitchedPtr((void*)(dev + (int64_t)q * plane), b.nx * sizeof(T), b.nx, b.ny);
+    p.dstPos = make_cudaPos(0, 0, 0);
+    p.extent = make_cudaExtent(b.nx * sizeof(T), b.ny, b.nz);
+    p.kind = cudaMemcpyHostToDevice;
+    cudaError_t e = cudaMemcpy3DAsync(&p, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+template <typename T>
+cudaError_t packed_to_fab(const T* dev, T* host, const Box& b, int ngrow, int ncomp, int64_t plane, cudaStream_t s) {
+  const int fx = b.nx + 2 * ngrow, fy = b.ny + 2 * ngrow, fz = b.nz + 2 * ngrow;
+  if (ngrow == 0) {
+    return cudaMemcpy2DAsync(host, b.N * sizeof(T), dev, plane * sizeof(T), b.N * sizeof(T), ncomp,
+                             cudaMemcpyDeviceToHost, s);
+  }
+  for (int q = 0; q < ncomp; ++q) {
+    cudaMemcpy3DParms p{};
+    p.srcPtr = make_cudaPitchedPtr((void*)(dev + (int64_t)q * plane), b.nx * sizeof(T), b.nx, b.ny);
+    p.srcPos = make_cudaPos(0, 0, 0);
+    p.dstPtr = make_cudaPitchedPtr((void*)(host + (int64_t)q * fx * fy * fz), fx * sizeof(T), fx, fy);
+    p.dstPos = make_cudaPos(ngrow * sizeof(T), ngrow, ngrow);
+    p.extent = make_cudaExtent(b.nx * sizeof(T), b.ny, b.nz);
+    p.kind = cudaMemcpyDeviceToHost;
+    cudaError_t e = cudaMemcpy3DAsync(&p, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// Pull-form decoding of one population's link (see include/elbm_gb300.h and
+// the push rules of looping/timestepping/streaming.f95:365-481).
+// Returns 0 and the link word, or a negative error code.
+int decode_link27(const int32_t* st, int64_t fab_plane, int64_t sidx, const int sstride[3], int x, int y, int z,
+                  const Box& b, const Level& lv, int j, uint16_t& word, bool& interior, std::string& why) {
+  const int i = D3Q27::opp[j];  // the link that leaves x along -c_j
+  const int32_t code = st[(int64_t)i * fab_plane + sidx];
+  interior = false;
+  if (code >= 0) {
+    const int sx = x - D3Q27::cx[j], sy = y - D3Q27::cy[j], sz = z - D3Q27::cz[j];
+    if (sx < 0 || sy < 0 || sz < 0 || sx >= b.nx || sy >= b.ny || sz >= b.nz) {
+      why = "fluid link leaves a single-box level";
+      return ELBM_E_UNSUPPORTED;
+    }
+    word = link_word(LK_PULL, j, off_code(-D3Q27::cx[j], -D3Q27::cy[j], -D3Q27::cz[j]));
+    interior = true;
+    return 0;
+  }
+  if (code == -10 || code == -5) {  // bounceback.f95:13-19 (halfway bounce-back), null_bc
+    word = link_word(LK_PULL, i, off_code(0, 0, 0));
+    return 0;
+  }
+  if (code == -11 || code == -12) {  // inviscid_edge.f95: specular reflection
+    const int c[3] = {D3Q27::cx[j], D3Q27::cy[j], D3Q27::cz[j]};
+    int src_c[3] = {c[0], c[1], c[2]}, disp[3] = {c[0], c[1], c[2]};
+    bool any = false;
+    for (int a = 0; a < 3; ++a) {
+      if (c[a] == 0) continue;
+      int card[3] = {0, 0, 0};
+      card[a] = -c[a];
+      const int k = find27(card[0], card[1], card[2]);
+      const int32_t cc = st[(int64_t)k * fab_plane + sidx];
+      if (cc == -11 || cc == -12) {
+        src_c[a] = -c[a];
+        disp[a] = 0;
+        any = true;
+      }
+    }
+    const int sx = x - disp[0], sy = y - disp[1], sz = z - disp[2];
+    const int src_pop = find27(src_c[0], src_c[1], src_c[2]);
+    bool ok = any && src_pop != j && sx >= 0 && sy >= 0 && sz >= 0 && sx < b.nx && sy < b.ny && sz < b.nz;
+    if (ok) {
+      const int64_t s2 = sidx - (int64_t)disp[0] * sstride[0] - (int64_t)disp[1] * sstride[1] -
+                         (int64_t)disp[2] * sstride[2];
+      ok = node_is_fluid(st[s2]);
+    }
+    if (ok) word = link_word(LK_PULL, src_pop, off_code(-disp[0], -disp[1], -disp[2]));
+    else word = link_word(LK_PULL, i, off_code(0, 0, 0));
+    return 0;
+  }
+  if (code == -3 || code == -8 || code == -1000) {  // freestream_bc.f95, freestream_edge_bc.f95
+    word = link_word(LK_EQ, 0, 0);
+    return 0;
+  }
+  if (code <= -100 && code >= -199) {  // inlet_bc.f95:21-53
+    const int k = -code - 100;
+    if (k < 1 || k > 8) {
+      why = "inlet number outside 1..8";
+      return ELBM_E_UNSUPPORTED;
+    }
+    word = link_word(LK_EQ, k, 0);
+    return 0;
+  }
+  if (code <= -200 && code >= -299) {  // outlet_bc.f95:23-58
+    const int k = -code - 200;
+    if (k < 1 || k > 8) {
+      why = "outlet number outside 1..8";
+      return ELBM_E_UNSUPPORTED;
+    }
+    const int t = lv.p27.outlet_type[k - 1];
+    if (t == 1 || t == 4) word = link_word(LK_EQ, 8 + k, 0);
+    else if (t == 2) word = link_word(LK_EQ, k, 0);  // press_temp_bc.f95:26-27 reads the inlet table
+    else if (t == 3) word = link_word(LK_EQ, 0, 0);
+    else if (t == 6) word = link_word(LK_PULL, j, off_code(0, 0, 0));  // pure_outflow_bc.f95:19-20
+    else {
+      why = "unsupported outlet type";
+      return ELBM_E_UNSUPPORTED;
+    }
+    return 0;
+  }
+  if (code == -666 || code == -1001) {  // null / plain solid: nothing streams in
+    word = link_word(LK_KEEP, j, 0);
+    return 0;
+  }
+  why = "unsupported link code " + std::to_string(code);
+  return ELBM_E_UNSUPPORTED;
+}
+
+}  // namespace
+
+extern "C" {
+
+int elbm_create(int device, elbm_ctx** out) {
+  if (!out) return ELBM_E_ARG;
+  *out = nullptr;
+  auto c = std::make_unique<elbm_ctx>();
+  c->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return ELBM_E_CUDA;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return ELBM_E_CUDA;
+  if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) return ELBM_E_CUDA;
+  if (c->stats.alloc(1) != cudaSuccess) return ELBM_E_CUDA;
+  *out = c.release();
+  return ELBM_OK;
+}
+
+void elbm_destroy(elbm_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  c->levels.clear();
+  c->stats.reset();
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* elbm_last_error_string(const elbm_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int elbm_level_register(elbm_ctx* c, int lvl, int lattice, int storage, int nbox, const int32_t* lo_hi, int ngrow) {
+  if (!c) return ELBM_E_ARG;
+  if (lvl < 0 || lvl > 30) return fail(c, ELBM_E_ARG, "level %d out of range", lvl);
+  if (lattice != ELBM_D3Q27) return fail(c, ELBM_E_UNSUPPORTED, "lattice %d not supported by this entry point", lattice);
+  if (storage != ELBM_STORE_FP64 && storage != ELBM_STORE_FP32_DEV) return fail(c, ELBM_E_ARG, "bad storage %d", storage);
+  if (nbox != 1) return fail(c, ELBM_E_UNSUPPORTED, "only single-box levels are supported (nbox=%d)", nbox);
+  if (!lo_hi || ngrow < 0) return fail(c, ELBM_E_ARG, "null lo_hi or negative ngrow");
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  if ((int)c->levels.size() <= lvl) c->levels.resize(lvl + 1);
+  Level& lv = c->levels[lvl];
+  lv = Level();
+  lv.lattice = lattice;
+  lv.storage = storage;
+  lv.ngrow = ngrow;
+  for (int k = 0; k < nbox; ++k) {
+    auto b = std::make_unique<Box>();
+    for (int a = 0; a < 3; ++a) {
+      b->lo[a] = lo_hi[6 * k + a];
+      b->hi[a] = lo_hi[6 * k + 3 + a];
+      if (b->hi[a] < b->lo[a]) return fail(c, ELBM_E_ARG, "empty box %d", k);
+    }
+    b->nx = b->hi[0] - b->lo[0] + 1;
+    b->ny = b->hi[1] - b->lo[1] + 1;
+    b->nz = b->hi[2] - b->lo[2] + 1;
+    b->N = (int64_t)b->nx * b->ny * b->nz;
+    b->plane = (b->N + 31) / 32 * 32;
+    const size_t bytes = (size_t)b->plane * Q27 * elem_size(storage);
+    for (int s = 0; s < 2; ++s) CUDA_TRY(b->buf[s].alloc(bytes), "population buffers");
+    CUDA_TRY(b->ntype.alloc(b->N), "node types");
+    CUDA_TRY(cudaMemsetAsync(b->ntype.p, 0, b->N, c->stream), "memset");
+    lv.boxes.push_back(std::move(b));
+  }
+  CUDA_TRY(lv.eq.alloc(kEqTables * Q27 * sizeof(double)), "eq tables");
+  lv.registered = true;
+  return ELBM_OK;
+}
+
+int elbm_set_d3q27_params(elbm_ctx* c, int lvl, const elbm_d3q27_params* p) {
+  Level* lv = get_level(c, lvl);
+  if (!lv || !p) return fail(c, ELBM_E_ARG, "unknown level or null params");
+  if (!(p->nu > 0.0) || p->max_newton < 1 || p->alpha_mode < 0 || p->alpha_mode > 2)
+    return fail(c, ELBM_E_ARG, "bad D3Q27 parameters");
+  if (p->alpha_mode == ELBM_ALPHA_LEARNED) return fail(c, ELBM_E_UNSUPPORTED, "learned alpha needs a trained network");
+  lv->p27 = *p;
+  lv->params_set = true;
+  double tab[kEqTables][Q27];
+  for (int j = 0; j < Q27; ++j) {
+    tab[0][j] = p->fs_feq[j];
+    for (int k = 0; k < 8; ++k) {
+      tab[1 + k][j] = p->inl_feq[k][j];
+      tab[9 + k][j] = p->outl_feq[k][j];
+    }
+  }
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  if (lv->storage == ELBM_STORE_FP64) {
+    CUDA_TRY(cudaMemcpyAsync(lv->eq.p, tab, sizeof tab, cudaMemcpyHostToDevice, c->stream), "eq upload");
+  } else {
+    float tf[kEqTables][Q27];
+    for (int t = 0; t < kEqTables; ++t)
+      for (int j = 0; j < Q27; ++j) tf[t][j] = (float)(tab[t][j] - w27(j));
+    CUDA_TRY(cudaMemcpyAsync(lv->eq.p, tf, sizeof tf, cudaMemcpyHostToDevice, c->stream), "eq upload");
+  }
+  CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  return ELBM_OK;
+}
+
+int elbm_set_links(elbm_ctx* c, int lvl, int box, const int32_t* state, int ngrow_state) {
+  Level* lv = nullptr;
+  Box* b = get_box(c, lvl, box, &lv);
+  if (!b || !state || ngrow_state < 0) return fail(c, ELBM_E_ARG, "unknown level/box or null state");
+  if (!lv->params_set) return fail(c, ELBM_E_STATE, "set the level parameters before the links");
+  const int g = ngrow_state;
+  const int fx = b->nx + 2 * g, fy = b->ny + 2 * g, fz = b->nz + 2 * g;
+  const int64_t fab_plane = (int64_t)fx * fy * fz;
+  const int sstride[3] = {1, fx, fx * fy};
+  std::vector<uint8_t> nt(b->N, NT_SKIP);
+  std::vector<int32_t> bi;
+  std::vector<uint16_t> words;
+  std::vector<int64_t> bnodes;
+  int64_t fluid = 0;
+  std::string why;
+  for (int z = 0; z < b->nz; ++z)
+    for (int y = 0; y < b->ny; ++y)
+      for (int x = 0; x < b->nx; ++x) {
+        const int64_t n = ((int64_t)z * b->ny + y) * b->nx + x;
+        const int64_t s = ((int64_t)(z + g) * fy + (y + g)) * fx + (x + g);
+        if (!node_is_fluid(state[s])) continue;
+        ++fluid;
+        uint16_t w[Q27];
+        bool all_interior = true;
+        w[0] = link_word(LK_PULL, 0, off_code(0, 0, 0));
+        for (int j = 1; j < Q27; ++j) {
+          bool interior;
+          const int rc = decode_link27(state, fab_plane, s, sstride, x, y, z, *b, *lv, j, w[j], interior, why);
+          if (rc) return fail(c, rc, "node (%d,%d,%d) population %d: %s", x + b->lo[0], y + b->lo[1], z + b->lo[2], j,
+                              why.c_str());
+          all_interior &= interior;
+        }
+        if (all_interior) {
+          nt[n] = NT_BULK;
+        } else {
+          nt[n] = NT_BOUNDARY;
+          bnodes.push_back(n);
+          words.insert(words.end(), w, w + Q27);
+        }
+      }
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  CUDA_TRY(cudaMemcpy(b->ntype.p, nt.data(), b->N, cudaMemcpyHostToDevice), "node types");
+  std::vector<int32_t> bidx(b->N, -1);
+  for (size_t k = 0; k < bnodes.size(); ++k) bidx[bnodes[k]] = (int32_t)k;
+  CUDA_TRY(b->bidx.alloc(b->N), "boundary index");
+  CUDA_TRY(cudaMemcpy(b->bidx.p, bidx.data(), b->N * sizeof(int32_t), cudaMemcpyHostToDevice), "boundary index");
+  CUDA_TRY(b->words.alloc(std::max<size_t>(words.size(), 1)), "link words");
+  if (!words.empty())
+    CUDA_TRY(cudaMemcpy(b->words.p, words.data(), words.size() * sizeof(uint16_t), cudaMemcpyHostToDevice), "words");
+  b->fluid_nodes = fluid;
+  b->boundary_nodes = (int64_t)bnodes.size();
+  b->links_set = true;
+  return ELBM_OK;
+}
+
+int elbm_upload_level(elbm_ctx* c, int lvl, int box, const double* fout) {
+  Level* lv = nullptr;
+  Box* b = get_box(c, lvl, box, &lv);
+  if (!b || !fout) return fail(c, ELBM_E_ARG, "unknown level/box or null data");
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  if (lv->storage == ELBM_STORE_FP64) {
+    CUDA_TRY(fab_to_packed(fout, (double*)b->buf[0].p, *b, lv->ngrow, Q27, b->plane, c->stream), "upload");
+  } else {
+    if (!b->staging.p) CUDA_TRY(b->staging.alloc((size_t)b->N * Q27), "staging");
+    CUDA_TRY(fab_to_packed(fout, b->staging.p, *b, lv->ngrow, Q27, b->N, c->stream), "upload");
+    dim3 grid((unsigned)((b->N + 255) / 256), Q27);
+    to_dev32_kernel<<<grid, 256, 0, c->stream>>>(b->staging.p, (float*)b->buf[0].p, b->N, b->plane);
+    CUDA_TRY(cudaGetLastError(), "to_dev32");
+  }
+  // both buffers start identical so that nodes a step never writes stay defined
+  CUDA_TRY(cudaMemcpyAsync(b->buf[1].p, b->buf[0].p, b->buf[0].n, cudaMemcpyDeviceToDevice, c->stream), "copy");
+  b->cur = 0;
+  b->data_set = true;
+  return ELBM_OK;
+}
+
+int elbm_download_level(elbm_ctx* c, int lvl, int box, double* fout) {
+  Level* lv = nullptr;
+  Box* b = get_box(c, lvl, box, &lv);
+  if (!b || !fout) return fail(c, ELBM_E_ARG, "unknown level/box or null data");
+  if (!b->data_set) return fail(c, ELBM_E_STATE, "no populations uploaded");
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  if (lv->storage == ELBM_STORE_FP64) {
+    CUDA_TRY(packed_to_fab((const double*)b->buf[b->cur].p, fout, *b, lv->ngrow, Q27, b->plane, c->stream), "download");
+  } else {
+    if (!b->staging.p) CUDA_TRY(b->staging.alloc((size_t)b->N * Q27), "staging");
+    dim3 grid((unsigned)((b->N + 255) / 256), Q27);
+    from_dev32_kernel<<<grid, 256, 0, c->stream>>>((const float*)b->buf[b->cur].p, b->staging.p, b->N, b->plane);
+    CUDA_TRY(cudaGetLastError(), "from_dev32");
+    CUDA_TRY(packed_to_fab((const double*)b->staging.p, fout, *b, lv->ngrow, Q27, b->N, c->stream), "download");
+  }
+  CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  return ELBM_OK;
+}
+
+int elbm_download_alpha(elbm_ctx* c, int lvl, int box, double* alpha) {
+  Box* b = get_box(c, lvl, box);
+  if (!b || !alpha) return fail(c, ELBM_E_ARG, "unknown level/box or null data");
+  if (!b->alpha.p) return fail(c, ELBM_E_STATE, "alpha recording is off (record_alpha = 0)");
+  std::vector<float> tmp(b->N);
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  CUDA_TRY(cudaMemcpyAsync(tmp.data(), b->alpha.p, b->N * sizeof(float), cudaMemcpyDeviceToHost, c->stream), "alpha");
+  CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  for (int64_t n = 0; n < b->N; ++n) alpha[n] = tmp[n];
+  return ELBM_OK;
+}
+
+int elbm_level_step(elbm_ctx* c, int lvl, int nsteps, elbm_stats* out) {
+  Level* lv = get_level(c, lvl);
+  if (!lv) return fail(c, ELBM_E_ARG, "unknown level %d", lvl);
+  if (nsteps < 0) return fail(c, ELBM_E_ARG, "negative step count");
+  if (!lv->params_set) return fail(c, ELBM_E_STATE, "level parameters not set");
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  CUDA_TRY(cudaMemsetAsync(c->stats.p, 0, sizeof(DevStats), c->stream), "stats reset");
+  const elbm_d3q27_params& p = lv->p27;
+  for (auto& bp : lv->boxes) {
+    Box& b = *bp;
+    if (!b.links_set || !b.data_set) return fail(c, ELBM_E_STATE, "links or populations missing");
+    if (p.record_alpha && !b.alpha.p) CUDA_TRY(b.alpha.alloc(b.N), "alpha buffer");
+  }
+  CUDA_TRY(cudaEventRecord(c->ev0, c->stream), "event");
+  for (int s = 0; s < nsteps; ++s) {
+    for (auto& bp : lv->boxes) {
+      Box& b = *bp;
+      Step27Args a{};
+      a.src = b.buf[b.cur].p;
+      a.dst = b.buf[b.cur ^ 1].p;
+      a.plane = b.plane;
+      a.nx = b.nx;
+      a.ny = b.ny;
+      a.nz = b.nz;
+      a.N = b.N;
+      a.ntype = b.ntype.p;
+      a.bidx = b.bidx.p;
+      a.words = b.words.p;
+      a.eq = lv->eq.p;
+      a.beta = 1.0 / (2.0 * p.nu / (1.0 / 3.0) + 1.0);
+      a.tol_alpha = p.tol_alpha;
+      a.tol_dH = p.tol_dH;
+      a.max_newton = p.max_newton;
+      a.alpha_mode = p.alpha_mode;
+      a.check_dH = p.check_dH;
+      a.alpha_out = (p.record_alpha && s == nsteps - 1) ? b.alpha.p : nullptr;
+      a.stats = c->stats.p;
+      if (lv->storage == ELBM_STORE_FP64) launch_d3q27_fp64(a, c->stream);
+      else launch_d3q27_fp32(a, c->stream);
+      CUDA_TRY(cudaGetLastError(), "step kernel launch");
+      b.cur ^= 1;
+    }
+  }
+  CUDA_TRY(cudaEventRecord(c->ev1, c->stream), "event");
+  if (out) {
+    DevStats ds{};
+    CUDA_TRY(cudaMemcpyAsync(&ds, c->stats.p, sizeof ds, cudaMemcpyDeviceToHost, c->stream), "stats");
+    CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+    float ms = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1), "elapsed");
+    std::memset(out, 0, sizeof *out);
+    out->node_updates = (int64_t)ds.node_updates;
+    out->newton_iters = (int64_t)ds.newton_iters;
+    out->exact_path_nodes = (int64_t)ds.exact_nodes;
+    out->fallbacks = (int64_t)ds.fallbacks;
+    out->status = ds.status;
+    double mx;
+    std::memcpy(&mx, &ds.max_dH_bits, sizeof mx);
+    out->max_abs_dH = mx;
+    out->kernel_ms = ms;
+  }
+  return ELBM_OK;
+}
+
+int elbm_sync(elbm_ctx* c) {
+  if (!c) return ELBM_E_ARG;
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  return ELBM_OK;
+}
+
+}  // extern "C"

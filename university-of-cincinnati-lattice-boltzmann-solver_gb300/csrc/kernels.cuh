@@ -1,0 +1,46 @@
+// Internal kernel interface of libelbm_gb300 (not part of the C ABI).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "lattice.cuh"
+
+namespace elbm {
+
+// Device-side statistics of one or more steps (accumulated with atomics).
+struct DevStats {
+  unsigned long long node_updates;
+  unsigned long long newton_iters;
+  unsigned long long exact_nodes;
+  unsigned long long fallbacks;
+  unsigned long long max_dH_bits;  // bit pattern of a non-negative double (monotone in value)
+  unsigned int status;
+  unsigned int pad;
+};
+
+// Arguments of one fused D3Q27 step on a single box (valid region, no ghosts).
+struct Step27Args {
+  const void* src;  // post-collision populations of the previous step, Q planes
+  void* dst;        // post-collision populations of this step
+  int64_t plane;    // elements between population planes (>= N, padded)
+  int nx, ny, nz;
+  int64_t N;
+  const uint8_t* ntype;   // NodeType per node
+  const int32_t* bidx;    // boundary record per boundary node
+  const uint16_t* words;  // Q link words per boundary record
+  const void* eq;         // kEqTables x Q equilibria (FP64: f; FP32: deviations)
+  double beta;
+  double tol_alpha;
+  double tol_dH;
+  int max_newton;
+  int alpha_mode;
+  int check_dH;
+  float* alpha_out;       // optional per-node alpha (FP32)
+  DevStats* stats;
+  const void* mlp;        // learned-alpha weights (ELBM_ALPHA_LEARNED)
+};
+
+void launch_d3q27_fp64(const Step27Args& a, cudaStream_t s);
+void launch_d3q27_fp32(const Step27Args& a, cudaStream_t s);
+
+}  // namespace elbm
