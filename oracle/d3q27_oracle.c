@@ -86,26 +86,44 @@ void o27_weights(double w[Q]) {
   for (int i = 0; i < Q; ++i) w[i] = weight(i);
 }
 
-/* H(f + alpha*Delta) - H(f) with H(f) = sum f ln(f/w), written term by term as
- * alpha*Delta*ln(f/w) + f(1+x)ln(1+x), x = alpha*Delta/f (an exact identity). */
-static double entropy_diff(const double* f, const double* d, const double* L, double alpha) {
+/* phi(x) = (1+x) ln(1+x) - x, with its Taylor series near 0 where the direct
+ * form cancels. */
+static double phi_fn(double x) {
+  if (fabs(x) < 1e-2) {
+    double p = 0.0;
+    for (int n = 12; n >= 2; --n) p = p * (-x) + 1.0 / (n * (n - 1.0));
+    return x * x * p;
+  }
+  return (1.0 + x) * log1p(x) - x;
+}
+
+/* Entropy difference H(f + alpha Delta) - H(f), H(f) = sum f ln(f/w), in the
+ * form that holds when Delta conserves mass and momentum exactly:
+ *   G(alpha) = sum_i f_i psi(y_i, alpha),  y_i = Delta_i / f_i,
+ *   psi(y, a) = phi(a y) - a y ln(1 + y).
+ * (Expanding (f + aD) ln((f + aD)/w) - f ln(f/w) = a D ln(f/w) + f (1+x) ln(1+x),
+ * x = a y, and using ln(f/w) = ln(feq/w) - ln(1+y) with ln(feq/w) linear in
+ * (1, c_i) for the entropic equilibrium, the terms a*sum D and a*sum c D vanish.)
+ * Dropping those analytically-zero terms keeps the root insensitive to the
+ * rounding residual of sum_i Delta_i, which the direct form multiplies by
+ * alpha / H'(alpha) ~ 1/|Delta|^2. */
+static double entropy_diff(const double* f, const double* d, const double* L1, double alpha) {
   double g = 0.0;
   for (int i = 0; i < Q; ++i) {
-    const double x = alpha * d[i] / f[i];
-    g += alpha * d[i] * L[i] + f[i] * (1.0 + x) * log1p(x);
+    const double y = d[i] / f[i];
+    g += f[i] * (phi_fn(alpha * y) - alpha * y * L1[i]);
   }
   return g;
 }
 
-/* Entropic alpha by Newton from alpha = 2 on G(alpha) = H(f + alpha Delta) - H(f).
+/* Entropic alpha by Newton from alpha = 2 on G(alpha) = 0 (non-trivial root).
  * Returns alpha; *iters = iterations; *fallback = 1 when the solve failed and
  * alpha fell back to 2 (clipped into the positivity bracket). */
 double o27_alpha_newton(const double f[Q], const double d[Q], double tol, int max_it, int* iters, int* fallback) {
-  double L[Q], w[Q];
-  o27_weights(w);
+  double L1[Q];
   double s2 = 0.0, amax = INFINITY;
   for (int i = 0; i < Q; ++i) {
-    L[i] = log(f[i] / w[i]);
+    L1[i] = log1p(d[i] / f[i]);
     s2 += d[i] * d[i] / f[i];
     if (d[i] < 0.0) {
       const double lim = -f[i] / d[i];
@@ -120,10 +138,9 @@ double o27_alpha_newton(const double f[Q], const double d[Q], double tol, int ma
   for (int it = 0; it < max_it; ++it) {
     double g = 0.0, gp = 0.0;
     for (int i = 0; i < Q; ++i) {
-      const double x = alpha * d[i] / f[i];
-      const double l1 = log1p(x);
-      g += alpha * d[i] * L[i] + f[i] * (1.0 + x) * l1;
-      gp += d[i] * (L[i] + l1 + 1.0);
+      const double y = d[i] / f[i];
+      g += f[i] * (phi_fn(alpha * y) - alpha * y * L1[i]);
+      gp += d[i] * (log1p(alpha * y) - L1[i]);
     }
     *iters = it + 1;
     if (!(gp > 0.0)) break;
@@ -138,7 +155,7 @@ double o27_alpha_newton(const double f[Q], const double d[Q], double tol, int ma
   }
   if (!ok) {
     /* iteration cap with a small entropy residual still counts as converged */
-    if (*iters >= max_it && fabs(entropy_diff(f, d, L, alpha)) <= 1e-10) return alpha;
+    if (*iters >= max_it && fabs(entropy_diff(f, d, L1, alpha)) <= 1e-10) return alpha;
     *fallback = 1;
     return (2.0 < amax) ? 2.0 : 0.5 * (1.0 + amax);
   }
@@ -146,10 +163,20 @@ double o27_alpha_newton(const double f[Q], const double d[Q], double tol, int ma
 }
 
 double o27_entropy_diff(const double f[Q], const double d[Q], double alpha) {
-  double L[Q], w[Q];
+  double L1[Q];
+  for (int i = 0; i < Q; ++i) L1[i] = log1p(d[i] / f[i]);
+  return entropy_diff(f, d, L1, alpha);
+}
+
+/* The direct form sum (f + alpha D) ln((f + alpha D)/w) - f ln(f/w), for reports. */
+double o27_entropy_diff_direct(const double f[Q], const double d[Q], double alpha) {
+  double w[Q], g = 0.0;
   o27_weights(w);
-  for (int i = 0; i < Q; ++i) L[i] = log(f[i] / w[i]);
-  return entropy_diff(f, d, L, alpha);
+  for (int i = 0; i < Q; ++i) {
+    const double x = alpha * d[i] / f[i];
+    g += alpha * d[i] * log(f[i] / w[i]) + f[i] * (1.0 + x) * log1p(x);
+  }
+  return g;
 }
 
 /* Collision of one node: moments, equilibrium, alpha, f_out = f + alpha*beta*Delta. */

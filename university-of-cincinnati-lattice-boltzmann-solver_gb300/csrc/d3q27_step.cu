@@ -97,27 +97,47 @@ __device__ __forceinline__ void warp_stats(DevStats* st, bool active, unsigned i
 }
 
 // ---------------------------------------------------------------------------
-// FP64 path: populations f_i in FP64, Newton on the exact entropy difference.
-// Same algorithm and stopping rules as the CPU oracle.
+// Entropy difference in the conservation-consistent form (see the oracle):
+//   G(alpha) = H(f + alpha Delta) - H(f) = sum_i f_i psi(y_i, alpha),
+//   y_i = Delta_i / f_i,  psi(y, a) = phi(a y) - a y ln(1 + y),
+//   phi(x) = (1 + x) ln(1 + x) - x,
+// exact when Delta conserves mass and momentum (it does analytically; the
+// dropped terms a*sum D (1 + ln feq/w) are pure rounding residuals, which the
+// direct form would amplify by 1/|Delta|^2 into alpha).
 // ---------------------------------------------------------------------------
 
-__device__ double entropy_diff64(const double (&f)[Q], const double (&d)[Q], const double (&L)[Q], double alpha) {
+__device__ __forceinline__ double phi64(double x) {
+  if (fabs(x) < 1e-2) {
+    double p = 1.0 / 132.0;
+#pragma unroll
+    for (int n = 11; n >= 2; --n) p = fma(p, -x, 1.0 / (n * (n - 1.0)));
+    return x * x * p;
+  }
+  return fma(1.0 + x, log1p(x), -x);
+}
+
+// ---------------------------------------------------------------------------
+// FP64 path: populations f_i in FP64, Newton from alpha = 2, tolerance on the
+// step; same algorithm and stopping rules as the CPU oracle.
+// ---------------------------------------------------------------------------
+
+__device__ double entropy_diff64(const double (&f)[Q], const double (&d)[Q], const double (&L1)[Q], double alpha) {
   double g = 0.0;
 #pragma unroll
   for (int i = 0; i < Q; ++i) {
-    const double x = alpha * d[i] / f[i];
-    g += alpha * d[i] * L[i] + f[i] * (1.0 + x) * log1p(x);
+    const double y = d[i] / f[i];
+    g += f[i] * (phi64(alpha * y) - alpha * y * L1[i]);
   }
   return g;
 }
 
 __device__ double alpha_newton64(const double (&f)[Q], const double (&d)[Q], double tol, double tol_dH, int max_it,
                                  unsigned& iters, bool& fallback) {
-  double L[Q];
+  double L1[Q];
   double s2 = 0.0, amax = INFINITY;
 #pragma unroll
   for (int i = 0; i < Q; ++i) {
-    L[i] = log(f[i] / w27(i));
+    L1[i] = log1p(d[i] / f[i]);
     s2 += d[i] * d[i] / f[i];
     if (d[i] < 0.0) amax = fmin(amax, -f[i] / d[i]);
   }
@@ -130,10 +150,9 @@ __device__ double alpha_newton64(const double (&f)[Q], const double (&d)[Q], dou
     double g = 0.0, gp = 0.0;
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
-      const double x = alpha * d[i] / f[i];
-      const double l1 = log1p(x);
-      g += alpha * d[i] * L[i] + f[i] * (1.0 + x) * l1;
-      gp += d[i] * (L[i] + l1 + 1.0);
+      const double y = d[i] / f[i];
+      g += f[i] * (phi64(alpha * y) - alpha * y * L1[i]);
+      gp += d[i] * (log1p(alpha * y) - L1[i]);
     }
     iters = it + 1;
     if (!(gp > 0.0)) break;
@@ -147,7 +166,7 @@ __device__ double alpha_newton64(const double (&f)[Q], const double (&d)[Q], dou
     }
   }
   if (!ok) {
-    if ((int)iters >= max_it && fabs(entropy_diff64(f, d, L, alpha)) <= tol_dH) return alpha;
+    if ((int)iters >= max_it && fabs(entropy_diff64(f, d, L1, alpha)) <= tol_dH) return alpha;
     fallback = true;
     return (2.0 < amax) ? 2.0 : 0.5 * (1.0 + amax);
   }
@@ -195,10 +214,10 @@ __global__ void __launch_bounds__(128) d3q27_fp64_kernel(const Step27Args a) {
   if (a.alpha_mode != 0) {
     alpha = alpha_newton64(f, d, a.tol_alpha, a.tol_dH, a.max_newton, iters, fb);
     if (a.check_dH) {
-      double Lg[Q];
+      double L1[Q];
 #pragma unroll
-      for (int i = 0; i < Q; ++i) Lg[i] = log(f[i] / w27(i));
-      dH = fabs(entropy_diff64(f, d, Lg, alpha));
+      for (int i = 0; i < Q; ++i) L1[i] = log1p(d[i] / f[i]);
+      dH = fabs(entropy_diff64(f, d, L1, alpha));
     }
   }
   unsigned flags = 0;
@@ -221,27 +240,24 @@ __global__ void __launch_bounds__(128) d3q27_fp64_kernel(const Step27Args a) {
 // ---------------------------------------------------------------------------
 // FP32 path: deviations d_i = f_i - w_i stored in FP32; collision in FP32.
 //
-// Entropic alpha without cancellation: with y_i = Delta_i / f_i and the power
-// sums S_n = sum_i f_i y_i^n, the entropy difference divided by alpha,
-//   g(alpha) = [H(f + alpha Delta) - H(f)] / alpha,
-// is  g(alpha) = A - sum_n (-1)^n S_n/(n-1) + sum_n (-1)^n S_n alpha^(n-1)/(n(n-1)),
-// A = sum_i Delta_i ln(f^eq_i / w_i).  For the entropic equilibrium ln(f^eq/w)
-// is linear in (1, c_i), so A = 0 by mass and momentum conservation.
-// Expanded around alpha = 2 the S_2 terms cancel analytically, so
-//   g(2 + delta) = sum_k t_k delta^k,  t_0 = sum_{n>=3} c_n S_n
-// is evaluated from small quantities only; Newton runs on delta.  The series
-// is used while max|y| <= kYSeries; beyond that the per-population logarithms
-// are evaluated directly ("exact path").
+// Entropic alpha without cancellation.  With y_i = Delta_i / f_i and the power
+// sums S_n = sum_i f_i y_i^n, the entropy difference divided by alpha is
+//   g(alpha) = G(alpha)/alpha = sum_n [b_n + a_n alpha^(n-1)] S_n,
+//   a_n = (-1)^n / (n(n-1)),  b_n = -(-1)^n / (n-1),
+// (the Taylor series of psi(y, alpha)/alpha in y).  Around alpha = 2 the S_2
+// terms cancel analytically:
+//   g(2 + delta) = sum_n [c0_n + a_n P_{n-1}(delta)] S_n,
+//   c0_n = a_n 2^(n-1) + b_n  (c0_2 = 0),  P_m = (2 + delta)^m - 2^m,
+// with P_m built by P_m = (2 + delta) P_{m-1} + delta 2^(m-1), so g is
+// evaluated from small quantities only and Newton runs on delta in FP32.
+// Populations with |y| > kYSmall, where the series converges slowly, are
+// summed individually in FP64 (rare: strongly non-equilibrium nodes).  The
+// series order K is chosen per warp from the warp's largest |y| so that the
+// truncation error in alpha stays below ~1e-9.
 // ---------------------------------------------------------------------------
 
-constexpr int kNMax = 9;           // power sums S_2 .. S_9
-constexpr float kYSeries = 0.06f;  // max |y| for the series path
+constexpr float kYSmall = 0.1f;
 
-__host__ __device__ constexpr double binom(int n, int k) {
-  double r = 1.0;
-  for (int i = 1; i <= k; ++i) r = r * (n - k + i) / i;
-  return r;
-}
 __host__ __device__ constexpr double pow2i(int e) {
   double r = 1.0;
   for (int i = 0; i < e; ++i) r *= 2.0;
@@ -249,76 +265,91 @@ __host__ __device__ constexpr double pow2i(int e) {
 }
 __host__ __device__ constexpr double a_n(int n) { return ((n & 1) ? -1.0 : 1.0) / (n * (n - 1.0)); }
 __host__ __device__ constexpr double b_n(int n) { return -((n & 1) ? -1.0 : 1.0) / (n - 1.0); }
-// coefficient of S_n in t_0 and t_k
-__host__ __device__ constexpr double c0(int n) { return a_n(n) * pow2i(n - 1) + b_n(n); }
-__host__ __device__ constexpr double ck(int k, int n) { return (n - 1 >= k) ? a_n(n) * binom(n - 1, k) * pow2i(n - 1 - k) : 0.0; }
-
-// phi(x) = (1+x) ln(1+x) - x and ln(1+x), accurate for all x > -1
-__device__ __forceinline__ void phi_and_log1p(float x, float& phi, float& l1) {
-  if (fabsf(x) < 0.125f) {
-    // ln(1+x) = sum (-1)^(m+1) x^m / m ; phi(x) = sum_{n>=2} (-1)^n x^n/(n(n-1))
-    float lp = 1.0f / 12.0f, pp = 1.0f / 132.0f;  // m = 12 ; n = 12
-#pragma unroll
-    for (int m = 11; m >= 1; --m) lp = fmaf(lp, -x, 1.0f / m);
-    l1 = x * lp;
-#pragma unroll
-    for (int k = 11; k >= 2; --k) pp = fmaf(pp, -x, 1.0f / (k * (k - 1.0f)));
-    phi = x * x * pp;
-  } else {
-    l1 = log1pf(x);
-    phi = fmaf(1.0f + x, l1, -x);
-  }
-}
+__host__ __device__ constexpr double c0_n(int n) { return a_n(n) * pow2i(n - 1) + b_n(n); }
 
 struct AlphaOut {
-  float alpha;
+  float delta;  // alpha = 2 + delta
   unsigned iters;
-  bool exact;
+  bool large;   // some population took the FP64 route
   bool fallback;
 };
 
-// Direct FP32 Newton on G(alpha) = sum f psi(y, alpha),
-// psi(y, a) = phi(a y) - a y ln(1+y), from alpha = 2 inside (1, amax).
-__device__ AlphaOut alpha_exact32(const float (&fv)[Q], const float (&y)[Q], float amax, int max_it) {
-  float Ly[Q];
+// FP64 sum over the populations with |y| > kYSmall: G_L(alpha), G_L'(alpha).
+__device__ __noinline__ void large_terms(const float (&d)[Q], const float (&D)[Q], double alpha, double& GL,
+                                         double& GLp) {
+  GL = 0.0;
+  GLp = 0.0;
 #pragma unroll
   for (int i = 0; i < Q; ++i) {
-    float ph;
-    phi_and_log1p(y[i], ph, Ly[i]);
+    const double f = (double)((float)w27(i) + d[i]), y = (double)D[i] / f;
+    if (fabs(y) > (double)kYSmall) {
+      const double l1 = log1p(y);
+      GL += f * (phi64(alpha * y) - alpha * y * l1);
+      GLp += f * y * (log1p(alpha * y) - l1);
+    }
   }
-  float alpha = (2.0f < amax) ? 2.0f : 0.5f * (1.0f + amax);
-  AlphaOut r{alpha, 0u, true, false};
+}
+
+template <int K>
+__device__ AlphaOut alpha_series32(const float (&d)[Q], const float (&D)[Q], const float (&y)[Q], bool any_large,
+                                   float amax, int max_it) {
+  float S[K + 1];
+#pragma unroll
+  for (int k = 0; k <= K; ++k) S[k] = 0.f;
+#pragma unroll
+  for (int i = 0; i < Q; ++i) {
+    const bool small = fabsf(y[i]) <= kYSmall;
+    const float yi = small ? y[i] : 0.f;
+    float p = small ? D[i] * y[i] : 0.f;  // f y^2
+    S[2] += p;
+#pragma unroll
+    for (int k = 3; k <= K; ++k) {
+      p *= yi;
+      S[k] += p;
+    }
+  }
+  AlphaOut r{0.f, 0u, any_large, false};
+  if (!any_large && !(S[2] > 1e-30f)) return r;  // at equilibrium: alpha = 2
+  float delta = 0.f;
   bool ok = false;
   for (int it = 0; it < max_it; ++it) {
-    // G(a) = sum f [phi(a y) - a y Ly];  G'(a) = sum f y [ln(1+a y) - Ly]
-    float G = 0.f, Gp = 0.f;
+    const float alpha = 2.0f + delta;
+    float g = 0.f, gp = 0.f, P = 0.f, pw = 1.f, two = 1.f;
 #pragma unroll
-    for (int i = 0; i < Q; ++i) {
-      float ph, l1;
-      phi_and_log1p(alpha * y[i], ph, l1);
-      const float fy = fv[i] * y[i];
-      G += fv[i] * ph - alpha * fy * Ly[i];
-      Gp += fy * (l1 - Ly[i]);
+    for (int n = 2; n <= K; ++n) {
+      gp = fmaf((float)(a_n(n) * (n - 1)) * pw, S[n], gp);
+      P = fmaf(alpha, P, delta * two);
+      two *= 2.f;
+      pw *= alpha;
+      g = fmaf(fmaf((float)a_n(n), P, (float)c0_n(n)), S[n], g);
+    }
+    if (any_large) {
+      double GL, GLp;
+      large_terms(d, D, 2.0 + (double)delta, GL, GLp);
+      const double al = 2.0 + (double)delta;
+      g += (float)(GL / al);
+      gp += (float)(GLp / al - GL / (al * al));
     }
     r.iters = it + 1;
-    if (!(Gp > 0.0f)) break;
-    const float step = G / Gp;
-    const float next = alpha - step;
-    if (!(next > 1.0f) || !(next < amax)) break;
-    alpha = next;
-    if (fabsf(step) <= 2e-7f * alpha) {
+    if (!(gp > 0.f)) break;
+    const float step = g / gp;
+    const float next = delta - step;
+    if (!(2.0f + next > 1.0f) || !(2.0f + next < amax)) break;
+    delta = next;
+    if (fabsf(step) <= fmaxf(4e-8f, 2e-7f * fabsf(delta))) {
       ok = true;
       break;
     }
   }
   if (!ok) {
     r.fallback = true;
-    alpha = (2.0f < amax) ? 2.0f : 0.5f * (1.0f + amax);
+    delta = (2.0f < amax) ? 0.f : 0.5f * (amax - 3.0f);
   }
-  r.alpha = alpha;
+  r.delta = delta;
   return r;
 }
 
+template <bool CHECK>
 __global__ void __launch_bounds__(128) d3q27_fp32_kernel(const Step27Args a) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= a.N) return;
@@ -363,87 +394,33 @@ __global__ void __launch_bounds__(128) d3q27_fp32_kernel(const Step27Args a) {
     D[i] = fmaf(wi, fmaf(dr, 1.0f + P, P), -d[i]);
   }
 
-  AlphaOut al{2.0f, 0u, false, false};
+  AlphaOut al{0.f, 0u, false, false};
   double dH = 0.0;
   if (a.alpha_mode != 0) {
-    float fv[Q], y[Q];
-    float ymax = 0.f, amax = INFINITY;
+    float y[Q];
+    float ysmall = 0.f, amax = INFINITY;
+    bool any_large = false;
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
-      fv[i] = (float)w27(i) + d[i];
-      y[i] = __fdividef(D[i], fv[i]);
-      ymax = fmaxf(ymax, fabsf(y[i]));
+      y[i] = D[i] / ((float)w27(i) + d[i]);
+      const float ay = fabsf(y[i]);
+      if (ay <= kYSmall) ysmall = fmaxf(ysmall, ay);
+      else any_large = true;
       if (y[i] < 0.f) amax = fminf(amax, -1.0f / y[i]);
     }
-    if (ymax <= kYSeries) {
-      float S[kNMax + 1];
-#pragma unroll
-      for (int k = 0; k <= kNMax; ++k) S[k] = 0.f;
-#pragma unroll
-      for (int i = 0; i < Q; ++i) {
-        float p = D[i] * y[i];  // f y^2
-        S[2] += p;
-#pragma unroll
-        for (int k = 3; k <= kNMax; ++k) {
-          p *= y[i];
-          S[k] += p;
-        }
-      }
-      if (S[2] < 1e-30f) {
-        al.alpha = 2.0f;
-      } else {
-        float tk[kNMax];  // t_0 .. t_{kNMax-1}
-        tk[0] = 0.f;
-#pragma unroll
-        for (int nn = 3; nn <= kNMax; ++nn) tk[0] = fmaf((float)c0(nn), S[nn], tk[0]);
-#pragma unroll
-        for (int k = 1; k < kNMax; ++k) {
-          float s = 0.f;
-#pragma unroll
-          for (int nn = 2; nn <= kNMax; ++nn)
-            if (nn - 1 >= k) s = fmaf((float)ck(k, nn), S[nn], s);
-          tk[k] = s;
-        }
-        float delta = 0.f;
-        unsigned it = 0;
-        bool ok = false;
-        for (; it < 6;) {
-          float p = tk[kNMax - 1], dp = 0.f;
-#pragma unroll
-          for (int k = kNMax - 2; k >= 0; --k) {
-            dp = fmaf(dp, delta, p);
-            p = fmaf(p, delta, tk[k]);
-          }
-          ++it;
-          if (!(dp > 0.f)) break;
-          const float step = p / dp;
-          delta -= step;
-          if (fabsf(step) <= 1e-7f * fmaxf(fabsf(delta), 1e-3f)) {
-            ok = true;
-            break;
-          }
-        }
-        al.iters = it;
-        const float alpha = 2.0f + delta;
-        if (ok && alpha > 1.0f && alpha < amax) {
-          al.alpha = alpha;
-        } else {
-          al = alpha_exact32(fv, y, amax, a.max_newton);
-        }
-      }
-    } else {
-      al = alpha_exact32(fv, y, amax, a.max_newton);
-    }
-    if (a.check_dH) {
-      // |H(f + alpha Delta) - H(f)| in FP64 from the FP32 populations
+    // warp-uniform series order from the warp's largest small |y|
+    const float wmax = __int_as_float(__reduce_max_sync(__activemask(), __float_as_int(ysmall)));
+    if (wmax <= 0.02f) al = alpha_series32<6>(d, D, y, any_large, amax, a.max_newton);
+    else if (wmax <= 0.04f) al = alpha_series32<8>(d, D, y, any_large, amax, a.max_newton);
+    else al = alpha_series32<12>(d, D, y, any_large, amax, a.max_newton);
+    if (CHECK) {
+      // |H(f + alpha Delta) - H(f)| in FP64 (conservation-consistent form) from the FP32 populations
+      const double al64 = 2.0 + (double)al.delta;
       double g = 0.0;
-      const double al64 = al.alpha;
 #pragma unroll
       for (int i = 0; i < Q; ++i) {
-        const double f64 = (double)w27(i) + (double)d[i];
-        const double d64 = (double)D[i];
-        const double x = al64 * d64 / f64;
-        g += al64 * d64 * log(f64 / w27(i)) + f64 * (1.0 + x) * log1p(x);
+        const double f64 = (double)((float)w27(i) + d[i]), y64 = (double)D[i] / f64;
+        g += f64 * (phi64(al64 * y64) - al64 * y64 * log1p(y64));
       }
       dH = fabs(g);
     }
@@ -451,8 +428,8 @@ __global__ void __launch_bounds__(128) d3q27_fp32_kernel(const Step27Args a) {
   unsigned flags = 0;
   if (!isfinite(rho) || !isfinite(u[0]) || !isfinite(u[1]) || !isfinite(u[2])) flags |= 0x1u;
   if (al.fallback) flags |= 0x2u;
-  if (a.check_dH && dH > a.tol_dH) flags |= 0x8u;
-  const float ab = al.alpha * (float)a.beta;
+  if (CHECK && dH > a.tol_dH) flags |= 0x8u;
+  const float ab = (2.0f + al.delta) * (float)a.beta;
   bool neg = false;
 #pragma unroll
   for (int i = 0; i < Q; ++i) {
@@ -461,8 +438,8 @@ __global__ void __launch_bounds__(128) d3q27_fp32_kernel(const Step27Args a) {
   }
   if (neg) flags |= 0x4u;
   store_dst(dst, a.plane, n, d);
-  if (a.alpha_out) a.alpha_out[n] = al.alpha;
-  warp_stats(a.stats, true, al.iters, al.exact, al.fallback, flags, dH);
+  if (a.alpha_out) a.alpha_out[n] = 2.0f + al.delta;
+  warp_stats(a.stats, true, al.iters, al.large, al.fallback, flags, dH);
 }
 
 }  // namespace
@@ -476,7 +453,8 @@ void launch_d3q27_fp64(const Step27Args& a, cudaStream_t s) {
 void launch_d3q27_fp32(const Step27Args& a, cudaStream_t s) {
   const int threads = 128;
   const int64_t blocks = (a.N + threads - 1) / threads;
-  d3q27_fp32_kernel<<<(unsigned)blocks, threads, 0, s>>>(a);
+  if (a.check_dH) d3q27_fp32_kernel<true><<<(unsigned)blocks, threads, 0, s>>>(a);
+  else d3q27_fp32_kernel<false><<<(unsigned)blocks, threads, 0, s>>>(a);
 }
 
 }  // namespace elbm
