@@ -188,7 +188,15 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--size", default=None, help="NXxNYxNZ override (profiling runs on a smaller box)")
+    ap.add_argument("--profile", action="store_true",
+                    help="timed steps only: no validation, end-to-end, FP64 or CPU legs (for ncu captures)")
     args = ap.parse_args()
+    if args.size:
+        global NX, NY, NZ
+        NX, NY, NZ = (int(v) for v in args.size.lower().split("x"))
+    if args.profile:
+        args.no_cpu_baseline = args.no_fp64 = True
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
@@ -242,6 +250,12 @@ def main():
     peak, peak_kind = measured_peak_hbm()
     achieved = BYTES_PER_NODE_FP32 * nodes_per_step / per_launch_s / 1e9
 
+    if args.profile:
+        if rank == 0:
+            print(json.dumps({"profile_run": True, "size": [NX, NY, NZ], "mlups": value, "ms_per_step": per_launch_s * 1e3,
+                              "achieved_gbs": achieved}), flush=True)
+        ctx.close()
+        return
     # entropy condition and fallbacks over a validation window (check mode, not timed)
     chk = cap.make_d3q27_params(**bp)
     chk.check_dH = 1
@@ -298,7 +312,8 @@ def main():
             "gpu_launches": args.steps,
             "clocks": clk,
             "wall_ms_per_step": wall / args.steps * 1e3,
-            "validation": {"max_abs_dH": vst["max_abs_dH"], "fallbacks": vst["fallbacks"],
+            "validation": {"max_abs_dH": vst["max_abs_dH"], "dh_over_tol": vst["dh_over_tol"],
+                           "fallbacks": vst["fallbacks"],
                            "exact_path_nodes": vst["exact_path_nodes"], "status": vst["status"],
                            "newton_iters_per_node": vst["newton_iters"] / max(1, vst["node_updates"])},
             "plain_fp64_newton_mlups": fp64,

@@ -77,6 +77,24 @@ typedef struct {
   double outl_feq[8][27];
 } elbm_d3q27_params;
 
+/* D3Q39 compressible level: the reference's background scalars (computed by the
+ * host like general/background_calcs/basic_fluids_calcs.f95, utilities/
+ * viscosity_and_timing.f95 and general/background_calcs/timing_calcs.f95). */
+typedef struct {
+  int32_t shifted;           /* Galilean-shifted lattice (directions_and_weights.f95:477-499) */
+  int32_t primary_flow_dir;  /* 1..6 */
+  int32_t turbulent;         /* closed-form entropic alpha (calculate_alpha.f95:118-289), else alpha = 2 */
+  int32_t lvl;               /* AMR level (beta_1 uses 2^(lvl+1)) */
+  int32_t startup_timesteps; /* start-up ramps of beta, epsilon and alpha */
+  int32_t max_lm_iters;      /* cap on the multiplier Newton (the reference has none) */
+  int32_t periodic;          /* bit 0/1/2: x/y/z periodic; this version requires 7 */
+  int32_t timestep;          /* timestep(amr_max_lvl) of the next step; advanced by elbm_level_step */
+  int32_t damp;              /* 1: run the negative-population repair of damp_it.f95 after collision */
+  int32_t pad;
+  double gama, t_ref, rho_ref, p_ref, mu_ref, kappa_ref, gas_const_R, const_vol, const_press, molec_weight;
+  double dt, elbm_epsilon, init_beta_1, init_beta_2, beta_1_scaling, beta_2_scaling;
+} elbm_d3q39_params;
+
 typedef struct {
   int64_t node_updates;     /* fluid nodes advanced, summed over steps */
   int64_t newton_iters;     /* total Newton iterations (scalar or per-population) */
@@ -85,6 +103,7 @@ typedef struct {
   uint32_t status;          /* ELBM_ST_* flags */
   uint32_t pad;
   double max_abs_dH;        /* check mode only */
+  int64_t dh_over_tol;      /* check mode: nodes whose |dH| exceeded tol_dH */
   double kernel_ms;         /* device time of the step kernels (CUDA events) */
 } elbm_stats;
 
@@ -103,6 +122,19 @@ int elbm_level_register(elbm_ctx* ctx, int lvl, int lattice, int storage, int nb
 
 /* D3Q27 physical parameters and boundary equilibria of a level. */
 int elbm_set_d3q27_params(elbm_ctx* ctx, int lvl, const elbm_d3q27_params* p);
+
+/* D3Q39 scalars of a level (replaces the module globals the reference's
+ * collision and flow-variable routines read). */
+int elbm_set_d3q39_params(elbm_ctx* ctx, int lvl, const elbm_d3q39_params* p);
+
+/* D3Q39 state of one box: fout, gout (39 comps), the 13 Lagrange multipliers
+ * (chi, zeta_xyz, pi_xx,yy,zz,xy,xz,yz, lambda_xyz; 13 comps) and the previous
+ * step's w velocity (1 comp), all as FABs with the level's ghost width. */
+int elbm_upload_level39(elbm_ctx* ctx, int lvl, int box, const double* fout, const double* gout, const double* lm,
+                        const double* w_vel);
+/* Any output pointer may be NULL.  macro: rho, u, v, w, T (5 comps). */
+int elbm_download_level39(elbm_ctx* ctx, int lvl, int box, double* fout, double* gout, double* lm, double* w_vel,
+                          double* alpha, double* macro);
 
 /* Node types and link codes of one box: the reference's integer `state` FAB
  * (Q components, ghost width ngrow_state; encoding of looping/timestepping/loop.f95:71-89,

@@ -11,7 +11,7 @@ import subprocess
 HERE = pathlib.Path(__file__).resolve().parent
 BUILD = HERE / "_build"
 LIB = BUILD / "liboracle.so"
-SOURCES = ["d3q27_oracle.c"]
+SOURCES = ["d3q27_oracle.c", "d3q39_oracle.c"]
 
 
 def build(verbose: bool = False) -> pathlib.Path:

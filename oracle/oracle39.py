@@ -1,0 +1,143 @@
+"""ctypes binding of the D3Q39 CPU oracle (test infrastructure only)."""
+from __future__ import annotations
+
+import ctypes as ct
+
+import numpy as np
+
+from . import oracle as _o27
+
+Q39 = 39
+NLM = 13
+
+
+class O39Consts(ct.Structure):
+    _fields_ = [
+        ("shifted", ct.c_int),
+        ("primary_flow_dir", ct.c_int),
+        ("turbulent", ct.c_int),
+        ("lvl", ct.c_int),
+        ("startup_timesteps", ct.c_int),
+        ("max_lm_iters", ct.c_int),
+        ("gama", ct.c_double),
+        ("t_ref", ct.c_double),
+        ("rho_ref", ct.c_double),
+        ("p_ref", ct.c_double),
+        ("mu_ref", ct.c_double),
+        ("kappa_ref", ct.c_double),
+        ("gas_const_R", ct.c_double),
+        ("const_vol", ct.c_double),
+        ("const_press", ct.c_double),
+        ("molec_weight", ct.c_double),
+        ("dt", ct.c_double),
+        ("elbm_epsilon", ct.c_double),
+        ("init_beta_1", ct.c_double),
+        ("init_beta_2", ct.c_double),
+        ("beta_1_scaling", ct.c_double),
+        ("beta_2_scaling", ct.c_double),
+        ("su_lm", ct.c_double * NLM),
+    ]
+
+
+class O39Stats(ct.Structure):
+    _fields_ = [(n, ct.c_int64) for n in ("nodes", "lm_iters", "lm_capped", "alpha_not2", "damped", "errors")]
+
+
+class O39Level(ct.Structure):
+    _fields_ = [("nx", ct.c_int), ("ny", ct.c_int), ("nz", ct.c_int)] + [
+        (n, ct.c_void_p) for n in ("fout", "gout", "lm", "w_vel", "alpha", "rho", "u", "v", "temp")]
+
+
+def lib():
+    L = _o27.lib()
+    vp = ct.c_void_p
+    if not getattr(L, "_o39_ready", False):
+        L.o39_step_periodic.restype = ct.c_int
+        L.o39_step_periodic.argtypes = [ct.POINTER(O39Consts), ct.POINTER(O39Level), ct.c_int, ct.POINTER(O39Stats)]
+        L.o39_init_node.restype = ct.c_int
+        L.o39_init_node.argtypes = [ct.POINTER(O39Consts)] + [ct.c_double] * 5 + [vp, vp, vp]
+        L.o39_lagrange_api.restype = ct.c_int
+        L.o39_lagrange_api.argtypes = [ct.POINTER(O39Consts)] + [ct.c_double] * 5 + [vp, vp, vp]
+        L.o39_alpha.restype = ct.c_double
+        L.o39_alpha.argtypes = [ct.POINTER(O39Consts), vp, vp, ct.c_double, ct.c_int]
+        L.o39_tables.restype = None
+        L.o39_tables.argtypes = [ct.c_int, ct.c_int, vp, vp, vp, vp]
+        L._o39_ready = True
+    return L
+
+
+def _p(a):
+    return a.ctypes.data_as(ct.c_void_p)
+
+
+def consts(c) -> O39Consts:
+    """O39Consts from a D3Q39Consts dataclass (same field names)."""
+    k = O39Consts()
+    for name, _ in O39Consts._fields_:
+        if name == "su_lm":
+            for i, v in enumerate(c.su_lm):
+                k.su_lm[i] = v
+        else:
+            setattr(k, name, getattr(c, name))
+    return k
+
+
+def tables(shifted, pfd=1):
+    cx, cy, cz, opp = (np.zeros(Q39, np.int32) for _ in range(4))
+    lib().o39_tables(shifted, pfd, _p(cx), _p(cy), _p(cz), _p(opp))
+    return cx, cy, cz, opp
+
+
+def lagrange(k: O39Consts, rho, u, v, w, T, P, lm0):
+    P = np.ascontiguousarray(P, np.float64)
+    lm = np.ascontiguousarray(lm0, np.float64).copy()
+    fe = np.zeros(Q39)
+    it = lib().o39_lagrange_api(ct.byref(k), rho, u, v, w, T, _p(P), _p(lm), _p(fe))
+    return lm, fe, it
+
+
+def init_node(k: O39Consts, rho, u, v, w, T, lm0):
+    lm = np.ascontiguousarray(lm0, np.float64).copy()
+    f = np.zeros(Q39)
+    g = np.zeros(Q39)
+    it = lib().o39_init_node(ct.byref(k), rho, u, v, w, T, _p(lm), _p(f), _p(g))
+    return lm, f, g, it
+
+
+def alpha(k: O39Consts, f, fd, T, step):
+    return lib().o39_alpha(ct.byref(k), _p(np.ascontiguousarray(f, np.float64)),
+                           _p(np.ascontiguousarray(fd, np.float64)), T, step)
+
+
+class Level39:
+    """Level state for the periodic-box oracle (component-major, x fastest)."""
+
+    def __init__(self, nx, ny, nz):
+        self.shape = (nz, ny, nx)
+        N = nx * ny * nz
+        self.fout = np.zeros((Q39,) + self.shape)
+        self.gout = np.zeros((Q39,) + self.shape)
+        self.lm = np.zeros((NLM,) + self.shape)
+        self.w_vel = np.zeros(self.shape)
+        self.alpha = np.zeros(self.shape)
+        self.rho = np.zeros(self.shape)
+        self.u = np.zeros(self.shape)
+        self.v = np.zeros(self.shape)
+        self.temp = np.zeros(self.shape)
+        self.nx, self.ny, self.nz, self.N = nx, ny, nz, N
+
+    def c(self):
+        s = O39Level()
+        s.nx, s.ny, s.nz = self.nx, self.ny, self.nz
+        for n in ("fout", "gout", "lm", "w_vel", "alpha", "rho", "u", "v", "temp"):
+            setattr(s, n, getattr(self, n).ctypes.data)
+        return s
+
+
+def step_periodic(k: O39Consts, lev: Level39, step: int):
+    st = O39Stats()
+    s = lev.c()
+    rc = lib().o39_step_periodic(ct.byref(k), ct.byref(s), step, ct.byref(st))
+    if rc != 0:
+        raise RuntimeError(f"o39 step failed {rc}")
+    return {n: getattr(st, n) for n, _ in st._fields_}

@@ -42,7 +42,7 @@ def test_struct_layout_matches_header(pkg, tmp_path):
 int main(void) {{
   printf("%zu %zu %zu %zu %zu\\n", sizeof(elbm_d3q27_params), offsetof(elbm_d3q27_params, outlet_type),
          offsetof(elbm_d3q27_params, fs_feq), offsetof(elbm_d3q27_params, outl_feq), sizeof(elbm_stats));
-  printf("%zu %zu\\n", offsetof(elbm_stats, status), offsetof(elbm_stats, kernel_ms));
+  printf("%zu %zu %zu\\n", offsetof(elbm_stats, status), offsetof(elbm_stats, kernel_ms), sizeof(elbm_d3q39_params));
   return 0;
 }}
 """)
@@ -51,5 +51,5 @@ int main(void) {{
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
     P, S = cap.D3Q27Params, cap.Stats
     expect = [ct.sizeof(P), P.outlet_type.offset, P.fs_feq.offset, P.outl_feq.offset, ct.sizeof(S), S.status.offset,
-              S.kernel_ms.offset]
+              S.kernel_ms.offset, ct.sizeof(cap.D3Q39Params)]
     assert list(map(int, out)) == expect

@@ -85,8 +85,8 @@ def test_fp32_entropy_condition(pkg, built_lib):
     ctx, *_ = _setup(pkg, 64, 32, 32, pkg.capi.ELBM_STORE_FP32_DEV, nu=2e-5, noise=5e-3, check_dH=1,
                      u0=(0.06, 0.0, 0.0))
     stats = ctx.step(0, 50)
-    assert stats["max_abs_dH"] <= 1e-10, stats
     assert stats["fallbacks"] == 0, stats
+    assert stats["dh_over_tol"] == 0 and stats["max_abs_dH"] <= 1e-10, stats
 
 
 @pytest.mark.parametrize("storage", [0, 1])
@@ -112,7 +112,9 @@ def test_fab_ghosts_round_trip(pkg, built_lib):
         out = np.zeros_like(fab)
         ctx.download(0, 0, out)
         inner = (slice(None), slice(g, g + nz), slice(g, g + ny), slice(g, g + nx))
-        assert np.max(np.abs(out[inner] - fab[inner]) / fab[inner]) <= tol
+        # FP32 deviation storage rounds d = f - w to float: error <= 2^-24 |f - w|
+        dev = np.abs(fab[inner] - pkg.lattice.W[:, None, None, None])
+        assert np.all(np.abs(out[inner] - fab[inner]) <= tol * dev + 1e-300)
         ctx.close()
 
 

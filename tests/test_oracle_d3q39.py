@@ -1,0 +1,106 @@
+"""CPU checks of the D3Q39 reference restatement (no GPU).  The reference has no
+tests or golden data; these known-answer invariants pin the oracle."""
+import numpy as np
+import pytest
+
+
+@pytest.fixture(scope="module")
+def o39():
+    from oracle import oracle39
+
+    oracle39.lib()
+    return oracle39
+
+
+@pytest.fixture(scope="module")
+def setup39(pkg):
+    import importlib
+
+    return importlib.import_module(pkg.__name__ + ".d3q39_setup")
+
+
+def test_tables(o39):
+    cx, cy, cz, opp = o39.tables(0, 1)
+    c = np.stack([cx, cy, cz], 1)
+    assert (c[opp] == -c).all() and (opp[opp] == np.arange(39)).all()
+    assert sorted(np.abs(c).sum(1)) .count(0) == 1
+    sx, sy, sz, sopp = o39.tables(1, 1)  # Galilean shift along +x (directions_and_weights.f95:477-499)
+    assert (sx == cx + 1).all() and (sy == cy).all() and (sopp == np.arange(39)).all()
+
+
+def test_reference_scales(setup39):
+    c = setup39.wedge_case_consts()
+    assert c.shifted == 1 and abs(c.mach - 1.5) < 1e-12
+    assert abs(c.temperature - 1 / 1.4) < 1e-15 and abs(c.const_vol - 2.5) < 1e-12
+    # sutherland constants are single-precision literals in the reference
+    assert c.dt == c.elbm_epsilon and c.dt > 0
+
+
+@pytest.mark.parametrize("shifted", [0, 1])
+def test_lagrange_reproduces_moments(o39, setup39, shifted):
+    c = setup39.wedge_case_consts(use_shifted=bool(shifted))
+    if not shifted:
+        c = setup39.reference_consts(288.15, 101325.0, 0.3 * 340.29, 1e-4)
+    k = o39.consts(c)
+    cx, cy, cz, _ = o39.tables(c.shifted, 1)
+    cmag = cx * cx + cy * cy + cz * cz
+    rng = np.random.default_rng(2)
+    for _ in range(5):
+        rho = 1 + rng.uniform(-0.05, 0.05)
+        u = c.mach * (1 + rng.uniform(-0.05, 0.05)) if shifted else rng.uniform(-0.1, 0.3)
+        v, w = rng.uniform(-0.05, 0.05, 2)
+        T = c.temperature * (1 + rng.uniform(-0.03, 0.03))
+        P = [rho * (T + u * u), rho * (T + v * v), rho * (T + w * w), rho * u * v, rho * u * w, rho * v * w]
+        lm, fe, it = o39.lagrange(k, rho, u, v, w, T, P, setup39.freestream_start_lm(c))
+        assert 0 < it < 50
+        # the returned equilibrium is evaluated before the last update: residual ~ Newton step
+        q = (rho * (u * u + v * v + w * w) + 5 * rho * T) * np.array([u, v, w])
+        assert abs(fe.sum() - rho) < 1e-6
+        assert np.allclose([(cx * fe).sum(), (cy * fe).sum(), (cz * fe).sum()], rho * np.array([u, v, w]), atol=1e-6)
+        assert np.allclose([(cx * cx * fe).sum(), (cy * cy * fe).sum(), (cz * cz * fe).sum()], P[:3], atol=1e-6)
+        assert np.allclose([(cx * cmag * fe).sum(), (cy * cmag * fe).sum(), (cz * cmag * fe).sum()], q, atol=1e-5)
+
+
+def _uniform_level(o39, setup39, c, k, nx, ny, nz, noise=0.0, seed=0):
+    lev = o39.Level39(nx, ny, nz)
+    rng = np.random.default_rng(seed)
+    lm0 = setup39.freestream_start_lm(c)
+    for z in range(nz):
+        for y in range(ny):
+            for x in range(nx):
+                rho = 1.0 + noise * rng.uniform(-1, 1)
+                u = c.mach * (1 + noise * rng.uniform(-1, 1))
+                v, w = noise * rng.uniform(-1, 1, 2)
+                T = c.temperature * (1 + noise * rng.uniform(-1, 1))
+                lm, f, g, it = o39.init_node(k, rho, u, v, w, T, lm0)
+                lev.fout[:, z, y, x] = f
+                lev.gout[:, z, y, x] = g
+                lev.lm[:, z, y, x] = lm
+                lev.w_vel[z, y, x] = w
+    return lev
+
+
+def test_periodic_uniform_flow_is_steady(o39, setup39):
+    c = setup39.wedge_case_consts()
+    k = o39.consts(c)
+    lev = _uniform_level(o39, setup39, c, k, 4, 3, 3)
+    f0 = lev.fout.copy()
+    for step in range(3):
+        st = o39.step_periodic(k, lev, step)
+    assert st["lm_capped"] == 0
+    assert np.max(np.abs(lev.fout - f0) / np.abs(f0)) < 1e-6
+
+
+def test_periodic_box_conserves_mass_and_momentum(o39, setup39):
+    c = setup39.wedge_case_consts()
+    k = o39.consts(c)
+    lev = _uniform_level(o39, setup39, c, k, 5, 4, 4, noise=0.01, seed=3)
+    cx, _, _, _ = o39.tables(1, 1)
+    m0 = lev.fout.sum()
+    j0 = np.tensordot(cx.astype(float), lev.fout, axes=(0, 0)).sum()
+    for step in range(4):
+        st = o39.step_periodic(k, lev, 150 + step)  # past start-up: closed-form alpha, full betas
+    assert st["lm_capped"] == 0
+    assert abs(lev.fout.sum() - m0) / m0 < 1e-6
+    assert abs(np.tensordot(cx.astype(float), lev.fout, axes=(0, 0)).sum() - j0) / abs(j0) < 1e-6
+    assert np.isfinite(lev.alpha).all()

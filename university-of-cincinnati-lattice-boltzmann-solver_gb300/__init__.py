@@ -6,6 +6,6 @@ package holds its build recipe, the ctypes binding used by Python callers and
 tests, and host-side set-up helpers (lattice tables, boundary equilibria,
 state arrays for box geometries).
 """
-from . import capi, geometry, lattice  # noqa: F401
+from . import capi, d3q39_setup, geometry, lattice  # noqa: F401
 from .build import build  # noqa: F401
 from .capi import Context, ElbmError, make_d3q27_params  # noqa: F401

@@ -26,6 +26,11 @@ NVFLAGS = ARCH + [
 ]
 
 
+# Per-file flags: the FP64 D3Q39 step keeps separately rounded multiply and add
+# (no contraction), like the CPU restatement it is checked against.
+FILE_FLAGS = {"d3q39_step.cu": ["-fmad=false"]}
+
+
 def _nvcc() -> str:
     for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
         if cand and os.path.exists(cand):
@@ -49,7 +54,7 @@ def build(verbose: bool = False, force: bool = False) -> pathlib.Path:
         obj = BUILD / (src.stem + ".o")
         if not force and obj.exists() and obj.stat().st_mtime > max(src.stat().st_mtime, newest_header):
             return obj
-        cmd = [nvcc, *NVFLAGS, "-c", str(src), "-o", str(obj)]
+        cmd = [nvcc, *NVFLAGS, *FILE_FLAGS.get(src.name, []), "-c", str(src), "-o", str(obj)]
         if verbose:
             print(" ".join(cmd))
         subprocess.run(cmd, check=True)

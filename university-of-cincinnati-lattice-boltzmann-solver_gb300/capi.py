@@ -53,6 +53,31 @@ class D3Q27Params(ct.Structure):
     ]
 
 
+class D3Q39Params(ct.Structure):
+    _fields_ = [(n, ct.c_int32) for n in ("shifted", "primary_flow_dir", "turbulent", "lvl", "startup_timesteps",
+                                         "max_lm_iters", "periodic", "timestep", "damp", "pad")] + [
+        (n, ct.c_double) for n in ("gama", "t_ref", "rho_ref", "p_ref", "mu_ref", "kappa_ref", "gas_const_R",
+                                   "const_vol", "const_press", "molec_weight", "dt", "elbm_epsilon", "init_beta_1",
+                                   "init_beta_2", "beta_1_scaling", "beta_2_scaling")]
+
+
+def make_d3q39_params(consts, timestep=0, periodic=7, damp=1) -> D3Q39Params:
+    """D3Q39Params from a d3q39_setup.D3Q39Consts."""
+    p = D3Q39Params()
+    for name, _ in D3Q39Params._fields_:
+        if name == "periodic":
+            p.periodic = periodic
+        elif name == "timestep":
+            p.timestep = timestep
+        elif name == "damp":
+            p.damp = damp
+        elif name == "pad":
+            p.pad = 0
+        else:
+            setattr(p, name, getattr(consts, name))
+    return p
+
+
 class Stats(ct.Structure):
     _fields_ = [
         ("node_updates", ct.c_int64),
@@ -62,6 +87,7 @@ class Stats(ct.Structure):
         ("status", ct.c_uint32),
         ("pad", ct.c_uint32),
         ("max_abs_dH", ct.c_double),
+        ("dh_over_tol", ct.c_int64),
         ("kernel_ms", ct.c_double),
     ]
 
@@ -81,6 +107,9 @@ SIGNATURES = {
     "elbm_download_alpha": (_c_int, [_vp, _c_int, _c_int, _vp]),
     "elbm_level_step": (_c_int, [_vp, _c_int, _c_int, ct.POINTER(Stats)]),
     "elbm_sync": (_c_int, [_vp]),
+    "elbm_set_d3q39_params": (_c_int, [_vp, _c_int, ct.POINTER(D3Q39Params)]),
+    "elbm_upload_level39": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _vp]),
+    "elbm_download_level39": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
 }
 
 _lib = None
@@ -213,6 +242,23 @@ class Context:
             return st.as_dict()
         self._check(self.lib.elbm_level_step(self.h, lvl, nsteps, None))
         return None
+
+    def set_d3q39_params(self, lvl, params: D3Q39Params):
+        self._check(self.lib.elbm_set_d3q39_params(self.h, lvl, ct.byref(params)))
+
+    def upload39(self, lvl, box, fout, gout, lm, w_vel):
+        arrs = [np.ascontiguousarray(a, np.float64) for a in (fout, gout, lm, w_vel)]
+        self._check(self.lib.elbm_upload_level39(self.h, lvl, box, *map(_ptr, arrs)))
+
+    def download39(self, lvl, box=0):
+        """Returns dict with fout, gout, lm, w_vel, alpha, macro (FAB layouts)."""
+        shp = self.box_shape(lvl, box)
+        out = {"fout": np.zeros((39,) + shp), "gout": np.zeros((39,) + shp), "lm": np.zeros((13,) + shp),
+               "w_vel": np.zeros(shp), "alpha": np.zeros(shp), "macro": np.zeros((5,) + shp)}
+        self._check(self.lib.elbm_download_level39(self.h, lvl, box, *(_ptr(out[k]) for k in
+                                                                      ("fout", "gout", "lm", "w_vel", "alpha",
+                                                                       "macro"))))
+        return out
 
     def sync(self):
         self._check(self.lib.elbm_sync(self.h))

@@ -13,6 +13,7 @@
 
 #include "../../include/elbm_gb300.h"
 #include "kernels.cuh"
+#include "kernels39.cuh"
 #include "lattice.cuh"
 
 using namespace elbm;
@@ -64,6 +65,10 @@ struct Box {
   DevBuf<uint16_t> words;
   DevBuf<float> alpha;
   DevBuf<double> staging;  // FP64 packed staging for FP32 conversion
+  // D3Q39: g populations, multipliers, previous w, alpha and macroscopic fields
+  DevBuf<uint8_t> gbuf[2];
+  int gcur = 0;
+  DevBuf<double> lm, w_vel, alpha64, macro;
   int64_t fluid_nodes = 0, boundary_nodes = 0;
   bool links_set = false, data_set = false;
 };
@@ -73,6 +78,7 @@ struct Level {
   int lattice = 0, storage = 0, ngrow = 0;
   std::vector<std::unique_ptr<Box>> boxes;
   elbm_d3q27_params p27{};
+  elbm_d3q39_params p39{};
   bool params_set = false;
   DevBuf<uint8_t> eq;  // kEqTables x Q, FP64 or FP32 deviations
 };
@@ -278,6 +284,93 @@ int decode_link27(const int32_t* st, int64_t fab_plane, int64_t sidx, const int 
   return ELBM_E_UNSUPPORTED;
 }
 
+
+int finish_stats(elbm_ctx* c, elbm_stats* out) {
+  if (!out) return ELBM_OK;
+  DevStats ds{};
+  CUDA_TRY(cudaMemcpyAsync(&ds, c->stats.p, sizeof ds, cudaMemcpyDeviceToHost, c->stream), "stats");
+  CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  float ms = 0.f;
+  CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1), "elapsed");
+  std::memset(out, 0, sizeof *out);
+  out->node_updates = (int64_t)ds.node_updates;
+  out->newton_iters = (int64_t)ds.newton_iters;
+  out->exact_path_nodes = (int64_t)ds.exact_nodes;
+  out->fallbacks = (int64_t)ds.fallbacks;
+  out->status = ds.status;
+  double mx;
+  std::memcpy(&mx, &ds.max_dH_bits, sizeof mx);
+  out->max_abs_dH = mx;
+  out->dh_over_tol = (int64_t)ds.dh_over;
+  out->kernel_ms = ms;
+  return ELBM_OK;
+}
+
+// D3Q39 level steps: fused stream/flow-variables/collision, then the optional repair.
+int step39(elbm_ctx* c, Level& lv, int nsteps) {
+  const elbm_d3q39_params& p = lv.p39;
+  for (auto& bp : lv.boxes)
+    if (!bp->data_set) return fail(c, ELBM_E_STATE, "populations missing");
+  CUDA_TRY(cudaEventRecord(c->ev0, c->stream), "event");
+  for (int s = 0; s < nsteps; ++s) {
+    for (auto& bp : lv.boxes) {
+      Box& b = *bp;
+      Step39Args a{};
+      a.fsrc = (const double*)b.buf[b.cur].p;
+      a.gsrc = (const double*)b.gbuf[b.gcur].p;
+      a.fdst = (double*)b.buf[b.cur ^ 1].p;
+      a.gdst = (double*)b.gbuf[b.gcur ^ 1].p;
+      a.lm = b.lm.p;
+      a.w_vel = b.w_vel.p;
+      a.alpha = b.alpha64.p;
+      a.macro = b.macro.p;
+      a.plane = b.plane;
+      a.nx = b.nx;
+      a.ny = b.ny;
+      a.nz = b.nz;
+      a.N = b.N;
+      a.step = lv.p39.timestep;
+      a.stats = c->stats.p;
+      D3Q39Dev& k = a.k;
+      k.shifted = p.shifted;
+      k.primary_flow_dir = p.primary_flow_dir;
+      k.turbulent = p.turbulent;
+      k.lvl = p.lvl;
+      k.startup_timesteps = p.startup_timesteps;
+      k.max_lm_iters = p.max_lm_iters;
+      k.gama = p.gama;
+      k.t_ref = p.t_ref;
+      k.rho_ref = p.rho_ref;
+      k.p_ref = p.p_ref;
+      k.mu_ref = p.mu_ref;
+      k.kappa_ref = p.kappa_ref;
+      k.gas_const_R = p.gas_const_R;
+      k.const_vol = p.const_vol;
+      k.const_press = p.const_press;
+      k.molec_weight = p.molec_weight;
+      k.dt = p.dt;
+      k.elbm_epsilon = p.elbm_epsilon;
+      k.init_beta_1 = p.init_beta_1;
+      k.init_beta_2 = p.init_beta_2;
+      k.beta_1_scaling = p.beta_1_scaling;
+      k.beta_2_scaling = p.beta_2_scaling;
+      launch_d3q39_fp64(a, c->stream);
+      CUDA_TRY(cudaGetLastError(), "d3q39 step launch");
+      b.cur ^= 1;
+      b.gcur ^= 1;
+      if (p.damp) {
+        launch_d3q39_damp((const double*)b.buf[b.cur].p, (double*)b.buf[b.cur ^ 1].p, b.nx, b.ny, b.nz, b.plane,
+                          c->stats.p, c->stream);
+        CUDA_TRY(cudaGetLastError(), "d3q39 damp launch");
+        b.cur ^= 1;
+      }
+    }
+    lv.p39.timestep += 1;  // steps_counter.f95:18-31
+  }
+  CUDA_TRY(cudaEventRecord(c->ev1, c->stream), "event");
+  return ELBM_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -313,8 +406,10 @@ const char* elbm_last_error_string(const elbm_ctx* c) { return c ? c->err.c_str(
 int elbm_level_register(elbm_ctx* c, int lvl, int lattice, int storage, int nbox, const int32_t* lo_hi, int ngrow) {
   if (!c) return ELBM_E_ARG;
   if (lvl < 0 || lvl > 30) return fail(c, ELBM_E_ARG, "level %d out of range", lvl);
-  if (lattice != ELBM_D3Q27) return fail(c, ELBM_E_UNSUPPORTED, "lattice %d not supported by this entry point", lattice);
+  if (lattice != ELBM_D3Q27 && lattice != ELBM_D3Q39) return fail(c, ELBM_E_UNSUPPORTED, "lattice %d", lattice);
   if (storage != ELBM_STORE_FP64 && storage != ELBM_STORE_FP32_DEV) return fail(c, ELBM_E_ARG, "bad storage %d", storage);
+  if (lattice == ELBM_D3Q39 && storage != ELBM_STORE_FP64)
+    return fail(c, ELBM_E_UNSUPPORTED, "the D3Q39 path stores FP64 populations");
   if (nbox != 1) return fail(c, ELBM_E_UNSUPPORTED, "only single-box levels are supported (nbox=%d)", nbox);
   if (!lo_hi || ngrow < 0) return fail(c, ELBM_E_ARG, "null lo_hi or negative ngrow");
   CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
@@ -336,8 +431,16 @@ int elbm_level_register(elbm_ctx* c, int lvl, int lattice, int storage, int nbox
     b->nz = b->hi[2] - b->lo[2] + 1;
     b->N = (int64_t)b->nx * b->ny * b->nz;
     b->plane = (b->N + 31) / 32 * 32;
-    const size_t bytes = (size_t)b->plane * Q27 * elem_size(storage);
+    const int q = lattice;
+    const size_t bytes = (size_t)b->plane * q * elem_size(storage);
     for (int s = 0; s < 2; ++s) CUDA_TRY(b->buf[s].alloc(bytes), "population buffers");
+    if (lattice == ELBM_D3Q39) {
+      for (int s = 0; s < 2; ++s) CUDA_TRY(b->gbuf[s].alloc(bytes), "g buffers");
+      CUDA_TRY(b->lm.alloc((size_t)b->plane * 13), "multipliers");
+      CUDA_TRY(b->w_vel.alloc((size_t)b->plane), "w");
+      CUDA_TRY(b->alpha64.alloc((size_t)b->plane), "alpha");
+      CUDA_TRY(b->macro.alloc((size_t)b->plane * 5), "macro");
+    }
     CUDA_TRY(b->ntype.alloc(b->N), "node types");
     CUDA_TRY(cudaMemsetAsync(b->ntype.p, 0, b->N, c->stream), "memset");
     lv.boxes.push_back(std::move(b));
@@ -350,6 +453,7 @@ int elbm_level_register(elbm_ctx* c, int lvl, int lattice, int storage, int nbox
 int elbm_set_d3q27_params(elbm_ctx* c, int lvl, const elbm_d3q27_params* p) {
   Level* lv = get_level(c, lvl);
   if (!lv || !p) return fail(c, ELBM_E_ARG, "unknown level or null params");
+  if (lv->lattice != ELBM_D3Q27) return fail(c, ELBM_E_ARG, "level %d is not a D3Q27 level", lvl);
   if (!(p->nu > 0.0) || p->max_newton < 1 || p->alpha_mode < 0 || p->alpha_mode > 2)
     return fail(c, ELBM_E_ARG, "bad D3Q27 parameters");
   if (p->alpha_mode == ELBM_ALPHA_LEARNED) return fail(c, ELBM_E_UNSUPPORTED, "learned alpha needs a trained network");
@@ -380,6 +484,7 @@ int elbm_set_links(elbm_ctx* c, int lvl, int box, const int32_t* state, int ngro
   Level* lv = nullptr;
   Box* b = get_box(c, lvl, box, &lv);
   if (!b || !state || ngrow_state < 0) return fail(c, ELBM_E_ARG, "unknown level/box or null state");
+  if (lv->lattice != ELBM_D3Q27) return fail(c, ELBM_E_UNSUPPORTED, "link tables of D3Q39 levels are not supported");
   if (!lv->params_set) return fail(c, ELBM_E_STATE, "set the level parameters before the links");
   const int g = ngrow_state;
   const int fx = b->nx + 2 * g, fy = b->ny + 2 * g, fz = b->nz + 2 * g;
@@ -436,6 +541,7 @@ int elbm_upload_level(elbm_ctx* c, int lvl, int box, const double* fout) {
   Level* lv = nullptr;
   Box* b = get_box(c, lvl, box, &lv);
   if (!b || !fout) return fail(c, ELBM_E_ARG, "unknown level/box or null data");
+  if (lv->lattice != ELBM_D3Q27) return fail(c, ELBM_E_ARG, "use elbm_upload_level39 for D3Q39 levels");
   CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
   if (lv->storage == ELBM_STORE_FP64) {
     CUDA_TRY(fab_to_packed(fout, (double*)b->buf[0].p, *b, lv->ngrow, Q27, b->plane, c->stream), "upload");
@@ -457,6 +563,7 @@ int elbm_download_level(elbm_ctx* c, int lvl, int box, double* fout) {
   Level* lv = nullptr;
   Box* b = get_box(c, lvl, box, &lv);
   if (!b || !fout) return fail(c, ELBM_E_ARG, "unknown level/box or null data");
+  if (lv->lattice != ELBM_D3Q27) return fail(c, ELBM_E_ARG, "use elbm_download_level39 for D3Q39 levels");
   if (!b->data_set) return fail(c, ELBM_E_STATE, "no populations uploaded");
   CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
   if (lv->storage == ELBM_STORE_FP64) {
@@ -491,6 +598,11 @@ int elbm_level_step(elbm_ctx* c, int lvl, int nsteps, elbm_stats* out) {
   if (!lv->params_set) return fail(c, ELBM_E_STATE, "level parameters not set");
   CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
   CUDA_TRY(cudaMemsetAsync(c->stats.p, 0, sizeof(DevStats), c->stream), "stats reset");
+  if (lv->lattice == ELBM_D3Q39) {
+    const int rc = step39(c, *lv, nsteps);
+    if (rc) return rc;
+    return finish_stats(c, out);
+  }
   const elbm_d3q27_params& p = lv->p27;
   for (auto& bp : lv->boxes) {
     Box& b = *bp;
@@ -528,24 +640,7 @@ int elbm_level_step(elbm_ctx* c, int lvl, int nsteps, elbm_stats* out) {
     }
   }
   CUDA_TRY(cudaEventRecord(c->ev1, c->stream), "event");
-  if (out) {
-    DevStats ds{};
-    CUDA_TRY(cudaMemcpyAsync(&ds, c->stats.p, sizeof ds, cudaMemcpyDeviceToHost, c->stream), "stats");
-    CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
-    float ms = 0.f;
-    CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1), "elapsed");
-    std::memset(out, 0, sizeof *out);
-    out->node_updates = (int64_t)ds.node_updates;
-    out->newton_iters = (int64_t)ds.newton_iters;
-    out->exact_path_nodes = (int64_t)ds.exact_nodes;
-    out->fallbacks = (int64_t)ds.fallbacks;
-    out->status = ds.status;
-    double mx;
-    std::memcpy(&mx, &ds.max_dH_bits, sizeof mx);
-    out->max_abs_dH = mx;
-    out->kernel_ms = ms;
-  }
-  return ELBM_OK;
+  return finish_stats(c, out);
 }
 
 int elbm_sync(elbm_ctx* c) {
@@ -555,4 +650,63 @@ int elbm_sync(elbm_ctx* c) {
   return ELBM_OK;
 }
 
+int elbm_set_d3q39_params(elbm_ctx* c, int lvl, const elbm_d3q39_params* p) {
+  Level* lv = get_level(c, lvl);
+  if (!lv || !p) return fail(c, ELBM_E_ARG, "unknown level or null params");
+  if (lv->lattice != ELBM_D3Q39) return fail(c, ELBM_E_ARG, "level %d is not a D3Q39 level", lvl);
+  if (p->periodic != 7) return fail(c, ELBM_E_UNSUPPORTED, "D3Q39 levels must be periodic on all axes in this version");
+  if (p->primary_flow_dir < 1 || p->primary_flow_dir > 6 || p->max_lm_iters < 1 || p->startup_timesteps < 1 ||
+      !(p->t_ref > 0) || !(p->mu_ref > 0) || !(p->kappa_ref > 0) || !(p->dt > 0))
+    return fail(c, ELBM_E_ARG, "bad D3Q39 parameters");
+  lv->p39 = *p;
+  Lattice39 L;
+  build_lattice39(p->shifted, p->primary_flow_dir, L);
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  upload_lattice39(L, c->stream);
+  CUDA_TRY(cudaGetLastError(), "lattice upload");
+  CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  lv->params_set = true;
+  return ELBM_OK;
+}
+
+int elbm_upload_level39(elbm_ctx* c, int lvl, int box, const double* fout, const double* gout, const double* lm,
+                        const double* w_vel) {
+  Level* lv = nullptr;
+  Box* b = get_box(c, lvl, box, &lv);
+  if (!b || !fout || !gout || !lm || !w_vel) return fail(c, ELBM_E_ARG, "unknown level/box or null data");
+  if (lv->lattice != ELBM_D3Q39) return fail(c, ELBM_E_ARG, "not a D3Q39 level");
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  CUDA_TRY(fab_to_packed(fout, (double*)b->buf[0].p, *b, lv->ngrow, 39, b->plane, c->stream), "upload f");
+  CUDA_TRY(fab_to_packed(gout, (double*)b->gbuf[0].p, *b, lv->ngrow, 39, b->plane, c->stream), "upload g");
+  CUDA_TRY(fab_to_packed(lm, b->lm.p, *b, lv->ngrow, 13, b->plane, c->stream), "upload lm");
+  CUDA_TRY(fab_to_packed(w_vel, b->w_vel.p, *b, lv->ngrow, 1, b->plane, c->stream), "upload w");
+  CUDA_TRY(cudaMemsetAsync(b->alpha64.p, 0, b->alpha64.n * sizeof(double), c->stream), "alpha");
+  CUDA_TRY(cudaMemsetAsync(b->macro.p, 0, b->macro.n * sizeof(double), c->stream), "macro");
+  CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  b->cur = 0;
+  b->gcur = 0;
+  b->data_set = true;
+  return ELBM_OK;
+}
+
+int elbm_download_level39(elbm_ctx* c, int lvl, int box, double* fout, double* gout, double* lm, double* w_vel,
+                          double* alpha, double* macro) {
+  Level* lv = nullptr;
+  Box* b = get_box(c, lvl, box, &lv);
+  if (!b) return fail(c, ELBM_E_ARG, "unknown level/box");
+  if (lv->lattice != ELBM_D3Q39) return fail(c, ELBM_E_ARG, "not a D3Q39 level");
+  if (!b->data_set) return fail(c, ELBM_E_STATE, "no populations uploaded");
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  const int g = lv->ngrow;
+  if (fout) CUDA_TRY(packed_to_fab((const double*)b->buf[b->cur].p, fout, *b, g, 39, b->plane, c->stream), "f");
+  if (gout) CUDA_TRY(packed_to_fab((const double*)b->gbuf[b->gcur].p, gout, *b, g, 39, b->plane, c->stream), "g");
+  if (lm) CUDA_TRY(packed_to_fab((const double*)b->lm.p, lm, *b, g, 13, b->plane, c->stream), "lm");
+  if (w_vel) CUDA_TRY(packed_to_fab((const double*)b->w_vel.p, w_vel, *b, g, 1, b->plane, c->stream), "w");
+  if (alpha) CUDA_TRY(packed_to_fab((const double*)b->alpha64.p, alpha, *b, g, 1, b->plane, c->stream), "alpha");
+  if (macro) CUDA_TRY(packed_to_fab((const double*)b->macro.p, macro, *b, g, 5, b->plane, c->stream), "macro");
+  CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  return ELBM_OK;
+}
+
 }  // extern "C"
+

@@ -75,6 +75,7 @@ __device__ __forceinline__ void store_dst(T* __restrict__ dst, int64_t plane, in
 __device__ __forceinline__ void warp_stats(DevStats* st, bool active, unsigned iters, bool exact, bool fb,
                                            unsigned flags, double dH) {
   const unsigned mask = __activemask();
+  const unsigned nover = __popc(__ballot_sync(mask, (flags & 0x8u) != 0));
   const unsigned nact = __popc(__ballot_sync(mask, active));
   const unsigned nexact = __popc(__ballot_sync(mask, exact));
   const unsigned nfb = __popc(__ballot_sync(mask, fb));
@@ -91,6 +92,7 @@ __device__ __forceinline__ void warp_stats(DevStats* st, bool active, unsigned i
     if (nexact) atomicAdd(&st->exact_nodes, (unsigned long long)nexact);
     if (nfb) atomicAdd(&st->fallbacks, (unsigned long long)nfb);
     if (fl) atomicOr(&st->status, fl);
+    if (nover) atomicAdd(&st->dh_over, (unsigned long long)nover);
     const unsigned long long m = ((unsigned long long)hi << 32) | lo;
     if (m) atomicMax(&st->max_dH_bits, m);
   }
@@ -274,31 +276,53 @@ struct AlphaOut {
   bool fallback;
 };
 
-// FP64 sum over the populations with |y| > kYSmall: G_L(alpha), G_L'(alpha).
-__device__ __noinline__ void large_terms(const float (&d)[Q], const float (&D)[Q], double alpha, double& GL,
-                                         double& GLp) {
-  GL = 0.0;
-  GLp = 0.0;
+// phi(x) = (1+x) ln(1+x) - x and ln(1+x) in FP32: 12-term series for |x| < 1/8,
+// the direct form (log1pf) beyond, where the cancellation costs at most ~8x.
+__device__ __forceinline__ void phi_log1p32(float x, float& phi, float& l1) {
+  if (fabsf(x) < 0.125f) {
+    float lp = 1.0f / 12.0f, pp = 1.0f / 132.0f;
+#pragma unroll
+    for (int m = 11; m >= 1; --m) lp = fmaf(lp, -x, 1.0f / m);
+#pragma unroll
+    for (int k = 11; k >= 2; --k) pp = fmaf(pp, -x, 1.0f / (k * (k - 1.0f)));
+    l1 = x * lp;
+    phi = x * x * pp;
+  } else {
+    l1 = log1pf(x);
+    phi = fmaf(1.0f + x, l1, -x);
+  }
+}
+
+// FP32 sum over the populations flagged in `mask` (|y| > kYSmall):
+// G_L(alpha) = sum f psi(y, alpha), G_L'(alpha) = sum f y [ln(1 + alpha y) - ln(1 + y)].
+__device__ __noinline__ void large_terms(const float (&d)[Q], const float (&y)[Q], unsigned mask, float alpha,
+                                         float& GL, float& GLp) {
+  GL = 0.f;
+  GLp = 0.f;
 #pragma unroll
   for (int i = 0; i < Q; ++i) {
-    const double f = (double)((float)w27(i) + d[i]), y = (double)D[i] / f;
-    if (fabs(y) > (double)kYSmall) {
-      const double l1 = log1p(y);
-      GL += f * (phi64(alpha * y) - alpha * y * l1);
-      GLp += f * y * (log1p(alpha * y) - l1);
+    if (mask & (1u << i)) {
+      const float f = (float)w27(i) + d[i];
+      float ph, la, p1, l1;
+      phi_log1p32(alpha * y[i], ph, la);
+      phi_log1p32(y[i], p1, l1);
+      const float fy = f * y[i];
+      GL += f * ph - alpha * fy * l1;
+      GLp += fy * (la - l1);
     }
   }
 }
 
 template <int K>
-__device__ AlphaOut alpha_series32(const float (&d)[Q], const float (&D)[Q], const float (&y)[Q], bool any_large,
+__device__ AlphaOut alpha_series32(const float (&d)[Q], const float (&D)[Q], const float (&y)[Q], unsigned large,
                                    float amax, int max_it) {
+  const bool any_large = large != 0u;
   float S[K + 1];
 #pragma unroll
   for (int k = 0; k <= K; ++k) S[k] = 0.f;
 #pragma unroll
   for (int i = 0; i < Q; ++i) {
-    const bool small = fabsf(y[i]) <= kYSmall;
+    const bool small = !(large & (1u << i));
     const float yi = small ? y[i] : 0.f;
     float p = small ? D[i] * y[i] : 0.f;  // f y^2
     S[2] += p;
@@ -324,11 +348,10 @@ __device__ AlphaOut alpha_series32(const float (&d)[Q], const float (&D)[Q], con
       g = fmaf(fmaf((float)a_n(n), P, (float)c0_n(n)), S[n], g);
     }
     if (any_large) {
-      double GL, GLp;
-      large_terms(d, D, 2.0 + (double)delta, GL, GLp);
-      const double al = 2.0 + (double)delta;
-      g += (float)(GL / al);
-      gp += (float)(GLp / al - GL / (al * al));
+      float GL, GLp;
+      large_terms(d, y, large, alpha, GL, GLp);
+      g += GL / alpha;
+      gp += GLp / alpha - GL / (alpha * alpha);
     }
     r.iters = it + 1;
     if (!(gp > 0.f)) break;
@@ -399,20 +422,20 @@ __global__ void __launch_bounds__(128) d3q27_fp32_kernel(const Step27Args a) {
   if (a.alpha_mode != 0) {
     float y[Q];
     float ysmall = 0.f, amax = INFINITY;
-    bool any_large = false;
+    unsigned large = 0u;
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
       y[i] = D[i] / ((float)w27(i) + d[i]);
       const float ay = fabsf(y[i]);
       if (ay <= kYSmall) ysmall = fmaxf(ysmall, ay);
-      else any_large = true;
+      else large |= 1u << i;
       if (y[i] < 0.f) amax = fminf(amax, -1.0f / y[i]);
     }
     // warp-uniform series order from the warp's largest small |y|
     const float wmax = __int_as_float(__reduce_max_sync(__activemask(), __float_as_int(ysmall)));
-    if (wmax <= 0.02f) al = alpha_series32<6>(d, D, y, any_large, amax, a.max_newton);
-    else if (wmax <= 0.04f) al = alpha_series32<8>(d, D, y, any_large, amax, a.max_newton);
-    else al = alpha_series32<12>(d, D, y, any_large, amax, a.max_newton);
+    if (wmax <= 0.02f) al = alpha_series32<6>(d, D, y, large, amax, a.max_newton);
+    else if (wmax <= 0.04f) al = alpha_series32<8>(d, D, y, large, amax, a.max_newton);
+    else al = alpha_series32<12>(d, D, y, large, amax, a.max_newton);
     if (CHECK) {
       // |H(f + alpha Delta) - H(f)| in FP64 (conservation-consistent form) from the FP32 populations
       const double al64 = 2.0 + (double)al.delta;

@@ -1,0 +1,433 @@
+// Fused D3Q39 compressible ELBM level step (two populations f, g; 13 Lagrange
+// multipliers per node), FP64, one thread per node.
+//
+// Replaces, for the reference's D3Q39 lattice, the per-level chain
+//   streaming (looping/timestepping/streaming.f95:266-369, interior links)
+//   calculate_flow_variables (calculate_flow_variables.f95:192-311)
+//   collision (collision.f95:153-300)
+// of looping/timestepping/loop.f95:104-139, with the same arithmetic:
+//   moments, then the Newton solve of calculate_lagrangian_mults.f95:696-1097
+//   with the Doolittle LU of lu_decomp.f95 (its two index quirks kept),
+//   the closed-form alpha of calculate_alpha.f95:118-289, and the collision
+//   with the heat-flux corrections of find_q_bar.f95 / find_little_q_bar.f95,
+//   Sutherland viscosity and conductivity of quick_calcs.f95 and the
+//   relaxation factors of amr_processes.f95:1751-1814.
+// Streaming is pull-form over periodic images; the negative-population repair
+// of damp_it.f95 runs as a second kernel.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+
+#include "kernels39.cuh"
+
+namespace elbm {
+
+__constant__ Lattice39 c39;
+
+void upload_lattice39(const Lattice39& L, cudaStream_t s) {
+  cudaMemcpyToSymbolAsync(c39, &L, sizeof(L), 0, cudaMemcpyHostToDevice, s);
+}
+
+namespace {
+
+constexpr int Q = 39;
+constexpr int NL = 13;
+
+__device__ __forceinline__ double fieq39(double rho, const double (&lm)[NL], int i) {
+  // amr_processes.f95:1729-1747, left-to-right sum of integer-weighted multipliers
+  return rho * exp(lm[0] + c39.cx[i] * lm[1] + c39.cy[i] * lm[2] + c39.cz[i] * lm[3] + c39.phi[4][i] * lm[4] +
+                   c39.phi[5][i] * lm[5] + c39.phi[6][i] * lm[6] + c39.phi[7][i] * lm[7] + c39.phi[8][i] * lm[8] +
+                   c39.phi[9][i] * lm[9] + c39.phi[10][i] * lm[10] + c39.phi[11][i] * lm[11] +
+                   c39.phi[12][i] * lm[12]);
+}
+
+// lu_decomp.f95: LU of J (row-major 13x13, overwritten), substitution,
+// lm -= delta; returns max |delta|.
+__device__ double lu_update39(double* J, const double (&target)[NL], double (&lm)[NL]) {
+  double lo[NL][NL];
+  double up[NL][NL];
+  for (int c = 0; c < NL; ++c) up[0][c] = J[c];
+  for (int r = 1; r < NL; ++r) {
+    for (int c = 0; c < r; ++c) {
+      double v = J[r * NL + c];
+      for (int k = 0; k < c; ++k) {
+        // lu_decomp.f95:105: lower(5,4) subtracts lower(5,2)*upper(3,4)
+        const double l = (r == 4 && c == 3 && k == 2) ? lo[4][1] : lo[r][k];
+        v -= l * up[k][c];
+      }
+      lo[r][c] = (c == 0) ? J[r * NL] / up[0][0] : v / up[c][c];
+    }
+    for (int c = r; c < NL; ++c) {
+      double v = J[r * NL + c];
+      for (int k = 0; k < r; ++k) v -= lo[r][k] * up[k][c];
+      up[r][c] = v;
+    }
+  }
+  double z[NL];
+  for (int r = 0; r < NL; ++r) {
+    double v = J[r] - target[r];
+    for (int k = 0; k < r; ++k) {
+      // lu_decomp.f95:441: z9 uses lower(9,7)*z8
+      const double zz = (r == 8 && k == 6) ? z[7] : z[k];
+      v -= lo[r][k] * zz;
+    }
+    z[r] = v;
+  }
+  double dl[NL];
+  for (int r = NL - 1; r >= 0; --r) {
+    double v = z[r];
+    for (int c = NL - 1; c > r; --c) v -= up[r][c] * dl[c];
+    dl[r] = v / up[r][r];
+  }
+  double md = fabs(dl[0]);
+  for (int r = 1; r < NL; ++r) md = fabs(dl[r]) > md ? fabs(dl[r]) : md;
+  for (int r = 0; r < NL; ++r) lm[r] -= dl[r];
+  return md;
+}
+
+// calculate_lagrangian_mults.f95:696-1097; returns iterations (negative at the cap).
+__device__ int lagrange39(int max_it, double rho, double u, double v, double w, double temp, const double (&P)[6],
+                          double (&lm)[NL], double (&fieq)[Q]) {
+  const double vel_mag = u * u + v * v + w * w;
+  const double qx = (rho * vel_mag + 5 * rho * temp) * u;
+  const double qy = (rho * vel_mag + 5 * rho * temp) * v;
+  const double qz = (rho * vel_mag + 5 * rho * temp) * w;
+  const double target[NL] = {rho, rho * u, rho * v, rho * w, P[0], P[1], P[2], P[3], P[4], P[5], qx, qy, qz};
+  double max_diff = 1.0;
+  int it = 0;
+  double J[NL * NL];
+  while (max_diff > 1.0e-7) {
+    if (it >= max_it) return -it;
+    ++it;
+    for (int i = 0; i < Q; ++i) fieq[i] = fieq39(rho, lm, i);
+    for (int r = 0; r < NL; ++r)
+      for (int c = r; c < NL; ++c) {
+        double s = 0.0;
+        for (int i = 0; i < Q; ++i) s += (double)(c39.phi[r][i] * c39.phi[c][i]) * fieq[i];
+        J[r * NL + c] = s;
+        J[c * NL + r] = s;
+      }
+    max_diff = lu_update39(J, target, lm);
+  }
+  return it;
+}
+
+__device__ void sutherland39(const D3Q39Dev& k, double T, double& mu, double& dim_mu, double& dim_temp) {
+  // quick_calcs.f95:24-64 (default-real literals rounded through float)
+  const double const_s = (double)110.15f, temp_ref = (double)273.15f, visc_ref = 1.716e-5;
+  const double unit_temp = T * k.t_ref * k.gama;
+  const double unit_mu = visc_ref * pow(unit_temp / temp_ref, 1.5) * ((temp_ref + const_s) / (unit_temp + const_s));
+  mu = unit_mu / k.mu_ref;
+  dim_mu = unit_mu;
+  dim_temp = unit_temp;
+}
+
+__device__ bool therm_cond39(const D3Q39Dev& k, double rho, double T, double& kappa) {
+  // quick_calcs.f95:70-215, kappa_bottom = kappa_ref
+  const double unit_temp = T * k.t_ref * k.gama;
+  if (unit_temp <= 500.0) {
+    kappa = 418.1 * (5.9776e-6 * pow(unit_temp, 1.5) / (unit_temp + (double)194.4f)) / k.kappa_ref;
+    return true;
+  }
+  const double A[2][3][5] = {{{0.334316, 3.28202, 11.9939, 20.0944, 4.62882},
+                              {0.413573, 3.83393, 13.1885, 20.7305, 4.27728},
+                              {0.208749, 1.92122, 6.58813, 10.7630, -1.27699}},
+                             {{10.9992, 387.106, 387.282, 5.48304, -1.20106},
+                              {82.1184, 308.927, 423.174, 250.668, 47.5889},
+                              {38.8677, 123.284, 144.224, 72.8083, 0.684807}}};
+  double unit_p = unit_temp * (rho * k.rho_ref) * k.gas_const_R;
+  int band;
+  if (unit_temp <= 2250.0) {
+    unit_p = (rho * k.rho_ref) * k.gas_const_R * unit_temp / 101300.0;
+    band = 0;
+  } else if (unit_temp <= 4250.0) {
+    band = 1;
+  } else {
+    return false;
+  }
+  int row;
+  if (unit_p < 10.0 && unit_p > 0.1) row = 0;
+  else if (unit_p > 10.0 && unit_p < 100.0) row = 1;
+  else if (unit_p > 100.0 && unit_p < 1000.0) row = 2;
+  else return false;
+  const double* c = A[band][row];
+  const double kek = log(unit_temp / 10000.0);
+  kappa = exp(c[0] * pow(kek, 4.0) + c[1] * pow(kek, 3.0) + c[2] * kek * kek + c[3] * kek + c[4]) / k.kappa_ref;
+  return true;
+}
+
+__device__ __forceinline__ double eps39(const D3Q39Dev& k, int step) {
+  // amr_processes.f95:1789-1814
+  if (step < k.startup_timesteps) return ((double)step + 1.0) / (double)k.startup_timesteps * k.elbm_epsilon;
+  return k.elbm_epsilon;
+}
+
+// calculate_alpha.f95:118-289
+__device__ double alpha39(const D3Q39Dev& k, const double (&fi)[Q], const double (&fd)[Q], double temp, int step) {
+  const double alpha_hi = 2.125, alpha_start = 1.0e-6, plus_epsilon = 1.24e-16, very_small = 1.0e-14;
+  const double pi = 3.1415926535, k_boltz = 1.38064852e-23;
+  double mu, dim_mu, dim_temp;
+  sutherland39(k, temp, mu, dim_mu, dim_temp);
+  const double mfp = dim_mu / k.p_ref * sqrt(pi * k_boltz * dim_temp / (2 * k.molec_weight));
+  const double mft = mfp / sqrt(3 * k_boltz * dim_temp / k.molec_weight);
+  const double bm = k.dt / (2 * mft + k.dt);
+  double c1 = 0, c2 = 0, c3 = 0;
+  for (int i = 0; i < Q; ++i) {
+    const double df = fi[i] < 0.0 ? fabs(fi[i]) : fi[i];
+    const double x = fd[i] / df;
+    c1 = c1 + df * (2.0 * (x * x) / (2 + x));
+    c2 = c2 + df * (x * x);
+    if (x <= 0.0 && x >= -1.0) c3 = c3 + df * (x * x * x);
+  }
+  if (fabs(c3) < plus_epsilon) return 2.0;
+  double asm_ = (c2 - sqrt(c2 * c2 - 8.0 * c3 * c1)) / (2.0 * c3);
+  if (asm_ > alpha_hi) asm_ = alpha_hi - 1.0e-9;
+  if (step < k.startup_timesteps) asm_ = (asm_ - alpha_start) / (double)k.startup_timesteps * step;
+  double t1 = 0, t2 = 0, t3 = 0, t4 = 0, s1 = 0, s2 = 0, third = 0;
+  for (int i = 0; i < Q; ++i) {
+    const double df = fi[i] < 0.0 ? fabs(fi[i]) : fi[i];
+    const double x1 = fd[i] / df, x2 = x1 * x1, x3 = x1 * x1 * x1;
+    const double f2 = x2 * df, f3 = x3 * df, f4 = x2 * x2 * df, f5 = x2 * x3 * df, f6 = x3 * x3 * df;
+    if (x1 <= 0.0 && x1 >= -1.0) {
+      t1 = t1 + f3;
+      t2 = t2 + f4;
+      t3 = t3 + f5;
+      t4 = t4 + f6;
+    }
+    s1 = s1 + f2;
+    if (x1 >= 0.0) s2 = s2 + f3 * (2.0 / (4 + asm_ * x1) + 1.0 / (4 + 2 * asm_ * x1) + 2.0 / (4 + 3 * asm_ * x1));
+    third = third - (60 * f2 + 60 * f3 + 11 * f4) / (60 + 90 * x1 + 36 * x2 + 3 * x3);
+  }
+  const double first = -(bm * bm) * (t1 / 6 - alpha_hi * bm * t2 / 12 + alpha_hi * alpha_hi * (bm * bm) * t3 / 20 -
+                                     alpha_hi * alpha_hi * alpha_hi * (bm * bm * bm) * t4 / 5);
+  const double second = s1 / 2 - 2 * asm_ * (bm * bm) * s2 / 15;
+  if (fabs(first) < very_small) return 2.0;
+  const double na = (-second + sqrt(second * second - 4 * first * third)) / (2 * first);
+  if (na < asm_) return asm_;
+  if (na > alpha_hi) return alpha_hi;
+  return na;
+}
+
+__global__ void __launch_bounds__(64) d3q39_fp64_kernel(const Step39Args a) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= a.N) return;
+  const D3Q39Dev& k = a.k;
+  const int x = (int)(n % a.nx), y = (int)((n / a.nx) % a.ny), z = (int)(n / ((int64_t)a.nx * a.ny));
+  double f[Q], g[Q];
+  // pull streaming over periodic images: f_j(x) = fout_j(x - c_j)
+  for (int j = 0; j < Q; ++j) {
+    int sx = x - c39.cx[j], sy = y - c39.cy[j], sz = z - c39.cz[j];
+    sx = (sx % a.nx + a.nx) % a.nx;
+    sy = (sy % a.ny + a.ny) % a.ny;
+    sz = (sz % a.nz + a.nz) % a.nz;
+    const int64_t s = ((int64_t)sz * a.ny + sy) * a.nx + sx;
+    f[j] = a.fsrc[(int64_t)j * a.plane + s];
+    g[j] = a.gsrc[(int64_t)j * a.plane + s];
+  }
+  double lm[NL];
+  for (int r = 0; r < NL; ++r) lm[r] = a.lm[(int64_t)r * a.plane + n];
+  // calculate_flow_variables.f95:201-228
+  double rs = 0, us = 0, vs = 0, ws = 0, es = 0;
+  for (int i = 0; i < Q; ++i) {
+    rs = rs + f[i];
+    us = us + c39.cx[i] * f[i];
+    vs = vs + c39.cy[i] * f[i];
+    es = es + c39.cmag[i] * f[i] + g[i];
+  }
+  const double rho = rs, u = us / rs, v = vs / rs;
+  for (int i = 0; i < Q; ++i) ws = ws + c39.cz[i] * f[i];
+  const double w = ws / rs;
+  const double w_old = a.w_vel[n];
+  const double vmag = u * u + v * v + w * w;
+  const double temp = (es - rho * vmag) / (2 * k.const_vol * rho);
+  const double P[6] = {rho * (temp + u * u), rho * (temp + v * v), rho * (temp + w_old * w_old),
+                       rho * u * v,          rho * u * w,          rho * v * w};
+  double fe[Q];
+  int it = lagrange39(k.max_lm_iters, rho, u, v, w, temp, P, lm, fe);
+  unsigned flags = 0;
+  if (it < 0) {
+    flags |= 0x2u;
+    it = -it;
+    for (int i = 0; i < Q; ++i) fe[i] = fieq39(rho, lm, i);
+  }
+  double fd[Q];
+  for (int i = 0; i < Q; ++i) fd[i] = fe[i] - f[i];
+  const double alpha = k.turbulent ? alpha39(k, f, fd, temp, a.step) : 2.0;
+  // collision.f95:153-300 with the final multipliers
+  const double lead = 2.0 * k.const_vol - 3;
+  double gd[Q];
+  for (int i = 0; i < Q; ++i) {
+    fe[i] = fieq39(rho, lm, i);
+    fd[i] = fe[i] - f[i];
+    gd[i] = lead * temp * fe[i] - g[i];
+  }
+  const double eps = eps39(k, a.step);
+  // find_q_bar.f95:33-220: ten central third moments of Delta f
+  double m[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // xxx yyy zzz xxy xxz xyy xyz xzz yyz yzz
+  for (int i = 0; i < Q; ++i) {
+    const double X = c39.cx[i] - u, Y = c39.cy[i] - v, Z = c39.cz[i] - w;
+    m[0] = m[0] + X * X * X * fd[i];
+    m[1] = m[1] + Y * Y * Y * fd[i];
+    m[2] = m[2] + Z * Z * Z * fd[i];
+    m[3] = m[3] + (X * X) * Y * fd[i];
+    m[4] = m[4] + (X * X) * Z * fd[i];
+    m[5] = m[5] + (Y * Y) * X * fd[i];
+    m[7] = m[7] + (Z * Z) * X * fd[i];
+    m[8] = m[8] + (Y * Y) * Z * fd[i];
+    m[9] = m[9] + (Z * Z) * Y * fd[i];
+    m[6] = m[6] + X * Y * Z * fd[i];
+  }
+  // qabc(27) of find_q_bar.f95 as indices into m
+  const int qmap[27] = {0, 3, 4, 3, 5, 6, 4, 6, 7, 3, 5, 6, 5, 1, 8, 6, 8, 9, 4, 6, 7, 6, 8, 9, 7, 9, 2};
+  const double temp_coeff = 6.0 * (temp * temp * temp);
+  // find_little_q_bar.f95:23-52
+  double q1 = 0, q2 = 0, q3 = 0;
+  for (int i = 0; i < Q; ++i) {
+    q1 = q1 + (c39.cx[i] - u) * gd[i];
+    q2 = q2 + (c39.cy[i] - v) * gd[i];
+    q3 = q3 + (c39.cz[i] - w) * gd[i];
+  }
+  const double q_lead = eps / temp;
+  double mu, dm, dt_;
+  sutherland39(k, temp, mu, dm, dt_);
+  double kappa = 0.0;
+  if (!therm_cond39(k, rho, temp, kappa)) flags |= 0x10u;
+  double b1, b2;
+  if (a.step < k.startup_timesteps) {
+    b1 = k.init_beta_1 + k.beta_1_scaling * a.step;
+    b2 = k.init_beta_2 + k.beta_2_scaling * a.step;
+  } else {
+    b1 = 1.0 / ((pow(2.0, (double)(k.lvl + 1)) * mu) / (rho * temp) + 1.0);
+    b2 = 1.0 / ((2.0 * kappa) / (rho * k.const_press * temp) + 1.0);
+  }
+  bool neg = false;
+  for (int i = 0; i < Q; ++i) {
+    double sy = 0.0, sk = 0.0;
+    for (int mm = 0; mm < 27; ++mm) sy = sy + m[qmap[mm]] * (double)c39.yi[mm][i];
+    for (int mm = 0; mm < 27; ++mm) sk = sk + m[qmap[mm]] * (double)c39.kroen[mm][i];
+    const double qb = eps * (sy - 3 * temp * sk) / temp_coeff;
+    const double ch = q_lead * (c39.cx[i] * q1 + c39.cy[i] * q2 + c39.cz[i] * q3);
+    const double fo = f[i] + alpha * b1 * (fd[i] - qb) + b2 * qb;
+    const double go = g[i] + alpha * b1 * (gd[i] - ch) + b2 * ch;
+    a.fdst[(int64_t)i * a.plane + n] = fo;
+    a.gdst[(int64_t)i * a.plane + n] = go;
+    neg |= fo < 0.0;
+  }
+  for (int r = 0; r < NL; ++r) a.lm[(int64_t)r * a.plane + n] = lm[r];
+  a.w_vel[n] = w;
+  if (a.alpha) a.alpha[n] = alpha;
+  if (a.macro) {
+    a.macro[n] = rho;
+    a.macro[a.plane + n] = u;
+    a.macro[2 * a.plane + n] = v;
+    a.macro[3 * a.plane + n] = w;
+    a.macro[4 * a.plane + n] = temp;
+  }
+  if (!isfinite(rho) || !isfinite(temp)) flags |= 0x1u;
+  if (neg) flags |= 0x4u;
+  // per-warp aggregation of the counters
+  const unsigned mask = __activemask();
+  const unsigned sit = __reduce_add_sync(mask, (unsigned)it);
+  const unsigned fl = __reduce_or_sync(mask, flags);
+  const unsigned nn = __popc(mask);
+  const unsigned capped = __popc(__ballot_sync(mask, (flags & 0x2u) != 0));
+  if ((int)(threadIdx.x & 31) == __ffs(mask) - 1) {
+    atomicAdd(&a.stats->node_updates, (unsigned long long)nn);
+    atomicAdd(&a.stats->newton_iters, (unsigned long long)sit);
+    if (capped) atomicAdd(&a.stats->fallbacks, (unsigned long long)capped);
+    if (fl) atomicOr(&a.stats->status, fl);
+  }
+}
+
+// damp_it.f95:64-177 for fout on a periodic box: a negative population takes
+// the mean of its +-c_i neighbours when both are positive, else the mean of
+// the positive one and its own magnitude, else its magnitude.  Neighbours are
+// read from the undamped field (identical to the reference's in-place sweep
+// unless two negative populations of one direction are adjacent along c_i).
+__global__ void d3q39_damp_kernel(const double* __restrict__ src, double* __restrict__ dst, int nx, int ny, int nz,
+                                  int64_t plane, DevStats* stats) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  const int64_t N = (int64_t)nx * ny * nz;
+  if (n >= N) return;
+  const double v = src[(int64_t)i * plane + n];
+  double out = v;
+  if (v < 0.0) {
+    const int x = (int)(n % nx), y = (int)((n / nx) % ny), z = (int)(n / ((int64_t)nx * ny));
+    auto at = [&](int s) {
+      const int xx = ((x + s * c39.cx[i]) % nx + nx) % nx, yy = ((y + s * c39.cy[i]) % ny + ny) % ny,
+                zz = ((z + s * c39.cz[i]) % nz + nz) % nz;
+      return src[(int64_t)i * plane + ((int64_t)zz * ny + yy) * nx + xx];
+    };
+    const double fp = at(1), fm = at(-1);
+    if (fp > 0.0 && fm > 0.0) out = (fp + fm) / 2.0;
+    else if (fp > 0.0 && fm < 0.0) out = (fp + fabs(v)) / 2;
+    else if (fp < 0.0 && fm > 0.0) out = (fm + fabs(v)) / 2;
+    else out = fabs(v);
+    atomicAdd(&stats->exact_nodes, 1ull);
+  }
+  dst[(int64_t)i * plane + n] = out;
+}
+
+}  // namespace
+
+void launch_d3q39_fp64(const Step39Args& a, cudaStream_t s) {
+  const int threads = 64;
+  const int64_t blocks = (a.N + threads - 1) / threads;
+  d3q39_fp64_kernel<<<(unsigned)blocks, threads, 0, s>>>(a);
+}
+
+void launch_d3q39_damp(const double* src, double* dst, int nx, int ny, int nz, int64_t plane, DevStats* stats,
+                       cudaStream_t s) {
+  const int64_t N = (int64_t)nx * ny * nz;
+  dim3 grid((unsigned)((N + 255) / 256), 39);
+  d3q39_damp_kernel<<<grid, 256, 0, s>>>(src, dst, nx, ny, nz, plane, stats);
+}
+
+}  // namespace elbm
+
+namespace elbm {
+
+// Host-side tables (directions_and_weights.f95:463-780).
+void build_lattice39(int shifted, int primary_flow_dir, Lattice39& L) {
+  static const int CX0[39] = {0, 1, 0, 0, -1, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1, 2, 0, 0, -2, 0,
+                              0, 2, 2, 0, -2, -2, 2, 2, -2, -2, 0, 0, 0, 3, 0, 0, -3, 0, 0};
+  static const int CY0[39] = {0, 0, 1, 0, 0, -1, 0, 1, 1, -1, -1, 1, 1, -1, -1, 0, 2, 0, 0, -2,
+                              0, 2, 0, 2, 2, -2, -2, 0, 0, 0, 2, -2, -2, 0, 3, 0, 0, -3, 0};
+  static const int CZ0[39] = {0, 0, 0, 1, 0, 0, -1, 1, 1, 1, 1, -1, -1, -1, -1, 0, 0, 2, 0, 0,
+                              -2, 0, 2, 2, 0, 0, 0, -2, -2, 2, -2, -2, 2, 0, 0, 3, 0, 0, -3};
+  static const int OPP0[39] = {1, 5, 6, 7, 2, 3, 4, 14, 15, 12, 13, 10, 11, 8, 9, 19, 20, 21, 16, 17,
+                               18, 26, 29, 32, 27, 22, 25, 30, 23, 28, 33, 24, 31, 37, 38, 39, 34, 35, 36};
+  for (int i = 0; i < 39; ++i) {
+    int x = CX0[i], y = CY0[i], z = CZ0[i];
+    if (shifted) {
+      if (primary_flow_dir == 1) x += 1;
+      else if (primary_flow_dir == 2) y += 1;
+      else if (primary_flow_dir == 3) z += 1;
+      else if (primary_flow_dir == 4) x -= 1;
+      else if (primary_flow_dir == 5) y -= 1;
+      else if (primary_flow_dir == 6) z -= 1;
+    }
+    L.cx[i] = x;
+    L.cy[i] = y;
+    L.cz[i] = z;
+    L.opp[i] = shifted ? i : OPP0[i] - 1;
+    L.cmag[i] = (double)x * x + (double)y * y + (double)z * z;
+    const int c2 = x * x + y * y + z * z;
+    const int mono[13] = {1, x, y, z, x * x, y * y, z * z, x * y, x * z, y * z, x * c2, y * c2, z * c2};
+    for (int r = 0; r < 13; ++r) L.phi[r][i] = mono[r];
+    const int cxxx = x * x * x, cyyy = y * y * y, czzz = z * z * z, cxyz = x * y * z;
+    const int cxxy = x * x * y, cxyy = x * y * y, cxxz = x * x * z, cxzz = x * z * z, cyyz = y * y * z,
+              cyzz = z * z * y;
+    const int yi[27] = {cxxx, cxxy, cxxz, cxxy, cxyy, cxyz, cxxz, cxyz, cxzz, cxxy, cxyy, cxyz, cxyy, cyyy,
+                        cyyz, cxyz, cyyz, cyzz, cxxz, cxyz, cxzz, cxyz, cyyz, cyzz, cxzz, cyzz, czzz};
+    const int kr[27] = {x, y, z, 0, 0, 0, 0, 0, 0, 0, 0, 0, x, y, z, 0, 0, 0, 0, 0, 0, 0, 0, 0, x, y, z};
+    for (int m = 0; m < 27; ++m) {
+      L.yi[m][i] = yi[m];
+      L.kroen[m][i] = kr[m];
+    }
+  }
+}
+
+}  // namespace elbm

@@ -14,6 +14,7 @@ struct DevStats {
   unsigned long long exact_nodes;
   unsigned long long fallbacks;
   unsigned long long max_dH_bits;  // bit pattern of a non-negative double (monotone in value)
+  unsigned long long dh_over;      // check mode: nodes with |dH| above the tolerance
   unsigned int status;
   unsigned int pad;
 };
