@@ -54,6 +54,6 @@ def test_d3q39_periodic_parity(pkg, o39, built_lib, start_step, steps):
         rel = np.max(np.abs(out[name] - ref) / np.abs(ref))
         assert rel <= 1e-12, (name, rel)
     assert np.max(np.abs(out["lm"] - lev.lm)) <= 1e-12 * np.max(np.abs(lev.lm))
-    assert np.max(np.abs(out["alpha"] - lev.alpha)) <= 1e-12
+    assert np.max(np.abs(out["alpha"] - lev.alpha)) <= 1e-11  # closed-form alpha: sqrt and divisions
     assert st["node_updates"] == steps * nx * ny * nz
     ctx.close()

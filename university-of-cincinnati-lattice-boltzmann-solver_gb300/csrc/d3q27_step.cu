@@ -276,47 +276,44 @@ struct AlphaOut {
   bool fallback;
 };
 
-// phi(x) = (1+x) ln(1+x) - x and ln(1+x) in FP32: 12-term series for |x| < 1/8,
-// the direct form (log1pf) beyond, where the cancellation costs at most ~8x.
-__device__ __forceinline__ void phi_log1p32(float x, float& phi, float& l1) {
-  if (fabsf(x) < 0.125f) {
-    float lp = 1.0f / 12.0f, pp = 1.0f / 132.0f;
+// ln(1+x) and phi(x) = (1+x) ln(1+x) - x in FP32 without cancellation, from
+// ln(1+x) = 2 atanh(s), s = x/(2+x):
+//   ln(1+x) = 2 s (1 + s^2/3 + s^4/5 + ...),
+//   phi(x)  = x^2/(2+x) + 2 (1+x) s^3 (1/3 + s^2/5 + s^4/7 + ...),
+// (the leading terms 2s(1+x) - x = x^2/(2+x) cancel exactly).  Eight terms
+// reach FP32 rounding for |s| <= 1/3, i.e. -1/2 <= x <= 1.
+__device__ __forceinline__ void log1p_phi32(float x, float& l1, float& phi) {
+  const float s = __fdividef(x, 2.0f + x), s2 = s * s;
+  float a = 1.0f / 17.0f, b = 1.0f / 19.0f;
 #pragma unroll
-    for (int m = 11; m >= 1; --m) lp = fmaf(lp, -x, 1.0f / m);
-#pragma unroll
-    for (int k = 11; k >= 2; --k) pp = fmaf(pp, -x, 1.0f / (k * (k - 1.0f)));
-    l1 = x * lp;
-    phi = x * x * pp;
-  } else {
-    l1 = log1pf(x);
-    phi = fmaf(1.0f + x, l1, -x);
+  for (int k = 7; k >= 0; --k) {
+    a = fmaf(a, s2, 1.0f / (2 * k + 1));  // 1 + s^2/3 + ... (k = 0 term is 1)
+    b = fmaf(b, s2, 1.0f / (2 * k + 3));  // 1/3 + s^2/5 + ...
   }
+  l1 = 2.0f * s * a;
+  phi = fmaf(2.0f * (1.0f + x) * s2 * s, b, __fdividef(x * x, 2.0f + x));
 }
 
-// FP32 sum over the populations flagged in `mask` (|y| > kYSmall):
-// G_L(alpha) = sum f psi(y, alpha), G_L'(alpha) = sum f y [ln(1 + alpha y) - ln(1 + y)].
-__device__ __noinline__ void large_terms(const float (&d)[Q], const float (&y)[Q], unsigned mask, float alpha,
-                                         float& GL, float& GLp) {
+// FP32 sum over the flagged populations (|y| > kYSmall), visiting only set
+// bits: G_L(alpha) = sum f psi(y, alpha), G_L'(alpha) = sum f y [ln(1 + alpha y) - ln(1 + y)].
+struct LargePop {
+  float f, y, l1;
+};
+__device__ __forceinline__ void large_terms(const LargePop* lp, int nl, float alpha, float& GL, float& GLp) {
   GL = 0.f;
   GLp = 0.f;
-#pragma unroll
-  for (int i = 0; i < Q; ++i) {
-    if (mask & (1u << i)) {
-      const float f = (float)w27(i) + d[i];
-      float ph, la, p1, l1;
-      phi_log1p32(alpha * y[i], ph, la);
-      phi_log1p32(y[i], p1, l1);
-      const float fy = f * y[i];
-      GL += f * ph - alpha * fy * l1;
-      GLp += fy * (la - l1);
-    }
+  for (int k = 0; k < nl; ++k) {
+    float la, ph;
+    log1p_phi32(alpha * lp[k].y, la, ph);
+    const float fy = lp[k].f * lp[k].y;
+    GL += fmaf(lp[k].f, ph, -alpha * fy * lp[k].l1);
+    GLp = fmaf(fy, la - lp[k].l1, GLp);
   }
 }
 
 template <int K>
 __device__ AlphaOut alpha_series32(const float (&d)[Q], const float (&D)[Q], const float (&y)[Q], unsigned large,
                                    float amax, int max_it) {
-  const bool any_large = large != 0u;
   float S[K + 1];
 #pragma unroll
   for (int k = 0; k <= K; ++k) S[k] = 0.f;
@@ -332,9 +329,30 @@ __device__ AlphaOut alpha_series32(const float (&d)[Q], const float (&D)[Q], con
       S[k] += p;
     }
   }
-  AlphaOut r{0.f, 0u, any_large, false};
-  if (!any_large && !(S[2] > 1e-30f)) return r;  // at equilibrium: alpha = 2
-  float delta = 0.f;
+  AlphaOut r{0.f, 0u, large != 0u, false};
+  // compact list of the large populations (rare): f, y and ln(1+y), computed once
+  LargePop lp[8];
+  int nl = 0;
+  if (large) {
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+      if ((large & (1u << i)) && nl < 8) {
+        float l1, ph;
+        log1p_phi32(y[i], l1, ph);
+        lp[nl].f = (float)w27(i) + d[i];
+        lp[nl].y = y[i];
+        lp[nl].l1 = l1;
+        ++nl;
+      }
+    }
+    if (__popc(large) > 8) {  // too many strongly non-equilibrium populations: not handled here
+      r.fallback = true;
+      r.delta = (2.0f < amax) ? 0.f : 0.5f * (amax - 3.0f);
+      return r;
+    }
+  }
+  if (nl == 0 && !(S[2] > 1e-30f)) return r;  // at equilibrium: alpha = 2
+  float delta = 0.f, last = INFINITY;
   bool ok = false;
   for (int it = 0; it < max_it; ++it) {
     const float alpha = 2.0f + delta;
@@ -347,11 +365,12 @@ __device__ AlphaOut alpha_series32(const float (&d)[Q], const float (&D)[Q], con
       pw *= alpha;
       g = fmaf(fmaf((float)a_n(n), P, (float)c0_n(n)), S[n], g);
     }
-    if (any_large) {
+    if (nl) {
       float GL, GLp;
-      large_terms(d, y, large, alpha, GL, GLp);
-      g += GL / alpha;
-      gp += GLp / alpha - GL / (alpha * alpha);
+      large_terms(lp, nl, alpha, GL, GLp);
+      const float ia = 1.0f / alpha;
+      g = fmaf(GL, ia, g);
+      gp += (GLp - GL * ia) * ia;
     }
     r.iters = it + 1;
     if (!(gp > 0.f)) break;
@@ -359,10 +378,13 @@ __device__ AlphaOut alpha_series32(const float (&d)[Q], const float (&D)[Q], con
     const float next = delta - step;
     if (!(2.0f + next > 1.0f) || !(2.0f + next < amax)) break;
     delta = next;
-    if (fabsf(step) <= fmaxf(4e-8f, 2e-7f * fabsf(delta))) {
+    const float as = fabsf(step);
+    // converged, or the step stopped shrinking at the FP32 noise floor
+    if (as <= fmaxf(4e-8f, 2e-7f * fabsf(delta)) || (it >= 2 && as >= 0.5f * last && as <= 1e-5f)) {
       ok = true;
       break;
     }
+    last = as;
   }
   if (!ok) {
     r.fallback = true;
@@ -425,7 +447,7 @@ __global__ void __launch_bounds__(128) d3q27_fp32_kernel(const Step27Args a) {
     unsigned large = 0u;
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
-      y[i] = D[i] / ((float)w27(i) + d[i]);
+      y[i] = __fdividef(D[i], (float)w27(i) + d[i]);
       const float ay = fabsf(y[i]);
       if (ay <= kYSmall) ysmall = fmaxf(ysmall, ay);
       else large |= 1u << i;

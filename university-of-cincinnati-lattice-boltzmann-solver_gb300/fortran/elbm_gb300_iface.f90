@@ -1,0 +1,140 @@
+! ISO_C_BINDING interface to libelbm_gb300 (include/elbm_gb300.h).
+!
+! The reference's per-level driver (looping/timestepping/loop.f95:94-147) keeps
+! its calls streaming(level_step,fine,lvl), calculate_flow_variables(...),
+! collision(...) and damp_it(...).  With this module their bodies become one
+! call of elbm_level_step per level and sub-cycle, after the level's boxes
+! were registered (from_scratch, amr/modules/amr_processes.f95:383-476) and
+! their FABs uploaded.  No Fortran compiler is available where this library is
+! built, so this file is shipped as source; the same entry points are
+! exercised from Python (ctypes) by the library's tests.
+module elbm_gb300_iface
+  use iso_c_binding
+  implicit none
+  private
+
+  integer(c_int), parameter, public :: ELBM_OK = 0, ELBM_E_ARG = -1, ELBM_E_CUDA = -2, &
+    ELBM_E_UNSUPPORTED = -3, ELBM_E_STATE = -4
+  integer(c_int), parameter, public :: ELBM_D3Q27 = 27, ELBM_D3Q39 = 39
+  integer(c_int), parameter, public :: ELBM_STORE_FP64 = 0, ELBM_STORE_FP32_DEV = 1
+  integer(c_int), parameter, public :: ELBM_ALPHA_FIXED2 = 0, ELBM_ALPHA_NEWTON = 1, ELBM_ALPHA_LEARNED = 2
+
+  type, bind(c), public :: elbm_d3q27_params
+    real(c_double) :: nu, tol_alpha, tol_dH
+    integer(c_int32_t) :: max_newton, alpha_mode, check_dH, record_alpha
+    integer(c_int32_t) :: outlet_type(8)
+    real(c_double) :: fs_feq(27)
+    real(c_double) :: inl_feq(27, 8)   ! C layout inl_feq[8][27]
+    real(c_double) :: outl_feq(27, 8)
+  end type
+
+  type, bind(c), public :: elbm_d3q39_params
+    integer(c_int32_t) :: shifted, primary_flow_dir, turbulent, lvl, startup_timesteps, max_lm_iters
+    integer(c_int32_t) :: periodic, timestep, damp, pad
+    real(c_double) :: gama, t_ref, rho_ref, p_ref, mu_ref, kappa_ref, gas_const_R, const_vol, &
+      const_press, molec_weight
+    real(c_double) :: dt, elbm_epsilon, init_beta_1, init_beta_2, beta_1_scaling, beta_2_scaling
+  end type
+
+  type, bind(c), public :: elbm_stats
+    integer(c_int64_t) :: node_updates, newton_iters, exact_path_nodes, fallbacks
+    integer(c_int32_t) :: status, pad
+    real(c_double) :: max_abs_dH
+    integer(c_int64_t) :: dh_over_tol
+    real(c_double) :: kernel_ms
+  end type
+
+  public :: elbm_create, elbm_destroy, elbm_level_register, elbm_set_d3q27_params, elbm_set_links, &
+    elbm_upload_level, elbm_download_level, elbm_download_alpha, elbm_level_step, elbm_sync, &
+    elbm_set_d3q39_params, elbm_upload_level39, elbm_download_level39
+
+  interface
+    integer(c_int) function elbm_create(device, ctx) bind(c, name="elbm_create")
+      import :: c_int, c_ptr
+      integer(c_int), value :: device
+      type(c_ptr) :: ctx
+    end function
+    subroutine elbm_destroy(ctx) bind(c, name="elbm_destroy")
+      import :: c_ptr
+      type(c_ptr), value :: ctx
+    end subroutine
+    integer(c_int) function elbm_level_register(ctx, lvl, lattice, storage, nbox, lo_hi, ngrow) &
+        bind(c, name="elbm_level_register")
+      import :: c_int, c_ptr, c_int32_t
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl, lattice, storage, nbox, ngrow
+      integer(c_int32_t), intent(in) :: lo_hi(6, *)   ! mfi%validbox() lo/hi, 0-based
+    end function
+    integer(c_int) function elbm_set_d3q27_params(ctx, lvl, p) bind(c, name="elbm_set_d3q27_params")
+      import :: c_int, c_ptr, elbm_d3q27_params
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl
+      type(elbm_d3q27_params), intent(in) :: p
+    end function
+    integer(c_int) function elbm_set_links(ctx, lvl, box, state, ngrow_state) bind(c, name="elbm_set_links")
+      import :: c_int, c_ptr, c_int32_t
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl, box, ngrow_state
+      integer(c_int32_t), intent(in) :: state(*)      ! mfstate(lvl)%dataptr(mfi)
+    end function
+    integer(c_int) function elbm_upload_level(ctx, lvl, box, fout) bind(c, name="elbm_upload_level")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl, box
+      real(c_double), intent(in) :: fout(*)           ! mffout(lvl)%dataptr(mfi)
+    end function
+    integer(c_int) function elbm_download_level(ctx, lvl, box, fout) bind(c, name="elbm_download_level")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl, box
+      real(c_double), intent(out) :: fout(*)
+    end function
+    integer(c_int) function elbm_download_alpha(ctx, lvl, box, alpha) bind(c, name="elbm_download_alpha")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl, box
+      real(c_double), intent(out) :: alpha(*)
+    end function
+    integer(c_int) function elbm_level_step(ctx, lvl, nsteps, stats) bind(c, name="elbm_level_step")
+      import :: c_int, c_ptr, elbm_stats
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl, nsteps
+      type(elbm_stats), intent(out) :: stats
+    end function
+    integer(c_int) function elbm_sync(ctx) bind(c, name="elbm_sync")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+    end function
+    integer(c_int) function elbm_set_d3q39_params(ctx, lvl, p) bind(c, name="elbm_set_d3q39_params")
+      import :: c_int, c_ptr, elbm_d3q39_params
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl
+      type(elbm_d3q39_params), intent(in) :: p
+    end function
+    integer(c_int) function elbm_upload_level39(ctx, lvl, box, fout, gout, lm, w_vel) &
+        bind(c, name="elbm_upload_level39")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl, box
+      real(c_double), intent(in) :: fout(*), gout(*), lm(*), w_vel(*)
+    end function
+    integer(c_int) function elbm_download_level39(ctx, lvl, box, fout, gout, lm, w_vel, alpha, macro) &
+        bind(c, name="elbm_download_level39")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl, box
+      type(c_ptr), value :: fout, gout, lm, w_vel, alpha, macro  ! c_loc(...) or c_null_ptr
+    end function
+  end interface
+end module elbm_gb300_iface
+
+! Example body of the reference's per-level collide-stream call with the
+! library (one box per level; `ctx` created once with elbm_create):
+!
+!   subroutine collision(level_step, fine, lvl)
+!     use elbm_gb300_iface
+!     ...
+!     if (.not. level_step(lvl)) return
+!     rc = elbm_level_step(ctx, lvl, 1, stats)
+!     if (rc /= ELBM_OK .or. iand(stats%status, 1) /= 0) call error_out
+!   end subroutine
