@@ -146,6 +146,20 @@ int elbm_set_links(elbm_ctx* ctx, int lvl, int box, const int32_t* state, int ng
 int elbm_upload_level(elbm_ctx* ctx, int lvl, int box, const double* fout);
 int elbm_download_level(elbm_ctx* ctx, int lvl, int box, double* fout);
 
+/* Allocation-free variant of elbm_upload_level for D3Q27 levels with FP32
+ * deviation storage.  No counterpart in the reference: it exists for callers
+ * that cannot let the library allocate device memory once the level is set
+ * up, such as an AMReX driver whose arena has already reserved the GPU's
+ * memory, or a time loop that must not stall on cudaMalloc's device-wide
+ * synchronisation.  The FP64 FAB is staged through a fixed 32 MiB buffer built
+ * into the library (held by every GPU that loads it, until exit) instead of a
+ * cudaMalloc'ed one; boxes needing more than 32 MiB of FP64 populations
+ * (27 x nodes x 8 bytes, i.e. more than 155,344 nodes) are rejected with
+ * ELBM_E_ARG.  The first call on a device looks the buffer's address up, so
+ * make it before any stream capture.  All calls share the buffer: calls that
+ * overlap on the GPU race.  The call returns after the copy has finished. */
+int elbm_upload_level_noalloc(elbm_ctx* ctx, int lvl, int box, const double* fout);
+
 /* Per-node alpha of the last step (valid-box layout without ghosts, FP64). */
 int elbm_download_alpha(elbm_ctx* ctx, int lvl, int box, double* alpha);
 

@@ -110,6 +110,7 @@ SIGNATURES = {
     "elbm_set_d3q39_params": (_c_int, [_vp, _c_int, ct.POINTER(D3Q39Params)]),
     "elbm_upload_level39": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _vp]),
     "elbm_download_level39": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "elbm_upload_level_noalloc": (_c_int, [_vp, _c_int, _c_int, _vp]),
 }
 
 _lib = None
