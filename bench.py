@@ -189,6 +189,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--size", default=None, help="NXxNYxNZ override (profiling runs on a smaller box)")
+    ap.add_argument("--alpha", default="newton", choices=["newton", "fixed2"],
+                    help="alpha of the timed path (fixed2 = LBGK limit, to separate the alpha solve's cost)")
     ap.add_argument("--profile", action="store_true",
                     help="timed steps only: no validation, end-to-end, FP64 or CPU legs (for ncu captures)")
     args = ap.parse_args()
@@ -218,6 +220,8 @@ def main():
     pkg = ge.load_package()
     cap = pkg.capi
     state, f0, bp = build_workload(pkg)
+    if args.alpha == "fixed2":
+        bp["alpha_mode"] = cap.ELBM_ALPHA_FIXED2
 
     ctx = cap.Context(local_rank)
     box = [[0, 0, 0, NX - 1, NY - 1, NZ - 1]]
@@ -252,8 +256,8 @@ def main():
 
     if args.profile:
         if rank == 0:
-            print(json.dumps({"profile_run": True, "size": [NX, NY, NZ], "mlups": value, "ms_per_step": per_launch_s * 1e3,
-                              "achieved_gbs": achieved}), flush=True)
+            print(json.dumps({"profile_run": True, "size": [NX, NY, NZ], "alpha": args.alpha, "mlups": value,
+                              "ms_per_step": per_launch_s * 1e3, "achieved_gbs": achieved}), flush=True)
         ctx.close()
         return
     # entropy condition and fallbacks over a validation window (check mode, not timed)

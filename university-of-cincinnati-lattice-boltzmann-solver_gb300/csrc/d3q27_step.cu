@@ -276,38 +276,55 @@ struct AlphaOut {
   bool fallback;
 };
 
-// ln(1+x) and phi(x) = (1+x) ln(1+x) - x in FP32 without cancellation, from
-// ln(1+x) = 2 atanh(s), s = x/(2+x):
-//   ln(1+x) = 2 s (1 + s^2/3 + s^4/5 + ...),
-//   phi(x)  = x^2/(2+x) + 2 (1+x) s^3 (1/3 + s^2/5 + s^4/7 + ...),
-// (the leading terms 2s(1+x) - x = x^2/(2+x) cancel exactly).  Eight terms
-// reach FP32 rounding for |s| <= 1/3, i.e. -1/2 <= x <= 1.
-__device__ __forceinline__ void log1p_phi32(float x, float& l1, float& phi) {
-  const float s = __fdividef(x, 2.0f + x), s2 = s * s;
+// Series of 2 atanh: with s = x/(2+x), ln(1+x) = 2 s A(s^2),
+// A(z) = 1 + z/3 + z^2/5 + ..., and B(z) = (A(z) - 1)/z = 1/3 + z/5 + ...;
+// eight terms reach FP32 rounding for |s| <= 1/3 (-1/2 <= x <= 1).
+__device__ __forceinline__ void atanh_series(float s2, float& A, float& B) {
   float a = 1.0f / 17.0f, b = 1.0f / 19.0f;
 #pragma unroll
   for (int k = 7; k >= 0; --k) {
-    a = fmaf(a, s2, 1.0f / (2 * k + 1));  // 1 + s^2/3 + ... (k = 0 term is 1)
-    b = fmaf(b, s2, 1.0f / (2 * k + 3));  // 1/3 + s^2/5 + ...
+    a = fmaf(a, s2, 1.0f / (2 * k + 1));
+    b = fmaf(b, s2, 1.0f / (2 * k + 3));
   }
-  l1 = 2.0f * s * a;
-  phi = fmaf(2.0f * (1.0f + x) * s2 * s, b, __fdividef(x * x, 2.0f + x));
+  A = a;
+  B = b;
 }
 
-// FP32 sum over the flagged populations (|y| > kYSmall), visiting only set
-// bits: G_L(alpha) = sum f psi(y, alpha), G_L'(alpha) = sum f y [ln(1 + alpha y) - ln(1 + y)].
+// psi(y, alpha) = phi(alpha y) - alpha y ln(1 + y) for one strongly
+// non-equilibrium population, without the cancellation of its O(y^2) terms:
+// with x = alpha y, s_x = x/(2+x), s_y = y/(2+y), delta = alpha - 2,
+//   psi = alpha y^2 (2 delta - x) / ((2+x)(2+y))
+//         + 2 (1+x) s_x^3 B(s_x^2) - 2 alpha y s_y^3 B(s_y^2)
+// (the O(y^2) parts of phi(x) = x^2/(2+x) + 2(1+x) s_x^3 B and of
+// alpha y ln(1+y) = 2 alpha y s_y (1 + s_y^2 B) are combined exactly).
+// dlog = ln(1 + alpha y) - ln(1 + y), for the derivative.
+__device__ __forceinline__ void psi_large(float y, float alpha, float delta, float& psi, float& dlog) {
+  const float x = alpha * y;
+  const float sx = __fdividef(x, 2.0f + x), sy = __fdividef(y, 2.0f + y);
+  float Ax, Bx, Ay, By;
+  atanh_series(sx * sx, Ax, Bx);
+  atanh_series(sy * sy, Ay, By);
+  const float t1 = __fdividef(alpha * y * y * fmaf(2.0f, delta, -x), (2.0f + x) * (2.0f + y));
+  const float t2 = 2.0f * (1.0f + x) * sx * sx * sx * Bx;
+  const float t3 = 2.0f * alpha * y * sy * sy * sy * By;
+  psi = t1 + t2 - t3;
+  dlog = 2.0f * fmaf(sx, Ax, -sy * Ay);
+}
+
+// FP32 sum over the flagged populations (|y| > kYSmall):
+// G_L(alpha) = sum f psi(y, alpha), G_L'(alpha) = sum f y [ln(1 + alpha y) - ln(1 + y)].
 struct LargePop {
-  float f, y, l1;
+  float f, y;
 };
-__device__ __forceinline__ void large_terms(const LargePop* lp, int nl, float alpha, float& GL, float& GLp) {
+__device__ __forceinline__ void large_terms(const LargePop* lp, int nl, float alpha, float delta, float& GL,
+                                            float& GLp) {
   GL = 0.f;
   GLp = 0.f;
   for (int k = 0; k < nl; ++k) {
-    float la, ph;
-    log1p_phi32(alpha * lp[k].y, la, ph);
-    const float fy = lp[k].f * lp[k].y;
-    GL += fmaf(lp[k].f, ph, -alpha * fy * lp[k].l1);
-    GLp = fmaf(fy, la - lp[k].l1, GLp);
+    float ps, dl;
+    psi_large(lp[k].y, alpha, delta, ps, dl);
+    GL = fmaf(lp[k].f, ps, GL);
+    GLp = fmaf(lp[k].f * lp[k].y, dl, GLp);
   }
 }
 
@@ -330,29 +347,21 @@ __device__ AlphaOut alpha_series32(const float (&d)[Q], const float (&D)[Q], con
     }
   }
   AlphaOut r{0.f, 0u, large != 0u, false};
-  // compact list of the large populations (rare): f, y and ln(1+y), computed once
-  LargePop lp[8];
+  // compact list of the large populations (rare), visited by the Newton loop only
+  LargePop lp[Q];
   int nl = 0;
   if (large) {
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
-      if ((large & (1u << i)) && nl < 8) {
-        float l1, ph;
-        log1p_phi32(y[i], l1, ph);
+      if (large & (1u << i)) {
         lp[nl].f = (float)w27(i) + d[i];
         lp[nl].y = y[i];
-        lp[nl].l1 = l1;
         ++nl;
       }
     }
-    if (__popc(large) > 8) {  // too many strongly non-equilibrium populations: not handled here
-      r.fallback = true;
-      r.delta = (2.0f < amax) ? 0.f : 0.5f * (amax - 3.0f);
-      return r;
-    }
   }
   if (nl == 0 && !(S[2] > 1e-30f)) return r;  // at equilibrium: alpha = 2
-  float delta = 0.f, last = INFINITY;
+  float delta = 0.f;
   bool ok = false;
   for (int it = 0; it < max_it; ++it) {
     const float alpha = 2.0f + delta;
@@ -367,7 +376,7 @@ __device__ AlphaOut alpha_series32(const float (&d)[Q], const float (&D)[Q], con
     }
     if (nl) {
       float GL, GLp;
-      large_terms(lp, nl, alpha, GL, GLp);
+      large_terms(lp, nl, alpha, delta, GL, GLp);
       const float ia = 1.0f / alpha;
       g = fmaf(GL, ia, g);
       gp += (GLp - GL * ia) * ia;
@@ -378,13 +387,10 @@ __device__ AlphaOut alpha_series32(const float (&d)[Q], const float (&D)[Q], con
     const float next = delta - step;
     if (!(2.0f + next > 1.0f) || !(2.0f + next < amax)) break;
     delta = next;
-    const float as = fabsf(step);
-    // converged, or the step stopped shrinking at the FP32 noise floor
-    if (as <= fmaxf(4e-8f, 2e-7f * fabsf(delta)) || (it >= 2 && as >= 0.5f * last && as <= 1e-5f)) {
+    if (fabsf(step) <= fmaxf(4e-8f, 2e-7f * fabsf(delta))) {
       ok = true;
       break;
     }
-    last = as;
   }
   if (!ok) {
     r.fallback = true;
@@ -395,7 +401,7 @@ __device__ AlphaOut alpha_series32(const float (&d)[Q], const float (&D)[Q], con
 }
 
 template <bool CHECK>
-__global__ void __launch_bounds__(128) d3q27_fp32_kernel(const Step27Args a) {
+__global__ void __launch_bounds__(128, 4) d3q27_fp32_kernel(const Step27Args a) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= a.N) return;
   const uint8_t t = __ldg(a.ntype + n);
