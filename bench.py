@@ -230,8 +230,10 @@ def main():
     ctx.set_links(0, 0, state)
     ctx.upload(0, 0, f0)
 
-    # warm-up, then the timed region: K fused steps, events on the library's stream
+    # warm-up, autotune the step-kernel variant, then the timed region: K fused steps,
+    # CUDA events on the library's stream
     ctx.step(0, args.warmup, want_stats=False)
+    variant, variant_ms = ctx.autotune(0, reps=3)
     ctx.sync()
     if pg:
         pg.barrier()
@@ -256,7 +258,8 @@ def main():
 
     if args.profile:
         if rank == 0:
-            print(json.dumps({"profile_run": True, "size": [NX, NY, NZ], "alpha": args.alpha, "mlups": value,
+            print(json.dumps({"profile_run": True, "size": [NX, NY, NZ], "alpha": args.alpha, "variant": variant,
+                              "variant_ms": list(variant_ms[:2]), "mlups": value,
                               "ms_per_step": per_launch_s * 1e3, "achieved_gbs": achieved}), flush=True)
         ctx.close()
         return
@@ -307,7 +310,8 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"D3Q27 boundary layer {NX}x{NY}x{NZ}, FP32 deviation storage, Newton alpha",
                        "alpha": "newton", "storage": "fp32_dev", "nu": NU, "u_in": U_IN[0], "noise": NOISE,
-                       "l2": "inputs (7.2 GB) larger than L2, no flush", "parallelism": f"replicas x{world}"},
+                       "l2": "inputs (7.2 GB) larger than L2, no flush", "parallelism": f"replicas x{world}",
+                       "kernel_variant": variant, "variant_ms": [float(x) for x in variant_ms[:2]]},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
                          "bytes_per_node": BYTES_PER_NODE_FP32},

@@ -169,6 +169,12 @@ int elbm_download_alpha(elbm_ctx* ctx, int lvl, int box, double* alpha);
  * when given, the call synchronises and fills it. */
 int elbm_level_step(elbm_ctx* ctx, int lvl, int nsteps, elbm_stats* stats);
 
+/* Time every variant of the level's step kernel on its current state (reps
+ * launches each, the state does not advance) and keep the fastest for
+ * elbm_level_step.  chosen and ms_per_variant (room for 8) may be NULL.  The
+ * reference has no counterpart (it has one code path per lattice). */
+int elbm_autotune(elbm_ctx* ctx, int lvl, int reps, int* chosen, double* ms_per_variant);
+
 /* Wait for all work of the context. */
 int elbm_sync(elbm_ctx* ctx);
 

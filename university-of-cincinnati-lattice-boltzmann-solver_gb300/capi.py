@@ -111,6 +111,7 @@ SIGNATURES = {
     "elbm_upload_level39": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _vp]),
     "elbm_download_level39": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
     "elbm_upload_level_noalloc": (_c_int, [_vp, _c_int, _c_int, _vp]),
+    "elbm_autotune": (_c_int, [_vp, _c_int, _c_int, _vp, _vp]),
 }
 
 _lib = None
@@ -260,6 +261,13 @@ class Context:
                                                                       ("fout", "gout", "lm", "w_vel", "alpha",
                                                                        "macro"))))
         return out
+
+    def autotune(self, lvl, reps=3):
+        """Pick the fastest step-kernel variant for the level; returns (index, ms per variant)."""
+        chosen = ct.c_int(0)
+        ms = np.zeros(8)
+        self._check(self.lib.elbm_autotune(self.h, lvl, reps, ct.byref(chosen), _ptr(ms)))
+        return chosen.value, ms
 
     def sync(self):
         self._check(self.lib.elbm_sync(self.h))

@@ -80,6 +80,7 @@ struct Level {
   elbm_d3q27_params p27{};
   elbm_d3q39_params p39{};
   bool params_set = false;
+  int variant = 0;  // FP32 D3Q27 kernel variant picked by elbm_autotune
   DevBuf<uint8_t> eq;  // kEqTables x Q, FP64 or FP32 deviations
 };
 
@@ -633,6 +634,7 @@ int elbm_level_step(elbm_ctx* c, int lvl, int nsteps, elbm_stats* out) {
       a.check_dH = p.check_dH;
       a.alpha_out = (p.record_alpha && s == nsteps - 1) ? b.alpha.p : nullptr;
       a.stats = c->stats.p;
+      a.variant = lv->variant;
       if (lv->storage == ELBM_STORE_FP64) launch_d3q27_fp64(a, c->stream);
       else launch_d3q27_fp32(a, c->stream);
       CUDA_TRY(cudaGetLastError(), "step kernel launch");
@@ -641,6 +643,67 @@ int elbm_level_step(elbm_ctx* c, int lvl, int nsteps, elbm_stats* out) {
   }
   CUDA_TRY(cudaEventRecord(c->ev1, c->stream), "event");
   return finish_stats(c, out);
+}
+
+int elbm_autotune(elbm_ctx* c, int lvl, int reps, int* chosen, double* ms_per_variant) {
+  Level* lv = get_level(c, lvl);
+  if (!lv || reps < 1) return fail(c, ELBM_E_ARG, "unknown level or reps < 1");
+  if (lv->lattice != ELBM_D3Q27 || lv->storage != ELBM_STORE_FP32_DEV || !lv->params_set) {
+    if (chosen) *chosen = 0;
+    return ELBM_OK;  // a single kernel variant exists for the other paths
+  }
+  for (auto& bp : lv->boxes)
+    if (!bp->links_set || !bp->data_set) return fail(c, ELBM_E_STATE, "links or populations missing");
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  const elbm_d3q27_params& p = lv->p27;
+  float best = INFINITY;
+  int best_v = 0;
+  for (int v = 0; v < kFp32Variants; ++v) {
+    CUDA_TRY(cudaEventRecord(c->ev0, c->stream), "event");
+    for (int r = 0; r < reps + 1; ++r) {
+      if (r == 1) CUDA_TRY(cudaEventRecord(c->ev0, c->stream), "event");
+      for (auto& bp : lv->boxes) {
+        Box& b = *bp;
+        Step27Args a{};
+        // read the current state, write the other buffer, do not swap: the level does not advance
+        a.src = b.buf[b.cur].p;
+        a.dst = b.buf[b.cur ^ 1].p;
+        a.plane = b.plane;
+        a.nx = b.nx;
+        a.ny = b.ny;
+        a.nz = b.nz;
+        a.N = b.N;
+        a.ntype = b.ntype.p;
+        a.bidx = b.bidx.p;
+        a.words = b.words.p;
+        a.eq = lv->eq.p;
+        a.beta = 1.0 / (2.0 * p.nu / (1.0 / 3.0) + 1.0);
+        a.tol_alpha = p.tol_alpha;
+        a.tol_dH = p.tol_dH;
+        a.max_newton = p.max_newton;
+        a.alpha_mode = p.alpha_mode;
+        a.check_dH = 0;
+        a.stats = c->stats.p;
+        a.variant = v;
+        launch_d3q27_fp32(a, c->stream);
+        CUDA_TRY(cudaGetLastError(), "autotune launch");
+      }
+    }
+    CUDA_TRY(cudaEventRecord(c->ev1, c->stream), "event");
+    CUDA_TRY(cudaEventSynchronize(c->ev1), "sync");
+    float ms = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1), "elapsed");
+    ms /= reps;
+    if (ms_per_variant) ms_per_variant[v] = ms;
+    if (ms < best) {
+      best = ms;
+      best_v = v;
+    }
+  }
+  lv->variant = best_v;
+  if (chosen) *chosen = best_v;
+  CUDA_TRY(cudaMemsetAsync(c->stats.p, 0, sizeof(DevStats), c->stream), "stats reset");
+  return ELBM_OK;
 }
 
 int elbm_sync(elbm_ctx* c) {

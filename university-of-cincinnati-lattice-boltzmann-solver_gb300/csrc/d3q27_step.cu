@@ -328,35 +328,79 @@ __device__ __forceinline__ void large_terms(const LargePop* lp, int nl, float al
   }
 }
 
+// g(2 + delta) and g'(2 + delta) of the truncated power series (see above).
 template <int K>
-__device__ AlphaOut alpha_series32(const float (&d)[Q], const float (&D)[Q], const float (&y)[Q], unsigned large,
-                                   float amax, int max_it) {
-  float S[K + 1];
+__device__ __forceinline__ void series_g(const float (&S)[K + 1], float delta, float& g, float& gp) {
+  const float alpha = 2.0f + delta;
+  float P = 0.f, pw = 1.f, two = 1.f;
+  g = 0.f;
+  gp = 0.f;
 #pragma unroll
-  for (int k = 0; k <= K; ++k) S[k] = 0.f;
+  for (int n = 2; n <= K; ++n) {
+    gp = fmaf((float)(a_n(n) * (n - 1)) * pw, S[n], gp);
+    P = fmaf(alpha, P, delta * two);
+    two *= 2.f;
+    pw *= alpha;
+    g = fmaf(fmaf((float)a_n(n), P, (float)c0_n(n)), S[n], g);
+  }
+}
+
+// The alpha solve of one node.  Populations come in pairs (float2) so that the
+// power sums run on the paired FP32 pipe.  Strongly non-equilibrium
+// populations (|y| > kYSmall) are left out of the sums, their truncated series
+// is added for a first root (delta0), and one or two Newton steps with their
+// exact psi polish it.
+template <int K>
+__device__ AlphaOut alpha_solve32(const float2 (&D2)[14], const float2 (&y2)[14], const float (&d)[Q],
+                                  unsigned large, float amax, int max_it) {
+  float2 S2[K + 1];
 #pragma unroll
-  for (int i = 0; i < Q; ++i) {
-    const bool small = !(large & (1u << i));
-    const float yi = small ? y[i] : 0.f;
-    float p = small ? D[i] * y[i] : 0.f;  // f y^2
-    S[2] += p;
+  for (int k = 0; k <= K; ++k) S2[k] = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int q = 0; q < 14; ++q) {
+    const bool sa = !(large & (1u << (2 * q))), sb = !(large & (1u << (2 * q + 1)));
+    const float2 ym = make_float2(sa ? y2[q].x : 0.f, sb ? y2[q].y : 0.f);
+    float2 p = __fmul2_rn(make_float2(sa ? D2[q].x : 0.f, sb ? D2[q].y : 0.f), ym);  // f y^2
+    S2[2] = __fadd2_rn(S2[2], p);
 #pragma unroll
     for (int k = 3; k <= K; ++k) {
-      p *= yi;
-      S[k] += p;
+      p = __fmul2_rn(p, ym);
+      S2[k] = __fadd2_rn(S2[k], p);
     }
   }
+  float S[K + 1];
+#pragma unroll
+  for (int k = 0; k <= K; ++k) S[k] = S2[k].x + S2[k].y;
+
   AlphaOut r{0.f, 0u, large != 0u, false};
-  // compact list of the large populations (rare), visited by the Newton loop only
   LargePop lp[Q];
   int nl = 0;
-  if (large) {
+  float SL[K + 1];
 #pragma unroll
-    for (int i = 0; i < Q; ++i) {
-      if (large & (1u << i)) {
-        lp[nl].f = (float)w27(i) + d[i];
-        lp[nl].y = y[i];
-        ++nl;
+  for (int k = 0; k <= K; ++k) SL[k] = S[k];
+  if (large) {
+    // compact list (static indexing keeps the pair arrays in registers)
+#pragma unroll
+    for (int q = 0; q < 14; ++q) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int i = 2 * q + h;
+        if (i < Q && (large & (1u << i))) {
+          lp[nl].f = (float)w27(i) + d[i];
+          lp[nl].y = h ? y2[q].y : y2[q].x;
+          ++nl;
+        }
+      }
+    }
+    // their truncated series joins the first solve
+    for (int k2 = 0; k2 < nl; ++k2) {
+      const float y = lp[k2].y;
+      float p = lp[k2].f * y * y;
+      SL[2] += p;
+#pragma unroll
+      for (int k = 3; k <= K; ++k) {
+        p *= y;
+        SL[k] += p;
       }
     }
   }
@@ -364,23 +408,8 @@ __device__ AlphaOut alpha_series32(const float (&d)[Q], const float (&D)[Q], con
   float delta = 0.f;
   bool ok = false;
   for (int it = 0; it < max_it; ++it) {
-    const float alpha = 2.0f + delta;
-    float g = 0.f, gp = 0.f, P = 0.f, pw = 1.f, two = 1.f;
-#pragma unroll
-    for (int n = 2; n <= K; ++n) {
-      gp = fmaf((float)(a_n(n) * (n - 1)) * pw, S[n], gp);
-      P = fmaf(alpha, P, delta * two);
-      two *= 2.f;
-      pw *= alpha;
-      g = fmaf(fmaf((float)a_n(n), P, (float)c0_n(n)), S[n], g);
-    }
-    if (nl) {
-      float GL, GLp;
-      large_terms(lp, nl, alpha, delta, GL, GLp);
-      const float ia = 1.0f / alpha;
-      g = fmaf(GL, ia, g);
-      gp += (GLp - GL * ia) * ia;
-    }
+    float g, gp;
+    series_g<K>(SL, delta, g, gp);
     r.iters = it + 1;
     if (!(gp > 0.f)) break;
     const float step = g / gp;
@@ -392,6 +421,28 @@ __device__ AlphaOut alpha_series32(const float (&d)[Q], const float (&D)[Q], con
       break;
     }
   }
+  if (ok && nl) {
+    ok = false;
+    for (int it = 0; it < 4; ++it) {
+      const float alpha = 2.0f + delta;
+      float g, gp, GL, GLp;
+      series_g<K>(S, delta, g, gp);
+      large_terms(lp, nl, alpha, delta, GL, GLp);
+      const float ia = 1.0f / alpha;
+      g = fmaf(GL, ia, g);
+      gp += (GLp - GL * ia) * ia;
+      r.iters += 1;
+      if (!(gp > 0.f)) break;
+      const float step = g / gp;
+      const float next = delta - step;
+      if (!(2.0f + next > 1.0f) || !(2.0f + next < amax)) break;
+      delta = next;
+      if (fabsf(step) <= fmaxf(4e-8f, 2e-7f * fabsf(delta))) {
+        ok = true;
+        break;
+      }
+    }
+  }
   if (!ok) {
     r.fallback = true;
     delta = (2.0f < amax) ? 0.f : 0.5f * (amax - 3.0f);
@@ -400,8 +451,10 @@ __device__ AlphaOut alpha_series32(const float (&d)[Q], const float (&D)[Q], con
   return r;
 }
 
-template <bool CHECK>
-__global__ void __launch_bounds__(128, 4) d3q27_fp32_kernel(const Step27Args a) {
+// MINB: minimum resident blocks per SM requested from the register allocator
+// (0: none).  Both variants are built; the level's autotuner picks one.
+template <bool CHECK, int MINB>
+__global__ void __launch_bounds__(128, MINB) d3q27_fp32_kernel(const Step27Args a) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= a.N) return;
   const uint8_t t = __ldg(a.ntype + n);
@@ -435,42 +488,67 @@ __global__ void __launch_bounds__(128, 4) d3q27_fp32_kernel(const Step27Args a) 
     e[k][2] = fmaf(1.0f - sm1, zm1, -sm1);
     e[k][0] = (-sm1 - zm1) / (1.0f + zm1);
   }
-  // Delta_i = f^eq_i - f_i in deviation form: w_i [(1+P)(1+dr) - 1] - d_i, P = prod(1+e) - 1
-  float D[Q];
+  // P_i = prod(1 + e) - 1 = A + (1 + A)(B + (1 + B) C), with the (y, z) part shared
+  float qyz[3][3];
 #pragma unroll
-  for (int i = 0; i < Q; ++i) {
-    const float A = e[0][cx27(i) + 1], B = e[1][cy27(i) + 1], C = e[2][cz27(i) + 1];
-    const float P = fmaf(1.0f + A, fmaf(1.0f + B, C, B), A);
-    const float wi = (float)w27(i);
-    D[i] = fmaf(wi, fmaf(dr, 1.0f + P, P), -d[i]);
+  for (int b = 0; b < 3; ++b)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) qyz[b][c] = fmaf(1.0f + e[1][b], e[2][c], e[1][b]);
+  // Delta_i = f^eq_i - f_i in deviation form: w_i [P (1 + dr) + dr] - d_i, kept in pairs
+  const float rp1 = 1.0f + dr;
+  float2 D2[14];
+#pragma unroll
+  for (int q = 0; q < 14; ++q) {
+    float v[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int i = 2 * q + h;
+      if (i < Q) {
+        const float A = e[0][cx27(i) + 1];
+        const float P = fmaf(1.0f + A, qyz[cy27(i) + 1][cz27(i) + 1], A);
+        v[h] = fmaf((float)w27(i), fmaf(P, rp1, dr), -d[i]);
+      } else {
+        v[h] = 0.f;
+      }
+    }
+    D2[q] = make_float2(v[0], v[1]);
   }
 
   AlphaOut al{0.f, 0u, false, false};
   double dH = 0.0;
   if (a.alpha_mode != 0) {
-    float y[Q];
-    float ysmall = 0.f, amax = INFINITY;
+    float2 y2[14];
+    float ysmall = 0.f, ymin = 0.f;
     unsigned large = 0u;
 #pragma unroll
-    for (int i = 0; i < Q; ++i) {
-      y[i] = __fdividef(D[i], (float)w27(i) + d[i]);
-      const float ay = fabsf(y[i]);
-      if (ay <= kYSmall) ysmall = fmaxf(ysmall, ay);
-      else large |= 1u << i;
-      if (y[i] < 0.f) amax = fminf(amax, -1.0f / y[i]);
+    for (int q = 0; q < 14; ++q) {
+      const int i0 = 2 * q, i1 = 2 * q + 1;
+      const float fa = (float)w27(i0) + d[i0];
+      const float fb = (i1 < Q) ? (float)w27(i1) + d[i1] : 1.0f;
+      y2[q] = make_float2(__fdividef(D2[q].x, fa), __fdividef(D2[q].y, fb));
+      const float aa = fabsf(y2[q].x), ab = fabsf(y2[q].y);
+      if (aa <= kYSmall) ysmall = fmaxf(ysmall, aa);
+      else large |= 1u << i0;
+      if (ab <= kYSmall) ysmall = fmaxf(ysmall, ab);
+      else large |= 1u << i1;
+      ymin = fminf(ymin, fminf(y2[q].x, y2[q].y));
     }
+    // positivity bracket: f + alpha Delta > 0 for all i  <=>  alpha < -1/min(y)
+    const float amax = (ymin < 0.f) ? -1.0f / ymin : INFINITY;
     // warp-uniform series order from the warp's largest small |y|
     const float wmax = __int_as_float(__reduce_max_sync(__activemask(), __float_as_int(ysmall)));
-    if (wmax <= 0.02f) al = alpha_series32<6>(d, D, y, large, amax, a.max_newton);
-    else if (wmax <= 0.04f) al = alpha_series32<8>(d, D, y, large, amax, a.max_newton);
-    else al = alpha_series32<12>(d, D, y, large, amax, a.max_newton);
+    if (wmax <= 0.02f) al = alpha_solve32<6>(D2, y2, d, large, amax, a.max_newton);
+    else if (wmax <= 0.04f) al = alpha_solve32<8>(D2, y2, d, large, amax, a.max_newton);
+    else if (wmax <= 0.06f) al = alpha_solve32<10>(D2, y2, d, large, amax, a.max_newton);
+    else al = alpha_solve32<12>(D2, y2, d, large, amax, a.max_newton);
     if (CHECK) {
       // |H(f + alpha Delta) - H(f)| in FP64 (conservation-consistent form) from the FP32 populations
       const double al64 = 2.0 + (double)al.delta;
       double g = 0.0;
 #pragma unroll
       for (int i = 0; i < Q; ++i) {
-        const double f64 = (double)((float)w27(i) + d[i]), y64 = (double)D[i] / f64;
+        const double f64 = (double)((float)w27(i) + d[i]);
+        const double y64 = (double)((i & 1) ? D2[i >> 1].y : D2[i >> 1].x) / f64;
         g += f64 * (phi64(al64 * y64) - al64 * y64 * log1p(y64));
       }
       dH = fabs(g);
@@ -484,7 +562,7 @@ __global__ void __launch_bounds__(128, 4) d3q27_fp32_kernel(const Step27Args a) 
   bool neg = false;
 #pragma unroll
   for (int i = 0; i < Q; ++i) {
-    d[i] = fmaf(ab, D[i], d[i]);
+    d[i] = fmaf(ab, (i & 1) ? D2[i >> 1].y : D2[i >> 1].x, d[i]);
     neg |= (d[i] + (float)w27(i)) < 0.f;
   }
   if (neg) flags |= 0x4u;
@@ -504,8 +582,9 @@ void launch_d3q27_fp64(const Step27Args& a, cudaStream_t s) {
 void launch_d3q27_fp32(const Step27Args& a, cudaStream_t s) {
   const int threads = 128;
   const int64_t blocks = (a.N + threads - 1) / threads;
-  if (a.check_dH) d3q27_fp32_kernel<true><<<(unsigned)blocks, threads, 0, s>>>(a);
-  else d3q27_fp32_kernel<false><<<(unsigned)blocks, threads, 0, s>>>(a);
+  if (a.check_dH) d3q27_fp32_kernel<true, 0><<<(unsigned)blocks, threads, 0, s>>>(a);
+  else if (a.variant == 1) d3q27_fp32_kernel<false, 4><<<(unsigned)blocks, threads, 0, s>>>(a);
+  else d3q27_fp32_kernel<false, 0><<<(unsigned)blocks, threads, 0, s>>>(a);
 }
 
 }  // namespace elbm

@@ -39,7 +39,10 @@ struct Step27Args {
   float* alpha_out;       // optional per-node alpha (FP32)
   DevStats* stats;
   const void* mlp;        // learned-alpha weights (ELBM_ALPHA_LEARNED)
+  int variant;            // kernel variant chosen by the autotuner
 };
+
+constexpr int kFp32Variants = 2;
 
 void launch_d3q27_fp64(const Step27Args& a, cudaStream_t s);
 void launch_d3q27_fp32(const Step27Args& a, cudaStream_t s);
