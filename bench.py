@@ -180,6 +180,52 @@ def cpu_baseline_sample(pkg, budget_s=15.0):
             "sample": f"{sx}x{sy}x{sz} sub-box of the workload, {steps} FP64 Newton-alpha steps, {dt:.1f} s"}
 
 
+def learned_alpha_leg(pkg, ctx, args, bp, local_rank):
+    """Harvest, train, and time the learned-alpha path; returns a summary dict."""
+    from oracle import mlp_ref  # initial weights only (a seeded Gaussian draw)
+
+    cap, geo = pkg.capi, pkg.geometry
+    recs = []
+    for kind in ("plate", "sphere"):
+        h = cap.Context(local_rank)
+        if kind == "plate":
+            n = (128, 64, 64)
+            st = geo.box_state27(*n, geo.flat_plate_faces())
+            f0 = geo.perturbed_equilibrium(*n, U_IN, NOISE, seed=SEED + 1)
+            hb = geo.d3q27_boundary_params(U_IN, NU)
+        else:
+            n = (128, 64, 64)
+            st = geo.box_state27(*n, geo.sphere_faces())
+            cap.mark_triangles(st, (0.0, 0.0, 0.0), 1.0, geo.icosphere(4, 8.0, (32.0, 32.0, 32.0)))
+            f0 = geo.perturbed_equilibrium(*n, (0.08, 0, 0), 1e-3, seed=SEED + 2)
+            f0[:, st[0] == -1001] = pkg.lattice.W[:, None]
+            hb = geo.d3q27_boundary_params((0.08, 0, 0), 5e-4)
+        h.level_register(0, cap.ELBM_D3Q27, cap.ELBM_STORE_FP32_DEV, [[0, 0, 0, n[0] - 1, n[1] - 1, n[2] - 1]])
+        h.set_d3q27_params(0, cap.make_d3q27_params(**hb))
+        h.set_links(0, 0, st)
+        h.upload(0, 0, f0)
+        recs.append(h.alpha_harvest(0, nsteps=40, stride=4, capacity=1 << 21))
+        h.close()
+    rec = np.concatenate(recs)
+    t0 = time.perf_counter()
+    w, hist = ctx.alpha_mlp_train(rec, mlp_ref.init(0).astype(np.float32), epochs=4, batch=8192, lr=2e-3, seed=1)
+    train_s = time.perf_counter() - t0
+    ctx.set_alpha_mlp(0, w)
+    lp = cap.make_d3q27_params(**dict(bp, alpha_mode=cap.ELBM_ALPHA_LEARNED))
+    ctx.set_d3q27_params(0, lp)
+    ctx.step(0, 2, want_stats=False)
+    st = ctx.step(0, args.steps)
+    mlups = st["node_updates"] / (st["kernel_ms"] / 1e3) / 1e6
+    chk = cap.make_d3q27_params(**dict(bp, alpha_mode=cap.ELBM_ALPHA_LEARNED, check_dH=1))
+    ctx.set_d3q27_params(0, chk)
+    v = ctx.step(0, 3)
+    ctx.set_d3q27_params(0, cap.make_d3q27_params(**bp))
+    return {"mlups": mlups, "records": int(rec.shape[0]), "train_s": train_s, "loss": [float(x) for x in hist],
+            "newton_iters_per_node": st["newton_iters"] / max(1, st["node_updates"]),
+            "guess_misses_per_node": st["guess_misses"] / max(1, st["node_updates"]),
+            "max_abs_dH": v["max_abs_dH"], "dh_over_tol": v["dh_over_tol"], "fallbacks": v["fallbacks"]}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -270,6 +316,11 @@ def main():
     vst = ctx.step(0, 3)
     ctx.set_d3q27_params(0, cap.make_d3q27_params(**bp))
 
+    # learned alpha: harvest (populations, alpha) records from Newton solves of smaller
+    # boxes of the boundary layer and of the sphere case, train the network on the GPU,
+    # then time the learned guess + at most two Newton steps on the same workload
+    learned = learned_alpha_leg(pkg, ctx, args, bp, local_rank)
+
     # end to end through the C ABI with host buffers: upload, K steps, download
     import torch
 
@@ -325,6 +376,7 @@ def main():
                            "exact_path_nodes": vst["exact_path_nodes"], "status": vst["status"],
                            "newton_iters_per_node": vst["newton_iters"] / max(1, vst["node_updates"])},
             "plain_fp64_newton_mlups": fp64,
+            "learned_alpha": learned,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)

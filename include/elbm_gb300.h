@@ -104,6 +104,7 @@ typedef struct {
   uint32_t pad;
   double max_abs_dH;        /* check mode only */
   int64_t dh_over_tol;      /* check mode: nodes whose |dH| exceeded tol_dH */
+  int64_t guess_misses;     /* learned alpha: guesses that needed the Newton fallback from alpha = 2 */
   double kernel_ms;         /* device time of the step kernels (CUDA events) */
 } elbm_stats;
 
@@ -142,6 +143,16 @@ int elbm_download_level39(elbm_ctx* ctx, int lvl, int box, double* fout, double*
  * per node and a compact table of boundary links. */
 int elbm_set_links(elbm_ctx* ctx, int lvl, int box, const int32_t* state, int ngrow_state);
 
+/* Set-up helper (host code, no GPU): mark the solid nodes of a closed
+ * triangulated surface (ray casting, like lbgrid/fluid_or_solid) and the wall
+ * links of the fluid nodes with their packed crossing fraction
+ * state = -1001 - floor(|x - x_w| / (|c_i| dx) * 1e9), the encoding of
+ * lbgrid/inter_bb_setup.f95:44-246 and linking/modules/linkwise.f95:45-57.
+ * state: 27 components of nx*ny*nz int32 (no ghosts), updated in place; node
+ * (i,j,k) sits at origin + (i,j,k)*dx; tri: 9 doubles per triangle. */
+int elbm_mark_triangles(int nx, int ny, int nz, const double* origin, double dx, int ntri, const double* tri,
+                        int32_t* state);
+
 /* Copy one box's post-collision populations (fout FAB, FP64, Q comps) to / from the device. */
 int elbm_upload_level(elbm_ctx* ctx, int lvl, int box, const double* fout);
 int elbm_download_level(elbm_ctx* ctx, int lvl, int box, double* fout);
@@ -174,6 +185,27 @@ int elbm_level_step(elbm_ctx* ctx, int lvl, int nsteps, elbm_stats* stats);
  * elbm_level_step.  chosen and ms_per_variant (room for 8) may be NULL.  The
  * reference has no counterpart (it has one code path per lattice). */
 int elbm_autotune(elbm_ctx* ctx, int lvl, int reps, int* chosen, double* ms_per_variant);
+
+/* Learned initial guess of alpha (no counterpart in the reference; its
+ * Future Work.txt:34 proposes machine learning to shorten the solves): a
+ * 27-64-64-1 GELU network maps y/lambda (y_i = Delta_i/f_i, lambda = max|y_i|)
+ * to (alpha - 2)/lambda.  Weights: 6017 floats, W1[27][64], b1[64], W2[64][64],
+ * b2[64], w3[64], b3.  Records: 29 floats, y/lambda (27), lambda, target. */
+#define ELBM_MLP_PARAMS 6017
+#define ELBM_MLP_RECORD 29
+
+/* Run nsteps Newton-alpha steps of an FP32 D3Q27 level and collect a record
+ * from every stride-th node whose solve converged (at most capacity). */
+int elbm_alpha_harvest(elbm_ctx* ctx, int lvl, int nsteps, int stride, float* records, int64_t capacity,
+                       int64_t* count);
+/* Mean-squared-error loss and its gradient for one batch (the training kernels). */
+int elbm_alpha_mlp_grad(elbm_ctx* ctx, const float* weights, const float* records, int64_t n, float* grad,
+                        double* loss);
+/* Adam training on the GPU; weights in/out; loss_per_epoch may be NULL. */
+int elbm_alpha_mlp_train(elbm_ctx* ctx, const float* records, int64_t n, int epochs, int batch, float lr,
+                         uint64_t seed, float* weights, double* loss_per_epoch);
+/* Weights used by ELBM_ALPHA_LEARNED on this level. */
+int elbm_set_alpha_mlp(elbm_ctx* ctx, int lvl, const float* weights);
 
 /* Wait for all work of the context. */
 int elbm_sync(elbm_ctx* ctx);

@@ -296,6 +296,22 @@ int o27_step(int nx, int ny, int nz, const int32_t* state, const double* fo_prev
             fi[(int64_t)o * N + n] = v;
           } else if (code == -666 || code == -1001) {
             /* null / solid neighbour without a wall fraction: nothing streams */
+          } else if (code < -1001) {
+            /* wall link with packed fraction (linkwise.f95:56), decoded as
+             * interpolative_bounceback_bc.f95:66; linear interpolated bounce-back
+             * (Bouzidi, Firdaouss, Lallemand 2001) */
+            const double q = fabs((double)code + 1001.0) / 1e9;
+            double v;
+            const int xb = x - CX[i], yb = y - CY[i], zb = z - CZ[i];
+            const int have2 = xb >= 0 && yb >= 0 && zb >= 0 && xb < nx && yb < ny && zb < nz &&
+                              node_is_fluid(state[idx(xb, yb, zb, nx, ny)]);
+            if (q < 0.5 && have2)
+              v = 2.0 * q * fv + (1.0 - 2.0 * q) * fo_prev[(int64_t)i * N + idx(xb, yb, zb, nx, ny)];
+            else if (q >= 0.5)
+              v = fv / (2.0 * q) + (1.0 - 1.0 / (2.0 * q)) * fo_prev[(int64_t)o * N + n];
+            else
+              v = fv;
+            fi[(int64_t)o * N + n] = v;
           } else {
             rc = -1;
             break;
@@ -351,4 +367,94 @@ void o27_moments(int64_t N, const double* f, double* rho, double* ux, double* uy
     uy[n] = jy / r;
     uz[n] = jz / r;
   }
+}
+
+/* Solid nodes and wall-link fractions of a closed triangulated surface, by
+ * testing every triangle for every node and link (the search of
+ * lbgrid/inter_bb_setup.f95:44-246 and fluid_or_solid ray casting), in the
+ * encoding of linkwise.f95:45-57.  Used to check the accelerated set-up code
+ * bit for bit.  Node (i,j,k) sits at origin + (i,j,k) dx. */
+static double o_seg_tri(const double* v, const double* p0, const double* p1) {
+  const double a[3] = {v[3] - v[0], v[4] - v[1], v[5] - v[2]}, b[3] = {v[6] - v[0], v[7] - v[1], v[8] - v[2]};
+  const double n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+  const double dotv = n[0] * v[0] + n[1] * v[1] + n[2] * v[2];
+  const double upper = dotv - (p0[0] * n[0] + p0[1] * n[1] + p0[2] * n[2]);
+  const double lower = (p1[0] - p0[0]) * n[0] + (p1[1] - p0[1]) * n[1] + (p1[2] - p0[2]) * n[2];
+  if (lower == 0.0) return -1.0;
+  const double t = upper / lower;
+  if (!(t > 0.0 && t <= 1.0)) return -1.0;
+  const double xc[3] = {p0[0] + t * (p1[0] - p0[0]), p0[1] + t * (p1[1] - p0[1]), p0[2] + t * (p1[2] - p0[2])};
+  double e[3][3];
+  for (int k = 0; k < 3; ++k)
+    for (int c = 0; c < 3; ++c) e[k][c] = v[3 * k + c] - p0[c];
+  const double r[3] = {xc[0] - p0[0], xc[1] - p0[1], xc[2] - p0[2]};
+#define VOL(A, B) (r[0] * (A[1] * B[2] - A[2] * B[1]) + r[1] * (A[2] * B[0] - A[0] * B[2]) + r[2] * (A[0] * B[1] - A[1] * B[0]))
+  const double v1 = VOL(e[0], e[1]), v2 = -VOL(e[0], e[2]), v3 = VOL(e[1], e[2]);
+#undef VOL
+  const int pos = v1 >= 0.0 && v2 >= 0.0 && v3 >= 0.0, neg = v1 <= 0.0 && v2 <= 0.0 && v3 <= 0.0;
+  return (pos || neg) ? t : -1.0;
+}
+
+static int o_ray_x(const double* v, const double* p) {
+  const double y = p[1], z = p[2];
+  const double y0 = v[1], z0 = v[2], y1 = v[4], z1 = v[5], y2 = v[7], z2 = v[8];
+  const double det = (y1 - y0) * (z2 - z0) - (y2 - y0) * (z1 - z0);
+  if (det == 0.0) return 0;
+  double w[3];
+  const double ay[3] = {y1, y2, y0}, az[3] = {z1, z2, z0}, by[3] = {y2, y0, y1}, bz[3] = {z2, z0, z1};
+  for (int k = 0; k < 3; ++k) {
+    double ww = (by[k] - ay[k]) * (z - az[k]) - (bz[k] - az[k]) * (y - ay[k]);
+    if (ww == 0.0) ww = ((bz[k] > az[k]) || (bz[k] == az[k] && by[k] < ay[k])) ? 1e-300 : -1e-300;
+    w[k] = (det < 0.0) ? -ww : ww;
+  }
+  if (!(w[0] > 0.0 && w[1] > 0.0 && w[2] > 0.0)) return 0;
+  const double a[3] = {v[3] - v[0], v[4] - v[1], v[5] - v[2]}, b[3] = {v[6] - v[0], v[7] - v[1], v[8] - v[2]};
+  const double n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+  if (n[0] == 0.0) return 0;
+  const double xs = v[0] - (n[1] * (y - y0) + n[2] * (z - z0)) / n[0];
+  return xs > p[0];
+}
+
+int o27_mark_triangles(int nx, int ny, int nz, const double* origin, double dx, int ntri, const double* tri,
+                       int32_t* state) {
+  const int64_t N = (int64_t)nx * ny * nz;
+  char* solid = (char*)calloc(N, 1);
+  if (!solid) return -1;
+#pragma omp parallel for schedule(dynamic)
+  for (int64_t n = 0; n < N; ++n) {
+    const int i = (int)(n % nx), j = (int)((n / nx) % ny), k = (int)(n / ((int64_t)nx * ny));
+    const double p[3] = {origin[0] + i * dx, origin[1] + j * dx, origin[2] + k * dx};
+    int cross = 0;
+    for (int t = 0; t < ntri; ++t) cross += o_ray_x(tri + 9 * t, p);
+    solid[n] = (char)(cross & 1);
+  }
+  for (int64_t n = 0; n < N; ++n)
+    if (solid[n])
+      for (int q = 0; q < Q; ++q) state[(int64_t)q * N + n] = -1001;
+#pragma omp parallel for schedule(dynamic)
+  for (int64_t n = 0; n < N; ++n) {
+    if (solid[n]) continue;
+    const int i = (int)(n % nx), j = (int)((n / nx) % ny), k = (int)(n / ((int64_t)nx * ny));
+    const double p0[3] = {origin[0] + i * dx, origin[1] + j * dx, origin[2] + k * dx};
+    for (int q = 1; q < Q; ++q) {
+      const double p1[3] = {p0[0] + CX[q] * dx, p0[1] + CY[q] * dx, p0[2] + CZ[q] * dx};
+      double tbest = INFINITY;
+      for (int t = 0; t < ntri; ++t) {
+        const double tt = o_seg_tri(tri + 9 * t, p0, p1);
+        if (tt > 0.0 && tt < tbest) tbest = tt;
+      }
+      if (tbest == INFINITY) {
+        const int it = i + CX[q], jt = j + CY[q], kt = k + CZ[q];
+        if (it >= 0 && jt >= 0 && kt >= 0 && it < nx && jt < ny && kt < nz && solid[idx(it, jt, kt, nx, ny)])
+          tbest = 1.0;
+        else
+          continue;
+      }
+      const double len = sqrt((double)(CX[q] * CX[q] + CY[q] * CY[q] + CZ[q] * CZ[q])) * dx;
+      const double dist = tbest * len;
+      state[(int64_t)q * N + n] = -1001 - (int32_t)floor(dist / len * 1e9);
+    }
+  }
+  free(solid);
+  return 0;
 }

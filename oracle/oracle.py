@@ -51,6 +51,8 @@ def lib():
         _lib.o27_alpha_newton.argtypes = [vp, vp, ct.c_double, ct.c_int, ct.POINTER(ct.c_int), ct.POINTER(ct.c_int)]
         _lib.o27_entropy_diff.restype = ct.c_double
         _lib.o27_entropy_diff.argtypes = [vp, vp, ct.c_double]
+        _lib.o27_mark_triangles.restype = ct.c_int
+        _lib.o27_mark_triangles.argtypes = [ct.c_int, ct.c_int, ct.c_int, vp, ct.c_double, ct.c_int, vp, vp]
         _lib.o27_equilibrium.restype = None
         _lib.o27_equilibrium.argtypes = [ct.c_double, vp, vp]
     return _lib
@@ -115,3 +117,13 @@ def equilibrium(rho, u):
     out = np.zeros(27)
     lib().o27_equilibrium(rho, _p(u), _p(out))
     return out
+
+
+def mark_triangles(state, origin, dx, tri):
+    """Brute-force solid marking and wall fractions (every triangle for every link)."""
+    _, nz, ny, nx = state.shape
+    o = np.ascontiguousarray(origin, np.float64)
+    t = np.ascontiguousarray(tri, np.float64).reshape(-1, 9)
+    rc = lib().o27_mark_triangles(nx, ny, nz, _p(o), dx, t.shape[0], _p(t), _p(state))
+    if rc != 0:
+        raise RuntimeError("oracle marking failed")

@@ -1,0 +1,62 @@
+"""Learned alpha end to end on the GPU: harvest (populations, alpha) records
+from Newton solves, train the network with the library's kernels, and run the
+step with the learned guess + at most two Newton steps (Newton from 2 as the
+fallback).  The result must satisfy the same entropy condition and agree with
+the Newton path; the test reports what the guess saves."""
+import numpy as np
+import pytest
+
+from oracle import mlp_ref
+
+pytestmark = pytest.mark.gpu
+
+
+def _level(pkg, alpha_mode, check=0, n=(64, 32, 32)):
+    geo, cap = pkg.geometry, pkg.capi
+    nx, ny, nz = n
+    st = geo.box_state27(nx, ny, nz, geo.flat_plate_faces())
+    f0 = geo.perturbed_equilibrium(nx, ny, nz, (0.06, 0, 0), 5e-3, seed=77)
+    bp = geo.d3q27_boundary_params((0.06, 0, 0), 2e-5)
+    bp.update(alpha_mode=alpha_mode, check_dH=check)
+    ctx = cap.Context(0)
+    ctx.level_register(0, cap.ELBM_D3Q27, cap.ELBM_STORE_FP32_DEV, [[0, 0, 0, nx - 1, ny - 1, nz - 1]])
+    return ctx, st, f0, bp
+
+
+def test_learned_alpha_pipeline(pkg, built_lib):
+    cap = pkg.capi
+    # harvest from Newton solves
+    ctx, st, f0, bp = _level(pkg, cap.ELBM_ALPHA_NEWTON)
+    ctx.set_d3q27_params(0, cap.make_d3q27_params(**bp))
+    ctx.set_links(0, 0, st)
+    ctx.upload(0, 0, f0)
+    rec = ctx.alpha_harvest(0, nsteps=30, stride=3, capacity=1 << 20)
+    assert rec.shape[0] > 100000 and np.isfinite(rec).all()
+    w, hist = ctx.alpha_mlp_train(rec, mlp_ref.init(0).astype(np.float32), epochs=8, batch=4096, lr=2e-3, seed=3)
+    assert hist[-1] < 0.5 * hist[0], hist
+    f_mid = ctx.download(0)
+    # Newton and learned steps from the same state
+    res = {}
+    for mode in (cap.ELBM_ALPHA_NEWTON, cap.ELBM_ALPHA_LEARNED):
+        c2, st2, _, bp2 = _level(pkg, mode, check=1)
+        if mode == cap.ELBM_ALPHA_LEARNED:
+            c2.set_alpha_mlp(0, w)
+        c2.set_d3q27_params(0, cap.make_d3q27_params(**bp2))
+        c2.set_links(0, 0, st2)
+        c2.upload(0, 0, f_mid)
+        s = c2.step(0, 10)
+        res[mode] = (s, c2.download(0))
+        c2.close()
+    sn, fn = res[cap.ELBM_ALPHA_NEWTON]
+    sl, fl = res[cap.ELBM_ALPHA_LEARNED]
+    assert sl["dh_over_tol"] == 0 and sl["max_abs_dH"] <= 1e-10, sl
+    assert sl["fallbacks"] <= 1e-5 * sl["node_updates"]
+    # both paths solve the same equation: the populations agree to FP32 level
+    assert np.max(np.abs(fl - fn)) <= 1e-6
+    it_newton = sn["newton_iters"] / sn["node_updates"]
+    it_learned = sl["newton_iters"] / sl["node_updates"]
+    print(f"Newton iterations per node: {it_newton:.3f} from alpha = 2, {it_learned:.3f} from the learned guess; "
+          f"guesses needing the fallback: {sl['guess_misses'] / sl['node_updates']:.2e}")
+    assert sl["guess_misses"] <= 0.01 * sl["node_updates"]
+    assert it_learned < it_newton
+    ctx.close()

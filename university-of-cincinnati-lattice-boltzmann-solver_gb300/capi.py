@@ -88,6 +88,7 @@ class Stats(ct.Structure):
         ("pad", ct.c_uint32),
         ("max_abs_dH", ct.c_double),
         ("dh_over_tol", ct.c_int64),
+        ("guess_misses", ct.c_int64),
         ("kernel_ms", ct.c_double),
     ]
 
@@ -112,7 +113,14 @@ SIGNATURES = {
     "elbm_download_level39": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
     "elbm_upload_level_noalloc": (_c_int, [_vp, _c_int, _c_int, _vp]),
     "elbm_autotune": (_c_int, [_vp, _c_int, _c_int, _vp, _vp]),
+    "elbm_mark_triangles": (_c_int, [_c_int, _c_int, _c_int, _vp, _c_double, _c_int, _vp, _vp]),
+    "elbm_alpha_harvest": (_c_int, [_vp, _c_int, _c_int, _c_int, _vp, ct.c_int64, _vp]),
+    "elbm_alpha_mlp_grad": (_c_int, [_vp, _vp, _vp, ct.c_int64, _vp, _vp]),
+    "elbm_alpha_mlp_train": (_c_int, [_vp, _vp, ct.c_int64, _c_int, _c_int, ct.c_float, ct.c_uint64, _vp, _vp]),
+    "elbm_set_alpha_mlp": (_c_int, [_vp, _c_int, _vp]),
 }
+MLP_PARAMS = 6017
+MLP_RECORD = 29
 
 _lib = None
 
@@ -167,6 +175,19 @@ def make_d3q27_params(nu, tol_alpha=1e-12, tol_dH=1e-10, max_newton=30, alpha_mo
             p.inl_feq[k][j] = inl[k, j]
             p.outl_feq[k][j] = outl[k, j]
     return p
+
+
+def mark_triangles(state: np.ndarray, origin, dx: float, tri: np.ndarray) -> None:
+    """Mark solid nodes and wall-link fractions of a closed triangulated surface
+    in a state array (27, nz, ny, nx), in place (host code, no GPU needed)."""
+    lib = load()
+    assert state.dtype == np.int32 and state.flags.c_contiguous and state.shape[0] == 27
+    _, nz, ny, nx = state.shape
+    o = np.ascontiguousarray(origin, np.float64)
+    t = np.ascontiguousarray(tri, np.float64).reshape(-1, 9)
+    rc = lib.elbm_mark_triangles(nx, ny, nz, _ptr(o), dx, t.shape[0], _ptr(t), _ptr(state))
+    if rc != ELBM_OK:
+        raise ElbmError(rc, "elbm_mark_triangles failed")
 
 
 class Context:
@@ -268,6 +289,32 @@ class Context:
         ms = np.zeros(8)
         self._check(self.lib.elbm_autotune(self.h, lvl, reps, ct.byref(chosen), _ptr(ms)))
         return chosen.value, ms
+
+    def alpha_harvest(self, lvl, nsteps, stride, capacity):
+        rec = np.zeros((capacity, MLP_RECORD), np.float32)
+        cnt = ct.c_int64(0)
+        self._check(self.lib.elbm_alpha_harvest(self.h, lvl, nsteps, stride, _ptr(rec), capacity, ct.byref(cnt)))
+        return rec[:cnt.value]
+
+    def alpha_mlp_grad(self, weights, records):
+        w = np.ascontiguousarray(weights, np.float32)
+        r = np.ascontiguousarray(records, np.float32)
+        g = np.zeros(MLP_PARAMS, np.float32)
+        loss = ct.c_double(0)
+        self._check(self.lib.elbm_alpha_mlp_grad(self.h, _ptr(w), _ptr(r), r.shape[0], _ptr(g), ct.byref(loss)))
+        return g, loss.value
+
+    def alpha_mlp_train(self, records, weights, epochs=4, batch=4096, lr=1e-3, seed=0):
+        w = np.ascontiguousarray(weights, np.float32).copy()
+        r = np.ascontiguousarray(records, np.float32)
+        hist = np.zeros(epochs)
+        self._check(self.lib.elbm_alpha_mlp_train(self.h, _ptr(r), r.shape[0], epochs, batch, lr, seed, _ptr(w),
+                                                  _ptr(hist)))
+        return w, hist
+
+    def set_alpha_mlp(self, lvl, weights):
+        w = np.ascontiguousarray(weights, np.float32)
+        self._check(self.lib.elbm_set_alpha_mlp(self.h, lvl, _ptr(w)))
 
     def sync(self):
         self._check(self.lib.elbm_sync(self.h))

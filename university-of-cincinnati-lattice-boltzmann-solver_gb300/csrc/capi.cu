@@ -14,6 +14,9 @@
 #include "../../include/elbm_gb300.h"
 #include "kernels.cuh"
 #include "kernels39.cuh"
+#include "mlp.cuh"
+#include <algorithm>
+#include <random>
 #include "lattice.cuh"
 
 using namespace elbm;
@@ -63,6 +66,7 @@ struct Box {
   DevBuf<uint8_t> ntype;
   DevBuf<int32_t> bidx;
   DevBuf<uint16_t> words;
+  DevBuf<uint8_t> qfrac;  // FP64 or FP32 wall fractions, like the populations
   DevBuf<float> alpha;
   DevBuf<double> staging;  // FP64 packed staging for FP32 conversion
   // D3Q39: g populations, multipliers, previous w, alpha and macroscopic fields
@@ -80,6 +84,7 @@ struct Level {
   elbm_d3q27_params p27{};
   elbm_d3q39_params p39{};
   bool params_set = false;
+  bool mlp_set = false;  // learned-alpha weights uploaded
   int variant = 0;  // FP32 D3Q27 kernel variant picked by elbm_autotune
   DevBuf<uint8_t> eq;  // kEqTables x Q, FP64 or FP32 deviations
 };
@@ -201,7 +206,8 @@ cudaError_t packed_to_fab(const T* dev, T* host, const Box& b, int ngrow, int nc
 // the push rules of looping/timestepping/streaming.f95:365-481).
 // Returns 0 and the link word, or a negative error code.
 int decode_link27(const int32_t* st, int64_t fab_plane, int64_t sidx, const int sstride[3], int x, int y, int z,
-                  const Box& b, const Level& lv, int j, uint16_t& word, bool& interior, std::string& why) {
+                  const Box& b, const Level& lv, int j, uint16_t& word, double& qf, bool& interior, std::string& why) {
+  qf = 0.0;
   const int i = D3Q27::opp[j];  // the link that leaves x along -c_j
   const int32_t code = st[(int64_t)i * fab_plane + sidx];
   interior = false;
@@ -281,6 +287,22 @@ int decode_link27(const int32_t* st, int64_t fab_plane, int64_t sidx, const int 
     word = link_word(LK_KEEP, j, 0);
     return 0;
   }
+  if (code < -1001) {
+    // wall link with the packed fraction of linkwise.f95:56; decoded as in
+    // interpolative_bounceback_bc.f95:66: q = |state + 1001| / 1e9
+    const double q = std::fabs((double)code + 1001.0) / 1e9;
+    qf = q;
+    // the second fluid node of the interpolation, x + c_j (one step away from the wall)
+    const int sx = x + D3Q27::cx[j], sy = y + D3Q27::cy[j], sz = z + D3Q27::cz[j];
+    int off = off_code(0, 0, 0);
+    if (sx >= 0 && sy >= 0 && sz >= 0 && sx < b.nx && sy < b.ny && sz < b.nz) {
+      const int64_t s2 = sidx + (int64_t)D3Q27::cx[j] * sstride[0] + (int64_t)D3Q27::cy[j] * sstride[1] +
+                         (int64_t)D3Q27::cz[j] * sstride[2];
+      if (node_is_fluid(st[s2])) off = off_code(D3Q27::cx[j], D3Q27::cy[j], D3Q27::cz[j]);
+    }
+    word = link_word(LK_IBB, i, off);
+    return 0;
+  }
   why = "unsupported link code " + std::to_string(code);
   return ELBM_E_UNSUPPORTED;
 }
@@ -303,6 +325,7 @@ int finish_stats(elbm_ctx* c, elbm_stats* out) {
   std::memcpy(&mx, &ds.max_dH_bits, sizeof mx);
   out->max_abs_dH = mx;
   out->dh_over_tol = (int64_t)ds.dh_over;
+  out->guess_misses = (int64_t)ds.guess_misses;
   out->kernel_ms = ms;
   return ELBM_OK;
 }
@@ -457,7 +480,8 @@ int elbm_set_d3q27_params(elbm_ctx* c, int lvl, const elbm_d3q27_params* p) {
   if (lv->lattice != ELBM_D3Q27) return fail(c, ELBM_E_ARG, "level %d is not a D3Q27 level", lvl);
   if (!(p->nu > 0.0) || p->max_newton < 1 || p->alpha_mode < 0 || p->alpha_mode > 2)
     return fail(c, ELBM_E_ARG, "bad D3Q27 parameters");
-  if (p->alpha_mode == ELBM_ALPHA_LEARNED) return fail(c, ELBM_E_UNSUPPORTED, "learned alpha needs a trained network");
+  if (p->alpha_mode == ELBM_ALPHA_LEARNED && (!lv->mlp_set || lv->storage != ELBM_STORE_FP32_DEV))
+    return fail(c, ELBM_E_STATE, "learned alpha needs an FP32-storage level and weights (elbm_set_alpha_mlp)");
   lv->p27 = *p;
   lv->params_set = true;
   double tab[kEqTables][Q27];
@@ -494,6 +518,7 @@ int elbm_set_links(elbm_ctx* c, int lvl, int box, const int32_t* state, int ngro
   std::vector<uint8_t> nt(b->N, NT_SKIP);
   std::vector<int32_t> bi;
   std::vector<uint16_t> words;
+  std::vector<double> qfr;
   std::vector<int64_t> bnodes;
   int64_t fluid = 0;
   std::string why;
@@ -505,11 +530,12 @@ int elbm_set_links(elbm_ctx* c, int lvl, int box, const int32_t* state, int ngro
         if (!node_is_fluid(state[s])) continue;
         ++fluid;
         uint16_t w[Q27];
+        double qv[Q27] = {0.0};
         bool all_interior = true;
         w[0] = link_word(LK_PULL, 0, off_code(0, 0, 0));
         for (int j = 1; j < Q27; ++j) {
           bool interior;
-          const int rc = decode_link27(state, fab_plane, s, sstride, x, y, z, *b, *lv, j, w[j], interior, why);
+          const int rc = decode_link27(state, fab_plane, s, sstride, x, y, z, *b, *lv, j, w[j], qv[j], interior, why);
           if (rc) return fail(c, rc, "node (%d,%d,%d) population %d: %s", x + b->lo[0], y + b->lo[1], z + b->lo[2], j,
                               why.c_str());
           all_interior &= interior;
@@ -520,6 +546,7 @@ int elbm_set_links(elbm_ctx* c, int lvl, int box, const int32_t* state, int ngro
           nt[n] = NT_BOUNDARY;
           bnodes.push_back(n);
           words.insert(words.end(), w, w + Q27);
+          qfr.insert(qfr.end(), qv, qv + Q27);
         }
       }
   CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
@@ -532,6 +559,19 @@ int elbm_set_links(elbm_ctx* c, int lvl, int box, const int32_t* state, int ngro
   CUDA_TRY(b->words.alloc(std::max<size_t>(words.size(), 1)), "link words");
   if (!words.empty())
     CUDA_TRY(cudaMemcpy(b->words.p, words.data(), words.size() * sizeof(uint16_t), cudaMemcpyHostToDevice), "words");
+  const size_t qes = elem_size(lv->storage);
+  CUDA_TRY(b->qfrac.alloc(std::max<size_t>(qfr.size(), 1) * qes), "wall fractions");
+  if (!qfr.empty()) {
+    std::vector<uint8_t> qbytes(qfr.size() * qes);
+    for (size_t k = 0; k < qfr.size(); ++k) {
+      if (qes == sizeof(double)) std::memcpy(&qbytes[k * qes], &qfr[k], sizeof(double));
+      else {
+        const float v = (float)qfr[k];
+        std::memcpy(&qbytes[k * qes], &v, sizeof(float));
+      }
+    }
+    CUDA_TRY(cudaMemcpy(b->qfrac.p, qbytes.data(), qbytes.size(), cudaMemcpyHostToDevice), "fractions");
+  }
   b->fluid_nodes = fluid;
   b->boundary_nodes = (int64_t)bnodes.size();
   b->links_set = true;
@@ -625,6 +665,7 @@ int elbm_level_step(elbm_ctx* c, int lvl, int nsteps, elbm_stats* out) {
       a.ntype = b.ntype.p;
       a.bidx = b.bidx.p;
       a.words = b.words.p;
+      a.qfrac = b.qfrac.p;
       a.eq = lv->eq.p;
       a.beta = 1.0 / (2.0 * p.nu / (1.0 / 3.0) + 1.0);
       a.tol_alpha = p.tol_alpha;
@@ -676,6 +717,7 @@ int elbm_autotune(elbm_ctx* c, int lvl, int reps, int* chosen, double* ms_per_va
         a.ntype = b.ntype.p;
         a.bidx = b.bidx.p;
         a.words = b.words.p;
+        a.qfrac = b.qfrac.p;
         a.eq = lv->eq.p;
         a.beta = 1.0 / (2.0 * p.nu / (1.0 / 3.0) + 1.0);
         a.tol_alpha = p.tol_alpha;
@@ -703,6 +745,153 @@ int elbm_autotune(elbm_ctx* c, int lvl, int reps, int* chosen, double* ms_per_va
   lv->variant = best_v;
   if (chosen) *chosen = best_v;
   CUDA_TRY(cudaMemsetAsync(c->stats.p, 0, sizeof(DevStats), c->stream), "stats reset");
+  return ELBM_OK;
+}
+
+int elbm_set_alpha_mlp(elbm_ctx* c, int lvl, const float* weights) {
+  Level* lv = get_level(c, lvl);
+  if (!lv || !weights) return fail(c, ELBM_E_ARG, "unknown level or null weights");
+  for (int k = 0; k < kMlpParams; ++k)
+    if (!std::isfinite(weights[k])) return fail(c, ELBM_E_ARG, "non-finite weight %d", k);
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  upload_alpha_mlp(weights, c->stream);
+  CUDA_TRY(cudaGetLastError(), "weights upload");
+  CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  lv->mlp_set = true;
+  return ELBM_OK;
+}
+
+int elbm_alpha_harvest(elbm_ctx* c, int lvl, int nsteps, int stride, float* records, int64_t capacity,
+                       int64_t* count) {
+  Level* lv = get_level(c, lvl);
+  if (!lv || nsteps < 1 || stride < 1 || !records || capacity < 1 || !count)
+    return fail(c, ELBM_E_ARG, "bad harvest arguments");
+  if (lv->lattice != ELBM_D3Q27 || lv->storage != ELBM_STORE_FP32_DEV || !lv->params_set ||
+      lv->p27.alpha_mode != ELBM_ALPHA_NEWTON)
+    return fail(c, ELBM_E_STATE, "harvesting needs an FP32-storage D3Q27 level with Newton alpha");
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  DevBuf<float> buf;
+  DevBuf<unsigned long long> cnt;
+  CUDA_TRY(buf.alloc((size_t)capacity * kMlpRecord), "harvest buffer");
+  CUDA_TRY(cnt.alloc(1), "harvest counter");
+  CUDA_TRY(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned long long), c->stream), "memset");
+  CUDA_TRY(cudaMemsetAsync(c->stats.p, 0, sizeof(DevStats), c->stream), "stats reset");
+  const elbm_d3q27_params& p = lv->p27;
+  for (int s = 0; s < nsteps; ++s) {
+    for (auto& bp : lv->boxes) {
+      Box& b = *bp;
+      if (!b.links_set || !b.data_set) return fail(c, ELBM_E_STATE, "links or populations missing");
+      Step27Args a{};
+      a.src = b.buf[b.cur].p;
+      a.dst = b.buf[b.cur ^ 1].p;
+      a.plane = b.plane;
+      a.nx = b.nx;
+      a.ny = b.ny;
+      a.nz = b.nz;
+      a.N = b.N;
+      a.ntype = b.ntype.p;
+      a.bidx = b.bidx.p;
+      a.words = b.words.p;
+      a.qfrac = b.qfrac.p;
+      a.eq = lv->eq.p;
+      a.beta = 1.0 / (2.0 * p.nu / (1.0 / 3.0) + 1.0);
+      a.tol_alpha = p.tol_alpha;
+      a.tol_dH = p.tol_dH;
+      a.max_newton = p.max_newton;
+      a.alpha_mode = p.alpha_mode;
+      a.stats = c->stats.p;
+      a.harvest = buf.p;
+      a.harvest_count = cnt.p;
+      a.harvest_cap = capacity;
+      a.harvest_stride = stride;
+      launch_d3q27_fp32(a, c->stream);
+      CUDA_TRY(cudaGetLastError(), "harvest launch");
+      b.cur ^= 1;
+    }
+  }
+  unsigned long long n = 0;
+  CUDA_TRY(cudaMemcpyAsync(&n, cnt.p, sizeof n, cudaMemcpyDeviceToHost, c->stream), "count");
+  CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  const int64_t m = (int64_t)std::min<unsigned long long>(n, (unsigned long long)capacity);
+  CUDA_TRY(cudaMemcpy(records, buf.p, (size_t)m * kMlpRecord * sizeof(float), cudaMemcpyDeviceToHost), "records");
+  *count = m;
+  return ELBM_OK;
+}
+
+int elbm_alpha_mlp_grad(elbm_ctx* c, const float* weights, const float* records, int64_t n, float* grad,
+                        double* loss) {
+  if (!c || !weights || !records || n < 1 || !grad) return fail(c, ELBM_E_ARG, "bad gradient arguments");
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  DevBuf<float> w, rec, scratch, g;
+  DevBuf<double> l;
+  CUDA_TRY(w.alloc(kMlpParams), "w");
+  CUDA_TRY(rec.alloc((size_t)n * kMlpRecord), "records");
+  CUDA_TRY(scratch.alloc((size_t)n * kMlpScratch), "scratch");
+  CUDA_TRY(g.alloc(kMlpParams), "grad");
+  CUDA_TRY(l.alloc(1), "loss");
+  CUDA_TRY(cudaMemcpyAsync(w.p, weights, kMlpParams * sizeof(float), cudaMemcpyHostToDevice, c->stream), "w");
+  CUDA_TRY(cudaMemcpyAsync(rec.p, records, (size_t)n * kMlpRecord * sizeof(float), cudaMemcpyHostToDevice, c->stream),
+           "records");
+  CUDA_TRY(cudaMemsetAsync(g.p, 0, kMlpParams * sizeof(float), c->stream), "memset");
+  CUDA_TRY(cudaMemsetAsync(l.p, 0, sizeof(double), c->stream), "memset");
+  mlp_batch_grad(w.p, rec.p, n, scratch.p, g.p, l.p, c->stream);
+  CUDA_TRY(cudaGetLastError(), "grad launch");
+  CUDA_TRY(cudaMemcpyAsync(grad, g.p, kMlpParams * sizeof(float), cudaMemcpyDeviceToHost, c->stream), "grad");
+  double lh = 0.0;
+  CUDA_TRY(cudaMemcpyAsync(&lh, l.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream), "loss");
+  CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  if (loss) *loss = lh / (double)n;
+  return ELBM_OK;
+}
+
+int elbm_alpha_mlp_train(elbm_ctx* c, const float* records, int64_t n, int epochs, int batch, float lr, uint64_t seed,
+                         float* weights, double* loss_per_epoch) {
+  if (!c || !records || n < 1 || epochs < 1 || batch < 1 || !(lr > 0.f) || !weights)
+    return fail(c, ELBM_E_ARG, "bad training arguments");
+  if ((uint64_t)n > 0xffffffffull) return fail(c, ELBM_E_ARG, "at most 2^32 - 1 records");
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  const int64_t B = std::min<int64_t>(batch, n);
+  DevBuf<float> w, m, v, g, rec, bat, scratch;
+  DevBuf<double> l;
+  DevBuf<uint32_t> perm;
+  CUDA_TRY(w.alloc(kMlpParams), "w");
+  CUDA_TRY(m.alloc(kMlpParams), "m");
+  CUDA_TRY(v.alloc(kMlpParams), "v");
+  CUDA_TRY(g.alloc(kMlpParams), "g");
+  CUDA_TRY(rec.alloc((size_t)n * kMlpRecord), "records");
+  CUDA_TRY(bat.alloc((size_t)B * kMlpRecord), "batch");
+  CUDA_TRY(scratch.alloc((size_t)B * kMlpScratch), "scratch");
+  CUDA_TRY(l.alloc(1), "loss");
+  CUDA_TRY(perm.alloc((size_t)n), "permutation");
+  CUDA_TRY(cudaMemcpyAsync(w.p, weights, kMlpParams * sizeof(float), cudaMemcpyHostToDevice, c->stream), "w");
+  CUDA_TRY(cudaMemcpyAsync(rec.p, records, (size_t)n * kMlpRecord * sizeof(float), cudaMemcpyHostToDevice, c->stream),
+           "records");
+  CUDA_TRY(cudaMemsetAsync(m.p, 0, kMlpParams * sizeof(float), c->stream), "m");
+  CUDA_TRY(cudaMemsetAsync(v.p, 0, kMlpParams * sizeof(float), c->stream), "v");
+  std::mt19937_64 rng(seed);
+  std::vector<uint32_t> hp((size_t)n);
+  int t = 0;
+  for (int e = 0; e < epochs; ++e) {
+    for (int64_t k = 0; k < n; ++k) hp[k] = (uint32_t)k;
+    std::shuffle(hp.begin(), hp.end(), rng);
+    CUDA_TRY(cudaMemcpyAsync(perm.p, hp.data(), (size_t)n * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream),
+             "perm");
+    CUDA_TRY(cudaMemsetAsync(l.p, 0, sizeof(double), c->stream), "memset");
+    int64_t seen = 0;
+    for (int64_t off = 0; off + B <= n; off += B) {
+      mlp_gather_batch(rec.p, perm.p, off, B, bat.p, c->stream);
+      CUDA_TRY(cudaMemsetAsync(g.p, 0, kMlpParams * sizeof(float), c->stream), "memset");
+      mlp_batch_grad(w.p, bat.p, B, scratch.p, g.p, l.p, c->stream);
+      mlp_adam(w.p, g.p, m.p, v.p, lr, ++t, c->stream);
+      CUDA_TRY(cudaGetLastError(), "train launch");
+      seen += B;
+    }
+    double lh = 0.0;
+    CUDA_TRY(cudaMemcpyAsync(&lh, l.p, sizeof(double), cudaMemcpyDeviceToHost, c->stream), "loss");
+    CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+    if (loss_per_epoch) loss_per_epoch[e] = seen ? lh / (double)seen : 0.0;
+  }
+  CUDA_TRY(cudaMemcpy(weights, w.p, kMlpParams * sizeof(float), cudaMemcpyDeviceToHost), "weights");
   return ELBM_OK;
 }
 

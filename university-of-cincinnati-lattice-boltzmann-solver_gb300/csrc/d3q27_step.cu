@@ -20,8 +20,18 @@
 
 #include "kernels.cuh"
 #include "lattice.cuh"
+#include "mlp.cuh"
 
 namespace elbm {
+
+// Learned-alpha network weights for inference: every thread reads the same
+// weight at the same time, so constant memory feeds them to the FMAs directly.
+__constant__ float c_mlp[kMlpParams];
+
+void upload_alpha_mlp(const float* w_host, cudaStream_t s) {
+  cudaMemcpyToSymbolAsync(c_mlp, w_host, sizeof(float) * kMlpParams, 0, cudaMemcpyHostToDevice, s);
+}
+
 namespace {
 
 constexpr int Q = Q27;
@@ -59,6 +69,22 @@ __device__ __forceinline__ void gather(const Step27Args& a, const T* __restrict_
         f[j] = load_src(src, a.plane, lw_pop(w), s);
       } else if (kind == LK_EQ) {
         f[j] = eq[lw_pop(w) * Q + j];
+      } else if (kind == LK_IBB) {
+        // linear interpolated bounce-back (Bouzidi, Firdaouss, Lallemand 2001) in pull form:
+        // q < 1/2: f_j = 2q f*_i(x) + (1 - 2q) f*_i(x + c_j); q >= 1/2: f_j = f*_i(x)/(2q) + (1 - 1/(2q)) f*_j(x)
+        // (the same combination holds for deviations: w_i = w_j)
+        const int i = lw_pop(w), off = lw_off(w);
+        const T q = __ldg(static_cast<const T*>(a.qfrac) + (int64_t)b * Q + j);
+        const T fi = load_src(src, a.plane, i, n);
+        if (q < (T)0.5 && off != 13) {
+          const int64_t s2 = n + (int64_t)(off % 3 - 1) + (int64_t)((off / 3) % 3 - 1) * a.nx +
+                             (int64_t)(off / 9 - 1) * nxy;
+          f[j] = (T)2 * q * fi + ((T)1 - (T)2 * q) * load_src(src, a.plane, i, s2);
+        } else if (q >= (T)0.5) {
+          f[j] = fi / ((T)2 * q) + ((T)1 - (T)1 / ((T)2 * q)) * load_src(src, a.plane, j, n);
+        } else {
+          f[j] = fi;
+        }
       } else {
         f[j] = load_src(src, a.plane, j, n);
       }
@@ -278,13 +304,27 @@ struct AlphaOut {
 
 // Series of 2 atanh: with s = x/(2+x), ln(1+x) = 2 s A(s^2),
 // A(z) = 1 + z/3 + z^2/5 + ..., and B(z) = (A(z) - 1)/z = 1/3 + z/5 + ...;
-// eight terms reach FP32 rounding for |s| <= 1/3 (-1/2 <= x <= 1).
+// eight terms reach FP32 rounding for |s| <= 1/3 (-1/2 <= x <= 1), 24 terms
+// for |s| <= 0.6 (x >= -0.75); s^2 <= 0.36 beyond that is not reached by the
+// populations of a node inside its positivity bracket at alpha near 2.
 __device__ __forceinline__ void atanh_series(float s2, float& A, float& B) {
-  float a = 1.0f / 17.0f, b = 1.0f / 19.0f;
+  float a, b;
+  if (s2 <= 1.0f / 9.0f) {
+    a = 1.0f / 17.0f;
+    b = 1.0f / 19.0f;
 #pragma unroll
-  for (int k = 7; k >= 0; --k) {
-    a = fmaf(a, s2, 1.0f / (2 * k + 1));
-    b = fmaf(b, s2, 1.0f / (2 * k + 3));
+    for (int k = 7; k >= 0; --k) {
+      a = fmaf(a, s2, 1.0f / (2 * k + 1));
+      b = fmaf(b, s2, 1.0f / (2 * k + 3));
+    }
+  } else {
+    a = 1.0f / 49.0f;
+    b = 1.0f / 51.0f;
+#pragma unroll 4
+    for (int k = 23; k >= 0; --k) {
+      a = fmaf(a, s2, 1.0f / (2 * k + 1));
+      b = fmaf(b, s2, 1.0f / (2 * k + 3));
+    }
   }
   A = a;
   B = b;
@@ -328,6 +368,36 @@ __device__ __forceinline__ void large_terms(const LargePop* lp, int nl, float al
   }
 }
 
+// Forward pass of the 27-64-64-1 GELU network (weights in c_mlp).
+__device__ __forceinline__ float fast_tanh(float u) {
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
+  return t;
+}
+__device__ __forceinline__ float gelu_fast(float z) {
+  return 0.5f * z * (1.0f + fast_tanh(0.7978845608028654f * fmaf(0.044715f * z * z, z, z)));
+}
+__device__ float mlp_forward(const float (&x)[Q]) {
+  constexpr int NH = kMlpHidden, OB1 = Q * NH, OW2 = OB1 + NH, OB2 = OW2 + NH * NH, OW3 = OB2 + NH, OB3 = OW3 + NH;
+  float h1[NH];
+#pragma unroll
+  for (int j = 0; j < NH; ++j) {
+    float z = c_mlp[OB1 + j];
+#pragma unroll
+    for (int i = 0; i < Q; ++i) z = fmaf(x[i], c_mlp[i * NH + j], z);
+    h1[j] = gelu_fast(z);
+  }
+  float out = c_mlp[OB3];
+#pragma unroll 4
+  for (int k = 0; k < NH; ++k) {
+    float z = c_mlp[OB2 + k];
+#pragma unroll
+    for (int j = 0; j < NH; ++j) z = fmaf(h1[j], c_mlp[OW2 + j * NH + k], z);
+    out = fmaf(gelu_fast(z), c_mlp[OW3 + k], out);
+  }
+  return out;
+}
+
 // g(2 + delta) and g'(2 + delta) of the truncated power series (see above).
 template <int K>
 __device__ __forceinline__ void series_g(const float (&S)[K + 1], float delta, float& g, float& gp) {
@@ -352,7 +422,8 @@ __device__ __forceinline__ void series_g(const float (&S)[K + 1], float delta, f
 // exact psi polish it.
 template <int K>
 __device__ AlphaOut alpha_solve32(const float2 (&D2)[14], const float2 (&y2)[14], const float (&d)[Q],
-                                  unsigned large, float amax, int max_it) {
+                                  unsigned large, float amax, int max_it, float delta_start = 0.f,
+                                  int series_it = -1) {
   float2 S2[K + 1];
 #pragma unroll
   for (int k = 0; k <= K; ++k) S2[k] = make_float2(0.f, 0.f);
@@ -405,9 +476,10 @@ __device__ AlphaOut alpha_solve32(const float2 (&D2)[14], const float2 (&y2)[14]
     }
   }
   if (nl == 0 && !(S[2] > 1e-30f)) return r;  // at equilibrium: alpha = 2
-  float delta = 0.f;
+  float delta = delta_start;
   bool ok = false;
-  for (int it = 0; it < max_it; ++it) {
+  const int n_series = (series_it > 0) ? series_it : max_it;
+  for (int it = 0; it < n_series; ++it) {
     float g, gp;
     series_g<K>(SL, delta, g, gp);
     r.iters = it + 1;
@@ -453,7 +525,9 @@ __device__ AlphaOut alpha_solve32(const float2 (&D2)[14], const float2 (&y2)[14]
 
 // MINB: minimum resident blocks per SM requested from the register allocator
 // (0: none).  Both variants are built; the level's autotuner picks one.
-template <bool CHECK, int MINB>
+// MODE 0: Newton from alpha = 2; 1: learned guess + at most two Newton steps,
+// Newton from 2 as the fallback; 2: Newton and harvesting of training records.
+template <bool CHECK, int MINB, int MODE = 0>
 __global__ void __launch_bounds__(128, MINB) d3q27_fp32_kernel(const Step27Args a) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= a.N) return;
@@ -516,6 +590,7 @@ __global__ void __launch_bounds__(128, MINB) d3q27_fp32_kernel(const Step27Args 
 
   AlphaOut al{0.f, 0u, false, false};
   double dH = 0.0;
+  bool guess_miss = false;
   if (a.alpha_mode != 0) {
     float2 y2[14];
     float ysmall = 0.f, ymin = 0.f;
@@ -537,10 +612,51 @@ __global__ void __launch_bounds__(128, MINB) d3q27_fp32_kernel(const Step27Args 
     const float amax = (ymin < 0.f) ? -1.0f / ymin : INFINITY;
     // warp-uniform series order from the warp's largest small |y|
     const float wmax = __int_as_float(__reduce_max_sync(__activemask(), __float_as_int(ysmall)));
-    if (wmax <= 0.02f) al = alpha_solve32<6>(D2, y2, d, large, amax, a.max_newton);
-    else if (wmax <= 0.04f) al = alpha_solve32<8>(D2, y2, d, large, amax, a.max_newton);
-    else if (wmax <= 0.06f) al = alpha_solve32<10>(D2, y2, d, large, amax, a.max_newton);
-    else al = alpha_solve32<12>(D2, y2, d, large, amax, a.max_newton);
+    const int korder = (wmax <= 0.02f) ? 6 : (wmax <= 0.04f) ? 8 : (wmax <= 0.06f) ? 10 : 12;
+    float delta0 = 0.f, lam = 0.f;
+    int series_it = -1;
+    if (MODE >= 1) {
+#pragma unroll
+      for (int q = 0; q < 14; ++q) lam = fmaxf(lam, fmaxf(fabsf(y2[q].x), fabsf(y2[q].y)));
+    }
+    if (MODE == 1 && lam > 0.f) {
+      // learned guess: alpha = 2 + lambda * net(y / lambda), then at most two Newton steps
+      float x[Q];
+      const float il = 1.0f / lam;
+#pragma unroll
+      for (int i = 0; i < Q; ++i) x[i] = ((i & 1) ? y2[i >> 1].y : y2[i >> 1].x) * il;
+      delta0 = lam * mlp_forward(x);
+      series_it = 2;
+    }
+    switch (korder) {
+      case 6: al = alpha_solve32<6>(D2, y2, d, large, amax, a.max_newton, delta0, series_it); break;
+      case 8: al = alpha_solve32<8>(D2, y2, d, large, amax, a.max_newton, delta0, series_it); break;
+      case 10: al = alpha_solve32<10>(D2, y2, d, large, amax, a.max_newton, delta0, series_it); break;
+      default: al = alpha_solve32<12>(D2, y2, d, large, amax, a.max_newton, delta0, series_it); break;
+    }
+    if (MODE == 1 && al.fallback) {
+      // the guess did not converge in two steps: plain Newton from alpha = 2
+      guess_miss = true;
+      const unsigned it0 = al.iters;
+      switch (korder) {
+        case 6: al = alpha_solve32<6>(D2, y2, d, large, amax, a.max_newton); break;
+        case 8: al = alpha_solve32<8>(D2, y2, d, large, amax, a.max_newton); break;
+        case 10: al = alpha_solve32<10>(D2, y2, d, large, amax, a.max_newton); break;
+        default: al = alpha_solve32<12>(D2, y2, d, large, amax, a.max_newton); break;
+      }
+      al.iters += it0;
+    }
+    if (MODE == 2 && !al.fallback && lam > 0.f && (n % a.harvest_stride) == 0) {
+      const unsigned long long slot = atomicAdd(a.harvest_count, 1ull);
+      if ((long long)slot < a.harvest_cap) {
+        float* r = a.harvest + slot * kMlpRecord;
+        const float il = 1.0f / lam;
+#pragma unroll
+        for (int i = 0; i < Q; ++i) r[i] = ((i & 1) ? y2[i >> 1].y : y2[i >> 1].x) * il;
+        r[Q] = lam;
+        r[Q + 1] = al.delta * il;
+      }
+    }
     if (CHECK) {
       // |H(f + alpha Delta) - H(f)| in FP64 (conservation-consistent form) from the FP32 populations
       const double al64 = 2.0 + (double)al.delta;
@@ -569,6 +685,11 @@ __global__ void __launch_bounds__(128, MINB) d3q27_fp32_kernel(const Step27Args 
   store_dst(dst, a.plane, n, d);
   if (a.alpha_out) a.alpha_out[n] = 2.0f + al.delta;
   warp_stats(a.stats, true, al.iters, al.large, al.fallback, flags, dH);
+  if (MODE == 1) {
+    const unsigned mk = __activemask();
+    const unsigned nm = __popc(__ballot_sync(mk, guess_miss));
+    if (nm && (int)(threadIdx.x & 31) == __ffs(mk) - 1) atomicAdd(&a.stats->guess_misses, (unsigned long long)nm);
+  }
 }
 
 }  // namespace
@@ -582,9 +703,19 @@ void launch_d3q27_fp64(const Step27Args& a, cudaStream_t s) {
 void launch_d3q27_fp32(const Step27Args& a, cudaStream_t s) {
   const int threads = 128;
   const int64_t blocks = (a.N + threads - 1) / threads;
-  if (a.check_dH) d3q27_fp32_kernel<true, 0><<<(unsigned)blocks, threads, 0, s>>>(a);
-  else if (a.variant == 1) d3q27_fp32_kernel<false, 4><<<(unsigned)blocks, threads, 0, s>>>(a);
-  else d3q27_fp32_kernel<false, 0><<<(unsigned)blocks, threads, 0, s>>>(a);
+  if (a.check_dH) {
+    if (a.alpha_mode == 2) d3q27_fp32_kernel<true, 0, 1><<<(unsigned)blocks, threads, 0, s>>>(a);
+    else d3q27_fp32_kernel<true, 0, 0><<<(unsigned)blocks, threads, 0, s>>>(a);
+  } else if (a.harvest) {
+    d3q27_fp32_kernel<false, 0, 2><<<(unsigned)blocks, threads, 0, s>>>(a);
+  } else if (a.alpha_mode == 2) {
+    if (a.variant == 1) d3q27_fp32_kernel<false, 4, 1><<<(unsigned)blocks, threads, 0, s>>>(a);
+    else d3q27_fp32_kernel<false, 0, 1><<<(unsigned)blocks, threads, 0, s>>>(a);
+  } else if (a.variant == 1) {
+    d3q27_fp32_kernel<false, 4, 0><<<(unsigned)blocks, threads, 0, s>>>(a);
+  } else {
+    d3q27_fp32_kernel<false, 0, 0><<<(unsigned)blocks, threads, 0, s>>>(a);
+  }
 }
 
 }  // namespace elbm

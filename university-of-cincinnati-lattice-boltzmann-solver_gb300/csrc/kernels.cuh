@@ -15,6 +15,7 @@ struct DevStats {
   unsigned long long fallbacks;
   unsigned long long max_dH_bits;  // bit pattern of a non-negative double (monotone in value)
   unsigned long long dh_over;      // check mode: nodes with |dH| above the tolerance
+  unsigned long long guess_misses; // learned alpha: guesses that needed the Newton fallback
   unsigned int status;
   unsigned int pad;
 };
@@ -29,6 +30,7 @@ struct Step27Args {
   const uint8_t* ntype;   // NodeType per node
   const int32_t* bidx;    // boundary record per boundary node
   const uint16_t* words;  // Q link words per boundary record
+  const void* qfrac;      // Q wall fractions per boundary record (LK_IBB links), FP64 or FP32 like the populations
   const void* eq;         // kEqTables x Q equilibria (FP64: f; FP32: deviations)
   double beta;
   double tol_alpha;
@@ -38,13 +40,19 @@ struct Step27Args {
   int check_dH;
   float* alpha_out;       // optional per-node alpha (FP32)
   DevStats* stats;
-  const void* mlp;        // learned-alpha weights (ELBM_ALPHA_LEARNED)
+  const float* mlp;       // learned-alpha weights, FP32 (ELBM_ALPHA_LEARNED)
   int variant;            // kernel variant chosen by the autotuner
+  // harvesting of (populations, alpha) records for training (nullptr: off)
+  float* harvest;
+  unsigned long long* harvest_count;
+  long long harvest_cap;
+  int harvest_stride;
 };
 
 constexpr int kFp32Variants = 2;
 
 void launch_d3q27_fp64(const Step27Args& a, cudaStream_t s);
+void upload_alpha_mlp(const float* w_host, cudaStream_t s);
 void launch_d3q27_fp32(const Step27Args& a, cudaStream_t s);
 
 }  // namespace elbm

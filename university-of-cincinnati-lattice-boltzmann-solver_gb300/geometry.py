@@ -96,7 +96,58 @@ def d3q27_boundary_params(u_in, nu: float, outlet_type: int = 1, tol_alpha: floa
     }
 
 
+def icosphere(subdivisions: int, radius: float, center) -> np.ndarray:
+    """Triangles (ntri, 3, 3) of an icosphere: the icosahedron with every
+    triangle split in four `subdivisions` times and the vertices projected on
+    the sphere (20 * 4**subdivisions triangles; 5120 for 4), outward normals."""
+    phi = (1.0 + 5.0 ** 0.5) / 2.0
+    v = [(-1, phi, 0), (1, phi, 0), (-1, -phi, 0), (1, -phi, 0), (0, -1, phi), (0, 1, phi), (0, -1, -phi),
+         (0, 1, -phi), (phi, 0, -1), (phi, 0, 1), (-phi, 0, -1), (-phi, 0, 1)]
+    verts = [np.array(x, np.float64) / np.linalg.norm(x) for x in v]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+             (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11),
+             (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    cache = {}
+
+    def mid(a, b):
+        key = (min(a, b), max(a, b))
+        if key not in cache:
+            m = verts[a] + verts[b]
+            verts.append(m / np.linalg.norm(m))
+            cache[key] = len(verts) - 1
+        return cache[key]
+
+    for _ in range(subdivisions):
+        nf = []
+        for a, b, c in faces:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        faces = nf
+    V = np.array(verts) * radius + np.asarray(center, np.float64)
+    return np.ascontiguousarray(V[np.array(faces)])
+
+
+def sphere_faces() -> dict:
+    """Flow past a sphere: inlet 1 at x=0, outlet 1 at x=nx-1, freestream on the other faces."""
+    return {"x-": inlet_code(1), "x+": outlet_code(1), "y-": CODE_FREESTREAM, "y+": CODE_FREESTREAM,
+            "z-": CODE_FREESTREAM, "z+": CODE_FREESTREAM}
+
+
+def sphere_state27(nx: int, ny: int, nz: int, radius: float, center, subdivisions: int = 4) -> np.ndarray:
+    """state array of a box with sphere_faces() and an icosphere whose wall links
+    carry packed fractions (elbm_mark_triangles, the library's set-up code)."""
+    from .capi import mark_triangles
+
+    st = box_state27(nx, ny, nz, sphere_faces())
+    tri = icosphere(subdivisions, radius, center)
+    mark_triangles(st, (0.0, 0.0, 0.0), 1.0, tri)
+    return st
+
+
 __all__ = [
+    "icosphere",
+    "sphere_faces",
+    "sphere_state27",
     "box_state27",
     "flat_plate_faces",
     "perturbed_equilibrium",
