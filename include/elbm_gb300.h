@@ -47,6 +47,7 @@ typedef struct elbm_ctx elbm_ctx;
 #define ELBM_ST_NEWTON_FALLBACK 0x2u /* some alpha solve fell back (count in .fallbacks) */
 #define ELBM_ST_NEG_POP 0x4u         /* a post-collision population was negative */
 #define ELBM_ST_DH_TOL 0x8u          /* check mode: some |dH| exceeded the tolerance */
+#define ELBM_ST_COPY_TIMEOUT 0x10u   /* staged kernel: a bulk copy did not arrive in time; the step is invalid */
 
 /* lattices */
 #define ELBM_D3Q27 27
@@ -186,6 +187,13 @@ int elbm_level_step(elbm_ctx* ctx, int lvl, int nsteps, elbm_stats* stats);
  * reference has no counterpart (it has one code path per lattice). */
 int elbm_autotune(elbm_ctx* ctx, int lvl, int reps, int* chosen, double* ms_per_variant);
 
+/* Use kernel variant v (0: direct loads; 1: direct, register-capped for
+ * occupancy; 2: rows staged in shared memory by bulk copies, persistent) for
+ * the level's FP32 D3Q27 steps, instead of the autotuner's choice.  Variant 2
+ * applies to boxes with nx and the plane size multiples of 4 and ny, nz >= 3;
+ * other boxes fall back to variant 0.  No counterpart in the reference. */
+int elbm_set_kernel_variant(elbm_ctx* ctx, int lvl, int variant);
+
 /* Learned initial guess of alpha (no counterpart in the reference; its
  * Future Work.txt:34 proposes machine learning to shorten the solves): a
  * 27-64-64-1 GELU network maps y/lambda (y_i = Delta_i/f_i, lambda = max|y_i|)
@@ -201,6 +209,12 @@ int elbm_alpha_harvest(elbm_ctx* ctx, int lvl, int nsteps, int stride, float* re
 /* Mean-squared-error loss and its gradient for one batch (the training kernels). */
 int elbm_alpha_mlp_grad(elbm_ctx* ctx, const float* weights, const float* records, int64_t n, float* grad,
                         double* loss);
+/* Network outputs for n feature rows (27 floats each: y/lambda) by the
+ * tensor-core inference the learned-alpha step uses (BF16 operands, FP32
+ * accumulation, 128 rows per tile).  status (may be NULL) receives
+ * ELBM_ST_COPY_TIMEOUT if a tile's matrix multiply did not complete. */
+int elbm_alpha_mlp_infer(elbm_ctx* ctx, const float* weights, const float* x, int64_t n, float* out,
+                         uint32_t* status);
 /* Adam training on the GPU; weights in/out; loss_per_epoch may be NULL. */
 int elbm_alpha_mlp_train(elbm_ctx* ctx, const float* records, int64_t n, int epochs, int batch, float lr,
                          uint64_t seed, float* weights, double* loss_per_epoch);

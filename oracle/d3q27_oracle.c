@@ -415,6 +415,9 @@ static int o_ray_x(const double* v, const double* p) {
   return xs > p[0];
 }
 
+#define RAY_DY 7.548776662466927e-7
+#define RAY_DZ 5.698402909980532e-7
+
 int o27_mark_triangles(int nx, int ny, int nz, const double* origin, double dx, int ntri, const double* tri,
                        int32_t* state) {
   const int64_t N = (int64_t)nx * ny * nz;
@@ -423,7 +426,9 @@ int o27_mark_triangles(int nx, int ny, int nz, const double* origin, double dx, 
 #pragma omp parallel for schedule(dynamic)
   for (int64_t n = 0; n < N; ++n) {
     const int i = (int)(n % nx), j = (int)((n / nx) % ny), k = (int)(n / ((int64_t)nx * ny));
-    const double p[3] = {origin[0] + i * dx, origin[1] + j * dx, origin[2] + k * dx};
+    /* the ray starts a tiny irrational offset off the lattice line, so that it
+     * passes through no vertex or edge of a surface built on lattice points */
+    const double p[3] = {origin[0] + i * dx, origin[1] + (j + RAY_DY) * dx, origin[2] + (k + RAY_DZ) * dx};
     int cross = 0;
     for (int t = 0; t < ntri; ++t) cross += o_ray_x(tri + 9 * t, p);
     solid[n] = (char)(cross & 1);
@@ -437,19 +442,18 @@ int o27_mark_triangles(int nx, int ny, int nz, const double* origin, double dx, 
     const int i = (int)(n % nx), j = (int)((n / nx) % ny), k = (int)(n / ((int64_t)nx * ny));
     const double p0[3] = {origin[0] + i * dx, origin[1] + j * dx, origin[2] + k * dx};
     for (int q = 1; q < Q; ++q) {
+      /* only links from a fluid node to a solid node are wall links
+       * (inter_bb_setup.f95:36-40: same-type neighbours skip the crossing search) */
+      const int it = i + CX[q], jt = j + CY[q], kt = k + CZ[q];
+      if (!(it >= 0 && jt >= 0 && kt >= 0 && it < nx && jt < ny && kt < nz && solid[idx(it, jt, kt, nx, ny)]))
+        continue;
       const double p1[3] = {p0[0] + CX[q] * dx, p0[1] + CY[q] * dx, p0[2] + CZ[q] * dx};
       double tbest = INFINITY;
       for (int t = 0; t < ntri; ++t) {
         const double tt = o_seg_tri(tri + 9 * t, p0, p1);
         if (tt > 0.0 && tt < tbest) tbest = tt;
       }
-      if (tbest == INFINITY) {
-        const int it = i + CX[q], jt = j + CY[q], kt = k + CZ[q];
-        if (it >= 0 && jt >= 0 && kt >= 0 && it < nx && jt < ny && kt < nz && solid[idx(it, jt, kt, nx, ny)])
-          tbest = 1.0;
-        else
-          continue;
-      }
+      if (tbest == INFINITY) tbest = 1.0; /* the link ends in a solid node without a recorded crossing */
       const double len = sqrt((double)(CX[q] * CX[q] + CY[q] * CY[q] + CZ[q] * CZ[q])) * dx;
       const double dist = tbest * len;
       state[(int64_t)q * N + n] = -1001 - (int32_t)floor(dist / len * 1e9);

@@ -17,7 +17,7 @@ def test_icosphere_counts(pkg):
 
 
 @pytest.mark.parametrize("sub,radius,center", [(2, 5.3, (14.3, 12.1, 11.7)), (3, 6.0, (16.0, 12.0, 12.0)),
-                                               (4, 7.5, (15.5, 11.25, 12.0))])
+                                               (4, 7.5, (15.5, 11.25, 12.0)), (3, 6.0, (12.0, 12.0, 12.0))])
 def test_marking_matches_bruteforce(pkg, orc, built_lib, sub, radius, center):
     geo = pkg.geometry
     tri = geo.icosphere(sub, radius, center)
@@ -29,6 +29,17 @@ def test_marking_matches_bruteforce(pkg, orc, built_lib, sub, radius, center):
     solid = a[0] == -1001
     # the marked solid volume approximates the sphere's
     assert abs(solid.sum() - 4 / 3 * np.pi * radius ** 3) < 0.12 * 4 / 3 * np.pi * radius ** 3
+    # no solid node outside the sphere (rays through the icosphere's vertices on
+    # lattice lines must not flip the inside test)
+    zs, ys, xs = np.nonzero(solid)
+    assert np.sqrt((xs - center[0]) ** 2 + (ys - center[1]) ** 2 + (zs - center[2]) ** 2).max() <= radius + 1e-9
+    # wall links join fluid nodes to solid nodes only
+    zf, yf, xf = np.nonzero(~solid)
+    for i in range(1, 27):
+        wl = a[i][~solid] < -1001
+        xt, yt, zt = xf + pkg.lattice.CX[i], yf + pkg.lattice.CY[i], zf + pkg.lattice.CZ[i]
+        inside = (xt >= 0) & (xt < 32) & (yt >= 0) & (yt < 24) & (zt >= 0) & (zt < 24)
+        assert not (wl & inside & ~solid[np.clip(zt, 0, 23), np.clip(yt, 0, 23), np.clip(xt, 0, 31)]).any()
     q = np.abs(a[a < -1001].astype(np.float64) + 1001) / 1e9
     assert q.size > 0 and q.min() > 0 and q.max() <= 1.0
     # every wall link of a fluid node points at a solid node or across the surface

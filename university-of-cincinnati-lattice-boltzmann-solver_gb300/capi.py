@@ -113,8 +113,10 @@ SIGNATURES = {
     "elbm_download_level39": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
     "elbm_upload_level_noalloc": (_c_int, [_vp, _c_int, _c_int, _vp]),
     "elbm_autotune": (_c_int, [_vp, _c_int, _c_int, _vp, _vp]),
+    "elbm_set_kernel_variant": (_c_int, [_vp, _c_int, _c_int]),
     "elbm_mark_triangles": (_c_int, [_c_int, _c_int, _c_int, _vp, _c_double, _c_int, _vp, _vp]),
     "elbm_alpha_harvest": (_c_int, [_vp, _c_int, _c_int, _c_int, _vp, ct.c_int64, _vp]),
+    "elbm_alpha_mlp_infer": (_c_int, [_vp, _vp, _vp, ct.c_int64, _vp, _vp]),
     "elbm_alpha_mlp_grad": (_c_int, [_vp, _vp, _vp, ct.c_int64, _vp, _vp]),
     "elbm_alpha_mlp_train": (_c_int, [_vp, _vp, ct.c_int64, _c_int, _c_int, ct.c_float, ct.c_uint64, _vp, _vp]),
     "elbm_set_alpha_mlp": (_c_int, [_vp, _c_int, _vp]),
@@ -290,11 +292,23 @@ class Context:
         self._check(self.lib.elbm_autotune(self.h, lvl, reps, ct.byref(chosen), _ptr(ms)))
         return chosen.value, ms
 
+    def set_kernel_variant(self, lvl, variant):
+        self._check(self.lib.elbm_set_kernel_variant(self.h, lvl, variant))
+
     def alpha_harvest(self, lvl, nsteps, stride, capacity):
         rec = np.zeros((capacity, MLP_RECORD), np.float32)
         cnt = ct.c_int64(0)
         self._check(self.lib.elbm_alpha_harvest(self.h, lvl, nsteps, stride, _ptr(rec), capacity, ct.byref(cnt)))
         return rec[:cnt.value]
+
+    def alpha_mlp_infer(self, weights, x):
+        """Tensor-core network outputs for feature rows x (n, 27); returns (out, status)."""
+        w = np.ascontiguousarray(weights, np.float32)
+        xs = np.ascontiguousarray(x, np.float32)
+        out = np.zeros(xs.shape[0], np.float32)
+        st = ct.c_uint32(0)
+        self._check(self.lib.elbm_alpha_mlp_infer(self.h, _ptr(w), _ptr(xs), xs.shape[0], _ptr(out), ct.byref(st)))
+        return out, st.value
 
     def alpha_mlp_grad(self, weights, records):
         w = np.ascontiguousarray(weights, np.float32)

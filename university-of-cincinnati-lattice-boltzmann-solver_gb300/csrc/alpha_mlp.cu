@@ -16,6 +16,7 @@
 #include <cstdint>
 
 #include "mlp.cuh"
+#include "mlp_tc.cuh"
 
 namespace elbm {
 namespace {
@@ -160,7 +161,30 @@ __global__ void gather_batch_kernel(const float* __restrict__ rec, const uint32_
   out[e] = rec[(int64_t)perm[off + s] * kMlpRecord + c];
 }
 
+// Tensor-core inference over n feature rows (27 floats each), 128 rows per tile.
+__global__ void __launch_bounds__(128) mlp_tc_infer_kernel(const float* __restrict__ w, const float* __restrict__ x,
+                                                           int64_t n, float* __restrict__ out, unsigned* status) {
+  extern __shared__ __align__(128) unsigned char smraw[];
+  MlpTcSmem& s = *reinterpret_cast<MlpTcSmem*>(smraw);
+  mlp_tc_setup(s, w);
+  for (int64_t t0 = (int64_t)blockIdx.x * kTcRows; t0 < n; t0 += (int64_t)gridDim.x * kTcRows) {
+    const int64_t i = t0 + threadIdx.x;
+    float xv[kMlpIn];
+#pragma unroll
+    for (int k = 0; k < kMlpIn; ++k) xv[k] = (i < n) ? x[i * kMlpIn + k] : 0.f;
+    const float o = mlp_tc_tile(s, xv, status);
+    if (i < n) out[i] = o;
+  }
+  mlp_tc_teardown(s);
+}
+
 }  // namespace
+
+void mlp_tc_infer(const float* w, const float* x, int64_t n, float* out, unsigned* status, cudaStream_t s) {
+  const int64_t tiles = (n + kTcRows - 1) / kTcRows;
+  const unsigned grid = (unsigned)(tiles < 152 * 4 ? tiles : 152 * 4);
+  mlp_tc_infer_kernel<<<grid, kTcRows, sizeof(MlpTcSmem), s>>>(w, x, n, out, status);
+}
 
 void mlp_batch_grad(const float* w, const float* rec, int64_t n, float* scratch, float* grad, double* loss,
                     cudaStream_t s) {

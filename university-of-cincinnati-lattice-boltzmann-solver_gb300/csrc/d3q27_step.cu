@@ -15,11 +15,14 @@
 // becomes a read of a word-described source in the previous step's buffer.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 
+#include "../../include/elbm_gb300.h"
 #include "kernels.cuh"
 #include "lattice.cuh"
+#include "dfloat.cuh"
 #include "mlp.cuh"
 
 namespace elbm {
@@ -296,9 +299,10 @@ __host__ __device__ constexpr double b_n(int n) { return -((n & 1) ? -1.0 : 1.0)
 __host__ __device__ constexpr double c0_n(int n) { return a_n(n) * pow2i(n - 1) + b_n(n); }
 
 struct AlphaOut {
-  float delta;  // alpha = 2 + delta
+  float delta;     // alpha = 2 + delta + delta_lo
+  float delta_lo;  // low part, non-zero after a float-pair solve
   unsigned iters;
-  bool large;   // some population took the FP64 route
+  bool large;      // some population took the individual (non-series) route
   bool fallback;
 };
 
@@ -338,7 +342,7 @@ __device__ __forceinline__ void atanh_series(float s2, float& A, float& B) {
 // (the O(y^2) parts of phi(x) = x^2/(2+x) + 2(1+x) s_x^3 B and of
 // alpha y ln(1+y) = 2 alpha y s_y (1 + s_y^2 B) are combined exactly).
 // dlog = ln(1 + alpha y) - ln(1 + y), for the derivative.
-__device__ __forceinline__ void psi_large(float y, float alpha, float delta, float& psi, float& dlog) {
+__device__ __forceinline__ void psi_large(float y, float alpha, float delta, float& psi, float& dlog, float& mag) {
   const float x = alpha * y;
   const float sx = __fdividef(x, 2.0f + x), sy = __fdividef(y, 2.0f + y);
   float Ax, Bx, Ay, By;
@@ -348,23 +352,45 @@ __device__ __forceinline__ void psi_large(float y, float alpha, float delta, flo
   const float t2 = 2.0f * (1.0f + x) * sx * sx * sx * Bx;
   const float t3 = 2.0f * alpha * y * sy * sy * sy * By;
   psi = t1 + t2 - t3;
+  mag = fabsf(t1) + fabsf(t2) + fabsf(t3);
   dlog = 2.0f * fmaf(sx, Ax, -sy * Ay);
 }
 
 // FP32 sum over the flagged populations (|y| > kYSmall):
-// G_L(alpha) = sum f psi(y, alpha), G_L'(alpha) = sum f y [ln(1 + alpha y) - ln(1 + y)].
+// G_L(alpha) = sum f psi(y, alpha), G_L'(alpha) = sum f y [ln(1 + alpha y) - ln(1 + y)],
+// and GLabs = sum f (|t1| + |t2| + |t3|), the scale of the rounding error of G_L.
 struct LargePop {
-  float f, y;
+  float f, y, ylo;  // y + ylo = Delta / f to float-pair accuracy
 };
 __device__ __forceinline__ void large_terms(const LargePop* lp, int nl, float alpha, float delta, float& GL,
-                                            float& GLp) {
+                                            float& GLp, float& GLabs) {
   GL = 0.f;
   GLp = 0.f;
+  GLabs = 0.f;
   for (int k = 0; k < nl; ++k) {
-    float ps, dl;
-    psi_large(lp[k].y, alpha, delta, ps, dl);
+    float ps, dl, mg;
+    psi_large(lp[k].y, alpha, delta, ps, dl, mg);
     GL = fmaf(lp[k].f, ps, GL);
     GLp = fmaf(lp[k].f * lp[k].y, dl, GLp);
+    GLabs = fmaf(lp[k].f, mg, GLabs);
+  }
+}
+
+// Float-pair sum over a list of populations:
+// G = sum f [(1 + x) ln(1 + x) - x - x ln(1 + y)], x = alpha y (the entropy
+// difference H(f + alpha Delta) - H(f) of those populations, conservation-
+// consistent form), and its derivative G' = sum f y [ln(1 + x) - ln(1 + y)]
+// in FP32 (Newton needs it to a few digits only).
+__device__ __noinline__ void df_terms(const LargePop* lp, int nl, df alpha, df& G, float& Gp) {
+  G = df_make(0.f);
+  Gp = 0.f;
+  for (int k = 0; k < nl; ++k) {
+    const df y{lp[k].y, lp[k].ylo};
+    const df x = df_mul(alpha, y);
+    const df lx = df_log1p(x), ly = df_log1p(y);
+    const df t = df_add(df_mul(df_add(df_make(1.0f), x), lx), df_neg(df_mul(x, df_add(df_make(1.0f), ly))));
+    G = df_add(G, df_mul_f(t, lp[k].f));
+    Gp = fmaf(lp[k].f * lp[k].y, lx.hi - ly.hi, Gp);
   }
 }
 
@@ -420,10 +446,33 @@ __device__ __forceinline__ void series_g(const float (&S)[K + 1], float delta, f
 // populations (|y| > kYSmall) are left out of the sums, their truncated series
 // is added for a first root (delta0), and one or two Newton steps with their
 // exact psi polish it.
+// Float-pair Newton over all 27 populations from alpha = 2: the fallback when
+// the FP32 solve fails (rare; never in the hot loop).
+__device__ __noinline__ bool df_newton_all(LargePop* lp, float amax, int max_it, float tol_dH, float& delta_hi,
+                                           float& delta_lo, unsigned& iters) {
+  df delta = df_make((2.0f < amax) ? 0.f : 0.5f * (amax - 3.0f));
+  for (int it = 0; it < max_it; ++it) {
+    df G;
+    float Gp;
+    df_terms(lp, Q, df_add(df_make(2.0f), delta), G, Gp);
+    iters += 1;
+    if (fabsf(G.hi) <= 0.25f * tol_dH) {
+      delta_hi = delta.hi;
+      delta_lo = delta.lo;
+      return true;
+    }
+    if (!(Gp > 0.f)) break;
+    const df next = df_add(delta, df_make(-G.hi / Gp));
+    if (!(2.0f + next.hi > 1.0f) || !(2.0f + next.hi < amax)) break;
+    delta = next;
+  }
+  return false;
+}
+
 template <int K>
 __device__ AlphaOut alpha_solve32(const float2 (&D2)[14], const float2 (&y2)[14], const float (&d)[Q],
-                                  unsigned large, float amax, int max_it, float delta_start = 0.f,
-                                  int series_it = -1) {
+                                  unsigned large, float amax, int max_it, float polish_thr, float tol_dH,
+                                  bool allow_df = true, float delta_start = 0.f, int series_it = -1) {
   float2 S2[K + 1];
 #pragma unroll
   for (int k = 0; k <= K; ++k) S2[k] = make_float2(0.f, 0.f);
@@ -443,7 +492,7 @@ __device__ AlphaOut alpha_solve32(const float2 (&D2)[14], const float2 (&y2)[14]
 #pragma unroll
   for (int k = 0; k <= K; ++k) S[k] = S2[k].x + S2[k].y;
 
-  AlphaOut r{0.f, 0u, large != 0u, false};
+  AlphaOut r{0.f, 0.f, 0u, large != 0u, false};
   LargePop lp[Q];
   int nl = 0;
   float SL[K + 1];
@@ -457,8 +506,10 @@ __device__ AlphaOut alpha_solve32(const float2 (&D2)[14], const float2 (&y2)[14]
       for (int h = 0; h < 2; ++h) {
         const int i = 2 * q + h;
         if (i < Q && (large & (1u << i))) {
-          lp[nl].f = (float)w27(i) + d[i];
-          lp[nl].y = h ? y2[q].y : y2[q].x;
+          const float f = (float)w27(i) + d[i], D = h ? D2[q].y : D2[q].x, y = h ? y2[q].y : y2[q].x;
+          lp[nl].f = f;
+          lp[nl].y = y;
+          lp[nl].ylo = __fdiv_rn(fmaf(-y, f, D), f);
           ++nl;
         }
       }
@@ -488,21 +539,27 @@ __device__ AlphaOut alpha_solve32(const float2 (&D2)[14], const float2 (&y2)[14]
     const float next = delta - step;
     if (!(2.0f + next > 1.0f) || !(2.0f + next < amax)) break;
     delta = next;
-    if (fabsf(step) <= fmaxf(4e-8f, 2e-7f * fabsf(delta))) {
+    // Newton converges quadratically: the error left after this step is about
+    // |g''/(2g')| step^2 <= (max|y|/3) step^2 <= 0.034 step^2 for the series
+    // (g' ~ S_2/2, g'' ~ -S_3/3), below FP32 resolution once |step| <= 2e-4 |delta|
+    if (fabsf(step) <= fmaxf(4e-8f, 2e-4f * fabsf(delta))) {
       ok = true;
       break;
     }
   }
+  float gsmall = 0.f, gp_last = 0.f, GLabs = 0.f;
   if (ok && nl) {
     ok = false;
     for (int it = 0; it < 4; ++it) {
       const float alpha = 2.0f + delta;
       float g, gp, GL, GLp;
       series_g<K>(S, delta, g, gp);
-      large_terms(lp, nl, alpha, delta, GL, GLp);
+      gsmall = g;
+      large_terms(lp, nl, alpha, delta, GL, GLp, GLabs);
       const float ia = 1.0f / alpha;
       g = fmaf(GL, ia, g);
       gp += (GLp - GL * ia) * ia;
+      gp_last = gp;
       r.iters += 1;
       if (!(gp > 0.f)) break;
       const float step = g / gp;
@@ -515,7 +572,52 @@ __device__ AlphaOut alpha_solve32(const float2 (&D2)[14], const float2 (&y2)[14]
       }
     }
   }
-  if (!ok) {
+  if (ok && nl && GLabs > polish_thr) {
+    // FP32 cannot resolve G_L to the tolerance (its rounding error is ~1e-7 GLabs):
+    // one Newton step with G_L in float pairs, the series part (accurate) in FP32
+    float g, gp;
+    series_g<K>(S, delta, g, gp);
+    const df alpha = df_add(df_make(2.0f), df_make(delta));
+    df G;
+    float Gp;
+    df_terms(lp, nl, alpha, G, Gp);
+    G = df_add(G, df_mul_f(alpha, g));  // G = alpha g_small + G_L
+    const float Gd = alpha.hi * gp_last;  // dG/dalpha at the root (g = 0)
+    if (Gd > 0.f) {
+      const df next = df_add(df_make(delta), df_make(-G.hi / Gd));
+      if (2.0f + next.hi > 1.0f && 2.0f + next.hi < amax) {
+        delta = next.hi;
+        r.delta_lo = next.lo;
+      }
+    }
+    r.iters += 1;
+    (void)gsmall;
+  }
+  if (!ok && allow_df) {
+    // float-pair Newton over all populations; alpha = 2 (or inside the bracket) if that fails too
+    nl = 0;
+#pragma unroll
+    for (int q = 0; q < 14; ++q) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int i = 2 * q + h;
+        if (i < Q) {
+          const float f = (float)w27(i) + d[i], D = h ? D2[q].y : D2[q].x, y = h ? y2[q].y : y2[q].x;
+          lp[i].f = f;
+          lp[i].y = y;
+          lp[i].ylo = __fdiv_rn(fmaf(-y, f, D), f);
+        }
+      }
+    }
+    float hi = 0.f, lo = 0.f;
+    if (df_newton_all(lp, amax, max_it, tol_dH, hi, lo, r.iters)) {
+      delta = hi;
+      r.delta_lo = lo;
+    } else {
+      r.fallback = true;
+      delta = (2.0f < amax) ? 0.f : 0.5f * (amax - 3.0f);
+    }
+  } else if (!ok) {
     r.fallback = true;
     delta = (2.0f < amax) ? 0.f : 0.5f * (amax - 3.0f);
   }
@@ -527,17 +629,10 @@ __device__ AlphaOut alpha_solve32(const float2 (&D2)[14], const float2 (&y2)[14]
 // (0: none).  Both variants are built; the level's autotuner picks one.
 // MODE 0: Newton from alpha = 2; 1: learned guess + at most two Newton steps,
 // Newton from 2 as the fallback; 2: Newton and harvesting of training records.
-template <bool CHECK, int MINB, int MODE = 0>
-__global__ void __launch_bounds__(128, MINB) d3q27_fp32_kernel(const Step27Args a) {
-  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= a.N) return;
-  const uint8_t t = __ldg(a.ntype + n);
-  if (t == NT_SKIP) return;
-  const float* __restrict__ src = static_cast<const float*>(a.src);
+// Everything after the gather: moments, equilibrium, alpha, relaxation, store.
+template <bool CHECK, int MODE>
+__device__ __forceinline__ void node_update(const Step27Args& a, int64_t n, float (&d)[Q]) {
   float* __restrict__ dst = static_cast<float*>(a.dst);
-  float d[Q];
-  gather(a, src, n, t, d);
-
   // moments of the deviations: rho = 1 + sum d, j = sum c d (sum c w = 0)
   float dr = 0.f, jx = 0.f, jy = 0.f, jz = 0.f;
 #pragma unroll
@@ -628,21 +723,23 @@ __global__ void __launch_bounds__(128, MINB) d3q27_fp32_kernel(const Step27Args 
       delta0 = lam * mlp_forward(x);
       series_it = 2;
     }
+    // float-pair polish above this error scale (the FP32 rounding of G_L stays below ~5e-7 GLabs)
+    const float pthr = (float)(a.tol_dH * 1e6), tdh = (float)a.tol_dH;
     switch (korder) {
-      case 6: al = alpha_solve32<6>(D2, y2, d, large, amax, a.max_newton, delta0, series_it); break;
-      case 8: al = alpha_solve32<8>(D2, y2, d, large, amax, a.max_newton, delta0, series_it); break;
-      case 10: al = alpha_solve32<10>(D2, y2, d, large, amax, a.max_newton, delta0, series_it); break;
-      default: al = alpha_solve32<12>(D2, y2, d, large, amax, a.max_newton, delta0, series_it); break;
+      case 6: al = alpha_solve32<6>(D2, y2, d, large, amax, a.max_newton, pthr, tdh, MODE != 1, delta0, series_it); break;
+      case 8: al = alpha_solve32<8>(D2, y2, d, large, amax, a.max_newton, pthr, tdh, MODE != 1, delta0, series_it); break;
+      case 10: al = alpha_solve32<10>(D2, y2, d, large, amax, a.max_newton, pthr, tdh, MODE != 1, delta0, series_it); break;
+      default: al = alpha_solve32<12>(D2, y2, d, large, amax, a.max_newton, pthr, tdh, MODE != 1, delta0, series_it); break;
     }
     if (MODE == 1 && al.fallback) {
       // the guess did not converge in two steps: plain Newton from alpha = 2
       guess_miss = true;
       const unsigned it0 = al.iters;
       switch (korder) {
-        case 6: al = alpha_solve32<6>(D2, y2, d, large, amax, a.max_newton); break;
-        case 8: al = alpha_solve32<8>(D2, y2, d, large, amax, a.max_newton); break;
-        case 10: al = alpha_solve32<10>(D2, y2, d, large, amax, a.max_newton); break;
-        default: al = alpha_solve32<12>(D2, y2, d, large, amax, a.max_newton); break;
+        case 6: al = alpha_solve32<6>(D2, y2, d, large, amax, a.max_newton, pthr, tdh); break;
+        case 8: al = alpha_solve32<8>(D2, y2, d, large, amax, a.max_newton, pthr, tdh); break;
+        case 10: al = alpha_solve32<10>(D2, y2, d, large, amax, a.max_newton, pthr, tdh); break;
+        default: al = alpha_solve32<12>(D2, y2, d, large, amax, a.max_newton, pthr, tdh); break;
       }
       al.iters += it0;
     }
@@ -659,7 +756,7 @@ __global__ void __launch_bounds__(128, MINB) d3q27_fp32_kernel(const Step27Args 
     }
     if (CHECK) {
       // |H(f + alpha Delta) - H(f)| in FP64 (conservation-consistent form) from the FP32 populations
-      const double al64 = 2.0 + (double)al.delta;
+      const double al64 = 2.0 + (double)al.delta + (double)al.delta_lo;
       double g = 0.0;
 #pragma unroll
       for (int i = 0; i < Q; ++i) {
@@ -692,6 +789,137 @@ __global__ void __launch_bounds__(128, MINB) d3q27_fp32_kernel(const Step27Args 
   }
 }
 
+// Direct variant: one thread per node, the 27 pulls are plain global loads.
+template <bool CHECK, int MINB, int MODE = 0>
+__global__ void __launch_bounds__(128, MINB) d3q27_fp32_kernel(const Step27Args a) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= a.N) return;
+  const uint8_t t = __ldg(a.ntype + n);
+  if (t == NT_SKIP) return;
+  float d[Q];
+  gather(a, static_cast<const float*>(a.src), n, t, d);
+  node_update<CHECK, MODE>(a, n, d);
+}
+
+// ---------------------------------------------------------------------------
+// Staged variant: a persistent CTA walks tiles of kTileX nodes along x.  For
+// a tile in an interior row, one thread issues 27 bulk copies (one per
+// population: the row segment the pull reads, x0-4 .. x0+kTileX+4) into a
+// shared-memory stage tracked by an mbarrier; kStages tiles are in flight
+// while the CTA computes, so the HBM traffic no longer waits on the
+// per-thread register budget.  Bulk nodes read their pulls from shared
+// memory; boundary nodes use the link-word gather from global memory.
+// ---------------------------------------------------------------------------
+constexpr int kTileX = 128, kHalo = 4, kSegLen = kTileX + 2 * kHalo, kStages = 2;
+constexpr int kStageFloats = Q * kSegLen;
+constexpr unsigned kStageBytes = kStageFloats * 4;
+// Bounded mbarrier waits: each poll suspends for at most ~1 us (time hint), and
+// a wait gives up after 2^20 polls or 2 s of the global timer, whichever first.
+constexpr int kSpinLimit = 1 << 20;
+constexpr unsigned long long kWaitLimitNs = 2000000000ull;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  const unsigned long long t0 = global_ns();
+  for (int i = 0; i < kSpinLimit; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity), "r"(1000u)
+        : "memory");
+    if (done) return true;
+    if ((i & 255) == 255 && global_ns() - t0 > kWaitLimitNs) return false;
+  }
+  return false;
+}
+
+// Issue the copies of one tile into one stage (one thread).  Returns false for
+// tiles whose row touches the box faces: all their nodes are boundary nodes.
+__device__ __forceinline__ void issue_tile(const Step27Args& a, const float* src, int64_t tile, int tiles_x,
+                                           float* stage, uint32_t bar) {
+  const int tx = (int)(tile % tiles_x);
+  const int64_t row = tile / tiles_x;
+  const int y = (int)(row % a.ny), z = (int)(row / a.ny);
+  const bool interior = y >= 1 && y <= a.ny - 2 && z >= 1 && z <= a.nz - 2;
+  const unsigned tx_bytes = interior ? kStageBytes : 0u;
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(tx_bytes) : "memory");
+  if (!interior) return;
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  const int64_t x0 = (int64_t)tx * kTileX;
+#pragma unroll 1
+  for (int j = 0; j < Q; ++j) {
+    const float* g = src + (int64_t)j * a.plane + ((int64_t)(z - cz27(j)) * a.ny + (y - cy27(j))) * a.nx + x0 - kHalo;
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(stage + j * kSegLen)),
+        "l"(g), "r"((unsigned)(kSegLen * 4)), "r"(bar)
+        : "memory");
+  }
+}
+
+template <bool CHECK, int MODE = 0>
+__global__ void __launch_bounds__(128, 3) d3q27_fp32_staged_kernel(const Step27Args a) {
+  extern __shared__ __align__(128) float sm[];
+  __shared__ __align__(8) unsigned long long bars[kStages];
+  const float* __restrict__ src = static_cast<const float*>(a.src);
+  const int tiles_x = (a.nx + kTileX - 1) / kTileX;
+  const int64_t ntiles = (int64_t)tiles_x * a.ny * a.nz;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bars[s])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    for (int s = 0; s < kStages; ++s) {
+      const int64_t tile = blockIdx.x + (int64_t)s * gridDim.x;
+      if (tile < ntiles) issue_tile(a, src, tile, tiles_x, sm + s * kStageFloats, smem_addr(&bars[s]));
+    }
+  }
+  __syncthreads();
+  int64_t it = 0;
+  bool failed = false;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+    const int s = (int)(it % kStages);
+    const bool ok = mbar_wait(smem_addr(&bars[s]), (uint32_t)((it / kStages) & 1));
+    if (__syncthreads_or(!ok)) {
+      failed = true;
+      break;
+    }
+    const int tx = (int)(tile % tiles_x);
+    const int64_t row = tile / tiles_x;
+    const int x = tx * kTileX + (int)threadIdx.x;
+    const int64_t n = row * a.nx + x;
+    const uint8_t t = x < a.nx ? __ldg(a.ntype + n) : (uint8_t)NT_SKIP;
+    float d[Q];
+    if (t == NT_BULK) {
+      const float* stg = sm + s * kStageFloats + kHalo + threadIdx.x;
+#pragma unroll
+      for (int j = 0; j < Q; ++j) d[j] = stg[j * kSegLen - cx27(j)];
+    } else if (t == NT_BOUNDARY) {
+      gather(a, src, n, t, d);
+    }
+    __syncthreads();  // every read of stage s is done: refill it
+    if (threadIdx.x == 0) {
+      const int64_t next = tile + (int64_t)kStages * gridDim.x;
+      if (next < ntiles) issue_tile(a, src, next, tiles_x, sm + s * kStageFloats, smem_addr(&bars[s]));
+    }
+    if (t != NT_SKIP) node_update<CHECK, MODE>(a, n, d);
+  }
+  if (failed && threadIdx.x == 0) {
+    // report, then wait (bounded) for this block's copies still in flight before the
+    // shared memory they target is released
+    atomicOr(&a.stats->status, (unsigned)ELBM_ST_COPY_TIMEOUT);
+    for (int64_t k = it; k < it + kStages; ++k)
+      if (blockIdx.x + k * gridDim.x < ntiles) mbar_wait(smem_addr(&bars[k % kStages]), (uint32_t)((k / kStages) & 1));
+  }
+}
+
 }  // namespace
 
 void launch_d3q27_fp64(const Step27Args& a, cudaStream_t s) {
@@ -700,9 +928,36 @@ void launch_d3q27_fp64(const Step27Args& a, cudaStream_t s) {
   d3q27_fp64_kernel<<<(unsigned)blocks, threads, 0, s>>>(a);
 }
 
+bool staged_eligible(const Step27Args& a) {
+  // 16-byte aligned row segments: x rows and planes in multiples of 4 floats
+  return a.nx % 4 == 0 && a.plane % 4 == 0 && a.ny >= 3 && a.nz >= 3;
+}
+
+template <bool CHECK, int MODE>
+void launch_staged(const Step27Args& a, cudaStream_t s) {
+  static int blocks_per_sm = -1, sms = 0;
+  const size_t smem = (size_t)kStages * kStageBytes;
+  if (blocks_per_sm < 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, d3q27_fp32_staged_kernel<CHECK, MODE>, 128, smem);
+    if (blocks_per_sm < 1) blocks_per_sm = 1;
+  }
+  const int tiles_x = (a.nx + kTileX - 1) / kTileX;
+  const int64_t ntiles = (int64_t)tiles_x * a.ny * a.nz;
+  const int64_t grid = std::min<int64_t>(ntiles, (int64_t)sms * blocks_per_sm);
+  d3q27_fp32_staged_kernel<CHECK, MODE><<<(unsigned)grid, 128, smem, s>>>(a);
+}
+
 void launch_d3q27_fp32(const Step27Args& a, cudaStream_t s) {
   const int threads = 128;
   const int64_t blocks = (a.N + threads - 1) / threads;
+  if (a.variant == 2 && !a.check_dH && !a.harvest && staged_eligible(a)) {
+    if (a.alpha_mode == 2) launch_staged<false, 1>(a, s);
+    else launch_staged<false, 0>(a, s);
+    return;
+  }
   if (a.check_dH) {
     if (a.alpha_mode == 2) d3q27_fp32_kernel<true, 0, 1><<<(unsigned)blocks, threads, 0, s>>>(a);
     else d3q27_fp32_kernel<true, 0, 0><<<(unsigned)blocks, threads, 0, s>>>(a);

@@ -6,8 +6,10 @@
 // fluid node and direction finds where the link crosses a surface triangle
 // and stores the crossing as state = -1001 - floor(|x - x_w| / link_dist * 1e9)
 // (linking/modules/linkwise.f95:45-57, link_dist = |c_i| dx, link_info.f95:27).
-// This file produces the same encoding with a uniform-grid acceleration of the
-// triangle search (the reference tests every triangle for every link).
+// Only links from a fluid node to a solid node are searched, as in the
+// reference, so a wall link never joins two fluid nodes.  This file produces
+// the same encoding with a uniform-grid acceleration of the triangle search
+// (the reference tests every triangle for every link).
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -119,11 +121,14 @@ extern "C" int elbm_mark_triangles(int nx, int ny, int nz, const double* origin,
         for (int c0 = lo[0]; c0 <= hi[0]; ++c0) grid[gidx(c0, c1, c2)].push_back(k);
   }
   auto coord = [&](int i, int a) { return origin[a] + i * dx; };
-  // 1) solid nodes: odd number of +x ray crossings (fluid_or_solid by ray casting)
+  // 1) solid nodes: odd number of +x ray crossings (fluid_or_solid by ray casting).
+  // The ray starts a tiny irrational offset off the lattice line, so that it passes
+  // through no vertex or edge of a surface built on lattice points.
+  constexpr double kRayDy = 7.548776662466927e-7, kRayDz = 5.698402909980532e-7;
   std::vector<uint8_t> solid(N, 0);
   for (int k = 0; k < nz; ++k)
     for (int j = 0; j < ny; ++j) {
-      const double y = coord(j, 1), z = coord(k, 2);
+      const double y = origin[1] + (j + kRayDy) * dx, z = origin[2] + (k + kRayDz) * dx;
       if (y < glo[1] || y > ghi[1] || z < glo[2] || z > ghi[2]) continue;
       std::vector<int> cand;
       for (int t = 0; t < ntri; ++t)
@@ -148,13 +153,22 @@ extern "C" int elbm_mark_triangles(int nx, int ny, int nz, const double* origin,
         const int64_t n = ((int64_t)k * ny + j) * nx + i;
         if (solid[n]) continue;
         const double p0[3] = {coord(i, 0), coord(j, 1), coord(k, 2)};
-        if (p0[0] < glo[0] - 2 * dx || p0[0] > ghi[0] + 2 * dx || p0[1] < glo[1] - 2 * dx || p0[1] > ghi[1] + 2 * dx ||
-            p0[2] < glo[2] - 2 * dx || p0[2] > ghi[2] + 2 * dx)
-          continue;
+        bool near_solid = false;
+        for (int q = 1; q < Q27 && !near_solid; ++q) {
+          const int it = i + D3Q27::cx[q], jt = j + D3Q27::cy[q], kt = k + D3Q27::cz[q];
+          near_solid = it >= 0 && jt >= 0 && kt >= 0 && it < nx && jt < ny && kt < nz &&
+                       solid[((int64_t)kt * ny + jt) * nx + it];
+        }
+        if (!near_solid) continue;
         const int gc[3] = {(int)std::floor((p0[0] - glo[0]) / cell), (int)std::floor((p0[1] - glo[1]) / cell),
                            (int)std::floor((p0[2] - glo[2]) / cell)};
         for (int q = 1; q < Q27; ++q) {
           const int c[3] = {D3Q27::cx[q], D3Q27::cy[q], D3Q27::cz[q]};
+          // only links from a fluid node to a solid node are wall links
+          // (inter_bb_setup.f95:36-40: same-type neighbours skip the crossing search)
+          const int it = i + c[0], jt = j + c[1], kt = k + c[2];
+          if (!(it >= 0 && jt >= 0 && kt >= 0 && it < nx && jt < ny && kt < nz && solid[((int64_t)kt * ny + jt) * nx + it]))
+            continue;
           const double p1[3] = {p0[0] + c[0] * dx, p0[1] + c[1] * dx, p0[2] + c[2] * dx};
           double tbest = INFINITY;
           for (int d2 = -1; d2 <= 1; ++d2)
@@ -167,14 +181,7 @@ extern "C" int elbm_mark_triangles(int nx, int ny, int nz, const double* origin,
                   if (tt > 0.0 && tt < tbest) tbest = tt;
                 }
               }
-          if (tbest == INFINITY) {
-            const int it = i + c[0], jt = j + c[1], kt = k + c[2];
-            if (it >= 0 && jt >= 0 && kt >= 0 && it < nx && jt < ny && kt < nz &&
-                solid[((int64_t)kt * ny + jt) * nx + it])
-              tbest = 1.0;  // the link ends in a solid node without a recorded crossing
-            else
-              continue;
-          }
+          if (tbest == INFINITY) tbest = 1.0;  // the link ends in a solid node without a recorded crossing
           // linkwise.f95:56: -1001 - floor(|x - x_w| / link_dist * 1e9)
           const double len = std::sqrt((double)(c[0] * c[0] + c[1] * c[1] + c[2] * c[2])) * dx;
           const double dist = tbest * len;

@@ -49,7 +49,11 @@ struct Step27Args {
   int harvest_stride;
 };
 
-constexpr int kFp32Variants = 2;
+constexpr int kFp32Variants = 3;  // 0: direct, 1: direct with 4 blocks/SM, 2: bulk-copy staged
+// Bytes allocated before and after each population buffer (never written):
+// room for the staged kernel's row-segment copies that start 4 floats before
+// a plane or run up to a tile past its end.
+constexpr size_t kPopGuardBytes = 1024;
 
 void launch_d3q27_fp64(const Step27Args& a, cudaStream_t s);
 void upload_alpha_mlp(const float* w_host, cudaStream_t s);

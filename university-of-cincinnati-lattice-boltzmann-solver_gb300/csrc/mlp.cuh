@@ -15,6 +15,7 @@ static_assert(kMlpParams == 6017, "27-64-64-1 network");
 void mlp_batch_grad(const float* w, const float* rec, int64_t n, float* scratch, float* grad, double* loss,
                     cudaStream_t s);
 void mlp_adam(float* w, const float* g, float* m, float* v, float lr, int t, cudaStream_t s);
+void mlp_tc_infer(const float* w, const float* x, int64_t n, float* out, unsigned* status, cudaStream_t s);
 void mlp_gather_batch(const float* rec, const uint32_t* perm, int64_t off, int64_t b, float* out, cudaStream_t s);
 
 }  // namespace elbm
