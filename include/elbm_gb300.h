@@ -188,7 +188,8 @@ int elbm_level_step(elbm_ctx* ctx, int lvl, int nsteps, elbm_stats* stats);
 int elbm_autotune(elbm_ctx* ctx, int lvl, int reps, int* chosen, double* ms_per_variant);
 
 /* Use kernel variant v (0: direct loads; 1: direct, register-capped for
- * occupancy; 2: rows staged in shared memory by bulk copies, persistent) for
+ * occupancy; 2: rows staged in shared memory by bulk copies, persistent;
+ * 3: direct loads, persistent warps striding over 32-node chunks) for
  * the level's FP32 D3Q27 steps, instead of the autotuner's choice.  Variant 2
  * applies to boxes with nx and the plane size multiples of 4 and ny, nz >= 3;
  * other boxes fall back to variant 0.  No counterpart in the reference. */

@@ -189,20 +189,22 @@ def test_sphere_ibb_fp32_vs_oracle(pkg, orc, built_lib):
     assert np.max(np.abs(ug - ur)) / 0.08 <= 1e-4
 
 
-@pytest.mark.parametrize("shape", [(128, 20, 16), (200, 12, 10)])
-def test_staged_variant_matches_direct(pkg, built_lib, shape):
-    """The bulk-copy staged kernel (variant 2) computes the same step as the
-    direct kernel (variant 0): same node updates, populations equal to FP32
-    rounding, no copy timeouts."""
+@pytest.mark.parametrize("shape,variant", [((128, 20, 16), 2), ((200, 12, 10), 2), ((200, 12, 10), 3),
+                                           ((64, 32, 32), 1)])
+def test_kernel_variants_match_direct(pkg, built_lib, shape, variant):
+    """Every step-kernel variant (1: register-capped, 2: bulk-copy staged,
+    3: persistent warps) computes the same step as the direct kernel
+    (variant 0): same node updates, populations equal to FP32 rounding, no
+    copy timeouts."""
     nx, ny, nz = shape
     out = {}
-    for v in (0, 2):
+    for v in (0, variant):
         ctx, *_ = _setup(pkg, nx, ny, nz, pkg.capi.ELBM_STORE_FP32_DEV, nu=2e-5, noise=5e-3, u0=(0.06, 0.0, 0.0))
         ctx.set_kernel_variant(0, v)
         s = ctx.step(0, 30)
         out[v] = (s, ctx.download(0))
         ctx.close()
-    (s0, f0), (s2, f2) = out[0], out[2]
+    (s0, f0), (s2, f2) = out[0], out[variant]
     assert s2["status"] & 0x10 == 0
     assert s0["node_updates"] == s2["node_updates"] == 30 * nx * ny * nz
     assert np.max(np.abs(f2 - f0)) <= 1e-6, np.max(np.abs(f2 - f0))

@@ -59,4 +59,19 @@ def test_learned_alpha_pipeline(pkg, built_lib):
           f"guesses needing the fallback: {sl['guess_misses'] / sl['node_updates']:.2e}")
     assert sl["guess_misses"] <= 0.01 * sl["node_updates"]
     assert it_learned < it_newton
+    # outside check mode the learned step runs the tensor-core inference kernel
+    c3, st3, _, bp3 = _level(pkg, cap.ELBM_ALPHA_LEARNED, check=0)
+    c3.set_alpha_mlp(0, w)
+    c3.set_d3q27_params(0, cap.make_d3q27_params(**bp3))
+    c3.set_links(0, 0, st3)
+    c3.upload(0, 0, f_mid)
+    s3 = c3.step(0, 10)
+    f3 = c3.download(0)
+    c3.close()
+    assert s3["status"] & 0x10 == 0 and s3["fallbacks"] <= 1e-5 * s3["node_updates"]
+    assert np.max(np.abs(f3 - fn)) <= 1e-6
+    it_tc = s3["newton_iters"] / s3["node_updates"]
+    print(f"tensor-core guess: {it_tc:.3f} iterations per node, guesses needing the fallback: "
+          f"{s3['guess_misses'] / s3['node_updates']:.2e}")
+    assert s3["guess_misses"] <= 0.02 * s3["node_updates"]
     ctx.close()

@@ -94,6 +94,7 @@ struct Level {
   elbm_d3q39_params p39{};
   bool params_set = false;
   bool mlp_set = false;  // learned-alpha weights uploaded
+  DevBuf<float> mlp_w;   // the level's network weights (FP32 master copy; BF16 in the tensor-core kernel)
   int variant = 0;  // FP32 D3Q27 kernel variant picked by elbm_autotune
   DevBuf<uint8_t> eq;  // kEqTables x Q, FP64 or FP32 deviations
 };
@@ -685,6 +686,7 @@ int elbm_level_step(elbm_ctx* c, int lvl, int nsteps, elbm_stats* out) {
       a.alpha_out = (p.record_alpha && s == nsteps - 1) ? b.alpha.p : nullptr;
       a.stats = c->stats.p;
       a.variant = lv->variant;
+      a.mlp = lv->mlp_set ? lv->mlp_w.p : nullptr;
       if (lv->storage == ELBM_STORE_FP64) launch_d3q27_fp64(a, c->stream);
       else launch_d3q27_fp32(a, c->stream);
       CUDA_TRY(cudaGetLastError(), "step kernel launch");
@@ -736,6 +738,7 @@ int elbm_autotune(elbm_ctx* c, int lvl, int reps, int* chosen, double* ms_per_va
         a.check_dH = 0;
         a.stats = c->stats.p;
         a.variant = v;
+        a.mlp = lv->mlp_set ? lv->mlp_w.p : nullptr;
         launch_d3q27_fp32(a, c->stream);
         CUDA_TRY(cudaGetLastError(), "autotune launch");
       }
@@ -771,6 +774,9 @@ int elbm_set_alpha_mlp(elbm_ctx* c, int lvl, const float* weights) {
   for (int k = 0; k < kMlpParams; ++k)
     if (!std::isfinite(weights[k])) return fail(c, ELBM_E_ARG, "non-finite weight %d", k);
   CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  if (!lv->mlp_w.p) CUDA_TRY(lv->mlp_w.alloc(kMlpParams), "weights");
+  CUDA_TRY(cudaMemcpyAsync(lv->mlp_w.p, weights, kMlpParams * sizeof(float), cudaMemcpyHostToDevice, c->stream),
+           "weights");
   upload_alpha_mlp(weights, c->stream);
   CUDA_TRY(cudaGetLastError(), "weights upload");
   CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");

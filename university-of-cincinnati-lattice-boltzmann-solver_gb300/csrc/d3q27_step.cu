@@ -24,6 +24,7 @@
 #include "lattice.cuh"
 #include "dfloat.cuh"
 #include "mlp.cuh"
+#include "mlp_tc.cuh"
 
 namespace elbm {
 
@@ -282,12 +283,16 @@ __global__ void __launch_bounds__(128) d3q27_fp64_kernel(const Step27Args a) {
 // with P_m built by P_m = (2 + delta) P_{m-1} + delta 2^(m-1), so g is
 // evaluated from small quantities only and Newton runs on delta in FP32.
 // Populations with |y| > kYSmall, where the series converges slowly, are
-// summed individually in FP64 (rare: strongly non-equilibrium nodes).  The
-// series order K is chosen per warp from the warp's largest |y| so that the
-// truncation error in alpha stays below ~1e-9.
+// summed individually (rare: strongly non-equilibrium nodes), in FP32 with a
+// cancellation-free form, and in float pairs where FP32 cannot resolve the
+// entropy difference to the tolerance.
 // ---------------------------------------------------------------------------
 
 constexpr float kYSmall = 0.1f;
+// One series order for every node: at |y| <= 0.1 the truncation leaves
+// |g| ~ f (2|y|)^13 / 338 <= 1e-12, and a single instantiation keeps the
+// kernel's code small enough for the instruction caches.
+constexpr int kSeriesK = 12;
 
 __host__ __device__ constexpr double pow2i(int e) {
   double r = 1.0;
@@ -441,11 +446,6 @@ __device__ __forceinline__ void series_g(const float (&S)[K + 1], float delta, f
   }
 }
 
-// The alpha solve of one node.  Populations come in pairs (float2) so that the
-// power sums run on the paired FP32 pipe.  Strongly non-equilibrium
-// populations (|y| > kYSmall) are left out of the sums, their truncated series
-// is added for a first root (delta0), and one or two Newton steps with their
-// exact psi polish it.
 // Float-pair Newton over all 27 populations from alpha = 2: the fallback when
 // the FP32 solve fails (rare; never in the hot loop).
 __device__ __noinline__ bool df_newton_all(LargePop* lp, float amax, int max_it, float tol_dH, float& delta_hi,
@@ -469,10 +469,34 @@ __device__ __noinline__ bool df_newton_all(LargePop* lp, float amax, int max_it,
   return false;
 }
 
+// The populations of one node as the alpha solve sees them: Delta (pairs),
+// y = Delta / f (pairs), the deviations d = f - w.
+struct NodePops {
+  float2 D2[14], y2[14];
+  float d[Q];
+};
+
+// Alpha solve of a node with strongly non-equilibrium populations
+// (|y| > kYSmall; out of line, rare).  The other populations enter through
+// their power sums; the strong ones add their truncated series for a first
+// root, then Newton steps with their exact psi polish it (FP32), and a
+// float-pair step follows where FP32 cannot resolve G to the tolerance.
 template <int K>
-__device__ AlphaOut alpha_solve32(const float2 (&D2)[14], const float2 (&y2)[14], const float (&d)[Q],
-                                  unsigned large, float amax, int max_it, float polish_thr, float tol_dH,
-                                  bool allow_df = true, float delta_start = 0.f, int series_it = -1) {
+__device__ __noinline__ AlphaOut alpha_solve_large(const NodePops& P, int max_it, float polish_thr, float tol_dH,
+                                                   bool allow_df, float delta_start, int series_it) {
+  const float2(&D2)[14] = P.D2;
+  const float2(&y2)[14] = P.y2;
+  const float(&d)[Q] = P.d;
+  unsigned large = 0u;
+  float ymin = 0.f;
+#pragma unroll
+  for (int q = 0; q < 14; ++q) {
+    if (fabsf(y2[q].x) > kYSmall) large |= 1u << (2 * q);
+    if (2 * q + 1 < Q && fabsf(y2[q].y) > kYSmall) large |= 1u << (2 * q + 1);
+    ymin = fminf(ymin, fminf(y2[q].x, y2[q].y));
+  }
+  // positivity bracket: f + alpha Delta > 0 for all i  <=>  alpha < -1/min(y)
+  const float amax = (ymin < 0.f) ? -1.0f / ymin : INFINITY;
   float2 S2[K + 1];
 #pragma unroll
   for (int k = 0; k <= K; ++k) S2[k] = make_float2(0.f, 0.f);
@@ -625,14 +649,121 @@ __device__ AlphaOut alpha_solve32(const float2 (&D2)[14], const float2 (&y2)[14]
   return r;
 }
 
+// Float-pair Newton over all populations for a node whose FP32 series solve
+// failed (out of line, rare).
+__device__ __noinline__ AlphaOut alpha_fallback(const NodePops& P, int max_it, float tol_dH, unsigned iters) {
+  LargePop lp[Q];
+  float ymin = 0.f;
+#pragma unroll
+  for (int q = 0; q < 14; ++q)
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int i = 2 * q + h;
+      if (i < Q) {
+        const float f = (float)w27(i) + P.d[i], D = h ? P.D2[q].y : P.D2[q].x, y = h ? P.y2[q].y : P.y2[q].x;
+        lp[i].f = f;
+        lp[i].y = y;
+        lp[i].ylo = __fdiv_rn(fmaf(-y, f, D), f);
+        ymin = fminf(ymin, y);
+      }
+    }
+  const float amax = (ymin < 0.f) ? -1.0f / ymin : INFINITY;
+  AlphaOut r{0.f, 0.f, iters, false, false};
+  float hi = 0.f, lo = 0.f;
+  if (df_newton_all(lp, amax, max_it, tol_dH, hi, lo, r.iters)) {
+    r.delta = hi;
+    r.delta_lo = lo;
+  } else {
+    r.fallback = true;
+    r.delta = (2.0f < amax) ? 0.f : 0.5f * (amax - 3.0f);
+  }
+  return r;
+}
+
+// The alpha solve of one node.  Populations come in pairs (float2) so that the
+// power sums run on the paired FP32 pipe.  ymax = max |y|.  Nodes with every
+// |y| <= kYSmall (nearly all) take the inline series path below; the others
+// the out-of-line solver above.
+template <int K>
+__device__ __forceinline__ AlphaOut alpha_solve32(const float2 (&D2)[14], const float2 (&y2)[14], const float (&d)[Q],
+                                                  float ymax, int max_it, float polish_thr, float tol_dH,
+                                                  bool allow_df = true, float delta_start = 0.f, int series_it = -1) {
+  if (ymax > kYSmall) {
+    NodePops P;
+#pragma unroll
+    for (int q = 0; q < 14; ++q) {
+      P.D2[q] = D2[q];
+      P.y2[q] = y2[q];
+    }
+#pragma unroll
+    for (int i = 0; i < Q; ++i) P.d[i] = d[i];
+    return alpha_solve_large<K>(P, max_it, polish_thr, tol_dH, allow_df, delta_start, series_it);
+  }
+  float2 S2[K + 1];
+#pragma unroll
+  for (int k = 0; k <= K; ++k) S2[k] = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int q = 0; q < 14; ++q) {
+    float2 p = __fmul2_rn(D2[q], y2[q]);  // f y^2  (the unused 28th lane holds 0)
+    S2[2] = __fadd2_rn(S2[2], p);
+#pragma unroll
+    for (int k = 3; k <= K; ++k) {
+      p = __fmul2_rn(p, y2[q]);
+      S2[k] = __fadd2_rn(S2[k], p);
+    }
+  }
+  float S[K + 1];
+#pragma unroll
+  for (int k = 0; k <= K; ++k) S[k] = S2[k].x + S2[k].y;
+  AlphaOut r{0.f, 0.f, 0u, false, false};
+  if (!(S[2] > 1e-30f)) return r;  // at equilibrium: alpha = 2
+  float delta = delta_start;
+  bool ok = false;
+  const int n_series = (series_it > 0) ? series_it : max_it;
+  for (int it = 0; it < n_series; ++it) {
+    float g, gp;
+    series_g<K>(S, delta, g, gp);
+    r.iters = it + 1;
+    if (!(gp > 0.f)) break;
+    const float step = g / gp;
+    const float next = delta - step;
+    // every |y| <= 0.1 puts the positivity bracket at alpha >= 10
+    if (!(next > -1.0f) || !(next < 8.0f)) break;
+    delta = next;
+    // quadratic convergence: the error left is <= 0.034 step^2 (see alpha_solve_large)
+    if (fabsf(step) <= fmaxf(4e-8f, 2e-4f * fabsf(delta))) {
+      ok = true;
+      break;
+    }
+  }
+  if (ok) {
+    r.delta = delta;
+    return r;
+  }
+  if (!allow_df) {
+    r.fallback = true;
+    return r;
+  }
+  NodePops P;
+#pragma unroll
+  for (int q = 0; q < 14; ++q) {
+    P.D2[q] = D2[q];
+    P.y2[q] = y2[q];
+  }
+#pragma unroll
+  for (int i = 0; i < Q; ++i) P.d[i] = d[i];
+  return alpha_fallback(P, max_it, tol_dH, r.iters);
+}
+
 // MINB: minimum resident blocks per SM requested from the register allocator
 // (0: none).  Both variants are built; the level's autotuner picks one.
 // MODE 0: Newton from alpha = 2; 1: learned guess + at most two Newton steps,
 // Newton from 2 as the fallback; 2: Newton and harvesting of training records.
-// Everything after the gather: moments, equilibrium, alpha, relaxation, store.
-template <bool CHECK, int MODE>
-__device__ __forceinline__ void node_update(const Step27Args& a, int64_t n, float (&d)[Q]) {
-  float* __restrict__ dst = static_cast<float*>(a.dst);
+// Moments, entropic equilibrium and Delta = f^eq - f of one node from its
+// deviations d (pairs D2); with want_y, also y = Delta / f (pairs y2) and
+// ymax = max |y|.  bad: rho or u not finite.
+__device__ __forceinline__ void node_prepare(const float (&d)[Q], bool want_y, float2 (&D2)[14], float2 (&y2)[14],
+                                             float& ymax, bool& bad) {
   // moments of the deviations: rho = 1 + sum d, j = sum c d (sum c w = 0)
   float dr = 0.f, jx = 0.f, jy = 0.f, jz = 0.f;
 #pragma unroll
@@ -665,7 +796,6 @@ __device__ __forceinline__ void node_update(const Step27Args& a, int64_t n, floa
     for (int c = 0; c < 3; ++c) qyz[b][c] = fmaf(1.0f + e[1][b], e[2][c], e[1][b]);
   // Delta_i = f^eq_i - f_i in deviation form: w_i [P (1 + dr) + dr] - d_i, kept in pairs
   const float rp1 = 1.0f + dr;
-  float2 D2[14];
 #pragma unroll
   for (int q = 0; q < 14; ++q) {
     float v[2];
@@ -682,65 +812,40 @@ __device__ __forceinline__ void node_update(const Step27Args& a, int64_t n, floa
     }
     D2[q] = make_float2(v[0], v[1]);
   }
-
-  AlphaOut al{0.f, 0u, false, false};
-  double dH = 0.0;
-  bool guess_miss = false;
-  if (a.alpha_mode != 0) {
-    float2 y2[14];
-    float ysmall = 0.f, ymin = 0.f;
-    unsigned large = 0u;
+  bad = !isfinite(rho) || !isfinite(u[0]) || !isfinite(u[1]) || !isfinite(u[2]);
+  ymax = 0.f;
+  if (want_y) {
 #pragma unroll
     for (int q = 0; q < 14; ++q) {
       const int i0 = 2 * q, i1 = 2 * q + 1;
       const float fa = (float)w27(i0) + d[i0];
       const float fb = (i1 < Q) ? (float)w27(i1) + d[i1] : 1.0f;
       y2[q] = make_float2(__fdividef(D2[q].x, fa), __fdividef(D2[q].y, fb));
-      const float aa = fabsf(y2[q].x), ab = fabsf(y2[q].y);
-      if (aa <= kYSmall) ysmall = fmaxf(ysmall, aa);
-      else large |= 1u << i0;
-      if (ab <= kYSmall) ysmall = fmaxf(ysmall, ab);
-      else large |= 1u << i1;
-      ymin = fminf(ymin, fminf(y2[q].x, y2[q].y));
+      ymax = fmaxf(ymax, fmaxf(fabsf(y2[q].x), fabsf(y2[q].y)));
     }
-    // positivity bracket: f + alpha Delta > 0 for all i  <=>  alpha < -1/min(y)
-    const float amax = (ymin < 0.f) ? -1.0f / ymin : INFINITY;
-    // warp-uniform series order from the warp's largest small |y|
-    const float wmax = __int_as_float(__reduce_max_sync(__activemask(), __float_as_int(ysmall)));
-    const int korder = (wmax <= 0.02f) ? 6 : (wmax <= 0.04f) ? 8 : (wmax <= 0.06f) ? 10 : 12;
-    float delta0 = 0.f, lam = 0.f;
-    int series_it = -1;
-    if (MODE >= 1) {
-#pragma unroll
-      for (int q = 0; q < 14; ++q) lam = fmaxf(lam, fmaxf(fabsf(y2[q].x), fabsf(y2[q].y)));
-    }
-    if (MODE == 1 && lam > 0.f) {
-      // learned guess: alpha = 2 + lambda * net(y / lambda), then at most two Newton steps
-      float x[Q];
-      const float il = 1.0f / lam;
-#pragma unroll
-      for (int i = 0; i < Q; ++i) x[i] = ((i & 1) ? y2[i >> 1].y : y2[i >> 1].x) * il;
-      delta0 = lam * mlp_forward(x);
-      series_it = 2;
-    }
+  }
+}
+
+// Alpha solve (from delta0 with at most series_it series steps when
+// series_it > 0, the learned guess), relaxation, store and statistics.
+template <bool CHECK, int MODE>
+__device__ __forceinline__ void node_finish(const Step27Args& a, int64_t n, float (&d)[Q], const float2 (&D2)[14],
+                                            const float2 (&y2)[14], float ymax, bool bad, float delta0,
+                                            int series_it) {
+  float* __restrict__ dst = static_cast<float*>(a.dst);
+  AlphaOut al{0.f, 0.f, 0u, false, false};
+  double dH = 0.0;
+  bool guess_miss = false;
+  if (a.alpha_mode != 0) {
+    const float lam = ymax;
     // float-pair polish above this error scale (the FP32 rounding of G_L stays below ~5e-7 GLabs)
     const float pthr = (float)(a.tol_dH * 1e6), tdh = (float)a.tol_dH;
-    switch (korder) {
-      case 6: al = alpha_solve32<6>(D2, y2, d, large, amax, a.max_newton, pthr, tdh, MODE != 1, delta0, series_it); break;
-      case 8: al = alpha_solve32<8>(D2, y2, d, large, amax, a.max_newton, pthr, tdh, MODE != 1, delta0, series_it); break;
-      case 10: al = alpha_solve32<10>(D2, y2, d, large, amax, a.max_newton, pthr, tdh, MODE != 1, delta0, series_it); break;
-      default: al = alpha_solve32<12>(D2, y2, d, large, amax, a.max_newton, pthr, tdh, MODE != 1, delta0, series_it); break;
-    }
+    al = alpha_solve32<kSeriesK>(D2, y2, d, ymax, a.max_newton, pthr, tdh, MODE != 1, delta0, series_it);
     if (MODE == 1 && al.fallback) {
       // the guess did not converge in two steps: plain Newton from alpha = 2
       guess_miss = true;
       const unsigned it0 = al.iters;
-      switch (korder) {
-        case 6: al = alpha_solve32<6>(D2, y2, d, large, amax, a.max_newton, pthr, tdh); break;
-        case 8: al = alpha_solve32<8>(D2, y2, d, large, amax, a.max_newton, pthr, tdh); break;
-        case 10: al = alpha_solve32<10>(D2, y2, d, large, amax, a.max_newton, pthr, tdh); break;
-        default: al = alpha_solve32<12>(D2, y2, d, large, amax, a.max_newton, pthr, tdh); break;
-      }
+      al = alpha_solve32<kSeriesK>(D2, y2, d, ymax, a.max_newton, pthr, tdh);
       al.iters += it0;
     }
     if (MODE == 2 && !al.fallback && lam > 0.f && (n % a.harvest_stride) == 0) {
@@ -768,7 +873,7 @@ __device__ __forceinline__ void node_update(const Step27Args& a, int64_t n, floa
     }
   }
   unsigned flags = 0;
-  if (!isfinite(rho) || !isfinite(u[0]) || !isfinite(u[1]) || !isfinite(u[2])) flags |= 0x1u;
+  if (bad) flags |= 0x1u;
   if (al.fallback) flags |= 0x2u;
   if (CHECK && dH > a.tol_dH) flags |= 0x8u;
   const float ab = (2.0f + al.delta) * (float)a.beta;
@@ -789,6 +894,27 @@ __device__ __forceinline__ void node_update(const Step27Args& a, int64_t n, floa
   }
 }
 
+// Everything after the gather: moments, equilibrium, alpha, relaxation, store.
+template <bool CHECK, int MODE>
+__device__ __forceinline__ void node_update(const Step27Args& a, int64_t n, float (&d)[Q]) {
+  float2 D2[14], y2[14];
+  float ymax;
+  bool bad;
+  node_prepare(d, a.alpha_mode != 0, D2, y2, ymax, bad);
+  float delta0 = 0.f;
+  int series_it = -1;
+  if (MODE == 1 && a.alpha_mode != 0 && ymax > 0.f) {
+    // learned guess: alpha = 2 + lambda * net(y / lambda), then at most two Newton steps
+    float x[Q];
+    const float il = 1.0f / ymax;
+#pragma unroll
+    for (int i = 0; i < Q; ++i) x[i] = ((i & 1) ? y2[i >> 1].y : y2[i >> 1].x) * il;
+    delta0 = ymax * mlp_forward(x);
+    series_it = 2;
+  }
+  node_finish<CHECK, MODE>(a, n, d, D2, y2, ymax, bad, delta0, series_it);
+}
+
 // Direct variant: one thread per node, the 27 pulls are plain global loads.
 template <bool CHECK, int MINB, int MODE = 0>
 __global__ void __launch_bounds__(128, MINB) d3q27_fp32_kernel(const Step27Args a) {
@@ -799,6 +925,25 @@ __global__ void __launch_bounds__(128, MINB) d3q27_fp32_kernel(const Step27Args 
   float d[Q];
   gather(a, static_cast<const float*>(a.src), n, t, d);
   node_update<CHECK, MODE>(a, n, d);
+}
+
+// Persistent variant: a fixed grid (every SM full) whose warps stride over
+// chunks of 32 consecutive nodes, so that no block waits for its slowest warp
+// before the SM can start new work.
+template <bool CHECK, int MINB, int MODE = 0>
+__global__ void __launch_bounds__(128, MINB) d3q27_fp32_persistent_kernel(const Step27Args a) {
+  const int64_t nchunks = (a.N + 31) / 32;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x / 32);
+  const int lane = threadIdx.x & 31;
+  for (int64_t c = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); c < nchunks; c += warps) {
+    const int64_t n = c * 32 + lane;
+    if (n >= a.N) continue;
+    const uint8_t t = __ldg(a.ntype + n);
+    if (t == NT_SKIP) continue;
+    float d[Q];
+    gather(a, static_cast<const float*>(a.src), n, t, d);
+    node_update<CHECK, MODE>(a, n, d);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -928,6 +1073,40 @@ void launch_d3q27_fp64(const Step27Args& a, cudaStream_t s) {
   d3q27_fp64_kernel<<<(unsigned)blocks, threads, 0, s>>>(a);
 }
 
+// Learned-alpha step with tensor-core inference: a persistent 128-thread
+// block walks tiles of 128 consecutive nodes; per tile every thread gathers
+// and prepares its node, the block runs the network on the tile with
+// tcgen05.mma (mlp_tc_tile), and each thread finishes its node from the guess.
+__global__ void __launch_bounds__(128, 2) d3q27_fp32_learned_tc_kernel(const Step27Args a) {
+  extern __shared__ __align__(128) unsigned char smraw[];
+  MlpTcSmem& s = *reinterpret_cast<MlpTcSmem*>(smraw);
+  mlp_tc_setup(s, a.mlp);
+  const float* __restrict__ src = static_cast<const float*>(a.src);
+  const int64_t ntiles = (a.N + 127) / 128;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t n = tile * 128 + threadIdx.x;
+    const uint8_t t = (n < a.N) ? __ldg(a.ntype + n) : (uint8_t)NT_SKIP;
+    float d[Q];
+    float2 D2[14], y2[14];
+    float ymax = 0.f;
+    bool bad = false;
+    float x[Q];
+    if (t != NT_SKIP) {
+      gather(a, src, n, t, d);
+      node_prepare(d, true, D2, y2, ymax, bad);
+      const float il = ymax > 0.f ? 1.0f / ymax : 0.f;
+#pragma unroll
+      for (int i = 0; i < Q; ++i) x[i] = ((i & 1) ? y2[i >> 1].y : y2[i >> 1].x) * il;
+    } else {
+#pragma unroll
+      for (int i = 0; i < Q; ++i) x[i] = 0.f;
+    }
+    const float out = mlp_tc_tile(s, x, &a.stats->status);
+    if (t != NT_SKIP) node_finish<false, 1>(a, n, d, D2, y2, ymax, bad, ymax * out, ymax > 0.f ? 2 : -1);
+  }
+  mlp_tc_teardown(s);
+}
+
 bool staged_eligible(const Step27Args& a) {
   // 16-byte aligned row segments: x rows and planes in multiples of 4 floats
   return a.nx % 4 == 0 && a.plane % 4 == 0 && a.ny >= 3 && a.nz >= 3;
@@ -953,6 +1132,35 @@ void launch_staged(const Step27Args& a, cudaStream_t s) {
 void launch_d3q27_fp32(const Step27Args& a, cudaStream_t s) {
   const int threads = 128;
   const int64_t blocks = (a.N + threads - 1) / threads;
+  if (a.alpha_mode == 2 && !a.check_dH && !a.harvest && a.mlp) {
+    // learned alpha: tensor-core inference over 128-node tiles, persistent blocks
+    static int bps = -1, sms = 0;
+    if (bps < 0) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, d3q27_fp32_learned_tc_kernel, 128, sizeof(MlpTcSmem));
+      bps = bps < 1 ? 1 : (bps > 4 ? 4 : bps);  // at most 4 blocks x 128 TMEM columns per SM
+    }
+    const int64_t ntiles = (a.N + 127) / 128;
+    const int64_t grid = std::min<int64_t>(ntiles, (int64_t)sms * bps);
+    d3q27_fp32_learned_tc_kernel<<<(unsigned)grid, 128, sizeof(MlpTcSmem), s>>>(a);
+    return;
+  }
+  if (a.variant == 3 && !a.check_dH && !a.harvest) {
+    static int bps = -1, sms = 0;
+    if (bps < 0) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, d3q27_fp32_persistent_kernel<false, 4, 0>, 128, 0);
+      if (bps < 1) bps = 1;
+    }
+    const int64_t grid = std::min<int64_t>(blocks, (int64_t)sms * bps);
+    if (a.alpha_mode == 2) d3q27_fp32_persistent_kernel<false, 4, 1><<<(unsigned)grid, threads, 0, s>>>(a);
+    else d3q27_fp32_persistent_kernel<false, 4, 0><<<(unsigned)grid, threads, 0, s>>>(a);
+    return;
+  }
   if (a.variant == 2 && !a.check_dH && !a.harvest && staged_eligible(a)) {
     if (a.alpha_mode == 2) launch_staged<false, 1>(a, s);
     else launch_staged<false, 0>(a, s);

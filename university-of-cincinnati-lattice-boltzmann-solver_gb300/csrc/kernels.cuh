@@ -49,7 +49,7 @@ struct Step27Args {
   int harvest_stride;
 };
 
-constexpr int kFp32Variants = 3;  // 0: direct, 1: direct with 4 blocks/SM, 2: bulk-copy staged
+constexpr int kFp32Variants = 4;  // 0: direct, 1: direct with 4 blocks/SM, 2: bulk-copy staged, 3: persistent warps
 // Bytes allocated before and after each population buffer (never written):
 // room for the staged kernel's row-segment copies that start 4 floats before
 // a plane or run up to a tile past its end.
