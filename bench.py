@@ -40,6 +40,9 @@ NU = 2e-5
 NOISE = 5e-3
 SEED = 1234 + 5
 BYTES_PER_NODE_FP32 = 216  # 27 x 4 B read + 27 x 4 B written
+# DRAM bytes (read + written) per node of the step kernel, from an ncu capture of a
+# 256x128x128 launch of the same workload (traffic grows in proportion to the nodes)
+DRAM_BYTES_PER_NODE_NCU = 223
 BYTES_PER_NODE_FP64 = 432
 
 
@@ -237,7 +240,7 @@ def main():
     ap.add_argument("--size", default=None, help="NXxNYxNZ override (profiling runs on a smaller box)")
     ap.add_argument("--alpha", default="newton", choices=["newton", "fixed2"],
                     help="alpha of the timed path (fixed2 = LBGK limit, to separate the alpha solve's cost)")
-    ap.add_argument("--variant", type=int, default=None, choices=[0, 1, 2, 3],
+    ap.add_argument("--variant", type=int, default=None, choices=[0, 1, 2, 3, 4, 5],
                     help="step-kernel variant instead of the autotuner's choice")
     ap.add_argument("--profile", action="store_true",
                     help="timed steps only: no validation, end-to-end, FP64 or CPU legs (for ncu captures)")
@@ -284,7 +287,7 @@ def main():
     if args.variant is None:
         variant, variant_ms = ctx.autotune(0, reps=3)
     else:
-        variant, variant_ms = args.variant, np.full(4, np.nan)
+        variant, variant_ms = args.variant, np.full(6, np.nan)
         ctx.set_kernel_variant(0, variant)
     ctx.sync()
     if pg:
@@ -311,7 +314,7 @@ def main():
     if args.profile:
         if rank == 0:
             print(json.dumps({"profile_run": True, "size": [NX, NY, NZ], "alpha": args.alpha, "variant": variant,
-                              "variant_ms": list(variant_ms[:4]), "mlups": value,
+                              "variant_ms": list(variant_ms[:6]), "mlups": value,
                               "ms_per_step": per_launch_s * 1e3, "achieved_gbs": achieved}), flush=True)
         ctx.close()
         return
@@ -368,9 +371,11 @@ def main():
             "config": {"workload": f"D3Q27 boundary layer {NX}x{NY}x{NZ}, FP32 deviation storage, Newton alpha",
                        "alpha": "newton", "storage": "fp32_dev", "nu": NU, "u_in": U_IN[0], "noise": NOISE,
                        "l2": "inputs (7.2 GB) larger than L2, no flush", "parallelism": f"replicas x{world}",
-                       "kernel_variant": variant, "variant_ms": [float(x) for x in variant_ms[:4]]},
+                       "kernel_variant": variant, "variant_ms": [float(x) for x in variant_ms[:6]]},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                         "frac": achieved / peak, "traffic": DRAM_BYTES_PER_NODE_NCU * nodes_per_step,
+                         "traffic_note": "bytes per launch: ncu DRAM bytes per node of a 256x128x128 launch x nodes",
+                         "peak_kind": peak_kind,
                          "bytes_per_node": BYTES_PER_NODE_FP32},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "note": "upload + K steps + download through the C ABI, pinned host FP64 FAB"},

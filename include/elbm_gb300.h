@@ -99,7 +99,7 @@ typedef struct {
 typedef struct {
   int64_t node_updates;     /* fluid nodes advanced, summed over steps */
   int64_t newton_iters;     /* total Newton iterations (scalar or per-population) */
-  int64_t exact_path_nodes; /* FP32 path: nodes solved with per-population logarithms */
+  int64_t exact_path_nodes; /* FP32 path: nodes with some |Delta_i/f_i| > 0.1 (solved out of line) */
   int64_t fallbacks;        /* alpha solves that fell back */
   uint32_t status;          /* ELBM_ST_* flags */
   uint32_t pad;
@@ -187,9 +187,10 @@ int elbm_level_step(elbm_ctx* ctx, int lvl, int nsteps, elbm_stats* stats);
  * reference has no counterpart (it has one code path per lattice). */
 int elbm_autotune(elbm_ctx* ctx, int lvl, int reps, int* chosen, double* ms_per_variant);
 
-/* Use kernel variant v (0: direct loads; 1: direct, register-capped for
- * occupancy; 2: rows staged in shared memory by bulk copies, persistent;
- * 3: direct loads, persistent warps striding over 32-node chunks) for
+/* Use kernel variant v (0: direct loads; 1, 4, 5: direct, registers capped
+ * for 4, 5, 6 blocks of 128 threads per SM; 2: rows staged in shared memory
+ * by bulk copies, persistent; 3: direct loads, persistent warps striding over
+ * 32-node chunks) for
  * the level's FP32 D3Q27 steps, instead of the autotuner's choice.  Variant 2
  * applies to boxes with nx and the plane size multiples of 4 and ny, nz >= 3;
  * other boxes fall back to variant 0.  No counterpart in the reference. */

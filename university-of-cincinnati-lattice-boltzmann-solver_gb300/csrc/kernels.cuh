@@ -25,8 +25,12 @@ struct Step27Args {
   const void* src;  // post-collision populations of the previous step, Q planes
   void* dst;        // post-collision populations of this step
   int64_t plane;    // elements between population planes (>= N, padded)
-  int nx, ny, nz;
-  int64_t N;
+  int nx, ny, nz;   // box dimensions when the level has one box
+  int64_t N;        // nodes of the level (all boxes, each padded to whole 32-node chunks)
+  int nbox;               // boxes of the level
+  const int32_t* chunk_box;  // box of every 32-node chunk (nbox > 1)
+  const int4* boxdim;        // nx, ny, nz of every box (nbox > 1)
+  const int32_t* xsrc;       // cross-box source index per population of a boundary record (-1: none)
   const uint8_t* ntype;   // NodeType per node
   const int32_t* bidx;    // boundary record per boundary node
   const uint16_t* words;  // Q link words per boundary record
@@ -49,7 +53,9 @@ struct Step27Args {
   int harvest_stride;
 };
 
-constexpr int kFp32Variants = 4;  // 0: direct, 1: direct with 4 blocks/SM, 2: bulk-copy staged, 3: persistent warps
+// 0: direct; 1, 4, 5: direct with registers capped for 4, 5, 6 blocks of 128 threads per SM;
+// 2: bulk-copy staged; 3: persistent warps
+constexpr int kFp32Variants = 6;
 // Bytes allocated before and after each population buffer (never written):
 // room for the staged kernel's row-segment copies that start 4 floats before
 // a plane or run up to a tile past its end.

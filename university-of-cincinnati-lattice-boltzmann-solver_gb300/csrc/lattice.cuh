@@ -50,8 +50,14 @@ ELBM_HD constexpr int opp27(int i) { return find27(-cx27(i), -cy27(i), -cz27(i))
 //   bits 5-9  : source node offset (dx+1) + 3(dy+1) + 9(dz+1), dx,dy,dz in {-1,0,1}; 13 = the node itself
 //   bits 10-12: kind
 // LK_IBB: interpolated bounce-back; source population = the wall-ward one, the
-// offset field holds the second fluid node (13 = none), the fraction is in a float array.
-enum LinkKind : uint16_t { LK_PULL = 0, LK_EQ = 1, LK_IBB = 2, LK_KEEP = 3 };
+// offset field holds the second fluid node (13 = none; kOffXbox = a node of
+// another box, its level index in the cross-box array), the fraction is in a
+// float array.
+// LK_XBOX: pull the source population from a node of another box of the level,
+// whose level index is in the cross-box array (one int32 per population of a
+// boundary record).
+enum LinkKind : uint16_t { LK_PULL = 0, LK_EQ = 1, LK_IBB = 2, LK_KEEP = 3, LK_XBOX = 4 };
+constexpr int kOffXbox = 27;
 ELBM_HD constexpr uint16_t link_word(int kind, int pop, int off) {
   return (uint16_t)((kind << 10) | (off << 5) | pop);
 }

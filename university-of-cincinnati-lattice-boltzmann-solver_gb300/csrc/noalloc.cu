@@ -55,9 +55,8 @@ namespace elbm {
 struct NoallocTarget {
   int device;
   cudaStream_t stream;
-  float* pops;      // population buffer that becomes current
-  float* other;     // the second population buffer (made identical)
-  size_t pop_bytes; // bytes of one population buffer
+  float* pops;   // the box's nodes in the current population buffer (plane stride `plane`)
+  float* other;  // the box's nodes in the second buffer (made identical)
   int nx, ny, nz, ngrow;
   int64_t N, plane;
 };
@@ -111,7 +110,8 @@ extern "C" int elbm_upload_level_noalloc(elbm_ctx* ctx, int lvl, int box, const 
   dim3 grid((unsigned)((t.N + 255) / 256), Q27);
   stage_to_dev32_kernel<<<grid, 256, 0, t.stream>>>(stage, t.pops, t.N, t.plane);
   if (cudaGetLastError() != cudaSuccess) return noalloc_fail(ctx, ELBM_E_CUDA, "conversion launch failed");
-  if (cudaMemcpyAsync(t.other, t.pops, t.pop_bytes, cudaMemcpyDeviceToDevice, t.stream) != cudaSuccess)
+  if (cudaMemcpy2DAsync(t.other, t.plane * sizeof(float), t.pops, t.plane * sizeof(float), t.N * sizeof(float), Q27,
+                        cudaMemcpyDeviceToDevice, t.stream) != cudaSuccess)
     return noalloc_fail(ctx, ELBM_E_CUDA, "buffer copy failed");
   // the staging buffer is shared by every call: finish before returning so the next call may reuse it
   if (cudaStreamSynchronize(t.stream) != cudaSuccess) return noalloc_fail(ctx, ELBM_E_CUDA, "sync failed");

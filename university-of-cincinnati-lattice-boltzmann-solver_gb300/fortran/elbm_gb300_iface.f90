@@ -40,13 +40,15 @@ module elbm_gb300_iface
     integer(c_int64_t) :: node_updates, newton_iters, exact_path_nodes, fallbacks
     integer(c_int32_t) :: status, pad
     real(c_double) :: max_abs_dH
-    integer(c_int64_t) :: dh_over_tol
+    integer(c_int64_t) :: dh_over_tol, guess_misses
     real(c_double) :: kernel_ms
   end type
 
   public :: elbm_create, elbm_destroy, elbm_level_register, elbm_set_d3q27_params, elbm_set_links, &
     elbm_upload_level, elbm_download_level, elbm_download_alpha, elbm_level_step, elbm_sync, &
-    elbm_set_d3q39_params, elbm_upload_level39, elbm_download_level39
+    elbm_set_d3q39_params, elbm_upload_level39, elbm_download_level39, elbm_mark_triangles, &
+    elbm_upload_level_noalloc, elbm_autotune, elbm_set_kernel_variant, elbm_alpha_harvest, &
+    elbm_alpha_mlp_train, elbm_set_alpha_mlp
 
   interface
     integer(c_int) function elbm_create(device, ctx) bind(c, name="elbm_create")
@@ -125,11 +127,65 @@ module elbm_gb300_iface
       integer(c_int), value :: lvl, box
       type(c_ptr), value :: fout, gout, lm, w_vel, alpha, macro  ! c_loc(...) or c_null_ptr
     end function
+    integer(c_int) function elbm_mark_triangles(nx, ny, nz, origin, dx, ntri, tri, state) &
+        bind(c, name="elbm_mark_triangles")
+      import :: c_int, c_double, c_int32_t
+      integer(c_int), value :: nx, ny, nz, ntri
+      real(c_double), intent(in) :: origin(3)
+      real(c_double), value :: dx
+      real(c_double), intent(in) :: tri(9, *)          ! vertex coordinates of each triangle
+      integer(c_int32_t), intent(inout) :: state(*)   ! 27 components of nx*ny*nz (no ghosts)
+    end function
+    integer(c_int) function elbm_upload_level_noalloc(ctx, lvl, box, fout) bind(c, name="elbm_upload_level_noalloc")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl, box
+      real(c_double), intent(in) :: fout(*)
+    end function
+    integer(c_int) function elbm_autotune(ctx, lvl, reps, chosen, ms_per_variant) bind(c, name="elbm_autotune")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl, reps
+      integer(c_int), intent(out) :: chosen
+      real(c_double), intent(out) :: ms_per_variant(8)
+    end function
+    integer(c_int) function elbm_set_kernel_variant(ctx, lvl, variant) bind(c, name="elbm_set_kernel_variant")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl, variant
+    end function
+    integer(c_int) function elbm_alpha_harvest(ctx, lvl, nsteps, stride, records, capacity, count) &
+        bind(c, name="elbm_alpha_harvest")
+      import :: c_int, c_ptr, c_float, c_int64_t
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl, nsteps, stride
+      real(c_float), intent(out) :: records(29, *)
+      integer(c_int64_t), value :: capacity
+      integer(c_int64_t), intent(out) :: count
+    end function
+    integer(c_int) function elbm_alpha_mlp_train(ctx, records, n, epochs, batch, lr, seed, weights, loss_per_epoch) &
+        bind(c, name="elbm_alpha_mlp_train")
+      import :: c_int, c_ptr, c_float, c_int64_t, c_double
+      type(c_ptr), value :: ctx
+      real(c_float), intent(in) :: records(29, *)
+      integer(c_int64_t), value :: n, seed
+      integer(c_int), value :: epochs, batch
+      real(c_float), value :: lr
+      real(c_float), intent(inout) :: weights(6017)
+      real(c_double), intent(out) :: loss_per_epoch(*)
+    end function
+    integer(c_int) function elbm_set_alpha_mlp(ctx, lvl, weights) bind(c, name="elbm_set_alpha_mlp")
+      import :: c_int, c_ptr, c_float
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl
+      real(c_float), intent(in) :: weights(6017)
+    end function
   end interface
 end module elbm_gb300_iface
 
 ! Example body of the reference's per-level collide-stream call with the
-! library (one box per level; `ctx` created once with elbm_create):
+! library (all boxes of the level registered at once; `ctx` created once with
+! elbm_create):
 !
 !   subroutine collision(level_step, fine, lvl)
 !     use elbm_gb300_iface
