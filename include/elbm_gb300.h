@@ -181,6 +181,35 @@ int elbm_download_alpha(elbm_ctx* ctx, int lvl, int box, double* alpha);
  * when given, the call synchronises and fills it. */
 int elbm_level_step(elbm_ctx* ctx, int lvl, int nsteps, elbm_stats* stats);
 
+/* Coarse-fine transfer between D3Q27 levels lvl - 1 (coarse) and lvl (fine),
+ * refinement ratio 2, nodal indexing (fine node X lies on coarse node X/2).
+ * Fine nodes whose state is a ghost code (1e7 .. 1.1e9) belong to the fine
+ * level's boxes, are stepped like fluid nodes, and are refilled from the
+ * coarse level.  Replaces interlevel_interpolation.f95:114-440 and
+ * fine_to_coarse.f95:28-64 for D3Q27 levels.
+ *   elbm_interlevel_setup: build the maps, after both levels' links.
+ *   elbm_fill_fine_ghosts: explosion, every fine ghost node <- nodal bilinear
+ *     interpolation of the coarse populations (negative or NaN: the entropic
+ *     equilibrium of the interpolated moments; repaired may be NULL).
+ *   elbm_average_down: coalescence, coarse nodes under valid fine nodes <-
+ *     the fine populations (nodal injection).
+ * Both act on the current (post-collision) populations; the driver calls
+ * them where the reference calls interlevel_interpolation and fine_to_coarse
+ * (loop.f95:116-128), on the sub-steps the reference does. */
+int elbm_interlevel_setup(elbm_ctx* ctx, int lvl);
+int elbm_fill_fine_ghosts(elbm_ctx* ctx, int lvl, int64_t* repaired);
+int elbm_average_down(elbm_ctx* ctx, int lvl);
+
+/* Advance D3Q27 levels 0 .. nlev-1 by ncycles coarse steps with 2:1
+ * sub-cycling (level l steps 2^l times per coarse step), the fine levels
+ * refilled from their coarse level before the first of their two steps
+ * completes and averaged down after the second, as in loop.f95:94-147.  The
+ * launches of two coarse cycles are captured once in a CUDA graph and
+ * replayed (the capture is redone when the levels' buffers, parameters or
+ * kernel variant change).  stats covers all levels (may be NULL).  No
+ * counterpart in the reference (its loop issues each phase from the host). */
+int elbm_amr_run(elbm_ctx* ctx, int nlev, int ncycles, elbm_stats* stats);
+
 /* Time every variant of the level's step kernel on its current state (reps
  * launches each, the state does not advance) and keep the fastest for
  * elbm_level_step.  chosen and ms_per_variant (room for 8) may be NULL.  The

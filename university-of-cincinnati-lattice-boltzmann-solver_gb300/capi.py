@@ -114,6 +114,10 @@ SIGNATURES = {
     "elbm_upload_level_noalloc": (_c_int, [_vp, _c_int, _c_int, _vp]),
     "elbm_autotune": (_c_int, [_vp, _c_int, _c_int, _vp, _vp]),
     "elbm_set_kernel_variant": (_c_int, [_vp, _c_int, _c_int]),
+    "elbm_interlevel_setup": (_c_int, [_vp, _c_int]),
+    "elbm_fill_fine_ghosts": (_c_int, [_vp, _c_int, _vp]),
+    "elbm_average_down": (_c_int, [_vp, _c_int]),
+    "elbm_amr_run": (_c_int, [_vp, _c_int, _c_int, _vp]),
     "elbm_mark_triangles": (_c_int, [_c_int, _c_int, _c_int, _vp, _c_double, _c_int, _vp, _vp]),
     "elbm_alpha_harvest": (_c_int, [_vp, _c_int, _c_int, _c_int, _vp, ct.c_int64, _vp]),
     "elbm_alpha_mlp_infer": (_c_int, [_vp, _vp, _vp, ct.c_int64, _vp, _vp]),
@@ -291,6 +295,24 @@ class Context:
         ms = np.zeros(8)
         self._check(self.lib.elbm_autotune(self.h, lvl, reps, ct.byref(chosen), _ptr(ms)))
         return chosen.value, ms
+
+    def interlevel_setup(self, lvl):
+        self._check(self.lib.elbm_interlevel_setup(self.h, lvl))
+
+    def fill_fine_ghosts(self, lvl):
+        """Explosion into level lvl from lvl - 1; returns the number of nodes set to equilibrium."""
+        r = ct.c_int64(0)
+        self._check(self.lib.elbm_fill_fine_ghosts(self.h, lvl, ct.byref(r)))
+        return r.value
+
+    def average_down(self, lvl):
+        self._check(self.lib.elbm_average_down(self.h, lvl))
+
+    def amr_run(self, nlev, ncycles):
+        """ncycles coarse steps of levels 0 .. nlev-1 with 2:1 sub-cycling (CUDA graph); returns stats."""
+        st = Stats()
+        self._check(self.lib.elbm_amr_run(self.h, nlev, ncycles, ct.byref(st)))
+        return st.as_dict()
 
     def set_kernel_variant(self, lvl, variant):
         self._check(self.lib.elbm_set_kernel_variant(self.h, lvl, variant))

@@ -78,6 +78,7 @@ struct Box {
   std::vector<uint16_t> h_words;   // Q per boundary node
   std::vector<double> h_qfrac;     // Q per boundary node
   std::vector<int32_t> h_xsrc;     // Q per boundary node (level index of a cross-box source, -1: none)
+  std::vector<int64_t> h_ghost;    // fine ghost nodes (state 1e7 .. 1.1e9), box-local index
   DevBuf<double> staging;  // FP64 packed staging for FP32 conversion
   // D3Q39: populations, g populations, multipliers, previous w, alpha and macroscopic fields
   DevBuf<uint8_t> buf[2];
@@ -112,7 +113,14 @@ struct Level {
   DevBuf<int32_t> chunk_box;
   DevBuf<int4> boxdim;
   DevBuf<float> alpha;      // per node (record_alpha)
+  DevBuf<unsigned long long> work;  // chunk counter of the persistent step variant
   bool links_ready = false; // every box's links decoded and uploaded
+  // coarse-fine transfer with level lvl - 1 (elbm_interlevel_setup)
+  DevBuf<int32_t> il_ghost, il_src, il_down_dst, il_down_src;
+  DevBuf<uint8_t> il_cnt;
+  DevBuf<unsigned long long> il_repaired;
+  int64_t il_nghost = 0, il_ndown = 0;
+  bool il_ready = false;
 };
 
 }  // namespace
@@ -124,6 +132,10 @@ struct elbm_ctx {
   std::string err;
   std::vector<Level> levels;
   DevBuf<DevStats> stats;
+  // CUDA graph of two coarse cycles of the AMR sub-cycle (elbm_amr_run)
+  cudaGraphExec_t amr_exec = nullptr;
+  int amr_nlev = 0;
+  uint64_t amr_key = 0;  // fingerprint of the level set-up the graph was captured for
 };
 
 namespace {
@@ -167,6 +179,10 @@ bool node_is_fluid(int32_t s0) {
   if (s0 >= 200 && s0 < 299) return false;
   return true;
 }
+
+// Fine nodes outside the level's valid region, filled from the coarse level
+// (loop.f95:71-89: 1e7 .. 1.1e9 ghost).
+bool node_is_ghost(int32_t s0) { return s0 >= 10000000 && s0 <= 1100000000; }
 
 size_t elem_size(int storage) { return storage == ELBM_STORE_FP64 ? sizeof(double) : sizeof(float); }
 
@@ -264,7 +280,7 @@ struct StateView {
 };
 
 int decode_link27(const int32_t* st, int64_t fab_plane, int64_t sidx, const int sstride[3], int ngs, int x, int y,
-                  int z, const Box& b, const Level& lv, int j, uint16_t& word, double& qf, int32_t& xs,
+                  int z, const Box& b, const Level& lv, int j, bool ghost, uint16_t& word, double& qf, int32_t& xs,
                   bool& interior, std::string& why) {
   qf = 0.0;
   xs = -1;
@@ -278,6 +294,11 @@ int decode_link27(const int32_t* st, int64_t fab_plane, int64_t sidx, const int 
       // the source lies in another box of the level (AMReX fills this box's
       // ghost cells from it; here the step reads it in place)
       const int64_t li = level_index(lv, b.lo[0] + x + dx, b.lo[1] + y + dy, b.lo[2] + z + dz);
+      if (li < 0 && ghost) {
+        // outermost ghost shell: the coarse level refills this node before it matters
+        word = link_word(LK_KEEP, j, 0);
+        return 0;
+      }
       if (li < 0) {
         why = "fluid link leaves the level's boxes (coarse-fine or domain edge without a boundary code)";
         return ELBM_E_UNSUPPORTED;
@@ -498,6 +519,7 @@ void elbm_destroy(elbm_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->amr_exec) cudaGraphExecDestroy(c->amr_exec);
   c->levels.clear();
   c->stats.reset();
   if (c->ev0) cudaEventDestroy(c->ev0);
@@ -564,6 +586,7 @@ int elbm_level_register(elbm_ctx* c, int lvl, int lattice, int storage, int nbox
     const size_t bytes = (size_t)lv.plane * Q27 * elem_size(storage);
     for (int s = 0; s < 2; ++s) CUDA_TRY(lv.pop[s].alloc(bytes, kPopGuardBytes), "population buffers");
     CUDA_TRY(lv.ntype.alloc(lv.plane), "node types");
+    CUDA_TRY(lv.work.alloc(1), "work counter");
     CUDA_TRY(cudaMemsetAsync(lv.ntype.p, 0, lv.plane, c->stream), "memset");
     std::vector<int32_t> cb(lv.plane / 32);
     std::vector<int4> bd(nbox);
@@ -627,7 +650,7 @@ int elbm_set_links(elbm_ctx* c, int lvl, int box, const int32_t* state, int ngro
   std::vector<uint16_t> words;
   std::vector<double> qfr;
   std::vector<int32_t> xsv;
-  std::vector<int64_t> bnodes;
+  std::vector<int64_t> bnodes, ghosts;
   int64_t fluid = 0;
   std::string why;
   for (int z = 0; z < b->nz; ++z)
@@ -637,6 +660,8 @@ int elbm_set_links(elbm_ctx* c, int lvl, int box, const int32_t* state, int ngro
         const int64_t s = ((int64_t)(z + g) * fy + (y + g)) * fx + (x + g);
         if (!node_is_fluid(state[s])) continue;
         ++fluid;
+        const bool ghost = node_is_ghost(state[s]);
+        if (ghost) ghosts.push_back(n);
         uint16_t w[Q27];
         double qv[Q27] = {0.0};
         int32_t xv[Q27];
@@ -645,8 +670,8 @@ int elbm_set_links(elbm_ctx* c, int lvl, int box, const int32_t* state, int ngro
         xv[0] = -1;
         for (int j = 1; j < Q27; ++j) {
           bool interior;
-          const int rc = decode_link27(state, fab_plane, s, sstride, g, x, y, z, *b, *lv, j, w[j], qv[j], xv[j],
-                                       interior, why);
+          const int rc = decode_link27(state, fab_plane, s, sstride, g, x, y, z, *b, *lv, j, ghost, w[j], qv[j],
+                                       xv[j], interior, why);
           if (rc) return fail(c, rc, "node (%d,%d,%d) population %d: %s", x + b->lo[0], y + b->lo[1], z + b->lo[2], j,
                               why.c_str());
           all_interior &= interior;
@@ -666,11 +691,13 @@ int elbm_set_links(elbm_ctx* c, int lvl, int box, const int32_t* state, int ngro
   b->h_words.swap(words);
   b->h_qfrac.swap(qfr);
   b->h_xsrc.swap(xsv);
+  b->h_ghost.swap(ghosts);
   b->fluid_nodes = fluid;
   b->boundary_nodes = (int64_t)b->h_bnodes.size();
   b->links_set = true;
   // once every box has its links, the level-wide tables go to the device
   lv->links_ready = false;
+  lv->il_ready = false;
   for (auto& bp : lv->boxes)
     if (!bp->links_set) return ELBM_OK;
   CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
@@ -795,6 +822,7 @@ Step27Args level_args27(elbm_ctx* c, Level& lv) {
   a.chunk_box = lv.chunk_box.p;
   a.boxdim = lv.boxdim.p;
   a.xsrc = lv.xsrc.p;
+  a.work_counter = lv.work.p;
   a.ntype = lv.ntype.p;
   a.bidx = lv.bidx.p;
   a.words = lv.words.p;
@@ -1047,6 +1075,206 @@ int elbm_alpha_mlp_train(elbm_ctx* c, const float* records, int64_t n, int epoch
   }
   CUDA_TRY(cudaMemcpy(weights, w.p, kMlpParams * sizeof(float), cudaMemcpyDeviceToHost), "weights");
   return ELBM_OK;
+}
+
+int elbm_interlevel_setup(elbm_ctx* c, int lvl) {
+  Level* fl = get_level(c, lvl);
+  Level* cl = lvl >= 1 ? get_level(c, lvl - 1) : nullptr;
+  if (!fl || !cl) return fail(c, ELBM_E_ARG, "levels %d and %d must both be registered", lvl - 1, lvl);
+  if (fl->lattice != ELBM_D3Q27 || cl->lattice != ELBM_D3Q27 || fl->storage != cl->storage)
+    return fail(c, ELBM_E_UNSUPPORTED, "coarse-fine transfer joins two D3Q27 levels of the same storage");
+  if (!fl->links_ready || !cl->links_ready) return fail(c, ELBM_E_STATE, "set the links of both levels first");
+  // explosion map: each fine ghost node from the 1, 2, 4 or 8 coarse nodes around it
+  std::vector<int32_t> gidx, gsrc;
+  std::vector<uint8_t> gcnt;
+  for (const auto& bp : fl->boxes) {
+    const Box& b = *bp;
+    for (int64_t n : b.h_ghost) {
+      const int X[3] = {b.lo[0] + (int)(n % b.nx), b.lo[1] + (int)((n / b.nx) % b.ny), b.lo[2] + (int)(n / ((int64_t)b.nx * b.ny))};
+      int lo[3], hi[3];
+      for (int a = 0; a < 3; ++a) {
+        lo[a] = (X[a] - ((X[a] % 2 + 2) % 2)) / 2;          // floor(X / 2)
+        hi[a] = ((X[a] % 2 + 2) % 2) ? lo[a] + 1 : lo[a];  // odd: the next coarse node too
+      }
+      int32_t src[8];
+      int k = 0;
+      for (int cz = lo[2]; cz <= hi[2]; ++cz)
+        for (int cy = lo[1]; cy <= hi[1]; ++cy)
+          for (int cxx = lo[0]; cxx <= hi[0]; ++cxx) {
+            const int64_t li = level_index(*cl, cxx, cy, cz);
+            if (li < 0)
+              return fail(c, ELBM_E_UNSUPPORTED, "fine ghost node (%d,%d,%d) lies outside the coarse level", X[0], X[1],
+                          X[2]);
+            src[k++] = (int32_t)li;
+          }
+      for (int m = k; m < 8; ++m) src[m] = src[0];
+      gidx.push_back((int32_t)(b.base + n));
+      gsrc.insert(gsrc.end(), src, src + 8);
+      gcnt.push_back((uint8_t)k);
+    }
+  }
+  // coalescence map: coarse fluid nodes under a valid fine fluid node
+  std::vector<int32_t> ddst, dsrc;
+  for (const auto& bp : cl->boxes) {
+    const Box& b = *bp;
+    for (int64_t n = 0; n < b.N; ++n) {
+      if (b.h_ntype[n] == NT_SKIP) continue;
+      const int C[3] = {b.lo[0] + (int)(n % b.nx), b.lo[1] + (int)((n / b.nx) % b.ny), b.lo[2] + (int)(n / ((int64_t)b.nx * b.ny))};
+      const int64_t fi = level_index(*fl, 2 * C[0], 2 * C[1], 2 * C[2]);
+      if (fi < 0) continue;
+      // the fine node must be a valid fluid node (not a ghost, not solid)
+      bool valid = false;
+      for (const auto& fp : fl->boxes) {
+        const Box& fb = *fp;
+        if (fi < fb.base || fi >= fb.base + fb.N) continue;
+        const int64_t ln = fi - fb.base;
+        valid = fb.h_ntype[ln] != NT_SKIP && !std::binary_search(fb.h_ghost.begin(), fb.h_ghost.end(), ln);
+      }
+      if (!valid) continue;
+      ddst.push_back((int32_t)(b.base + n));
+      dsrc.push_back((int32_t)fi);
+    }
+  }
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  fl->il_nghost = (int64_t)gidx.size();
+  fl->il_ndown = (int64_t)ddst.size();
+  CUDA_TRY(fl->il_ghost.alloc(std::max<size_t>(gidx.size(), 1)), "interlevel map");
+  CUDA_TRY(fl->il_src.alloc(std::max<size_t>(gsrc.size(), 1)), "interlevel map");
+  CUDA_TRY(fl->il_cnt.alloc(std::max<size_t>(gcnt.size(), 1)), "interlevel map");
+  CUDA_TRY(fl->il_down_dst.alloc(std::max<size_t>(ddst.size(), 1)), "interlevel map");
+  CUDA_TRY(fl->il_down_src.alloc(std::max<size_t>(dsrc.size(), 1)), "interlevel map");
+  CUDA_TRY(fl->il_repaired.alloc(1), "interlevel counter");
+  if (!gidx.empty()) {
+    CUDA_TRY(cudaMemcpy(fl->il_ghost.p, gidx.data(), gidx.size() * 4, cudaMemcpyHostToDevice), "map");
+    CUDA_TRY(cudaMemcpy(fl->il_src.p, gsrc.data(), gsrc.size() * 4, cudaMemcpyHostToDevice), "map");
+    CUDA_TRY(cudaMemcpy(fl->il_cnt.p, gcnt.data(), gcnt.size(), cudaMemcpyHostToDevice), "map");
+  }
+  if (!ddst.empty()) {
+    CUDA_TRY(cudaMemcpy(fl->il_down_dst.p, ddst.data(), ddst.size() * 4, cudaMemcpyHostToDevice), "map");
+    CUDA_TRY(cudaMemcpy(fl->il_down_src.p, dsrc.data(), dsrc.size() * 4, cudaMemcpyHostToDevice), "map");
+  }
+  fl->il_ready = true;
+  return ELBM_OK;
+}
+
+int elbm_fill_fine_ghosts(elbm_ctx* c, int lvl, int64_t* repaired) {
+  Level* fl = get_level(c, lvl);
+  Level* cl = lvl >= 1 ? get_level(c, lvl - 1) : nullptr;
+  if (!fl || !cl) return fail(c, ELBM_E_ARG, "unknown levels");
+  if (!fl->il_ready) return fail(c, ELBM_E_STATE, "call elbm_interlevel_setup first");
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  CUDA_TRY(cudaMemsetAsync(fl->il_repaired.p, 0, sizeof(unsigned long long), c->stream), "memset");
+  launch_explode(fl->storage == ELBM_STORE_FP32_DEV, cl->pop[cl->cur].p, cl->plane, fl->pop[fl->cur].p, fl->plane,
+                 fl->il_ghost.p, fl->il_src.p, fl->il_cnt.p, fl->il_nghost, fl->il_repaired.p, c->stream);
+  CUDA_TRY(cudaGetLastError(), "explosion launch");
+  if (repaired) {
+    unsigned long long r = 0;
+    CUDA_TRY(cudaMemcpyAsync(&r, fl->il_repaired.p, sizeof r, cudaMemcpyDeviceToHost, c->stream), "counter");
+    CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+    *repaired = (int64_t)r;
+  }
+  return ELBM_OK;
+}
+
+int elbm_average_down(elbm_ctx* c, int lvl) {
+  Level* fl = get_level(c, lvl);
+  Level* cl = lvl >= 1 ? get_level(c, lvl - 1) : nullptr;
+  if (!fl || !cl) return fail(c, ELBM_E_ARG, "unknown levels");
+  if (!fl->il_ready) return fail(c, ELBM_E_STATE, "call elbm_interlevel_setup first");
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  launch_average_down(fl->storage == ELBM_STORE_FP32_DEV, fl->pop[fl->cur].p, fl->plane, cl->pop[cl->cur].p, cl->plane,
+                      fl->il_down_dst.p, fl->il_down_src.p, fl->il_ndown, c->stream);
+  CUDA_TRY(cudaGetLastError(), "average-down launch");
+  return ELBM_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Launches of one step of a D3Q27 level (no host synchronisation: capturable).
+void enqueue_step27(elbm_ctx* c, Level& lv) {
+  Step27Args a = level_args27(c, lv);
+  a.check_dH = 0;
+  if (lv.storage == ELBM_STORE_FP64) launch_d3q27_fp64(a, c->stream);
+  else launch_d3q27_fp32(a, c->stream);
+  lv.cur ^= 1;
+}
+
+// One step of level l with the 2:1 sub-cycle of the finer levels below it, in
+// the reference's order (loop.f95:94-147, valid_levels): the level steps, then
+// its finer level takes two steps, refilled from this level before its first
+// (odd) step completes and averaged down onto this level after its second.
+void enqueue_cycle(elbm_ctx* c, int l, int nlev) {
+  enqueue_step27(c, c->levels[l]);
+  if (l + 1 >= nlev) return;
+  Level& fl = c->levels[l + 1];
+  Level& cl = c->levels[l];
+  for (int k = 0; k < 2; ++k) {
+    enqueue_cycle(c, l + 1, nlev);
+    if (k == 0)
+      launch_explode(fl.storage == ELBM_STORE_FP32_DEV, cl.pop[cl.cur].p, cl.plane, fl.pop[fl.cur].p, fl.plane,
+                     fl.il_ghost.p, fl.il_src.p, fl.il_cnt.p, fl.il_nghost, fl.il_repaired.p, c->stream);
+  }
+  launch_average_down(fl.storage == ELBM_STORE_FP32_DEV, fl.pop[fl.cur].p, fl.plane, cl.pop[cl.cur].p, cl.plane,
+                      fl.il_down_dst.p, fl.il_down_src.p, fl.il_ndown, c->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int elbm_amr_run(elbm_ctx* c, int nlev, int ncycles, elbm_stats* out) {
+  if (!c || nlev < 1 || nlev > 8 || ncycles < 0) return fail(c, ELBM_E_ARG, "bad AMR run arguments");
+  uint64_t key = 1469598103934665603ull;
+  for (int l = 0; l < nlev; ++l) {
+    Level* lv = get_level(c, l);
+    if (!lv || lv->lattice != ELBM_D3Q27 || !lv->params_set || lv->p27.check_dH || lv->p27.record_alpha)
+      return fail(c, ELBM_E_STATE, "level %d: a registered D3Q27 level without check mode or alpha recording", l);
+    if (const int rc = ready27(c, *lv)) return rc;
+    if (l > 0 && !lv->il_ready) return fail(c, ELBM_E_STATE, "level %d: call elbm_interlevel_setup first", l);
+    // the graph bakes in buffer addresses and parameters
+    const uintptr_t parts[4] = {(uintptr_t)lv->pop[0].p, (uintptr_t)lv->il_ghost.p, (uintptr_t)lv->p27.alpha_mode,
+                                (uintptr_t)lv->variant};
+    for (uintptr_t v : parts) key = (key ^ (uint64_t)v) * 1099511628211ull;
+    uint64_t pb;
+    std::memcpy(&pb, &lv->p27.nu, sizeof pb);
+    key = (key ^ pb) * 1099511628211ull;
+    key = (key ^ (uint64_t)lv->cur) * 1099511628211ull;
+  }
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  if (!c->amr_exec || c->amr_nlev != nlev || c->amr_key != key) {
+    if (c->amr_exec) {
+      cudaGraphExecDestroy(c->amr_exec);
+      c->amr_exec = nullptr;
+    }
+    // capture two coarse cycles: every level then takes an even number of steps, so
+    // its ping-pong buffers are back where they started and the graph can be replayed
+    std::vector<int> cur0(nlev);
+    for (int l = 0; l < nlev; ++l) cur0[l] = c->levels[l].cur;
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    for (int k = 0; k < 2; ++k) enqueue_cycle(c, 0, nlev);
+    const cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+    for (int l = 0; l < nlev; ++l) c->levels[l].cur = cur0[l];
+    if (ce != cudaSuccess) return cuda_fail(c, ce, "end capture");
+    const cudaError_t ie = cudaGraphInstantiate(&c->amr_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+      c->amr_exec = nullptr;
+      return cuda_fail(c, ie, "graph instantiate");
+    }
+    c->amr_nlev = nlev;
+    c->amr_key = key;
+  }
+  CUDA_TRY(cudaMemsetAsync(c->stats.p, 0, sizeof(DevStats), c->stream), "stats reset");
+  CUDA_TRY(cudaEventRecord(c->ev0, c->stream), "event");
+  for (int r = 0; r < ncycles / 2; ++r) CUDA_TRY(cudaGraphLaunch(c->amr_exec, c->stream), "graph launch");
+  if (ncycles % 2) enqueue_cycle(c, 0, nlev);  // an odd count: the last cycle by plain launches
+  CUDA_TRY(cudaGetLastError(), "AMR cycle");
+  CUDA_TRY(cudaEventRecord(c->ev1, c->stream), "event");
+  return finish_stats(c, out);
 }
 
 int elbm_sync(elbm_ctx* c) {

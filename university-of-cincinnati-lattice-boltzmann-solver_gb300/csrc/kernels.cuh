@@ -31,6 +31,7 @@ struct Step27Args {
   const int32_t* chunk_box;  // box of every 32-node chunk (nbox > 1)
   const int4* boxdim;        // nx, ny, nz of every box (nbox > 1)
   const int32_t* xsrc;       // cross-box source index per population of a boundary record (-1: none)
+  unsigned long long* work_counter;  // chunk counter of the persistent variant (zeroed before each launch)
   const uint8_t* ntype;   // NodeType per node
   const int32_t* bidx;    // boundary record per boundary node
   const uint16_t* words;  // Q link words per boundary record
@@ -64,5 +65,9 @@ constexpr size_t kPopGuardBytes = 1024;
 void launch_d3q27_fp64(const Step27Args& a, cudaStream_t s);
 void upload_alpha_mlp(const float* w_host, cudaStream_t s);
 void launch_d3q27_fp32(const Step27Args& a, cudaStream_t s);
+void launch_explode(bool fp32, const void* coarse, int64_t cplane, void* fine, int64_t fplane, const int32_t* ghost,
+                    const int32_t* src, const uint8_t* cnt, int64_t n, unsigned long long* repaired, cudaStream_t s);
+void launch_average_down(bool fp32, const void* fine, int64_t fplane, void* coarse, int64_t cplane, const int32_t* dst,
+                         const int32_t* src, int64_t n, cudaStream_t s);
 
 }  // namespace elbm
