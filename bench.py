@@ -338,9 +338,14 @@ def main():
     ctx.sync()
     te = time.perf_counter()
     ctx.upload(0, 0, host_in.numpy())
+    ctx.sync()
+    t_up = time.perf_counter() - te
     ctx.step(0, args.steps, want_stats=False)
+    ctx.sync()
+    t_steps = time.perf_counter() - te - t_up
     ctx.download(0, 0, host_out.numpy())
     e2e_s = time.perf_counter() - te
+    e2e_phases_ms = {"upload": t_up * 1e3, "steps": t_steps * 1e3, "download": (e2e_s - t_up - t_steps) * 1e3}
     e2e = nodes_per_step * args.steps * world / e2e_s / 1e6
     h2d = f0.nbytes / args.steps
     d2h = f0.nbytes / args.steps
@@ -378,7 +383,8 @@ def main():
                          "peak_kind": peak_kind,
                          "bytes_per_node": BYTES_PER_NODE_FP32},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "note": "upload + K steps + download through the C ABI, pinned host FP64 FAB"},
+                    "note": "upload + K steps + download through the C ABI, pinned host FP64 FAB",
+                    "phases_ms": e2e_phases_ms},
             "gpu_launches": args.steps,
             "clocks": clk,
             "wall_ms_per_step": wall / args.steps * 1e3,

@@ -48,7 +48,8 @@ module elbm_gb300_iface
     elbm_upload_level, elbm_download_level, elbm_download_alpha, elbm_level_step, elbm_sync, &
     elbm_set_d3q39_params, elbm_upload_level39, elbm_download_level39, elbm_mark_triangles, &
     elbm_upload_level_noalloc, elbm_autotune, elbm_set_kernel_variant, elbm_alpha_harvest, &
-    elbm_alpha_mlp_train, elbm_set_alpha_mlp
+    elbm_alpha_mlp_train, elbm_set_alpha_mlp, elbm_interlevel_setup, elbm_fill_fine_ghosts, &
+    elbm_average_down, elbm_amr_run
 
   interface
     integer(c_int) function elbm_create(device, ctx) bind(c, name="elbm_create")
@@ -179,6 +180,28 @@ module elbm_gb300_iface
       type(c_ptr), value :: ctx
       integer(c_int), value :: lvl
       real(c_float), intent(in) :: weights(6017)
+    end function
+    integer(c_int) function elbm_interlevel_setup(ctx, lvl) bind(c, name="elbm_interlevel_setup")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl
+    end function
+    integer(c_int) function elbm_fill_fine_ghosts(ctx, lvl, repaired) bind(c, name="elbm_fill_fine_ghosts")
+      import :: c_int, c_ptr, c_int64_t
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl
+      integer(c_int64_t), intent(out) :: repaired
+    end function
+    integer(c_int) function elbm_average_down(ctx, lvl) bind(c, name="elbm_average_down")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl
+    end function
+    integer(c_int) function elbm_amr_run(ctx, nlev, ncycles, stats) bind(c, name="elbm_amr_run")
+      import :: c_int, c_ptr, elbm_stats
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: nlev, ncycles
+      type(elbm_stats), intent(out) :: stats
     end function
   end interface
 end module elbm_gb300_iface
