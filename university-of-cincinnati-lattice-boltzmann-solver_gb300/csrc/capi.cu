@@ -206,8 +206,14 @@ template <typename T>
 cudaError_t fab_to_packed(const T* host, T* dev, const Box& b, int ngrow, int ncomp, int64_t plane, cudaStream_t s) {
   const int fx = b.nx + 2 * ngrow, fy = b.ny + 2 * ngrow, fz = b.nz + 2 * ngrow;
   if (ngrow == 0) {
-    return cudaMemcpy2DAsync(dev, plane * sizeof(T), host, b.N * sizeof(T), b.N * sizeof(T), ncomp,
-                             cudaMemcpyHostToDevice, s);
+    // whole component planes: plain copies (one when the device planes are not padded)
+    if (plane == b.N) return cudaMemcpyAsync(dev, host, (size_t)b.N * ncomp * sizeof(T), cudaMemcpyHostToDevice, s);
+    for (int q = 0; q < ncomp; ++q) {
+      const cudaError_t e = cudaMemcpyAsync(dev + (int64_t)q * plane, host + (int64_t)q * b.N, (size_t)b.N * sizeof(T),
+                                            cudaMemcpyHostToDevice, s);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
   }
   for (int q = 0; q < ncomp; ++q) {
     cudaMemcpy3DParms p{};
@@ -227,8 +233,13 @@ template <typename T>
 cudaError_t packed_to_fab(const T* dev, T* host, const Box& b, int ngrow, int ncomp, int64_t plane, cudaStream_t s) {
   const int fx = b.nx + 2 * ngrow, fy = b.ny + 2 * ngrow, fz = b.nz + 2 * ngrow;
   if (ngrow == 0) {
-    return cudaMemcpy2DAsync(host, b.N * sizeof(T), dev, plane * sizeof(T), b.N * sizeof(T), ncomp,
-                             cudaMemcpyDeviceToHost, s);
+    if (plane == b.N) return cudaMemcpyAsync(host, dev, (size_t)b.N * ncomp * sizeof(T), cudaMemcpyDeviceToHost, s);
+    for (int q = 0; q < ncomp; ++q) {
+      const cudaError_t e = cudaMemcpyAsync(host + (int64_t)q * b.N, dev + (int64_t)q * plane, (size_t)b.N * sizeof(T),
+                                            cudaMemcpyDeviceToHost, s);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
   }
   for (int q = 0; q < ncomp; ++q) {
     cudaMemcpy3DParms p{};

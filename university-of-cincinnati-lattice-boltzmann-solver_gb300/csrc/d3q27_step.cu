@@ -1114,18 +1114,21 @@ __global__ void __launch_bounds__(128, 2) d3q27_fp32_learned_tc_kernel(const Ste
     float2 D2[14], y2[14];
     float ymax = 0.f;
     bool bad = false;
-    float x[Q];
     if (t != NT_SKIP) {
       gather(a, src, n, t, d);
       node_prepare(d, true, D2, y2, ymax, bad);
-      const float il = ymax > 0.f ? 1.0f / ymax : 0.f;
-#pragma unroll
-      for (int i = 0; i < Q; ++i) x[i] = ((i & 1) ? y2[i >> 1].y : y2[i >> 1].x) * il;
-    } else {
-#pragma unroll
-      for (int i = 0; i < Q; ++i) x[i] = 0.f;
     }
-    const float out = mlp_tc_tile(s, x, &a.stats->status);
+    // features y / max|y| straight into the tile (zeros for a thread without a node)
+    const float il = (t != NT_SKIP && ymax > 0.f) ? 1.0f / ymax : 0.f;
+#pragma unroll
+    for (int q = 0; q < 14; ++q) {
+      const float v0 = (t != NT_SKIP) ? y2[q].x * il : 0.f;
+      const float v1 = (t != NT_SKIP && 2 * q + 1 < Q) ? y2[q].y * il : 0.f;
+      mlp_tc_put(s, 2 * q, v0, v1);
+    }
+    mlp_tc_put(s, 28, 0.f, 0.f);
+    mlp_tc_put(s, 30, 0.f, 0.f);
+    const float out = mlp_tc_run(s, &a.stats->status);
     if (t != NT_SKIP) node_finish<false, 1>(a, n, d, D2, y2, ymax, bad, ymax * out, ymax > 0.f ? 2 : -1);
   }
   mlp_tc_teardown(s);

@@ -164,15 +164,25 @@ __device__ __forceinline__ void mlp_tc_teardown(MlpTcSmem& s) {
 // One tile (all 128 threads, block-uniform call): x = this thread's 27
 // features (zeros for a thread without a node); returns the network output.
 // Each call completes the barrier twice, so the parities are 0 then 1.
+// Features k and k + 1 (k even) of this thread's row of the input tile.
+__device__ __forceinline__ void mlp_tc_put(MlpTcSmem& s, int k, float v0, float v1) {
+  __nv_bfloat162 v;
+  v.x = __float2bfloat16_rn(v0);
+  v.y = __float2bfloat16_rn(v1);
+  *reinterpret_cast<__nv_bfloat162*>(&s.a1[tc_off(threadIdx.x, k, kTcK1 / 8)]) = v;
+}
+
+__device__ __forceinline__ float mlp_tc_run(MlpTcSmem& s, unsigned* status);
+
 __device__ __forceinline__ float mlp_tc_tile(MlpTcSmem& s, const float (&x)[kMlpIn], unsigned* status) {
-  const int r = threadIdx.x;
 #pragma unroll
-  for (int k = 0; k < kTcK1; k += 2) {
-    __nv_bfloat162 v;
-    v.x = __float2bfloat16_rn(k < kMlpIn ? x[k] : 0.f);
-    v.y = __float2bfloat16_rn(k + 1 < kMlpIn ? x[k + 1] : 0.f);
-    *reinterpret_cast<__nv_bfloat162*>(&s.a1[tc_off(r, k, kTcK1 / 8)]) = v;
-  }
+  for (int k = 0; k < kTcK1; k += 2) mlp_tc_put(s, k, k < kMlpIn ? x[k] : 0.f, k + 1 < kMlpIn ? x[k + 1] : 0.f);
+  return mlp_tc_run(s, status);
+}
+
+// The network on the tile whose features every thread has put (mlp_tc_put).
+__device__ __forceinline__ float mlp_tc_run(MlpTcSmem& s, unsigned* status) {
+  const int r = threadIdx.x;
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   tc_fence_before();
   __syncthreads();
