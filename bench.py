@@ -42,7 +42,7 @@ SEED = 1234 + 5
 BYTES_PER_NODE_FP32 = 216  # 27 x 4 B read + 27 x 4 B written
 # DRAM bytes (read + written) per node of the step kernel, from an ncu capture of a
 # 256x128x128 launch of the same workload (traffic grows in proportion to the nodes)
-DRAM_BYTES_PER_NODE_NCU = 223
+DRAM_BYTES_PER_NODE_NCU = 245
 BYTES_PER_NODE_FP64 = 432
 
 
