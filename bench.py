@@ -240,7 +240,7 @@ def main():
     ap.add_argument("--size", default=None, help="NXxNYxNZ override (profiling runs on a smaller box)")
     ap.add_argument("--alpha", default="newton", choices=["newton", "fixed2"],
                     help="alpha of the timed path (fixed2 = LBGK limit, to separate the alpha solve's cost)")
-    ap.add_argument("--variant", type=int, default=None, choices=[0, 1, 2, 3, 4, 5],
+    ap.add_argument("--variant", type=int, default=None, choices=[0, 1, 2, 3, 4, 5, 6, 7],
                     help="step-kernel variant instead of the autotuner's choice")
     ap.add_argument("--profile", action="store_true",
                     help="timed steps only: no validation, end-to-end, FP64 or CPU legs (for ncu captures)")
@@ -287,7 +287,7 @@ def main():
     if args.variant is None:
         variant, variant_ms = ctx.autotune(0, reps=3)
     else:
-        variant, variant_ms = args.variant, np.full(6, np.nan)
+        variant, variant_ms = args.variant, np.full(8, np.nan)
         ctx.set_kernel_variant(0, variant)
     ctx.sync()
     if pg:
@@ -314,7 +314,7 @@ def main():
     if args.profile:
         if rank == 0:
             print(json.dumps({"profile_run": True, "size": [NX, NY, NZ], "alpha": args.alpha, "variant": variant,
-                              "variant_ms": list(variant_ms[:6]), "mlups": value,
+                              "variant_ms": list(variant_ms[:8]), "mlups": value,
                               "ms_per_step": per_launch_s * 1e3, "achieved_gbs": achieved}), flush=True)
         ctx.close()
         return
@@ -380,7 +380,7 @@ def main():
             "config": {"workload": f"D3Q27 boundary layer {NX}x{NY}x{NZ}, FP32 deviation storage, Newton alpha",
                        "alpha": "newton", "storage": "fp32_dev", "nu": NU, "u_in": U_IN[0], "noise": NOISE,
                        "l2": "inputs (7.2 GB) larger than L2, no flush", "parallelism": f"replicas x{world}",
-                       "kernel_variant": variant, "variant_ms": [float(x) for x in variant_ms[:6]]},
+                       "kernel_variant": variant, "variant_ms": [float(x) for x in variant_ms[:8]]},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": DRAM_BYTES_PER_NODE_NCU * nodes_per_step,
                          "traffic_note": "bytes per launch: ncu DRAM bytes per node of a 256x128x128 launch x nodes",

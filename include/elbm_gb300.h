@@ -76,6 +76,10 @@ typedef struct {
   double fs_feq[27];
   double inl_feq[8][27];
   double outl_feq[8][27];
+  /* 1: every step repairs the negative post-collision populations it produced,
+   * as damp_it.f95:64-177 does for unshifted lattices (see elbm_damp_level) */
+  int32_t damp;
+  int32_t pad_damp;
 } elbm_d3q27_params;
 
 /* D3Q39 compressible level: the reference's background scalars (computed by the
@@ -210,16 +214,27 @@ int elbm_average_down(elbm_ctx* ctx, int lvl);
  * counterpart in the reference (its loop issues each phase from the host). */
 int elbm_amr_run(elbm_ctx* ctx, int nlev, int ncycles, elbm_stats* stats);
 
+/* Repair the negative populations of a D3Q27 level's current post-collision
+ * state, as damp_it.f95:64-177 (unshifted lattice): a negative f_i at x takes
+ * the mean of f_i(x + c_i) and f_i(x - c_i) when both links from x are fluid
+ * links and both values positive; with one positive fluid-link neighbour, the
+ * mean of it and |f_i|; otherwise |f_i|.  Neighbours are read before any
+ * repair (the reference repairs in place, so the two differ only when two
+ * negative populations of one direction are adjacent along c_i).  repaired
+ * (may be NULL) receives the number of populations changed; a level holds at
+ * most 2^22 pending repairs per call (more: ELBM_E_STATE, nothing changed). */
+int elbm_damp_level(elbm_ctx* ctx, int lvl, int64_t* repaired);
+
 /* Time every variant of the level's step kernel on its current state (reps
  * launches each, the state does not advance) and keep the fastest for
  * elbm_level_step.  chosen and ms_per_variant (room for 8) may be NULL.  The
  * reference has no counterpart (it has one code path per lattice). */
 int elbm_autotune(elbm_ctx* ctx, int lvl, int reps, int* chosen, double* ms_per_variant);
 
-/* Use kernel variant v (0: direct loads; 1, 4, 5: direct, registers capped
- * for 4, 5, 6 blocks of 128 threads per SM; 2: rows staged in shared memory
- * by bulk copies, persistent; 3: direct loads, persistent warps striding over
- * 32-node chunks) for
+/* Use kernel variant v (0: direct loads; 1, 4, 5, 6, 7: direct, registers
+ * capped for 4, 5, 6, 8, 10 blocks of 128 threads per SM; 2: rows staged in
+ * shared memory by bulk copies, persistent; 3: direct loads, persistent warps
+ * taking 32-node chunks from a counter) for
  * the level's FP32 D3Q27 steps, instead of the autotuner's choice.  Variant 2
  * applies to boxes with nx and the plane size multiples of 4 and ny, nz >= 3;
  * other boxes fall back to variant 0.  No counterpart in the reference. */

@@ -50,6 +50,8 @@ class D3Q27Params(ct.Structure):
         ("fs_feq", ct.c_double * 27),
         ("inl_feq", (ct.c_double * 27) * 8),
         ("outl_feq", (ct.c_double * 27) * 8),
+        ("damp", ct.c_int32),
+        ("pad_damp", ct.c_int32),
     ]
 
 
@@ -118,6 +120,7 @@ SIGNATURES = {
     "elbm_fill_fine_ghosts": (_c_int, [_vp, _c_int, _vp]),
     "elbm_average_down": (_c_int, [_vp, _c_int]),
     "elbm_amr_run": (_c_int, [_vp, _c_int, _c_int, _vp]),
+    "elbm_damp_level": (_c_int, [_vp, _c_int, _vp]),
     "elbm_mark_triangles": (_c_int, [_c_int, _c_int, _c_int, _vp, _c_double, _c_int, _vp, _vp]),
     "elbm_alpha_harvest": (_c_int, [_vp, _c_int, _c_int, _c_int, _vp, ct.c_int64, _vp]),
     "elbm_alpha_mlp_infer": (_c_int, [_vp, _vp, _vp, ct.c_int64, _vp, _vp]),
@@ -160,8 +163,10 @@ def _ptr(a: np.ndarray):
 
 
 def make_d3q27_params(nu, tol_alpha=1e-12, tol_dH=1e-10, max_newton=30, alpha_mode=ELBM_ALPHA_NEWTON, check_dH=0,
-                      record_alpha=0, outlet_type=(1,) * 8, fs_feq=None, inl_feq=None, outl_feq=None) -> D3Q27Params:
+                      record_alpha=0, outlet_type=(1,) * 8, fs_feq=None, inl_feq=None, outl_feq=None,
+                      damp=0) -> D3Q27Params:
     p = D3Q27Params()
+    p.damp = damp
     p.nu = nu
     p.tol_alpha = tol_alpha
     p.tol_dH = tol_dH
@@ -307,6 +312,12 @@ class Context:
 
     def average_down(self, lvl):
         self._check(self.lib.elbm_average_down(self.h, lvl))
+
+    def damp_level(self, lvl):
+        """Repair negative populations of the level's current state; returns how many changed."""
+        r = ct.c_int64(0)
+        self._check(self.lib.elbm_damp_level(self.h, lvl, ct.byref(r)))
+        return r.value
 
     def amr_run(self, nlev, ncycles):
         """ncycles coarse steps of levels 0 .. nlev-1 with 2:1 sub-cycling (CUDA graph); returns stats."""

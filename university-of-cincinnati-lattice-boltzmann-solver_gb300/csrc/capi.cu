@@ -114,6 +114,9 @@ struct Level {
   DevBuf<int4> boxdim;
   DevBuf<float> alpha;      // per node (record_alpha)
   DevBuf<unsigned long long> work;  // chunk counter of the persistent step variant
+  // negative-population repair: (node * 27 + population) list, its count, repaired values
+  DevBuf<unsigned long long> damp_list, damp_count;
+  DevBuf<double> damp_vals;
   bool links_ready = false; // every box's links decoded and uploaded
   // coarse-fine transfer with level lvl - 1 (elbm_interlevel_setup)
   DevBuf<int32_t> il_ghost, il_src, il_down_dst, il_down_src;
@@ -616,12 +619,31 @@ int elbm_level_register(elbm_ctx* c, int lvl, int lattice, int storage, int nbox
   return ELBM_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+int damp_buffers(elbm_ctx* c, Level& lv) {
+  if (!lv.damp_list.p) CUDA_TRY(lv.damp_list.alloc(kDampCap), "repair list");
+  if (!lv.damp_count.p) CUDA_TRY(lv.damp_count.alloc(1), "repair count");
+  if (!lv.damp_vals.p) CUDA_TRY(lv.damp_vals.alloc(kDampCap), "repair values");
+  return ELBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int elbm_set_d3q27_params(elbm_ctx* c, int lvl, const elbm_d3q27_params* p) {
   Level* lv = get_level(c, lvl);
   if (!lv || !p) return fail(c, ELBM_E_ARG, "unknown level or null params");
   if (lv->lattice != ELBM_D3Q27) return fail(c, ELBM_E_ARG, "level %d is not a D3Q27 level", lvl);
-  if (!(p->nu > 0.0) || p->max_newton < 1 || p->alpha_mode < 0 || p->alpha_mode > 2)
+  if (!(p->nu > 0.0) || p->max_newton < 1 || p->alpha_mode < 0 || p->alpha_mode > 2 || p->damp < 0 || p->damp > 1)
     return fail(c, ELBM_E_ARG, "bad D3Q27 parameters");
+  if (p->damp) {
+    CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+    if (const int rc = damp_buffers(c, *lv)) return rc;
+  }
   if (p->alpha_mode == ELBM_ALPHA_LEARNED && (!lv->mlp_set || lv->storage != ELBM_STORE_FP32_DEV))
     return fail(c, ELBM_E_STATE, "learned alpha needs an FP32-storage level and weights (elbm_set_alpha_mlp)");
   lv->p27 = *p;
@@ -851,6 +873,27 @@ Step27Args level_args27(elbm_ctx* c, Level& lv) {
   return a;
 }
 
+// One step of a D3Q27 level (no host synchronisation: capturable); with
+// p27.damp, the step lists the negative populations it writes and the repair
+// follows on the new state (collision then damp_it, loop.f95:133-139).
+void enqueue_step27_args(elbm_ctx* c, Level& lv, Step27Args a) {
+  const bool damp = lv.p27.damp && lv.damp_list.p;
+  if (damp) {
+    cudaMemsetAsync(lv.damp_count.p, 0, sizeof(unsigned long long), c->stream);
+    a.neg_list = lv.damp_list.p;
+    a.neg_count = lv.damp_count.p;
+    a.neg_cap = kDampCap;
+  }
+  if (lv.storage == ELBM_STORE_FP64) launch_d3q27_fp64(a, c->stream);
+  else launch_d3q27_fp32(a, c->stream);
+  lv.cur ^= 1;
+  if (damp) {
+    Step27Args r = a;
+    r.src = lv.pop[lv.cur].p;
+    launch_damp27_fix(r, lv.storage == ELBM_STORE_FP32_DEV, lv.damp_vals.p, c->stream);
+  }
+}
+
 int ready27(elbm_ctx* c, Level& lv) {
   for (auto& bp : lv.boxes)
     if (!bp->links_set || !bp->data_set) return fail(c, ELBM_E_STATE, "links or populations missing");
@@ -880,10 +923,8 @@ int elbm_level_step(elbm_ctx* c, int lvl, int nsteps, elbm_stats* out) {
   for (int s = 0; s < nsteps; ++s) {
     Step27Args a = level_args27(c, *lv);
     a.alpha_out = (p.record_alpha && s == nsteps - 1) ? lv->alpha.p : nullptr;
-    if (lv->storage == ELBM_STORE_FP64) launch_d3q27_fp64(a, c->stream);
-    else launch_d3q27_fp32(a, c->stream);
+    enqueue_step27_args(c, *lv, a);
     CUDA_TRY(cudaGetLastError(), "step kernel launch");
-    lv->cur ^= 1;
   }
   CUDA_TRY(cudaEventRecord(c->ev1, c->stream), "event");
   return finish_stats(c, out);
@@ -1208,9 +1249,7 @@ namespace {
 void enqueue_step27(elbm_ctx* c, Level& lv) {
   Step27Args a = level_args27(c, lv);
   a.check_dH = 0;
-  if (lv.storage == ELBM_STORE_FP64) launch_d3q27_fp64(a, c->stream);
-  else launch_d3q27_fp32(a, c->stream);
-  lv.cur ^= 1;
+  enqueue_step27_args(c, lv, a);
 }
 
 // One step of level l with the 2:1 sub-cycle of the finer levels below it, in
@@ -1246,8 +1285,8 @@ int elbm_amr_run(elbm_ctx* c, int nlev, int ncycles, elbm_stats* out) {
     if (const int rc = ready27(c, *lv)) return rc;
     if (l > 0 && !lv->il_ready) return fail(c, ELBM_E_STATE, "level %d: call elbm_interlevel_setup first", l);
     // the graph bakes in buffer addresses and parameters
-    const uintptr_t parts[4] = {(uintptr_t)lv->pop[0].p, (uintptr_t)lv->il_ghost.p, (uintptr_t)lv->p27.alpha_mode,
-                                (uintptr_t)lv->variant};
+    const uintptr_t parts[5] = {(uintptr_t)lv->pop[0].p, (uintptr_t)lv->il_ghost.p, (uintptr_t)lv->p27.alpha_mode,
+                                (uintptr_t)lv->variant, (uintptr_t)lv->p27.damp};
     for (uintptr_t v : parts) key = (key ^ (uint64_t)v) * 1099511628211ull;
     uint64_t pb;
     std::memcpy(&pb, &lv->p27.nu, sizeof pb);
@@ -1286,6 +1325,34 @@ int elbm_amr_run(elbm_ctx* c, int nlev, int ncycles, elbm_stats* out) {
   CUDA_TRY(cudaGetLastError(), "AMR cycle");
   CUDA_TRY(cudaEventRecord(c->ev1, c->stream), "event");
   return finish_stats(c, out);
+}
+
+int elbm_damp_level(elbm_ctx* c, int lvl, int64_t* repaired) {
+  Level* lv = get_level(c, lvl);
+  if (!lv) return fail(c, ELBM_E_ARG, "unknown level %d", lvl);
+  if (lv->lattice != ELBM_D3Q27) return fail(c, ELBM_E_UNSUPPORTED, "D3Q39 levels repair inside elbm_level_step");
+  if (!lv->params_set) return fail(c, ELBM_E_STATE, "level parameters not set");
+  if (const int rc = ready27(c, *lv)) return rc;
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  if (const int rc = damp_buffers(c, *lv)) return rc;
+  Step27Args a = level_args27(c, *lv);
+  a.neg_list = lv->damp_list.p;
+  a.neg_count = lv->damp_count.p;
+  a.neg_cap = kDampCap;
+  const bool fp32 = lv->storage == ELBM_STORE_FP32_DEV;
+  CUDA_TRY(cudaMemsetAsync(lv->damp_count.p, 0, sizeof(unsigned long long), c->stream), "memset");
+  launch_damp27_scan(a, fp32, c->stream);
+  CUDA_TRY(cudaGetLastError(), "repair scan");
+  unsigned long long cnt = 0;
+  CUDA_TRY(cudaMemcpyAsync(&cnt, lv->damp_count.p, sizeof cnt, cudaMemcpyDeviceToHost, c->stream), "count");
+  CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  if ((long long)cnt > kDampCap)
+    return fail(c, ELBM_E_STATE, "%llu negative populations: more than the %lld one call repairs", cnt, kDampCap);
+  launch_damp27_fix(a, fp32, lv->damp_vals.p, c->stream);
+  CUDA_TRY(cudaGetLastError(), "repair");
+  CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  if (repaired) *repaired = (int64_t)cnt;
+  return ELBM_OK;
 }
 
 int elbm_sync(elbm_ctx* c) {

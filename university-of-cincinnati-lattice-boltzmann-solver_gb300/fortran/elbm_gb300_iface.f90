@@ -26,6 +26,7 @@ module elbm_gb300_iface
     real(c_double) :: fs_feq(27)
     real(c_double) :: inl_feq(27, 8)   ! C layout inl_feq[8][27]
     real(c_double) :: outl_feq(27, 8)
+    integer(c_int32_t) :: damp, pad_damp
   end type
 
   type, bind(c), public :: elbm_d3q39_params
@@ -49,7 +50,7 @@ module elbm_gb300_iface
     elbm_set_d3q39_params, elbm_upload_level39, elbm_download_level39, elbm_mark_triangles, &
     elbm_upload_level_noalloc, elbm_autotune, elbm_set_kernel_variant, elbm_alpha_harvest, &
     elbm_alpha_mlp_train, elbm_set_alpha_mlp, elbm_interlevel_setup, elbm_fill_fine_ghosts, &
-    elbm_average_down, elbm_amr_run
+    elbm_average_down, elbm_amr_run, elbm_damp_level
 
   interface
     integer(c_int) function elbm_create(device, ctx) bind(c, name="elbm_create")
@@ -202,6 +203,12 @@ module elbm_gb300_iface
       type(c_ptr), value :: ctx
       integer(c_int), value :: nlev, ncycles
       type(elbm_stats), intent(out) :: stats
+    end function
+    integer(c_int) function elbm_damp_level(ctx, lvl, repaired) bind(c, name="elbm_damp_level")
+      import :: c_int, c_ptr, c_int64_t
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl
+      integer(c_int64_t), intent(out) :: repaired
     end function
   end interface
 end module elbm_gb300_iface
