@@ -92,7 +92,7 @@ typedef struct {
   int32_t lvl;               /* AMR level (beta_1 uses 2^(lvl+1)) */
   int32_t startup_timesteps; /* start-up ramps of beta, epsilon and alpha */
   int32_t max_lm_iters;      /* cap on the multiplier Newton (the reference has none) */
-  int32_t periodic;          /* bit 0/1/2: x/y/z periodic; this version requires 7 */
+  int32_t periodic;          /* bit 0/1/2: x/y/z periodic; not 7 needs elbm_set_links39 */
   int32_t timestep;          /* timestep(amr_max_lvl) of the next step; advanced by elbm_level_step */
   int32_t damp;              /* 1: run the negative-population repair of damp_it.f95 after collision */
   int32_t pad;
@@ -141,6 +141,43 @@ int elbm_upload_level39(elbm_ctx* ctx, int lvl, int box, const double* fout, con
 /* Any output pointer may be NULL.  macro: rho, u, v, w, T (5 comps). */
 int elbm_download_level39(elbm_ctx* ctx, int lvl, int box, double* fout, double* gout, double* lm, double* w_vel,
                           double* alpha, double* macro);
+
+/* Boundary data of a D3Q39 level with link codes (see elbm_set_links39):
+ * inlet/outlet types per number (inlets 1, 2, 4: inlet table; 3: freestream;
+ * outlets 1, 4: outlet table; 2: inlet table; 3: freestream; 6: pure outflow)
+ * and the equilibria of f and g, computed by the host like
+ * freestream_basis_calcs.f90 and inlet_outlet_basis_calcs.f90. */
+typedef struct {
+  int32_t inlet_type[8], outlet_type[8];
+  double fs_fieq[39], fs_gieq[39];
+  double inl_fieq[8][39], inl_gieq[8][39];
+  double outl_fieq[8][39], outl_gieq[8][39];
+} elbm_d3q39_bc;
+
+/* Link codes of a D3Q39 box (state FAB, 39 comps, ngrow_state ghosts), for
+ * levels that are not periodic on every axis.  The library works out, for
+ * every node and population, what the reference's push loop
+ * (streaming.f95:266-481: direction outermost, boundary rules applied to fout
+ * in place before fi is written, the interior push as well on the shifted
+ * lattice) leaves in the post-streaming slot: a population of a node within 4
+ * links, a boundary equilibrium, or the slot's value of the previous step.
+ * Supported codes: >= 0, -5, -8, -10, -100-k, -200-k, -300-k, -400-k, -666,
+ * -1000; others (inviscid walls, interpolated walls) give ELBM_E_UNSUPPORTED.
+ * Nodes with state < 0 neither push nor collide; state >= 0 must be fluid
+ * (outside 200..298 and 1000..50999).  The negative-population repair
+ * (damp = 1) is not available with link codes. */
+int elbm_set_links39(elbm_ctx* ctx, int lvl, int box, const int32_t* state, int ngrow_state,
+                     const elbm_d3q39_bc* bc);
+
+/* The tables elbm_set_links39 builds, on the host only (no device, no
+ * context): per node a type (0 neither pushes nor collides, 1 plain pulls,
+ * 2 boundary record) and, for each of the *nrec records (at most capacity),
+ * the node and 39 link words (bits 0-1 kind: 0 previous post-streaming value,
+ * 1 pull, 2 equilibrium; bits 2-7 population; 8-12 table; 13-22 offset
+ * (dx+4) + 9(dy+4) + 81(dz+4)).  For inspection and tests. */
+int elbm_links39_tables(int nx, int ny, int nz, const int32_t* state, int ngrow_state, int periodic, int shifted,
+                        int primary_flow_dir, const int32_t* inlet_type, const int32_t* outlet_type, uint8_t* ntype,
+                        int32_t* rec_node, uint32_t* words, int64_t capacity, int64_t* nrec);
 
 /* Node types and link codes of one box: the reference's integer `state` FAB
  * (Q components, ghost width ngrow_state; encoding of looping/timestepping/loop.f95:71-89,

@@ -344,32 +344,25 @@ typedef struct {
 static inline int64_t idx3(int x, int y, int z, int nx, int ny) { return ((int64_t)z * ny + y) * nx + x; }
 static inline int wrap(int a, int n) { return ((a % n) + n) % n; }
 
-/* One level step on a periodic box (all nodes fluid): push streaming with
- * periodic images (AMReX fill_boundary on a periodic domain), flow variables,
- * collision, fout repair.  step = timestep(lvl) = timestep(amr_max_lvl). */
-int o39_step_periodic(const o39_consts* k, o39_level* s, int step, o39_stats* st) {
-  o39_lattice L;
-  o39_lattice_init(&L, k->shifted, k->primary_flow_dir);
-  const int nx = s->nx, ny = s->ny, nz = s->nz;
-  const int64_t N = (int64_t)nx * ny * nz;
-  double* fi = (double*)malloc(sizeof(double) * Q * N);
-  double* gi = (double*)malloc(sizeof(double) * Q * N);
-  if (!fi || !gi) return -100;
-  memset(st, 0, sizeof *st);
-  /* streaming.f95:266-369 (interior links only) */
-  for (int i = 0; i < Q; ++i)
-    for (int z = 0; z < nz; ++z)
-      for (int y = 0; y < ny; ++y)
-        for (int x = 0; x < nx; ++x) {
-          const int64_t n = idx3(x, y, z, nx, ny);
-          const int64_t t = idx3(wrap(x + L.cx[i], nx), wrap(y + L.cy[i], ny), wrap(z + L.cz[i], nz), nx, ny);
-          fi[(int64_t)i * N + t] = s->fout[(int64_t)i * N + n];
-          gi[(int64_t)i * N + t] = s->gout[(int64_t)i * N + n];
-        }
+/* calculate_flow_variables.f95:192-311 and collision.f95:153-300 for every
+ * node (state == NULL) or every fluid node (state[0] of the node >= 0, outside
+ * 1000..50999 and 200..298). */
+static int node_is_fluid39(int32_t s0) {
+  if (s0 < 0) return 0;
+  if (s0 >= 1000 && s0 < 51000) return 0;
+  if (s0 >= 200 && s0 < 299) return 0;
+  return 1;
+}
+
+static void collide39(const o39_consts* k, const o39_lattice* Lp, o39_level* s, const double* fi, const double* gi,
+                      int step, const int32_t* state, int64_t* lm_iters_out, int64_t* capped_out, int64_t* not2_out) {
+  const o39_lattice L = *Lp;
+  const int64_t N = (int64_t)s->nx * s->ny * s->nz;
   int64_t lm_iters = 0, capped = 0, not2 = 0;
   /* calculate_flow_variables.f95:192-311 and collision.f95:153-300, per node */
 #pragma omp parallel for schedule(static) reduction(+ : lm_iters, capped, not2)
   for (int64_t n = 0; n < N; ++n) {
+    if (state && !node_is_fluid39(state[n])) continue;
     double f[Q], g[Q], lm[NLM], fieq_a[Q], fd[Q];
     for (int i = 0; i < Q; ++i) {
       f[i] = fi[(int64_t)i * N + n];
@@ -434,6 +427,35 @@ int o39_step_periodic(const o39_consts* k, o39_level* s, int step, o39_stats* st
     if (s->v) s->v[n] = v;
     if (s->temp) s->temp[n] = temp;
   }
+  *lm_iters_out = lm_iters;
+  *capped_out = capped;
+  *not2_out = not2;
+}
+
+/* One level step on a periodic box (all nodes fluid): push streaming with
+ * periodic images (AMReX fill_boundary on a periodic domain), flow variables,
+ * collision, fout repair.  step = timestep(lvl) = timestep(amr_max_lvl). */
+int o39_step_periodic(const o39_consts* k, o39_level* s, int step, o39_stats* st) {
+  o39_lattice L;
+  o39_lattice_init(&L, k->shifted, k->primary_flow_dir);
+  const int nx = s->nx, ny = s->ny, nz = s->nz;
+  const int64_t N = (int64_t)nx * ny * nz;
+  double* fi = (double*)malloc(sizeof(double) * Q * N);
+  double* gi = (double*)malloc(sizeof(double) * Q * N);
+  if (!fi || !gi) return -100;
+  memset(st, 0, sizeof *st);
+  /* streaming.f95:266-369 (interior links only) */
+  for (int i = 0; i < Q; ++i)
+    for (int z = 0; z < nz; ++z)
+      for (int y = 0; y < ny; ++y)
+        for (int x = 0; x < nx; ++x) {
+          const int64_t n = idx3(x, y, z, nx, ny);
+          const int64_t t = idx3(wrap(x + L.cx[i], nx), wrap(y + L.cy[i], ny), wrap(z + L.cz[i], nz), nx, ny);
+          fi[(int64_t)i * N + t] = s->fout[(int64_t)i * N + n];
+          gi[(int64_t)i * N + t] = s->gout[(int64_t)i * N + n];
+        }
+  int64_t lm_iters = 0, capped = 0, not2 = 0;
+  collide39(k, &L, s, fi, gi, step, NULL, &lm_iters, &capped, &not2);
   /* damp_it.f95:64-177, fout part: a negative population is replaced by the
    * mean of its neighbours along +-c_i when both are positive (interior links). */
   int64_t damped = 0;
@@ -466,6 +488,150 @@ int o39_step_periodic(const o39_consts* k, o39_level* s, int step, o39_stats* st
   st->damped = damped;
   free(fi);
   free(gi);
+  return 0;
+}
+
+/* Boundary equilibria and types of the link-aware D3Q39 step. */
+typedef struct {
+  int inlet_type[8], outlet_type[8];
+  double fs_fieq[Q], fs_gieq[Q];
+  double inl_fieq[8][Q], inl_gieq[8][Q];
+  double outl_fieq[8][Q], outl_gieq[8][Q];
+} o39_bc;
+
+/* One level step of a box with the reference's link codes: the push loop of
+ * streaming.f95:266-481 in its order (direction outermost, then z, y, x), with
+ * the boundary rules it applies in place to fout before writing fi:
+ *   >= 0            fi(x + c_i, i) = fout(x, i)
+ *   -10             bounceback.f95: swap fout(x, i) <-> fout(x, opp(i)) (f and g), then fi(x, opp(i)) = fout(x, i)
+ *   -5              null_bc: fi(x, opp(i)) = fout(x, i)
+ *   -8, -1000       freestream_edge_bc: fout(x, i) = fs_eq(opp(i)); fi(x, opp(i)) = fout(x, i)
+ *   -100 - k        inlet_bc.f95 (types 1, 2, 4: inl_eq(opp(i), k); 3: fs_eq(opp(i))); fi(x, opp(i)) = fout(x, i)
+ *   -200 - k        outlet_bc.f95 (types 1, 4: outl_eq; 2: inl_eq (press_temp_bc.f95:26-27); 3: fs_eq;
+ *                   6: pure_outflow_bc, fout(x, i) = fout(x, opp(i))); fi(x, opp(i)) = fout(x, i)
+ *   -300 - k, -400 - k  fi(x, i) = fout(x, i)
+ *   -666            nothing
+ * and, on the shifted lattice, the interior push as well for every boundary
+ * code, and the rest population pushed only when x + c_1 is a node with
+ * state >= 0.  Slots no rule writes keep their value of the previous step
+ * (fi_prev / gi_prev, updated here).  Periodic axes wrap (bit 0/1/2 = x/y/z);
+ * pushes across a non-periodic face leave the box.  Then every fluid node
+ * collides.  Returns -1 for a code outside this list. */
+int o39_step_links(const o39_consts* k, o39_level* s, int step, o39_stats* st, const int32_t* state, int periodic,
+                   const o39_bc* bc, double* fi_prev, double* gi_prev) {
+  o39_lattice L;
+  o39_lattice_init(&L, k->shifted, k->primary_flow_dir);
+  const int nx = s->nx, ny = s->ny, nz = s->nz;
+  const int64_t N = (int64_t)nx * ny * nz;
+  double* fo = (double*)malloc(sizeof(double) * Q * N);
+  double* go = (double*)malloc(sizeof(double) * Q * N);
+  if (!fo || !go) return -100;
+  memcpy(fo, s->fout, sizeof(double) * Q * N);
+  memcpy(go, s->gout, sizeof(double) * Q * N);
+  double* fi = fi_prev;
+  double* gi = gi_prev;
+  memset(st, 0, sizeof *st);
+  int rc = 0;
+#define O39_TARGET(xx, yy, zz, tt)                                                              \
+  int tx_ = (xx), ty_ = (yy), tz_ = (zz);                                                        \
+  int in_ = 1;                                                                                   \
+  if (periodic & 1) tx_ = wrap(tx_, nx); else in_ &= tx_ >= 0 && tx_ < nx;                        \
+  if (periodic & 2) ty_ = wrap(ty_, ny); else in_ &= ty_ >= 0 && ty_ < ny;                        \
+  if (periodic & 4) tz_ = wrap(tz_, nz); else in_ &= tz_ >= 0 && tz_ < nz;                        \
+  const int64_t tt = in_ ? idx3(tx_, ty_, tz_, nx, ny) : -1
+  for (int i = 0; i < Q && rc == 0; ++i)
+    for (int z = 0; z < nz && rc == 0; ++z)
+      for (int y = 0; y < ny && rc == 0; ++y)
+        for (int x = 0; x < nx; ++x) {
+          const int64_t n = idx3(x, y, z, nx, ny);
+          const int32_t s0 = state[n];
+          if (s0 < 0) continue;
+          O39_TARGET(x + L.cx[i], y + L.cy[i], z + L.cz[i], t);
+          const int64_t a = (int64_t)i * N + n, o = (int64_t)L.opp[i] * N + n;
+          if (i == 0 && k->shifted) {
+            if (t >= 0 && state[t] >= 0) {
+              fi[(int64_t)i * N + t] = fo[a];
+              gi[(int64_t)i * N + t] = go[a];
+            }
+            continue;
+          }
+          const int32_t code = (i == 0) ? s0 : state[(int64_t)i * N + n];
+          if (code >= 0 && code <= 1100000000) {
+            if (t >= 0) {
+              fi[(int64_t)i * N + t] = fo[a];
+              gi[(int64_t)i * N + t] = go[a];
+            }
+            continue;
+          }
+          if (code == -666) continue;
+          const int shifted_push = k->shifted && t >= 0;
+          if (shifted_push) {
+            fi[(int64_t)i * N + t] = fo[a];
+            gi[(int64_t)i * N + t] = go[a];
+          }
+          const int oi = L.opp[i];
+          if (code == -10) {
+            double d = fo[a];
+            fo[a] = fo[o];
+            fo[o] = d;
+            d = go[a];
+            go[a] = go[o];
+            go[o] = d;
+          } else if (code == -5) {
+          } else if (code == -8 || code == -1000) {
+            fo[a] = bc->fs_fieq[oi];
+            go[a] = bc->fs_gieq[oi];
+          } else if (code <= -100 && code >= -199) {
+            const int kk = -code - 100;
+            if (kk < 1 || kk > 8) { rc = -1; break; }
+            const int ty = bc->inlet_type[kk - 1];
+            if (ty == 1 || ty == 2 || ty == 4) {
+              fo[a] = bc->inl_fieq[kk - 1][oi];
+              go[a] = bc->inl_gieq[kk - 1][oi];
+            } else if (ty == 3) {
+              fo[a] = bc->fs_fieq[oi];
+              go[a] = bc->fs_gieq[oi];
+            } else { rc = -1; break; }
+          } else if (code <= -200 && code >= -299) {
+            const int kk = -code - 200;
+            if (kk < 1 || kk > 8) { rc = -1; break; }
+            const int ty = bc->outlet_type[kk - 1];
+            if (ty == 1 || ty == 4) {
+              fo[a] = bc->outl_fieq[kk - 1][oi];
+              go[a] = bc->outl_gieq[kk - 1][oi];
+            } else if (ty == 2) {
+              fo[a] = bc->inl_fieq[kk - 1][oi];
+              go[a] = bc->inl_gieq[kk - 1][oi];
+            } else if (ty == 3) {
+              fo[a] = bc->fs_fieq[oi];
+              go[a] = bc->fs_gieq[oi];
+            } else if (ty == 6) {
+              fo[a] = fo[o];
+              go[a] = go[o];
+            } else { rc = -1; break; }
+          } else if (code <= -300 && code >= -499) {
+            fi[a] = fo[a];
+            gi[a] = go[a];
+            continue;
+          } else {
+            rc = -1;
+            break;
+          }
+          fi[o] = fo[a];
+          gi[o] = go[a];
+        }
+#undef O39_TARGET
+  free(fo);
+  free(go);
+  if (rc) return rc;
+  int64_t lm_iters = 0, capped = 0, not2 = 0;
+  collide39(k, &L, s, fi, gi, step, state, &lm_iters, &capped, &not2);
+  int64_t nodes = 0;
+  for (int64_t n = 0; n < N; ++n) nodes += node_is_fluid39(state[n]);
+  st->nodes = nodes;
+  st->lm_iters = lm_iters;
+  st->lm_capped = capped;
+  st->alpha_not2 = not2;
   return 0;
 }
 

@@ -141,3 +141,44 @@ def step_periodic(k: O39Consts, lev: Level39, step: int):
     if rc != 0:
         raise RuntimeError(f"o39 step failed {rc}")
     return {n: getattr(st, n) for n, _ in st._fields_}
+
+
+class O39Bc(ct.Structure):
+    _fields_ = [("inlet_type", ct.c_int * 8), ("outlet_type", ct.c_int * 8),
+                ("fs_fieq", ct.c_double * Q39), ("fs_gieq", ct.c_double * Q39),
+                ("inl_fieq", (ct.c_double * Q39) * 8), ("inl_gieq", (ct.c_double * Q39) * 8),
+                ("outl_fieq", (ct.c_double * Q39) * 8), ("outl_gieq", (ct.c_double * Q39) * 8)]
+
+
+def bc(inlet_type, outlet_type, fs_f, fs_g, inl_f, inl_g, outl_f, outl_g) -> O39Bc:
+    b = O39Bc()
+    for k in range(8):
+        b.inlet_type[k] = int(inlet_type[k])
+        b.outlet_type[k] = int(outlet_type[k])
+        for i in range(Q39):
+            b.inl_fieq[k][i], b.inl_gieq[k][i] = inl_f[k][i], inl_g[k][i]
+            b.outl_fieq[k][i], b.outl_gieq[k][i] = outl_f[k][i], outl_g[k][i]
+    for i in range(Q39):
+        b.fs_fieq[i], b.fs_gieq[i] = fs_f[i], fs_g[i]
+    return b
+
+
+def step_links(k: O39Consts, lev: Level39, step: int, state: np.ndarray, periodic: int, b: O39Bc,
+               fi_prev: np.ndarray, gi_prev: np.ndarray):
+    """One step with the reference's link codes (state: (39, nz, ny, nx) int32); fi_prev and gi_prev
+    hold the post-streaming populations of the previous step and are updated in place."""
+    L = lib()
+    if not getattr(L, "_o39_links_ready", False):
+        L.o39_step_links.restype = ct.c_int
+        L.o39_step_links.argtypes = [ct.POINTER(O39Consts), ct.POINTER(O39Level), ct.c_int, ct.POINTER(O39Stats),
+                                     ct.c_void_p, ct.c_int, ct.POINTER(O39Bc), ct.c_void_p, ct.c_void_p]
+        L._o39_links_ready = True
+    st = O39Stats()
+    s = lev.c()
+    stc = np.ascontiguousarray(state, np.int32)
+    assert fi_prev.flags.c_contiguous and gi_prev.flags.c_contiguous
+    rc = L.o39_step_links(ct.byref(k), ct.byref(s), step, ct.byref(st), _p(stc), periodic, ct.byref(b),
+                          _p(fi_prev), _p(gi_prev))
+    if rc != 0:
+        raise RuntimeError(f"o39 link step failed {rc}")
+    return {n: getattr(st, n) for n, _ in st._fields_}

@@ -80,6 +80,27 @@ def make_d3q39_params(consts, timestep=0, periodic=7, damp=1) -> D3Q39Params:
     return p
 
 
+class D3Q39Bc(ct.Structure):
+    _fields_ = [("inlet_type", ct.c_int32 * 8), ("outlet_type", ct.c_int32 * 8),
+                ("fs_fieq", ct.c_double * 39), ("fs_gieq", ct.c_double * 39),
+                ("inl_fieq", (ct.c_double * 39) * 8), ("inl_gieq", (ct.c_double * 39) * 8),
+                ("outl_fieq", (ct.c_double * 39) * 8), ("outl_gieq", (ct.c_double * 39) * 8)]
+
+
+def make_d3q39_bc(inlet_type, outlet_type, fs_f, fs_g, inl_f, inl_g, outl_f, outl_g) -> D3Q39Bc:
+    """Boundary equilibria (f and g) and inlet/outlet types of a D3Q39 level with link codes."""
+    b = D3Q39Bc()
+    for k in range(8):
+        b.inlet_type[k] = int(inlet_type[k])
+        b.outlet_type[k] = int(outlet_type[k])
+        for i in range(39):
+            b.inl_fieq[k][i], b.inl_gieq[k][i] = inl_f[k][i], inl_g[k][i]
+            b.outl_fieq[k][i], b.outl_gieq[k][i] = outl_f[k][i], outl_g[k][i]
+    for i in range(39):
+        b.fs_fieq[i], b.fs_gieq[i] = fs_f[i], fs_g[i]
+    return b
+
+
 class Stats(ct.Structure):
     _fields_ = [
         ("node_updates", ct.c_int64),
@@ -121,6 +142,9 @@ SIGNATURES = {
     "elbm_average_down": (_c_int, [_vp, _c_int]),
     "elbm_amr_run": (_c_int, [_vp, _c_int, _c_int, _vp]),
     "elbm_damp_level": (_c_int, [_vp, _c_int, _vp]),
+    "elbm_set_links39": (_c_int, [_vp, _c_int, _c_int, _vp, _c_int, _vp]),
+    "elbm_links39_tables": (_c_int, [_c_int, _c_int, _c_int, _vp, _c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp,
+                                     _vp, _vp, ct.c_int64, _vp]),
     "elbm_mark_triangles": (_c_int, [_c_int, _c_int, _c_int, _vp, _c_double, _c_int, _vp, _vp]),
     "elbm_alpha_harvest": (_c_int, [_vp, _c_int, _c_int, _c_int, _vp, ct.c_int64, _vp]),
     "elbm_alpha_mlp_infer": (_c_int, [_vp, _vp, _vp, ct.c_int64, _vp, _vp]),
@@ -186,6 +210,26 @@ def make_d3q27_params(nu, tol_alpha=1e-12, tol_dH=1e-10, max_newton=30, alpha_mo
             p.inl_feq[k][j] = inl[k, j]
             p.outl_feq[k][j] = outl[k, j]
     return p
+
+
+def links39_tables(state: np.ndarray, periodic: int, shifted: int, primary_flow_dir: int, inlet_type, outlet_type,
+                   ngrow_state: int = 0):
+    """Host-side D3Q39 link tables of a box state (39, nz, ny, nx): (ntype, record nodes, words (nrec, 39))."""
+    st = np.ascontiguousarray(state, np.int32)
+    g = ngrow_state
+    nz, ny, nx = (st.shape[1] - 2 * g, st.shape[2] - 2 * g, st.shape[3] - 2 * g)
+    it = np.ascontiguousarray(inlet_type, np.int32)
+    ot = np.ascontiguousarray(outlet_type, np.int32)
+    ntype = np.zeros(nx * ny * nz, np.uint8)
+    cap = nx * ny * nz
+    rec = np.zeros(cap, np.int32)
+    words = np.zeros((cap, 39), np.uint32)
+    nrec = ct.c_int64(0)
+    rc = load().elbm_links39_tables(nx, ny, nz, _ptr(st), g, periodic, shifted, primary_flow_dir, _ptr(it), _ptr(ot),
+                                    _ptr(ntype), _ptr(rec), _ptr(words), cap, ct.byref(nrec))
+    if rc != ELBM_OK:
+        raise ElbmError(rc, "elbm_links39_tables failed")
+    return ntype.reshape(nz, ny, nx), rec[:nrec.value], words[:nrec.value]
 
 
 def mark_triangles(state: np.ndarray, origin, dx: float, tri: np.ndarray) -> None:
@@ -279,6 +323,10 @@ class Context:
 
     def set_d3q39_params(self, lvl, params: D3Q39Params):
         self._check(self.lib.elbm_set_d3q39_params(self.h, lvl, ct.byref(params)))
+
+    def set_links39(self, lvl, box, state: np.ndarray, bc: D3Q39Bc, ngrow_state=0):
+        st = np.ascontiguousarray(state, np.int32)
+        self._check(self.lib.elbm_set_links39(self.h, lvl, box, _ptr(st), ngrow_state, ct.byref(bc)))
 
     def upload39(self, lvl, box, fout, gout, lm, w_vel):
         arrs = [np.ascontiguousarray(a, np.float64) for a in (fout, gout, lm, w_vel)]

@@ -14,6 +14,7 @@
 #include "../../include/elbm_gb300.h"
 #include "kernels.cuh"
 #include "kernels39.cuh"
+#include "links39.h"
 #include "mlp.cuh"
 #include <algorithm>
 #include <random>
@@ -86,6 +87,13 @@ struct Box {
   DevBuf<uint8_t> gbuf[2];
   int gcur = 0;
   DevBuf<double> lm, w_vel, alpha64, macro;
+  // D3Q39 link codes (elbm_set_links39)
+  bool links39 = false;
+  DevBuf<uint8_t> ntype39;
+  DevBuf<int32_t> bidx39, bnodes39;
+  DevBuf<uint32_t> words39;
+  DevBuf<double> fprev39, gprev39;
+  int64_t nrec39 = 0;
   int64_t fluid_nodes = 0, boundary_nodes = 0;
   bool links_set = false, data_set = false;
 };
@@ -101,6 +109,7 @@ struct Level {
   DevBuf<float> mlp_w;   // the level's network weights (FP32 master copy; BF16 in the tensor-core kernel)
   int variant = 0;  // FP32 D3Q27 kernel variant picked by elbm_autotune
   DevBuf<uint8_t> eq;  // kEqTables x Q, FP64 or FP32 deviations
+  DevBuf<double> eq39f, eq39g;  // D3Q39 boundary equilibria of f and g, kEqTables x 39
   // D3Q27: every box of the level in one set of arrays (one launch per step)
   int64_t plane = 0;        // nodes per population plane: the boxes, each padded to whole 32-node chunks
   DevBuf<uint8_t> pop[2];   // population ping-pong (bytes: FP64 or FP32)
@@ -188,6 +197,27 @@ bool node_is_fluid(int32_t s0) {
 bool node_is_ghost(int32_t s0) { return s0 >= 10000000 && s0 <= 1100000000; }
 
 size_t elem_size(int storage) { return storage == ELBM_STORE_FP64 ? sizeof(double) : sizeof(float); }
+
+// Post-streaming slots of the D3Q39 boundary records before the first step:
+// the node's own populations (fi = fout at the start).
+__global__ void stale39_init_kernel(const double* __restrict__ f, const double* __restrict__ g,
+                                    const int32_t* __restrict__ bnodes, int64_t nrec, int64_t plane,
+                                    double* __restrict__ fprev, double* __restrict__ gprev) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nrec * 39) return;
+  const int64_t r = e / 39;
+  const int j = (int)(e % 39);
+  fprev[e] = f[(int64_t)j * plane + bnodes[r]];
+  gprev[e] = g[(int64_t)j * plane + bnodes[r]];
+}
+
+void launch_stale39_init(Box& b, cudaStream_t s) {
+  if (b.nrec39 <= 0) return;
+  const int64_t n = b.nrec39 * 39;
+  stale39_init_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>((const double*)b.buf[b.cur].p,
+                                                                  (const double*)b.gbuf[b.gcur].p, b.bnodes39.p,
+                                                                  b.nrec39, b.plane, b.fprev39.p, b.gprev39.p);
+}
 
 // ---- conversion kernels between the FP64 host layout and FP32 deviations ----
 __global__ void to_dev32_kernel(const double* __restrict__ f, float* __restrict__ d, int64_t N, int64_t plane) {
@@ -449,8 +479,13 @@ int finish_stats(elbm_ctx* c, elbm_stats* out) {
 // D3Q39 level steps: fused stream/flow-variables/collision, then the optional repair.
 int step39(elbm_ctx* c, Level& lv, int nsteps) {
   const elbm_d3q39_params& p = lv.p39;
-  for (auto& bp : lv.boxes)
+  for (auto& bp : lv.boxes) {
     if (!bp->data_set) return fail(c, ELBM_E_STATE, "populations missing");
+    if (!bp->links39 && p.periodic != 7)
+      return fail(c, ELBM_E_STATE, "a D3Q39 box that is not periodic on every axis needs elbm_set_links39");
+    if (bp->links39 && p.damp)
+      return fail(c, ELBM_E_UNSUPPORTED, "the negative-population repair is not available with D3Q39 link codes");
+  }
   CUDA_TRY(cudaEventRecord(c->ev0, c->stream), "event");
   for (int s = 0; s < nsteps; ++s) {
     for (auto& bp : lv.boxes) {
@@ -471,6 +506,16 @@ int step39(elbm_ctx* c, Level& lv, int nsteps) {
       a.N = b.N;
       a.step = lv.p39.timestep;
       a.stats = c->stats.p;
+      a.periodic = p.periodic;
+      if (b.links39) {
+        a.ntype = b.ntype39.p;
+        a.bidx = b.bidx39.p;
+        a.words = b.words39.p;
+        a.eqf = lv.eq39f.p;
+        a.eqg = lv.eq39g.p;
+        a.fprev = b.fprev39.p;
+        a.gprev = b.gprev39.p;
+      }
       D3Q39Dev& k = a.k;
       k.shifted = p.shifted;
       k.primary_flow_dir = p.primary_flow_dir;
@@ -1366,7 +1411,7 @@ int elbm_set_d3q39_params(elbm_ctx* c, int lvl, const elbm_d3q39_params* p) {
   Level* lv = get_level(c, lvl);
   if (!lv || !p) return fail(c, ELBM_E_ARG, "unknown level or null params");
   if (lv->lattice != ELBM_D3Q39) return fail(c, ELBM_E_ARG, "level %d is not a D3Q39 level", lvl);
-  if (p->periodic != 7) return fail(c, ELBM_E_UNSUPPORTED, "D3Q39 levels must be periodic on all axes in this version");
+  if (p->periodic < 0 || p->periodic > 7) return fail(c, ELBM_E_ARG, "periodic is a 3-bit mask");
   if (p->primary_flow_dir < 1 || p->primary_flow_dir > 6 || p->max_lm_iters < 1 || p->startup_timesteps < 1 ||
       !(p->t_ref > 0) || !(p->mu_ref > 0) || !(p->kappa_ref > 0) || !(p->dt > 0))
     return fail(c, ELBM_E_ARG, "bad D3Q39 parameters");
@@ -1378,6 +1423,57 @@ int elbm_set_d3q39_params(elbm_ctx* c, int lvl, const elbm_d3q39_params* p) {
   CUDA_TRY(cudaGetLastError(), "lattice upload");
   CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
   lv->params_set = true;
+  return ELBM_OK;
+}
+
+int elbm_set_links39(elbm_ctx* c, int lvl, int box, const int32_t* state, int ngrow_state, const elbm_d3q39_bc* bc) {
+  Level* lv = nullptr;
+  Box* b = get_box(c, lvl, box, &lv);
+  if (!b || !state || !bc || ngrow_state < 0) return fail(c, ELBM_E_ARG, "unknown level/box or null state/bc");
+  if (lv->lattice != ELBM_D3Q39) return fail(c, ELBM_E_ARG, "not a D3Q39 level");
+  if (!lv->params_set) return fail(c, ELBM_E_STATE, "set the level parameters before the links");
+  Links39 L;
+  std::string why;
+  const int rc = decode_links39(state, ngrow_state, b->nx, b->ny, b->nz, lv->p39.periodic, lv->p39.shifted,
+                                lv->p39.primary_flow_dir, bc->inlet_type, bc->outlet_type, L, why);
+  if (rc) return fail(c, rc, "%s", why.c_str());
+  double tf[kEqTables][39], tg[kEqTables][39];
+  for (int j = 0; j < 39; ++j) {
+    tf[0][j] = bc->fs_fieq[j];
+    tg[0][j] = bc->fs_gieq[j];
+    for (int k = 0; k < 8; ++k) {
+      tf[1 + k][j] = bc->inl_fieq[k][j];
+      tg[1 + k][j] = bc->inl_gieq[k][j];
+      tf[9 + k][j] = bc->outl_fieq[k][j];
+      tg[9 + k][j] = bc->outl_gieq[k][j];
+    }
+  }
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  if (!lv->eq39f.p) CUDA_TRY(lv->eq39f.alloc(kEqTables * 39), "equilibria");
+  if (!lv->eq39g.p) CUDA_TRY(lv->eq39g.alloc(kEqTables * 39), "equilibria");
+  CUDA_TRY(cudaMemcpy(lv->eq39f.p, tf, sizeof tf, cudaMemcpyHostToDevice), "equilibria");
+  CUDA_TRY(cudaMemcpy(lv->eq39g.p, tg, sizeof tg, cudaMemcpyHostToDevice), "equilibria");
+  CUDA_TRY(b->ntype39.alloc(b->N), "node types");
+  CUDA_TRY(cudaMemcpy(b->ntype39.p, L.ntype.data(), b->N, cudaMemcpyHostToDevice), "node types");
+  CUDA_TRY(b->bidx39.alloc(b->N), "records");
+  CUDA_TRY(cudaMemcpy(b->bidx39.p, L.bidx.data(), b->N * sizeof(int32_t), cudaMemcpyHostToDevice), "records");
+  b->nrec39 = (int64_t)L.bnodes.size();
+  const size_t nr = std::max<size_t>(L.bnodes.size(), 1);
+  CUDA_TRY(b->bnodes39.alloc(nr), "records");
+  CUDA_TRY(b->words39.alloc(nr * 39), "link words");
+  CUDA_TRY(b->fprev39.alloc(nr * 39), "post-streaming f");
+  CUDA_TRY(b->gprev39.alloc(nr * 39), "post-streaming g");
+  if (!L.bnodes.empty()) {
+    CUDA_TRY(cudaMemcpy(b->bnodes39.p, L.bnodes.data(), L.bnodes.size() * sizeof(int32_t), cudaMemcpyHostToDevice),
+             "records");
+    CUDA_TRY(cudaMemcpy(b->words39.p, L.words.data(), L.words.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
+             "link words");
+  }
+  b->links39 = true;
+  // until a step has run, a slot that no rule writes holds the node's uploaded fout
+  if (b->data_set) launch_stale39_init(*b, c->stream);
+  CUDA_TRY(cudaGetLastError(), "stale init");
   return ELBM_OK;
 }
 
@@ -1393,6 +1489,7 @@ int elbm_upload_level39(elbm_ctx* c, int lvl, int box, const double* fout, const
   CUDA_TRY(fab_to_packed(lm, b->lm.p, *b, lv->ngrow, 13, b->plane, c->stream), "upload lm");
   CUDA_TRY(fab_to_packed(w_vel, b->w_vel.p, *b, lv->ngrow, 1, b->plane, c->stream), "upload w");
   CUDA_TRY(cudaMemsetAsync(b->alpha64.p, 0, b->alpha64.n * sizeof(double), c->stream), "alpha");
+  if (b->links39) launch_stale39_init(*b, c->stream);
   CUDA_TRY(cudaMemsetAsync(b->macro.p, 0, b->macro.n * sizeof(double), c->stream), "macro");
   CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
   b->cur = 0;

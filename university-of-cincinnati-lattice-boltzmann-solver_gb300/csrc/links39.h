@@ -1,0 +1,19 @@
+// Pull-form link tables of a D3Q39 box (csrc/links39.cu).
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace elbm {
+
+struct Links39 {
+  std::vector<uint8_t> ntype;   // per node: 0 neither pushes nor collides, 1 bulk, 2 boundary record
+  std::vector<int32_t> bidx;    // per node: boundary record or -1
+  std::vector<int32_t> bnodes;  // per record: node
+  std::vector<uint32_t> words;  // 39 per record
+};
+
+int decode_links39(const int32_t* st, int ngs, int nx, int ny, int nz, int periodic, int shifted, int pfd,
+                   const int32_t* inlet_type, const int32_t* outlet_type, Links39& out, std::string& why);
+
+}  // namespace elbm

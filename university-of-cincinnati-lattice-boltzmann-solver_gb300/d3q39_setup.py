@@ -134,3 +134,57 @@ def wedge_case_consts(**kw) -> D3Q39Consts:
     args = dict(temperature_K=T, pressure_Pa=p, v_inf_ms=1.5 * c, dx_m=1e-4, gama=gama, primary_flow_dir=1)
     args.update(kw)
     return reference_consts(**args)
+
+
+# D3Q39 velocities in the reference's order and its opposites (1-based in the
+# reference, general/background_calcs/directions_and_weights.f95:463-499).
+CX39 = [0, 1, 0, 0, -1, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1, 2, 0, 0, -2, 0,
+        0, 2, 2, 0, -2, -2, 2, 2, -2, -2, 0, 0, 0, 3, 0, 0, -3, 0, 0]
+CY39 = [0, 0, 1, 0, 0, -1, 0, 1, 1, -1, -1, 1, 1, -1, -1, 0, 2, 0, 0, -2,
+        0, 2, 0, 2, 2, -2, -2, 0, 0, 0, 2, -2, -2, 0, 3, 0, 0, -3, 0]
+CZ39 = [0, 0, 0, 1, 0, 0, -1, 1, 1, 1, 1, -1, -1, -1, -1, 0, 0, 2, 0, 0,
+        -2, 0, 2, 2, 0, 0, 0, -2, -2, 2, -2, -2, 2, 0, 0, 3, 0, 0, -3]
+OPP39 = [1, 5, 6, 7, 2, 3, 4, 14, 15, 12, 13, 10, 11, 8, 9, 19, 20, 21, 16, 17,
+         18, 26, 29, 32, 27, 22, 25, 30, 23, 28, 33, 24, 31, 37, 38, 39, 34, 35, 36]
+
+
+def lattice39(shifted: int, primary_flow_dir: int = 1):
+    """Streaming velocities (cx, cy, cz) and opposites (0-based) of the D3Q39
+    set; the shifted set adds one unit along the primary flow direction and
+    maps every direction to itself as its opposite (directions_and_weights.f95:477-499)."""
+    cx, cy, cz = (np.array(v, np.int64) for v in (CX39, CY39, CZ39))
+    if shifted:
+        axis, sign = (primary_flow_dir - 1) % 3, (1 if primary_flow_dir <= 3 else -1)
+        (cx, cy, cz)[axis][:] += sign
+        opp = np.arange(39)
+    else:
+        opp = np.array(OPP39) - 1
+    return cx, cy, cz, opp
+
+
+def box_state39(nx: int, ny: int, nz: int, faces: dict, shifted: int, primary_flow_dir: int = 1, periodic: int = 0,
+                priority=("x-", "x+", "z-", "z+", "y-", "y+")) -> np.ndarray:
+    """int32 state (39, nz, ny, nx) of a box: a link that leaves the box across a
+    non-periodic face carries that face's code (faces: 'x-', 'x+', 'y-', 'y+',
+    'z-', 'z+'); links crossing two faces take the code of the first in
+    `priority`; component 0 (node type) is 0."""
+    cx, cy, cz, _ = lattice39(shifted, primary_flow_dir)
+    st = np.zeros((39, nz, ny, nx), np.int32)
+    x = np.arange(nx)[None, None, :]
+    y = np.arange(ny)[None, :, None]
+    z = np.arange(nz)[:, None, None]
+    shape = (nz, ny, nx)
+    for i in range(1, 39):
+        comp = np.zeros(shape, np.int32)
+        crossed = {
+            "x-": np.broadcast_to((x + cx[i] < 0) & (not periodic & 1), shape),
+            "x+": np.broadcast_to((x + cx[i] >= nx) & (not periodic & 1), shape),
+            "y-": np.broadcast_to((y + cy[i] < 0) & (not periodic & 2), shape),
+            "y+": np.broadcast_to((y + cy[i] >= ny) & (not periodic & 2), shape),
+            "z-": np.broadcast_to((z + cz[i] < 0) & (not periodic & 4), shape),
+            "z+": np.broadcast_to((z + cz[i] >= nz) & (not periodic & 4), shape),
+        }
+        for face in reversed(priority):
+            comp[crossed[face]] = faces[face]
+        st[i] = comp
+    return st

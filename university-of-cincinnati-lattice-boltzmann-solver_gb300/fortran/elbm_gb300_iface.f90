@@ -37,6 +37,13 @@ module elbm_gb300_iface
     real(c_double) :: dt, elbm_epsilon, init_beta_1, init_beta_2, beta_1_scaling, beta_2_scaling
   end type
 
+  type, bind(c), public :: elbm_d3q39_bc
+    integer(c_int32_t) :: inlet_type(8), outlet_type(8)
+    real(c_double) :: fs_fieq(39), fs_gieq(39)
+    real(c_double) :: inl_fieq(39, 8), inl_gieq(39, 8)    ! C layout [8][39]
+    real(c_double) :: outl_fieq(39, 8), outl_gieq(39, 8)
+  end type
+
   type, bind(c), public :: elbm_stats
     integer(c_int64_t) :: node_updates, newton_iters, exact_path_nodes, fallbacks
     integer(c_int32_t) :: status, pad
@@ -50,7 +57,7 @@ module elbm_gb300_iface
     elbm_set_d3q39_params, elbm_upload_level39, elbm_download_level39, elbm_mark_triangles, &
     elbm_upload_level_noalloc, elbm_autotune, elbm_set_kernel_variant, elbm_alpha_harvest, &
     elbm_alpha_mlp_train, elbm_set_alpha_mlp, elbm_interlevel_setup, elbm_fill_fine_ghosts, &
-    elbm_average_down, elbm_amr_run, elbm_damp_level
+    elbm_average_down, elbm_amr_run, elbm_damp_level, elbm_set_links39
 
   interface
     integer(c_int) function elbm_create(device, ctx) bind(c, name="elbm_create")
@@ -209,6 +216,13 @@ module elbm_gb300_iface
       type(c_ptr), value :: ctx
       integer(c_int), value :: lvl
       integer(c_int64_t), intent(out) :: repaired
+    end function
+    integer(c_int) function elbm_set_links39(ctx, lvl, box, state, ngrow_state, bc) bind(c, name="elbm_set_links39")
+      import :: c_int, c_ptr, c_int32_t, elbm_d3q39_bc
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl, box, ngrow_state
+      integer(c_int32_t), intent(in) :: state(*)      ! mfstate(lvl)%dataptr(mfi), 39 comps
+      type(elbm_d3q39_bc), intent(in) :: bc
     end function
   end interface
 end module elbm_gb300_iface
