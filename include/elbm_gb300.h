@@ -98,6 +98,8 @@ typedef struct {
   int32_t pad;
   double gama, t_ref, rho_ref, p_ref, mu_ref, kappa_ref, gas_const_R, const_vol, const_press, molec_weight;
   double dt, elbm_epsilon, init_beta_1, init_beta_2, beta_1_scaling, beta_2_scaling;
+  double su_lm[13];          /* start-up multipliers su_chi .. su_lambda_z (freestream_basis_calcs.f90:127-150):
+                                the warm start next to interpolated walls in the first steps */
 } elbm_d3q39_params;
 
 typedef struct {
@@ -138,6 +140,12 @@ int elbm_set_d3q39_params(elbm_ctx* ctx, int lvl, const elbm_d3q39_params* p);
  * step's w velocity (1 comp), all as FABs with the level's ghost width. */
 int elbm_upload_level39(elbm_ctx* ctx, int lvl, int box, const double* fout, const double* gout, const double* lm,
                         const double* w_vel);
+/* The macroscopic fields rho, u, v, w, T (5 comps, FAB layout) the step
+ * starts from: the reference's rho, u_vel, v_vel, w_vel, temp after
+ * initialisation (multilevel_initialization.f90).  Needed by interpolated wall
+ * links, which read the previous step's fields of the wall nodes and their
+ * neighbours; call after elbm_upload_level39 (which clears them). */
+int elbm_upload_macro39(elbm_ctx* ctx, int lvl, int box, const double* macro);
 /* Any output pointer may be NULL.  macro: rho, u, v, w, T (5 comps). */
 int elbm_download_level39(elbm_ctx* ctx, int lvl, int box, double* fout, double* gout, double* lm, double* w_vel,
                           double* alpha, double* macro);
@@ -152,6 +160,8 @@ typedef struct {
   double fs_fieq[39], fs_gieq[39];
   double inl_fieq[8][39], inl_gieq[8][39];
   double outl_fieq[8][39], outl_gieq[8][39];
+  double fs_u, fs_v, fs_w, fs_temp; /* freestream velocity and temperature (fs_u .. temperature of the
+                                       reference), read by the interpolated wall links */
 } elbm_d3q39_bc;
 
 /* Link codes of a D3Q39 box (state FAB, 39 comps, ngrow_state ghosts), for
@@ -162,18 +172,25 @@ typedef struct {
  * lattice) leaves in the post-streaming slot: a population of a node within 4
  * links, a boundary equilibrium, or the slot's value of the previous step.
  * Supported codes: >= 0, -5, -8, -10, -100-k, -200-k, -300-k, -400-k, -666,
- * -1000; others (inviscid walls, interpolated walls) give ELBM_E_UNSUPPORTED.
- * Nodes with state < 0 neither push nor collide; state >= 0 must be fluid
- * (outside 200..298 and 1000..50999).  The negative-population repair
- * (damp = 1) is not available with link codes. */
+ * -1000, and on the shifted lattice with primary_flow_dir 1 the interpolated
+ * wall links -1001 - floor(q 1e9) (Grad-type closure of shifted_ibb.f95 with
+ * the targets of target_finder.f95; they read the previous step's macroscopic
+ * fields, so elbm_upload_macro39 must follow elbm_upload_level39).  Inviscid
+ * walls (-11, -12) give ELBM_E_UNSUPPORTED.  Nodes with state < 0 neither
+ * push nor collide; state >= 0 must be fluid (outside 200..298 and
+ * 1000..50999); nodes outside the box on a non-periodic axis count as null
+ * nodes (-666), as lbgrid/fluid_or_solid.f95:69-119 marks them for an
+ * external flow.  The negative-population repair (damp = 1) is not available
+ * with link codes. */
 int elbm_set_links39(elbm_ctx* ctx, int lvl, int box, const int32_t* state, int ngrow_state,
                      const elbm_d3q39_bc* bc);
 
 /* The tables elbm_set_links39 builds, on the host only (no device, no
  * context): per node a type (0 neither pushes nor collides, 1 plain pulls,
- * 2 boundary record) and, for each of the *nrec records (at most capacity),
- * the node and 39 link words (bits 0-1 kind: 0 previous post-streaming value,
- * 1 pull, 2 equilibrium; bits 2-7 population; 8-12 table; 13-22 offset
+ * 2 boundary record, 3 boundary record with interpolated wall links) and, for
+ * each of the *nrec records (at most capacity), the node and 39 link words
+ * (bits 0-1 kind: 0 previous post-streaming value, 1 pull, 2 equilibrium,
+ * 3 interpolated wall value; bits 2-7 population; 8-12 table; 13-22 offset
  * (dx+4) + 9(dy+4) + 81(dz+4)).  For inspection and tests. */
 int elbm_links39_tables(int nx, int ny, int nz, const int32_t* state, int ngrow_state, int periodic, int shifted,
                         int primary_flow_dir, const int32_t* inlet_type, const int32_t* outlet_type, uint8_t* ntype,

@@ -369,6 +369,13 @@ static void collide39(const o39_consts* k, const o39_lattice* Lp, o39_level* s, 
       g[i] = gi[(int64_t)i * N + n];
     }
     for (int r = 0; r < NLM; ++r) lm[r] = s->lm[(int64_t)r * N + n];
+    if (state && k->shifted && step <= 1) {
+      /* calculate_flow_variables.f95:236-271: next to a wall in the first steps the solve starts from su_* */
+      int wall = 0;
+      for (int i = 0; i < Q; ++i) wall |= state[(int64_t)i * N + n] < -1000;
+      if (wall)
+        for (int r = 0; r < NLM; ++r) lm[r] = k->su_lm[r];
+    }
     double rs = 0, us = 0, vs = 0, ws = 0, es = 0;
     for (int i = 0; i < Q; ++i) {
       rs = rs + f[i];
@@ -497,7 +504,202 @@ typedef struct {
   double fs_fieq[Q], fs_gieq[Q];
   double inl_fieq[8][Q], inl_gieq[8][Q];
   double outl_fieq[8][Q], outl_gieq[8][Q];
+  double fs_u, fs_v, fs_w, fs_temp; /* freestream velocity and temperature (lattice units) */
 } o39_bc;
+
+/* ---- Grad-type interpolated wall links on the shifted lattice ----
+ *
+ * streaming.f95:478-1133 (case -1100000000..-1001), target_finder.f95:89-140,
+ * shifted_ibb.f95:45-267 and derivatives.f95:816-1300.  The code of link i of
+ * node x packs the wall distance q = |code + 1001| / 1e9 (linkwise.f95:56).
+ * A node is "adjacent" when one of its components 0..14 is below -1000
+ * (streaming.f95:492): it then takes targets from target_finder and a Newton
+ * solve of the target equilibrium at its first wall link of the step
+ * (node_pt, streaming.f95:261, 488, 1129); otherwise the node's own previous
+ * macroscopic values and multipliers are the targets. */
+
+/* direction 1..39 of the unshifted D3Q39 order as 0-based; erp = the unshifted opposites */
+static int erp39(int i) { return OPP0[i] - 1; }
+
+/* derivatives.f95:816-1300: for direction i and axis (0 x, 1 y, 2 z), 1 when the
+ * one-sided wall derivative is taken (up = 1: (q_target - q_wall), else
+ * (q_wall - q_target)), 0 for the local central/one-sided difference.  Wall
+ * derivatives on every axis where the unshifted velocity has a component,
+ * up when it is negative; the rest direction takes the wall derivative along
+ * x; directions 28, 30, 31 and 33 (1-based) carry the opposite up flags on
+ * their two non-zero axes. */
+static int ibb_wall_axis(int i, int axis, int* up) {
+  const int c = axis == 0 ? CX0[i] : axis == 1 ? CY0[i] : CZ0[i];
+  if (i == 0) {
+    *up = 0;
+    return axis == 0;
+  }
+  if (c == 0) return 0;
+  *up = c < 0;
+  if (i == 27 || i == 29 || i == 30 || i == 32) *up = !*up;
+  return 1;
+}
+
+/* dudx_local (derivatives.f95) */
+static double d_local(double q_rest, double q_up, double q_down, int s_up, int s_down) {
+  if (s_up >= 0 && s_down >= 0) return (q_down - q_up) / 2.0;
+  if (s_up >= 0) return q_rest - q_up;
+  if (s_down >= 0) return q_down - q_rest;
+  return 0.0;
+}
+
+/* first_order_shifted_{vel,temp}_cond_unknown: the wall form is dudx_ibb(q_target, q_wall);
+ * the velocity passes q_wall = 0, the temperature q_wall = q_target */
+static double d_shifted(const o39_lattice* L, double q_rest, double q_target, double q_up, double q_down, int i,
+                        int axis, int s_up, int s_down, int temperature) {
+  int up = 0;
+  if (ibb_wall_axis(i, axis, &up)) {
+    const double dir_state = (fabs((double)s_down + 1001.0) / 1.0e9) * sqrt(L->cmag[i]);
+    const double q_wall = temperature ? q_target : 0.0;
+    return up ? (q_target - q_wall) / (1.0 + dir_state) : (q_wall - q_target) / (1.0 + dir_state);
+  }
+  return d_local(q_rest, q_up, q_down, s_up, s_down);
+}
+
+/* shifted_ibb.f95:45-267: the missing post-streaming populations of wall link i */
+static void shifted_ibb39(const o39_consts* k, const o39_lattice* L, int i, int step, double fieq, double gieq,
+                          double rho, double ut, double vt, double wt, double Tt, const double* ul, const double* vl,
+                          const double* wl, const double* Tl, const int* sp, double* fout, double* gout) {
+  const double cv = k->const_vol;
+  const double k_fi = -(rho * Tt) / 2.0;
+  const double k_gi = -(rho * Tt * (2.0 * cv - 3)) / 2.0;
+  const double eps = epsilon_at(k, step);
+  double mu, kappa;
+  sutherland(k, Tt, &mu, NULL, NULL);
+  therm_cond(k, rho, Tt, &kappa);
+  double b1, b2;
+  if (step < k->startup_timesteps) {
+    b1 = k->init_beta_1 + k->beta_1_scaling * step;
+    b2 = k->init_beta_2 + k->beta_2_scaling * step;
+  } else {
+    b1 = 1.0 / ((pow(2.0, k->lvl + 1) * mu) / (rho * Tt) + 1.0);
+    b2 = 1.0 / ((2.0 * kappa) / (rho * k->const_press * Tt) + 1.0);
+  }
+  /* stencil points 0 rest, 1 +x, 2 +y, 3 +z, 4 -x, 5 -y, 6 -z; up = minus side, down = plus side */
+  double du[3], dv[3], dw[3], dT[3];
+  for (int a = 0; a < 3; ++a) {
+    du[a] = d_shifted(L, ul[0], ut, ul[4 + a], ul[1 + a], i, a, sp[4 + a], sp[1 + a], 0);
+    dv[a] = d_shifted(L, vl[0], vt, vl[4 + a], vl[1 + a], i, a, sp[4 + a], sp[1 + a], 0);
+    dw[a] = d_shifted(L, wl[0], wt, wl[4 + a], wl[1 + a], i, a, sp[4 + a], sp[1 + a], 0);
+    dT[a] = d_shifted(L, Tl[0], Tt, Tl[4 + a], Tl[1 + a], i, a, sp[4 + a], sp[1 + a], 1);
+  }
+  const double dudx = du[0], dudy = du[1], dudz = du[2], dvdx = dv[0], dvdy = dv[1], dvdz = dv[2];
+  const double dwdx = dw[0], dwdy = dw[1], dwdz = dw[2], dTdx = dT[0], dTdy = dT[1], dTdz = dT[2];
+  /* pressure-tensor gradients (27 ordered pairs, xx.. zz, with the trace parts) */
+  double p[27];
+  p[0] = 2 * dudx - dudx / cv;
+  p[1] = 2 * dudx - dvdy / cv;
+  p[2] = 2 * dudx - dwdz / cv;
+  p[3] = p[4] = p[5] = dudy + dvdx;
+  p[6] = p[7] = p[8] = dudz + dwdx;
+  p[9] = p[10] = p[11] = dudy + dvdx;
+  p[12] = 2 * dvdy - dudx / cv;
+  p[13] = 2 * dvdy - dvdy / cv;
+  p[14] = 2 * dvdy - dwdz / cv;
+  p[15] = p[16] = p[17] = dvdz + dwdy;
+  p[18] = p[19] = p[20] = dudz + dwdx;
+  p[21] = p[22] = p[23] = dvdz + dwdy;
+  p[24] = 2 * dwdz - dudx / cv;
+  p[25] = 2 * dwdz - dvdy / cv;
+  p[26] = 2 * dwdz - dwdz / cv;
+  for (int m = 0; m < 27; ++m) p[m] = p[m] / b1;
+  double q[27];
+  q[0] = 3 * (dTdx / b2 + ut * p[0]);
+  q[1] = (dTdy / b2 + vt * p[1] + 2 * ut * p[3]);
+  q[2] = (dTdz / b2 + wt * p[2] + 2 * ut * p[6]);
+  q[3] = (dTdy / b2 + 2 * ut * p[3] + vt * p[0]);
+  q[4] = (dTdx / b2 + ut * p[12] + 2 * vt * p[3]);
+  q[5] = (ut * p[21] + vt * p[6] + wt * p[3]);
+  q[6] = (dTdz / b2 + wt * p[2] + 2 * ut * p[6]);
+  q[7] = (ut * p[21] + vt * p[6] + wt * p[3]);
+  q[8] = (dTdx / b2 + ut * p[24] + 2 * wt * p[6]);
+  q[9] = (dTdy / b2 + vt * p[1] + 2 * ut * p[3]);
+  q[10] = (dTdx / b2 + 2 * vt * p[3] + ut * p[12]);
+  q[11] = (ut * p[21] + vt * p[6] + wt * p[3]);
+  q[12] = (dTdx / b2 + ut * p[12] + 2 * vt * p[3]);
+  q[13] = 3 * (dTdy / b2 + vt * p[13]);
+  q[14] = (dTdz / b2 + wt * p[14] + 2 * vt * p[21]);
+  q[15] = (ut * p[21] + vt * p[6] + wt * p[3]);
+  q[16] = (dTdz / b2 + wt * p[14] + 2 * vt * p[21]);
+  q[17] = (dTdy / b2 + vt * p[25] + 2 * wt * p[21]);
+  q[18] = (dTdx / b2 + wt * p[2] + 2 * ut * p[6]);
+  q[19] = (ut * p[21] + vt * p[6] + wt * p[3]);
+  q[20] = (dTdx / b2 + ut * p[24] + 2 * wt * p[6]);
+  q[21] = (ut * p[21] + vt * p[6] + wt * p[3]);
+  q[22] = (dTdz / b2 + wt * p[14] + 2 * vt * p[21]);
+  q[23] = (dTdy / b2 + vt * p[25] + 2 * wt * p[21]);
+  q[24] = (dTdx / b2 + ut * p[24] + 2 * wt * p[6]);
+  q[25] = (dTdy / b2 + vt * p[25] + 2 * wt * p[21]);
+  q[26] = 3 * (dTdz / b2 + wt * p[26]);
+  const int cx = L->cx[i], cy = L->cy[i], cz = L->cz[i];
+  /* sum of p_ab (c_a c_b - T delta_ab) in the reference's term order (its 25th term appears twice) */
+  const double xx = cx * cx - Tt, yy = cy * cy - Tt, zz = cz * cz - Tt;
+  const double p_comp =
+      (p[0] * xx + p[1] * xx + p[2] * xx + p[3] * cx * cy + p[4] * cx * cy + p[5] * cx * cy + p[6] * cx * cz +
+       p[7] * cx * cz + p[8] * cx * cz + p[9] * cy * cx + p[10] * cy * cx + p[11] * cy * cx + p[12] * yy +
+       p[13] * yy + p[14] * yy + p[15] * cy * cz + p[16] * cy * cz + p[17] * cy * cz + p[18] * cz * cx +
+       p[19] * cz * cx + p[20] * cz * cx + p[21] * cz * cy + p[22] * cz * cy + p[23] * cz * cy + p[24] * zz +
+       p[24] * zz + p[25] * zz + p[26] * zz) /
+      (2 * (Tt * Tt));
+  const int cx2 = cx * cx, cy2 = cy * cy, cz2 = cz * cz;
+  const double q_comp =
+      (q[0] * (cx2 * cx - 3 * cx * Tt) + q[1] * (cx2 * cy - 3 * cy * Tt) + q[2] * (cx2 * cz - 3 * cz * Tt) +
+       q[3] * cx2 * cy + q[4] * cx * cy2 + q[5] * cx * cy * cz + q[6] * cx2 * cz + q[7] * cx * cy * cz +
+       q[8] * cx * cz2 + q[9] * cx2 * cy + q[10] * cy2 * cx + q[11] * cx * cy * cz +
+       q[12] * (cy2 * cx - 3 * cx * Tt) + q[13] * (cy2 * cy - 3 * cy * Tt) + q[14] * (cy2 * cz - 3 * cz * Tt) +
+       q[15] * cx * cy * cz + q[16] * cy2 * cz + q[17] * cz2 * cy + q[18] * cx2 * cz + q[19] * cx * cy * cz +
+       q[20] * cz2 * cx + q[21] * cx * cy * cz + q[22] * cz * cy2 + q[23] * cz2 * cy +
+       q[24] * (cz2 * cx - 3 * cx * Tt) + q[25] * (cz2 * cy - 3 * cy * Tt) + q[26] * (cz2 * cz - 3 * cz * Tt)) /
+      (6 * (Tt * Tt * Tt));
+  double fo = fieq + eps * k_fi * (p_comp + q_comp);
+  const double k_one = 3 * (dTdx + dTdy + dTdz) / (b1 * cv);
+  const double g_alpha = cx / Tt * (9 * dTdx / b2 + ut * k_one) + cy / Tt * (9 * dTdy / b2 + vt * k_one) +
+                         cz / Tt * (9 * dTdz / b2 + wt * k_one);
+  double r[27];
+  r[0] = 2 * Tt * dudx + 2 * ut * dTdx - dudx / cv * (2 * Tt + ut * ut);
+  r[1] = 2 * Tt * dudx + 2 * ut * dTdx - dvdy / cv * (2 * Tt + ut * ut);
+  r[2] = 2 * Tt * dudx + 2 * ut * dTdx - dwdz / cv * (2 * Tt + ut * ut);
+  r[3] = Tt * (dudy + dvdx) + ut * dTdy + vt * dTdx - dudx / cv * ut * vt;
+  r[4] = Tt * (dudy + dvdx) + ut * dTdy + vt * dTdx - dvdy / cv * ut * vt;
+  r[5] = Tt * (dudy + dvdx) + ut * dTdy + vt * dTdx - dwdz / cv * ut * vt;
+  r[6] = Tt * (dudz + dwdx) + ut * dTdz + wt * dTdx - dudx / cv * ut * wt;
+  r[7] = Tt * (dudz + dwdx) + ut * dTdz + wt * dTdx - dvdy / cv * ut * wt;
+  r[8] = Tt * (dudz + dwdx) + ut * dTdz + wt * dTdx - dwdz / cv * ut * wt;
+  r[9] = r[3];
+  r[10] = r[4];
+  r[11] = r[5];
+  r[12] = 2 * Tt * dvdy + 2 * vt * dTdy - dudx / cv * (2 * Tt + vt * vt);
+  r[13] = 2 * Tt * dvdy + 2 * vt * dTdy - dvdy / cv * (2 * Tt + vt * vt);
+  r[14] = 2 * Tt * dvdy + 2 * vt * dTdy - dwdz / cv * (2 * Tt + vt * vt);
+  r[15] = Tt * (dvdz + dwdy) + wt * dTdy + vt * dTdz - dudx / cv * vt * wt;
+  r[16] = Tt * (dvdz + dwdy) + wt * dTdy + vt * dTdz - dvdy / cv * vt * wt;
+  r[17] = Tt * (dvdz + dwdy) + wt * dTdy + vt * dTdz - dwdz / cv * vt * wt;
+  r[18] = r[6];
+  r[19] = r[7];
+  r[20] = r[8];
+  r[21] = r[12];
+  r[22] = r[13];
+  r[23] = r[14];
+  r[24] = 2 * Tt * dwdz + 2 * wt * dTdz - dudx / cv * (2 * Tt + wt * wt);
+  r[25] = 2 * Tt * dwdz + 2 * wt * dTdz - dvdy / cv * (2 * Tt + wt * wt);
+  r[26] = 2 * Tt * dwdz + 2 * wt * dTdz - dwdz / cv * (2 * Tt + wt * wt);
+  const double r_sum = r[0] * xx + r[1] * xx + r[2] * xx + r[3] * cx * cy + r[4] * cx * cy + r[5] * cx * cy +
+                       r[6] * cx * cz + r[7] * cx * cz + r[8] * cx * cz + r[9] * cy * cx + r[10] * cy * cx +
+                       r[11] * cy * cx + r[12] * yy + r[13] * yy + r[14] * yy + r[15] * cy * cz + r[16] * cy * cz +
+                       r[17] * cy * cz + r[18] * cz * cx + r[19] * cz * cx + r[20] * cz * cx + r[21] * cz * cy +
+                       r[22] * cz * cy + r[23] * cz * cy + r[24] * zz + r[25] * zz + r[26] * zz;
+  const double gi_neq = k_gi * (3 * k_one + g_alpha + r_sum / (2 * b1 * Tt));
+  double go = gieq + eps * gi_neq;
+  if (fo < 0.0) fo = fabs(fo);
+  if (go < 0.0) go = fabs(go);
+  *fout = fo;
+  *gout = go;
+}
 
 /* One level step of a box with the reference's link codes: the push loop of
  * streaming.f95:266-481 in its order (direction outermost, then z, y, x), with
@@ -517,6 +719,137 @@ typedef struct {
  * (fi_prev / gi_prev, updated here).  Periodic axes wrap (bit 0/1/2 = x/y/z);
  * pushes across a non-periodic face leave the box.  Then every fluid node
  * collides.  Returns -1 for a code outside this list. */
+/* Per-step target cache of the wall-link nodes (node_pt and the *_temp fields of streaming.f95). */
+typedef struct {
+  unsigned char* done;
+  double* tgt; /* rho, u, v, w, T per node */
+  double* tlm; /* 13 multipliers per node */
+} o39_targets;
+
+/* index of (x, y, z) with periodic wrap, -1 outside the box on a non-periodic axis */
+static int64_t nb39(int x, int y, int z, int nx, int ny, int nz, int periodic) {
+  if (periodic & 1) x = wrap(x, nx); else if (x < 0 || x >= nx) return -1;
+  if (periodic & 2) y = wrap(y, ny); else if (y < 0 || y >= ny) return -1;
+  if (periodic & 4) z = wrap(z, nz); else if (z < 0 || z >= nz) return -1;
+  return idx3(x, y, z, nx, ny);
+}
+
+/* Wall link i of fluid node n at (x, y, z) during the push loop: the value
+ * shifted_ibb writes into fi(x, i) and gi(x, i).  fi, gi are the post-streaming
+ * arrays as the loop has left them so far (target_finder reads them).  Node
+ * types outside the box on a non-periodic axis count as -666 (the outside
+ * nodes of an external flow, fluid_or_solid.f95:69-119).  Returns -2 when a
+ * read leaves the box. */
+static int ibb_link39(const o39_consts* k, const o39_lattice* L, const o39_level* s, const int32_t* state,
+                      int periodic, const o39_bc* bc, int step, int64_t n, int x, int y, int z, int i,
+                      const double* fi, o39_targets* tc, double* fv, double* gv) {
+  const int nx = s->nx, ny = s->ny, nz = s->nz;
+  const int64_t N = (int64_t)nx * ny * nz;
+#define CODE39(j) ((j) == 0 ? state[n] : state[(int64_t)(j) * N + n])
+  int adjacent = 0;
+  for (int j = 0; j < 15; ++j) adjacent |= CODE39(j) < -1000;
+  const int first = !tc->done[n];
+  double rho_t, ut, vt, wt, Tt, lm_t[NLM];
+  if (adjacent) {
+    if (first) {
+      /* target_finder.f95:89-140 */
+      int count = 0;
+      double r_ = 0, u_ = 0, v_ = 0, w_ = 0, T_ = 0;
+      for (int j = 0; j < Q; ++j) {
+        const int32_t cj = CODE39(j);
+        if (cj <= -1001) {
+          const double d = fabs(((double)cj + 1001.0) / 1.0e9);
+          count++;
+          const int src = CODE39(erp39(j)) == -666 ? j : 4;
+          const int64_t m = nb39(x + L->cx[src], y + L->cy[src], z + L->cz[src], nx, ny, nz, periodic);
+          if (m < 0) return -2;
+          u_ = u_ + (d * s->u[m]) / (d + 1.0);
+          v_ = v_ + (d * s->v[m]) / (d + 1.0);
+          w_ = w_ + (d * s->w_vel[m]) / (d + 1.0);
+          T_ = T_ + (d * s->temp[m] + s->temp[m]) / (d + 1.0);
+        }
+        if (CODE39(L->opp[j]) < -1000) r_ = r_ + fi[(int64_t)erp39(j) * N + n];
+        else r_ = r_ + fi[(int64_t)j * N + n];
+      }
+      rho_t = r_;
+      ut = u_ / count;
+      vt = v_ / count;
+      wt = w_ / count;
+      Tt = T_ / count;
+      /* streaming.f95:788-850: warm start from the node's multipliers (the start-up set for timestep <= 4) */
+      for (int r = 0; r < NLM; ++r) lm_t[r] = (step <= 4) ? k->su_lm[r] : s->lm[(int64_t)r * N + n];
+      const double P[6] = {rho_t * Tt + rho_t * (ut * ut), rho_t * Tt + rho_t * (vt * vt),
+                           rho_t * Tt + rho_t * (wt * wt), rho_t * ut * vt, rho_t * ut * wt, rho_t * vt * wt};
+      double fe[Q];
+      o39_lagrange(L, k->max_lm_iters, rho_t, ut, vt, wt, Tt, P, lm_t, fe);
+      tc->tgt[5 * n + 0] = rho_t;
+      tc->tgt[5 * n + 1] = ut;
+      tc->tgt[5 * n + 2] = vt;
+      tc->tgt[5 * n + 3] = wt;
+      tc->tgt[5 * n + 4] = Tt;
+      for (int r = 0; r < NLM; ++r) tc->tlm[NLM * n + r] = lm_t[r];
+    } else {
+      rho_t = tc->tgt[5 * n + 0];
+      ut = tc->tgt[5 * n + 1];
+      vt = tc->tgt[5 * n + 2];
+      wt = tc->tgt[5 * n + 3];
+      Tt = tc->tgt[5 * n + 4];
+      for (int r = 0; r < NLM; ++r) lm_t[r] = tc->tlm[NLM * n + r];
+    }
+  } else {
+    rho_t = s->rho[n];
+    ut = s->u[n];
+    vt = s->v[n];
+    wt = s->w_vel[n];
+    Tt = s->temp[n];
+    for (int r = 0; r < NLM; ++r) lm_t[r] = s->lm[(int64_t)r * N + n];
+  }
+  tc->done[n] = 1;
+  const double fieq = fieq39(L, rho_t, lm_t, i);
+  const double gieq = (2.0 * k->const_vol - 3) * Tt * fieq;
+  /* the seven-point stencil: rest, +x, +y, +z, -x, -y, -z (cx_27 of linkwise.f95) */
+  static const int SX[7] = {0, 1, 0, 0, -1, 0, 0}, SY[7] = {0, 0, 1, 0, 0, -1, 0}, SZ[7] = {0, 0, 0, 1, 0, 0, -1};
+  double ul[7], vl[7], wl[7], Tl[7];
+  int sp[7];
+  for (int j = 0; j < 7; ++j) {
+    const int64_t m = nb39(x + SX[j], y + SY[j], z + SZ[j], nx, ny, nz, periodic);
+    const int32_t t = m < 0 ? -666 : state[m];
+    sp[j] = t;
+    if (t >= 0) {
+      ul[j] = s->u[m];
+      vl[j] = s->v[m];
+      wl[j] = s->w_vel[m];
+      /* the adjacent branch reads T at the stencil node; the other branch one lattice shift further
+       * (temp(a + cx(j), ...) with the shifted cx, streaming.f95:1059 and :714) */
+      int64_t mt = m;
+      if (!adjacent) {
+        mt = first ? nb39(x + L->cx[j], y + L->cy[j], z + L->cz[j], nx, ny, nz, periodic)
+                   : nb39(x + L->cx[j], y + SY[j], z + SZ[j], nx, ny, nz, periodic);
+        if (mt < 0) return -2;
+      }
+      Tl[j] = s->temp[mt];
+    } else if (t == -11) {
+      ul[j] = s->u[n];
+      vl[j] = s->v[n];
+      wl[j] = s->w_vel[n];
+      Tl[j] = s->temp[n];
+    } else if (t == -1000 || (t <= -100 && t >= -499)) {
+      ul[j] = bc->fs_u;
+      vl[j] = bc->fs_v;
+      wl[j] = bc->fs_w;
+      Tl[j] = bc->fs_temp;
+    } else {
+      ul[j] = 0.0;
+      vl[j] = 0.0;
+      wl[j] = 0.0;
+      Tl[j] = bc->fs_temp;
+    }
+  }
+#undef CODE39
+  shifted_ibb39(k, L, i, step, fieq, gieq, rho_t, ut, vt, wt, Tt, ul, vl, wl, Tl, sp, fv, gv);
+  return 0;
+}
+
 int o39_step_links(const o39_consts* k, o39_level* s, int step, o39_stats* st, const int32_t* state, int periodic,
                    const o39_bc* bc, double* fi_prev, double* gi_prev) {
   o39_lattice L;
@@ -528,6 +861,11 @@ int o39_step_links(const o39_consts* k, o39_level* s, int step, o39_stats* st, c
   if (!fo || !go) return -100;
   memcpy(fo, s->fout, sizeof(double) * Q * N);
   memcpy(go, s->gout, sizeof(double) * Q * N);
+  o39_targets tc;
+  tc.done = (unsigned char*)calloc((size_t)N, 1);
+  tc.tgt = (double*)malloc(sizeof(double) * 5 * N);
+  tc.tlm = (double*)malloc(sizeof(double) * NLM * N);
+  if (!tc.done || !tc.tgt || !tc.tlm) return -100;
   double* fi = fi_prev;
   double* gi = gi_prev;
   memset(st, 0, sizeof *st);
@@ -564,6 +902,22 @@ int o39_step_links(const o39_consts* k, o39_level* s, int step, o39_stats* st, c
             continue;
           }
           if (code == -666) continue;
+          if (code <= -1001 && code >= -1100000000) {
+            /* wall link (streaming.f95:478-1133): shifted lattice, primary flow along +x only */
+            if (!k->shifted || k->primary_flow_dir != 1) { rc = -3; break; }
+            if (t >= 0 && state[t] >= 0) {
+              fi[(int64_t)i * N + t] = fo[a];
+              gi[(int64_t)i * N + t] = go[a];
+            }
+            double fv, gv;
+            const int r2 = ibb_link39(k, &L, s, state, periodic, bc, step, n, x, y, z, i, fi, &tc, &fv, &gv);
+            if (r2) { rc = r2; break; }
+            fo[a] = fv;
+            go[a] = gv;
+            fi[a] = fo[a];
+            gi[a] = go[a];
+            continue;
+          }
           const int shifted_push = k->shifted && t >= 0;
           if (shifted_push) {
             fi[(int64_t)i * N + t] = fo[a];
@@ -623,6 +977,9 @@ int o39_step_links(const o39_consts* k, o39_level* s, int step, o39_stats* st, c
 #undef O39_TARGET
   free(fo);
   free(go);
+  free(tc.done);
+  free(tc.tgt);
+  free(tc.tlm);
   if (rc) return rc;
   int64_t lm_iters = 0, capped = 0, not2 = 0;
   collide39(k, &L, s, fi, gi, step, state, &lm_iters, &capped, &not2);
@@ -669,4 +1026,10 @@ void o39_tables(int shifted, int primary_flow_dir, int* cx, int* cy, int* cz, in
     cz[i] = L.cz[i];
     opp[i] = L.opp[i];
   }
+}
+
+/* Exposed for the test of the derivative table (derivatives.f95:816-1300). */
+int o39_ibb_wall_axis(int i, int axis, int* up) {
+  *up = 0;
+  return ibb_wall_axis(i, axis, up);
 }

@@ -147,11 +147,13 @@ class O39Bc(ct.Structure):
     _fields_ = [("inlet_type", ct.c_int * 8), ("outlet_type", ct.c_int * 8),
                 ("fs_fieq", ct.c_double * Q39), ("fs_gieq", ct.c_double * Q39),
                 ("inl_fieq", (ct.c_double * Q39) * 8), ("inl_gieq", (ct.c_double * Q39) * 8),
-                ("outl_fieq", (ct.c_double * Q39) * 8), ("outl_gieq", (ct.c_double * Q39) * 8)]
+                ("outl_fieq", (ct.c_double * Q39) * 8), ("outl_gieq", (ct.c_double * Q39) * 8),
+                ("fs_u", ct.c_double), ("fs_v", ct.c_double), ("fs_w", ct.c_double), ("fs_temp", ct.c_double)]
 
 
-def bc(inlet_type, outlet_type, fs_f, fs_g, inl_f, inl_g, outl_f, outl_g) -> O39Bc:
+def bc(inlet_type, outlet_type, fs_f, fs_g, inl_f, inl_g, outl_f, outl_g, fs_uvwT=(0.0, 0.0, 0.0, 0.0)) -> O39Bc:
     b = O39Bc()
+    b.fs_u, b.fs_v, b.fs_w, b.fs_temp = (float(x) for x in fs_uvwT)
     for k in range(8):
         b.inlet_type[k] = int(inlet_type[k])
         b.outlet_type[k] = int(outlet_type[k])
@@ -166,7 +168,8 @@ def bc(inlet_type, outlet_type, fs_f, fs_g, inl_f, inl_g, outl_f, outl_g) -> O39
 def step_links(k: O39Consts, lev: Level39, step: int, state: np.ndarray, periodic: int, b: O39Bc,
                fi_prev: np.ndarray, gi_prev: np.ndarray):
     """One step with the reference's link codes (state: (39, nz, ny, nx) int32); fi_prev and gi_prev
-    hold the post-streaming populations of the previous step and are updated in place."""
+    hold the post-streaming populations of the previous step and are updated in place.  Wall links
+    (codes -1001 - q*1e9) read the previous step's macroscopic fields lev.rho, u, v, w_vel, temp."""
     L = lib()
     if not getattr(L, "_o39_links_ready", False):
         L.o39_step_links.restype = ct.c_int
@@ -182,3 +185,15 @@ def step_links(k: O39Consts, lev: Level39, step: int, state: np.ndarray, periodi
     if rc != 0:
         raise RuntimeError(f"o39 link step failed {rc}")
     return {n: getattr(st, n) for n, _ in st._fields_}
+
+
+def ibb_wall_axis(i, axis):
+    """(wall form?, up-wind?) of the oracle's derivative rule for direction i (0-based), axis 0..2."""
+    L = lib()
+    if not getattr(L, "_o39_axis_ready", False):
+        L.o39_ibb_wall_axis.restype = ct.c_int
+        L.o39_ibb_wall_axis.argtypes = [ct.c_int, ct.c_int, ct.POINTER(ct.c_int)]
+        L._o39_axis_ready = True
+    up = ct.c_int(0)
+    wall = L.o39_ibb_wall_axis(i, axis, ct.byref(up))
+    return bool(wall), bool(up.value)

@@ -1,6 +1,8 @@
 """GPU parity of the D3Q39 compressible step (two populations, 13 multipliers,
 closed-form alpha, heat-flux corrections) against the CPU restatement of the
 reference routines.  Tolerance: 1e-12 relative in f, g and the multipliers."""
+import math
+
 import numpy as np
 import pytest
 
@@ -108,3 +110,121 @@ def test_d3q39_link_codes_parity(pkg, o39, built_lib, shifted, outlet_type):
         rel = np.max(np.abs(out[name][:, fluid] - ref[:, fluid]) / np.abs(ref[:, fluid]))
         assert rel <= 1e-12, (name, rel)
     ctx.close()
+
+
+def _wall_case(pkg, o39, seed, outlet_type, nx=16, ny=6, nz=8, mach=1.5):
+    """Shifted D3Q39 box (Mach 1.5 along +x): inlet at x-, outlet at x+, a
+    bounce-back floor, a freestream top, periodic in y, and a solid block on
+    the floor whose fluid neighbours carry interpolated wall links with random
+    wall distances; one wall node also has a null link (target_finder's
+    erp(i) = -666 branch).  Random rho, u, v, w, T per node."""
+    s39 = pkg.d3q39_setup
+    c = s39.wedge_case_consts(v_inf_ms=mach * math.sqrt(1.4 * s39.GAS_CONST_R * 288.15), use_shifted=True)
+    k = o39.consts(c)
+    lm0 = s39.freestream_start_lm(c)
+    eq = [o39.init_node(k, r, c.mach, 0.0, 0.0, c.temperature, lm0)[1:3] for r in (1.0, 1.02, 0.98)]
+    (ff, gf), (fi, gi), (fo, go) = eq
+    faces = {"x-": -101, "x+": -201, "z-": -10, "z+": -1000, "y-": 0, "y+": 0}
+    periodic = 2
+    st = s39.box_state39(nx, ny, nz, faces, 1, 1, periodic=periodic)
+    solid = np.zeros((nz, ny, nx), bool)
+    solid[0:3, 1:4, 6:9] = True
+    rng = np.random.default_rng(seed)
+    s39.wall_links39(st, solid, rng.uniform(0.05, 0.95, (39, nz, ny, nx)), 1, 1, periodic=periodic)
+    cx, cy, cz, _ = s39.lattice39(1, 1)
+    erp = np.array(s39.OPP39) - 1
+    for z, y, x, j in zip(*np.nonzero((st[0] >= 0)[None] & (st[1:15] <= -1001))[1:], np.nonzero(
+            (st[0] >= 0)[None] & (st[1:15] <= -1001))[0] + 1):
+        if 0 <= x + cx[j] < nx and 0 <= z + cz[j] < nz:  # target_finder reads node x + c_j
+            st[erp[j], z, y, x] = -666
+            break
+    lev = o39.Level39(nx, ny, nz)
+    for z in range(nz):
+        for y in range(ny):
+            for x in range(nx):
+                rho = 1.0 + 0.01 * rng.uniform(-1, 1)
+                u = c.mach * (1 + 0.01 * rng.uniform(-1, 1))
+                v, w = 0.01 * rng.uniform(-1, 1, 2)
+                T = c.temperature * (1 + 0.01 * rng.uniform(-1, 1))
+                lm, f, g, _ = o39.init_node(k, rho, u, v, w, T, lm0)
+                lev.fout[:, z, y, x], lev.gout[:, z, y, x], lev.lm[:, z, y, x] = f, g, lm
+                lev.rho[z, y, x], lev.u[z, y, x], lev.v[z, y, x], lev.w_vel[z, y, x] = rho, u, v, w
+                lev.temp[z, y, x] = T
+    inl_t, out_t = [1] * 8, [outlet_type] + [1] * 7
+    fs = (c.mach, 0.0, 0.0, c.temperature)
+    args = (inl_t, out_t, ff, gf, [fi] * 8, [gi] * 8, [fo] * 8, [go] * 8, fs)
+    return c, k, st, lev, periodic, o39.bc(*args), pkg.capi.make_d3q39_bc(*args)
+
+
+@pytest.mark.parametrize("seed,outlet_type,mach,warm,steps", [(3, 6, 1.5, 0, 5), (4, 1, 0.8, 0, 8),
+                                                             (5, 6, 0.8, 97, 6)])
+def test_d3q39_wall_links_parity(pkg, o39, built_lib, seed, outlet_type, mach, warm, steps):
+    """Interpolated wall links on the shifted lattice (target_finder, the target
+    Newton solve, shifted_ibb) next to the other boundary codes: the GPU step
+    against the oracle's push loop, 1e-12 relative.  Steps 0..4 (start-up
+    multipliers), 0..7 (warm starts from the node's multipliers), and 97..102
+    across the end of the start-up ramps: the oracle runs the first 97 steps
+    alone and both continue from its state (slots no rule writes then hold
+    the uploaded fout on both sides).  By then the flow past the block is
+    strongly non-uniform and the step itself amplifies rounding (the target
+    Newton stops at |delta| <= 1e-7, the closed-form alpha cancels where it is
+    small): the oracle fed its own state with 1-ulp noise moves by ~1e-12 per
+    step at the wall nodes.  That late run is held to 20 times the oracle's own
+    spread under such noise (and never looser than 1e-9)."""
+    cap = pkg.capi
+    c, k, st, lev, periodic, b, cb = _wall_case(pkg, o39, seed, outlet_type, mach=mach)
+    nz, ny, nx = lev.shape
+    prev_f, prev_g = lev.fout.copy(), lev.gout.copy()
+    for step in range(warm):
+        o39.step_links(k, lev, step, st, periodic, b, prev_f, prev_g)
+    prev_f, prev_g = lev.fout.copy(), lev.gout.copy()
+    fluid = st[0] >= 0
+    tol = 1e-12
+    if warm:
+        # the oracle's own sensitivity: the same steps from the state with 1-ulp noise
+        noisy = o39.Level39(nx, ny, nz)
+        rng = np.random.default_rng(seed)
+        for name in ("fout", "gout", "lm", "w_vel", "rho", "u", "v", "temp"):
+            a = getattr(lev, name)
+            getattr(noisy, name)[...] = a * (1 + 2.2e-16 * rng.uniform(-1, 1, a.shape))
+        nf, ng = noisy.fout.copy(), noisy.gout.copy()
+        clean = o39.Level39(nx, ny, nz)
+        for name in ("fout", "gout", "lm", "w_vel", "rho", "u", "v", "temp"):
+            getattr(clean, name)[...] = getattr(lev, name)
+        cf, cg = clean.fout.copy(), clean.gout.copy()
+        for step in range(warm, warm + steps):
+            o39.step_links(k, noisy, step, st, periodic, b, nf, ng)
+            o39.step_links(k, clean, step, st, periodic, b, cf, cg)
+        spread = np.max(np.abs(noisy.fout[:, fluid] - clean.fout[:, fluid]) / np.abs(clean.fout[:, fluid]))
+        tol = min(max(1e-12, 20 * spread), 1e-9)
+    ctx = cap.Context(0)
+    ctx.level_register(0, cap.ELBM_D3Q39, cap.ELBM_STORE_FP64, [[0, 0, 0, nx - 1, ny - 1, nz - 1]])
+    ctx.set_d3q39_params(0, cap.make_d3q39_params(c, timestep=warm, periodic=periodic, damp=0))
+    ctx.set_links39(0, 0, st, cb)
+    ctx.upload39(0, 0, lev.fout, lev.gout, lev.lm, lev.w_vel)
+    ctx.upload_macro39(0, 0, np.stack([lev.rho, lev.u, lev.v, lev.w_vel, lev.temp]))
+    s = ctx.step(0, steps)
+    out = ctx.download39(0)
+    for step in range(warm, warm + steps):
+        so = o39.step_links(k, lev, step, st, periodic, b, prev_f, prev_g)
+    assert np.isfinite(lev.fout[:, fluid]).all()
+    assert s["node_updates"] == steps * fluid.sum() and s["fallbacks"] == 0 and so["lm_capped"] == 0
+    for name, ref in (("fout", lev.fout), ("gout", lev.gout)):
+        rel = np.max(np.abs(out[name][:, fluid] - ref[:, fluid]) / np.abs(ref[:, fluid]))
+        assert rel <= tol, (name, rel, tol)
+    macro = out["macro"]
+    for m, ref in ((0, lev.rho), (4, lev.temp)):
+        assert np.max(np.abs(macro[m][fluid] - ref[fluid]) / np.abs(ref[fluid])) <= tol
+
+
+def test_d3q39_wall_links_need_macro(pkg, o39, built_lib):
+    cap = pkg.capi
+    c, k, st, lev, periodic, b, cb = _wall_case(pkg, o39, 3, 6)
+    nz, ny, nx = lev.shape
+    ctx = cap.Context(0)
+    ctx.level_register(0, cap.ELBM_D3Q39, cap.ELBM_STORE_FP64, [[0, 0, 0, nx - 1, ny - 1, nz - 1]])
+    ctx.set_d3q39_params(0, cap.make_d3q39_params(c, timestep=0, periodic=periodic, damp=0))
+    ctx.set_links39(0, 0, st, cb)
+    ctx.upload39(0, 0, lev.fout, lev.gout, lev.lm, lev.w_vel)
+    with pytest.raises(cap.ElbmError):
+        ctx.step(0, 1)

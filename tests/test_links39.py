@@ -97,3 +97,53 @@ def test_pull_tables_match_push_loop(pkg, built_lib, shifted, outlet_type):
         o39.step_links(k, lev, step, st, periodic, b, prev_f, prev_g)  # prev_* become this step's post-streaming
         assert np.array_equal(F[:, fluid], prev_f[:, fluid]), step
         assert np.array_equal(G[:, fluid], prev_g[:, fluid]), step
+
+
+def test_wall_link_slots_match_push_loop(pkg, built_lib):
+    """Interpolated wall links on the shifted lattice: every slot the tables
+    do not mark as a wall value matches the oracle's push loop bit for bit,
+    and the wall-value slots are exactly the fluid nodes' wall links."""
+    s39, cap = pkg.d3q39_setup, pkg.capi
+    c, k, lm0, (ff, gf, fi, gi, fo, go) = _case(pkg, 1)
+    nx, ny, nz, periodic = 14, 6, 7, 2
+    faces = {"x-": -101, "x+": -201, "z-": -10, "z+": -1000, "y-": 0, "y+": 0}
+    st = s39.box_state39(nx, ny, nz, faces, 1, 1, periodic=periodic)
+    solid = np.zeros((nz, ny, nx), bool)
+    solid[0:2, 1:4, 5:8] = True
+    rng = np.random.default_rng(9)
+    s39.wall_links39(st, solid, rng.uniform(0.05, 0.95, (39, nz, ny, nx)), 1, 1, periodic=periodic)
+    inl_t, out_t = [1] * 8, [6] + [1] * 7
+    fs = (c.mach, 0.0, 0.0, c.temperature)
+    b = o39.bc(inl_t, out_t, ff, gf, [fi] * 8, [gi] * 8, [fo] * 8, [go] * 8, fs)
+    eqf = [ff] + [fi] * 8 + [fo] * 8
+    eqg = [gf] + [gi] * 8 + [go] * 8
+    ntype, rec, words = cap.links39_tables(st, periodic, 1, 1, inl_t, out_t)
+    fluid = st[0] >= 0
+    wall_link = (st <= -1001) & fluid[None]
+    wall_link[0] = False
+    assert (ntype == 3).sum() == wall_link.any(axis=0).sum() > 0
+    wall_slot = np.zeros_like(wall_link)
+    for r, n in enumerate(rec):
+        zz, yy, xx = n // (nx * ny), (n // nx) % ny, n % nx
+        wall_slot[:, zz, yy, xx] = (words[r] & 3) == 3
+    assert np.array_equal(wall_slot, wall_link)
+    lev = o39.Level39(nx, ny, nz)
+    for zz in range(nz):
+        for yy in range(ny):
+            for xx in range(nx):
+                rho, u = 1 + 0.02 * rng.uniform(-1, 1), c.mach * (1 + 0.02 * rng.uniform(-1, 1))
+                v = 0.01 * rng.uniform(-1, 1)
+                lm, f, g, _ = o39.init_node(k, rho, u, v, 0.0, c.temperature, lm0)
+                lev.fout[:, zz, yy, xx], lev.gout[:, zz, yy, xx], lev.lm[:, zz, yy, xx] = f, g, lm
+                lev.rho[zz, yy, xx], lev.u[zz, yy, xx], lev.v[zz, yy, xx] = rho, u, v
+                lev.temp[zz, yy, xx] = c.temperature
+    prev_f, prev_g = lev.fout.copy(), lev.gout.copy()
+    cx, cy, cz, _ = s39.lattice39(1, 1)
+    check = fluid[None] & ~wall_slot
+    for step in range(3):
+        fout0, gout0 = lev.fout.copy(), lev.gout.copy()
+        F, G = pull39(None, fout0, gout0, ntype, rec, words, prev_f, prev_g, eqf, eqg, cx, cy, cz, periodic)
+        o39.step_links(k, lev, step, st, periodic, b, prev_f, prev_g)
+        assert np.isfinite(prev_f[:, fluid]).all()
+        assert np.array_equal(F[check], prev_f[check]), step
+        assert np.array_equal(G[check], prev_g[check]), step

@@ -104,3 +104,22 @@ def test_periodic_box_conserves_mass_and_momentum(o39, setup39):
     assert abs(lev.fout.sum() - m0) / m0 < 1e-6
     assert abs(np.tensordot(cx.astype(float), lev.fout, axes=(0, 0)).sum() - j0) / abs(j0) < 1e-6
     assert np.isfinite(lev.alpha).all()
+
+
+def test_wall_derivative_rule_matches_reference_table(o39):
+    """The oracle's rule for the seven-point wall derivatives (which axes take
+    the one-sided wall form and with which up-wind flag) against the
+    reference's 117-case table of first_order_shifted_vel_cond_unknown and
+    first_order_shifted_temp_cond_unknown (tests/golden/ibb_deriv_table.json,
+    written by tests/golden/make_ibb_deriv_table.py)."""
+    import json
+    import pathlib
+
+    data = json.loads((pathlib.Path(__file__).parent / "golden" / "ibb_deriv_table.json").read_text())
+    for kind in ("velocity", "temperature"):
+        assert len(data[kind]) == 117
+        for e in data[kind]:
+            wall, up = o39.ibb_wall_axis(e["dir"] - 1, e["card"] - 1)
+            assert wall == (e["form"] == "wall"), (kind, e)
+            if wall:
+                assert up == e["up"], (kind, e)

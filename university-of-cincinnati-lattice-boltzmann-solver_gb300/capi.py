@@ -60,7 +60,8 @@ class D3Q39Params(ct.Structure):
                                          "max_lm_iters", "periodic", "timestep", "damp", "pad")] + [
         (n, ct.c_double) for n in ("gama", "t_ref", "rho_ref", "p_ref", "mu_ref", "kappa_ref", "gas_const_R",
                                    "const_vol", "const_press", "molec_weight", "dt", "elbm_epsilon", "init_beta_1",
-                                   "init_beta_2", "beta_1_scaling", "beta_2_scaling")]
+                                   "init_beta_2", "beta_1_scaling", "beta_2_scaling")] + [
+        ("su_lm", ct.c_double * 13)]
 
 
 def make_d3q39_params(consts, timestep=0, periodic=7, damp=1) -> D3Q39Params:
@@ -75,6 +76,9 @@ def make_d3q39_params(consts, timestep=0, periodic=7, damp=1) -> D3Q39Params:
             p.damp = damp
         elif name == "pad":
             p.pad = 0
+        elif name == "su_lm":
+            for r, v in enumerate(consts.su_lm):
+                p.su_lm[r] = v
         else:
             setattr(p, name, getattr(consts, name))
     return p
@@ -84,12 +88,16 @@ class D3Q39Bc(ct.Structure):
     _fields_ = [("inlet_type", ct.c_int32 * 8), ("outlet_type", ct.c_int32 * 8),
                 ("fs_fieq", ct.c_double * 39), ("fs_gieq", ct.c_double * 39),
                 ("inl_fieq", (ct.c_double * 39) * 8), ("inl_gieq", (ct.c_double * 39) * 8),
-                ("outl_fieq", (ct.c_double * 39) * 8), ("outl_gieq", (ct.c_double * 39) * 8)]
+                ("outl_fieq", (ct.c_double * 39) * 8), ("outl_gieq", (ct.c_double * 39) * 8),
+                ("fs_u", ct.c_double), ("fs_v", ct.c_double), ("fs_w", ct.c_double), ("fs_temp", ct.c_double)]
 
 
-def make_d3q39_bc(inlet_type, outlet_type, fs_f, fs_g, inl_f, inl_g, outl_f, outl_g) -> D3Q39Bc:
-    """Boundary equilibria (f and g) and inlet/outlet types of a D3Q39 level with link codes."""
+def make_d3q39_bc(inlet_type, outlet_type, fs_f, fs_g, inl_f, inl_g, outl_f, outl_g,
+                  fs_uvwT=(0.0, 0.0, 0.0, 0.0)) -> D3Q39Bc:
+    """Boundary equilibria (f and g), inlet/outlet types and the freestream velocity and
+    temperature of a D3Q39 level with link codes."""
     b = D3Q39Bc()
+    b.fs_u, b.fs_v, b.fs_w, b.fs_temp = (float(x) for x in fs_uvwT)
     for k in range(8):
         b.inlet_type[k] = int(inlet_type[k])
         b.outlet_type[k] = int(outlet_type[k])
@@ -134,6 +142,7 @@ SIGNATURES = {
     "elbm_set_d3q39_params": (_c_int, [_vp, _c_int, ct.POINTER(D3Q39Params)]),
     "elbm_upload_level39": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _vp]),
     "elbm_download_level39": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "elbm_upload_macro39": (_c_int, [_vp, _c_int, _c_int, _vp]),
     "elbm_upload_level_noalloc": (_c_int, [_vp, _c_int, _c_int, _vp]),
     "elbm_autotune": (_c_int, [_vp, _c_int, _c_int, _vp, _vp]),
     "elbm_set_kernel_variant": (_c_int, [_vp, _c_int, _c_int]),
@@ -331,6 +340,11 @@ class Context:
     def upload39(self, lvl, box, fout, gout, lm, w_vel):
         arrs = [np.ascontiguousarray(a, np.float64) for a in (fout, gout, lm, w_vel)]
         self._check(self.lib.elbm_upload_level39(self.h, lvl, box, *map(_ptr, arrs)))
+
+    def upload_macro39(self, lvl, box, macro):
+        """rho, u, v, w, T (5, nz, ny, nx) the next step starts from (after upload39)."""
+        m = np.ascontiguousarray(macro, np.float64)
+        self._check(self.lib.elbm_upload_macro39(self.h, lvl, box, _ptr(m)))
 
     def download39(self, lvl, box=0):
         """Returns dict with fout, gout, lm, w_vel, alpha, macro (FAB layouts)."""

@@ -248,6 +248,10 @@ __global__ void __launch_bounds__(64) d3q39_fp64_kernel(const Step39Args a) {
         const int table = (int)((w >> 8) & 31u);
         f[j] = a.eqf[table * Q + pop];
         g[j] = a.eqg[table * Q + pop];
+      } else if (kind == L39_WALL) {
+        const int64_t r = a.recwall[b];
+        f[j] = a.wallf[r * Q + pop];
+        g[j] = a.wallg[r * Q + pop];
       } else {
         f[j] = a.fprev[b * Q + j];
         g[j] = a.gprev[b * Q + j];
@@ -260,6 +264,9 @@ __global__ void __launch_bounds__(64) d3q39_fp64_kernel(const Step39Args a) {
   }
   double lm[NL];
   for (int r = 0; r < NL; ++r) lm[r] = a.lm[(int64_t)r * a.plane + n];
+  // calculate_flow_variables.f95:236-271: next to a wall the first steps solve from the start-up set
+  if (t == 3 && k.shifted && a.step <= 1)
+    for (int r = 0; r < NL; ++r) lm[r] = k.su_lm[r];
   // calculate_flow_variables.f95:201-228
   double rs = 0, us = 0, vs = 0, ws = 0, es = 0;
   for (int i = 0; i < Q; ++i) {
@@ -373,6 +380,289 @@ __global__ void __launch_bounds__(64) d3q39_fp64_kernel(const Step39Args a) {
   }
 }
 
+// ---- interpolated wall links on the shifted lattice ----
+
+// derivatives.f95:816-1300: 1 when the derivative along axis (0 x, 1 y, 2 z)
+// of direction i is the one-sided wall form (up: q_target - q_wall, else
+// q_wall - q_target), 0 for the local difference.  Wall form on the axes where
+// the unshifted velocity has a component, up when it is negative; the rest
+// direction along x; directions 28, 30, 31 and 33 (1-based) carry the opposite
+// up flags.
+__device__ __forceinline__ bool wall_axis39(int i, int axis, bool& up) {
+  const int c = axis == 0 ? c39.ucx[i] : axis == 1 ? c39.ucy[i] : c39.ucz[i];
+  if (i == 0) {
+    up = false;
+    return axis == 0;
+  }
+  if (c == 0) return false;
+  up = c < 0;
+  if (i == 27 || i == 29 || i == 30 || i == 32) up = !up;
+  return true;
+}
+
+// first_order_shifted_{vel,temp}_cond_unknown with dudx_ibb / dudx_local
+__device__ double deriv39(double q_rest, double q_target, double q_up, double q_down, int i, int axis, int s_up,
+                          int s_down, bool temperature) {
+  bool up = false;
+  if (wall_axis39(i, axis, up)) {
+    const double dir_state = (fabs((double)s_down + 1001.0) / 1.0e9) * sqrt(c39.cmag[i]);
+    const double q_wall = temperature ? q_target : 0.0;
+    return up ? (q_target - q_wall) / (1.0 + dir_state) : (q_wall - q_target) / (1.0 + dir_state);
+  }
+  if (s_up >= 0 && s_down >= 0) return (q_down - q_up) / 2.0;
+  if (s_up >= 0) return q_rest - q_up;
+  if (s_down >= 0) return q_down - q_rest;
+  return 0.0;
+}
+
+// shifted_ibb.f95:45-267 for wall link i: f and g of the missing population.
+__device__ void shifted_ibb39(const D3Q39Dev& k, int i, int step, double fieq, double gieq, double rho, double ut,
+                              double vt, double wt, double Tt, const double (&ul)[7], const double (&vl)[7],
+                              const double (&wl)[7], const double (&Tl)[7], const int (&sp)[7], double& fout,
+                              double& gout) {
+  const double cv = k.const_vol;
+  const double k_fi = -(rho * Tt) / 2.0;
+  const double k_gi = -(rho * Tt * (2.0 * cv - 3)) / 2.0;
+  const double eps = eps39(k, step);
+  double mu, dm, dt_;
+  sutherland39(k, Tt, mu, dm, dt_);
+  double kappa = 0.0;
+  therm_cond39(k, rho, Tt, kappa);
+  double b1, b2;
+  if (step < k.startup_timesteps) {
+    b1 = k.init_beta_1 + k.beta_1_scaling * step;
+    b2 = k.init_beta_2 + k.beta_2_scaling * step;
+  } else {
+    b1 = 1.0 / ((pow(2.0, (double)(k.lvl + 1)) * mu) / (rho * Tt) + 1.0);
+    b2 = 1.0 / ((2.0 * kappa) / (rho * k.const_press * Tt) + 1.0);
+  }
+  double du[3], dv[3], dw[3], dT[3];
+  for (int ax = 0; ax < 3; ++ax) {
+    du[ax] = deriv39(ul[0], ut, ul[4 + ax], ul[1 + ax], i, ax, sp[4 + ax], sp[1 + ax], false);
+    dv[ax] = deriv39(vl[0], vt, vl[4 + ax], vl[1 + ax], i, ax, sp[4 + ax], sp[1 + ax], false);
+    dw[ax] = deriv39(wl[0], wt, wl[4 + ax], wl[1 + ax], i, ax, sp[4 + ax], sp[1 + ax], false);
+    dT[ax] = deriv39(Tl[0], Tt, Tl[4 + ax], Tl[1 + ax], i, ax, sp[4 + ax], sp[1 + ax], true);
+  }
+  const double dudx = du[0], dudy = du[1], dudz = du[2], dvdx = dv[0], dvdy = dv[1], dvdz = dv[2];
+  const double dwdx = dw[0], dwdy = dw[1], dwdz = dw[2], dTdx = dT[0], dTdy = dT[1], dTdz = dT[2];
+  // 27 ordered pairs of the pressure-tensor gradient, then / beta_1
+  const double sxy = dudy + dvdx, sxz = dudz + dwdx, syz = dvdz + dwdy;
+  double p[27];
+  p[0] = 2 * dudx - dudx / cv;
+  p[1] = 2 * dudx - dvdy / cv;
+  p[2] = 2 * dudx - dwdz / cv;
+  p[3] = p[4] = p[5] = p[9] = p[10] = p[11] = sxy;
+  p[6] = p[7] = p[8] = p[18] = p[19] = p[20] = sxz;
+  p[12] = 2 * dvdy - dudx / cv;
+  p[13] = 2 * dvdy - dvdy / cv;
+  p[14] = 2 * dvdy - dwdz / cv;
+  p[15] = p[16] = p[17] = p[21] = p[22] = p[23] = syz;
+  p[24] = 2 * dwdz - dudx / cv;
+  p[25] = 2 * dwdz - dvdy / cv;
+  p[26] = 2 * dwdz - dwdz / cv;
+  for (int m = 0; m < 27; ++m) p[m] = p[m] / b1;
+  // third-moment gradients: ten distinct sums over the 27 slots
+  const double qxxx = 3 * (dTdx / b2 + ut * p[0]);
+  const double qxxy = (dTdy / b2 + vt * p[1] + 2 * ut * p[3]);
+  const double qxxz = (dTdz / b2 + wt * p[2] + 2 * ut * p[6]);
+  const double qxyx = (dTdy / b2 + 2 * ut * p[3] + vt * p[0]);
+  const double qxyy = (dTdx / b2 + ut * p[12] + 2 * vt * p[3]);
+  const double qxyz = (ut * p[21] + vt * p[6] + wt * p[3]);
+  const double qxzz = (dTdx / b2 + ut * p[24] + 2 * wt * p[6]);
+  const double qyxy = (dTdx / b2 + 2 * vt * p[3] + ut * p[12]);
+  const double qyyy = 3 * (dTdy / b2 + vt * p[13]);
+  const double qyyz = (dTdz / b2 + wt * p[14] + 2 * vt * p[21]);
+  const double qyzz = (dTdy / b2 + vt * p[25] + 2 * wt * p[21]);
+  const double qzxx = (dTdx / b2 + wt * p[2] + 2 * ut * p[6]);
+  const double qzzz = 3 * (dTdz / b2 + wt * p[26]);
+  const double q[27] = {qxxx, qxxy, qxxz, qxyx, qxyy, qxyz, qxxz, qxyz, qxzz, qxxy, qyxy, qxyz, qxyy, qyyy,
+                        qyyz, qxyz, qyyz, qyzz, qzxx, qxyz, qxzz, qxyz, qyyz, qyzz, qxzz, qyzz, qzzz};
+  const int cx = c39.cx[i], cy = c39.cy[i], cz = c39.cz[i];
+  const double xx = cx * cx - Tt, yy = cy * cy - Tt, zz = cz * cz - Tt;
+  // the reference's term order, its 25th pressure term counted twice
+  const double p_comp =
+      (p[0] * xx + p[1] * xx + p[2] * xx + p[3] * cx * cy + p[4] * cx * cy + p[5] * cx * cy + p[6] * cx * cz +
+       p[7] * cx * cz + p[8] * cx * cz + p[9] * cy * cx + p[10] * cy * cx + p[11] * cy * cx + p[12] * yy +
+       p[13] * yy + p[14] * yy + p[15] * cy * cz + p[16] * cy * cz + p[17] * cy * cz + p[18] * cz * cx +
+       p[19] * cz * cx + p[20] * cz * cx + p[21] * cz * cy + p[22] * cz * cy + p[23] * cz * cy + p[24] * zz +
+       p[24] * zz + p[25] * zz + p[26] * zz) /
+      (2 * (Tt * Tt));
+  const int cx2 = cx * cx, cy2 = cy * cy, cz2 = cz * cz;
+  const double q_comp =
+      (q[0] * (cx2 * cx - 3 * cx * Tt) + q[1] * (cx2 * cy - 3 * cy * Tt) + q[2] * (cx2 * cz - 3 * cz * Tt) +
+       q[3] * cx2 * cy + q[4] * cx * cy2 + q[5] * cx * cy * cz + q[6] * cx2 * cz + q[7] * cx * cy * cz +
+       q[8] * cx * cz2 + q[9] * cx2 * cy + q[10] * cy2 * cx + q[11] * cx * cy * cz +
+       q[12] * (cy2 * cx - 3 * cx * Tt) + q[13] * (cy2 * cy - 3 * cy * Tt) + q[14] * (cy2 * cz - 3 * cz * Tt) +
+       q[15] * cx * cy * cz + q[16] * cy2 * cz + q[17] * cz2 * cy + q[18] * cx2 * cz + q[19] * cx * cy * cz +
+       q[20] * cz2 * cx + q[21] * cx * cy * cz + q[22] * cz * cy2 + q[23] * cz2 * cy +
+       q[24] * (cz2 * cx - 3 * cx * Tt) + q[25] * (cz2 * cy - 3 * cy * Tt) + q[26] * (cz2 * cz - 3 * cz * Tt)) /
+      (6 * (Tt * Tt * Tt));
+  double fo = fieq + eps * k_fi * (p_comp + q_comp);
+  const double k_one = 3 * (dTdx + dTdy + dTdz) / (b1 * cv);
+  const double g_alpha = cx / Tt * (9 * dTdx / b2 + ut * k_one) + cy / Tt * (9 * dTdy / b2 + vt * k_one) +
+                         cz / Tt * (9 * dTdz / b2 + wt * k_one);
+  // heat-flux gradients of g (rab of shifted_ibb.f95), summed against c_a c_b - T delta_ab
+  const double rxx0 = 2 * Tt * dudx + 2 * ut * dTdx - dudx / cv * (2 * Tt + ut * ut);
+  const double rxx1 = 2 * Tt * dudx + 2 * ut * dTdx - dvdy / cv * (2 * Tt + ut * ut);
+  const double rxx2 = 2 * Tt * dudx + 2 * ut * dTdx - dwdz / cv * (2 * Tt + ut * ut);
+  const double rxy0 = Tt * (dudy + dvdx) + ut * dTdy + vt * dTdx - dudx / cv * ut * vt;
+  const double rxy1 = Tt * (dudy + dvdx) + ut * dTdy + vt * dTdx - dvdy / cv * ut * vt;
+  const double rxy2 = Tt * (dudy + dvdx) + ut * dTdy + vt * dTdx - dwdz / cv * ut * vt;
+  const double rxz0 = Tt * (dudz + dwdx) + ut * dTdz + wt * dTdx - dudx / cv * ut * wt;
+  const double rxz1 = Tt * (dudz + dwdx) + ut * dTdz + wt * dTdx - dvdy / cv * ut * wt;
+  const double rxz2 = Tt * (dudz + dwdx) + ut * dTdz + wt * dTdx - dwdz / cv * ut * wt;
+  const double ryy0 = 2 * Tt * dvdy + 2 * vt * dTdy - dudx / cv * (2 * Tt + vt * vt);
+  const double ryy1 = 2 * Tt * dvdy + 2 * vt * dTdy - dvdy / cv * (2 * Tt + vt * vt);
+  const double ryy2 = 2 * Tt * dvdy + 2 * vt * dTdy - dwdz / cv * (2 * Tt + vt * vt);
+  const double ryz0 = Tt * (dvdz + dwdy) + wt * dTdy + vt * dTdz - dudx / cv * vt * wt;
+  const double ryz1 = Tt * (dvdz + dwdy) + wt * dTdy + vt * dTdz - dvdy / cv * vt * wt;
+  const double ryz2 = Tt * (dvdz + dwdy) + wt * dTdy + vt * dTdz - dwdz / cv * vt * wt;
+  const double rzz0 = 2 * Tt * dwdz + 2 * wt * dTdz - dudx / cv * (2 * Tt + wt * wt);
+  const double rzz1 = 2 * Tt * dwdz + 2 * wt * dTdz - dvdy / cv * (2 * Tt + wt * wt);
+  const double rzz2 = 2 * Tt * dwdz + 2 * wt * dTdz - dwdz / cv * (2 * Tt + wt * wt);
+  // rab(22..24) repeat rab(13..15) in the reference
+  const double r_sum = rxx0 * xx + rxx1 * xx + rxx2 * xx + rxy0 * cx * cy + rxy1 * cx * cy + rxy2 * cx * cy +
+                       rxz0 * cx * cz + rxz1 * cx * cz + rxz2 * cx * cz + rxy0 * cy * cx + rxy1 * cy * cx +
+                       rxy2 * cy * cx + ryy0 * yy + ryy1 * yy + ryy2 * yy + ryz0 * cy * cz + ryz1 * cy * cz +
+                       ryz2 * cy * cz + rxz0 * cz * cx + rxz1 * cz * cx + rxz2 * cz * cx + ryy0 * cz * cy +
+                       ryy1 * cz * cy + ryy2 * cz * cy + rzz0 * zz + rzz1 * zz + rzz2 * zz;
+  const double gi_neq = k_gi * (3 * k_one + g_alpha + r_sum / (2 * b1 * Tt));
+  double go = gieq + eps * gi_neq;
+  if (fo < 0.0) fo = fabs(fo);
+  if (go < 0.0) go = fabs(go);
+  fout = fo;
+  gout = go;
+}
+
+// Value of a post-streaming slot described by a link word (PULL / EQ / STALE).
+__device__ __forceinline__ void slot39(const Step39Args& a, uint32_t w, int64_t b, int j, int x, int y, int z,
+                                       double& f, double& g) {
+  const uint32_t kind = w & 3u;
+  const int pop = (int)((w >> 2) & 63u);
+  if (kind == L39_PULL) {
+    const int off = (int)(w >> 13);
+    int sx = x + off % 9 - 4, sy = y + (off / 9) % 9 - 4, sz = z + off / 81 - 4;
+    sx = (sx % a.nx + a.nx) % a.nx;
+    sy = (sy % a.ny + a.ny) % a.ny;
+    sz = (sz % a.nz + a.nz) % a.nz;
+    const int64_t s = ((int64_t)sz * a.ny + sy) * a.nx + sx;
+    f = a.fsrc[(int64_t)pop * a.plane + s];
+    g = a.gsrc[(int64_t)pop * a.plane + s];
+  } else if (kind == L39_EQ) {
+    const int table = (int)((w >> 8) & 31u);
+    f = a.eqf[table * Q + pop];
+    g = a.eqg[table * Q + pop];
+  } else {
+    f = a.fprev[b * Q + j];
+    g = a.gprev[b * Q + j];
+  }
+}
+
+// One thread per node with wall links: targets (target_finder.f95:89-140 and the
+// Newton solve of streaming.f95:788-850, or the node's own previous fields when
+// no wall link is among directions 1..14), the seven-point stencil
+// (streaming.f95:577-603, 1055-1082) and shifted_ibb for every wall link.
+// Reads the previous step's macroscopic planes, multipliers and post-collision
+// populations before the step kernel overwrites them (same stream).
+__global__ void __launch_bounds__(64) d3q39_wall_kernel(const Step39Args a) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= a.nwall) return;
+  const D3Q39Dev& k = a.k;
+  const Wall39Rec& R = a.walls[r];
+  const int64_t n = R.node, b = R.rec;
+  const int x = (int)(n % a.nx), y = (int)((n / a.nx) % a.ny), z = (int)(n / ((int64_t)a.nx * a.ny));
+  const double* mrho = a.macro;
+  const double* mu = a.macro + a.plane;
+  const double* mv = a.macro + 2 * a.plane;
+  const double* mT = a.macro + 4 * a.plane;
+  const double* mw = a.w_vel;
+  double rho_t, ut, vt, wt, Tt, lm[NL];
+  unsigned flags = 0;
+  int it = 0;
+  if (R.adjacent) {
+    int count = 0;
+    double r_ = 0, u_ = 0, v_ = 0, w_ = 0, T_ = 0;
+    for (int j = 0; j < Q; ++j) {
+      const int32_t c = R.code[j];
+      if (c <= -1001) {
+        const double d = fabs(((double)c + 1001.0) / 1.0e9);
+        count++;
+        const int64_t m = R.upass[R.code[c39.erp[j]] == -666 ? j : 4];
+        u_ = u_ + (d * mu[m]) / (d + 1.0);
+        v_ = v_ + (d * mv[m]) / (d + 1.0);
+        w_ = w_ + (d * mw[m]) / (d + 1.0);
+        T_ = T_ + (d * mT[m] + mT[m]) / (d + 1.0);
+      }
+      const int s = R.code[c39.opp[j]] < -1000 ? c39.erp[j] : j;
+      double fs, gs;
+      slot39(a, R.snap[s], b, s, x, y, z, fs, gs);
+      r_ = r_ + fs;
+    }
+    rho_t = r_;
+    ut = u_ / count;
+    vt = v_ / count;
+    wt = w_ / count;
+    Tt = T_ / count;
+    for (int q = 0; q < NL; ++q) lm[q] = a.step <= 4 ? k.su_lm[q] : a.lm[(int64_t)q * a.plane + n];
+    const double P[6] = {rho_t * Tt + rho_t * (ut * ut), rho_t * Tt + rho_t * (vt * vt),
+                         rho_t * Tt + rho_t * (wt * wt), rho_t * ut * vt, rho_t * ut * wt, rho_t * vt * wt};
+    double fe[Q];
+    it = lagrange39(k.max_lm_iters, rho_t, ut, vt, wt, Tt, P, lm, fe);
+    if (it < 0) {
+      flags |= 0x2u;
+      it = -it;
+    }
+  } else {
+    rho_t = mrho[n];
+    ut = mu[n];
+    vt = mv[n];
+    wt = mw[n];
+    Tt = mT[n];
+    for (int q = 0; q < NL; ++q) lm[q] = a.lm[(int64_t)q * a.plane + n];
+  }
+  double ul[7], vl[7], wl[7], Tl[7];
+  int sp[7];
+  for (int j = 0; j < 7; ++j) {
+    const int t = R.st[j];
+    const int64_t m = R.sidx[j];
+    sp[j] = t;
+    if (t >= 0) {
+      ul[j] = mu[m];
+      vl[j] = mv[m];
+      wl[j] = mw[m];
+      Tl[j] = mT[R.adjacent ? m : (int64_t)R.tidx[j]];
+    } else if (t == -11) {
+      ul[j] = mu[n];
+      vl[j] = mv[n];
+      wl[j] = mw[n];
+      Tl[j] = mT[n];
+    } else if (t == -1000 || (t <= -100 && t >= -499)) {
+      ul[j] = k.fs_u;
+      vl[j] = k.fs_v;
+      wl[j] = k.fs_w;
+      Tl[j] = k.fs_temp;
+    } else {
+      ul[j] = 0.0;
+      vl[j] = 0.0;
+      wl[j] = 0.0;
+      Tl[j] = k.fs_temp;
+    }
+  }
+  for (int i = 1; i < Q; ++i) {
+    if (R.code[i] > -1001) continue;
+    const double fieq = fieq39(rho_t, lm, i);
+    const double gieq = (2.0 * k.const_vol - 3) * Tt * fieq;
+    double fo, go;
+    shifted_ibb39(k, i, a.step, fieq, gieq, rho_t, ut, vt, wt, Tt, ul, vl, wl, Tl, sp, fo, go);
+    a.wallf[r * Q + i] = fo;
+    a.wallg[r * Q + i] = go;
+  }
+  if (!isfinite(rho_t) || !isfinite(Tt)) flags |= 0x1u;
+  if (it) atomicAdd(&a.stats->newton_iters, (unsigned long long)it);
+  if (flags & 0x2u) atomicAdd(&a.stats->fallbacks, 1ull);
+  if (flags) atomicOr(&a.stats->status, flags);
+}
+
 // damp_it.f95:64-177 for fout on a periodic box: a negative population takes
 // the mean of its +-c_i neighbours when both are positive, else the mean of
 // the positive one and its own magnitude, else its magnitude.  Neighbours are
@@ -411,6 +701,12 @@ void launch_d3q39_fp64(const Step39Args& a, cudaStream_t s) {
   d3q39_fp64_kernel<<<(unsigned)blocks, threads, 0, s>>>(a);
 }
 
+void launch_d3q39_walls(const Step39Args& a, cudaStream_t s) {
+  if (a.nwall <= 0) return;
+  const int threads = 64;
+  d3q39_wall_kernel<<<(unsigned)((a.nwall + threads - 1) / threads), threads, 0, s>>>(a);
+}
+
 void launch_d3q39_damp(const double* src, double* dst, int nx, int ny, int nz, int64_t plane, DevStats* stats,
                        cudaStream_t s) {
   const int64_t N = (int64_t)nx * ny * nz;
@@ -446,6 +742,10 @@ void build_lattice39(int shifted, int primary_flow_dir, Lattice39& L) {
     L.cy[i] = y;
     L.cz[i] = z;
     L.opp[i] = shifted ? i : OPP0[i] - 1;
+    L.ucx[i] = CX0[i];
+    L.ucy[i] = CY0[i];
+    L.ucz[i] = CZ0[i];
+    L.erp[i] = OPP0[i] - 1;
     L.cmag[i] = (double)x * x + (double)y * y + (double)z * z;
     const int c2 = x * x + y * y + z * z;
     const int mono[13] = {1, x, y, z, x * x, y * y, z * z, x * y, x * z, y * z, x * c2, y * c2, z * c2};

@@ -11,6 +11,7 @@ namespace elbm {
 // after the optional Galilean shift; filled on the host, read from constant memory.
 struct Lattice39 {
   int cx[39], cy[39], cz[39], opp[39];
+  int ucx[39], ucy[39], ucz[39], erp[39];  // the unshifted set and its opposites
   double cmag[39];
   int phi[13][39];  // 1, cx, cy, cz, cx2, cy2, cz2, cxcy, cxcz, cycz, cx c2, cy c2, cz c2
   int yi[27][39];
@@ -22,6 +23,23 @@ struct D3Q39Dev {
   int shifted, primary_flow_dir, turbulent, lvl, startup_timesteps, max_lm_iters;
   double gama, t_ref, rho_ref, p_ref, mu_ref, kappa_ref, gas_const_R, const_vol, const_press, molec_weight;
   double dt, elbm_epsilon, init_beta_1, init_beta_2, beta_1_scaling, beta_2_scaling;
+  double su_lm[13];                    // start-up multipliers (su_chi .. su_lambda_z)
+  double fs_u, fs_v, fs_w, fs_temp;    // freestream velocity and temperature
+};
+
+// A fluid node with interpolated wall links (codes -1001 - q 1e9) on the
+// shifted lattice: what target_finder and shifted_ibb read for it.
+struct Wall39Rec {
+  int32_t node;       // box node
+  int32_t rec;        // its boundary record
+  int32_t adjacent;   // a wall link among directions 1..14: targets from target_finder plus a Newton solve
+  int32_t pad;
+  int32_t code[39];   // the node's state components (0: node type)
+  uint32_t snap[39];  // adjacent nodes: the post-streaming slot as target_finder finds it (link word)
+  int32_t upass[39];  // node whose previous macroscopic values target_finder takes for direction j (-1: none)
+  int32_t st[7];      // node types of the stencil rest, +x, +y, +z, -x, -y, -z (-666 outside the box)
+  int32_t sidx[7];    // stencil nodes (-1 outside the box)
+  int32_t tidx[7];    // non-adjacent nodes: temperature source of each fluid stencil node (one lattice shift on)
 };
 
 struct Step39Args {
@@ -48,10 +66,16 @@ struct Step39Args {
   const double* eqg;          // same for g
   double* fprev;              // 39 per record: post-streaming f of the previous step
   double* gprev;
+  // interpolated wall links (nwall records; the step's macro planes hold the previous step's fields)
+  const Wall39Rec* walls;
+  int64_t nwall;
+  const int32_t* recwall;     // per boundary record: its wall record or -1
+  double* wallf;              // 39 per wall record: the wall values of f, then g, of this step
+  double* wallg;
 };
 
 // Link words of D3Q39 boundary records.
-enum Link39Kind : uint32_t { L39_STALE = 0, L39_PULL = 1, L39_EQ = 2 };
+enum Link39Kind : uint32_t { L39_STALE = 0, L39_PULL = 1, L39_EQ = 2, L39_WALL = 3 };
 __host__ __device__ constexpr uint32_t link39(uint32_t kind, int pop, int table, int dx, int dy, int dz) {
   return kind | ((uint32_t)pop << 2) | ((uint32_t)table << 8) |
          ((uint32_t)((dx + 4) + 9 * (dy + 4) + 81 * (dz + 4)) << 13);
@@ -60,6 +84,7 @@ __host__ __device__ constexpr uint32_t link39(uint32_t kind, int pop, int table,
 void build_lattice39(int shifted, int primary_flow_dir, Lattice39& L);
 void upload_lattice39(const Lattice39& L, cudaStream_t s);
 void launch_d3q39_fp64(const Step39Args& a, cudaStream_t s);
+void launch_d3q39_walls(const Step39Args& a, cudaStream_t s);
 void launch_d3q39_damp(const double* src, double* dst, int nx, int ny, int nz, int64_t plane, DevStats* stats,
                        cudaStream_t s);
 

@@ -12,6 +12,13 @@
 // p", every write carries its loop position, and the last write of each slot
 // wins.  A node whose 39 slots all end up as the plain pull fout(y - c_j, j)
 // is a bulk node; the others get 39 link words.
+//
+// Interpolated wall links (codes -1001 - q 1e9, shifted lattice,
+// streaming.f95:478-1133) write a value that the step computes from the
+// node's targets (target_finder.f95, shifted_ibb.f95).  target_finder sums
+// the node's post-streaming slots as the loop has left them at the node's
+// first wall link, so the decoder also records, for such nodes, the last
+// write of every slot up to that point.
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -24,7 +31,7 @@ namespace elbm {
 namespace {
 
 struct Sym {
-  int8_t kind = 0;  // 0 none, 1 fout(node, pop), 2 equilibrium(table, pop)
+  int8_t kind = 0;  // 0 none, 1 fout(node, pop), 2 equilibrium(table, pop), 3 wall value(pop)
   int8_t pop = 0;
   int8_t table = 0;
   int64_t node = -1;
@@ -61,6 +68,11 @@ int decode_links39(const int32_t* st, int ngs, int nx, int ny, int nz, int perio
     else if (tz < 0 || tz >= nz) return -1;
     return ((int64_t)tz * ny + ty) * nx + tx;
   };
+  auto is_wall = [](int32_t c) { return c <= -1001 && c >= -1100000000; };
+  // nodes with wall links; "adjacent" ones (a wall among components 1..14, streaming.f95:492)
+  // take their targets at their first wall link, loop position (i0, node)
+  std::vector<int32_t> adj(N, -1);
+  std::vector<int64_t> k0;
   for (int z = 0; z < nz; ++z)
     for (int y = 0; y < ny; ++y)
       for (int x = 0; x < nx; ++x) {
@@ -69,15 +81,40 @@ int decode_links39(const int32_t* st, int ngs, int nx, int ny, int nz, int perio
           why = "a node with state >= 0 that does not collide (200..298, 1000..50999)";
           return ELBM_E_UNSUPPORTED;
         }
+        if (s0 < 0) continue;
+        int i0 = -1, adjacent = 0;
+        for (int i = 1; i < Q39; ++i) {
+          const int32_t c = code(i, x, y, z);
+          if (is_wall(c) && i0 < 0) i0 = i;
+          if (i < 15 && c < -1000) adjacent = 1;
+        }
+        if (i0 >= 0 && !(shifted && pfd == 1)) {
+          why = "interpolated wall links are available on the shifted lattice with primary_flow_dir 1 only";
+          return ELBM_E_UNSUPPORTED;
+        }
+        if (i0 >= 0 && adjacent) {
+          const int64_t n = ((int64_t)z * ny + y) * nx + x;
+          adj[n] = (int32_t)k0.size();
+          k0.push_back(((int64_t)i0 * N + n) * 2);
+        }
       }
-  // last write of every post-streaming slot: loop position and symbol
+  // last write of every post-streaming slot: loop position (direction, node, then 0 for the
+  // push and 1 for the node's own boundary write) and symbol; and for the adjacent wall nodes
+  // the last write up to the push at their first wall link
   std::vector<int64_t> key((size_t)N * Q39, -1);
   std::vector<Sym> val((size_t)N * Q39);
+  std::vector<int64_t> skey(k0.size() * Q39, -1);
+  std::vector<Sym> sval(k0.size() * Q39);
   auto emit = [&](int64_t t, int j, int64_t k, const Sym& v) {
     const size_t e = (size_t)t * Q39 + j;
     if (k > key[e]) {
       key[e] = k;
       val[e] = v;
+    }
+    const int32_t a = adj[t];
+    if (a >= 0 && k <= k0[a] && k > skey[(size_t)a * Q39 + j]) {
+      skey[(size_t)a * Q39 + j] = k;
+      sval[(size_t)a * Q39 + j] = v;
     }
   };
   Sym fo[Q39];
@@ -93,7 +130,7 @@ int decode_links39(const int32_t* st, int ngs, int nx, int ny, int nz, int perio
           fo[i].pop = (int8_t)i;
         }
         for (int i = 0; i < Q39; ++i) {
-          const int64_t kpos = (int64_t)i * N + n;  // loop order: i, then z, y, x
+          const int64_t kpos = ((int64_t)i * N + n) * 2;  // loop order: i, then z, y, x
           int tx, ty, tz;
           const int64_t t = target(x, y, z, i, tx, ty, tz);
           if (i == 0 && shifted) {
@@ -107,6 +144,16 @@ int decode_links39(const int32_t* st, int ngs, int nx, int ny, int nz, int perio
             continue;
           }
           if (c == -666) continue;
+          if (is_wall(c)) {
+            // streaming.f95:482-486 pushes onto a node with state >= 0; shifted_ibb then rewrites
+            // fout(x, opp(i)) and fi(x, opp(i)) = fout(x, i) (opp(i) = i on the shifted lattice)
+            if (t >= 0 && code(0, tx, ty, tz) >= 0) emit(t, i, kpos, fo[i]);
+            fo[i].kind = 3;
+            fo[i].pop = (int8_t)i;
+            fo[i].node = -1;
+            emit(n, i, kpos + 1, fo[i]);
+            continue;
+          }
           if (shifted && t >= 0) emit(t, i, kpos, fo[i]);
           const int o = L.opp[i];
           Sym eq;
@@ -157,60 +204,132 @@ int decode_links39(const int32_t* st, int ngs, int nx, int ny, int nz, int perio
               return ELBM_E_UNSUPPORTED;
             }
           } else if (c <= -300 && c >= -499) {
-            emit(n, i, kpos, fo[i]);
+            emit(n, i, kpos + 1, fo[i]);
             continue;
           } else {
             why = "unsupported D3Q39 link code " + std::to_string(c);
             return ELBM_E_UNSUPPORTED;
           }
-          emit(n, o, kpos, fo[i]);
+          emit(n, o, kpos + 1, fo[i]);
         }
       }
+  // link word of a symbol seen from node (x, y, z); false when it cannot be encoded
+  auto encode = [&](const Sym& v, bool written, int x, int y, int z, uint32_t& w) -> bool {
+    if (!written || v.kind == 0) {
+      w = link39(L39_STALE, 0, 0, 0, 0, 0);
+      return true;
+    }
+    if (v.kind == 2) {
+      w = link39(L39_EQ, v.pop, v.table, 0, 0, 0);
+      return true;
+    }
+    if (v.kind == 3) {
+      w = link39(L39_WALL, v.pop, 0, 0, 0, 0);
+      return true;
+    }
+    // fout(m, k): displacement from this node, minimal image on periodic axes
+    const int mx = (int)(v.node % nx), my = (int)((v.node / nx) % ny), mz = (int)(v.node / ((int64_t)nx * ny));
+    int dx = mx - x, dy = my - y, dz = mz - z;
+    if (periodic & 1) dx = ((dx % nx) + nx + nx / 2) % nx - nx / 2;
+    if (periodic & 2) dy = ((dy % ny) + ny + ny / 2) % ny - ny / 2;
+    if (periodic & 4) dz = ((dz % nz) + nz + nz / 2) % nz - nz / 2;
+    if (dx < -4 || dx > 4 || dy < -4 || dy > 4 || dz < -4 || dz > 4) return false;
+    w = link39(L39_PULL, v.pop, 0, dx, dy, dz);
+    return true;
+  };
+  // node index of (x, y, z) with periodic wrap, -1 outside the box
+  auto node_at = [&](int x, int y, int z) -> int64_t {
+    if (periodic & 1) x = ((x % nx) + nx) % nx;
+    else if (x < 0 || x >= nx) return -1;
+    if (periodic & 2) y = ((y % ny) + ny) % ny;
+    else if (y < 0 || y >= ny) return -1;
+    if (periodic & 4) z = ((z % nz) + nz) % nz;
+    else if (z < 0 || z >= nz) return -1;
+    return ((int64_t)z * ny + y) * nx + x;
+  };
+  Lattice39 L0;  // the unshifted set: erp = its opposites (linking/modules/linkwise.f95:39)
+  build_lattice39(0, pfd, L0);
   // classify the fluid nodes and encode the boundary records
   out.ntype.assign(N, 0);
   out.bidx.assign(N, -1);
   out.words.clear();
   out.bnodes.clear();
+  out.walls.clear();
+  out.recwall.clear();
   for (int z = 0; z < nz; ++z)
     for (int y = 0; y < ny; ++y)
       for (int x = 0; x < nx; ++x) {
         const int64_t n = ((int64_t)z * ny + y) * nx + x;
         if (!fluid39(code(0, x, y, z))) continue;
         uint32_t w[Q39];
-        bool bulk = true;
+        bool bulk = true, wall = false;
         for (int j = 0; j < Q39; ++j) {
           const Sym& v = val[(size_t)n * Q39 + j];
-          if (key[(size_t)n * Q39 + j] < 0 || v.kind == 0) {
-            w[j] = link39(L39_STALE, 0, 0, 0, 0, 0);
-            bulk = false;
-            continue;
-          }
-          if (v.kind == 2) {
-            w[j] = link39(L39_EQ, v.pop, v.table, 0, 0, 0);
-            bulk = false;
-            continue;
-          }
-          // fout(m, k): displacement from this node, minimal image on periodic axes
-          const int mx = (int)(v.node % nx), my = (int)((v.node / nx) % ny), mz = (int)(v.node / ((int64_t)nx * ny));
-          int dx = mx - x, dy = my - y, dz = mz - z;
-          if (periodic & 1) dx = ((dx % nx) + nx + nx / 2) % nx - nx / 2;
-          if (periodic & 2) dy = ((dy % ny) + ny + ny / 2) % ny - ny / 2;
-          if (periodic & 4) dz = ((dz % nz) + nz + nz / 2) % nz - nz / 2;
-          if (dx < -4 || dx > 4 || dy < -4 || dy > 4 || dz < -4 || dz > 4) {
+          if (!encode(v, key[(size_t)n * Q39 + j] >= 0, x, y, z, w[j])) {
             why = "a slot reads a node more than 4 links away (box too small on a periodic axis)";
             return ELBM_E_UNSUPPORTED;
           }
-          w[j] = link39(L39_PULL, v.pop, 0, dx, dy, dz);
-          if (!(v.pop == j && dx == -L.cx[j] && dy == -L.cy[j] && dz == -L.cz[j])) bulk = false;
+          if (w[j] != link39(L39_PULL, j, 0, -L.cx[j], -L.cy[j], -L.cz[j])) bulk = false;
+          if (j > 0 && is_wall(code(j, x, y, z))) wall = true;
         }
-        if (bulk) {
+        if (bulk && !wall) {
           out.ntype[n] = 1;
-        } else {
-          out.ntype[n] = 2;
-          out.bidx[n] = (int32_t)out.bnodes.size();
-          out.bnodes.push_back((int32_t)n);
-          out.words.insert(out.words.end(), w, w + Q39);
+          continue;
         }
+        out.ntype[n] = wall ? 3 : 2;
+        out.bidx[n] = (int32_t)out.bnodes.size();
+        out.bnodes.push_back((int32_t)n);
+        out.words.insert(out.words.end(), w, w + Q39);
+        out.recwall.push_back(wall ? (int32_t)out.walls.size() : -1);
+        if (!wall) continue;
+        Wall39Rec r{};
+        r.node = (int32_t)n;
+        r.rec = out.bidx[n];
+        r.adjacent = adj[n] >= 0;
+        for (int j = 0; j < Q39; ++j) {
+          r.code[j] = code(j, x, y, z);
+          r.upass[j] = -1;
+          r.snap[j] = link39(L39_STALE, 0, 0, 0, 0, 0);
+        }
+        if (r.adjacent) {
+          const size_t a = (size_t)adj[n];
+          for (int j = 0; j < Q39; ++j) {
+            const Sym& v = sval[a * Q39 + j];
+            if (v.kind == 3 || !encode(v, skey[a * Q39 + j] >= 0, x, y, z, r.snap[j])) {
+              why = "target_finder would read a slot this decoder cannot express";
+              return ELBM_E_UNSUPPORTED;
+            }
+          }
+          // target_finder.f95:95-125: velocity and temperature of node x + c_j where link erp(j)
+          // is null, else of node x + c_5 (1-based)
+          for (int j = 1; j < Q39; ++j) {
+            if (!is_wall(r.code[j])) continue;
+            const int src = r.code[L0.opp[j]] == -666 ? j : 4;
+            const int64_t m = node_at(x + L.cx[src], y + L.cy[src], z + L.cz[src]);
+            if (m < 0) {
+              why = "target_finder reads the velocity of a node outside the box";
+              return ELBM_E_UNSUPPORTED;
+            }
+            r.upass[src] = (int32_t)m;
+          }
+        }
+        static const int SX[7] = {0, 1, 0, 0, -1, 0, 0}, SY[7] = {0, 0, 1, 0, 0, -1, 0},
+                         SZ[7] = {0, 0, 0, 1, 0, 0, -1};
+        for (int j = 0; j < 7; ++j) {
+          const int64_t m = node_at(x + SX[j], y + SY[j], z + SZ[j]);
+          r.sidx[j] = (int32_t)m;
+          r.st[j] = m < 0 ? -666 : code(0, (int)(m % nx), (int)((m / nx) % ny), (int)(m / ((int64_t)nx * ny)));
+          r.tidx[j] = -1;
+          if (!r.adjacent && r.st[j] >= 0) {
+            const int64_t mt = node_at(x + L.cx[j], y + L.cy[j], z + L.cz[j]);
+            if (mt < 0) {
+              why = "the wall stencil reads a temperature outside the box";
+              return ELBM_E_UNSUPPORTED;
+            }
+            r.tidx[j] = (int32_t)mt;
+          }
+        }
+        out.walls.push_back(r);
       }
   return ELBM_OK;
 }

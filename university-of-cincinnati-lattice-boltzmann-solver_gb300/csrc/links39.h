@@ -4,13 +4,18 @@
 #include <string>
 #include <vector>
 
+#include "kernels39.cuh"
+
 namespace elbm {
 
 struct Links39 {
-  std::vector<uint8_t> ntype;   // per node: 0 neither pushes nor collides, 1 bulk, 2 boundary record
+  std::vector<uint8_t> ntype;   // per node: 0 neither pushes nor collides, 1 bulk, 2 boundary record,
+                                //   3 boundary record with interpolated wall links
   std::vector<int32_t> bidx;    // per node: boundary record or -1
   std::vector<int32_t> bnodes;  // per record: node
   std::vector<uint32_t> words;  // 39 per record
+  std::vector<Wall39Rec> walls; // nodes with interpolated wall links
+  std::vector<int32_t> recwall; // per record: wall record or -1
 };
 
 int decode_links39(const int32_t* st, int ngs, int nx, int ny, int nz, int periodic, int shifted, int pfd,

@@ -35,6 +35,7 @@ module elbm_gb300_iface
     real(c_double) :: gama, t_ref, rho_ref, p_ref, mu_ref, kappa_ref, gas_const_R, const_vol, &
       const_press, molec_weight
     real(c_double) :: dt, elbm_epsilon, init_beta_1, init_beta_2, beta_1_scaling, beta_2_scaling
+    real(c_double) :: su_lm(13)   ! su_chi .. su_lambda_z
   end type
 
   type, bind(c), public :: elbm_d3q39_bc
@@ -42,6 +43,7 @@ module elbm_gb300_iface
     real(c_double) :: fs_fieq(39), fs_gieq(39)
     real(c_double) :: inl_fieq(39, 8), inl_gieq(39, 8)    ! C layout [8][39]
     real(c_double) :: outl_fieq(39, 8), outl_gieq(39, 8)
+    real(c_double) :: fs_u, fs_v, fs_w, fs_temp
   end type
 
   type, bind(c), public :: elbm_stats
@@ -57,7 +59,7 @@ module elbm_gb300_iface
     elbm_set_d3q39_params, elbm_upload_level39, elbm_download_level39, elbm_mark_triangles, &
     elbm_upload_level_noalloc, elbm_autotune, elbm_set_kernel_variant, elbm_alpha_harvest, &
     elbm_alpha_mlp_train, elbm_set_alpha_mlp, elbm_interlevel_setup, elbm_fill_fine_ghosts, &
-    elbm_average_down, elbm_amr_run, elbm_damp_level, elbm_set_links39
+    elbm_average_down, elbm_amr_run, elbm_damp_level, elbm_set_links39, elbm_upload_macro39
 
   interface
     integer(c_int) function elbm_create(device, ctx) bind(c, name="elbm_create")
@@ -128,6 +130,12 @@ module elbm_gb300_iface
       type(c_ptr), value :: ctx
       integer(c_int), value :: lvl, box
       real(c_double), intent(in) :: fout(*), gout(*), lm(*), w_vel(*)
+    end function
+    integer(c_int) function elbm_upload_macro39(ctx, lvl, box, macro) bind(c, name="elbm_upload_macro39")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl, box
+      real(c_double), intent(in) :: macro(*)   ! rho, u_vel, v_vel, w_vel, temp as one 5-component FAB
     end function
     integer(c_int) function elbm_download_level39(ctx, lvl, box, fout, gout, lm, w_vel, alpha, macro) &
         bind(c, name="elbm_download_level39")
