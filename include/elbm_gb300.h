@@ -175,8 +175,11 @@ typedef struct {
  * -1000, and on the shifted lattice with primary_flow_dir 1 the interpolated
  * wall links -1001 - floor(q 1e9) (Grad-type closure of shifted_ibb.f95 with
  * the targets of target_finder.f95; they read the previous step's macroscopic
- * fields, so elbm_upload_macro39 must follow elbm_upload_level39).  Inviscid
- * walls (-11, -12) give ELBM_E_UNSUPPORTED.  Nodes with state < 0 neither
+ * fields, so elbm_upload_macro39 must follow elbm_upload_level39), and the
+ * inviscid links -11 / -12 (specular reflection of inviscid_edge.f95: the
+ * population goes to the mirror direction at a displaced node; an inviscid
+ * link needs a -11 among the node's unit or speed-2 axis links, which the
+ * reference's table selects on).  Nodes with state < 0 neither
  * push nor collide; state >= 0 must be fluid (outside 200..298 and
  * 1000..50999); nodes outside the box on a non-periodic axis count as null
  * nodes (-666), as lbgrid/fluid_or_solid.f95:69-119 marks them for an

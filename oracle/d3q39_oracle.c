@@ -713,12 +713,71 @@ static void shifted_ibb39(const o39_consts* k, const o39_lattice* L, int i, int 
  *                   6: pure_outflow_bc, fout(x, i) = fout(x, opp(i))); fi(x, opp(i)) = fout(x, i)
  *   -300 - k, -400 - k  fi(x, i) = fout(x, i)
  *   -666            nothing
+ *   -11, -12        inviscid_edge.f95: fi(x + d, j) = fout(x, i), j the specular reflection (o39_inviscid)
+ *   -1001 - q 1e9   interpolated wall link (shifted lattice, ibb_link39)
  * and, on the shifted lattice, the interior push as well for every boundary
  * code, and the rest population pushed only when x + c_1 is a node with
  * state >= 0.  Slots no rule writes keep their value of the previous step
  * (fi_prev / gi_prev, updated here).  Periodic axes wrap (bit 0/1/2 = x/y/z);
  * pushes across a non-periodic face leave the box.  Then every fluid node
  * collides.  Returns -1 for a code outside this list. */
+/* inviscid_edge.f95 (D3Q39 branch): an inviscid link (-11/-12) of direction i
+ * sends fout(x, i) to fi(x + d, j), j the specular reflection.  Per axis where
+ * the unshifted velocity has a component: if the node's unit link along that
+ * component is -11 the component reflects (displacement 0 for speed-1
+ * diagonals, -c/2 for speed-2 ones); else, for speed-2 diagonals, if the
+ * speed-2 link along it is -11 it reflects with displacement +c/2; else it
+ * keeps its value and displacement c.  Axis directions reflect whatever the
+ * other links are (displacement 0, c/2, -2c/3 for speeds 1, 2, 3).  Two
+ * entries of the reference's table differ from this rule and are kept:
+ * direction 9 (1-based) with x and y (x and z) reflecting goes to 12 (11),
+ * and direction 27 with only y reflecting is displaced by the opposite y.
+ * Returns 0 when no component reflects (the reference leaves the direction
+ * unset there). */
+int o39_inviscid(int i, const int32_t* code, int* j, int* d) {
+  const int c[3] = {CX0[i], CY0[i], CZ0[i]};
+  int sp = 0, nz = 0;
+  for (int a = 0; a < 3; ++a) {
+    if (abs(c[a]) > sp) sp = abs(c[a]);
+    nz += c[a] != 0;
+  }
+  int r[3] = {c[0], c[1], c[2]};
+  int refl[3] = {0, 0, 0};
+  if (nz == 1) {
+    for (int a = 0; a < 3; ++a) {
+      r[a] = -c[a];
+      d[a] = sp == 1 ? 0 : sp == 2 ? c[a] / 2 : -(2 * c[a]) / 3;
+    }
+  } else {
+    int any = 0;
+    for (int a = 0; a < 3; ++a) {
+      d[a] = c[a];
+      if (c[a] == 0) continue;
+      const int neg = c[a] < 0;
+      const int unit = 1 + a + 3 * neg, two = 15 + a + 3 * neg;
+      if (code[unit] == -11) {
+        r[a] = -c[a];
+        d[a] = sp == 1 ? 0 : -c[a] / 2;
+        refl[a] = any = 1;
+      } else if (sp == 2 && code[two] == -11) {
+        r[a] = -c[a];
+        d[a] = c[a] / 2;
+        refl[a] = any = 1;
+      }
+    }
+    if (!any) return 0;
+    if (i == 8 && refl[0] && !refl[2] && refl[1]) { r[0] = 1; r[1] = 1; r[2] = -1; }
+    else if (i == 8 && refl[0] && !refl[1] && refl[2]) { r[0] = 1; r[1] = -1; r[2] = 1; }
+    if (i == 26 && !refl[0] && refl[1]) d[1] = -d[1];
+  }
+  for (int k = 0; k < Q; ++k)
+    if (CX0[k] == r[0] && CY0[k] == r[1] && CZ0[k] == r[2]) {
+      *j = k;
+      return 1;
+    }
+  return 0;
+}
+
 /* Per-step target cache of the wall-link nodes (node_pt and the *_temp fields of streaming.f95). */
 typedef struct {
   unsigned char* done;
@@ -902,6 +961,24 @@ int o39_step_links(const o39_consts* k, o39_level* s, int step, o39_stats* st, c
             continue;
           }
           if (code == -666) continue;
+          if (code == -11 || code == -12) {
+            /* streaming.f95:370-382: the shifted push, then fi(x + d, j) = fout(x, i) */
+            if (k->shifted && t >= 0) {
+              fi[(int64_t)i * N + t] = fo[a];
+              gi[(int64_t)i * N + t] = go[a];
+            }
+            int32_t codes[Q];
+            for (int q2 = 0; q2 < Q; ++q2) codes[q2] = q2 == 0 ? s0 : state[(int64_t)q2 * N + n];
+            int j = 0, d[3];
+            if (!o39_inviscid(i, codes, &j, d)) { rc = -4; break; }
+            /* a reflection that lands outside the box leaves it, like a push across a face */
+            const int64_t r2 = nb39(x + d[0], y + d[1], z + d[2], nx, ny, nz, periodic);
+            if (r2 >= 0) {
+              fi[(int64_t)j * N + r2] = fo[a];
+              gi[(int64_t)j * N + r2] = go[a];
+            }
+            continue;
+          }
           if (code <= -1001 && code >= -1100000000) {
             /* wall link (streaming.f95:478-1133): shifted lattice, primary flow along +x only */
             if (!k->shifted || k->primary_flow_dir != 1) { rc = -3; break; }

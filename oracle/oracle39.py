@@ -197,3 +197,18 @@ def ibb_wall_axis(i, axis):
     up = ct.c_int(0)
     wall = L.o39_ibb_wall_axis(i, axis, ct.byref(up))
     return bool(wall), bool(up.value)
+
+
+def inviscid(i, codes):
+    """(found, j, d) of the oracle's specular rule for an inviscid link of direction i (0-based),
+    given the node's 39 state components."""
+    L = lib()
+    if not getattr(L, "_o39_inv_ready", False):
+        L.o39_inviscid.restype = ct.c_int
+        L.o39_inviscid.argtypes = [ct.c_int, ct.c_void_p, ct.POINTER(ct.c_int), ct.c_void_p]
+        L._o39_inv_ready = True
+    c = np.ascontiguousarray(codes, np.int32)
+    j = ct.c_int(0)
+    d = np.zeros(3, np.int32)
+    ok = L.o39_inviscid(i, _p(c), ct.byref(j), _p(d))
+    return bool(ok), j.value, tuple(int(x) for x in d)

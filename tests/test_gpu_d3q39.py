@@ -61,11 +61,13 @@ def test_d3q39_periodic_parity(pkg, o39, built_lib, start_step, steps):
     ctx.close()
 
 
-@pytest.mark.parametrize("shifted,outlet_type", [(0, 6), (1, 6), (1, 2)])
-def test_d3q39_link_codes_parity(pkg, o39, built_lib, shifted, outlet_type):
+@pytest.mark.parametrize("shifted,outlet_type,side", [(0, 6, 0), (1, 6, 0), (1, 2, 0), (0, 1, -11), (1, 6, -11)])
+def test_d3q39_link_codes_parity(pkg, o39, built_lib, shifted, outlet_type, side):
     """A D3Q39 box with an inlet, an outlet, a bounce-back wall, a freestream
-    face, solid nodes and a periodic axis: the GPU step with the library's
-    pull tables against the oracle's push loop, 1e-12 relative."""
+    face, solid nodes and either a periodic axis (side 0) or inviscid side
+    walls (side -11, specular reflection of inviscid_edge.f95): the GPU step
+    with the library's pull tables against the oracle's push loop, 1e-12
+    relative."""
     import math
     setup39, cap = pkg.d3q39_setup, pkg.capi
     if shifted:
@@ -78,9 +80,10 @@ def test_d3q39_link_codes_parity(pkg, o39, built_lib, shifted, outlet_type):
     _, ff, gf, _ = o39.init_node(k, 1.0, c.mach, 0.0, 0.0, c.temperature, lm0)
     _, fi, gi, _ = o39.init_node(k, 1.02, c.mach, 0.0, 0.0, c.temperature, lm0)
     _, fo, go, _ = o39.init_node(k, 0.98, c.mach, 0.0, 0.0, c.temperature, lm0)
-    nx, ny, nz, periodic = 16, 6, 7, 2
-    faces = {"x-": -101, "x+": -201, "z-": -10, "z+": -1000, "y-": 0, "y+": 0}
-    st = setup39.box_state39(nx, ny, nz, faces, shifted, 1, periodic=periodic)
+    nx, ny, nz, periodic = 16, 6, 7, (2 if side == 0 else 0)
+    faces = {"x-": -101, "x+": -201, "z-": -10, "z+": -1000, "y-": side, "y+": side}
+    prio = ("x-", "x+", "z-", "z+", "y-", "y+") if side == 0 else ("y-", "y+", "x-", "x+", "z-", "z+")
+    st = setup39.box_state39(nx, ny, nz, faces, shifted, 1, periodic=periodic, priority=prio)
     st[0, 3, 2:4, 6:8] = -1
     cx, cy, cz, _ = setup39.lattice39(shifted, 1)
     for i in range(1, 39):

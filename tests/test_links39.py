@@ -55,13 +55,17 @@ def pull39(words_kind, lev_f, lev_g, ntype, rec, words, prev_f, prev_g, eqf, eqg
     return F, G
 
 
-@pytest.mark.parametrize("shifted,outlet_type", [(0, 6), (0, 1), (1, 6), (1, 2)])
-def test_pull_tables_match_push_loop(pkg, built_lib, shifted, outlet_type):
+@pytest.mark.parametrize("shifted,outlet_type,side", [(0, 6, 0), (0, 1, 0), (1, 6, 0), (1, 2, 0), (0, 6, -11),
+                                                      (1, 1, -11)])
+def test_pull_tables_match_push_loop(pkg, built_lib, shifted, outlet_type, side):
+    """side 0: periodic in y; -11 / -12: inviscid side walls (specular reflection), which take the
+    links that also cross another face (so every inviscid link has an inviscid axis link)."""
     s39, cap = pkg.d3q39_setup, pkg.capi
     c, k, lm0, (ff, gf, fi, gi, fo, go) = _case(pkg, shifted)
-    nx, ny, nz, periodic = 14, 6, 7, 2
-    faces = {"x-": -101, "x+": -201, "z-": -10, "z+": -1000, "y-": 0, "y+": 0}
-    st = s39.box_state39(nx, ny, nz, faces, shifted, 1, periodic=periodic)
+    nx, ny, nz, periodic = 14, 6, 7, (2 if side == 0 else 0)
+    faces = {"x-": -101, "x+": -201, "z-": -10, "z+": -1000, "y-": side, "y+": side}
+    prio = ("x-", "x+", "z-", "z+", "y-", "y+") if side == 0 else ("y-", "y+", "x-", "x+", "z-", "z+")
+    st = s39.box_state39(nx, ny, nz, faces, shifted, 1, periodic=periodic, priority=prio)
     # a few solid nodes with bounce-back links around them, and a null link
     st[0, 3, 2:4, 5:7] = -1
     cx, cy, cz, opp = s39.lattice39(shifted, 1)

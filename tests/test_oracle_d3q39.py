@@ -123,3 +123,36 @@ def test_wall_derivative_rule_matches_reference_table(o39):
             assert wall == (e["form"] == "wall"), (kind, e)
             if wall:
                 assert up == e["up"], (kind, e)
+
+
+def test_inviscid_rule_matches_reference_table(o39):
+    """The oracle's specular-reflection rule for D3Q39 inviscid links against
+    the reference's table (tests/golden/inviscid_table.json, written by
+    tests/golden/make_inviscid_table.py from inviscid_edge.f95): for every
+    direction and every combination of its unit and speed-2 axis links being
+    -11, the first branch of the reference's IF chain that applies gives the
+    reflected direction and the displacement."""
+    import itertools
+    import json
+    import pathlib
+
+    table = json.loads((pathlib.Path(__file__).parent / "golden" / "inviscid_table.json").read_text())
+    assert len(table) == 38
+    checked = 0
+    for key, branches in table.items():
+        i = int(key) - 1
+        comps = sorted({c for b in branches for c in b["cond"]})
+        for r in range(len(comps) + 1):
+            for walls in itertools.combinations(comps, r):
+                codes = np.zeros(39, np.int32)
+                codes[i] = -11
+                for c in walls:
+                    codes[c - 1] = -11
+                want = next((b for b in branches if set(b["cond"]) <= set(walls)), None)
+                ok, j, d = o39.inviscid(i, codes)
+                if want is None:
+                    assert not ok, (key, walls)
+                else:
+                    assert ok and j + 1 == want["dir"] and list(d) == want["loc"], (key, walls, j + 1, d, want)
+                checked += 1
+    assert checked == 274

@@ -19,7 +19,9 @@
 // the node's post-streaming slots as the loop has left them at the node's
 // first wall link, so the decoder also records, for such nodes, the last
 // write of every slot up to that point.
+#include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -36,6 +38,58 @@ struct Sym {
   int8_t table = 0;
   int64_t node = -1;
 };
+
+// inviscid_edge.f95 (D3Q39 branch): the specular reflection j of an inviscid
+// link (-11/-12) of direction i and the displacement d of the node that
+// receives fout(x, i).  Per axis where the unshifted velocity has a component:
+// the unit link along it being -11 reflects it (displacement 0 for speed-1
+// diagonals, -c/2 for speed-2 ones), else for speed-2 diagonals the speed-2
+// link being -11 reflects it (displacement +c/2), else it keeps c.  Axis
+// directions always reflect (displacement 0, c/2, -2c/3 for speeds 1, 2, 3).
+// The reference's table departs from this in two entries, kept here:
+// direction 9 (1-based) with x and y (x and z) reflecting goes to 12 (11), and
+// direction 27 with only y reflecting is displaced by the opposite y.
+bool inviscid39(const Lattice39& U, int i, const int32_t* code, int& j, int (&d)[3]) {
+  const int c[3] = {U.cx[i], U.cy[i], U.cz[i]};
+  const int sp = std::max(std::abs(c[0]), std::max(std::abs(c[1]), std::abs(c[2])));
+  const int nz = (c[0] != 0) + (c[1] != 0) + (c[2] != 0);
+  int r[3] = {c[0], c[1], c[2]};
+  bool refl[3] = {false, false, false};
+  if (nz == 1) {
+    for (int a = 0; a < 3; ++a) {
+      r[a] = -c[a];
+      d[a] = sp == 1 ? 0 : sp == 2 ? c[a] / 2 : -(2 * c[a]) / 3;
+    }
+  } else {
+    for (int a = 0; a < 3; ++a) {
+      d[a] = c[a];
+      if (c[a] == 0) continue;
+      const int side = c[a] < 0 ? 3 : 0;
+      if (code[1 + a + side] == -11) {
+        r[a] = -c[a];
+        d[a] = sp == 1 ? 0 : -c[a] / 2;
+        refl[a] = true;
+      } else if (sp == 2 && code[15 + a + side] == -11) {
+        r[a] = -c[a];
+        d[a] = c[a] / 2;
+        refl[a] = true;
+      }
+    }
+    if (!refl[0] && !refl[1] && !refl[2]) return false;
+    if (i == 8 && refl[0] && refl[1] && !refl[2]) {
+      r[0] = 1, r[1] = 1, r[2] = -1;
+    } else if (i == 8 && refl[0] && refl[2] && !refl[1]) {
+      r[0] = 1, r[1] = -1, r[2] = 1;
+    }
+    if (i == 26 && !refl[0] && refl[1]) d[1] = -d[1];
+  }
+  for (int k = 0; k < Q39; ++k)
+    if (U.cx[k] == r[0] && U.cy[k] == r[1] && U.cz[k] == r[2]) {
+      j = k;
+      return true;
+    }
+  return false;
+}
 
 bool fluid39(int32_t s0) {
   if (s0 < 0) return false;
@@ -68,6 +122,18 @@ int decode_links39(const int32_t* st, int ngs, int nx, int ny, int nz, int perio
     else if (tz < 0 || tz >= nz) return -1;
     return ((int64_t)tz * ny + ty) * nx + tx;
   };
+  // node index of (x, y, z) with periodic wrap, -1 outside the box
+  auto node_at = [&](int x, int y, int z) -> int64_t {
+    if (periodic & 1) x = ((x % nx) + nx) % nx;
+    else if (x < 0 || x >= nx) return -1;
+    if (periodic & 2) y = ((y % ny) + ny) % ny;
+    else if (y < 0 || y >= ny) return -1;
+    if (periodic & 4) z = ((z % nz) + nz) % nz;
+    else if (z < 0 || z >= nz) return -1;
+    return ((int64_t)z * ny + y) * nx + x;
+  };
+  Lattice39 L0;  // the unshifted set: erp = its opposites (linking/modules/linkwise.f95:39)
+  build_lattice39(0, pfd, L0);
   auto is_wall = [](int32_t c) { return c <= -1001 && c >= -1100000000; };
   // nodes with wall links; "adjacent" ones (a wall among components 1..14, streaming.f95:492)
   // take their targets at their first wall link, loop position (i0, node)
@@ -144,6 +210,21 @@ int decode_links39(const int32_t* st, int ngs, int nx, int ny, int nz, int perio
             continue;
           }
           if (c == -666) continue;
+          if (c == -11 || c == -12) {
+            // streaming.f95:370-382: the shifted push, then fi(x + d, j) = fout(x, i); a reflection
+            // landing outside the box leaves it, like a push across a face
+            if (shifted && t >= 0) emit(t, i, kpos, fo[i]);
+            int32_t codes[Q39];
+            for (int q = 0; q < Q39; ++q) codes[q] = code(q, x, y, z);
+            int j = 0, d[3];
+            if (!inviscid39(L0, i, codes, j, d)) {
+              why = "an inviscid link whose unit and speed-2 axis links carry no -11 (the reference leaves it unset)";
+              return ELBM_E_UNSUPPORTED;
+            }
+            const int64_t r = node_at(x + d[0], y + d[1], z + d[2]);
+            if (r >= 0) emit(r, j, kpos + 1, fo[i]);
+            continue;
+          }
           if (is_wall(c)) {
             // streaming.f95:482-486 pushes onto a node with state >= 0; shifted_ibb then rewrites
             // fout(x, opp(i)) and fi(x, opp(i)) = fout(x, i) (opp(i) = i on the shifted lattice)
@@ -237,18 +318,6 @@ int decode_links39(const int32_t* st, int ngs, int nx, int ny, int nz, int perio
     w = link39(L39_PULL, v.pop, 0, dx, dy, dz);
     return true;
   };
-  // node index of (x, y, z) with periodic wrap, -1 outside the box
-  auto node_at = [&](int x, int y, int z) -> int64_t {
-    if (periodic & 1) x = ((x % nx) + nx) % nx;
-    else if (x < 0 || x >= nx) return -1;
-    if (periodic & 2) y = ((y % ny) + ny) % ny;
-    else if (y < 0 || y >= ny) return -1;
-    if (periodic & 4) z = ((z % nz) + nz) % nz;
-    else if (z < 0 || z >= nz) return -1;
-    return ((int64_t)z * ny + y) * nx + x;
-  };
-  Lattice39 L0;  // the unshifted set: erp = its opposites (linking/modules/linkwise.f95:39)
-  build_lattice39(0, pfd, L0);
   // classify the fluid nodes and encode the boundary records
   out.ntype.assign(N, 0);
   out.bidx.assign(N, -1);
