@@ -937,6 +937,26 @@ __device__ __forceinline__ void node_update(const Step27Args& a, int64_t n, floa
   float ymax;
   bool bad;
   node_prepare(d, a.alpha_mode != 0, D2, y2, ymax, bad);
+  if (MODE != 1 && a.defer_on && a.alpha_mode != 0) {
+    // a node whose populations leave the series range takes the out-of-line solver, which would
+    // hold its whole warp: list it for the second kernel instead (warp-aggregated slots)
+    const bool defer = ymax > kYSmall;
+    const unsigned mk = __activemask();
+    const unsigned dm = __ballot_sync(mk, defer);
+    if (dm) {
+      const int lane = (int)(threadIdx.x & 31), leader = __ffs(dm) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(a.defer_count, (unsigned long long)__popc(dm));
+      base = __shfl_sync(mk, base, leader);
+      if (defer) {
+        const unsigned long long slot = base + __popc(dm & ((1u << lane) - 1u));
+        if ((long long)slot < a.defer_cap) {
+          a.defer_list[slot] = (uint32_t)n;
+          return;
+        }
+      }
+    }
+  }
   float delta0 = 0.f;
   int series_it = -1;
   if (MODE == 1 && a.alpha_mode != 0 && ymax > 0.f) {
@@ -961,6 +981,24 @@ __global__ void __launch_bounds__(128, MINB) d3q27_fp32_kernel(const Step27Args 
   float d[Q];
   gather(a, static_cast<const float*>(a.src), n, t, d);
   node_update<CHECK, MODE>(a, n, d);
+}
+
+// The listed nodes of a step (strongly non-equilibrium ones), one thread each:
+// the same gather and update as in the step kernel, so that a node's result
+// does not depend on where it is finished.  A fixed grid strides over the list.
+template <bool CHECK, int MODE>
+__global__ void __launch_bounds__(128) d3q27_fp32_deferred_kernel(const Step27Args a) {
+  const unsigned long long cnt = *a.defer_count;
+  const long long m = (long long)cnt < a.defer_cap ? (long long)cnt : a.defer_cap;
+  Step27Args b = a;
+  b.defer_on = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (long long)gridDim.x * blockDim.x) {
+    const int64_t n = a.defer_list[i];
+    const uint8_t t = __ldg(a.ntype + n);
+    float d[Q];
+    gather(b, static_cast<const float*>(b.src), n, t, d);
+    node_update<CHECK, MODE>(b, n, d);
+  }
 }
 
 // Persistent variant: a fixed grid (every SM full) whose warps take chunks of
@@ -1275,7 +1313,29 @@ void launch_staged(const Step27Args& a, cudaStream_t s) {
   d3q27_fp32_staged_kernel<CHECK, MODE><<<(unsigned)grid, 128, smem, s>>>(a);
 }
 
-void launch_d3q27_fp32(const Step27Args& a, cudaStream_t s) {
+void launch_d3q27_fp32_main(const Step27Args& a, cudaStream_t s);
+
+// Step kernel, then (with a list) the listed nodes.
+void launch_d3q27_fp32(const Step27Args& a0, cudaStream_t s) {
+  Step27Args a = a0;
+  const bool defer = a.defer_list && a.alpha_mode == 1;  // Newton alpha (the learned guess keeps its own path)
+  a.defer_on = defer ? 1 : 0;
+  if (defer) cudaMemsetAsync(a.defer_count, 0, sizeof(unsigned long long), s);
+  launch_d3q27_fp32_main(a, s);
+  if (!defer) return;
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  const long long grid = std::min<long long>((a.defer_cap + 127) / 128, (long long)sms * 8);
+  if (a.check_dH) d3q27_fp32_deferred_kernel<true, 0><<<(unsigned)grid, 128, 0, s>>>(a);
+  else if (a.harvest) d3q27_fp32_deferred_kernel<false, 2><<<(unsigned)grid, 128, 0, s>>>(a);
+  else d3q27_fp32_deferred_kernel<false, 0><<<(unsigned)grid, 128, 0, s>>>(a);
+}
+
+void launch_d3q27_fp32_main(const Step27Args& a, cudaStream_t s) {
   const int threads = 128;
   const int64_t blocks = (a.N + threads - 1) / threads;
   if (a.alpha_mode == 2 && !a.check_dH && !a.harvest && a.mlp) {

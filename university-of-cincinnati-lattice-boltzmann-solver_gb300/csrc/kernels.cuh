@@ -36,6 +36,12 @@ struct Step27Args {
   unsigned long long* neg_list;
   unsigned long long* neg_count;
   long long neg_cap;
+  // FP32 path: nodes with some |Delta_i / f_i| > 0.1 are listed here by the step kernel and
+  // finished by a second kernel (nullptr: solved in place)
+  uint32_t* defer_list;
+  unsigned long long* defer_count;
+  long long defer_cap;
+  int defer_on;           // 0 inside the kernel that finishes the listed nodes
   const uint8_t* ntype;   // NodeType per node
   const int32_t* bidx;    // boundary record per boundary node
   const uint16_t* words;  // Q link words per boundary record
