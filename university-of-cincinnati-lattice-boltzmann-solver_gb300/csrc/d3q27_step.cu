@@ -457,18 +457,22 @@ __device__ float mlp_forward(const float (&x)[Q]) {
 // g(2 + delta) and g'(2 + delta) of the truncated power series (see above).
 template <int K>
 __device__ __forceinline__ void series_g(const float (&S)[K + 1], float delta, float& g, float& gp) {
+  // (P, alpha^(n-2)) and (g, g') advance as pairs on the paired FP32 pipe
   const float alpha = 2.0f + delta;
-  float P = 0.f, pw = 1.f, two = 1.f;
-  g = 0.f;
-  gp = 0.f;
+  const float2 aa = make_float2(alpha, alpha);
+  float2 Pw = make_float2(0.f, 1.f);  // P_{n-2}, alpha^(n-2)
+  float2 G = make_float2(0.f, 0.f);   // g, g'
+  float two = 1.f;
 #pragma unroll
   for (int n = 2; n <= K; ++n) {
-    gp = fmaf((float)(a_n(n) * (n - 1)) * pw, S[n], gp);
-    P = fmaf(alpha, P, delta * two);
+    const float cgp = (float)(a_n(n) * (n - 1)) * Pw.y;
+    Pw = __ffma2_rn(aa, Pw, make_float2(delta * two, 0.f));
     two *= 2.f;
-    pw *= alpha;
-    g = fmaf(fmaf((float)a_n(n), P, (float)c0_n(n)), S[n], g);
+    const float cg = fmaf((float)a_n(n), Pw.x, (float)c0_n(n));
+    G = __ffma2_rn(make_float2(cg, cgp), make_float2(S[n], S[n]), G);
   }
+  g = G.x;
+  gp = G.y;
 }
 
 // Float-pair Newton over all 27 populations from alpha = 2: the fallback when
@@ -906,16 +910,22 @@ __device__ __forceinline__ void node_finish(const Step27Args& a, int64_t n, floa
   if (CHECK && dH > a.tol_dH) flags |= 0x8u;
   const float ab = (2.0f + al.delta) * (float)a.beta;
   bool neg = false;
+  const float2 ab2 = make_float2(ab, ab);
 #pragma unroll
-  for (int i = 0; i < Q; ++i) {
-    d[i] = fmaf(ab, (i & 1) ? D2[i >> 1].y : D2[i >> 1].x, d[i]);
-    neg |= (d[i] + (float)w27(i)) < 0.f;
+  for (int q = 0; q < 13; ++q) {
+    const float2 r = __ffma2_rn(ab2, D2[q], make_float2(d[2 * q], d[2 * q + 1]));
+    d[2 * q] = r.x;
+    d[2 * q + 1] = r.y;
   }
+  d[26] = fmaf(ab, D2[13].x, d[26]);
+  // f = w + d < 0, compared without forming the sum (same outcome without flush-to-zero)
+#pragma unroll
+  for (int i = 0; i < Q; ++i) neg |= d[i] < -(float)w27(i);
   if (neg) flags |= 0x4u;
   if (neg && a.neg_list) {
 #pragma unroll
     for (int i = 0; i < Q; ++i)
-      if (d[i] + (float)w27(i) < 0.f) {
+      if (d[i] < -(float)w27(i)) {
         const unsigned long long slot = atomicAdd(a.neg_count, 1ull);
         if ((long long)slot < a.neg_cap) a.neg_list[slot] = (unsigned long long)n * Q + i;
       }
