@@ -718,7 +718,7 @@ __device__ __forceinline__ bool series_newton(const float (&S)[K + 1], int n, fl
     series_g<K>(S, delta, g, gp);
     iters = it + 1;
     if (!(gp > 0.f)) return false;
-    const float step = g / gp;
+    const float step = __fdividef(g, gp);
     const float next = delta - step;
     // every |y| <= 0.1 puts the positivity bracket at alpha >= 10
     if (!(next > -1.0f) || !(next < 8.0f)) return false;
@@ -806,19 +806,20 @@ __device__ __forceinline__ void node_prepare(const float (&d)[Q], bool want_y, f
     if (cz27(i)) jz += cz27(i) * d[i];
   }
   const float rho = 1.0f + dr;
-  const float inv_rho = 1.0f / rho;
+  const float inv_rho = __fdividef(1.0f, rho);
   const float u[3] = {jx * inv_rho, jy * inv_rho, jz * inv_rho};
   // per-axis factor of the entropic equilibrium relative to its weight, minus one:
   // e_0 = psi - 1, e_+ = psi*zeta - 1, e_- = psi/zeta - 1, from small quantities only
+  // (quotients of well-scaled operands near 1: the fast reciprocal-based division)
   float e[3][3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const float uu = u[k] * u[k];
-    const float sm1 = 3.0f * uu / (1.0f + sqrtf(fmaf(3.0f, uu, 1.0f)));  // sqrt(1+3u^2) - 1
-    const float zm1 = (3.0f * u[k] + sm1) / (1.0f - u[k]);                 // zeta - 1
+    const float sm1 = __fdividef(3.0f * uu, 1.0f + sqrtf(fmaf(3.0f, uu, 1.0f)));  // sqrt(1+3u^2) - 1
+    const float zm1 = __fdividef(3.0f * u[k] + sm1, 1.0f - u[k]);                 // zeta - 1
     e[k][1] = -sm1;
     e[k][2] = fmaf(1.0f - sm1, zm1, -sm1);
-    e[k][0] = (-sm1 - zm1) / (1.0f + zm1);
+    e[k][0] = __fdividef(-sm1 - zm1, 1.0f + zm1);
   }
   // P_i = prod(1 + e) - 1 = A + (1 + A)(B + (1 + B) C), with the (y, z) part shared
   float qyz[3][3];
