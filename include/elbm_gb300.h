@@ -289,7 +289,7 @@ int elbm_damp_level(elbm_ctx* ctx, int lvl, int64_t* repaired);
 int elbm_autotune(elbm_ctx* ctx, int lvl, int reps, int* chosen, double* ms_per_variant);
 
 /* Use kernel variant v (0: direct loads; 1, 4, 5, 6, 7: direct, registers
- * capped for 4, 5, 6, 8, 10 blocks of 128 threads per SM; 2: rows staged in
+ * capped for 4, 5, 6, 8, 7 blocks of 128 threads per SM; 2: rows staged in
  * shared memory by bulk copies, persistent; 3: direct loads, persistent warps
  * taking 32-node chunks from a counter) for
  * the level's FP32 D3Q27 steps, instead of the autotuner's choice.  Variant 2

@@ -1401,7 +1401,7 @@ void launch_d3q27_fp32_main(const Step27Args& a, cudaStream_t s) {
   } else if (a.variant == 6) {
     d3q27_fp32_kernel<false, 8, 0><<<(unsigned)blocks, threads, 0, s>>>(a);
   } else if (a.variant == 7) {
-    d3q27_fp32_kernel<false, 10, 0><<<(unsigned)blocks, threads, 0, s>>>(a);
+    d3q27_fp32_kernel<false, 7, 0><<<(unsigned)blocks, threads, 0, s>>>(a);
   } else {
     d3q27_fp32_kernel<false, 0, 0><<<(unsigned)blocks, threads, 0, s>>>(a);
   }

@@ -64,7 +64,7 @@ struct Step27Args {
   int harvest_stride;
 };
 
-// 0: direct; 1, 4, 5, 6, 7: direct with registers capped for 4, 5, 6, 8, 10 blocks of 128 threads
+// 0: direct; 1, 4, 5, 6, 7: direct with registers capped for 4, 5, 6, 8, 7 blocks of 128 threads
 // per SM; 2: bulk-copy staged; 3: persistent warps taking chunks from a counter (4 blocks per SM)
 constexpr int kFp32Variants = 8;
 // Bytes allocated before and after each population buffer (never written):
