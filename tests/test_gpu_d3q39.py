@@ -115,7 +115,7 @@ def test_d3q39_link_codes_parity(pkg, o39, built_lib, shifted, outlet_type, side
     ctx.close()
 
 
-def _wall_case(pkg, o39, seed, outlet_type, nx=16, ny=6, nz=8, mach=1.5):
+def _wall_case(pkg, o39, seed, outlet_type, nx=16, ny=6, nz=8, mach=1.5, wedge=False):
     """Shifted D3Q39 box (Mach 1.5 along +x): inlet at x-, outlet at x+, a
     bounce-back floor, a freestream top, periodic in y, and a solid block on
     the floor whose fluid neighbours carry interpolated wall links with random
@@ -129,11 +129,15 @@ def _wall_case(pkg, o39, seed, outlet_type, nx=16, ny=6, nz=8, mach=1.5):
     (ff, gf), (fi, gi), (fo, go) = eq
     faces = {"x-": -101, "x+": -201, "z-": -10, "z+": -1000, "y-": 0, "y+": 0}
     periodic = 2
-    st = s39.box_state39(nx, ny, nz, faces, 1, 1, periodic=periodic)
-    solid = np.zeros((nz, ny, nx), bool)
-    solid[0:3, 1:4, 6:9] = True
     rng = np.random.default_rng(seed)
-    s39.wall_links39(st, solid, rng.uniform(0.05, 0.95, (39, nz, ny, nx)), 1, 1, periodic=periodic)
+    if wedge:
+        # a 20-degree wedge across the span from x = 5 to x = 12, wall distances from the geometry
+        st = s39.wedge_state39(nx, ny, nz, 5.0, 12.0, 20.0, faces, periodic=periodic)
+    else:
+        st = s39.box_state39(nx, ny, nz, faces, 1, 1, periodic=periodic)
+        solid = np.zeros((nz, ny, nx), bool)
+        solid[0:3, 1:4, 6:9] = True
+        s39.wall_links39(st, solid, rng.uniform(0.05, 0.95, (39, nz, ny, nx)), 1, 1, periodic=periodic)
     cx, cy, cz, _ = s39.lattice39(1, 1)
     erp = np.array(s39.OPP39) - 1
     for z, y, x, j in zip(*np.nonzero((st[0] >= 0)[None] & (st[1:15] <= -1001))[1:], np.nonzero(
@@ -159,9 +163,9 @@ def _wall_case(pkg, o39, seed, outlet_type, nx=16, ny=6, nz=8, mach=1.5):
     return c, k, st, lev, periodic, o39.bc(*args), pkg.capi.make_d3q39_bc(*args)
 
 
-@pytest.mark.parametrize("seed,outlet_type,mach,warm,steps", [(3, 6, 1.5, 0, 5), (4, 1, 0.8, 0, 8),
-                                                             (5, 6, 0.8, 97, 6)])
-def test_d3q39_wall_links_parity(pkg, o39, built_lib, seed, outlet_type, mach, warm, steps):
+@pytest.mark.parametrize("seed,outlet_type,mach,warm,steps,wedge", [(3, 6, 1.5, 0, 5, False), (4, 1, 0.8, 0, 8, False),
+                                                                   (5, 6, 0.8, 97, 6, False), (6, 6, 1.5, 0, 5, True)])
+def test_d3q39_wall_links_parity(pkg, o39, built_lib, seed, outlet_type, mach, warm, steps, wedge):
     """Interpolated wall links on the shifted lattice (target_finder, the target
     Newton solve, shifted_ibb) next to the other boundary codes: the GPU step
     against the oracle's push loop, 1e-12 relative.  Steps 0..4 (start-up
@@ -175,7 +179,8 @@ def test_d3q39_wall_links_parity(pkg, o39, built_lib, seed, outlet_type, mach, w
     step at the wall nodes.  That late run is held to 20 times the oracle's own
     spread under such noise (and never looser than 1e-9)."""
     cap = pkg.capi
-    c, k, st, lev, periodic, b, cb = _wall_case(pkg, o39, seed, outlet_type, mach=mach)
+    c, k, st, lev, periodic, b, cb = _wall_case(pkg, o39, seed, outlet_type, mach=mach, wedge=wedge,
+                                                nx=20 if wedge else 16, nz=10 if wedge else 8)
     nz, ny, nx = lev.shape
     prev_f, prev_g = lev.fout.copy(), lev.gout.copy()
     for step in range(warm):

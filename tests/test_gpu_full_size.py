@@ -10,8 +10,9 @@ not depend on size (the CPU oracle cannot run these sizes in a test):
 - three nested D3Q27 levels (128x64x64 coarse, 2:1 refinement twice) stepped by
   the graph-driven sub-cycle: finite, no fallbacks, the coarse mass steady;
 - D3Q39 384x192x48 on the shifted lattice at Mach 1.5 with inlet, outflow,
-  freestream, a bounce-back floor and a periodic span: finite, every node
-  updated, the multiplier solve never capped.
+  freestream, a bounce-back floor and a periodic span, with and without the
+  10-degree wedge's interpolated wall links: finite, every node updated, the
+  multiplier solve never capped.
 """
 import numpy as np
 import pytest
@@ -116,6 +117,44 @@ def test_three_levels_graph_subcycle(pkg, built_lib):
         assert np.isfinite(ctx.download(l)).all()
     m1 = ctx.download(0).sum(dtype=np.float64)
     assert abs(m1 - m0) <= 1e-3 * m0
+    ctx.close()
+
+
+def test_d3q39_wedge_384x192x48(pkg, built_lib):
+    """The Mach 1.5 wedge case at its full size: a 10-degree wedge on the floor from x = 96 to
+    x = 300 with interpolated wall links (wall distances from the geometry), inlet, pure
+    outflow, freestream top, bounce-back floor, periodic span; 3 steps from a uniform
+    freestream: finite, every fluid node updated, no multiplier solve capped."""
+    from oracle import oracle39 as o39
+
+    setup39, cap = pkg.d3q39_setup, pkg.capi
+    c = setup39.wedge_case_consts()
+    k = o39.consts(c)
+    lm, f, g, _ = o39.init_node(k, 1.0, c.mach, 0.0, 0.0, c.temperature, setup39.freestream_start_lm(c))
+    nx, ny, nz, periodic = 384, 192, 48, 2
+    faces = {"x-": -101, "x+": -201, "z-": -10, "z+": -1000, "y-": 0, "y+": 0}
+    st = setup39.wedge_state39(nx, ny, nz, 96.0, 300.0, 10.0, faces, periodic=periodic)
+    shape = (nz, ny, nx)
+    fluid = st[0] >= 0
+    walls = fluid & (st[1:] <= -1001).any(axis=0)
+    assert walls.sum() > 20000
+    fout = np.broadcast_to(f[:, None, None, None], (39,) + shape).copy()
+    gout = np.broadcast_to(g[:, None, None, None], (39,) + shape).copy()
+    lms = np.broadcast_to(lm[:, None, None, None], (13,) + shape).copy()
+    macro = np.stack([np.full(shape, 1.0), np.full(shape, c.mach), np.zeros(shape), np.zeros(shape),
+                      np.full(shape, c.temperature)])
+    bc = cap.make_d3q39_bc([1] * 8, [6] + [1] * 7, f, g, [f] * 8, [g] * 8, [f] * 8, [g] * 8,
+                           (c.mach, 0.0, 0.0, c.temperature))
+    ctx = cap.Context(0)
+    ctx.level_register(0, cap.ELBM_D3Q39, cap.ELBM_STORE_FP64, [[0, 0, 0, nx - 1, ny - 1, nz - 1]])
+    ctx.set_d3q39_params(0, cap.make_d3q39_params(c, timestep=0, periodic=periodic, damp=0))
+    ctx.set_links39(0, 0, st, bc)
+    ctx.upload39(0, 0, fout, gout, lms, np.zeros(shape))
+    ctx.upload_macro39(0, 0, macro)
+    s = ctx.step(0, 3)
+    out = ctx.download39(0)
+    assert s["node_updates"] == 3 * fluid.sum() and s["fallbacks"] == 0 and s["status"] & 1 == 0
+    assert np.isfinite(out["fout"][:, fluid]).all() and np.isfinite(out["gout"][:, fluid]).all()
     ctx.close()
 
 

@@ -218,3 +218,37 @@ def wall_links39(state: np.ndarray, solid: np.ndarray, q, shifted: int = 1, prim
         mark = up_solid & ~solid
         state[i][mark] = (-1001 - np.floor(qa[i][mark] * 1e9)).astype(np.int32)
     return state
+
+
+def wedge_state39(nx: int, ny: int, nz: int, x0: float, x1: float, angle_deg: float, faces: dict,
+                  primary_flow_dir: int = 1, periodic: int = 2) -> np.ndarray:
+    """State array (39, nz, ny, nx) of the shifted-lattice wedge case: box faces as in
+    box_state39 and a wedge across the whole span, its ramp rising at the given angle from
+    the floor at x = x0 to a vertical back face at x = x1 (nodes with x0 <= x <= x1 and
+    z <= tan(angle) (x - x0) are solid).  Every fluid node x whose upstream node x - c_i is
+    solid gets the wall code of the first crossing of the segment from x to x - c_i with
+    the wedge surface, at the fraction q of the segment (lbgrid/inter_bb_setup.f95: ray from
+    the node towards x - c_i on the shifted lattice; linking/modules/linkwise.f95:45-57)."""
+    st = box_state39(nx, ny, nz, faces, 1, primary_flow_dir, periodic=periodic)
+    cx, cy, cz, _ = lattice39(1, primary_flow_dir)
+    t = math.tan(math.radians(angle_deg))
+    z, y, x = np.meshgrid(np.arange(nz, dtype=np.float64), np.arange(ny, dtype=np.float64),
+                          np.arange(nx, dtype=np.float64), indexing="ij")
+    solid = (z <= t * (x - x0)) & (x >= x0) & (x <= x1)
+    q = np.full((39, nz, ny, nx), 0.5)
+    for i in range(1, 39):
+        best = np.full(solid.shape, np.inf)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            # ramp plane z = t (x - x0), between x0 and x1
+            dh = cz[i] - t * cx[i]
+            lam = (z - t * (x - x0)) / dh
+            X = x - lam * cx[i]
+            ok = (dh != 0.0) & (lam >= 0.0) & (lam <= 1.0) & (X >= x0) & (X <= x1)
+            best = np.where(ok, np.minimum(best, lam), best)
+            # back face x = x1, below the ramp's top
+            lam = (x - x1) / cx[i] if cx[i] != 0 else np.full(solid.shape, np.inf)
+            Z = z - lam * cz[i]
+            ok = (lam >= 0.0) & (lam <= 1.0) & (Z <= t * (x1 - x0))
+            best = np.where(ok, np.minimum(best, lam), best)
+        q[i] = np.where(np.isfinite(best), np.clip(best, 0.0, 1.0 - 1e-9), 0.5)
+    return wall_links39(st, solid, q, 1, primary_flow_dir, periodic=periodic)
