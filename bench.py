@@ -47,6 +47,7 @@ BYTES_PER_NODE_FP32 = 216  # 27 x 4 B read + 27 x 4 B written
 DRAM_BYTES_PER_NODE_NCU = 233
 KERNELS_PER_STEP = 2  # the step kernel and the listed-node kernel
 BYTES_PER_NODE_FP64 = 432
+BYTES_PER_NODE_D3Q39 = 1456  # f, g: 39 x 8 B read + written each; 13 multipliers x 8 B read + written
 
 
 def dist_env():
@@ -186,9 +187,43 @@ def cpu_baseline_sample(pkg, budget_s=15.0):
             "sample": f"{sx}x{sy}x{sz} sub-box of the workload, {steps} FP64 Newton-alpha steps, {dt:.1f} s"}
 
 
+def d3q39_wedge_leg(pkg, local_rank, steps=3):
+    """The compressible D3Q39 wedge case at its full size (384x192x48, Mach 1.5, shifted
+    lattice, 10-degree wedge with interpolated wall links, FP64): MLUPS of the fused
+    level step from CUDA events, after one untimed step."""
+    s39, cap = pkg.d3q39_setup, pkg.capi
+    c = s39.wedge_case_consts()
+    nx, ny, nz, periodic = 384, 192, 48, 2
+    faces = {"x-": -101, "x+": -201, "z-": -10, "z+": -1000, "y-": 0, "y+": 0}
+    t0 = time.perf_counter()
+    ctx = cap.Context(local_rank)
+    params = cap.make_d3q39_params(c, timestep=0, periodic=periodic, damp=0)
+    lm0 = s39.freestream_start_lm(c)
+    _, f, g = ctx.d3q39_equilibrium(params, 1.0, c.mach, 0.0, 0.0, c.temperature, lm0)  # freestream equilibria
+    st = s39.wedge_state39(nx, ny, nz, 96.0, 300.0, 10.0, faces, periodic=periodic)
+    shape = (nz, ny, nx)
+    bc = cap.make_d3q39_bc([1] * 8, [6] + [1] * 7, f, g, [f] * 8, [g] * 8, [f] * 8, [g] * 8,
+                           (c.mach, 0.0, 0.0, c.temperature))
+    ctx.level_register(0, cap.ELBM_D3Q39, cap.ELBM_STORE_FP64, [[0, 0, 0, nx - 1, ny - 1, nz - 1]])
+    ctx.set_d3q39_params(0, params)
+    ctx.set_links39(0, 0, st, bc)
+    setup_s = time.perf_counter() - t0
+    # every node starts at the freestream (multilevel_initialization.f90), solved on the device
+    ctx.init_level39(0, 0, np.stack([np.full(shape, 1.0), np.full(shape, c.mach), np.zeros(shape),
+                                     np.zeros(shape), np.full(shape, c.temperature)]), lm0)
+    ctx.step(0, 1, want_stats=False)
+    s = ctx.step(0, steps)
+    ctx.close()
+    walls = int(((st[0] >= 0) & (st[1:] <= -1001).any(axis=0)).sum())
+    return {"workload": "D3Q39 Mach 1.5 wedge 384x192x48, FP64, shifted lattice", "steps": steps,
+            "mlups": s["node_updates"] / (s["kernel_ms"] / 1e3) / 1e6, "ms_per_step": s["kernel_ms"] / steps,
+            "wall_nodes": walls, "fallbacks": s["fallbacks"], "status": s["status"],
+            "lm_iters_per_node": s["newton_iters"] / max(1, s["node_updates"]), "setup_s": setup_s,
+            "algorithmic_bytes_per_node": BYTES_PER_NODE_D3Q39}
+
+
 def learned_alpha_leg(pkg, ctx, args, bp, local_rank):
     """Harvest, train, and time the learned-alpha path; returns a summary dict."""
-    from oracle import mlp_ref  # initial weights only (a seeded Gaussian draw)
 
     cap, geo = pkg.capi, pkg.geometry
     recs = []
@@ -214,7 +249,7 @@ def learned_alpha_leg(pkg, ctx, args, bp, local_rank):
         h.close()
     rec = np.concatenate(recs)
     t0 = time.perf_counter()
-    w, hist = ctx.alpha_mlp_train(rec, mlp_ref.init(0).astype(np.float32), epochs=4, batch=8192, lr=2e-3, seed=1)
+    w, hist = ctx.alpha_mlp_train(rec, cap.mlp_init_weights(0), epochs=4, batch=8192, lr=2e-3, seed=1)
     train_s = time.perf_counter() - t0
     ctx.set_alpha_mlp(0, w)
     lp = cap.make_d3q27_params(**dict(bp, alpha_mode=cap.ELBM_ALPHA_LEARNED))
@@ -240,6 +275,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-d3q39", action="store_true", help="skip the D3Q39 wedge leg")
     ap.add_argument("--size", default=None, help="NXxNYxNZ override (profiling runs on a smaller box)")
     ap.add_argument("--alpha", default="newton", choices=["newton", "fixed2"],
                     help="alpha of the timed path (fixed2 = LBGK limit, to separate the alpha solve's cost)")
@@ -252,7 +288,7 @@ def main():
         global NX, NY, NZ
         NX, NY, NZ = (int(v) for v in args.size.lower().split("x"))
     if args.profile:
-        args.no_cpu_baseline = args.no_fp64 = True
+        args.no_cpu_baseline = args.no_fp64 = args.no_d3q39 = True
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
@@ -371,6 +407,10 @@ def main():
         fp64 = s64["node_updates"] / (s64["kernel_ms"] / 1e3) / 1e6
         c64.close()
 
+    wedge = None
+    if not args.no_d3q39:
+        wedge = d3q39_wedge_leg(pkg, local_rank)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline_sample(pkg)
@@ -404,6 +444,7 @@ def main():
                            "exact_path_nodes": vst["exact_path_nodes"], "status": vst["status"],
                            "newton_iters_per_node": vst["newton_iters"] / max(1, vst["node_updates"])},
             "plain_fp64_newton_mlups": fp64,
+            "d3q39_wedge": wedge,
             "learned_alpha": learned,
             "cpu_baseline": cpu,
         }

@@ -41,6 +41,7 @@ typedef struct elbm_ctx elbm_ctx;
 #define ELBM_E_CUDA -2        /* CUDA runtime error */
 #define ELBM_E_UNSUPPORTED -3 /* unsupported link code / configuration */
 #define ELBM_E_STATE -4       /* call out of order (e.g. step before upload) */
+#define ELBM_E_NUMERIC -5     /* a set-up solve did not converge */
 
 /* numerical health flags in elbm_stats.status */
 #define ELBM_ST_NAN 0x1u             /* a density or velocity became NaN/Inf */
@@ -140,6 +141,24 @@ int elbm_set_d3q39_params(elbm_ctx* ctx, int lvl, const elbm_d3q39_params* p);
  * step's w velocity (1 comp), all as FABs with the level's ghost width. */
 int elbm_upload_level39(elbm_ctx* ctx, int lvl, int box, const double* fout, const double* gout, const double* lm,
                         const double* w_vel);
+/* Initial state of a D3Q39 box from its macroscopic fields rho, u, v, w, T
+ * (5 comps, FAB layout), computed on the device node by node like
+ * multilevel_initialization.f90:229-278: the multiplier Newton from lm_start
+ * (13 values, e.g. the freestream start of freestream_basis_calcs.f90:24-90)
+ * for rho, u and the equilibrium pressure tensor, then f = f_eq,
+ * g = (2 C_v - 3) T f_eq; the multipliers, w and the fields are stored.
+ * Replaces elbm_upload_level39 + elbm_upload_macro39 when the populations
+ * start at equilibrium.  *capped (may be NULL): nodes whose Newton hit
+ * max_lm_iters. */
+int elbm_init_level39(elbm_ctx* ctx, int lvl, int box, const double* macro, const double* lm_start,
+                      int64_t* capped);
+/* The same solve for one state (rho, u, v, w, T in macro[5]), e.g. the
+ * freestream or inlet equilibria elbm_set_links39 takes
+ * (freestream_basis_calcs.f90): lm (13) is the start and returns the
+ * multipliers; fieq, gieq receive 39 values each.  Uses the context's device;
+ * no level needed.  ELBM_E_NUMERIC if the Newton does not converge. */
+int elbm_d3q39_equilibrium(elbm_ctx* ctx, const elbm_d3q39_params* p, const double* macro, double* lm,
+                           double* fieq, double* gieq);
 /* The macroscopic fields rho, u, v, w, T (5 comps, FAB layout) the step
  * starts from: the reference's rho, u_vel, v_vel, w_vel, temp after
  * initialisation (multilevel_initialization.f90).  Needed by interpolated wall

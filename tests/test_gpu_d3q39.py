@@ -236,3 +236,41 @@ def test_d3q39_wall_links_need_macro(pkg, o39, built_lib):
     ctx.upload39(0, 0, lev.fout, lev.gout, lev.lm, lev.w_vel)
     with pytest.raises(cap.ElbmError):
         ctx.step(0, 1)
+
+
+def test_d3q39_initial_state_on_device(pkg, o39, built_lib):
+    """elbm_init_level39 (multiplier Newton per node from its macroscopic fields, then
+    f = f_eq, g = (2 C_v - 3) T f_eq) and elbm_d3q39_equilibrium against the oracle's
+    o39_init_node, 1e-12 relative, on the shifted and the unshifted lattice."""
+    setup39, cap = pkg.d3q39_setup, pkg.capi
+    for shifted in (1, 0):
+        mach = 1.5 if shifted else 0.3
+        c = setup39.wedge_case_consts(v_inf_ms=mach * math.sqrt(1.4 * setup39.GAS_CONST_R * 288.15))
+        k = o39.consts(c)
+        lm0 = setup39.freestream_start_lm(c)
+        nx, ny, nz = 7, 5, 4
+        rng = np.random.default_rng(21 + shifted)
+        shape = (nz, ny, nx)
+        macro = np.stack([1 + 0.02 * rng.uniform(-1, 1, shape), c.mach * (1 + 0.02 * rng.uniform(-1, 1, shape)),
+                          0.01 * rng.uniform(-1, 1, shape), 0.01 * rng.uniform(-1, 1, shape),
+                          c.temperature * (1 + 0.02 * rng.uniform(-1, 1, shape))])
+        ctx = cap.Context(0)
+        params = cap.make_d3q39_params(c, timestep=0, periodic=7, damp=0)
+        ctx.level_register(0, cap.ELBM_D3Q39, cap.ELBM_STORE_FP64, [[0, 0, 0, nx - 1, ny - 1, nz - 1]])
+        ctx.set_d3q39_params(0, params)
+        assert ctx.init_level39(0, 0, macro, lm0) == 0
+        out = ctx.download39(0)
+        for z in range(nz):
+            for y in range(ny):
+                for x in range(nx):
+                    lm, f, g, _ = o39.init_node(k, *macro[:, z, y, x], lm0)
+                    for name, ref in (("fout", f), ("gout", g), ("lm", lm)):
+                        got = out[name][:, z, y, x]
+                        # relative for the populations; multipliers near zero against max(|lm|, 1)
+                        scale = np.abs(ref) if name != "lm" else np.maximum(np.abs(ref), 1.0)
+                        assert np.max(np.abs(got - ref) / scale) <= 1e-12, name
+        assert np.array_equal(out["w_vel"], macro[3])
+        lm_e, f_e, g_e = ctx.d3q39_equilibrium(params, 1.0, c.mach, 0.0, 0.0, c.temperature, lm0)
+        lm_r, f_r, g_r, _ = o39.init_node(k, 1.0, c.mach, 0.0, 0.0, c.temperature, lm0)
+        assert np.max(np.abs(f_e - f_r) / f_r) <= 1e-12 and np.max(np.abs(g_e - g_r) / g_r) <= 1e-12
+        ctx.close()

@@ -92,6 +92,18 @@ class D3Q39Bc(ct.Structure):
                 ("fs_u", ct.c_double), ("fs_v", ct.c_double), ("fs_w", ct.c_double), ("fs_temp", ct.c_double)]
 
 
+def mlp_init_weights(seed: int = 0) -> np.ndarray:
+    """Initial weights of the 27-64-64-1 alpha network in the library's packed order
+    (W1 27x64 row-major, b1, W2 64x64, b2, w3, b3): normal draws scaled by 1/sqrt(fan-in),
+    zero biases."""
+    rng = np.random.default_rng(seed)
+    ni, nh = 27, 64
+    w1 = rng.normal(0, 1 / np.sqrt(ni), (ni, nh))
+    w2 = rng.normal(0, 1 / np.sqrt(nh), (nh, nh))
+    w3 = rng.normal(0, 1 / np.sqrt(nh), nh)
+    return np.concatenate([w1.ravel(), np.zeros(nh), w2.ravel(), np.zeros(nh), w3, np.zeros(1)]).astype(np.float32)
+
+
 def make_d3q39_bc(inlet_type, outlet_type, fs_f, fs_g, inl_f, inl_g, outl_f, outl_g,
                   fs_uvwT=(0.0, 0.0, 0.0, 0.0)) -> D3Q39Bc:
     """Boundary equilibria (f and g), inlet/outlet types and the freestream velocity and
@@ -143,6 +155,8 @@ SIGNATURES = {
     "elbm_upload_level39": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _vp]),
     "elbm_download_level39": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
     "elbm_upload_macro39": (_c_int, [_vp, _c_int, _c_int, _vp]),
+    "elbm_init_level39": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp]),
+    "elbm_d3q39_equilibrium": (_c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "elbm_upload_level_noalloc": (_c_int, [_vp, _c_int, _c_int, _vp]),
     "elbm_autotune": (_c_int, [_vp, _c_int, _c_int, _vp, _vp]),
     "elbm_set_kernel_variant": (_c_int, [_vp, _c_int, _c_int]),
@@ -340,6 +354,24 @@ class Context:
     def upload39(self, lvl, box, fout, gout, lm, w_vel):
         arrs = [np.ascontiguousarray(a, np.float64) for a in (fout, gout, lm, w_vel)]
         self._check(self.lib.elbm_upload_level39(self.h, lvl, box, *map(_ptr, arrs)))
+
+    def init_level39(self, lvl, box, macro, lm_start):
+        """Equilibrium initial state of a D3Q39 box from rho, u, v, w, T (5, nz, ny, nx) on the
+        device; returns the number of nodes whose multiplier Newton hit the cap."""
+        m = np.ascontiguousarray(macro, np.float64)
+        l0 = np.ascontiguousarray(lm_start, np.float64)
+        capped = ct.c_int64(0)
+        self._check(self.lib.elbm_init_level39(self.h, lvl, box, _ptr(m), _ptr(l0), ct.byref(capped)))
+        return capped.value
+
+    def d3q39_equilibrium(self, params, rho, u, v, w, T, lm_start):
+        """(lm, fieq, gieq) of one state: the multiplier Newton from lm_start."""
+        m = np.array([rho, u, v, w, T], np.float64)
+        lm = np.ascontiguousarray(lm_start, np.float64).copy()
+        f = np.zeros(39)
+        g = np.zeros(39)
+        self._check(self.lib.elbm_d3q39_equilibrium(self.h, ct.byref(params), _ptr(m), _ptr(lm), _ptr(f), _ptr(g)))
+        return lm, f, g
 
     def upload_macro39(self, lvl, box, macro):
         """rho, u, v, w, T (5, nz, ny, nx) the next step starts from (after upload39)."""

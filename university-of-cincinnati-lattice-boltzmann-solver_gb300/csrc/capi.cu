@@ -485,6 +485,39 @@ int finish_stats(elbm_ctx* c, elbm_stats* out) {
   return ELBM_OK;
 }
 
+// The level's scalars in the form the D3Q39 kernels read.
+D3Q39Dev dev39(const elbm_d3q39_params& p, const Level& lv) {
+  D3Q39Dev k{};
+  k.shifted = p.shifted;
+  k.primary_flow_dir = p.primary_flow_dir;
+  k.turbulent = p.turbulent;
+  k.lvl = p.lvl;
+  k.startup_timesteps = p.startup_timesteps;
+  k.max_lm_iters = p.max_lm_iters;
+  k.gama = p.gama;
+  k.t_ref = p.t_ref;
+  k.rho_ref = p.rho_ref;
+  k.p_ref = p.p_ref;
+  k.mu_ref = p.mu_ref;
+  k.kappa_ref = p.kappa_ref;
+  k.gas_const_R = p.gas_const_R;
+  k.const_vol = p.const_vol;
+  k.const_press = p.const_press;
+  k.molec_weight = p.molec_weight;
+  k.dt = p.dt;
+  k.elbm_epsilon = p.elbm_epsilon;
+  k.init_beta_1 = p.init_beta_1;
+  k.init_beta_2 = p.init_beta_2;
+  k.beta_1_scaling = p.beta_1_scaling;
+  k.beta_2_scaling = p.beta_2_scaling;
+  for (int r = 0; r < 13; ++r) k.su_lm[r] = p.su_lm[r];
+  k.fs_u = lv.fs39[0];
+  k.fs_v = lv.fs39[1];
+  k.fs_w = lv.fs39[2];
+  k.fs_temp = lv.fs39[3];
+  return k;
+}
+
 // D3Q39 level steps: fused stream/flow-variables/collision, then the optional repair.
 int step39(elbm_ctx* c, Level& lv, int nsteps) {
   const elbm_d3q39_params& p = lv.p39;
@@ -532,34 +565,7 @@ int step39(elbm_ctx* c, Level& lv, int nsteps) {
         a.wallf = b.wallf39.p;
         a.wallg = b.wallg39.p;
       }
-      D3Q39Dev& k = a.k;
-      k.shifted = p.shifted;
-      k.primary_flow_dir = p.primary_flow_dir;
-      k.turbulent = p.turbulent;
-      k.lvl = p.lvl;
-      k.startup_timesteps = p.startup_timesteps;
-      k.max_lm_iters = p.max_lm_iters;
-      k.gama = p.gama;
-      k.t_ref = p.t_ref;
-      k.rho_ref = p.rho_ref;
-      k.p_ref = p.p_ref;
-      k.mu_ref = p.mu_ref;
-      k.kappa_ref = p.kappa_ref;
-      k.gas_const_R = p.gas_const_R;
-      k.const_vol = p.const_vol;
-      k.const_press = p.const_press;
-      k.molec_weight = p.molec_weight;
-      k.dt = p.dt;
-      k.elbm_epsilon = p.elbm_epsilon;
-      k.init_beta_1 = p.init_beta_1;
-      k.init_beta_2 = p.init_beta_2;
-      k.beta_1_scaling = p.beta_1_scaling;
-      k.beta_2_scaling = p.beta_2_scaling;
-      for (int r = 0; r < 13; ++r) k.su_lm[r] = p.su_lm[r];
-      k.fs_u = lv.fs39[0];
-      k.fs_v = lv.fs39[1];
-      k.fs_w = lv.fs39[2];
-      k.fs_temp = lv.fs39[3];
+      a.k = dev39(p, lv);
       if (a.nwall > 0) {
         launch_d3q39_walls(a, c->stream);
         CUDA_TRY(cudaGetLastError(), "d3q39 wall launch");
@@ -1544,6 +1550,89 @@ int elbm_upload_level39(elbm_ctx* c, int lvl, int box, const double* fout, const
   b->gcur = 0;
   b->data_set = true;
   b->macro_set = false;
+  return ELBM_OK;
+}
+
+int elbm_init_level39(elbm_ctx* c, int lvl, int box, const double* macro, const double* lm_start,
+                      int64_t* capped) {
+  Level* lv = nullptr;
+  Box* b = get_box(c, lvl, box, &lv);
+  if (!b || !macro || !lm_start) return fail(c, ELBM_E_ARG, "unknown level/box or null data");
+  if (lv->lattice != ELBM_D3Q39) return fail(c, ELBM_E_ARG, "not a D3Q39 level");
+  if (!lv->params_set) return fail(c, ELBM_E_STATE, "set the level parameters first");
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  CUDA_TRY(fab_to_packed(macro, b->macro.p, *b, lv->ngrow, 5, b->plane, c->stream), "upload macro");
+  DevBuf<double> lm0;
+  DevBuf<unsigned long long> cnt;
+  CUDA_TRY(lm0.alloc(13), "start multipliers");
+  CUDA_TRY(cnt.alloc(1), "counter");
+  CUDA_TRY(cudaMemcpyAsync(lm0.p, lm_start, 13 * sizeof(double), cudaMemcpyHostToDevice, c->stream), "lm start");
+  CUDA_TRY(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned long long), c->stream), "counter");
+  Step39Args a{};
+  a.fdst = (double*)b->buf[0].p;
+  a.gdst = (double*)b->gbuf[0].p;
+  a.lm = b->lm.p;
+  a.w_vel = b->w_vel.p;
+  a.macro = b->macro.p;
+  a.plane = b->plane;
+  a.nx = b->nx;
+  a.ny = b->ny;
+  a.nz = b->nz;
+  a.N = b->N;
+  a.k = dev39(lv->p39, *lv);
+  launch_d3q39_init(a, lm0.p, cnt.p, c->stream);
+  CUDA_TRY(cudaGetLastError(), "init launch");
+  CUDA_TRY(cudaMemsetAsync(b->alpha64.p, 0, b->alpha64.n * sizeof(double), c->stream), "alpha");
+  b->cur = 0;
+  b->gcur = 0;
+  if (b->links39) launch_stale39_init(*b, c->stream);
+  unsigned long long h = 0;
+  CUDA_TRY(cudaMemcpyAsync(&h, cnt.p, sizeof h, cudaMemcpyDeviceToHost, c->stream), "counter");
+  CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  if (capped) *capped = (int64_t)h;
+  b->data_set = true;
+  b->macro_set = true;
+  return ELBM_OK;
+}
+
+int elbm_d3q39_equilibrium(elbm_ctx* c, const elbm_d3q39_params* p, const double* macro, double* lm,
+                           double* fieq, double* gieq) {
+  if (!c || !p || !macro || !lm || !fieq || !gieq) return fail(c, ELBM_E_ARG, "null argument");
+  if (p->primary_flow_dir < 1 || p->primary_flow_dir > 6 || p->max_lm_iters < 1)
+    return fail(c, ELBM_E_ARG, "bad D3Q39 parameters");
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  Lattice39 L;
+  build_lattice39(p->shifted, p->primary_flow_dir, L);
+  upload_lattice39(L, c->stream);
+  // one node: macro (5), lm (13), f, g (39 each), w, counter
+  DevBuf<double> buf;
+  DevBuf<unsigned long long> cnt;
+  CUDA_TRY(buf.alloc(5 + 13 + 13 + 39 + 39 + 1), "scratch");
+  CUDA_TRY(cnt.alloc(1), "counter");
+  double* d = buf.p;
+  CUDA_TRY(cudaMemcpyAsync(d, macro, 5 * sizeof(double), cudaMemcpyHostToDevice, c->stream), "macro");
+  CUDA_TRY(cudaMemcpyAsync(d + 5, lm, 13 * sizeof(double), cudaMemcpyHostToDevice, c->stream), "lm");
+  CUDA_TRY(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned long long), c->stream), "counter");
+  Level none;
+  Step39Args a{};
+  a.macro = d;
+  a.lm = d + 18;
+  a.fdst = d + 31;
+  a.gdst = d + 70;
+  a.w_vel = d + 109;
+  a.plane = 1;
+  a.nx = a.ny = a.nz = 1;
+  a.N = 1;
+  a.k = dev39(*p, none);
+  launch_d3q39_init(a, d + 5, cnt.p, c->stream);
+  CUDA_TRY(cudaGetLastError(), "init launch");
+  unsigned long long h = 0;
+  CUDA_TRY(cudaMemcpyAsync(lm, d + 18, 13 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "lm");
+  CUDA_TRY(cudaMemcpyAsync(fieq, d + 31, 39 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "fieq");
+  CUDA_TRY(cudaMemcpyAsync(gieq, d + 70, 39 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "gieq");
+  CUDA_TRY(cudaMemcpyAsync(&h, cnt.p, sizeof h, cudaMemcpyDeviceToHost, c->stream), "counter");
+  CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  if (h) return fail(c, ELBM_E_NUMERIC, "the multiplier Newton did not converge within max_lm_iters");
   return ELBM_OK;
 }
 

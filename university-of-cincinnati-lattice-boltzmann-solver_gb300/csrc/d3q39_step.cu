@@ -663,6 +663,34 @@ __global__ void __launch_bounds__(64) d3q39_wall_kernel(const Step39Args a) {
   if (flags) atomicOr(&a.stats->status, flags);
 }
 
+// Initial state of every node from its macroscopic fields
+// (multilevel_initialization.f90:229-278 with the freestream multipliers of
+// freestream_basis_calcs.f90:24-90 as the start): the multiplier Newton for
+// rho, u, T and the equilibrium pressure tensor, then f = f_eq,
+// g = (2 C_v - D) T f_eq, and the multipliers, w and the fields stored.
+__global__ void __launch_bounds__(64) d3q39_init_kernel(const Step39Args a, const double* __restrict__ lm0,
+                                                        unsigned long long* capped) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= a.N) return;
+  const D3Q39Dev& k = a.k;
+  const double rho = a.macro[n], u = a.macro[a.plane + n], v = a.macro[2 * a.plane + n],
+               w = a.macro[3 * a.plane + n], T = a.macro[4 * a.plane + n];
+  double lm[NL];
+  for (int r = 0; r < NL; ++r) lm[r] = lm0[r];
+  const double P[6] = {rho * (T + u * u), rho * (T + v * v), rho * (T + w * w), rho * u * v, rho * u * w, rho * v * w};
+  double fe[Q];
+  const int it = lagrange39(k.max_lm_iters, rho, u, v, w, T, P, lm, fe);
+  if (it < 0) atomicAdd(capped, 1ull);
+  const double lead = (2 * k.const_vol - 3) * T;
+  for (int i = 0; i < Q; ++i) {
+    const double f = fieq39(rho, lm, i);
+    a.fdst[(int64_t)i * a.plane + n] = f;
+    a.gdst[(int64_t)i * a.plane + n] = f * lead;
+  }
+  for (int r = 0; r < NL; ++r) a.lm[(int64_t)r * a.plane + n] = lm[r];
+  a.w_vel[n] = w;
+}
+
 // damp_it.f95:64-177 for fout on a periodic box: a negative population takes
 // the mean of its +-c_i neighbours when both are positive, else the mean of
 // the positive one and its own magnitude, else its magnitude.  Neighbours are
@@ -699,6 +727,11 @@ void launch_d3q39_fp64(const Step39Args& a, cudaStream_t s) {
   const int threads = 64;
   const int64_t blocks = (a.N + threads - 1) / threads;
   d3q39_fp64_kernel<<<(unsigned)blocks, threads, 0, s>>>(a);
+}
+
+void launch_d3q39_init(const Step39Args& a, const double* lm0, unsigned long long* capped, cudaStream_t s) {
+  const int threads = 64;
+  d3q39_init_kernel<<<(unsigned)((a.N + threads - 1) / threads), threads, 0, s>>>(a, lm0, capped);
 }
 
 void launch_d3q39_walls(const Step39Args& a, cudaStream_t s) {

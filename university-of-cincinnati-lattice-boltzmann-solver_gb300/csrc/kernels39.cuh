@@ -85,6 +85,7 @@ void build_lattice39(int shifted, int primary_flow_dir, Lattice39& L);
 void upload_lattice39(const Lattice39& L, cudaStream_t s);
 void launch_d3q39_fp64(const Step39Args& a, cudaStream_t s);
 void launch_d3q39_walls(const Step39Args& a, cudaStream_t s);
+void launch_d3q39_init(const Step39Args& a, const double* lm0, unsigned long long* capped, cudaStream_t s);
 void launch_d3q39_damp(const double* src, double* dst, int nx, int ny, int nz, int64_t plane, DevStats* stats,
                        cudaStream_t s);
 

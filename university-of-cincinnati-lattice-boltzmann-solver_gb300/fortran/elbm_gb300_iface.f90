@@ -59,7 +59,8 @@ module elbm_gb300_iface
     elbm_set_d3q39_params, elbm_upload_level39, elbm_download_level39, elbm_mark_triangles, &
     elbm_upload_level_noalloc, elbm_autotune, elbm_set_kernel_variant, elbm_alpha_harvest, &
     elbm_alpha_mlp_train, elbm_set_alpha_mlp, elbm_interlevel_setup, elbm_fill_fine_ghosts, &
-    elbm_average_down, elbm_amr_run, elbm_damp_level, elbm_set_links39, elbm_upload_macro39
+    elbm_average_down, elbm_amr_run, elbm_damp_level, elbm_set_links39, elbm_upload_macro39, &
+    elbm_init_level39, elbm_d3q39_equilibrium
 
   interface
     integer(c_int) function elbm_create(device, ctx) bind(c, name="elbm_create")
@@ -130,6 +131,23 @@ module elbm_gb300_iface
       type(c_ptr), value :: ctx
       integer(c_int), value :: lvl, box
       real(c_double), intent(in) :: fout(*), gout(*), lm(*), w_vel(*)
+    end function
+    integer(c_int) function elbm_init_level39(ctx, lvl, box, macro, lm_start, capped) &
+        bind(c, name="elbm_init_level39")
+      import :: c_int, c_ptr, c_double, c_int64_t
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl, box
+      real(c_double), intent(in) :: macro(*), lm_start(13)
+      integer(c_int64_t), intent(out) :: capped
+    end function
+    integer(c_int) function elbm_d3q39_equilibrium(ctx, p, macro, lm, fieq, gieq) &
+        bind(c, name="elbm_d3q39_equilibrium")
+      import :: c_int, c_ptr, c_double, elbm_d3q39_params
+      type(c_ptr), value :: ctx
+      type(elbm_d3q39_params), intent(in) :: p
+      real(c_double), intent(in) :: macro(5)
+      real(c_double), intent(inout) :: lm(13)
+      real(c_double), intent(out) :: fieq(39), gieq(39)
     end function
     integer(c_int) function elbm_upload_macro39(ctx, lvl, box, macro) bind(c, name="elbm_upload_macro39")
       import :: c_int, c_ptr, c_double
