@@ -25,8 +25,33 @@ namespace elbm {
 
 __constant__ Lattice39 c39;
 
+// The integer tables as doubles (exact), so that the FP64 sums multiply by a
+// constant operand instead of converting an integer in every term: the 13
+// moment monomials, their 91 pairwise products (the Jacobian, r <= c row by
+// row) and the third-moment tables of q-bar.
+struct Lattice39D {
+  double phi[13][39];
+  double pp[91][39];
+  double yi[27][39];
+  double kr[27][39];
+};
+__constant__ Lattice39D c39d;
+
 void upload_lattice39(const Lattice39& L, cudaStream_t s) {
   cudaMemcpyToSymbolAsync(c39, &L, sizeof(L), 0, cudaMemcpyHostToDevice, s);
+  static Lattice39D D;  // host staging (pageable: the copy completes before the call returns)
+  int k = 0;
+  for (int r = 0; r < 13; ++r) {
+    for (int i = 0; i < 39; ++i) D.phi[r][i] = (double)L.phi[r][i];
+    for (int c = r; c < 13; ++c, ++k)
+      for (int i = 0; i < 39; ++i) D.pp[k][i] = (double)(L.phi[r][i] * L.phi[c][i]);
+  }
+  for (int m = 0; m < 27; ++m)
+    for (int i = 0; i < 39; ++i) {
+      D.yi[m][i] = (double)L.yi[m][i];
+      D.kr[m][i] = (double)L.kroen[m][i];
+    }
+  cudaMemcpyToSymbolAsync(c39d, &D, sizeof(D), 0, cudaMemcpyHostToDevice, s);
 }
 
 namespace {
@@ -36,10 +61,10 @@ constexpr int NL = 13;
 
 __device__ __forceinline__ double fieq39(double rho, const double (&lm)[NL], int i) {
   // amr_processes.f95:1729-1747, left-to-right sum of integer-weighted multipliers
-  return rho * exp(lm[0] + c39.cx[i] * lm[1] + c39.cy[i] * lm[2] + c39.cz[i] * lm[3] + c39.phi[4][i] * lm[4] +
-                   c39.phi[5][i] * lm[5] + c39.phi[6][i] * lm[6] + c39.phi[7][i] * lm[7] + c39.phi[8][i] * lm[8] +
-                   c39.phi[9][i] * lm[9] + c39.phi[10][i] * lm[10] + c39.phi[11][i] * lm[11] +
-                   c39.phi[12][i] * lm[12]);
+  return rho * exp(lm[0] + c39d.phi[1][i] * lm[1] + c39d.phi[2][i] * lm[2] + c39d.phi[3][i] * lm[3] +
+                   c39d.phi[4][i] * lm[4] + c39d.phi[5][i] * lm[5] + c39d.phi[6][i] * lm[6] +
+                   c39d.phi[7][i] * lm[7] + c39d.phi[8][i] * lm[8] + c39d.phi[9][i] * lm[9] +
+                   c39d.phi[10][i] * lm[10] + c39d.phi[11][i] * lm[11] + c39d.phi[12][i] * lm[12]);
 }
 
 // lu_decomp.f95: LU of J (row-major 13x13, overwritten), substitution,
@@ -101,10 +126,11 @@ __device__ int lagrange39(int max_it, double rho, double u, double v, double w, 
     if (it >= max_it) return -it;
     ++it;
     for (int i = 0; i < Q; ++i) fieq[i] = fieq39(rho, lm, i);
+    int k = 0;
     for (int r = 0; r < NL; ++r)
-      for (int c = r; c < NL; ++c) {
+      for (int c = r; c < NL; ++c, ++k) {
         double s = 0.0;
-        for (int i = 0; i < Q; ++i) s += (double)(c39.phi[r][i] * c39.phi[c][i]) * fieq[i];
+        for (int i = 0; i < Q; ++i) s += c39d.pp[k][i] * fieq[i];
         J[r * NL + c] = s;
         J[c * NL + r] = s;
       }
@@ -344,8 +370,8 @@ __global__ void __launch_bounds__(64) d3q39_fp64_kernel(const Step39Args a) {
   bool neg = false;
   for (int i = 0; i < Q; ++i) {
     double sy = 0.0, sk = 0.0;
-    for (int mm = 0; mm < 27; ++mm) sy = sy + m[qmap[mm]] * (double)c39.yi[mm][i];
-    for (int mm = 0; mm < 27; ++mm) sk = sk + m[qmap[mm]] * (double)c39.kroen[mm][i];
+    for (int mm = 0; mm < 27; ++mm) sy = sy + m[qmap[mm]] * c39d.yi[mm][i];
+    for (int mm = 0; mm < 27; ++mm) sk = sk + m[qmap[mm]] * c39d.kr[mm][i];
     const double qb = eps * (sy - 3 * temp * sk) / temp_coeff;
     const double ch = q_lead * (c39.cx[i] * q1 + c39.cy[i] * q2 + c39.cz[i] * q3);
     const double fo = f[i] + alpha * b1 * (fd[i] - qb) + b2 * qb;
