@@ -202,8 +202,11 @@ typedef struct {
  * push nor collide; state >= 0 must be fluid (outside 200..298 and
  * 1000..50999); nodes outside the box on a non-periodic axis count as null
  * nodes (-666), as lbgrid/fluid_or_solid.f95:69-119 marks them for an
- * external flow.  The negative-population repair (damp = 1) is not available
- * with link codes. */
+ * external flow.  With damp = 1 the fout part of damp_it.f95 follows every
+ * step with the rules for boundary links (unshifted: interior links select
+ * the neighbours; shifted: the band near the box's high faces and the node
+ * types >= -500); its fi part, which only matters for slots no rule writes,
+ * is not applied. */
 int elbm_set_links39(elbm_ctx* ctx, int lvl, int box, const int32_t* state, int ngrow_state,
                      const elbm_d3q39_bc* bc);
 

@@ -343,6 +343,9 @@ typedef struct {
 
 static inline int64_t idx3(int x, int y, int z, int nx, int ny) { return ((int64_t)z * ny + y) * nx + x; }
 static inline int wrap(int a, int n) { return ((a % n) + n) % n; }
+static int64_t nb39(int x, int y, int z, int nx, int ny, int nz, int periodic);
+static int64_t damp39_links(const o39_consts* k, const o39_lattice* L, double* fo, const int32_t* state, int nx,
+                            int ny, int nz, int periodic, const int* lo, const int* hi, const double* fs_fieq);
 
 /* calculate_flow_variables.f95:192-311 and collision.f95:153-300 for every
  * node (state == NULL) or every fluid node (state[0] of the node >= 0, outside
@@ -463,31 +466,12 @@ int o39_step_periodic(const o39_consts* k, o39_level* s, int step, o39_stats* st
         }
   int64_t lm_iters = 0, capped = 0, not2 = 0;
   collide39(k, &L, s, fi, gi, step, NULL, &lm_iters, &capped, &not2);
-  /* damp_it.f95:64-177, fout part: a negative population is replaced by the
-   * mean of its neighbours along +-c_i when both are positive (interior links). */
-  int64_t damped = 0;
-  for (int i = 0; i < Q; ++i)
-    for (int z = 0; z < nz; ++z)
-      for (int y = 0; y < ny; ++y)
-        for (int x = 0; x < nx; ++x) {
-          const int64_t n = idx3(x, y, z, nx, ny);
-          double* fo = s->fout + (int64_t)i * N;
-          if (!(fo[n] < 0.0)) continue;
-          damped++;
-          const double fp = fo[idx3(wrap(x + L.cx[i], nx), wrap(y + L.cy[i], ny), wrap(z + L.cz[i], nz), nx, ny)];
-          const double fm = fo[idx3(wrap(x - L.cx[i], nx), wrap(y - L.cy[i], ny), wrap(z - L.cz[i], nz), nx, ny)];
-          if (!k->shifted) {
-            if (fp > 0.0 && fm > 0.0) fo[n] = (fp + fm) / 2.0;
-            else if (fp > 0.0 && fm < 0.0) fo[n] = (fp + fabs(fo[n])) / 2;
-            else if (fp < 0.0 && fm > 0.0) fo[n] = (fm + fabs(fo[n])) / 2;
-            else fo[n] = fabs(fo[n]);
-          } else {
-            if (fp > 0.0 && fm > 0.0) fo[n] = (fp + fm) / 2.0;
-            else if (fp > 0.0 && fm < 0.0) fo[n] = (fp + fabs(fo[n])) / 2;
-            else if (fp < 0.0 && fm > 0.0) fo[n] = (fm + fabs(fo[n])) / 2;
-            else fo[n] = fabs(fo[n]);
-          }
-        }
+  /* damp_it.f95:64-177, fout part (damp39_links with every link interior; the box at the origin) */
+  int32_t* zst = (int32_t*)calloc((size_t)Q * N, sizeof(int32_t));
+  if (!zst) return -100;
+  const int lo[3] = {0, 0, 0}, hi[3] = {nx - 1, ny - 1, nz - 1};
+  const int64_t damped = damp39_links(k, &L, s->fout, zst, nx, ny, nz, 7, lo, hi, NULL);
+  free(zst);
   st->nodes = N;
   st->lm_iters = lm_iters;
   st->lm_capped = capped;
@@ -791,6 +775,78 @@ static int64_t nb39(int x, int y, int z, int nx, int ny, int nz, int periodic) {
   if (periodic & 2) y = wrap(y, ny); else if (y < 0 || y >= ny) return -1;
   if (periodic & 4) z = wrap(z, nz); else if (z < 0 || z >= nz) return -1;
   return idx3(x, y, z, nx, ny);
+}
+
+/* damp_it.f95:64-177, fout part, on a box with link codes, in the reference's
+ * in-place sweep (direction outermost, then z, y, x).  lo, hi: the box in the
+ * level's index space.  Unshifted lattice: the neighbours x +- c_i enter when
+ * the links i / opp(i) of the node are interior (state >= 0).  Shifted: nodes
+ * whose x + c_i or y + c_y, z + c_z come within nghosts_mid = 8 of the box's
+ * high faces (the reference's band test, its a - cx(i) < lo(2) - nghosts_mid
+ * included) take (fout(x + c_i) + |fout|) / 2 when link i is >= -500;
+ * elsewhere the link and the node type of x - c_i (>= -500) select the
+ * neighbours, and a population with neither keeps its value.  Outside the box
+ * on a non-periodic axis a node type is -666 and fout the freestream
+ * equilibrium (the initial value of the nodes outside an external-flow domain,
+ * multilevel_initialization.f90:185-268, which never collide).  nghosts_mid is
+ * 8 for D3Q39: directions_and_weights.f95:355-362 sets it before the same
+ * routine sets shifted (:479). */
+static int64_t damp39_links(const o39_consts* k, const o39_lattice* L, double* fo, const int32_t* state, int nx,
+                            int ny, int nz, int periodic, const int* lo, const int* hi, const double* fs_fieq) {
+  const int64_t N = (int64_t)nx * ny * nz;
+  const int ngm = 8;
+  int64_t damped = 0;
+  for (int i = 0; i < Q; ++i)
+    for (int z = 0; z < nz; ++z)
+      for (int y = 0; y < ny; ++y)
+        for (int x = 0; x < nx; ++x) {
+          const int64_t n = idx3(x, y, z, nx, ny);
+          double* f = fo + (int64_t)i * N;
+          const double v = f[n];
+          if (!(v < 0.0)) continue;
+          damped++;
+          const int64_t mp = nb39(x + L->cx[i], y + L->cy[i], z + L->cz[i], nx, ny, nz, periodic);
+          const int64_t mm = nb39(x - L->cx[i], y - L->cy[i], z - L->cz[i], nx, ny, nz, periodic);
+          const double fp = mp >= 0 ? f[mp] : fs_fieq[i];
+          const double fmv = mm >= 0 ? f[mm] : fs_fieq[i];
+          const int32_t si = i == 0 ? state[n] : state[(int64_t)i * N + n];
+          if (!k->shifted) {
+            const int oi = L->opp[i];
+            const int32_t so = oi == 0 ? state[n] : state[(int64_t)oi * N + n];
+            if (si >= 0 && so >= 0) {
+              if (fp > 0.0 && fmv > 0.0) f[n] = (fp + fmv) / 2.0;
+              else if (fp > 0.0 && fmv < 0.0) f[n] = (fp + fabs(v)) / 2;
+              else if (fp < 0.0 && fmv > 0.0) f[n] = (fmv + fabs(v)) / 2;
+              else f[n] = fabs(v);
+            } else if (si >= 0 && so < 0) {
+              f[n] = fp > 0.0 ? (fp + fabs(v)) / 2 : fabs(v);
+            } else if (si < 0 && so >= 0) {
+              f[n] = fmv > 0.0 ? (fmv + fabs(v)) / 2 : fabs(v);
+            } else {
+              f[n] = fabs(v);
+            }
+            continue;
+          }
+          const int a = lo[0] + x, b = lo[1] + y, c = lo[2] + z;
+          const int edge = a - L->cx[i] < lo[0] - ngm || a - L->cx[i] < lo[1] - ngm || c - L->cz[i] < lo[2] - ngm ||
+                           a + L->cx[i] > hi[0] - ngm || b + L->cy[i] > hi[1] - ngm || c + L->cz[i] > hi[2] - ngm;
+          if (edge) {
+            f[n] = si >= -500 ? (fp + fabs(v)) / 2 : fabs(v);
+            continue;
+          }
+          const int32_t up = mm >= 0 ? state[mm] : -666;
+          if (si >= -500 && up >= -500) {
+            if (fp > 0.0 && fmv > 0.0) f[n] = (fp + fmv) / 2.0;
+            else if (fp > 0.0 && fmv < 0.0) f[n] = (fp + fabs(v)) / 2;
+            else if (fp < 0.0 && fmv > 0.0) f[n] = (fmv + fabs(v)) / 2;
+            else f[n] = fabs(v);
+          } else if (si >= -500 && up < -500) {
+            f[n] = fp > 0.0 ? (fp + fabs(v)) / 2 : fabs(v);
+          } else if (si < -500 && up >= -500) {
+            f[n] = fmv > 0.0 ? (fmv + fabs(v)) / 2 : fabs(v);
+          }
+        }
+  return damped;
 }
 
 /* Wall link i of fluid node n at (x, y, z) during the push loop: the value
@@ -1109,4 +1165,18 @@ void o39_tables(int shifted, int primary_flow_dir, int* cx, int* cy, int* cz, in
 int o39_ibb_wall_axis(int i, int axis, int* up) {
   *up = 0;
   return ibb_wall_axis(i, axis, up);
+}
+
+/* o39_step_links followed by the fout part of damp_it.f95 on the box (see
+ * damp39_links); lo, hi: the box in the level's index space.  st->damped
+ * counts the repaired populations. */
+int o39_step_links_damp(const o39_consts* k, o39_level* s, int step, o39_stats* st, const int32_t* state,
+                        int periodic, const o39_bc* bc, double* fi_prev, double* gi_prev, const int* lo,
+                        const int* hi) {
+  const int rc = o39_step_links(k, s, step, st, state, periodic, bc, fi_prev, gi_prev);
+  if (rc) return rc;
+  o39_lattice L;
+  o39_lattice_init(&L, k->shifted, k->primary_flow_dir);
+  st->damped = damp39_links(k, &L, s->fout, state, s->nx, s->ny, s->nz, periodic, lo, hi, bc->fs_fieq);
+  return 0;
 }

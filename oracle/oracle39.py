@@ -212,3 +212,25 @@ def inviscid(i, codes):
     d = np.zeros(3, np.int32)
     ok = L.o39_inviscid(i, _p(c), ct.byref(j), _p(d))
     return bool(ok), j.value, tuple(int(x) for x in d)
+
+
+def step_links_damp(k: O39Consts, lev: Level39, step: int, state: np.ndarray, periodic: int, b: O39Bc,
+                    fi_prev: np.ndarray, gi_prev: np.ndarray, lo, hi):
+    """step_links, then the fout part of damp_it on the box (lo, hi: its index-space corners)."""
+    L = lib()
+    if not getattr(L, "_o39_damp_ready", False):
+        L.o39_step_links_damp.restype = ct.c_int
+        L.o39_step_links_damp.argtypes = [ct.POINTER(O39Consts), ct.POINTER(O39Level), ct.c_int,
+                                          ct.POINTER(O39Stats), ct.c_void_p, ct.c_int, ct.POINTER(O39Bc),
+                                          ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p]
+        L._o39_damp_ready = True
+    st = O39Stats()
+    s = lev.c()
+    stc = np.ascontiguousarray(state, np.int32)
+    lo_a = np.ascontiguousarray(lo, np.int32)
+    hi_a = np.ascontiguousarray(hi, np.int32)
+    rc = L.o39_step_links_damp(ct.byref(k), ct.byref(s), step, ct.byref(st), _p(stc), periodic, ct.byref(b),
+                               _p(fi_prev), _p(gi_prev), _p(lo_a), _p(hi_a))
+    if rc != 0:
+        raise RuntimeError(f"o39 link step failed {rc}")
+    return {n: getattr(st, n) for n, _ in st._fields_}

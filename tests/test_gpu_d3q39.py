@@ -274,3 +274,52 @@ def test_d3q39_initial_state_on_device(pkg, o39, built_lib):
         lm_r, f_r, g_r, _ = o39.init_node(k, 1.0, c.mach, 0.0, 0.0, c.temperature, lm0)
         assert np.max(np.abs(f_e - f_r) / f_r) <= 1e-12 and np.max(np.abs(g_e - g_r) / g_r) <= 1e-12
         ctx.close()
+
+
+@pytest.mark.parametrize("shifted", [0, 1])
+def test_d3q39_repair_with_link_codes(pkg, o39, built_lib, shifted):
+    """The fout part of damp_it.f95 after the step on a box with link codes (inlet, outlet,
+    bounce-back floor, freestream top, periodic span), past the start-up ramps: a few
+    populations are inflated so that the over-relaxed collision drives isolated neighbours
+    negative; GPU against the oracle's in-place sweep, 1e-12 relative."""
+    setup39, cap = pkg.d3q39_setup, pkg.capi
+    mach = 1.5 if shifted else 0.3
+    c = setup39.wedge_case_consts(v_inf_ms=mach * math.sqrt(1.4 * setup39.GAS_CONST_R * 288.15))
+    k = o39.consts(c)
+    lm0 = setup39.freestream_start_lm(c)
+    _, ff, gf, _ = o39.init_node(k, 1.0, c.mach, 0.0, 0.0, c.temperature, lm0)
+    nx, ny, nz, periodic = 20, 6, 14, 2
+    faces = {"x-": -101, "x+": -201, "z-": -10, "z+": -1000, "y-": 0, "y+": 0}
+    st = setup39.box_state39(nx, ny, nz, faces, shifted, 1, periodic=periodic)
+    lev = _init(o39, setup39, c, k, nx, ny, nz, noise=0.005, seed=31 + shifted)
+    rng = np.random.default_rng(7 + shifted)
+    # inflate one population at isolated nodes (every fourth node along x and z)
+    picks = [(int(i), int(z), int(y), int(x)) for i, z, y, x in zip(
+        rng.integers(1, 39, 6), [2, 5, 9, 12, 3, 10], rng.integers(0, ny, 6), [2, 6, 10, 14, 17, 8])]
+    for i, z, y, x in picks:
+        lev.fout[i, z, y, x] *= 6.0
+        lev.gout[i, z, y, x] *= 6.0
+    bc_args = ([1] * 8, [6] + [1] * 7, ff, gf, [ff] * 8, [gf] * 8, [ff] * 8, [gf] * 8,
+               (c.mach, 0.0, 0.0, c.temperature))
+    ctx = cap.Context(0)
+    lo, hi = (0, 0, 0), (nx - 1, ny - 1, nz - 1)
+    ctx.level_register(0, cap.ELBM_D3Q39, cap.ELBM_STORE_FP64, [list(lo) + list(hi)])
+    start = 150
+    ctx.set_d3q39_params(0, cap.make_d3q39_params(c, timestep=start, periodic=periodic, damp=1))
+    ctx.set_links39(0, 0, st, cap.make_d3q39_bc(*bc_args))
+    ctx.upload39(0, 0, lev.fout, lev.gout, lev.lm, lev.w_vel)
+    steps = 2
+    s = ctx.step(0, steps)
+    out = ctx.download39(0)
+    prev_f, prev_g = lev.fout.copy(), lev.gout.copy()
+    b = o39.bc(*bc_args)
+    damped = 0
+    for step in range(start, start + steps):
+        so = o39.step_links_damp(k, lev, step, st, periodic, b, prev_f, prev_g, lo, hi)
+        damped += so["damped"]
+    assert damped > 0 and s["exact_path_nodes"] == damped
+    fluid = st[0] >= 0
+    for name, ref in (("fout", lev.fout), ("gout", lev.gout)):
+        rel = np.max(np.abs(out[name][:, fluid] - ref[:, fluid]) / np.abs(ref[:, fluid]))
+        assert rel <= 1e-12, (name, rel)
+    assert (out["fout"][:, fluid] >= 0).all()

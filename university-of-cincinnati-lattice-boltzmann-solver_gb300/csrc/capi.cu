@@ -99,6 +99,7 @@ struct Box {
   DevBuf<int32_t> recwall39;
   DevBuf<double> wallf39, wallg39;
   int64_t nwall39 = 0;
+  DevBuf<unsigned long long> dmask39;  // link classes of the repair, per node
   bool macro_set = false;  // elbm_upload_macro39 since the last elbm_upload_level39
   int64_t fluid_nodes = 0, boundary_nodes = 0;
   bool links_set = false, data_set = false;
@@ -525,8 +526,6 @@ int step39(elbm_ctx* c, Level& lv, int nsteps) {
     if (!bp->data_set) return fail(c, ELBM_E_STATE, "populations missing");
     if (!bp->links39 && p.periodic != 7)
       return fail(c, ELBM_E_STATE, "a D3Q39 box that is not periodic on every axis needs elbm_set_links39");
-    if (bp->links39 && p.damp)
-      return fail(c, ELBM_E_UNSUPPORTED, "the negative-population repair is not available with D3Q39 link codes");
     if (bp->nwall39 > 0 && !bp->macro_set)
       return fail(c, ELBM_E_STATE, "interpolated wall links need the macroscopic fields (elbm_upload_macro39)");
   }
@@ -575,8 +574,10 @@ int step39(elbm_ctx* c, Level& lv, int nsteps) {
       b.cur ^= 1;
       b.gcur ^= 1;
       if (p.damp) {
-        launch_d3q39_damp((const double*)b.buf[b.cur].p, (double*)b.buf[b.cur ^ 1].p, b.nx, b.ny, b.nz, b.plane,
-                          c->stats.p, c->stream);
+        // damp_it.f95:64-177 (fout part) on the new state; a box without link codes is periodic on every axis
+        launch_d3q39_damp_links((const double*)b.buf[b.cur].p, (double*)b.buf[b.cur ^ 1].p,
+                                b.links39 ? b.dmask39.p : nullptr, b.nx, b.ny, b.nz, b.plane, p.periodic, p.shifted,
+                                b.lo, b.hi, b.links39 ? lv.eq39f.p : nullptr, c->stats.p, c->stream);
         CUDA_TRY(cudaGetLastError(), "d3q39 damp launch");
         b.cur ^= 1;
       }
@@ -1508,6 +1509,8 @@ int elbm_set_links39(elbm_ctx* c, int lvl, int box, const int32_t* state, int ng
     CUDA_TRY(cudaMemcpy(b->words39.p, L.words.data(), L.words.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
              "link words");
   }
+  CUDA_TRY(b->dmask39.alloc(b->N), "repair classes");
+  CUDA_TRY(cudaMemcpy(b->dmask39.p, L.dmask.data(), b->N * sizeof(uint64_t), cudaMemcpyHostToDevice), "repair classes");
   b->nwall39 = (int64_t)L.walls.size();
   const size_t nw = std::max<size_t>(L.walls.size(), 1);
   CUDA_TRY(b->recwall39.alloc(nr), "wall map");

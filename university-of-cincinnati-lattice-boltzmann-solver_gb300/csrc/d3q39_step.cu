@@ -717,42 +717,112 @@ __global__ void __launch_bounds__(64) d3q39_init_kernel(const Step39Args a, cons
   a.w_vel[n] = w;
 }
 
-// damp_it.f95:64-177 for fout on a periodic box: a negative population takes
-// the mean of its +-c_i neighbours when both are positive, else the mean of
-// the positive one and its own magnitude, else its magnitude.  Neighbours are
-// read from the undamped field (identical to the reference's in-place sweep
-// unless two negative populations of one direction are adjacent along c_i).
-__global__ void d3q39_damp_kernel(const double* __restrict__ src, double* __restrict__ dst, int nx, int ny, int nz,
-                                  int64_t plane, DevStats* stats) {
-  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = blockIdx.y;
-  const int64_t N = (int64_t)nx * ny * nz;
-  if (n >= N) return;
-  const double v = src[(int64_t)i * plane + n];
-  double out = v;
-  if (v < 0.0) {
-    const int x = (int)(n % nx), y = (int)((n / nx) % ny), z = (int)(n / ((int64_t)nx * ny));
-    auto at = [&](int s) {
-      const int xx = ((x + s * c39.cx[i]) % nx + nx) % nx, yy = ((y + s * c39.cy[i]) % ny + ny) % ny,
-                zz = ((z + s * c39.cz[i]) % nz + nz) % nz;
-      return src[(int64_t)i * plane + ((int64_t)zz * ny + yy) * nx + xx];
-    };
-    const double fp = at(1), fm = at(-1);
-    if (fp > 0.0 && fm > 0.0) out = (fp + fm) / 2.0;
-    else if (fp > 0.0 && fm < 0.0) out = (fp + fabs(v)) / 2;
-    else if (fp < 0.0 && fm > 0.0) out = (fm + fabs(v)) / 2;
-    else out = fabs(v);
-    atomicAdd(&stats->exact_nodes, 1ull);
-  }
-  dst[(int64_t)i * plane + n] = out;
-}
-
 }  // namespace
 
 void launch_d3q39_fp64(const Step39Args& a, cudaStream_t s) {
   const int threads = 64;
   const int64_t blocks = (a.N + threads - 1) / threads;
   d3q39_fp64_kernel<<<(unsigned)blocks, threads, 0, s>>>(a);
+}
+
+// damp_it.f95:64-177, fout part, on a box with link codes (see the oracle's
+// damp39_links for the rules).  dmask per node: bit i link i interior
+// (unshifted: state >= 0; shifted: >= -500), bit 63 node type >= -500.
+// Outside the box on a non-periodic axis a node type is -666 and fout the
+// freestream equilibrium eq[i] (the initial value of the nodes outside an
+// external-flow domain).  The reference repairs in place, direction by
+// direction in z, y, x order, so a neighbour that comes earlier in that order
+// and is itself negative is read repaired: damp39_value follows such chains
+// (up to kDampChain links; longer chains read the unrepaired value).
+struct Damp39 {
+  const double* src;
+  const unsigned long long* dmask;
+  const double* eq;
+  int nx, ny, nz, periodic, shifted;
+  int64_t plane;
+  int3 lo, hi;
+};
+constexpr int kDampChain = 6;
+
+__device__ int64_t damp39_node(const Damp39& P, int x, int y, int z) {
+  if (P.periodic & 1) x = (x % P.nx + P.nx) % P.nx;
+  else if (x < 0 || x >= P.nx) return -1;
+  if (P.periodic & 2) y = (y % P.ny + P.ny) % P.ny;
+  else if (y < 0 || y >= P.ny) return -1;
+  if (P.periodic & 4) z = (z % P.nz + P.nz) % P.nz;
+  else if (z < 0 || z >= P.nz) return -1;
+  return ((int64_t)z * P.ny + y) * P.nx + x;
+}
+
+__device__ double damp39_value(const Damp39& P, int i, int64_t n, int depth) {
+  const double v = P.src[(int64_t)i * P.plane + n];
+  if (!(v < 0.0)) return v;
+  const int x = (int)(n % P.nx), y = (int)((n / P.nx) % P.ny), z = (int)(n / ((int64_t)P.nx * P.ny));
+  const int cx = c39.cx[i], cy = c39.cy[i], cz = c39.cz[i];
+  const int64_t mp = damp39_node(P, x + cx, y + cy, z + cz), mm = damp39_node(P, x - cx, y - cy, z - cz);
+  auto read = [&](int64_t m) -> double {
+    if (m < 0) return P.eq[i];
+    if (m < n && depth > 0) return damp39_value(P, i, m, depth - 1);  // already repaired in the sweep
+    return P.src[(int64_t)i * P.plane + m];
+  };
+  const double fp = read(mp), fm = read(mm);
+  const unsigned long long msk = P.dmask ? P.dmask[n] : ~0ull;  // no link codes: every link interior
+  const bool si = (msk >> i) & 1ull;
+  bool four = false, plus = false, minus = false;
+  double out = v;
+  if (!P.shifted) {
+    const bool so = (msk >> c39.opp[i]) & 1ull;
+    four = si && so;
+    plus = si && !so;
+    minus = !si && so;
+    if (!four && !plus && !minus) out = fabs(v);
+  } else {
+    const int a = P.lo.x + x, b = P.lo.y + y, c = P.lo.z + z, ngm = 8;
+    const bool edge = a - cx < P.lo.x - ngm || a - cx < P.lo.y - ngm || c - cz < P.lo.z - ngm ||
+                      a + cx > P.hi.x - ngm || b + cy > P.hi.y - ngm || c + cz > P.hi.z - ngm;
+    if (edge) {
+      out = si ? (fp + fabs(v)) / 2 : fabs(v);
+    } else {
+      const bool up = mm >= 0 && (!P.dmask || ((P.dmask[mm] >> 63) & 1ull));
+      four = si && up;
+      plus = si && !up;
+      minus = !si && up;
+    }
+  }
+  if (four) {
+    if (fp > 0.0 && fm > 0.0) out = (fp + fm) / 2.0;
+    else if (fp > 0.0 && fm < 0.0) out = (fp + fabs(v)) / 2;
+    else if (fp < 0.0 && fm > 0.0) out = (fm + fabs(v)) / 2;
+    else out = fabs(v);
+  } else if (plus) {
+    out = fp > 0.0 ? (fp + fabs(v)) / 2 : fabs(v);
+  } else if (minus) {
+    out = fm > 0.0 ? (fm + fabs(v)) / 2 : fabs(v);
+  }
+  return out;
+}
+
+__global__ void d3q39_damp_links_kernel(const Damp39 P, double* __restrict__ dst, DevStats* stats) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  if (n >= (int64_t)P.nx * P.ny * P.nz) return;
+  const double v = P.src[(int64_t)i * P.plane + n];
+  double out = v;
+  if (v < 0.0) {
+    out = damp39_value(P, i, n, kDampChain);
+    atomicAdd(&stats->exact_nodes, 1ull);
+  }
+  dst[(int64_t)i * P.plane + n] = out;
+}
+
+void launch_d3q39_damp_links(const double* src, double* dst, const unsigned long long* dmask, int nx, int ny, int nz,
+                             int64_t plane, int periodic, int shifted, const int* lo, const int* hi, const double* eq,
+                             DevStats* stats, cudaStream_t s) {
+  const int64_t N = (int64_t)nx * ny * nz;
+  Damp39 P{src, dmask, eq, nx, ny, nz, periodic, shifted, plane, make_int3(lo[0], lo[1], lo[2]),
+           make_int3(hi[0], hi[1], hi[2])};
+  dim3 grid((unsigned)((N + 255) / 256), 39);
+  d3q39_damp_links_kernel<<<grid, 256, 0, s>>>(P, dst, stats);
 }
 
 void launch_d3q39_init(const Step39Args& a, const double* lm0, unsigned long long* capped, cudaStream_t s) {
@@ -766,12 +836,6 @@ void launch_d3q39_walls(const Step39Args& a, cudaStream_t s) {
   d3q39_wall_kernel<<<(unsigned)((a.nwall + threads - 1) / threads), threads, 0, s>>>(a);
 }
 
-void launch_d3q39_damp(const double* src, double* dst, int nx, int ny, int nz, int64_t plane, DevStats* stats,
-                       cudaStream_t s) {
-  const int64_t N = (int64_t)nx * ny * nz;
-  dim3 grid((unsigned)((N + 255) / 256), 39);
-  d3q39_damp_kernel<<<grid, 256, 0, s>>>(src, dst, nx, ny, nz, plane, stats);
-}
 
 }  // namespace elbm
 

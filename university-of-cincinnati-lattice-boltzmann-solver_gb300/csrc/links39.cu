@@ -318,6 +318,19 @@ int decode_links39(const int32_t* st, int ngs, int nx, int ny, int nz, int perio
     w = link39(L39_PULL, v.pop, 0, dx, dy, dz);
     return true;
   };
+  // link classes of the repair (damp_it.f95:64-177)
+  out.dmask.assign(N, 0ull);
+  for (int z = 0; z < nz; ++z)
+    for (int y = 0; y < ny; ++y)
+      for (int x = 0; x < nx; ++x) {
+        uint64_t m = 0;
+        for (int i = 0; i < Q39; ++i) {
+          const int32_t c = code(i, x, y, z);
+          if (shifted ? c >= -500 : c >= 0) m |= 1ull << i;
+        }
+        if (code(0, x, y, z) >= -500) m |= 1ull << 63;
+        out.dmask[((int64_t)z * ny + y) * nx + x] = m;
+      }
   // classify the fluid nodes and encode the boundary records
   out.ntype.assign(N, 0);
   out.bidx.assign(N, -1);

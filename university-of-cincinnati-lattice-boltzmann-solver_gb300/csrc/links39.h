@@ -16,6 +16,9 @@ struct Links39 {
   std::vector<uint32_t> words;  // 39 per record
   std::vector<Wall39Rec> walls; // nodes with interpolated wall links
   std::vector<int32_t> recwall; // per record: wall record or -1
+  // per node, for the negative-population repair: bit i (0..38) link i interior (state >= 0;
+  // shifted lattice: >= -500), bit 63 node type >= -500
+  std::vector<uint64_t> dmask;
 };
 
 int decode_links39(const int32_t* st, int ngs, int nx, int ny, int nz, int periodic, int shifted, int pfd,
