@@ -141,6 +141,16 @@ int elbm_set_d3q39_params(elbm_ctx* ctx, int lvl, const elbm_d3q39_params* p);
  * step's w velocity (1 comp), all as FABs with the level's ghost width. */
 int elbm_upload_level39(elbm_ctx* ctx, int lvl, int box, const double* fout, const double* gout, const double* lm,
                         const double* w_vel);
+/* Level checkpoints (restart; the reference's restart writer is commented
+ * out, output/restart/restart_write.f95): the dynamic state of a level —
+ * D3Q27: the post-collision populations; D3Q39, per box: f, g, the
+ * multipliers, w, the macroscopic fields and, with link codes, the slots
+ * that keep last step's values — and the D3Q39 timestep, written to one file
+ * and read back bit for bit into a level registered, parameterised and
+ * linked the same way.  No counterpart in the reference. */
+int elbm_checkpoint_write(elbm_ctx* ctx, int lvl, const char* path);
+int elbm_checkpoint_read(elbm_ctx* ctx, int lvl, const char* path);
+
 /* Initial state of a D3Q39 box from its macroscopic fields rho, u, v, w, T
  * (5 comps, FAB layout), computed on the device node by node like
  * multilevel_initialization.f90:229-278: the multiplier Newton from lm_start

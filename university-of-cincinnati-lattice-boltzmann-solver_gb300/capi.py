@@ -156,6 +156,8 @@ SIGNATURES = {
     "elbm_download_level39": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
     "elbm_upload_macro39": (_c_int, [_vp, _c_int, _c_int, _vp]),
     "elbm_init_level39": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp]),
+    "elbm_checkpoint_write": (_c_int, [_vp, _c_int, ct.c_char_p]),
+    "elbm_checkpoint_read": (_c_int, [_vp, _c_int, ct.c_char_p]),
     "elbm_d3q39_equilibrium": (_c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "elbm_upload_level_noalloc": (_c_int, [_vp, _c_int, _c_int, _vp]),
     "elbm_autotune": (_c_int, [_vp, _c_int, _c_int, _vp, _vp]),
@@ -354,6 +356,12 @@ class Context:
     def upload39(self, lvl, box, fout, gout, lm, w_vel):
         arrs = [np.ascontiguousarray(a, np.float64) for a in (fout, gout, lm, w_vel)]
         self._check(self.lib.elbm_upload_level39(self.h, lvl, box, *map(_ptr, arrs)))
+
+    def checkpoint_write(self, lvl, path):
+        self._check(self.lib.elbm_checkpoint_write(self.h, lvl, str(path).encode()))
+
+    def checkpoint_read(self, lvl, path):
+        self._check(self.lib.elbm_checkpoint_read(self.h, lvl, str(path).encode()))
 
     def init_level39(self, lvl, box, macro, lm_start):
         """Equilibrium initial state of a D3Q39 box from rho, u, v, w, T (5, nz, ny, nx) on the
