@@ -141,6 +141,20 @@ int elbm_set_d3q39_params(elbm_ctx* ctx, int lvl, const elbm_d3q39_params* p);
  * step's w velocity (1 comp), all as FABs with the level's ghost width. */
 int elbm_upload_level39(elbm_ctx* ctx, int lvl, int box, const double* fout, const double* gout, const double* lm,
                         const double* w_vel);
+/* Refinement tags of a D3Q39 box by the gradient of the gradient magnitude
+ * of one macroscopic field (GGM/derivatives/calculate_grad_mag.f95 and
+ * calculate_gradgrad_mag.f95, on the device from the fields the step keeps):
+ * variable as populate_q.f95 numbers it (1 rho, 2 u, 3 v, 4 w, 5 pressure,
+ * 6 T, 7 |u|, 8 0.5 rho |u|); scheme 0 central, 1 up-wind, 2 down-wind
+ * differences (the namelist's central_diff / upwind_calculation /
+ * downwind_calculation); limit: the level's ggm_tag_limit (the sensitivity
+ * times 0.9^lvl, timing_calcs.f95:88-97).  tags (nx*ny*nz bytes, x fastest):
+ * 1 where the node's GGM >= limit; ggm (may be NULL): the GGM values;
+ * *ntagged (may be NULL): the tagged count.  The predictive splitting
+ * option (GGM/PGS) is not included. */
+int elbm_ggm_tags(elbm_ctx* ctx, int lvl, int box, int variable, int scheme, double limit, uint8_t* tags, double* ggm,
+                  int64_t* ntagged);
+
 /* Level checkpoints (restart; the reference's restart writer is commented
  * out, output/restart/restart_write.f95): the dynamic state of a level —
  * D3Q27: the post-collision populations; D3Q39, per box: f, g, the

@@ -323,3 +323,38 @@ def test_d3q39_repair_with_link_codes(pkg, o39, built_lib, shifted):
         rel = np.max(np.abs(out[name][:, fluid] - ref[:, fluid]) / np.abs(ref[:, fluid]))
         assert rel <= 1e-12, (name, rel)
     assert (out["fout"][:, fluid] >= 0).all()
+
+
+@pytest.mark.parametrize("variable,scheme", [(1, 0), (7, 1), (5, 2), (6, 1)])
+def test_d3q39_ggm_tags(pkg, o39, built_lib, variable, scheme):
+    """Refinement tags by the gradient of the gradient magnitude on the device against the
+    numpy restatement of calculate_grad_mag / calculate_gradgrad_mag (ggm to 1e-12, tags
+    identical), on a wedge box with link codes after a few steps."""
+    from oracle import ggm as og
+
+    s39, cap = pkg.d3q39_setup, pkg.capi
+    c = s39.wedge_case_consts(v_inf_ms=0.8 * math.sqrt(1.4 * s39.GAS_CONST_R * 288.15), use_shifted=True)
+    nx, ny, nz, periodic = 22, 6, 12, 2
+    faces = {"x-": -101, "x+": -201, "z-": -10, "z+": -1000, "y-": 0, "y+": 0}
+    st = s39.wedge_state39(nx, ny, nz, 6.0, 14.0, 20.0, faces, periodic=periodic)
+    lm0 = s39.freestream_start_lm(c)
+    params = cap.make_d3q39_params(c, timestep=0, periodic=periodic, damp=0)
+    shape = (nz, ny, nx)
+    ctx = cap.Context(0)
+    _, f, g = ctx.d3q39_equilibrium(params, 1.0, c.mach, 0.0, 0.0, c.temperature, lm0)
+    fs = (c.mach, 0.0, 0.0, c.temperature)
+    ctx.level_register(0, cap.ELBM_D3Q39, cap.ELBM_STORE_FP64, [[0, 0, 0, nx - 1, ny - 1, nz - 1]])
+    ctx.set_d3q39_params(0, params)
+    ctx.set_links39(0, 0, st, cap.make_d3q39_bc([1] * 8, [6] + [1] * 7, f, g, [f] * 8, [g] * 8, [f] * 8, [g] * 8, fs))
+    macro = np.stack([np.full(shape, 1.0), np.full(shape, c.mach), np.zeros(shape), np.zeros(shape),
+                      np.full(shape, c.temperature)])
+    ctx.init_level39(0, 0, macro, lm0)
+    ctx.step(0, 4, want_stats=False)
+    m = ctx.download39(0)["macro"]
+    gm_all = og.ggm_tags(m, st, periodic, variable, scheme, 0.0, (1.0,) + fs)[1]
+    limit = float(np.quantile(gm_all[st[0] >= 0], 0.8))  # tag about a fifth of the fluid nodes
+    tags, ggm, n = ctx.ggm_tags(0, 0, variable, scheme, limit)
+    rt, rg, _ = og.ggm_tags(m, st, periodic, variable, scheme, limit, (1.0,) + fs)
+    ctx.close()
+    assert np.max(np.abs(ggm - rg)) <= 1e-12 * max(1e-300, np.max(np.abs(rg)))
+    assert np.array_equal(tags, rt) and n == int(rt.sum()) > 0

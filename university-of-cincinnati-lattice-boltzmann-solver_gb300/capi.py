@@ -156,6 +156,7 @@ SIGNATURES = {
     "elbm_download_level39": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
     "elbm_upload_macro39": (_c_int, [_vp, _c_int, _c_int, _vp]),
     "elbm_init_level39": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp]),
+    "elbm_ggm_tags": (_c_int, [_vp, _c_int, _c_int, _c_int, _c_int, _c_double, _vp, _vp, _vp]),
     "elbm_checkpoint_write": (_c_int, [_vp, _c_int, ct.c_char_p]),
     "elbm_checkpoint_read": (_c_int, [_vp, _c_int, ct.c_char_p]),
     "elbm_d3q39_equilibrium": (_c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
@@ -356,6 +357,16 @@ class Context:
     def upload39(self, lvl, box, fout, gout, lm, w_vel):
         arrs = [np.ascontiguousarray(a, np.float64) for a in (fout, gout, lm, w_vel)]
         self._check(self.lib.elbm_upload_level39(self.h, lvl, box, *map(_ptr, arrs)))
+
+    def ggm_tags(self, lvl, box, variable, scheme, limit):
+        """(tags, ggm, ntagged) of a D3Q39 box, arrays (nz, ny, nx)."""
+        shp = self.box_shape(lvl, box, ghosts=False)
+        tags = np.zeros(shp, np.uint8)
+        ggm = np.zeros(shp)
+        n = ct.c_int64(0)
+        self._check(self.lib.elbm_ggm_tags(self.h, lvl, box, variable, scheme, limit, _ptr(tags), _ptr(ggm),
+                                           ct.byref(n)))
+        return tags, ggm, n.value
 
     def checkpoint_write(self, lvl, path):
         self._check(self.lib.elbm_checkpoint_write(self.h, lvl, str(path).encode()))

@@ -100,6 +100,7 @@ struct Box {
   DevBuf<double> wallf39, wallg39;
   int64_t nwall39 = 0;
   DevBuf<unsigned long long> dmask39;  // link classes of the repair, per node
+  DevBuf<uint16_t> gmask39;            // links of the GGM differences, per node
   bool macro_set = false;  // elbm_upload_macro39 since the last elbm_upload_level39
   int64_t fluid_nodes = 0, boundary_nodes = 0;
   bool links_set = false, data_set = false;
@@ -1509,6 +1510,8 @@ int elbm_set_links39(elbm_ctx* c, int lvl, int box, const int32_t* state, int ng
     CUDA_TRY(cudaMemcpy(b->words39.p, L.words.data(), L.words.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
              "link words");
   }
+  CUDA_TRY(b->gmask39.alloc(b->N), "ggm links");
+  CUDA_TRY(cudaMemcpy(b->gmask39.p, L.gmask.data(), b->N * sizeof(uint16_t), cudaMemcpyHostToDevice), "ggm links");
   CUDA_TRY(b->dmask39.alloc(b->N), "repair classes");
   CUDA_TRY(cudaMemcpy(b->dmask39.p, L.dmask.data(), b->N * sizeof(uint64_t), cudaMemcpyHostToDevice), "repair classes");
   b->nwall39 = (int64_t)L.walls.size();
@@ -1669,6 +1672,42 @@ int elbm_checkpoint_read(elbm_ctx* c, int lvl, const char* path) {
     bp->data_set = true;
     bp->macro_set = true;
   }
+  return ELBM_OK;
+}
+
+int elbm_ggm_tags(elbm_ctx* c, int lvl, int box, int variable, int scheme, double limit, uint8_t* tags, double* ggm,
+                  int64_t* ntagged) {
+  Level* lv = nullptr;
+  Box* b = get_box(c, lvl, box, &lv);
+  if (!b || !tags) return fail(c, ELBM_E_ARG, "unknown level/box or null tags");
+  if (lv->lattice != ELBM_D3Q39) return fail(c, ELBM_E_UNSUPPORTED, "GGM tagging reads the D3Q39 fields");
+  if (variable < 1 || variable > 8 || scheme < 0 || scheme > 2) return fail(c, ELBM_E_ARG, "bad variable or scheme");
+  if (!b->data_set) return fail(c, ELBM_E_STATE, "no state");
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  if (!b->links39 && !b->gmask39.p) {
+    // a box without link codes (periodic on every axis): every link interior
+    CUDA_TRY(b->gmask39.alloc(b->N), "ggm links");
+    std::vector<uint16_t> all((size_t)b->N, (uint16_t)((1u << 13) - 1u));
+    CUDA_TRY(cudaMemcpy(b->gmask39.p, all.data(), b->N * sizeof(uint16_t), cudaMemcpyHostToDevice), "ggm links");
+  }
+  DevBuf<double> gm, gg;
+  DevBuf<uint8_t> tg;
+  DevBuf<unsigned long long> cnt;
+  CUDA_TRY(gm.alloc(b->N), "gm");
+  CUDA_TRY(gg.alloc(b->N), "ggm");
+  CUDA_TRY(tg.alloc(b->N), "tags");
+  CUDA_TRY(cnt.alloc(1), "count");
+  CUDA_TRY(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned long long), c->stream), "count");
+  const double fs[5] = {1.0, lv->fs39[0], lv->fs39[1], lv->fs39[2], lv->fs39[3]};  // rho_inf = 1 in lattice units
+  launch_ggm(b->macro.p, b->plane, b->nx, b->ny, b->nz, lv->p39.periodic, b->gmask39.p, variable, scheme, fs, limit,
+             gm.p, gg.p, tg.p, cnt.p, c->stream);
+  CUDA_TRY(cudaGetLastError(), "ggm launch");
+  unsigned long long h = 0;
+  CUDA_TRY(cudaMemcpyAsync(tags, tg.p, b->N, cudaMemcpyDeviceToHost, c->stream), "tags");
+  if (ggm) CUDA_TRY(cudaMemcpyAsync(ggm, gg.p, b->N * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "ggm");
+  CUDA_TRY(cudaMemcpyAsync(&h, cnt.p, sizeof h, cudaMemcpyDeviceToHost, c->stream), "count");
+  CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  if (ntagged) *ntagged = (int64_t)h;
   return ELBM_OK;
 }
 

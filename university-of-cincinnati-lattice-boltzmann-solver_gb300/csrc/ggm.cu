@@ -1,0 +1,145 @@
+// Refinement tagging by the gradient of the gradient magnitude (GGM) of a
+// macroscopic field of a D3Q39 level, on the device, from the fields the step
+// keeps (GGM/derivatives/calculate_grad_mag.f95, calculate_gradgrad_mag.f95,
+// GGM/populate_q.f95, derivatives/modules/derivatives.f95:644-760):
+//   gm  = |grad q| with the second-order "windage" differences of every axis,
+//   ggm = |grad gm| the same way, and a tag where ggm >= the level's limit.
+// The differences pick their points from the node's link codes (a point is
+// used when the link to it is >= 0), the reference's quirks kept: the central
+// form is (q(-1) - q(+1)) / 2, and the up-wind form for a non-positive wind
+// reads q(-1), q(-2) while it tests the links to +1, +2.  Points outside the
+// box on a non-periodic axis hold the freestream value of q (the initial
+// value of the nodes outside an external-flow domain) and gm = 0 there.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+
+#include "kernels.cuh"
+
+namespace elbm {
+namespace {
+
+struct GgmArgs {
+  const double* macro;  // rho, u, v, w, T planes
+  int64_t plane;
+  int nx, ny, nz, periodic;
+  const uint16_t* mask;  // per node: bits 0-11 links +1,+2,-1,-2 of x, y, z >= 0; 12 node >= 0; 13 node == -666
+  int variable, scheme;  // populate_q variable (1-8); 0 central, 1 up-wind, 2 down-wind
+  double fs[5];          // freestream rho, u, v, w, T
+};
+
+__device__ __forceinline__ double q_of(int var, double rho, double u, double v, double w, double T) {
+  switch (var) {
+    case 1: return rho;
+    case 2: return u;
+    case 3: return v;
+    case 4: return w;
+    case 5: return rho * (T + (u * u + v * v + w * w) / 2.0);  // calculate_flow_variables.f95: press
+    case 6: return T;
+    case 7: return sqrt(u * u + v * v + w * w);
+    default: return 0.5 * rho * sqrt(u * u + v * v + w * w);  // calculate_v_mag.f95 choice 2
+  }
+}
+
+__device__ __forceinline__ int64_t ggm_node(const GgmArgs& a, int x, int y, int z) {
+  if (a.periodic & 1) x = (x % a.nx + a.nx) % a.nx;
+  else if (x < 0 || x >= a.nx) return -1;
+  if (a.periodic & 2) y = (y % a.ny + a.ny) % a.ny;
+  else if (y < 0 || y >= a.ny) return -1;
+  if (a.periodic & 4) z = (z % a.nz + a.nz) % a.nz;
+  else if (z < 0 || z >= a.nz) return -1;
+  return ((int64_t)z * a.ny + y) * a.nx + x;
+}
+
+// derivative_windage_secondord (and _firstord for its fall-backs); q: q0, q+1, q+2, q-1, q-2;
+// s: link bits +1, +2, -1, -2
+__device__ double windage2(const double (&q)[5], const bool (&s)[4], double wind, int scheme) {
+  const bool p1 = s[0], p2 = s[1], m1 = s[2], m2 = s[3];
+  if (scheme == 0) {
+    if (p1 && m1) return (q[3] - q[1]) / 2.0;
+    if (p1) return q[1] - q[0];
+    if (m1) return q[0] - q[3];
+    return 0.0;
+  }
+  const bool pos = scheme == 1 ? wind > 0.0 : wind < 0.0;
+  if (pos) {
+    if (m1 && m2) return (3 * q[0] - 4 * q[3] + q[4]) / 2;
+    return m1 ? q[3] - q[0] : 0.0;  // first order: the -1 point
+  }
+  if (p1 && p2) return (-3 * q[0] + 4 * q[3] - q[4]) / 2;
+  return p1 ? q[0] - q[1] : 0.0;  // first order: the +1 point
+}
+
+__global__ void ggm_gm_kernel(const GgmArgs a, double* __restrict__ gm) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = (int64_t)a.nx * a.ny * a.nz;
+  if (n >= N) return;
+  const uint16_t m = a.mask[n];
+  if (!((m >> 12) & 1u) && !((m >> 13) & 1u)) {  // state < 0 and not -666: solid
+    gm[n] = 0.0;
+    return;
+  }
+  const int x = (int)(n % a.nx), y = (int)((n / a.nx) % a.ny), z = (int)(n / ((int64_t)a.nx * a.ny));
+  auto q_at = [&](int64_t k) -> double {
+    if (k < 0) return q_of(a.variable, a.fs[0], a.fs[1], a.fs[2], a.fs[3], a.fs[4]);
+    return q_of(a.variable, a.macro[k], a.macro[a.plane + k], a.macro[2 * a.plane + k], a.macro[3 * a.plane + k],
+                a.macro[4 * a.plane + k]);
+  };
+  double sum = 0.0;
+  for (int ax = 0; ax < 3; ++ax) {
+    const int dx = ax == 0, dy = ax == 1, dz = ax == 2;
+    const double q[5] = {q_at(n), q_at(ggm_node(a, x + dx, y + dy, z + dz)),
+                         q_at(ggm_node(a, x + 2 * dx, y + 2 * dy, z + 2 * dz)),
+                         q_at(ggm_node(a, x - dx, y - dy, z - dz)), q_at(ggm_node(a, x - 2 * dx, y - 2 * dy, z - 2 * dz))};
+    const bool s[4] = {(bool)((m >> (4 * ax)) & 1u), (bool)((m >> (4 * ax + 1)) & 1u),
+                       (bool)((m >> (4 * ax + 2)) & 1u), (bool)((m >> (4 * ax + 3)) & 1u)};
+    const double d = windage2(q, s, a.macro[(1 + ax) * a.plane + n], a.scheme);
+    sum = (ax == 0) ? d * d : sum + d * d;
+  }
+  gm[n] = sqrt(sum);
+}
+
+__global__ void ggm_tag_kernel(const GgmArgs a, const double* __restrict__ gm, double limit, double* __restrict__ ggm,
+                               uint8_t* __restrict__ tags, unsigned long long* ntag) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = (int64_t)a.nx * a.ny * a.nz;
+  if (n >= N) return;
+  const uint16_t m = a.mask[n];
+  double g = 0.0;
+  if ((m >> 12) & 1u) {
+    const int x = (int)(n % a.nx), y = (int)((n / a.nx) % a.ny), z = (int)(n / ((int64_t)a.nx * a.ny));
+    auto gm_at = [&](int64_t k) -> double { return k < 0 ? 0.0 : gm[k]; };
+    double sum = 0.0;
+    for (int ax = 0; ax < 3; ++ax) {
+      const int dx = ax == 0, dy = ax == 1, dz = ax == 2;
+      const double q[5] = {gm[n], gm_at(ggm_node(a, x + dx, y + dy, z + dz)),
+                           gm_at(ggm_node(a, x + 2 * dx, y + 2 * dy, z + 2 * dz)),
+                           gm_at(ggm_node(a, x - dx, y - dy, z - dz)),
+                           gm_at(ggm_node(a, x - 2 * dx, y - 2 * dy, z - 2 * dz))};
+      const bool s[4] = {(bool)((m >> (4 * ax)) & 1u), (bool)((m >> (4 * ax + 1)) & 1u),
+                         (bool)((m >> (4 * ax + 2)) & 1u), (bool)((m >> (4 * ax + 3)) & 1u)};
+      const double d = windage2(q, s, a.macro[(1 + ax) * a.plane + n], a.scheme);
+      sum = (ax == 0) ? d * d : sum + d * d;
+    }
+    g = sqrt(sum);
+  }
+  if (ggm) ggm[n] = g;
+  const bool t = ((m >> 12) & 1u) && g >= limit;
+  tags[n] = t ? 1 : 0;
+  if (t) atomicAdd(ntag, 1ull);
+}
+
+}  // namespace
+
+void launch_ggm(const double* macro, int64_t plane, int nx, int ny, int nz, int periodic, const uint16_t* mask,
+                int variable, int scheme, const double* fs, double limit, double* gm, double* ggm, uint8_t* tags,
+                unsigned long long* ntag, cudaStream_t s) {
+  GgmArgs a{macro, plane, nx, ny, nz, periodic, mask, variable, scheme, {fs[0], fs[1], fs[2], fs[3], fs[4]}};
+  const int64_t N = (int64_t)nx * ny * nz;
+  const unsigned blocks = (unsigned)((N + 255) / 256);
+  ggm_gm_kernel<<<blocks, 256, 0, s>>>(a, gm);
+  ggm_tag_kernel<<<blocks, 256, 0, s>>>(a, gm, limit, ggm, tags, ntag);
+}
+
+}  // namespace elbm

@@ -320,6 +320,7 @@ int decode_links39(const int32_t* st, int ngs, int nx, int ny, int nz, int perio
   };
   // link classes of the repair (damp_it.f95:64-177)
   out.dmask.assign(N, 0ull);
+  out.gmask.assign(N, 0);
   for (int z = 0; z < nz; ++z)
     for (int y = 0; y < ny; ++y)
       for (int x = 0; x < nx; ++x) {
@@ -330,6 +331,9 @@ int decode_links39(const int32_t* st, int ngs, int nx, int ny, int nz, int perio
         }
         if (code(0, x, y, z) >= -500) m |= 1ull << 63;
         out.dmask[((int64_t)z * ny + y) * nx + x] = m;
+        int32_t cs[Q39];
+        for (int i = 0; i < Q39; ++i) cs[i] = code(i, x, y, z);
+        out.gmask[((int64_t)z * ny + y) * nx + x] = ggm_mask39(cs);
       }
   // classify the fluid nodes and encode the boundary records
   out.ntype.assign(N, 0);
