@@ -155,6 +155,25 @@ int elbm_upload_level39(elbm_ctx* ctx, int lvl, int box, const double* fout, con
 int elbm_ggm_tags(elbm_ctx* ctx, int lvl, int box, int variable, int scheme, double limit, uint8_t* tags, double* ggm,
                   int64_t* ntagged);
 
+/* Plot3D output of a D3Q39 level from the device buffers, in the
+ * reference's layout (output/plot3d_output.f95:77-215): Fortran unformatted
+ * sequential records; grid file: block count, (nx, ny, nz) per block, then per
+ * block x, y, z (4-byte reals: origin + (lo + i) dx) and blanks (1 node
+ * type >= 0, -1 null node -666, 0 otherwise); data file: block count, the
+ * dimensions with 6 variables and 0, then per block the header record and
+ * rho, u, v, w, T, alpha (8-byte reals).  Every box of the level is a block. */
+typedef struct {
+  double mach, reynolds, time, gama, t_ref, stag_temperature, const_vol, const_press, non_dim_R;
+} elbm_plot3d_header;
+int elbm_write_plot3d(elbm_ctx* ctx, int lvl, const char* grid_path, const char* data_path, const double* origin,
+                      double dx, const elbm_plot3d_header* hdr);
+/* Microphones of a D3Q39 box (mic_write.f95:45-110): for each of nmic
+ * microphones the weighted sums over its 8 nodes (box-local indices, x
+ * fastest; weights from the microphone set-up) of pressure, T, rho, u, v, w,
+ * gathered on the device; out: 6 values per microphone. */
+int elbm_mic_sample(elbm_ctx* ctx, int lvl, int box, int nmic, const int32_t* nodes, const double* weights,
+                    double* out);
+
 /* Level checkpoints (restart; the reference's restart writer is commented
  * out, output/restart/restart_write.f95): the dynamic state of a level —
  * D3Q27: the post-collision populations; D3Q39, per box: f, g, the

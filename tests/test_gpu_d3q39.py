@@ -358,3 +358,73 @@ def test_d3q39_ggm_tags(pkg, o39, built_lib, variable, scheme):
     ctx.close()
     assert np.max(np.abs(ggm - rg)) <= 1e-12 * max(1e-300, np.max(np.abs(rg)))
     assert np.array_equal(tags, rt) and n == int(rt.sum()) > 0
+
+
+def _f_records(path):
+    """Fortran unformatted sequential records of a file (4-byte length markers)."""
+    data = open(path, "rb").read()
+    out, k = [], 0
+    while k < len(data):
+        n = int(np.frombuffer(data, np.int32, 1, k)[0])
+        out.append(data[k + 4:k + 4 + n])
+        assert int(np.frombuffer(data, np.int32, 1, k + 4 + n)[0]) == n
+        k += n + 8
+    return out
+
+
+def test_d3q39_plot3d_and_microphones(pkg, o39, built_lib, tmp_path):
+    """Plot3D grid and data files written from the device buffers in the reference's record
+    layout (plot3d_output.f95), read back and compared with the downloaded fields; microphone
+    samples (weighted sums over 8 nodes, mic_write.f95) against numpy on the same fields."""
+    s39, cap = pkg.d3q39_setup, pkg.capi
+    c = s39.wedge_case_consts(v_inf_ms=0.8 * math.sqrt(1.4 * s39.GAS_CONST_R * 288.15), use_shifted=True)
+    nx, ny, nz, periodic = 22, 6, 12, 2
+    faces = {"x-": -101, "x+": -201, "z-": -10, "z+": -1000, "y-": 0, "y+": 0}
+    st = s39.wedge_state39(nx, ny, nz, 6.0, 14.0, 20.0, faces, periodic=periodic)
+    lm0 = s39.freestream_start_lm(c)
+    params = cap.make_d3q39_params(c, timestep=0, periodic=periodic, damp=0)
+    shape = (nz, ny, nx)
+    ctx = cap.Context(0)
+    _, f, g = ctx.d3q39_equilibrium(params, 1.0, c.mach, 0.0, 0.0, c.temperature, lm0)
+    lo = (4, 0, 2)
+    ctx.level_register(0, cap.ELBM_D3Q39, cap.ELBM_STORE_FP64, [[lo[0], lo[1], lo[2], lo[0] + nx - 1, ny - 1,
+                                                                   lo[2] + nz - 1]])
+    ctx.set_d3q39_params(0, params)
+    ctx.set_links39(0, 0, st, cap.make_d3q39_bc([1] * 8, [6] + [1] * 7, f, g, [f] * 8, [g] * 8, [f] * 8, [g] * 8,
+                                                 (c.mach, 0.0, 0.0, c.temperature)))
+    macro0 = np.stack([np.full(shape, 1.0), np.full(shape, c.mach), np.zeros(shape), np.zeros(shape),
+                       np.full(shape, c.temperature)])
+    ctx.init_level39(0, 0, macro0, lm0)
+    ctx.step(0, 3, want_stats=False)
+    out = ctx.download39(0)
+    hdr = cap.Plot3DHeader(mach=c.mach, reynolds=1.0e5, time=3 * c.dt, gama=c.gama, t_ref=c.t_ref,
+                           stag_temperature=1.2, const_vol=c.const_vol, const_press=c.const_press, non_dim_R=1.0)
+    origin, dx = (0.5, -1.0, 0.25), 1e-4
+    ctx.write_plot3d(0, tmp_path / "g.x", tmp_path / "d.q", origin, dx, hdr)
+    rng = np.random.default_rng(2)
+    nodes = rng.integers(0, nx * ny * nz, (5, 8)).astype(np.int32)
+    wts = rng.uniform(0, 1, (5, 8))
+    wts /= wts.sum(axis=1, keepdims=True)
+    mic = ctx.mic_sample(0, 0, nodes, wts)
+    ctx.close()
+    N = nx * ny * nz
+    g_rec = _f_records(tmp_path / "g.x")
+    d_rec = _f_records(tmp_path / "d.q")
+    assert np.frombuffer(g_rec[0], np.int32)[0] == 1 and np.frombuffer(d_rec[0], np.int32)[0] == 1
+    assert list(np.frombuffer(g_rec[1], np.int32)) == [nx, ny, nz]
+    assert list(np.frombuffer(d_rec[1], np.int32)) == [nx, ny, nz, 6, 0]
+    xyz = np.frombuffer(g_rec[2], np.float32, 3 * N).reshape(3, nz, ny, nx)
+    blanks = np.frombuffer(g_rec[2], np.int32, N, 12 * N).reshape(shape)
+    xs = (origin[0] + lo[0] * dx + dx * np.arange(nx)).astype(np.float32)
+    assert np.array_equal(xyz[0, 0, 0], xs)
+    assert np.array_equal(blanks, np.where(st[0] >= 0, 1, np.where(st[0] == -666, -1, 0)))
+    head = d_rec[2]
+    assert len(head) == 8 * 14 + 4 * 2 and np.frombuffer(head, np.float64, 1, 0)[0] == c.mach
+    assert np.frombuffer(head, np.int32, 1, len(head) - 4)[0] == 3  # timestep after 3 steps
+    vals = np.frombuffer(d_rec[3], np.float64).reshape(6, nz, ny, nx)
+    assert np.array_equal(vals[:5], out["macro"]) and np.array_equal(vals[5], out["alpha"])
+    m = out["macro"].reshape(5, N)
+    press = m[0] * (m[4] + (m[1] ** 2 + m[2] ** 2 + m[3] ** 2) / 2.0)
+    for k, field in enumerate([press, m[4], m[0], m[1], m[2], m[3]]):
+        ref = (wts * field[nodes]).sum(axis=1)
+        assert np.allclose(mic[:, k], ref, rtol=1e-13, atol=0), k

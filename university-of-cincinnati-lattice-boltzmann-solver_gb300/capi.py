@@ -121,6 +121,11 @@ def make_d3q39_bc(inlet_type, outlet_type, fs_f, fs_g, inl_f, inl_g, outl_f, out
     return b
 
 
+class Plot3DHeader(ct.Structure):
+    _fields_ = [(n, ct.c_double) for n in ("mach", "reynolds", "time", "gama", "t_ref", "stag_temperature",
+                                           "const_vol", "const_press", "non_dim_R")]
+
+
 class Stats(ct.Structure):
     _fields_ = [
         ("node_updates", ct.c_int64),
@@ -157,6 +162,8 @@ SIGNATURES = {
     "elbm_upload_macro39": (_c_int, [_vp, _c_int, _c_int, _vp]),
     "elbm_init_level39": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp]),
     "elbm_ggm_tags": (_c_int, [_vp, _c_int, _c_int, _c_int, _c_int, _c_double, _vp, _vp, _vp]),
+    "elbm_write_plot3d": (_c_int, [_vp, _c_int, ct.c_char_p, ct.c_char_p, _vp, _c_double, _vp]),
+    "elbm_mic_sample": (_c_int, [_vp, _c_int, _c_int, _c_int, _vp, _vp, _vp]),
     "elbm_checkpoint_write": (_c_int, [_vp, _c_int, ct.c_char_p]),
     "elbm_checkpoint_read": (_c_int, [_vp, _c_int, ct.c_char_p]),
     "elbm_d3q39_equilibrium": (_c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
@@ -367,6 +374,19 @@ class Context:
         self._check(self.lib.elbm_ggm_tags(self.h, lvl, box, variable, scheme, limit, _ptr(tags), _ptr(ggm),
                                            ct.byref(n)))
         return tags, ggm, n.value
+
+    def write_plot3d(self, lvl, grid_path, data_path, origin, dx, header: Plot3DHeader):
+        o = np.ascontiguousarray(origin, np.float64)
+        self._check(self.lib.elbm_write_plot3d(self.h, lvl, str(grid_path).encode(), str(data_path).encode(), _ptr(o),
+                                               dx, ct.byref(header)))
+
+    def mic_sample(self, lvl, box, nodes, weights):
+        """nodes, weights: (nmic, 8); returns (nmic, 6): pressure, T, rho, u, v, w."""
+        nd = np.ascontiguousarray(nodes, np.int32)
+        wt = np.ascontiguousarray(weights, np.float64)
+        out = np.zeros((nd.shape[0], 6))
+        self._check(self.lib.elbm_mic_sample(self.h, lvl, box, nd.shape[0], _ptr(nd), _ptr(wt), _ptr(out)))
+        return out
 
     def checkpoint_write(self, lvl, path):
         self._check(self.lib.elbm_checkpoint_write(self.h, lvl, str(path).encode()))

@@ -1675,6 +1675,112 @@ int elbm_checkpoint_read(elbm_ctx* c, int lvl, const char* path) {
   return ELBM_OK;
 }
 
+// ---- output from the device buffers (output/plot3d_output.f95, output/mic_setup_stuff/mic_write.f95) ----
+namespace {
+// one Fortran unformatted sequential record: 4-byte length, payload, 4-byte length
+bool f_record(FILE* fp, const std::vector<std::pair<const void*, size_t>>& parts) {
+  size_t n = 0;
+  for (auto& q : parts) n += q.second;
+  if (n > 0x7fffffffu) return false;
+  const int32_t m = (int32_t)n;
+  bool ok = std::fwrite(&m, 4, 1, fp) == 1;
+  for (auto& q : parts) ok = ok && (q.second == 0 || std::fwrite(q.first, 1, q.second, fp) == q.second);
+  return ok && std::fwrite(&m, 4, 1, fp) == 1;
+}
+}  // namespace
+
+int elbm_write_plot3d(elbm_ctx* c, int lvl, const char* grid_path, const char* data_path, const double* origin,
+                      double dx, const elbm_plot3d_header* hdr) {
+  Level* lv = get_level(c, lvl);
+  if (!lv || !grid_path || !data_path || !origin || !hdr || !(dx > 0)) return fail(c, ELBM_E_ARG, "bad arguments");
+  if (lv->lattice != ELBM_D3Q39) return fail(c, ELBM_E_UNSUPPORTED, "Plot3D output writes the D3Q39 fields");
+  for (auto& bp : lv->boxes)
+    if (!bp->data_set) return fail(c, ELBM_E_STATE, "no state");
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  FILE* g = std::fopen(grid_path, "wb");
+  FILE* d = std::fopen(data_path, "wb");
+  if (!g || !d) {
+    if (g) std::fclose(g);
+    if (d) std::fclose(d);
+    return fail(c, ELBM_E_ARG, "cannot open the output files");
+  }
+  const int32_t nb = (int32_t)lv->boxes.size();
+  std::vector<int32_t> dims, ddims;
+  for (auto& bp : lv->boxes) {
+    dims.insert(dims.end(), {bp->nx, bp->ny, bp->nz});
+  }
+  ddims = dims;
+  ddims.push_back(6);  // rho, u, v, w, T, alpha
+  ddims.push_back(0);
+  bool ok = f_record(g, {{&nb, 4}}) && f_record(d, {{&nb, 4}}) && f_record(g, {{dims.data(), dims.size() * 4}}) &&
+            f_record(d, {{ddims.data(), ddims.size() * 4}});
+  const double zero = 0.0;
+  const int32_t izero = 0, ts = lv->p39.timestep;
+  std::vector<double> macro, alpha;
+  std::vector<uint16_t> gm;
+  std::vector<float> xyz;
+  std::vector<int32_t> blank;
+  for (auto& bp : lv->boxes) {
+    Box& b = *bp;
+    const size_t N = (size_t)b.N;
+    macro.resize(5 * N);
+    alpha.resize(N);
+    for (int k = 0; k < 5; ++k)
+      CUDA_TRY(cudaMemcpy(macro.data() + k * N, b.macro.p + (size_t)k * b.plane, N * sizeof(double),
+                          cudaMemcpyDeviceToHost), "fields");
+    CUDA_TRY(cudaMemcpy(alpha.data(), b.alpha64.p, N * sizeof(double), cudaMemcpyDeviceToHost), "alpha");
+    gm.assign(N, (uint16_t)(1u << 12));
+    if (b.gmask39.p) CUDA_TRY(cudaMemcpy(gm.data(), b.gmask39.p, N * 2, cudaMemcpyDeviceToHost), "node types");
+    xyz.resize(3 * N);
+    blank.resize(N);
+    const double start[3] = {origin[0] + b.lo[0] * dx, origin[1] + b.lo[1] * dx, origin[2] + b.lo[2] * dx};
+    for (int z = 0; z < b.nz; ++z)
+      for (int y = 0; y < b.ny; ++y)
+        for (int x = 0; x < b.nx; ++x) {
+          const size_t n = ((size_t)z * b.ny + y) * b.nx + x;
+          xyz[n] = (float)(start[0] + dx * x);
+          xyz[N + n] = (float)(start[1] + dx * y);
+          xyz[2 * N + n] = (float)(start[2] + dx * z);
+          blank[n] = ((gm[n] >> 12) & 1u) ? 1 : ((gm[n] >> 13) & 1u) ? -1 : 0;
+        }
+    ok = ok && f_record(g, {{xyz.data(), 3 * N * 4}, {blank.data(), N * 4}});
+    ok = ok && f_record(d, {{&hdr->mach, 8}, {&zero, 8}, {&hdr->reynolds, 8}, {&hdr->time, 8}, {&hdr->gama, 8},
+                            {&zero, 8}, {&hdr->t_ref, 8}, {&izero, 4}, {&hdr->stag_temperature, 8},
+                            {&hdr->const_vol, 8}, {&hdr->const_press, 8}, {&hdr->non_dim_R, 8},
+                            {&hdr->non_dim_R, 8}, {&hdr->mach, 8}, {&hdr->time, 8}, {&ts, 4}});
+    ok = ok && f_record(d, {{macro.data(), 5 * N * 8}, {alpha.data(), N * 8}});
+  }
+  ok = (std::fclose(g) == 0) && ok;
+  ok = (std::fclose(d) == 0) && ok;
+  if (!ok) return fail(c, ELBM_E_ARG, "writing the Plot3D files failed");
+  return ELBM_OK;
+}
+
+int elbm_mic_sample(elbm_ctx* c, int lvl, int box, int nmic, const int32_t* nodes, const double* weights,
+                    double* out) {
+  Level* lv = nullptr;
+  Box* b = get_box(c, lvl, box, &lv);
+  if (!b || nmic < 0 || (nmic > 0 && (!nodes || !weights || !out))) return fail(c, ELBM_E_ARG, "bad arguments");
+  if (lv->lattice != ELBM_D3Q39) return fail(c, ELBM_E_UNSUPPORTED, "microphones read the D3Q39 fields");
+  for (int k = 0; k < 8 * nmic; ++k)
+    if (nodes[k] < 0 || nodes[k] >= b->N) return fail(c, ELBM_E_ARG, "microphone node outside the box");
+  if (nmic == 0) return ELBM_OK;
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  DevBuf<int32_t> dn;
+  DevBuf<double> dw, dout;
+  CUDA_TRY(dn.alloc((size_t)8 * nmic), "mic nodes");
+  CUDA_TRY(dw.alloc((size_t)8 * nmic), "mic weights");
+  CUDA_TRY(dout.alloc((size_t)6 * nmic), "mic values");
+  CUDA_TRY(cudaMemcpyAsync(dn.p, nodes, (size_t)8 * nmic * 4, cudaMemcpyHostToDevice, c->stream), "mic nodes");
+  CUDA_TRY(cudaMemcpyAsync(dw.p, weights, (size_t)8 * nmic * 8, cudaMemcpyHostToDevice, c->stream), "mic weights");
+  launch_mic_sample(b->macro.p, b->plane, nmic, dn.p, dw.p, dout.p, c->stream);
+  CUDA_TRY(cudaGetLastError(), "mic launch");
+  CUDA_TRY(cudaMemcpyAsync(out, dout.p, (size_t)6 * nmic * 8, cudaMemcpyDeviceToHost, c->stream), "mic values");
+  CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  return ELBM_OK;
+}
+
 int elbm_ggm_tags(elbm_ctx* c, int lvl, int box, int variable, int scheme, double limit, uint8_t* tags, double* ggm,
                   int64_t* ntagged) {
   Level* lv = nullptr;

@@ -86,6 +86,8 @@ void upload_lattice39(const Lattice39& L, cudaStream_t s);
 void launch_d3q39_fp64(const Step39Args& a, cudaStream_t s);
 void launch_d3q39_walls(const Step39Args& a, cudaStream_t s);
 void launch_d3q39_init(const Step39Args& a, const double* lm0, unsigned long long* capped, cudaStream_t s);
+void launch_mic_sample(const double* macro, int64_t plane, int nmic, const int32_t* nodes, const double* wts,
+                       double* out, cudaStream_t s);
 void launch_ggm(const double* macro, int64_t plane, int nx, int ny, int nz, int periodic, const uint16_t* mask,
                 int variable, int scheme, const double* fs, double limit, double* gm, double* ggm, uint8_t* tags,
                 unsigned long long* ntag, cudaStream_t s);

@@ -46,6 +46,10 @@ module elbm_gb300_iface
     real(c_double) :: fs_u, fs_v, fs_w, fs_temp
   end type
 
+  type, bind(c), public :: elbm_plot3d_header
+    real(c_double) :: mach, reynolds, time, gama, t_ref, stag_temperature, const_vol, const_press, non_dim_R
+  end type
+
   type, bind(c), public :: elbm_stats
     integer(c_int64_t) :: node_updates, newton_iters, exact_path_nodes, fallbacks
     integer(c_int32_t) :: status, pad
@@ -60,7 +64,8 @@ module elbm_gb300_iface
     elbm_upload_level_noalloc, elbm_autotune, elbm_set_kernel_variant, elbm_alpha_harvest, &
     elbm_alpha_mlp_train, elbm_set_alpha_mlp, elbm_interlevel_setup, elbm_fill_fine_ghosts, &
     elbm_average_down, elbm_amr_run, elbm_damp_level, elbm_set_links39, elbm_upload_macro39, &
-    elbm_init_level39, elbm_d3q39_equilibrium, elbm_checkpoint_write, elbm_checkpoint_read, elbm_ggm_tags
+    elbm_init_level39, elbm_d3q39_equilibrium, elbm_checkpoint_write, elbm_checkpoint_read, elbm_ggm_tags, &
+    elbm_write_plot3d, elbm_mic_sample
 
   interface
     integer(c_int) function elbm_create(device, ctx) bind(c, name="elbm_create")
@@ -141,6 +146,25 @@ module elbm_gb300_iface
       integer(c_int8_t), intent(out) :: tags(*)
       type(c_ptr), value :: ggm            ! c_loc(ggm values) or c_null_ptr
       integer(c_int64_t), intent(out) :: ntagged
+    end function
+    integer(c_int) function elbm_write_plot3d(ctx, lvl, grid_path, data_path, origin, dx, hdr) &
+        bind(c, name="elbm_write_plot3d")
+      import :: c_int, c_ptr, c_char, c_double, elbm_plot3d_header
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl
+      character(kind=c_char), intent(in) :: grid_path(*), data_path(*)   ! NUL-terminated
+      real(c_double), intent(in) :: origin(3)
+      real(c_double), value :: dx
+      type(elbm_plot3d_header), intent(in) :: hdr
+    end function
+    integer(c_int) function elbm_mic_sample(ctx, lvl, box, nmic, nodes, weights, values) &
+        bind(c, name="elbm_mic_sample")
+      import :: c_int, c_ptr, c_int32_t, c_double
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl, box, nmic
+      integer(c_int32_t), intent(in) :: nodes(8, *)
+      real(c_double), intent(in) :: weights(8, *)
+      real(c_double), intent(out) :: values(6, *)
     end function
     integer(c_int) function elbm_checkpoint_write(ctx, lvl, path) bind(c, name="elbm_checkpoint_write")
       import :: c_int, c_ptr, c_char
