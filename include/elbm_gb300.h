@@ -279,6 +279,13 @@ int elbm_set_links(elbm_ctx* ctx, int lvl, int box, const int32_t* state, int ng
  * (i,j,k) sits at origin + (i,j,k)*dx; tri: 9 doubles per triangle. */
 int elbm_mark_triangles(int nx, int ny, int nz, const double* origin, double dx, int ntri, const double* tri,
                         int32_t* state);
+/* The same marking on the context's device (a block per +x ray for the
+ * solid test, a thread per node for the wall links, the uniform triangle grid
+ * built on the host): the same codes bit for bit, the set-up cost of large
+ * levels moved off the host (ELBM_E_UNSUPPORTED when more than 4096 triangles
+ * meet one +x ray; elbm_mark_triangles handles those). */
+int elbm_mark_triangles_gpu(elbm_ctx* ctx, int nx, int ny, int nz, const double* origin, double dx, int ntri,
+                            const double* tri, int32_t* state);
 
 /* Copy one box's post-collision populations (fout FAB, FP64, Q comps) to / from the device. */
 int elbm_upload_level(elbm_ctx* ctx, int lvl, int box, const double* fout);

@@ -179,6 +179,7 @@ SIGNATURES = {
     "elbm_links39_tables": (_c_int, [_c_int, _c_int, _c_int, _vp, _c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp,
                                      _vp, _vp, ct.c_int64, _vp]),
     "elbm_mark_triangles": (_c_int, [_c_int, _c_int, _c_int, _vp, _c_double, _c_int, _vp, _vp]),
+    "elbm_mark_triangles_gpu": (_c_int, [_vp, _c_int, _c_int, _c_int, _vp, _c_double, _c_int, _vp, _vp]),
     "elbm_alpha_harvest": (_c_int, [_vp, _c_int, _c_int, _c_int, _vp, ct.c_int64, _vp]),
     "elbm_alpha_mlp_infer": (_c_int, [_vp, _vp, _vp, ct.c_int64, _vp, _vp]),
     "elbm_alpha_mlp_grad": (_c_int, [_vp, _vp, _vp, ct.c_int64, _vp, _vp]),
@@ -387,6 +388,15 @@ class Context:
         out = np.zeros((nd.shape[0], 6))
         self._check(self.lib.elbm_mic_sample(self.h, lvl, box, nd.shape[0], _ptr(nd), _ptr(wt), _ptr(out)))
         return out
+
+    def mark_triangles(self, state: np.ndarray, origin, dx: float, tri: np.ndarray) -> None:
+        """elbm_mark_triangles on this context's device (state (27, nz, ny, nx) int32, updated in place)."""
+        assert state.dtype == np.int32 and state.flags.c_contiguous
+        nz, ny, nx = state.shape[1:]
+        o = np.ascontiguousarray(origin, np.float64)
+        t = np.ascontiguousarray(tri, np.float64)
+        self._check(self.lib.elbm_mark_triangles_gpu(self.h, nx, ny, nz, _ptr(o), dx, t.shape[0], _ptr(t),
+                                                     _ptr(state)))
 
     def checkpoint_write(self, lvl, path):
         self._check(self.lib.elbm_checkpoint_write(self.h, lvl, str(path).encode()))

@@ -1,11 +1,17 @@
 // Internal kernel interface of libelbm_gb300 (not part of the C ABI).
 #pragma once
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 
 #include "lattice.cuh"
 
 namespace elbm {
+
+// Solid nodes and wall links of a triangulated surface on the device (csrc/geometry.cu);
+// state is the host array, read and written back.
+int mark_triangles_device(int nx, int ny, int nz, const double* origin, double dx, int ntri, const double* tri,
+                          int32_t* state, cudaStream_t s, std::string& why);
 
 // Device-side statistics of one or more steps (accumulated with atomics).
 struct DevStats {

@@ -65,7 +65,7 @@ module elbm_gb300_iface
     elbm_alpha_mlp_train, elbm_set_alpha_mlp, elbm_interlevel_setup, elbm_fill_fine_ghosts, &
     elbm_average_down, elbm_amr_run, elbm_damp_level, elbm_set_links39, elbm_upload_macro39, &
     elbm_init_level39, elbm_d3q39_equilibrium, elbm_checkpoint_write, elbm_checkpoint_read, elbm_ggm_tags, &
-    elbm_write_plot3d, elbm_mic_sample
+    elbm_write_plot3d, elbm_mic_sample, elbm_mark_triangles_gpu
 
   interface
     integer(c_int) function elbm_create(device, ctx) bind(c, name="elbm_create")
@@ -146,6 +146,15 @@ module elbm_gb300_iface
       integer(c_int8_t), intent(out) :: tags(*)
       type(c_ptr), value :: ggm            ! c_loc(ggm values) or c_null_ptr
       integer(c_int64_t), intent(out) :: ntagged
+    end function
+    integer(c_int) function elbm_mark_triangles_gpu(ctx, nx, ny, nz, origin, dx, ntri, tri, state) &
+        bind(c, name="elbm_mark_triangles_gpu")
+      import :: c_int, c_ptr, c_double, c_int32_t
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: nx, ny, nz, ntri
+      real(c_double), intent(in) :: origin(3), tri(9, *)
+      real(c_double), value :: dx
+      integer(c_int32_t), intent(inout) :: state(*)
     end function
     integer(c_int) function elbm_write_plot3d(ctx, lvl, grid_path, data_path, origin, dx, hdr) &
         bind(c, name="elbm_write_plot3d")
