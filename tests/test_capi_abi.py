@@ -53,3 +53,53 @@ int main(void) {{
     expect = [ct.sizeof(P), P.outlet_type.offset, P.fs_feq.offset, P.outl_feq.offset, ct.sizeof(S), S.status.offset,
               S.kernel_ms.offset, ct.sizeof(cap.D3Q39Params)]
     assert list(map(int, out)) == expect
+
+
+def test_more_struct_layouts(pkg, tmp_path):
+    """The D3Q39 boundary block and the Plot3D header keep the header's layout in ctypes."""
+    cap = pkg.capi
+    src = tmp_path / "layout39.c"
+    src.write_text(f"""
+#include <stddef.h>
+#include <stdio.h>
+#include "{ROOT / 'include' / 'elbm_gb300.h'}"
+int main(void) {{
+  printf("%zu %zu %zu %zu %zu\\n", sizeof(elbm_d3q39_bc), offsetof(elbm_d3q39_bc, fs_u), offsetof(elbm_d3q39_bc, fs_temp),
+         offsetof(elbm_d3q39_params, su_lm), sizeof(elbm_plot3d_header));
+  return 0;
+}}
+""")
+    exe = tmp_path / "layout39"
+    subprocess.run(["gcc", str(src), "-o", str(exe)], check=True)
+    out = list(map(int, subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()))
+    B, P = cap.D3Q39Bc, cap.D3Q39Params
+    assert out == [ct.sizeof(B), B.fs_u.offset, B.fs_temp.offset, P.su_lm.offset, ct.sizeof(cap.Plot3DHeader)]
+
+
+def test_errors_without_a_context_or_a_gpu(pkg, built_lib):
+    """Entry points return ELBM_E_* codes and never abort: a null context, host-only set-up
+    helpers with bad sizes, and (where this machine has no GPU) context creation."""
+    cap = pkg.capi
+    lib = ct.CDLL(str(built_lib))
+    vp = ct.c_void_p
+    lib.elbm_level_step.argtypes = [vp, ct.c_int, ct.c_int, vp]
+    assert lib.elbm_level_step(None, 0, 1, None) == cap.ELBM_E_ARG
+    lib.elbm_last_error_string.restype = ct.c_char_p
+    lib.elbm_last_error_string.argtypes = [vp]
+    assert lib.elbm_last_error_string(None) == b"null context"
+    lib.elbm_mark_triangles.argtypes = [ct.c_int, ct.c_int, ct.c_int, vp, ct.c_double, ct.c_int, vp, vp]
+    assert lib.elbm_mark_triangles(0, 4, 4, None, 1.0, 1, None, None) == cap.ELBM_E_ARG
+    import numpy as np
+    st = np.zeros((39, 3, 3, 3), np.int32)
+    with __import__("pytest").raises(cap.ElbmError):
+        cap.links39_tables(st, 8, 0, 1, [1] * 8, [1] * 8)  # periodic mask out of range
+    try:
+        import torch
+
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if not has_gpu:
+        out = vp()
+        lib.elbm_create.argtypes = [ct.c_int, ct.POINTER(vp)]
+        assert lib.elbm_create(0, ct.byref(out)) == cap.ELBM_E_CUDA and not out.value

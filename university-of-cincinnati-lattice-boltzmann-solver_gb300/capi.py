@@ -19,6 +19,7 @@ ELBM_E_ARG = -1
 ELBM_E_CUDA = -2
 ELBM_E_UNSUPPORTED = -3
 ELBM_E_STATE = -4
+ELBM_E_NUMERIC = -5
 
 ELBM_ST_NAN = 0x1
 ELBM_ST_NEWTON_FALLBACK = 0x2
