@@ -26,8 +26,9 @@ NVFLAGS = ARCH + [
 ]
 
 
-# Per-file flags: the FP64 D3Q39 step keeps separately rounded multiply and add
-# (no contraction), like the CPU restatement it is checked against.
+# Per-file flags: the GGM tags and the surface marking keep separately rounded
+# multiply and add (no contraction), so that they match their host and CPU
+# counterparts bit for bit.
 FILE_FLAGS = {"ggm.cu": ["-fmad=false"],
               "geometry.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]}
 
