@@ -70,23 +70,22 @@ __device__ __forceinline__ double fieq39(double rho, const double (&lm)[NL], int
 // lu_decomp.f95: LU of J (row-major 13x13, overwritten), substitution,
 // lm -= delta; returns max |delta|.
 __device__ double lu_update39(double* J, const double (&target)[NL], double (&lm)[NL]) {
-  double lo[NL][NL];
-  double up[NL][NL];
-  for (int c = 0; c < NL; ++c) up[0][c] = J[c];
+  // Doolittle in place: L (unit diagonal, below) and U (from the diagonal up) overwrite J row by
+  // row; row 0 of U is row 0 of J, whose entries are also the moments the residual needs
   for (int r = 1; r < NL; ++r) {
     for (int c = 0; c < r; ++c) {
       double v = J[r * NL + c];
       for (int k = 0; k < c; ++k) {
         // lu_decomp.f95:105: lower(5,4) subtracts lower(5,2)*upper(3,4)
-        const double l = (r == 4 && c == 3 && k == 2) ? lo[4][1] : lo[r][k];
-        v -= l * up[k][c];
+        const double l = (r == 4 && c == 3 && k == 2) ? J[4 * NL + 1] : J[r * NL + k];
+        v -= l * J[k * NL + c];
       }
-      lo[r][c] = (c == 0) ? J[r * NL] / up[0][0] : v / up[c][c];
+      J[r * NL + c] = (c == 0) ? J[r * NL] / J[0] : v / J[c * NL + c];
     }
     for (int c = r; c < NL; ++c) {
       double v = J[r * NL + c];
-      for (int k = 0; k < r; ++k) v -= lo[r][k] * up[k][c];
-      up[r][c] = v;
+      for (int k = 0; k < r; ++k) v -= J[r * NL + k] * J[k * NL + c];
+      J[r * NL + c] = v;
     }
   }
   double z[NL];
@@ -95,15 +94,15 @@ __device__ double lu_update39(double* J, const double (&target)[NL], double (&lm
     for (int k = 0; k < r; ++k) {
       // lu_decomp.f95:441: z9 uses lower(9,7)*z8
       const double zz = (r == 8 && k == 6) ? z[7] : z[k];
-      v -= lo[r][k] * zz;
+      v -= J[r * NL + k] * zz;
     }
     z[r] = v;
   }
   double dl[NL];
   for (int r = NL - 1; r >= 0; --r) {
     double v = z[r];
-    for (int c = NL - 1; c > r; --c) v -= up[r][c] * dl[c];
-    dl[r] = v / up[r][r];
+    for (int c = NL - 1; c > r; --c) v -= J[r * NL + c] * dl[c];
+    dl[r] = v / J[r * NL + r];
   }
   double md = fabs(dl[0]);
   for (int r = 1; r < NL; ++r) md = fabs(dl[r]) > md ? fabs(dl[r]) : md;
