@@ -319,13 +319,23 @@ int elbm_level_step(elbm_ctx* ctx, int lvl, int nsteps, elbm_stats* stats);
  * Fine nodes whose state is a ghost code (1e7 .. 1.1e9) belong to the fine
  * level's boxes, are stepped like fluid nodes, and are refilled from the
  * coarse level.  Replaces interlevel_interpolation.f95:114-440 and
- * fine_to_coarse.f95:28-64 for D3Q27 levels.
+ * fine_to_coarse.f95:13-64 for two D3Q27 levels of one storage or two D3Q39
+ * levels (both with link codes, elbm_set_links39).
  *   elbm_interlevel_setup: build the maps, after both levels' links.
  *   elbm_fill_fine_ghosts: explosion, every fine ghost node <- nodal bilinear
- *     interpolation of the coarse populations (negative or NaN: the entropic
- *     equilibrium of the interpolated moments; repaired may be NULL).
+ *     interpolation of the coarse populations.  D3Q27: a negative or NaN
+ *     population sends the node to the entropic equilibrium of the
+ *     interpolated moments.  D3Q39: f, g, the 13 multipliers, rho and T are
+ *     interpolated; each population with f < 0, g < 0 or NaN takes the coarse
+ *     equilibrium f_eq(rho_c, lm_c), g = (2 C_v - 3) T_c f; then the node's
+ *     moments, its multiplier Newton from the interpolated multipliers and its
+ *     alpha are stored (the coarse level needs its fields: a step,
+ *     elbm_upload_macro39 or elbm_init_level39).  repaired (may be NULL):
+ *     ghost nodes with a replaced population; with repaired non-NULL a D3Q39
+ *     multiplier solve that hit the iteration cap returns ELBM_E_NUMERIC.
  *   elbm_average_down: coalescence, coarse nodes under valid fine nodes <-
- *     the fine populations (nodal injection).
+ *     the fine populations (nodal injection; D3Q39 also g, multipliers, w,
+ *     alpha and the fields).
  * Both act on the current (post-collision) populations; the driver calls
  * them where the reference calls interlevel_interpolation and fine_to_coarse
  * (loop.f95:116-128), on the sub-steps the reference does. */

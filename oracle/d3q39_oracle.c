@@ -1142,6 +1142,56 @@ int o39_init_node(const o39_consts* k, double rho, double u, double v, double w,
   return it;
 }
 
+/* One fine ghost node of the explosion (looping/timestepping/interlevel/interlevel_interpolation.f95:364-440).
+ * In: f, g, lm, rho_c, temp_c are the coarse interpolants at the node.  Each population with f < 0,
+ * g < 0 or a NaN takes fieq(rho_c, lm) and g = f (2 Cv - D) temp_c (:389-431); then the sums of
+ * :432-438, the multiplier solve of the node from the interpolated multipliers (:445-451) and
+ * alpha (:452-458).  Out: f, g, lm in place, rho u v w T in macro5, *alpha.  Returns bit 0 when
+ * a population was replaced, bit 1 when the Newton hit the cap. */
+int o39_explode_node(const o39_consts* k, int step, double* f, double* g, double* lm, double rho_c, double temp_c,
+                     double* macro5, double* alpha) {
+  o39_lattice L;
+  o39_lattice_init(&L, k->shifted, k->primary_flow_dir);
+  int ret = 0;
+  double rho_sum = 0.0, u_sum = 0.0, v_sum = 0.0, w_sum = 0.0, energy_sum = 0.0;
+  for (int i = 0; i < Q; ++i) {
+    if (f[i] < 0.0 || g[i] < 0.0 || isnan(f[i]) || isnan(g[i])) {
+      f[i] = fieq39(&L, rho_c, lm, i);
+      g[i] = f[i] * ((2 * k->const_vol - 3) * temp_c);
+      ret |= 1;
+    }
+    rho_sum = rho_sum + f[i];
+    u_sum = u_sum + L.rcx[i] * f[i];
+    v_sum = v_sum + L.rcy[i] * f[i];
+    w_sum = w_sum + L.rcz[i] * f[i];
+    energy_sum = energy_sum + L.cmag[i] * f[i] + g[i];
+  }
+  const double rho = rho_sum, u = u_sum / rho_sum, v = v_sum / rho_sum, w = w_sum / rho_sum;
+  const double v_mag = u * u + v * v + w * w;
+  const double temp = (energy_sum - rho * v_mag) / (2 * k->const_vol * rho);
+  const double P[6] = {rho * (temp + u * u), rho * (temp + v * v), rho * (temp + w * w),
+                       rho * u * v,          rho * u * w,          rho * v * w};
+  double fe[Q];
+  const int it = o39_lagrange(&L, k->max_lm_iters, rho, u, v, w, temp, P, lm, fe);
+  if (it < 0) {
+    ret |= 2;
+    for (int i = 0; i < Q; ++i) fe[i] = fieq39(&L, rho, lm, i);
+  }
+  if (k->turbulent) {
+    double fd[Q];
+    for (int i = 0; i < Q; ++i) fd[i] = fe[i] - f[i];
+    *alpha = o39_alpha(k, f, fd, temp, step);
+  } else {
+    *alpha = 2.0;
+  }
+  macro5[0] = rho;
+  macro5[1] = u;
+  macro5[2] = v;
+  macro5[3] = w;
+  macro5[4] = temp;
+  return ret;
+}
+
 /* Exposed for unit tests of the pieces. */
 int o39_lagrange_api(const o39_consts* k, double rho, double u, double v, double w, double temp, const double* P,
                      double* lm, double* fieq) {

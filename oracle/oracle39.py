@@ -104,6 +104,25 @@ def init_node(k: O39Consts, rho, u, v, w, T, lm0):
     return lm, f, g, it
 
 
+def explode_node(k: O39Consts, step, f, g, lm, rho_c, temp_c):
+    """One fine ghost node of the D3Q39 explosion from its coarse interpolants:
+    returns (f, g, lm, macro5, alpha, flags) (flags bit 0: a population was
+    replaced by the coarse equilibrium, bit 1: the multiplier Newton hit the cap)."""
+    L = lib()
+    if not getattr(L, "_o39_explode_ready", False):
+        L.o39_explode_node.restype = ct.c_int
+        L.o39_explode_node.argtypes = [ct.POINTER(O39Consts), ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_void_p,
+                                       ct.c_double, ct.c_double, ct.c_void_p, ct.POINTER(ct.c_double)]
+        L._o39_explode_ready = True
+    f = np.ascontiguousarray(f, np.float64).copy()
+    g = np.ascontiguousarray(g, np.float64).copy()
+    lm = np.ascontiguousarray(lm, np.float64).copy()
+    m5 = np.zeros(5)
+    a = ct.c_double(0.0)
+    flags = L.o39_explode_node(ct.byref(k), step, _p(f), _p(g), _p(lm), rho_c, temp_c, _p(m5), ct.byref(a))
+    return f, g, lm, m5, a.value, flags
+
+
 def alpha(k: O39Consts, f, fd, T, step):
     return lib().o39_alpha(ct.byref(k), _p(np.ascontiguousarray(f, np.float64)),
                            _p(np.ascontiguousarray(fd, np.float64)), T, step)

@@ -156,3 +156,31 @@ def test_inviscid_rule_matches_reference_table(o39):
                     assert ok and j + 1 == want["dir"] and list(d) == want["loc"], (key, walls, j + 1, d, want)
                 checked += 1
     assert checked == 274
+
+
+@pytest.mark.parametrize("shifted", [0, 1])
+def test_explode_node_known_answers(o39, setup39, shifted):
+    """The ghost-node explosion of interlevel_interpolation.f95:364-440 on an equilibrium
+    interpolant keeps f and g, returns the node's own moments, re-solves to the same
+    multipliers and gives alpha = 2 (no departure from equilibrium); a negative f or a NaN g
+    takes the coarse equilibrium f_eq(rho_c, lm) and g = (2 C_v - 3) T_c f."""
+    c = setup39.wedge_case_consts(use_shifted=bool(shifted), v_inf_ms=0.8 * 340.29)
+    k = o39.consts(c)
+    lm0 = setup39.freestream_start_lm(c)
+    rho, u, v, w, T = 1.02, 0.9 * c.mach, 0.01, -0.02, c.temperature * 1.01
+    lm, f, g, it = o39.init_node(k, rho, u, v, w, T, lm0)
+    assert it > 0
+    f2, g2, lm2, m5, a, flags = o39.explode_node(k, 3, f, g, lm, rho, T)
+    assert flags == 0 and a == 2.0
+    assert np.array_equal(f2, f) and np.array_equal(g2, g)
+    assert np.allclose(m5, [rho, u, v, w, T], rtol=1e-9, atol=1e-12)
+    assert np.max(np.abs(lm2 - lm)) < 1e-7
+    fb, gb = f.copy(), g.copy()
+    fb[4], gb[9] = -0.01, np.nan
+    f3, g3, _, _, _, flags = o39.explode_node(k, 3, fb, gb, lm, rho, T)
+    assert flags & 1
+    lead = (2 * c.const_vol - 3) * T
+    for i in (4, 9):
+        assert abs(f3[i] - f[i]) <= 1e-14 * f[i]  # the equilibrium of (rho_c, lm) is the uploaded f
+        assert abs(g3[i] - f3[i] * lead) <= 1e-15 * g3[i]
+    assert np.array_equal(np.delete(f3, [4, 9]), np.delete(fb, [4, 9]))

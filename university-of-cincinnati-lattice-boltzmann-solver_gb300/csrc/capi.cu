@@ -144,6 +144,16 @@ struct Level {
   DevBuf<unsigned long long> il_repaired;
   int64_t il_nghost = 0, il_ndown = 0;
   bool il_ready = false;
+  // the same for two D3Q39 levels: ghost lists of the fine boxes (box k: entries il39_goff[k] ..
+  // il39_goff[k + 1]) with their coarse sources as (box, local index), coalescence lists of the
+  // coarse boxes (offsets il39_doff) with their fine sources; device tables of both levels' box views
+  DevBuf<int32_t> il39_ghost, il39_gsrc, il39_ddst, il39_dsrc;
+  DevBuf<uint16_t> il39_gbox, il39_dbox;
+  DevBuf<uint8_t> il39_gcnt;
+  std::vector<int64_t> il39_goff, il39_doff;
+  DevBuf<Box39View> il39_cview, il39_fview;
+  std::vector<Box39View> il39_hcview, il39_hfview;
+  DevBuf<unsigned long long> il39_counters;
 };
 
 }  // namespace
@@ -574,6 +584,7 @@ int step39(elbm_ctx* c, Level& lv, int nsteps) {
       CUDA_TRY(cudaGetLastError(), "d3q39 step launch");
       b.cur ^= 1;
       b.gcur ^= 1;
+      b.macro_set = true;  // the step wrote the fields
       if (p.damp) {
         // damp_it.f95:64-177 (fout part) on the new state; a box without link codes is periodic on every axis
         launch_d3q39_damp_links((const double*)b.buf[b.cur].p, (double*)b.buf[b.cur ^ 1].p,
@@ -1214,12 +1225,133 @@ int elbm_alpha_mlp_train(elbm_ctx* c, const float* records, int64_t n, int epoch
   return ELBM_OK;
 }
 
+namespace {
+
+// (box, box-local index) of level coordinates, or box -1.
+int box_of(const Level& lv, int gx, int gy, int gz, int64_t& local) {
+  for (size_t k = 0; k < lv.boxes.size(); ++k) {
+    const Box& b = *lv.boxes[k];
+    if (gx < b.lo[0] || gx > b.hi[0] || gy < b.lo[1] || gy > b.hi[1] || gz < b.lo[2] || gz > b.hi[2]) continue;
+    local = ((int64_t)(gz - b.lo[2]) * b.ny + (gy - b.lo[1])) * b.nx + (gx - b.lo[0]);
+    return (int)k;
+  }
+  return -1;
+}
+
+// The maps of the coarse-fine transfer between two D3Q39 levels (boxes with link codes).
+int interlevel_setup39(elbm_ctx* c, Level* fl, Level* cl) {
+  if (fl->boxes.size() > 65535 || cl->boxes.size() > 65535) return fail(c, ELBM_E_ARG, "too many boxes");
+  for (const auto* lv : {fl, cl})
+    for (const auto& bp : lv->boxes)
+      if (!bp->links39) return fail(c, ELBM_E_STATE, "set the links of both levels first (elbm_set_links39)");
+  // explosion: each fine ghost node from the 1, 2, 4 or 8 coarse nodes around it (z-, y-, x-major)
+  std::vector<int32_t> gidx, gsrc;
+  std::vector<uint16_t> gbox;
+  std::vector<uint8_t> gcnt;
+  std::vector<int64_t> goff{0};
+  for (const auto& bp : fl->boxes) {
+    const Box& b = *bp;
+    for (int64_t n : b.h_ghost) {
+      const int X[3] = {b.lo[0] + (int)(n % b.nx), b.lo[1] + (int)((n / b.nx) % b.ny),
+                        b.lo[2] + (int)(n / ((int64_t)b.nx * b.ny))};
+      int lo[3], hi[3];
+      for (int a = 0; a < 3; ++a) {
+        lo[a] = (X[a] - ((X[a] % 2 + 2) % 2)) / 2;          // floor(X / 2)
+        hi[a] = ((X[a] % 2 + 2) % 2) ? lo[a] + 1 : lo[a];  // odd: the next coarse node too
+      }
+      int32_t src[8];
+      uint16_t sb[8];
+      int k = 0;
+      for (int cz = lo[2]; cz <= hi[2]; ++cz)
+        for (int cy = lo[1]; cy <= hi[1]; ++cy)
+          for (int cxx = lo[0]; cxx <= hi[0]; ++cxx) {
+            int64_t li = 0;
+            const int bi = box_of(*cl, cxx, cy, cz, li);
+            if (bi < 0)
+              return fail(c, ELBM_E_UNSUPPORTED, "fine ghost node (%d,%d,%d) lies outside the coarse level", X[0], X[1],
+                          X[2]);
+            src[k] = (int32_t)li;
+            sb[k++] = (uint16_t)bi;
+          }
+      for (int m = k; m < 8; ++m) {
+        src[m] = src[0];
+        sb[m] = sb[0];
+      }
+      gidx.push_back((int32_t)n);
+      gsrc.insert(gsrc.end(), src, src + 8);
+      gbox.insert(gbox.end(), sb, sb + 8);
+      gcnt.push_back((uint8_t)k);
+    }
+    goff.push_back((int64_t)gidx.size());
+  }
+  // coalescence: coarse nodes (not skipped) under a valid fine node (not skipped, not a ghost)
+  std::vector<int32_t> ddst, dsrc;
+  std::vector<uint16_t> dbox;
+  std::vector<int64_t> doff{0};
+  for (const auto& bp : cl->boxes) {
+    const Box& b = *bp;
+    for (int64_t n = 0; n < b.N; ++n) {
+      if (b.h_ntype[n] == 0) continue;
+      const int C[3] = {b.lo[0] + (int)(n % b.nx), b.lo[1] + (int)((n / b.nx) % b.ny),
+                        b.lo[2] + (int)(n / ((int64_t)b.nx * b.ny))};
+      int64_t li = 0;
+      const int fb = box_of(*fl, 2 * C[0], 2 * C[1], 2 * C[2], li);
+      if (fb < 0) continue;
+      const Box& f = *fl->boxes[fb];
+      if (f.h_ntype[li] == 0 || std::binary_search(f.h_ghost.begin(), f.h_ghost.end(), li)) continue;
+      ddst.push_back((int32_t)n);
+      dsrc.push_back((int32_t)li);
+      dbox.push_back((uint16_t)fb);
+    }
+    doff.push_back((int64_t)ddst.size());
+  }
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  auto put = [&](auto& buf, const auto& v) -> cudaError_t {
+    cudaError_t e = buf.alloc(std::max<size_t>(v.size(), 1));
+    if (e == cudaSuccess && !v.empty())
+      e = cudaMemcpy(buf.p, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice);
+    return e;
+  };
+  CUDA_TRY(put(fl->il39_ghost, gidx), "interlevel map");
+  CUDA_TRY(put(fl->il39_gsrc, gsrc), "interlevel map");
+  CUDA_TRY(put(fl->il39_gbox, gbox), "interlevel map");
+  CUDA_TRY(put(fl->il39_gcnt, gcnt), "interlevel map");
+  CUDA_TRY(put(fl->il39_ddst, ddst), "interlevel map");
+  CUDA_TRY(put(fl->il39_dsrc, dsrc), "interlevel map");
+  CUDA_TRY(put(fl->il39_dbox, dbox), "interlevel map");
+  CUDA_TRY(fl->il39_cview.alloc(cl->boxes.size()), "box views");
+  CUDA_TRY(fl->il39_fview.alloc(fl->boxes.size()), "box views");
+  CUDA_TRY(fl->il39_counters.alloc(2), "interlevel counters");
+  fl->il39_goff.swap(goff);
+  fl->il39_doff.swap(doff);
+  fl->il_nghost = (int64_t)gidx.size();
+  fl->il_ndown = (int64_t)ddst.size();
+  fl->il_ready = true;
+  return ELBM_OK;
+}
+
+Box39View view39(Box& b) {
+  return Box39View{(double*)b.buf[b.cur].p, (double*)b.gbuf[b.gcur].p, b.lm.p, b.w_vel.p, b.alpha64.p, b.macro.p,
+                   b.plane};
+}
+
+// Upload the box views of a level (their ping-pong halves change every step).
+cudaError_t views39(elbm_ctx* c, Level& lv, std::vector<Box39View>& host, DevBuf<Box39View>& dev) {
+  host.clear();
+  for (auto& bp : lv.boxes) host.push_back(view39(*bp));
+  return cudaMemcpyAsync(dev.p, host.data(), host.size() * sizeof(Box39View), cudaMemcpyHostToDevice, c->stream);
+}
+
+}  // namespace
+
 int elbm_interlevel_setup(elbm_ctx* c, int lvl) {
   Level* fl = get_level(c, lvl);
   Level* cl = lvl >= 1 ? get_level(c, lvl - 1) : nullptr;
   if (!fl || !cl) return fail(c, ELBM_E_ARG, "levels %d and %d must both be registered", lvl - 1, lvl);
+  if (fl->lattice == ELBM_D3Q39 && cl->lattice == ELBM_D3Q39) return interlevel_setup39(c, fl, cl);
   if (fl->lattice != ELBM_D3Q27 || cl->lattice != ELBM_D3Q27 || fl->storage != cl->storage)
-    return fail(c, ELBM_E_UNSUPPORTED, "coarse-fine transfer joins two D3Q27 levels of the same storage");
+    return fail(c, ELBM_E_UNSUPPORTED, "coarse-fine transfer joins two D3Q27 levels of the same storage or two D3Q39 levels");
   if (!fl->links_ready || !cl->links_ready) return fail(c, ELBM_E_STATE, "set the links of both levels first");
   // explosion map: each fine ghost node from the 1, 2, 4 or 8 coarse nodes around it
   std::vector<int32_t> gidx, gsrc;
@@ -1301,6 +1433,32 @@ int elbm_fill_fine_ghosts(elbm_ctx* c, int lvl, int64_t* repaired) {
   if (!fl || !cl) return fail(c, ELBM_E_ARG, "unknown levels");
   if (!fl->il_ready) return fail(c, ELBM_E_STATE, "call elbm_interlevel_setup first");
   CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  if (fl->lattice == ELBM_D3Q39) {
+    for (const auto& bp : cl->boxes)
+      if (!bp->data_set || !bp->macro_set)
+        return fail(c, ELBM_E_STATE, "the coarse level needs its populations and fields (a step, "
+                                     "elbm_upload_macro39 or elbm_init_level39)");
+    for (const auto& bp : fl->boxes)
+      if (!bp->data_set) return fail(c, ELBM_E_STATE, "populations missing on the fine level");
+    CUDA_TRY(cudaMemsetAsync(fl->il39_counters.p, 0, 2 * sizeof(unsigned long long), c->stream), "memset");
+    CUDA_TRY(views39(c, *cl, fl->il39_hcview, fl->il39_cview), "box views");
+    const D3Q39Dev k = dev39(fl->p39, *fl);
+    for (size_t bi = 0; bi < fl->boxes.size(); ++bi) {
+      const int64_t o = fl->il39_goff[bi], n = fl->il39_goff[bi + 1] - o;
+      launch_d3q39_explode(fl->il39_cview.p, view39(*fl->boxes[bi]), fl->il39_ghost.p + o, fl->il39_gsrc.p + 8 * o,
+                           fl->il39_gbox.p + 8 * o, fl->il39_gcnt.p + o, n, k, fl->p39.timestep,
+                           fl->il39_counters.p, c->stream);
+      CUDA_TRY(cudaGetLastError(), "explosion launch");
+    }
+    if (repaired) {
+      unsigned long long r[2] = {0, 0};
+      CUDA_TRY(cudaMemcpyAsync(r, fl->il39_counters.p, sizeof r, cudaMemcpyDeviceToHost, c->stream), "counters");
+      CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+      *repaired = (int64_t)r[0];
+      if (r[1]) return fail(c, ELBM_E_NUMERIC, "%llu ghost-node multiplier solves hit the iteration cap", r[1]);
+    }
+    return ELBM_OK;
+  }
   CUDA_TRY(cudaMemsetAsync(fl->il_repaired.p, 0, sizeof(unsigned long long), c->stream), "memset");
   launch_explode(fl->storage == ELBM_STORE_FP32_DEV, cl->pop[cl->cur].p, cl->plane, fl->pop[fl->cur].p, fl->plane,
                  fl->il_ghost.p, fl->il_src.p, fl->il_cnt.p, fl->il_nghost, fl->il_repaired.p, c->stream);
@@ -1320,6 +1478,16 @@ int elbm_average_down(elbm_ctx* c, int lvl) {
   if (!fl || !cl) return fail(c, ELBM_E_ARG, "unknown levels");
   if (!fl->il_ready) return fail(c, ELBM_E_STATE, "call elbm_interlevel_setup first");
   CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  if (fl->lattice == ELBM_D3Q39) {
+    CUDA_TRY(views39(c, *fl, fl->il39_hfview, fl->il39_fview), "box views");
+    for (size_t bi = 0; bi < cl->boxes.size(); ++bi) {
+      const int64_t o = fl->il39_doff[bi], n = fl->il39_doff[bi + 1] - o;
+      launch_d3q39_average_down(fl->il39_fview.p, view39(*cl->boxes[bi]), fl->il39_ddst.p + o, fl->il39_dsrc.p + o,
+                                fl->il39_dbox.p + o, n, c->stream);
+      CUDA_TRY(cudaGetLastError(), "average-down launch");
+    }
+    return ELBM_OK;
+  }
   launch_average_down(fl->storage == ELBM_STORE_FP32_DEV, fl->pop[fl->cur].p, fl->plane, cl->pop[cl->cur].p, cl->plane,
                       fl->il_down_dst.p, fl->il_down_src.p, fl->il_ndown, c->stream);
   CUDA_TRY(cudaGetLastError(), "average-down launch");
@@ -1530,6 +1698,22 @@ int elbm_set_links39(elbm_ctx* c, int lvl, int box, const int32_t* state, int ng
   lv->fs39[1] = bc->fs_v;
   lv->fs39[2] = bc->fs_w;
   lv->fs39[3] = bc->fs_temp;
+  // node types and fine ghost nodes (state 1e7 .. 1.1e9) for the coarse-fine transfer
+  b->h_ntype = L.ntype;
+  b->h_ghost.clear();
+  {
+    const int g = ngrow_state;
+    const int fx = b->nx + 2 * g, fy = b->ny + 2 * g;
+    for (int z = 0; z < b->nz; ++z)
+      for (int y = 0; y < b->ny; ++y)
+        for (int x = 0; x < b->nx; ++x) {
+          const int64_t n = ((int64_t)z * b->ny + y) * b->nx + x;
+          if (L.ntype[n] != 0 && node_is_ghost(state[((int64_t)(z + g) * fy + (y + g)) * fx + (x + g)]))
+            b->h_ghost.push_back(n);
+        }
+  }
+  lv->il_ready = false;
+  if (lvl + 1 < (int)c->levels.size()) c->levels[lvl + 1].il_ready = false;
   b->links39 = true;
   // until a step has run, a slot that no rule writes holds the node's uploaded fout
   if (b->data_set) launch_stale39_init(*b, c->stream);

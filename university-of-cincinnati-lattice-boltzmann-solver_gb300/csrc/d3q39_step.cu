@@ -716,6 +716,120 @@ __global__ void __launch_bounds__(64) d3q39_init_kernel(const Step39Args a, cons
   a.w_vel[n] = w;
 }
 
+// Explosion into the fine ghost nodes of a D3Q39 level
+// (interlevel_interpolation.f95:364-440), one thread per ghost node:
+// f, g, the 13 multipliers, rho and T from the mean of the 1, 2, 4 or 8 coarse
+// nodes around the node (nodal bilinear at ratio 2; src lists them z-, y-,
+// x-major, sbox their coarse boxes); each population with f < 0, g < 0 or a
+// NaN takes the coarse equilibrium f = f_eq(rho_c, lm_c), g = (2 C_v - D) T_c f;
+// then the moments, the multiplier Newton from the interpolated multipliers
+// and alpha of the node, as the reference does before the collision.
+__global__ void __launch_bounds__(64) d3q39_explode_kernel(const Box39View* __restrict__ cb, const Box39View fb,
+                                                           const int32_t* __restrict__ ghost,
+                                                           const int32_t* __restrict__ src,
+                                                           const uint16_t* __restrict__ sbox,
+                                                           const uint8_t* __restrict__ cnt, int64_t n,
+                                                           const D3Q39Dev k, int step,
+                                                           unsigned long long* __restrict__ counters) {
+  const int64_t gi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= n) return;
+  const int kk = cnt[gi];
+  const double inv = 1.0 / (double)kk;  // kk in {1, 2, 4, 8}: exact
+  auto mean = [&](int which, int comp) {
+    double s = 0.0;
+    for (int m = 0; m < kk; ++m) {
+      const Box39View& B = cb[sbox[8 * gi + m]];
+      const double* p = which == 0 ? B.f : which == 1 ? B.g : which == 2 ? B.lm : B.macro;
+      s += p[(int64_t)comp * B.plane + src[8 * gi + m]];
+    }
+    return s * inv;
+  };
+  double lmc[NL];
+  for (int r = 0; r < NL; ++r) lmc[r] = mean(2, r);
+  const double rho_c = mean(3, 0), temp_c = mean(3, 4);
+  const double lead_c = (2 * k.const_vol - 3) * temp_c;
+  double f[Q], g[Q];
+  bool repaired = false;
+  double rs = 0, us = 0, vs = 0, ws = 0, es = 0;
+  for (int i = 0; i < Q; ++i) {
+    f[i] = mean(0, i);
+    g[i] = mean(1, i);
+    if (!(f[i] >= 0.0) || !(g[i] >= 0.0)) {  // negative or NaN
+      f[i] = fieq39(rho_c, lmc, i);
+      g[i] = f[i] * lead_c;
+      repaired = true;
+    }
+    rs = rs + f[i];
+    us = us + c39.cx[i] * f[i];
+    vs = vs + c39.cy[i] * f[i];
+    ws = ws + c39.cz[i] * f[i];
+    es = es + c39.cmag[i] * f[i] + g[i];
+  }
+  const double rho = rs, u = us / rs, v = vs / rs, w = ws / rs;
+  const double vmag = u * u + v * v + w * w;
+  const double temp = (es - rho * vmag) / (2 * k.const_vol * rho);
+  const double P[6] = {rho * (temp + u * u), rho * (temp + v * v), rho * (temp + w * w),
+                       rho * u * v,          rho * u * w,          rho * v * w};
+  double lm[NL];
+  for (int r = 0; r < NL; ++r) lm[r] = lmc[r];
+  double fe[Q];
+  const int it = lagrange39(k.max_lm_iters, rho, u, v, w, temp, P, lm, fe);
+  if (it < 0)
+    for (int i = 0; i < Q; ++i) fe[i] = fieq39(rho, lm, i);
+  double alpha = 2.0;
+  if (k.turbulent) {
+    double fd[Q];
+    for (int i = 0; i < Q; ++i) fd[i] = fe[i] - f[i];
+    alpha = alpha39(k, f, fd, temp, step);
+  }
+  const int64_t d = ghost[gi];
+  for (int i = 0; i < Q; ++i) {
+    fb.f[(int64_t)i * fb.plane + d] = f[i];
+    fb.g[(int64_t)i * fb.plane + d] = g[i];
+  }
+  for (int r = 0; r < NL; ++r) fb.lm[(int64_t)r * fb.plane + d] = lm[r];
+  fb.w_vel[d] = w;
+  fb.alpha[d] = alpha;
+  const double mv[5] = {rho, u, v, w, temp};
+  for (int r = 0; r < 5; ++r) fb.macro[(int64_t)r * fb.plane + d] = mv[r];
+  if (repaired) atomicAdd(&counters[0], 1ull);
+  if (it < 0) atomicAdd(&counters[1], 1ull);
+}
+
+// Coalescence onto a D3Q39 coarse box (fine_to_coarse.f95:13-45, nodal
+// injection): coarse node dst[p] takes every per-node array of fine node
+// src[p] of fine box sbox[p].  Thread e = component * n + p, so that a warp
+// writes consecutive coarse entries of one plane.
+constexpr int kDownComps39 = 2 * Q + NL + 1 + 1 + 5;  // f, g, lm, w, alpha, rho u v w T
+
+__global__ void d3q39_average_down_kernel(const Box39View* __restrict__ fbs, const Box39View cbx,
+                                          const int32_t* __restrict__ dst, const int32_t* __restrict__ src,
+                                          const uint16_t* __restrict__ sbox, int64_t n) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n * kDownComps39) return;
+  const int c = (int)(e / n);
+  const int64_t p = e - (int64_t)c * n;
+  const Box39View& F = fbs[sbox[p]];
+  const int64_t s = src[p], d = dst[p];
+  const double* from;
+  double* to;
+  int comp;
+  if (c < Q) {
+    from = F.f, to = cbx.f, comp = c;
+  } else if (c < 2 * Q) {
+    from = F.g, to = cbx.g, comp = c - Q;
+  } else if (c < 2 * Q + NL) {
+    from = F.lm, to = cbx.lm, comp = c - 2 * Q;
+  } else if (c == 2 * Q + NL) {
+    from = F.w_vel, to = cbx.w_vel, comp = 0;
+  } else if (c == 2 * Q + NL + 1) {
+    from = F.alpha, to = cbx.alpha, comp = 0;
+  } else {
+    from = F.macro, to = cbx.macro, comp = c - (2 * Q + NL + 2);
+  }
+  to[(int64_t)comp * cbx.plane + d] = from[(int64_t)comp * F.plane + s];
+}
+
 }  // namespace
 
 void launch_d3q39_fp64(const Step39Args& a, cudaStream_t s) {
@@ -833,6 +947,22 @@ void launch_d3q39_walls(const Step39Args& a, cudaStream_t s) {
   if (a.nwall <= 0) return;
   const int threads = 64;
   d3q39_wall_kernel<<<(unsigned)((a.nwall + threads - 1) / threads), threads, 0, s>>>(a);
+}
+
+void launch_d3q39_explode(const Box39View* coarse, const Box39View& fine, const int32_t* ghost, const int32_t* src,
+                          const uint16_t* sbox, const uint8_t* cnt, int64_t n, const D3Q39Dev& k, int step,
+                          unsigned long long* counters, cudaStream_t s) {
+  if (n <= 0) return;
+  const int threads = 64;
+  d3q39_explode_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, s>>>(coarse, fine, ghost, src, sbox,
+                                                                                   cnt, n, k, step, counters);
+}
+
+void launch_d3q39_average_down(const Box39View* fine, const Box39View& coarse, const int32_t* dst, const int32_t* src,
+                               const uint16_t* sbox, int64_t n, cudaStream_t s) {
+  if (n <= 0) return;
+  const int64_t total = n * kDownComps39;
+  d3q39_average_down_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(fine, coarse, dst, src, sbox, n);
 }
 
 

@@ -81,6 +81,17 @@ __host__ __device__ constexpr uint32_t link39(uint32_t kind, int pop, int table,
          ((uint32_t)((dx + 4) + 9 * (dy + 4) + 81 * (dz + 4)) << 13);
 }
 
+// One box's latest D3Q39 state as the coarse-fine transfer reads or writes it.
+struct Box39View {
+  double* f;
+  double* g;
+  double* lm;     // 13 planes
+  double* w_vel;
+  double* alpha;
+  double* macro;  // rho, u, v, w, T planes
+  int64_t plane;
+};
+
 void build_lattice39(int shifted, int primary_flow_dir, Lattice39& L);
 void upload_lattice39(const Lattice39& L, cudaStream_t s);
 void launch_d3q39_fp64(const Step39Args& a, cudaStream_t s);
@@ -91,6 +102,13 @@ void launch_mic_sample(const double* macro, int64_t plane, int nmic, const int32
 void launch_ggm(const double* macro, int64_t plane, int nx, int ny, int nz, int periodic, const uint16_t* mask,
                 int variable, int scheme, const double* fs, double limit, double* gm, double* ggm, uint8_t* tags,
                 unsigned long long* ntag, cudaStream_t s);
+// coarse-fine transfer: coarse / fine are device tables of box views; counters[0] counts ghost
+// nodes with a repaired population, counters[1] multiplier solves that hit the iteration cap
+void launch_d3q39_explode(const Box39View* coarse, const Box39View& fine, const int32_t* ghost, const int32_t* src,
+                          const uint16_t* sbox, const uint8_t* cnt, int64_t n, const D3Q39Dev& k, int step,
+                          unsigned long long* counters, cudaStream_t s);
+void launch_d3q39_average_down(const Box39View* fine, const Box39View& coarse, const int32_t* dst, const int32_t* src,
+                               const uint16_t* sbox, int64_t n, cudaStream_t s);
 // dmask nullptr: a box without link codes (every link interior)
 void launch_d3q39_damp_links(const double* src, double* dst, const unsigned long long* dmask, int nx, int ny, int nz,
                              int64_t plane, int periodic, int shifted, const int* lo, const int* hi, const double* eq,
