@@ -115,14 +115,15 @@ def test_d3q39_link_codes_parity(pkg, o39, built_lib, shifted, outlet_type, side
     ctx.close()
 
 
-def _wall_case(pkg, o39, seed, outlet_type, nx=16, ny=6, nz=8, mach=1.5, wedge=False):
+def _wall_case(pkg, o39, seed, outlet_type, nx=16, ny=6, nz=8, mach=1.5, wedge=False, shifted=True):
     """Shifted D3Q39 box (Mach 1.5 along +x): inlet at x-, outlet at x+, a
     bounce-back floor, a freestream top, periodic in y, and a solid block on
     the floor whose fluid neighbours carry interpolated wall links with random
     wall distances; one wall node also has a null link (target_finder's
     erp(i) = -666 branch).  Random rho, u, v, w, T per node."""
     s39 = pkg.d3q39_setup
-    c = s39.wedge_case_consts(v_inf_ms=mach * math.sqrt(1.4 * s39.GAS_CONST_R * 288.15), use_shifted=True)
+    c = s39.wedge_case_consts(v_inf_ms=mach * math.sqrt(1.4 * s39.GAS_CONST_R * 288.15), use_shifted=shifted)
+    sh = int(c.shifted)
     k = o39.consts(c)
     lm0 = s39.freestream_start_lm(c)
     eq = [o39.init_node(k, r, c.mach, 0.0, 0.0, c.temperature, lm0)[1:3] for r in (1.0, 1.02, 0.98)]
@@ -134,11 +135,11 @@ def _wall_case(pkg, o39, seed, outlet_type, nx=16, ny=6, nz=8, mach=1.5, wedge=F
         # a 20-degree wedge across the span from x = 5 to x = 12, wall distances from the geometry
         st = s39.wedge_state39(nx, ny, nz, 5.0, 12.0, 20.0, faces, periodic=periodic)
     else:
-        st = s39.box_state39(nx, ny, nz, faces, 1, 1, periodic=periodic)
+        st = s39.box_state39(nx, ny, nz, faces, sh, 1, periodic=periodic)
         solid = np.zeros((nz, ny, nx), bool)
         solid[0:3, 1:4, 6:9] = True
-        s39.wall_links39(st, solid, rng.uniform(0.05, 0.95, (39, nz, ny, nx)), 1, 1, periodic=periodic)
-    cx, cy, cz, _ = s39.lattice39(1, 1)
+        s39.wall_links39(st, solid, rng.uniform(0.05, 0.95, (39, nz, ny, nx)), sh, 1, periodic=periodic)
+    cx, cy, cz, _ = s39.lattice39(sh, 1)
     erp = np.array(s39.OPP39) - 1
     for z, y, x, j in zip(*np.nonzero((st[0] >= 0)[None] & (st[1:15] <= -1001))[1:], np.nonzero(
             (st[0] >= 0)[None] & (st[1:15] <= -1001))[0] + 1):
@@ -223,6 +224,38 @@ def test_d3q39_wall_links_parity(pkg, o39, built_lib, seed, outlet_type, mach, w
     macro = out["macro"]
     for m, ref in ((0, lev.rho), (4, lev.temp)):
         assert np.max(np.abs(macro[m][fluid] - ref[fluid]) / np.abs(ref[fluid])) <= tol
+
+
+@pytest.mark.parametrize("seed,outlet_type", [(7, 6), (8, 1)])
+def test_d3q39_unshifted_wall_links_parity(pkg, o39, built_lib, seed, outlet_type):
+    """Interpolated wall links on the unshifted lattice (Mach 0.5): target_finder's
+    unshifted branch, the node's own multipliers as the Newton start, and the
+    hand-expanded closure of interpolative_bounceback_bc for direction opp(i)
+    (from the coefficient tables) written to fout(x, i) and streamed into
+    fi(x, opp(i)); GPU against the oracle's push loop, 1e-12 relative, steps 0..5."""
+    cap = pkg.capi
+    c, k, st, lev, periodic, b, cb = _wall_case(pkg, o39, seed, outlet_type, mach=0.5, shifted=False)
+    assert not c.shifted and (st[1:] <= -1001).any()
+    nz, ny, nx = lev.shape
+    prev_f, prev_g = lev.fout.copy(), lev.gout.copy()
+    fluid = st[0] >= 0
+    steps = 6
+    ctx = cap.Context(0)
+    ctx.level_register(0, cap.ELBM_D3Q39, cap.ELBM_STORE_FP64, [[0, 0, 0, nx - 1, ny - 1, nz - 1]])
+    ctx.set_d3q39_params(0, cap.make_d3q39_params(c, timestep=0, periodic=periodic, damp=0))
+    ctx.set_links39(0, 0, st, cb)
+    ctx.upload39(0, 0, lev.fout, lev.gout, lev.lm, lev.w_vel)
+    ctx.upload_macro39(0, 0, np.stack([lev.rho, lev.u, lev.v, lev.w_vel, lev.temp]))
+    s = ctx.step(0, steps)
+    out = ctx.download39(0)
+    for step in range(steps):
+        so = o39.step_links(k, lev, step, st, periodic, b, prev_f, prev_g)
+    ctx.close()
+    assert np.isfinite(lev.fout[:, fluid]).all()
+    assert s["node_updates"] == steps * fluid.sum() and s["fallbacks"] == 0 and so["lm_capped"] == 0
+    for name, ref in (("fout", lev.fout), ("gout", lev.gout)):
+        rel = np.max(np.abs(out[name][:, fluid] - ref[:, fluid]) / np.abs(ref[:, fluid]))
+        assert rel <= 1e-12, (name, rel)
 
 
 def test_d3q39_wall_links_need_macro(pkg, o39, built_lib):

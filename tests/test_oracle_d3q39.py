@@ -184,3 +184,27 @@ def test_explode_node_known_answers(o39, setup39, shifted):
         assert abs(f3[i] - f[i]) <= 1e-14 * f[i]  # the equilibrium of (rho_c, lm) is the uploaded f
         assert abs(g3[i] - f3[i] * lead) <= 1e-15 * g3[i]
     assert np.array_equal(np.delete(f3, [4, 9]), np.delete(fb, [4, 9]))
+
+
+def test_unshifted_wall_closure_matches_reference_formulas(o39):
+    """The coefficient tables of the unshifted D3Q39 wall closure (generated from
+    interpolative_bounceback_bc.f95:834-2838) evaluated by the oracle against the
+    reference's own statements run in float64 (tests/golden/ibb39_unshifted_golden.json):
+    fi_neq / k_fi and gi_neq / k_gi of all 38 directions, 3 input sets each, to 1e-12."""
+    import ctypes as ct
+    import json
+    import pathlib
+
+    L = o39.lib()
+    L.o39_ibb39_unshifted_terms.restype = None
+    L.o39_ibb39_unshifted_terms.argtypes = [ct.c_int, ct.c_void_p] + [ct.c_double] * 7 + [ct.POINTER(ct.c_double)] * 2
+    gold = json.loads((pathlib.Path(__file__).parent / "golden" / "ibb39_unshifted_golden.json").read_text())
+    assert sorted(int(d) for d in gold) == list(range(1, 39))
+    for d, rows in gold.items():
+        for r in rows:
+            D = np.ascontiguousarray(r["D"], np.float64)
+            fp, gp = ct.c_double(), ct.c_double()
+            L.o39_ibb39_unshifted_terms(int(d), D.ctypes.data, r["u"], r["v"], r["w"], r["T"], r["b1"], r["b2"],
+                                        r["cv"], ct.byref(fp), ct.byref(gp))
+            assert abs(fp.value - r["fpoly"]) <= 1e-12 * abs(r["fpoly"]), (d, fp.value, r["fpoly"])
+            assert abs(gp.value - r["gpoly"]) <= 1e-12 * abs(r["gpoly"]), (d, gp.value, r["gpoly"])

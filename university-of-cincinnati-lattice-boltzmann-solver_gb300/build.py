@@ -49,7 +49,7 @@ def build(verbose: bool = False, force: bool = False) -> pathlib.Path:
     nvcc = _nvcc()
     BUILD.mkdir(exist_ok=True)
     srcs = sources()
-    headers = list(CSRC.glob("*.cuh")) + list((HERE.parent / "include").glob("*.h"))
+    headers = list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + list((HERE.parent / "include").glob("*.h"))
     newest_header = max((h.stat().st_mtime for h in headers), default=0.0)
 
     def compile_one(src: pathlib.Path) -> pathlib.Path:

@@ -13,9 +13,10 @@
 // wins.  A node whose 39 slots all end up as the plain pull fout(y - c_j, j)
 // is a bulk node; the others get 39 link words.
 //
-// Interpolated wall links (codes -1001 - q 1e9, shifted lattice,
-// streaming.f95:478-1133) write a value that the step computes from the
-// node's targets (target_finder.f95, shifted_ibb.f95).  target_finder sums
+// Interpolated wall links (codes -1001 - q 1e9, streaming.f95:478-1133) write
+// a value that the step computes from the node's targets (target_finder.f95,
+// then shifted_ibb.f95 on the shifted lattice or interpolative_bounceback_bc.f95
+// on the unshifted one).  target_finder sums
 // the node's post-streaming slots as the loop has left them at the node's
 // first wall link, so the decoder also records, for such nodes, the last
 // write of every slot up to that point.
@@ -154,8 +155,8 @@ int decode_links39(const int32_t* st, int ngs, int nx, int ny, int nz, int perio
           if (is_wall(c) && i0 < 0) i0 = i;
           if (i < 15 && c < -1000) adjacent = 1;
         }
-        if (i0 >= 0 && !(shifted && pfd == 1)) {
-          why = "interpolated wall links are available on the shifted lattice with primary_flow_dir 1 only";
+        if (i0 >= 0 && shifted && pfd != 1) {
+          why = "interpolated wall links on the shifted lattice need primary_flow_dir 1";
           return ELBM_E_UNSUPPORTED;
         }
         if (i0 >= 0 && adjacent) {
@@ -226,13 +227,15 @@ int decode_links39(const int32_t* st, int ngs, int nx, int ny, int nz, int perio
             continue;
           }
           if (is_wall(c)) {
-            // streaming.f95:482-486 pushes onto a node with state >= 0; shifted_ibb then rewrites
-            // fout(x, opp(i)) and fi(x, opp(i)) = fout(x, i) (opp(i) = i on the shifted lattice)
-            if (t >= 0 && code(0, tx, ty, tz) >= 0) emit(t, i, kpos, fo[i]);
+            // streaming.f95:482-486: the shifted lattice pushes onto a node with state >= 0; the
+            // closure (shifted_ibb, or interpolative_bounceback_bc of direction opp(i) on the
+            // unshifted lattice) rewrites fout(x, i) in place, then fi(x, opp(i)) = fout(x, i)
+            // (opp(i) = i on the shifted lattice)
+            if (shifted && t >= 0 && code(0, tx, ty, tz) >= 0) emit(t, i, kpos, fo[i]);
             fo[i].kind = 3;
             fo[i].pop = (int8_t)i;
             fo[i].node = -1;
-            emit(n, i, kpos + 1, fo[i]);
+            emit(n, L.opp[i], kpos + 1, fo[i]);
             continue;
           }
           if (shifted && t >= 0) emit(t, i, kpos, fo[i]);
@@ -386,9 +389,21 @@ int decode_links39(const int32_t* st, int ngs, int nx, int ny, int nz, int perio
               return ELBM_E_UNSUPPORTED;
             }
           }
-          // target_finder.f95:95-125: velocity and temperature of node x + c_j where link erp(j)
-          // is null, else of node x + c_5 (1-based)
-          for (int j = 1; j < Q39; ++j) {
+          // target_finder.f95:36-58 (unshifted): velocity and temperature of node x + c_opp(j) when
+          // that link is fluid, else of the node itself
+          for (int j = 1; j < Q39 && !shifted; ++j) {
+            if (!is_wall(r.code[j]) || r.code[L.opp[j]] < 0) continue;
+            const int o = L.opp[j];
+            const int64_t m = node_at(x + L.cx[o], y + L.cy[o], z + L.cz[o]);
+            if (m < 0) {
+              why = "target_finder reads the velocity of a node outside the box";
+              return ELBM_E_UNSUPPORTED;
+            }
+            r.upass[o] = (int32_t)m;
+          }
+          // target_finder.f95:95-125 (shifted): velocity and temperature of node x + c_j where link
+          // erp(j) is null, else of node x + c_5 (1-based)
+          for (int j = 1; j < Q39 && shifted; ++j) {
             if (!is_wall(r.code[j])) continue;
             const int src = r.code[L0.opp[j]] == -666 ? j : 4;
             const int64_t m = node_at(x + L.cx[src], y + L.cy[src], z + L.cz[src]);

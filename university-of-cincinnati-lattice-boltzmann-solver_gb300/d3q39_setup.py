@@ -193,13 +193,17 @@ def box_state39(nx: int, ny: int, nz: int, faces: dict, shifted: int, primary_fl
 def wall_links39(state: np.ndarray, solid: np.ndarray, q, shifted: int = 1, primary_flow_dir: int = 1,
                  periodic: int = 0) -> np.ndarray:
     """Mark solid nodes and interpolated wall links in a D3Q39 state array
-    (39, nz, ny, nx), in place, with the shifted lattice's conventions of
-    lbgrid/shifted_state_directions.f95:54-68: a solid node gets node type
-    -1001 and -666 on every link; a fluid node x whose upstream node x - c_i
-    is solid gets, on link i, the code -1001 - floor(q 1e9)
-    (linking/modules/linkwise.f95:45-57), q being the wall distance along the
-    link as a fraction of its length.  q: array (39, nz, ny, nx) or a number."""
+    (39, nz, ny, nx), in place: a solid node gets node type -1001 and -666 on
+    every link; on the shifted lattice (lbgrid/shifted_state_directions.f95:
+    54-68) a fluid node x whose upstream node x - c_i is solid gets, on link i,
+    the code -1001 - floor(q 1e9) (linking/modules/linkwise.f95:45-57), q being
+    the wall distance along the link as a fraction of its length; on the
+    unshifted lattice (lbgrid/state_directions.f95:696) the link i whose
+    downstream node x + c_i is solid gets it.  q: array (39, nz, ny, nx) or a
+    number."""
     cx, cy, cz, _ = lattice39(shifted, primary_flow_dir)
+    if not shifted:
+        cx, cy, cz = -np.asarray(cx), -np.asarray(cy), -np.asarray(cz)
     nz, ny, nx = solid.shape
     state[0][solid] = -1001
     state[1:, solid] = -666
