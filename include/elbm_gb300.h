@@ -234,10 +234,12 @@ typedef struct {
  * lattice) leaves in the post-streaming slot: a population of a node within 4
  * links, a boundary equilibrium, or the slot's value of the previous step.
  * Supported codes: >= 0, -5, -8, -10, -100-k, -200-k, -300-k, -400-k, -666,
- * -1000, and on the shifted lattice with primary_flow_dir 1 the interpolated
- * wall links -1001 - floor(q 1e9) (Grad-type closure of shifted_ibb.f95 with
- * the targets of target_finder.f95; they read the previous step's macroscopic
- * fields, so elbm_upload_macro39 must follow elbm_upload_level39), and the
+ * -1000, the interpolated wall links -1001 - floor(q 1e9) (the targets of
+ * target_finder.f95, then the Grad-type closure of shifted_ibb.f95 on the
+ * shifted lattice with primary_flow_dir 1, or the per-direction closure of
+ * interpolative_bounceback_bc.f95:834-2838 on the unshifted lattice, whose
+ * value of link i is streamed into slot opp(i); they read the previous step's
+ * macroscopic fields, so elbm_upload_macro39 must follow elbm_upload_level39), and the
  * inviscid links -11 / -12 (specular reflection of inviscid_edge.f95: the
  * population goes to the mirror direction at a displaced node; an inviscid
  * link needs a -11 among the node's unit or speed-2 axis links, which the
