@@ -150,10 +150,17 @@ int elbm_upload_level39(elbm_ctx* ctx, int lvl, int box, const double* fout, con
  * downwind_calculation); limit: the level's ggm_tag_limit (the sensitivity
  * times 0.9^lvl, timing_calcs.f95:88-97).  tags (nx*ny*nz bytes, x fastest):
  * 1 where the node's GGM >= limit; ggm (may be NULL): the GGM values;
- * *ntagged (may be NULL): the tagged count.  The predictive splitting
- * option (GGM/PGS) is not included. */
+ * *ntagged (may be NULL): the tagged count. */
 int elbm_ggm_tags(elbm_ctx* ctx, int lvl, int box, int variable, int scheme, double limit, uint8_t* tags, double* ggm,
                   int64_t* ntagged);
+/* The same with predictive splitting (GGM/PGS/predictive_splitter.f95, the
+ * namelist's pgs_on / pgs_reach) after the GGM tags: pgs_sensitivity is the
+ * namelist's ggm_sensitivity (scan hits need ggm >= 2x, the isotropic case
+ * 3x), pgs_reach the scan length in nodes (pgs_max_scan; < 0: no splitting).
+ * The scans stay inside the box (the reference's reach also covers the FAB's
+ * ghost nodes).  *ntagged counts every tag. */
+int elbm_ggm_tags_pgs(elbm_ctx* ctx, int lvl, int box, int variable, int scheme, double limit, double pgs_sensitivity,
+                      int pgs_reach, uint8_t* tags, double* ggm, int64_t* ntagged);
 
 /* Plot3D output of a D3Q39 level from the device buffers, in the
  * reference's layout (output/plot3d_output.f95:77-215): Fortran unformatted

@@ -115,3 +115,56 @@ def ggm_tags(macro, state, periodic, var, scheme, limit, fs):
                 ggm[z, y, x] = grad(gm, 0.0, z, y, x)
                 tags[z, y, x] = 1 if ggm[z, y, x] >= limit else 0
     return tags, ggm, gm
+
+
+def pgs_tags(tags, ggm, macro, state, sensitivity, reach):
+    """Predictive splitting (GGM/PGS/predictive_splitter.f95:36-316) added to tags (in place),
+    the scans kept inside the box.  state (39, nz, ny, nx) or None (node type 0 everywhere)."""
+    _, nz, ny, nx = macro.shape
+    dims = (nx, ny, nz)
+    s0 = np.zeros((nz, ny, nx), np.int64) if state is None else state[0].astype(np.int64)
+    limit, upper = 2 * sensitivity, 3 * sensitivity
+
+    def at(p):
+        return p[2], p[1], p[0]
+
+    def eligible(p):
+        return 0 <= s0[at(p)] < 100000
+
+    for z in range(nz):
+        for y in range(ny):
+            for x in range(nx):
+                if s0[z, y, x] < 0:
+                    continue
+                u, v, w = macro[1:4, z, y, x]
+                p = [x, y, z]
+                lo = [p[a] - reach if p[a] > reach else 0 for a in range(3)]
+                hi = [p[a] + reach if dims[a] - 1 - p[a] > reach else dims[a] - 1 for a in range(3)]
+                if abs(u) > 5 * abs(v) and abs(u) > 5 * abs(w):
+                    ax, vel = 0, u
+                elif abs(v) > 5 * abs(u) and abs(v) > 5 * abs(w):
+                    ax, vel = 1, v
+                elif abs(w) > 5 * abs(v) and abs(w) > 5 * abs(u):
+                    ax, vel = 2, w
+                else:
+                    ax = None
+                if ax is not None:
+                    def pt(q):
+                        r = list(p)
+                        r[ax] = q
+                        return r
+                    scan = range(lo[ax], p[ax] + 1) if vel > 0.0 else range(p[ax], hi[ax] + 1)
+                    hit = next((q for q in scan if eligible(pt(q)) and ggm[at(pt(q))] >= limit), None)
+                    if hit is not None:
+                        a, b = (hit, p[ax]) if vel > 0.0 else (p[ax], hit)
+                        for q in range(a, b + 1):
+                            if s0[at(pt(q))] >= 0:
+                                tags[at(pt(q))] = 1
+                    continue
+                for b in range(3):
+                    for q in range(lo[b], hi[b] + 1):
+                        r = list(p)
+                        r[b] = q
+                        if eligible(r) and ggm[at(r)] >= upper:
+                            tags[at(r)] = 1
+    return tags

@@ -393,6 +393,49 @@ def test_d3q39_ggm_tags(pkg, o39, built_lib, variable, scheme):
     assert np.array_equal(tags, rt) and n == int(rt.sum()) > 0
 
 
+@pytest.mark.parametrize("reach,variable", [(4, 1), (2, 7)])
+def test_d3q39_ggm_predictive_splitting(pkg, o39, built_lib, reach, variable):
+    """Predictive splitting (predictive_splitter.f95) on the device after the GGM tags: the
+    tags equal the GGM tags of the device's own ggm plus the numpy restatement's splitting
+    scans over the same ggm (so that no threshold hangs on 1e-12 differences), on the
+    wedge box, where the flow along +x makes u dominant almost everywhere."""
+    from oracle import ggm as og
+
+    s39, cap = pkg.d3q39_setup, pkg.capi
+    c = s39.wedge_case_consts(v_inf_ms=0.8 * math.sqrt(1.4 * s39.GAS_CONST_R * 288.15), use_shifted=True)
+    nx, ny, nz, periodic = 22, 6, 12, 2
+    faces = {"x-": -101, "x+": -201, "z-": -10, "z+": -1000, "y-": 0, "y+": 0}
+    st = s39.wedge_state39(nx, ny, nz, 6.0, 14.0, 20.0, faces, periodic=periodic)
+    lm0 = s39.freestream_start_lm(c)
+    params = cap.make_d3q39_params(c, timestep=0, periodic=periodic, damp=0)
+    shape = (nz, ny, nx)
+    ctx = cap.Context(0)
+    _, f, g = ctx.d3q39_equilibrium(params, 1.0, c.mach, 0.0, 0.0, c.temperature, lm0)
+    fs = (c.mach, 0.0, 0.0, c.temperature)
+    ctx.level_register(0, cap.ELBM_D3Q39, cap.ELBM_STORE_FP64, [[0, 0, 0, nx - 1, ny - 1, nz - 1]])
+    ctx.set_d3q39_params(0, params)
+    ctx.set_links39(0, 0, st, cap.make_d3q39_bc([1] * 8, [6] + [1] * 7, f, g, [f] * 8, [g] * 8, [f] * 8, [g] * 8, fs))
+    macro = np.stack([np.full(shape, 1.0), np.full(shape, c.mach), np.zeros(shape), np.zeros(shape),
+                      np.full(shape, c.temperature)])
+    ctx.init_level39(0, 0, macro, lm0)
+    ctx.step(0, 4, want_stats=False)
+    m = ctx.download39(0)["macro"]
+    # a small v or w on a few nodes takes them out of the u-dominant branch (the isotropic scan)
+    m[2, :, :, ::5] = 0.5 * m[1, :, :, ::5]
+    ctx.upload_macro39(0, 0, m)
+    _, ggm0, _ = ctx.ggm_tags(0, 0, variable, 0, 1e300)
+    fluid = st[0] >= 0
+    sens = float(np.quantile(ggm0[fluid], 0.9)) / 2.0
+    limit = float(np.quantile(ggm0[fluid], 0.97))
+    tags, ggm, n = ctx.ggm_tags(0, 0, variable, 0, limit, pgs_sensitivity=sens, pgs_reach=reach)
+    base, _, _ = ctx.ggm_tags(0, 0, variable, 0, limit)
+    ctx.close()
+    assert np.array_equal(ggm, ggm0)
+    assert np.array_equal(base, ((ggm0 >= limit) & fluid).astype(np.uint8))
+    ref = og.pgs_tags(base.copy(), ggm0, m, st, sens, reach)
+    assert np.array_equal(tags, ref) and n == int(ref.sum()) > int(base.sum())
+
+
 def _f_records(path):
     """Fortran unformatted sequential records of a file (4-byte length markers)."""
     data = open(path, "rb").read()

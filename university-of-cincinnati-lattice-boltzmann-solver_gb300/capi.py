@@ -163,6 +163,7 @@ SIGNATURES = {
     "elbm_upload_macro39": (_c_int, [_vp, _c_int, _c_int, _vp]),
     "elbm_init_level39": (_c_int, [_vp, _c_int, _c_int, _vp, _vp, _vp]),
     "elbm_ggm_tags": (_c_int, [_vp, _c_int, _c_int, _c_int, _c_int, _c_double, _vp, _vp, _vp]),
+    "elbm_ggm_tags_pgs": (_c_int, [_vp, _c_int, _c_int, _c_int, _c_int, _c_double, _c_double, _c_int, _vp, _vp, _vp]),
     "elbm_write_plot3d": (_c_int, [_vp, _c_int, ct.c_char_p, ct.c_char_p, _vp, _c_double, _vp]),
     "elbm_mic_sample": (_c_int, [_vp, _c_int, _c_int, _c_int, _vp, _vp, _vp]),
     "elbm_checkpoint_write": (_c_int, [_vp, _c_int, ct.c_char_p]),
@@ -367,14 +368,19 @@ class Context:
         arrs = [np.ascontiguousarray(a, np.float64) for a in (fout, gout, lm, w_vel)]
         self._check(self.lib.elbm_upload_level39(self.h, lvl, box, *map(_ptr, arrs)))
 
-    def ggm_tags(self, lvl, box, variable, scheme, limit):
-        """(tags, ggm, ntagged) of a D3Q39 box, arrays (nz, ny, nx)."""
+    def ggm_tags(self, lvl, box, variable, scheme, limit, pgs_sensitivity=None, pgs_reach=-1):
+        """(tags, ggm, ntagged) of a D3Q39 box, arrays (nz, ny, nx); with pgs_sensitivity
+        and pgs_reach >= 0 the predictive splitting tags are added."""
         shp = self.box_shape(lvl, box, ghosts=False)
         tags = np.zeros(shp, np.uint8)
         ggm = np.zeros(shp)
         n = ct.c_int64(0)
-        self._check(self.lib.elbm_ggm_tags(self.h, lvl, box, variable, scheme, limit, _ptr(tags), _ptr(ggm),
-                                           ct.byref(n)))
+        if pgs_sensitivity is None:
+            self._check(self.lib.elbm_ggm_tags(self.h, lvl, box, variable, scheme, limit, _ptr(tags), _ptr(ggm),
+                                               ct.byref(n)))
+        else:
+            self._check(self.lib.elbm_ggm_tags_pgs(self.h, lvl, box, variable, scheme, limit, pgs_sensitivity,
+                                                   pgs_reach, _ptr(tags), _ptr(ggm), ct.byref(n)))
         return tags, ggm, n.value
 
     def write_plot3d(self, lvl, grid_path, data_path, origin, dx, header: Plot3DHeader):

@@ -1978,6 +1978,11 @@ int elbm_mic_sample(elbm_ctx* c, int lvl, int box, int nmic, const int32_t* node
 
 int elbm_ggm_tags(elbm_ctx* c, int lvl, int box, int variable, int scheme, double limit, uint8_t* tags, double* ggm,
                   int64_t* ntagged) {
+  return elbm_ggm_tags_pgs(c, lvl, box, variable, scheme, limit, 0.0, -1, tags, ggm, ntagged);
+}
+
+int elbm_ggm_tags_pgs(elbm_ctx* c, int lvl, int box, int variable, int scheme, double limit, double pgs_sensitivity,
+                      int pgs_reach, uint8_t* tags, double* ggm, int64_t* ntagged) {
   Level* lv = nullptr;
   Box* b = get_box(c, lvl, box, &lv);
   if (!b || !tags) return fail(c, ELBM_E_ARG, "unknown level/box or null tags");
@@ -1988,7 +1993,7 @@ int elbm_ggm_tags(elbm_ctx* c, int lvl, int box, int variable, int scheme, doubl
   if (!b->links39 && !b->gmask39.p) {
     // a box without link codes (periodic on every axis): every link interior
     CUDA_TRY(b->gmask39.alloc(b->N), "ggm links");
-    std::vector<uint16_t> all((size_t)b->N, (uint16_t)((1u << 13) - 1u));
+    std::vector<uint16_t> all((size_t)b->N, (uint16_t)(((1u << 13) - 1u) | (1u << 14)));
     CUDA_TRY(cudaMemcpy(b->gmask39.p, all.data(), b->N * sizeof(uint16_t), cudaMemcpyHostToDevice), "ggm links");
   }
   DevBuf<double> gm, gg;
@@ -2003,11 +2008,20 @@ int elbm_ggm_tags(elbm_ctx* c, int lvl, int box, int variable, int scheme, doubl
   launch_ggm(b->macro.p, b->plane, b->nx, b->ny, b->nz, lv->p39.periodic, b->gmask39.p, variable, scheme, fs, limit,
              gm.p, gg.p, tg.p, cnt.p, c->stream);
   CUDA_TRY(cudaGetLastError(), "ggm launch");
+  if (pgs_reach >= 0) {
+    launch_ggm_pgs(b->macro.p, b->plane, b->nx, b->ny, b->nz, b->gmask39.p, gg.p, pgs_sensitivity, pgs_reach, tg.p,
+                   c->stream);
+    CUDA_TRY(cudaGetLastError(), "pgs launch");
+  }
   unsigned long long h = 0;
   CUDA_TRY(cudaMemcpyAsync(tags, tg.p, b->N, cudaMemcpyDeviceToHost, c->stream), "tags");
   if (ggm) CUDA_TRY(cudaMemcpyAsync(ggm, gg.p, b->N * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "ggm");
   CUDA_TRY(cudaMemcpyAsync(&h, cnt.p, sizeof h, cudaMemcpyDeviceToHost, c->stream), "count");
   CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  if (pgs_reach >= 0) {
+    h = 0;  // predictive splitting adds tags: count them all
+    for (int64_t k = 0; k < b->N; ++k) h += tags[k] != 0;
+  }
   if (ntagged) *ntagged = (int64_t)h;
   return ELBM_OK;
 }

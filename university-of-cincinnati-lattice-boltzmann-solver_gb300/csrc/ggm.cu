@@ -25,7 +25,8 @@ struct GgmArgs {
   const double* macro;  // rho, u, v, w, T planes
   int64_t plane;
   int nx, ny, nz, periodic;
-  const uint16_t* mask;  // per node: bits 0-11 links +1,+2,-1,-2 of x, y, z >= 0; 12 node >= 0; 13 node == -666
+  const uint16_t* mask;  // per node: bits 0-11 links +1,+2,-1,-2 of x, y, z >= 0; 12 node >= 0; 13 node == -666;
+                         // 14: 0 <= node < 100000
   int variable, scheme;  // populate_q variable (1-8); 0 central, 1 up-wind, 2 down-wind
   double fs[5];          // freestream rho, u, v, w, T
 };
@@ -131,6 +132,69 @@ __global__ void ggm_tag_kernel(const GgmArgs a, const double* __restrict__ gm, d
   if (t) atomicAdd(ntag, 1ull);
 }
 
+// Predictive splitting (GGM/PGS/predictive_splitter.f95:36-316), after the GGM tags of
+// the same variable: for a node with state >= 0 whose velocity has a dominant component
+// (|u| > 5|v| and > 5|w|, else v, else w), scan along that axis on the side the flow comes
+// from (u > 0: from pgs_reach nodes upstream, or the box edge, towards the node, taking the
+// farthest hit; u <= 0: from the node outwards, taking the nearest) for a node with
+// 0 <= state < 100000 and ggm >= 2 sensitivity, and tag the nodes with state >= 0 from
+// the hit to the node; with no dominant component, tag every node within pgs_reach on the
+// three axes (both sides) with 0 <= state < 100000 and ggm >= 3 sensitivity.  The scan
+// stays inside the box (the reference's FABs add nghosts ghost nodes to its reach).
+__global__ void ggm_pgs_kernel(const GgmArgs a, const double* __restrict__ ggm, double sens, int reach,
+                               uint8_t* __restrict__ tags) {
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t N = (int64_t)a.nx * a.ny * a.nz;
+  if (n >= N || !((a.mask[n] >> 12) & 1u)) return;
+  const int p3[3] = {(int)(n % a.nx), (int)((n / a.nx) % a.ny), (int)(n / ((int64_t)a.nx * a.ny))};
+  const int dim[3] = {a.nx, a.ny, a.nz};
+  const int64_t stride[3] = {1, a.nx, (int64_t)a.nx * a.ny};
+  const double vel[3] = {a.macro[a.plane + n], a.macro[2 * a.plane + n], a.macro[3 * a.plane + n]};
+  const double pgs_limit = 2 * sens, pgs_upper = 3 * sens;
+  auto eligible = [&](int64_t k) { return ((a.mask[k] >> 14) & 1u) != 0; };
+  auto lo_of = [&](int ax) { return (p3[ax] - 0 > reach) ? p3[ax] - reach : 0; };
+  auto hi_of = [&](int ax) { return (dim[ax] - 1 - p3[ax] > reach) ? p3[ax] + reach : dim[ax] - 1; };
+  int ax = -1;
+  if (fabs(vel[0]) > 5 * fabs(vel[1]) && fabs(vel[0]) > 5 * fabs(vel[2])) ax = 0;
+  else if (fabs(vel[1]) > 5 * fabs(vel[0]) && fabs(vel[1]) > 5 * fabs(vel[2])) ax = 1;
+  else if (fabs(vel[2]) > 5 * fabs(vel[1]) && fabs(vel[2]) > 5 * fabs(vel[0])) ax = 2;
+  const int64_t base = n - (int64_t)p3[ax < 0 ? 0 : ax] * stride[ax < 0 ? 0 : ax];
+  if (ax >= 0) {
+    int hit = -1;
+    if (vel[ax] > 0.0) {
+      for (int q = lo_of(ax); q <= p3[ax]; ++q) {
+        const int64_t k = base + q * stride[ax];
+        if (eligible(k) && ggm[k] >= pgs_limit) {
+          hit = q;
+          break;
+        }
+      }
+      if (hit >= 0)
+        for (int q = hit; q <= p3[ax]; ++q)
+          if ((a.mask[base + q * stride[ax]] >> 12) & 1u) tags[base + q * stride[ax]] = 1;
+    } else {
+      for (int q = p3[ax]; q <= hi_of(ax); ++q) {
+        const int64_t k = base + q * stride[ax];
+        if (eligible(k) && ggm[k] >= pgs_limit) {
+          hit = q;
+          break;
+        }
+      }
+      if (hit >= 0)
+        for (int q = p3[ax]; q <= hit; ++q)
+          if ((a.mask[base + q * stride[ax]] >> 12) & 1u) tags[base + q * stride[ax]] = 1;
+    }
+    return;
+  }
+  for (int b = 0; b < 3; ++b) {
+    const int64_t bb = n - (int64_t)p3[b] * stride[b];
+    for (int q = lo_of(b); q <= hi_of(b); ++q) {
+      const int64_t k = bb + q * stride[b];
+      if (eligible(k) && ggm[k] >= pgs_upper) tags[k] = 1;
+    }
+  }
+}
+
 // mic_write.f95:45-110: per microphone the weighted sums over its 8 nodes of
 // pressure, T, rho, u, v, w (pressure = rho (T + |u|^2 / 2) as the flow variables keep it)
 __global__ void mic_sample_kernel(const double* __restrict__ macro, int64_t plane, int nmic,
@@ -174,6 +238,13 @@ void launch_ggm(const double* macro, int64_t plane, int nx, int ny, int nz, int 
   const unsigned blocks = (unsigned)((N + 255) / 256);
   ggm_gm_kernel<<<blocks, 256, 0, s>>>(a, gm);
   ggm_tag_kernel<<<blocks, 256, 0, s>>>(a, gm, limit, ggm, tags, ntag);
+}
+
+void launch_ggm_pgs(const double* macro, int64_t plane, int nx, int ny, int nz, const uint16_t* mask,
+                    const double* ggm, double sensitivity, int reach, uint8_t* tags, cudaStream_t s) {
+  GgmArgs a{macro, plane, nx, ny, nz, 0, mask, 0, 0, {0, 0, 0, 0, 0}};
+  const int64_t N = (int64_t)nx * ny * nz;
+  ggm_pgs_kernel<<<(unsigned)((N + 255) / 256), 256, 0, s>>>(a, ggm, sensitivity, reach, tags);
 }
 
 }  // namespace elbm

@@ -27,8 +27,8 @@ struct D3Q39Dev {
   double fs_u, fs_v, fs_w, fs_temp;    // freestream velocity and temperature
 };
 
-// A fluid node with interpolated wall links (codes -1001 - q 1e9) on the
-// shifted lattice: what target_finder and shifted_ibb read for it.
+// A fluid node with interpolated wall links (codes -1001 - q 1e9): what
+// target_finder and the wall closure read for it.
 struct Wall39Rec {
   int32_t node;       // box node
   int32_t rec;        // its boundary record
@@ -109,6 +109,8 @@ void launch_d3q39_explode(const Box39View* coarse, const Box39View& fine, const 
                           unsigned long long* counters, cudaStream_t s);
 void launch_d3q39_average_down(const Box39View* fine, const Box39View& coarse, const int32_t* dst, const int32_t* src,
                                const uint16_t* sbox, int64_t n, cudaStream_t s);
+void launch_ggm_pgs(const double* macro, int64_t plane, int nx, int ny, int nz, const uint16_t* mask,
+                    const double* ggm, double sensitivity, int reach, uint8_t* tags, cudaStream_t s);
 // dmask nullptr: a box without link codes (every link interior)
 void launch_d3q39_damp_links(const double* src, double* dst, const unsigned long long* dmask, int nx, int ny, int nz,
                              int64_t plane, int periodic, int shifted, const int* lo, const int* hi, const double* eq,

@@ -20,7 +20,8 @@ struct Links39 {
   // shifted lattice: >= -500), bit 63 node type >= -500
   std::vector<uint64_t> dmask;
   // per node, for the GGM differences: bits 0-11 the links to x+1, x+2, x-1, x-2, then y, z (state
-  // components 2, 16, 5, 19 / 3, 17, 6, 20 / 4, 18, 7, 21, 1-based) >= 0; bit 12 node >= 0; bit 13 node == -666
+  // components 2, 16, 5, 19 / 3, 17, 6, 20 / 4, 18, 7, 21, 1-based) >= 0; bit 12 node >= 0; bit 13 node == -666;
+  // bit 14 0 <= node < 100000 (the cells predictive splitting scans)
   std::vector<uint16_t> gmask;
 };
 
@@ -32,6 +33,7 @@ inline uint16_t ggm_mask39(const int32_t* code) {
     if (code[comp[k]] >= 0) m |= (uint16_t)(1u << k);
   if (code[0] >= 0) m |= 1u << 12;
   if (code[0] == -666) m |= 1u << 13;
+  if (code[0] >= 0 && code[0] < 100000) m |= 1u << 14;
   return m;
 }
 

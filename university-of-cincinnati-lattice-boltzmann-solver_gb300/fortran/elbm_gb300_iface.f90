@@ -64,7 +64,7 @@ module elbm_gb300_iface
     elbm_upload_level_noalloc, elbm_autotune, elbm_set_kernel_variant, elbm_alpha_harvest, &
     elbm_alpha_mlp_train, elbm_set_alpha_mlp, elbm_interlevel_setup, elbm_fill_fine_ghosts, &
     elbm_average_down, elbm_amr_run, elbm_damp_level, elbm_set_links39, elbm_upload_macro39, &
-    elbm_init_level39, elbm_d3q39_equilibrium, elbm_checkpoint_write, elbm_checkpoint_read, elbm_ggm_tags, &
+    elbm_init_level39, elbm_d3q39_equilibrium, elbm_checkpoint_write, elbm_checkpoint_read, elbm_ggm_tags, elbm_ggm_tags_pgs, &
     elbm_write_plot3d, elbm_mic_sample, elbm_mark_triangles_gpu
 
   interface
@@ -143,6 +143,16 @@ module elbm_gb300_iface
       type(c_ptr), value :: ctx
       integer(c_int), value :: lvl, box, variable, scheme
       real(c_double), value :: limit
+      integer(c_int8_t), intent(out) :: tags(*)
+      type(c_ptr), value :: ggm            ! c_loc(ggm values) or c_null_ptr
+      integer(c_int64_t), intent(out) :: ntagged
+    end function
+    integer(c_int) function elbm_ggm_tags_pgs(ctx, lvl, box, variable, scheme, limit, pgs_sensitivity, pgs_reach, &
+        tags, ggm, ntagged) bind(c, name="elbm_ggm_tags_pgs")
+      import :: c_int, c_ptr, c_double, c_int64_t, c_int8_t
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: lvl, box, variable, scheme, pgs_reach
+      real(c_double), value :: limit, pgs_sensitivity
       integer(c_int8_t), intent(out) :: tags(*)
       type(c_ptr), value :: ggm            ! c_loc(ggm values) or c_null_ptr
       integer(c_int64_t), intent(out) :: ntagged
