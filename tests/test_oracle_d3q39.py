@@ -208,3 +208,24 @@ def test_unshifted_wall_closure_matches_reference_formulas(o39):
                                         r["cv"], ct.byref(fp), ct.byref(gp))
             assert abs(fp.value - r["fpoly"]) <= 1e-12 * abs(r["fpoly"]), (d, fp.value, r["fpoly"])
             assert abs(gp.value - r["gpoly"]) <= 1e-12 * abs(r["gpoly"]), (d, gp.value, r["gpoly"])
+
+
+@pytest.mark.parametrize("u,expect", [(0.1, [2, 3, 4, 5]), (-0.1, [0, 1, 2])])
+def test_predictive_splitting_known_answers(u, expect):
+    """predictive_splitter.f95 on a line of 10 nodes with one ggm spike at x = 2, reach 3:
+    flow along +x tags from the spike to every node up to 3 downstream of it; flow along -x
+    tags the nodes up to 3 upstream of the spike (scan from the node outwards)."""
+    from oracle import ggm as og
+
+    nx = 10
+    macro = np.zeros((5, 1, 1, nx))
+    macro[1] = u
+    ggm = np.zeros((1, 1, nx))
+    ggm[0, 0, 2] = 1.0
+    tags = og.pgs_tags(np.zeros((1, 1, nx), np.uint8), ggm, macro, None, 0.4, 3)
+    assert np.nonzero(tags[0, 0])[0].tolist() == expect
+    # no dominant component: only the spike itself, when it reaches 3 x sensitivity
+    macro[2] = u
+    assert og.pgs_tags(np.zeros((1, 1, nx), np.uint8), ggm, macro, None, 0.3, 3)[0, 0].tolist() == \
+        [0, 0, 1] + [0] * 7
+    assert og.pgs_tags(np.zeros((1, 1, nx), np.uint8), ggm, macro, None, 0.4, 3).sum() == 0
