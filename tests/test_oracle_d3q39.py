@@ -229,3 +229,38 @@ def test_predictive_splitting_known_answers(u, expect):
     assert og.pgs_tags(np.zeros((1, 1, nx), np.uint8), ggm, macro, None, 0.3, 3)[0, 0].tolist() == \
         [0, 0, 1] + [0] * 7
     assert og.pgs_tags(np.zeros((1, 1, nx), np.uint8), ggm, macro, None, 0.4, 3).sum() == 0
+
+
+def test_explode39_uniform_coarse_state_is_kept(o39, setup39):
+    """The D3Q39 explosion restatement on a uniform coarse equilibrium: every fine ghost
+    node takes that state unchanged (means of equal values, no population replaced, the
+    multiplier solve converging where it starts, alpha = 2), and the coalescence copies a
+    valid fine node's arrays onto the coarse node under it."""
+    from oracle import interlevel as il
+
+    c = setup39.wedge_case_consts(use_shifted=True, v_inf_ms=0.8 * 340.29)
+    k = o39.consts(c)
+    lm0 = setup39.freestream_start_lm(c)
+    rho, u, T = 1.0, c.mach, c.temperature
+    lm, f, g, _ = o39.init_node(k, rho, u, 0.0, 0.0, T, lm0)
+    shape = (4, 4, 4)
+    coarse = {"f": np.broadcast_to(f[:, None, None, None], (39,) + shape).copy(),
+              "g": np.broadcast_to(g[:, None, None, None], (39,) + shape).copy(),
+              "lm": np.broadcast_to(lm[:, None, None, None], (13,) + shape).copy(),
+              "w": np.zeros(shape), "alpha": np.full(shape, 2.0),
+              "macro": np.broadcast_to(np.array([rho, u, 0.0, 0.0, T])[:, None, None, None], (5,) + shape).copy()}
+    fshape = (5, 5, 5)
+    fine = {"f": np.zeros((39,) + fshape), "g": np.zeros((39,) + fshape), "lm": np.zeros((13,) + fshape),
+            "w": np.ones(fshape), "alpha": np.zeros(fshape), "macro": np.zeros((5,) + fshape)}
+    ghost = np.zeros(fshape, bool)
+    ghost[0] = ghost[-1] = True
+    rep, capped = il.explode39(k, 3, coarse, (0, 0, 0), fine, (1, 1, 1), ghost)
+    assert rep == 0 and capped == 0
+    assert np.allclose(fine["f"][:, ghost], f[:, None], rtol=1e-14, atol=0)
+    assert np.allclose(fine["g"][:, ghost], g[:, None], rtol=1e-14, atol=0)
+    assert np.max(np.abs(fine["lm"][:, ghost] - lm[:, None])) < 1e-7
+    assert np.allclose(fine["alpha"][ghost], 2.0) and np.allclose(fine["macro"][1][ghost], u, rtol=1e-12)
+    assert np.all(fine["f"][:, ~ghost] == 0.0)  # valid fine nodes untouched
+    fine["f"][:, 1, 1, 1] = 7.0  # fine (1,1,1) at global (2,2,2) lies over coarse (1,1,1)
+    il.average_down39(fine, (1, 1, 1), ~ghost, coarse, (0, 0, 0), np.ones(shape, bool))
+    assert np.all(coarse["f"][:, 1, 1, 1] == 7.0) and np.all(coarse["f"][:, 0, 0, 0] == f)
