@@ -309,9 +309,11 @@ int elbm_download_level(elbm_ctx* ctx, int lvl, int box, double* fout);
  * into the library (held by every GPU that loads it, until exit) instead of a
  * cudaMalloc'ed one; boxes needing more than 32 MiB of FP64 populations
  * (27 x nodes x 8 bytes, i.e. more than 155,344 nodes) are rejected with
- * ELBM_E_ARG.  The first call on a device looks the buffer's address up, so
- * make it before any stream capture.  All calls share the buffer: calls that
- * overlap on the GPU race.  The call returns after the copy has finished. */
+ * ELBM_E_ARG.  The buffer is reserved, and its address looked up, when a
+ * context is created on the device (elbm_create), so this call loads nothing
+ * and allocates nothing.  All calls share the buffer and it keeps the last
+ * call's contents (each call overwrites what it reads): calls that overlap on
+ * the GPU race.  The call returns after the copy has finished. */
 int elbm_upload_level_noalloc(elbm_ctx* ctx, int lvl, int box, const double* fout);
 
 /* Per-node alpha of the last step (valid-box layout without ghosts, FP64). */

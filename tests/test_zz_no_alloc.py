@@ -37,9 +37,25 @@ def _fab(geo, nx, ny, nz, g, seed):
     return np.ascontiguousarray(f)
 
 
-def test_noalloc_upload_matches_upload(pkg, built_lib):
+def _free_device_bytes():
+    """cudaMemGetInfo's free bytes of the current device (the CUDA runtime the library uses)."""
+    for name in ("libcudart.so.13", "libcudart.so.12", "libcudart.so"):
+        try:
+            rt = ct.CDLL(name)
+            break
+        except OSError:
+            continue
+    else:
+        pytest.skip("no CUDA runtime library to query free memory")
+    free, total = ct.c_size_t(0), ct.c_size_t(0)
+    assert rt.cudaMemGetInfo(ct.byref(free), ct.byref(total)) == 0
+    return free.value
+
+
+@pytest.mark.parametrize("g", [1, 0])
+def test_noalloc_upload_matches_upload(pkg, built_lib, g):
     cap, geo = pkg.capi, pkg.geometry
-    nx, ny, nz, g = 24, 16, 12, 1
+    nx, ny, nz = 24, 16, 12
     ref = _level(cap, geo, nx, ny, nz, g)
     new = _level(cap, geo, nx, ny, nz, g)
     upload_noalloc = _noalloc_fn(new.lib)
@@ -69,3 +85,27 @@ def test_noalloc_upload_rejects_oversized_box(pkg, built_lib):
     assert rc == cap.ELBM_E_ARG
     assert "at most" in ctx.lib.elbm_last_error_string(ctx.h).decode()
     ctx.close()
+
+
+def test_noalloc_upload_allocates_nothing(pkg, built_lib):
+    """The property the entry point exists for: once the context is created and
+    the level set up, uploads through it leave the device's free memory as it
+    was, while the ordinary upload's first call allocates its staging buffer
+    (which shows that the measurement sees an allocation of this size)."""
+    cap, geo = pkg.capi, pkg.geometry
+    nx, ny, nz = 64, 64, 32  # 131,072 nodes: 28.3 MB of FP64 staging, inside the 32 MiB buffer
+    new = _level(cap, geo, nx, ny, nz, 0)
+    upload_noalloc = _noalloc_fn(new.lib)
+    fab = _fab(geo, nx, ny, nz, 0, 11)
+    free0 = _free_device_bytes()
+    for _ in range(3):
+        rc = upload_noalloc(new.h, 0, 0, fab.ctypes.data_as(ct.c_void_p))
+        assert rc == cap.ELBM_OK, new.lib.elbm_last_error_string(new.h).decode()
+    assert _free_device_bytes() == free0
+    ref = _level(cap, geo, nx, ny, nz, 0)
+    free1 = _free_device_bytes()
+    ref.upload(0, 0, fab)
+    assert free1 - _free_device_bytes() >= nx * ny * nz * 27 * 8
+    assert np.array_equal(ref.download(0, 0), new.download(0, 0))
+    ref.close()
+    new.close()

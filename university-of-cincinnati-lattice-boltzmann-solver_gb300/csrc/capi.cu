@@ -614,6 +614,8 @@ int elbm_create(int device, elbm_ctx** out) {
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return ELBM_E_CUDA;
   if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) return ELBM_E_CUDA;
   if (c->stats.alloc(1) != cudaSuccess) return ELBM_E_CUDA;
+  // reserve the allocation-free upload's staging buffer on this device now (csrc/noalloc.cu)
+  if (noalloc_setup(device) != cudaSuccess) return ELBM_E_CUDA;
   *out = c.release();
   return ELBM_OK;
 }
@@ -1732,6 +1734,9 @@ int elbm_upload_level39(elbm_ctx* c, int lvl, int box, const double* fout, const
   CUDA_TRY(fab_to_packed(gout, (double*)b->gbuf[0].p, *b, lv->ngrow, 39, b->plane, c->stream), "upload g");
   CUDA_TRY(fab_to_packed(lm, b->lm.p, *b, lv->ngrow, 13, b->plane, c->stream), "upload lm");
   CUDA_TRY(fab_to_packed(w_vel, b->w_vel.p, *b, lv->ngrow, 1, b->plane, c->stream), "upload w");
+  // both buffers start identical so that the nodes a step skips (solid) stay defined in either
+  CUDA_TRY(cudaMemcpyAsync(b->buf[1].p, b->buf[0].p, b->buf[0].n, cudaMemcpyDeviceToDevice, c->stream), "copy f");
+  CUDA_TRY(cudaMemcpyAsync(b->gbuf[1].p, b->gbuf[0].p, b->gbuf[0].n, cudaMemcpyDeviceToDevice, c->stream), "copy g");
   CUDA_TRY(cudaMemsetAsync(b->alpha64.p, 0, b->alpha64.n * sizeof(double), c->stream), "alpha");
   if (b->links39) launch_stale39_init(*b, c->stream);
   CUDA_TRY(cudaMemsetAsync(b->macro.p, 0, b->macro.n * sizeof(double), c->stream), "macro");
@@ -1851,6 +1856,16 @@ int elbm_checkpoint_read(elbm_ctx* c, int lvl, const char* path) {
     CUDA_TRY(cudaMemcpy(a.first, host.data(), a.second, cudaMemcpyHostToDevice), "checkpoint upload");
   }
   std::fclose(fp);
+  // the second population buffer takes the same state, as after an upload: a step never
+  // writes the nodes it skips (solid nodes), and reading them from either buffer must agree
+  if (lv->lattice == ELBM_D3Q27) {
+    CUDA_TRY(cudaMemcpy(lv->pop[1].p, lv->pop[0].p, lv->pop[0].n, cudaMemcpyDeviceToDevice), "checkpoint copy");
+  } else {
+    for (auto& bp : lv->boxes) {
+      CUDA_TRY(cudaMemcpy(bp->buf[1].p, bp->buf[0].p, bp->buf[0].n, cudaMemcpyDeviceToDevice), "checkpoint copy f");
+      CUDA_TRY(cudaMemcpy(bp->gbuf[1].p, bp->gbuf[0].p, bp->gbuf[0].n, cudaMemcpyDeviceToDevice), "checkpoint copy g");
+    }
+  }
   if (lv->lattice == ELBM_D3Q39) lv->p39.timestep = h.timestep;
   for (auto& bp : lv->boxes) {
     bp->data_set = true;
@@ -2055,6 +2070,9 @@ int elbm_init_level39(elbm_ctx* c, int lvl, int box, const double* macro, const 
   a.k = dev39(lv->p39, *lv);
   launch_d3q39_init(a, lm0.p, cnt.p, c->stream);
   CUDA_TRY(cudaGetLastError(), "init launch");
+  // both buffers start identical so that the nodes a step skips (solid) stay defined in either
+  CUDA_TRY(cudaMemcpyAsync(b->buf[1].p, b->buf[0].p, b->buf[0].n, cudaMemcpyDeviceToDevice, c->stream), "copy f");
+  CUDA_TRY(cudaMemcpyAsync(b->gbuf[1].p, b->gbuf[0].p, b->gbuf[0].n, cudaMemcpyDeviceToDevice, c->stream), "copy g");
   CUDA_TRY(cudaMemsetAsync(b->alpha64.p, 0, b->alpha64.n * sizeof(double), c->stream), "alpha");
   b->cur = 0;
   b->gcur = 0;

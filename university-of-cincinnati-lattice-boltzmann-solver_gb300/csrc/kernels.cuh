@@ -78,6 +78,10 @@ constexpr int kFp32Variants = 8;
 // a plane or run up to a tile past its end.
 constexpr size_t kPopGuardBytes = 1024;
 
+// Brings the allocation-free upload's module and staging buffer onto `device`
+// (current) and records the buffer's address (csrc/noalloc.cu); elbm_create calls it.
+cudaError_t noalloc_setup(int device);
+
 void launch_d3q27_fp64(const Step27Args& a, cudaStream_t s);
 void upload_alpha_mlp(const float* w_host, cudaStream_t s);
 void launch_d3q27_fp32(const Step27Args& a, cudaStream_t s);

@@ -12,12 +12,24 @@
 // The staging buffer is a file-scope __device__ array of kStageBytes (32 MiB):
 // every GPU that loads the library holds it until the process exits.  Boxes
 // whose FP64 populations (27 x nodes x 8 bytes) exceed it are rejected with
-// ELBM_E_ARG.  The first call on a device looks the buffer's device address up
-// (cudaGetSymbolAddress, with that device current); make that first call
-// before any stream capture.  All calls share the buffer and it keeps the
-// last call's contents; nothing in it needs to start at zero (each call
-// overwrites the part it reads).  Calls that overlap on the GPU, e.g. from
-// two host threads on two contexts of one device, race on the buffer.
+// ELBM_E_ARG.
+//
+// Set-up: this file's device code is a module of its own, and under CUDA's
+// default lazy module loading the module -- and with it the 32 MiB array -- is
+// only brought onto a device when one of its symbols or kernels is first
+// used.  noalloc_setup() does that at context creation (elbm_create, with the
+// context's device current): it looks the array's device address up
+// (cudaGetSymbolAddress) and queries the conversion kernel, so the reservation
+// happens before the caller's arena or time loop starts and no later call
+// loads a module or synchronises the device.  Each context creation refreshes
+// the per-device address; a cudaDeviceReset invalidates every context's
+// device buffers as well, so contexts (and with them the address) are created
+// anew after one.
+//
+// All calls share the buffer and it keeps the last call's contents; nothing in
+// it needs to start at zero (each call overwrites the part it reads).  Calls
+// that overlap on the GPU, e.g. from two host threads on two contexts of one
+// device, race on the buffer.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -49,6 +61,22 @@ __global__ void stage_to_dev32_kernel(const double* __restrict__ f, float* __res
 }  // namespace
 
 namespace elbm {
+
+// Loads this file's module on `device` (current) and records the staging
+// buffer's device address; called by elbm_create.  Returns a CUDA error code.
+cudaError_t noalloc_setup(int device) {
+  if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+  double* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress((void**)&p, g_stage);
+  if (e != cudaSuccess) return e;
+  if (!p) return cudaErrorInvalidSymbol;
+  cudaFuncAttributes attr;
+  e = cudaFuncGetAttributes(&attr, stage_to_dev32_kernel);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(g_stage_mu);
+  g_stage_ptr[device] = p;
+  return cudaSuccess;
+}
 
 // Internal hooks into the context (defined in capi.cu): target buffers of a
 // registered D3Q27 FP32 box and its stream.
@@ -85,15 +113,10 @@ extern "C" int elbm_upload_level_noalloc(elbm_ctx* ctx, int lvl, int box, const 
   double* stage = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_stage_mu);
-    if (!g_stage_ptr[t.device]) {
-      // first call on this device: find the device address of the static buffer
-      double* p = nullptr;
-      const cudaError_t e = cudaGetSymbolAddress((void**)&p, g_stage);
-      if (e != cudaSuccess || !p) return noalloc_fail(ctx, ELBM_E_CUDA, "cudaGetSymbolAddress of the staging buffer failed");
-      g_stage_ptr[t.device] = p;
-    }
     stage = g_stage_ptr[t.device];
   }
+  // elbm_create has set this device up; a context made otherwise is not supported
+  if (!stage) return noalloc_fail(ctx, ELBM_E_STATE, "the staging buffer of this device was not set up");
   // host FAB (ghost width ngrow) -> packed staging: one 3-D copy per population
   const int g = t.ngrow;
   const int fx = t.nx + 2 * g, fy = t.ny + 2 * g, fz = t.nz + 2 * g;
