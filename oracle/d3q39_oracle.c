@@ -360,6 +360,38 @@ static int node_is_fluid39(int32_t s0) {
   return 1;
 }
 
+/* collision.f95:153-300 for one node: equilibria from the node's final
+ * multipliers, heat-flux corrections, beta_1 / beta_2 (quick_calcs.f95,
+ * amr_processes.f95:1751-1785) and the two relaxations. */
+static void collide_node39(const o39_consts* k, const o39_lattice* Lp, const double* f, const double* g,
+                           const double* lm, double rho, double u, double v, double w, double temp, double alpha,
+                           int step, double* fo, double* go) {
+  double fq[Q], fd[Q], gd[Q], qb[Q], ch[Q];
+  const double lead = 2.0 * k->const_vol - 3;
+  for (int i = 0; i < Q; ++i) {
+    fq[i] = fieq39(Lp, rho, lm, i);
+    fd[i] = fq[i] - f[i];
+    gd[i] = lead * temp * fq[i] - g[i];
+  }
+  q_bar(Lp, k, fd, u, v, w, temp, step, qb);
+  little_q_bar(Lp, k, gd, u, v, w, temp, step, ch);
+  double mu, kappa;
+  sutherland(k, temp, &mu, NULL, NULL);
+  therm_cond(k, rho, temp, &kappa);
+  double b1, b2;
+  if (step < k->startup_timesteps) {
+    b1 = k->init_beta_1 + k->beta_1_scaling * step;
+    b2 = k->init_beta_2 + k->beta_2_scaling * step;
+  } else {
+    b1 = 1.0 / ((pow(2.0, k->lvl + 1) * mu) / (rho * temp) + 1.0);
+    b2 = 1.0 / ((2.0 * kappa) / (rho * k->const_press * temp) + 1.0);
+  }
+  for (int i = 0; i < Q; ++i) {
+    fo[i] = f[i] + alpha * b1 * (fd[i] - qb[i]) + b2 * qb[i];
+    go[i] = g[i] + alpha * b1 * (gd[i] - ch[i]) + b2 * ch[i];
+  }
+}
+
 static void collide39(const o39_consts* k, const o39_lattice* Lp, o39_level* s, const double* fi, const double* gi,
                       int step, const int32_t* state, int64_t* lm_iters_out, int64_t* capped_out, int64_t* not2_out) {
   const o39_lattice L = *Lp;
@@ -408,29 +440,11 @@ static void collide39(const o39_consts* k, const o39_lattice* Lp, o39_level* s, 
     const double alpha = k->turbulent ? o39_alpha(k, f, fd, temp, step) : 2.0;
     if (alpha != 2.0) not2++;
     /* collision with the stored (final) multipliers */
-    double fq[Q], gd[Q], qb[Q], ch[Q];
-    const double lead = 2.0 * k->const_vol - 3;
+    double fo[Q], go[Q];
+    collide_node39(k, &L, f, g, lm, rho, u, v, w, temp, alpha, step, fo, go);
     for (int i = 0; i < Q; ++i) {
-      fq[i] = fieq39(&L, rho, lm, i);
-      fd[i] = fq[i] - f[i];
-      gd[i] = lead * temp * fq[i] - g[i];
-    }
-    q_bar(&L, k, fd, u, v, w, temp, step, qb);
-    little_q_bar(&L, k, gd, u, v, w, temp, step, ch);
-    double mu, kappa;
-    sutherland(k, temp, &mu, NULL, NULL);
-    therm_cond(k, rho, temp, &kappa);
-    double b1, b2;
-    if (step < k->startup_timesteps) {
-      b1 = k->init_beta_1 + k->beta_1_scaling * step;
-      b2 = k->init_beta_2 + k->beta_2_scaling * step;
-    } else {
-      b1 = 1.0 / ((pow(2.0, k->lvl + 1) * mu) / (rho * temp) + 1.0);
-      b2 = 1.0 / ((2.0 * kappa) / (rho * k->const_press * temp) + 1.0);
-    }
-    for (int i = 0; i < Q; ++i) {
-      s->fout[(int64_t)i * N + n] = f[i] + alpha * b1 * (fd[i] - qb[i]) + b2 * qb[i];
-      s->gout[(int64_t)i * N + n] = g[i] + alpha * b1 * (gd[i] - ch[i]) + b2 * ch[i];
+      s->fout[(int64_t)i * N + n] = fo[i];
+      s->gout[(int64_t)i * N + n] = go[i];
     }
     for (int r = 0; r < NLM; ++r) s->lm[(int64_t)r * N + n] = lm[r];
     s->w_vel[n] = w;
@@ -1325,4 +1339,54 @@ int o39_step_links_damp(const o39_consts* k, o39_level* s, int step, o39_stats* 
   o39_lattice_init(&L, k->shifted, k->primary_flow_dir);
   st->damped = damp39_links(k, &L, s->fout, state, s->nx, s->ny, s->nz, periodic, lo, hi, bc->fs_fieq);
   return 0;
+}
+
+/* Exposed for the golden fixtures run from the reference's own statements
+ * (tests/golden/make_d3q39_core_golden.py): the pieces of the multiplier
+ * solve, the heat-flux corrections and the two-population collision of one
+ * node, each on given inputs. */
+void o39_fieq_api(int shifted, int primary_flow_dir, double rho, const double* lm, double* out) {
+  o39_lattice L;
+  o39_lattice_init(&L, shifted, primary_flow_dir);
+  for (int i = 0; i < Q; ++i) out[i] = fieq39(&L, rho, lm, i);
+}
+
+/* Jacobian of one Newton iteration from that iteration's expo (row-major 13 x 13). */
+void o39_jacobian_api(int shifted, int primary_flow_dir, const double* expo, double* J) {
+  o39_lattice L;
+  o39_lattice_init(&L, shifted, primary_flow_dir);
+  for (int r = 0; r < NLM; ++r)
+    for (int c = 0; c < NLM; ++c) {
+      double s = 0.0;
+      for (int i = 0; i < Q; ++i) s += (double)(L.phi[r][i] * L.phi[c][i]) * expo[i];
+      J[r * NLM + c] = s;
+    }
+}
+
+/* One LU update: lm -= J^-1 (J[0][.] - target), returns max |delta|. */
+double o39_lu_api(const double* J, const double* target, double* lm) {
+  double Jm[NLM][NLM];
+  memcpy(Jm, J, sizeof Jm);
+  return lu_update(Jm, target, lm);
+}
+
+void o39_q_bar_api(const o39_consts* k, const double* fd, double u, double v, double w, double T, int step,
+                   double* out) {
+  o39_lattice L;
+  o39_lattice_init(&L, k->shifted, k->primary_flow_dir);
+  q_bar(&L, k, fd, u, v, w, T, step, out);
+}
+
+void o39_little_q_bar_api(const o39_consts* k, const double* gd, double u, double v, double w, double T, int step,
+                          double* out) {
+  o39_lattice L;
+  o39_lattice_init(&L, k->shifted, k->primary_flow_dir);
+  little_q_bar(&L, k, gd, u, v, w, T, step, out);
+}
+
+void o39_collide_node_api(const o39_consts* k, const double* f, const double* g, const double* lm, double rho,
+                          double u, double v, double w, double temp, double alpha, int step, double* fo, double* go) {
+  o39_lattice L;
+  o39_lattice_init(&L, k->shifted, k->primary_flow_dir);
+  collide_node39(k, &L, f, g, lm, rho, u, v, w, temp, alpha, step, fo, go);
 }

@@ -253,3 +253,65 @@ def step_links_damp(k: O39Consts, lev: Level39, step: int, state: np.ndarray, pe
     if rc != 0:
         raise RuntimeError(f"o39 link step failed {rc}")
     return {n: getattr(st, n) for n, _ in st._fields_}
+
+
+# ---- pieces of the step, for the golden fixtures run from the reference's statements ----
+def _pieces():
+    L = lib()
+    if not getattr(L, "_o39_pieces", False):
+        vp, d, i = ct.c_void_p, ct.c_double, ct.c_int
+        L.o39_fieq_api.restype = None
+        L.o39_fieq_api.argtypes = [i, i, d, vp, vp]
+        L.o39_jacobian_api.restype = None
+        L.o39_jacobian_api.argtypes = [i, i, vp, vp]
+        L.o39_lu_api.restype = d
+        L.o39_lu_api.argtypes = [vp, vp, vp]
+        L.o39_q_bar_api.restype = None
+        L.o39_q_bar_api.argtypes = [ct.POINTER(O39Consts), vp, d, d, d, d, i, vp]
+        L.o39_little_q_bar_api.restype = None
+        L.o39_little_q_bar_api.argtypes = [ct.POINTER(O39Consts), vp, d, d, d, d, i, vp]
+        L.o39_collide_node_api.restype = None
+        L.o39_collide_node_api.argtypes = [ct.POINTER(O39Consts), vp, vp, vp, d, d, d, d, d, d, i, vp, vp]
+        L._o39_pieces = True
+    return L
+
+
+def _a(x):
+    return np.ascontiguousarray(x, np.float64)
+
+
+def fieq(shifted, pfd, rho, lm):
+    out = np.zeros(Q39)
+    _pieces().o39_fieq_api(shifted, pfd, rho, _p(_a(lm)), _p(out))
+    return out
+
+
+def jacobian(shifted, pfd, expo):
+    J = np.zeros(NLM * NLM)
+    _pieces().o39_jacobian_api(shifted, pfd, _p(_a(expo)), _p(J))
+    return J.reshape(NLM, NLM)
+
+
+def lu_update(J, target, lm):
+    lm = _a(lm).copy()
+    md = _pieces().o39_lu_api(_p(_a(J)), _p(_a(target)), _p(lm))
+    return lm, md
+
+
+def q_bar(k: O39Consts, fd, u, v, w, T, step):
+    out = np.zeros(Q39)
+    _pieces().o39_q_bar_api(ct.byref(k), _p(_a(fd)), u, v, w, T, step, _p(out))
+    return out
+
+
+def little_q_bar(k: O39Consts, gd, u, v, w, T, step):
+    out = np.zeros(Q39)
+    _pieces().o39_little_q_bar_api(ct.byref(k), _p(_a(gd)), u, v, w, T, step, _p(out))
+    return out
+
+
+def collide_node(k: O39Consts, f, g, lm, rho, u, v, w, T, alpha, step):
+    fo, go = np.zeros(Q39), np.zeros(Q39)
+    _pieces().o39_collide_node_api(ct.byref(k), _p(_a(f)), _p(_a(g)), _p(_a(lm)), rho, u, v, w, T, alpha, step,
+                                   _p(fo), _p(go))
+    return fo, go

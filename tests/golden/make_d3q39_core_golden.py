@@ -1,0 +1,278 @@
+"""Golden values of the D3Q39 core, run straight from the reference's own
+Fortran statements (tests/golden/f95_subset.py interprets them in float64):
+
+  lattice tables        general/background_calcs/directions_and_weights.f95 (D3Q39 branch)
+  equilibrium           amr/modules/amr_processes.f95 fieq_comp_39, fieq_comp_39_shifted
+  multiplier solve      looping/timestepping/lagrangian_multipliers/calculate_lagrangian_mults.f95
+                        (unshifted hand-expanded Jacobian :341-695, shifted generic :696-1097)
+  LU update             looping/timestepping/lagrangian_multipliers/lu_decomp.f95 (both index quirks)
+  closed-form alpha     looping/timestepping/calculate_alpha.f95
+  heat-flux corrections looping/timestepping/component_subroutines/find_q_bar.f95, find_little_q_bar.f95
+  collision of a node   looping/timestepping/collision.f95 (the body of the per-node loop)
+  transport             utilities/modules/quick_calcs.f95, amr_processes.f95 beta_1/2_calculator,
+                        epsilon_calculator
+
+Each case records its inputs and the reference's outputs; tests/test_oracle_d3q39_golden.py
+runs the oracle's restatement on the same inputs.  The constants of a case (reference scales,
+relaxation ramps) come from the package's host set-up of the wedge case (d3q39_setup), which
+restates basic_fluids_calcs / viscosity_and_timing; they are inputs here and are stored with the
+case.
+
+Run: python make_d3q39_core_golden.py <reference root>   (writes d3q39_core_golden.json)
+"""
+from __future__ import annotations
+
+import importlib.util
+import json
+import math
+import pathlib
+import re
+import sys
+
+import numpy as np
+
+HERE = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE))
+import f95_subset as F  # noqa: E402
+
+PKG = HERE.parents[1] / "university-of-cincinnati-lattice-boltzmann-solver_gb300"
+
+CONST_FIELDS = ("shifted", "primary_flow_dir", "turbulent", "lvl", "startup_timesteps", "max_lm_iters", "gama",
+                "t_ref", "rho_ref", "p_ref", "mu_ref", "kappa_ref", "gas_const_R", "const_vol", "const_press",
+                "molec_weight", "dt", "elbm_epsilon", "init_beta_1", "init_beta_2", "beta_1_scaling",
+                "beta_2_scaling")
+LM_NAMES = ("chi", "zeta_x", "zeta_y", "zeta_z", "pi_xx", "pi_yy", "pi_zz", "pi_xy", "pi_xz", "pi_yz", "lambda_x",
+            "lambda_y", "lambda_z")
+
+
+def _setup_module():
+    spec = importlib.util.spec_from_file_location("d3q39_setup", PKG / "d3q39_setup.py")
+    m = importlib.util.module_from_spec(spec)
+    sys.modules["d3q39_setup"] = m
+    spec.loader.exec_module(m)
+    return m
+
+
+def _module_values(path: pathlib.Path, out: dict):
+    """Initialised module variables and PARAMETERs of a module file, in order."""
+    interp = F.Interp({}, {})
+    sc = F.ChainMap(out, F.INTRINSICS)
+    for no, s in F.logical_lines(path.read_text()):
+        if "::" in s and "=" in s.split("::", 1)[1] and F._DECL.match(s):
+            interp.declare(s, out, sc, set())
+
+
+def _int_arrays(*paths):
+    """Names of the INTEGER allocatable arrays declared in module files."""
+    names = set()
+    for p in paths:
+        for no, s in F.logical_lines(p.read_text()):
+            m = re.match(r"^integer\b[^:]*allocatable[^:]*::(.*)$", s)
+            if m:
+                for item in F.split_top(m.group(1)):
+                    names.add(re.match(r"(\w+)", item).group(1))
+    return names
+
+
+class Reference:
+    """The reference's routines with the module state of one lattice and case."""
+
+    def __init__(self, root: pathlib.Path, c, shifted: bool):
+        R = root
+        files = [R / "amr/modules/amr_processes.f95",
+                 R / "looping/timestepping/lagrangian_multipliers/calculate_lagrangian_mults.f95",
+                 R / "looping/timestepping/lagrangian_multipliers/lu_decomp.f95",
+                 R / "looping/timestepping/calculate_alpha.f95",
+                 R / "looping/timestepping/component_subroutines/find_q_bar.f95",
+                 R / "looping/timestepping/component_subroutines/find_little_q_bar.f95",
+                 R / "utilities/modules/quick_calcs.f95",
+                 R / "general/background_calcs/directions_and_weights.f95"]
+        wanted = {"fieq_comp_39", "fieq_comp_39_shifted", "beta_1_calculator", "beta_2_calculator",
+                  "epsilon_calculator", "calculate_lagrangian_mults", "lu_decomp", "calculate_alpha", "find_q_bar",
+                  "find_little_q_bar", "quick_sutherlands", "quick_therm_cond", "directions_and_weights"}
+        self.procs = {}
+        for p in files:
+            self.procs.update(F.parse_units(F.logical_lines(p.read_text()), only=wanted))
+        missing = wanted - set(self.procs)
+        if missing:
+            raise RuntimeError(f"reference routines not found: {sorted(missing)}")
+        g = {"dp": F.FInt(8), "sp": F.FInt(4)}
+        _module_values(R / "general/modules/precise.f95", g)
+        _module_values(R / "general/modules/constants.f95", g)
+        # case values of the modules (constants, timing, amr_info_holder, grid_data, namelists)
+        g.update(dimensions=F.FInt(3), primary_flow_dir=F.FInt(c.primary_flow_dir), gama=c.gama, t_ref=c.t_ref,
+                 rho_ref=c.rho_ref, p_ref=c.p_ref, mu_ref=c.mu_ref, kappa_ref=c.kappa_ref, gas_const_r=c.gas_const_R,
+                 const_vol=c.const_vol, const_press=c.const_press, molec_weight=c.molec_weight,
+                 init_beta_1=c.init_beta_1, init_beta_2=c.init_beta_2, beta_1_scaling=c.beta_1_scaling,
+                 beta_2_scaling=c.beta_2_scaling, startup_timesteps=F.FInt(c.startup_timesteps),
+                 self=F.FInt(0), amr_max_lvl=F.FInt(0), mach=(1.5 if shifted else 0.5), use_shifted=bool(shifted),
+                 shifted=bool(shifted), turbulent=True,
+                 dt=F.FArray(np.array([c.dt]), [0]), elbm_epsilon=F.FArray(np.array([c.elbm_epsilon]), [0]),
+                 timestep=F.FArray(np.array([0], np.int64), [0]))
+        g["__int_arrays"] = _int_arrays(R / "linking/modules/linkwise.f95") | {"opp"}
+        self.interp = F.Interp(self.procs, g)
+        self.g = g
+        self.interp.call("directions_and_weights", [])
+        assert int(g["dir"]) == 39 and bool(g["shifted"]) == bool(shifted)
+        self.lu_log = []
+        real_lu = self.real_lu = self.procs["lu_decomp"]
+
+        def val(a):
+            return a.get() if isinstance(a, F.Ref) else a
+
+        def lu_hook(*acts):
+            jac = np.array(val(acts[0]).a, copy=True)
+            moments = [float(val(a)) for a in acts[2:15]]
+            lm_in = [float(val(r)) for r in acts[15:28]]
+            self.interp.call_proc(real_lu, list(acts))
+            lm_out = [float(val(r)) for r in acts[15:28]]
+            self.lu_log.append({"jacobian": jac.ravel().tolist(), "moments": moments, "lm_in": lm_in,
+                                "lm_out": lm_out, "max_diff": float(val(acts[28]))})
+            if len(self.lu_log) > 200:
+                raise RuntimeError("multiplier solve did not converge in 200 iterations")
+
+        self.procs["lu_decomp"] = lu_hook
+
+    def set_step(self, step: int):
+        self.g["timestep"].set((0,), step)
+
+    def tables(self):
+        return {k: [int(v) for v in self.g[k].a] for k in ("cx", "cy", "cz", "opp")}
+
+    def fieq(self, rho, lm):
+        name = "fieq_comp_39_shifted" if self.g["shifted"] else "fieq_comp_39"
+        return [float(self.interp.call(name, [rho] + list(lm) + [F.FInt(i)])) for i in range(1, 40)]
+
+    def lagrange(self, rho, u, v, w, T, P, lm0):
+        self.lu_log = []
+        lm = {n: float(x) for n, x in zip(LM_NAMES, lm0)}
+        fe = F.FArray(np.full(39, np.nan))
+        acts = [rho, u, v, w, T] + list(P) + [F.Ref(lm, n) for n in LM_NAMES] + [fe, F.FInt(1), F.FInt(1),
+                                                                                   F.FInt(1)]
+        self.interp.call("calculate_lagrangian_mults", acts)
+        return [lm[n] for n in LM_NAMES], fe.a.tolist(), list(self.lu_log)
+
+    def alpha(self, fi, fd, T):
+        out = {"a": float("nan")}
+        fi4 = F.FArray(np.asarray(fi, np.float64).reshape(1, 1, 1, 39), [1, 1, 1, 1])
+        self.interp.call("calculate_alpha", [fi4, F.FArray(np.asarray(fd, np.float64)), F.Ref(out, "a"), T,
+                                             F.FInt(0), F.FInt(0), F.FInt(1), F.FInt(1), F.FInt(1)])
+        return out["a"]
+
+    def q_bar(self, fd, fe, u, v, w, T):
+        qb = F.FArray(np.full(39, np.nan))
+        self.interp.call("find_q_bar", [F.FArray(np.asarray(fd, np.float64)), F.FArray(np.asarray(fe, np.float64)),
+                                        qb, u, v, w, T, F.FInt(0)])
+        return qb.a.tolist()
+
+    def little_q_bar(self, gd, u, v, w, T):
+        ch = F.FArray(np.full(39, np.nan))
+        self.interp.call("find_little_q_bar", [F.FArray(np.asarray(gd, np.float64)), u, v, w, T, ch, F.FInt(0)])
+        return ch.a.tolist()
+
+    def collide(self, root, f, g, lm, rho, u, v, w, T, alpha):
+        """The body of collision.f95's per-node loop for one node (a = b = c = 1)."""
+        lines = F.logical_lines((root / "looping/timestepping/collision.f95").read_text())
+        i0 = next(k for k, (no, s) in enumerate(lines) if re.match(r"^if\s*\(state\(a,b,c,1\)\s*<\s*0\)\s*cycle", s))
+        body, _ = F.parse_block(lines, i0, r"^end\s*do")
+        k_lead = next(k for k, (no, s) in enumerate(lines) if s.startswith("lead_gieq_const"))
+        # the routine's declarations, then its set-up statement lead_gieq_const = 2 C_v - D (collision.f95:73)
+        local = {}
+        scope = self.interp.scope_for(local)
+        for no, s in lines[1:k_lead]:
+            if F._DECL.match(s):
+                self.interp.declare(s, local, scope, set())
+        for name in ("loc_fieq", "loc_gieq", "loc_fi_diff", "q_bar_dir", "contr_heat_flux", "loc_gi_diff",
+                     "old_fout"):
+            local[name] = F.FArray(np.full(39, np.nan))
+        self.interp.run([F.parse_stmt(lines, k_lead)[0]], local, scope)
+
+        def node_arr(vals):
+            a = np.asarray(vals, np.float64).reshape(1, 1, 1, -1)
+            return F.FArray(a.copy(), [1, 1, 1, 1])
+
+        local.update(a=F.FInt(1), b=F.FInt(1), c=F.FInt(1), lvl=F.FInt(0),
+                     state=F.FArray(np.zeros((1, 1, 1, 39), np.int64), [1, 1, 1, 1]),
+                     fi=node_arr(f), gi=node_arr(g), fout=node_arr(np.full(39, np.nan)),
+                     gout=node_arr(np.full(39, np.nan)), rho=node_arr([rho]), u_vel=node_arr([u]),
+                     v_vel=node_arr([v]), w_vel=node_arr([w]), temp=node_arr([T]), alpha=node_arr([alpha]))
+        for n, x in zip(LM_NAMES, lm):
+            local[n] = node_arr([x])
+        try:
+            self.interp.run(body, local, scope)
+        except F._Cycle:
+            raise RuntimeError("the node was skipped")
+        return local["fout"].a.ravel().tolist(), local["gout"].a.ravel().tolist()
+
+
+def case_consts(s39, shifted: bool):
+    if shifted:
+        c = s39.wedge_case_consts()
+    else:
+        c = s39.wedge_case_consts(v_inf_ms=0.5 * math.sqrt(1.4 * s39.GAS_CONST_R * 288.15), use_shifted=False)
+    # a Knudsen-scale epsilon large enough that the heat-flux corrections show in every population
+    c.elbm_epsilon = 0.37
+    return c
+
+
+def main(root: pathlib.Path) -> None:
+    s39 = _setup_module()
+    rng = np.random.default_rng(20241204)
+    out = {"lattices": {}}
+    for shifted in (True, False):
+        c = case_consts(s39, shifted)
+        ref = Reference(root, c, shifted)
+        lat = {"consts": {k: getattr(c, k) for k in CONST_FIELDS}, "su_lm": list(c.su_lm),
+               "tables": ref.tables(), "cases": []}
+        lat["consts"]["shifted"] = int(shifted)
+        lm_start = s39.freestream_start_lm(c)
+        for k in range(3):
+            rho = float(rng.uniform(0.92, 1.08))
+            u = float(c.mach * rng.uniform(0.9, 1.1))
+            v, w = (float(x) for x in rng.uniform(-0.25, 0.25, 2))
+            T = float(c.temperature * rng.uniform(0.95, 1.05))
+            P = [rho * (T + u * u) * rng.uniform(0.995, 1.005), rho * (T + v * v) * rng.uniform(0.995, 1.005),
+                 rho * (T + w * w) * rng.uniform(0.995, 1.005), rho * u * v + rng.uniform(-1e-3, 1e-3),
+                 rho * u * w + rng.uniform(-1e-3, 1e-3), rho * v * w + rng.uniform(-1e-3, 1e-3)]
+            P = [float(x) for x in P]
+            lm, fe, lus = ref.lagrange(rho, u, v, w, T, P, lm_start)
+            expo0 = ref.fieq(rho, lus[0]["lm_in"])
+            # a non-equilibrium node around the solved equilibrium
+            f = (np.asarray(fe) * (1.0 + rng.uniform(-0.03, 0.03, 39))).tolist()
+            lead = 2.0 * c.const_vol - 3
+            g = (lead * T * np.asarray(fe) * (1.0 + rng.uniform(-0.03, 0.03, 39))).tolist()
+            fd = (np.asarray(fe) - np.asarray(f)).tolist()
+            gd = (lead * T * np.asarray(fe) - np.asarray(g)).tolist()
+            steps = {}
+            for step in (3, c.startup_timesteps + 7):
+                ref.set_step(step)
+                a = ref.alpha(f, fd, T)
+                fo, go = ref.collide(root, f, g, lm, rho, u, v, w, T, a)
+                steps[str(step)] = {"alpha": a, "q_bar": ref.q_bar(fd, fe, u, v, w, T),
+                                    "little_q_bar": ref.little_q_bar(gd, u, v, w, T), "fout": fo, "gout": go}
+            lat["cases"].append({
+                "rho": rho, "u": u, "v": v, "w": w, "T": T, "P": P, "lm0": list(lm_start),
+                "lm": lm, "fieq": fe, "iterations": len(lus), "expo0": expo0, "lu": lus[:2],
+                "f": f, "g": g, "fd": fd, "gd": gd, "steps": steps})
+        out["lattices"]["shifted" if shifted else "unshifted"] = lat
+    # lu_decomp on dense, diagonally dominant matrices, where both index quirks change the result at O(1)
+    recs = []
+    for k in range(4):
+        J = rng.uniform(-1.0, 1.0, (13, 13)) + np.eye(13) * 6.0
+        moments = [float(x) for x in rng.uniform(-1.0, 1.0, 13)]
+        lm = {n: float(x) for n, x in zip(LM_NAMES, rng.uniform(-1.0, 1.0, 13))}
+        lm_in = [lm[n] for n in LM_NAMES]
+        md = {"v": 0.0}
+        jac = F.FArray(J.copy())
+        ref.interp.call_proc(ref.real_lu, [jac, F.FInt(13)] + moments + [F.Ref(lm, n) for n in LM_NAMES] +
+                             [F.Ref(md, "v")])
+        recs.append({"jacobian": J.ravel().tolist(), "moments": moments, "lm_in": lm_in,
+                     "lm_out": [lm[n] for n in LM_NAMES], "max_diff": md["v"]})
+    out["lu_dense"] = recs
+    (HERE / "d3q39_core_golden.json").write_text(json.dumps(out))
+
+
+if __name__ == "__main__":
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_d3q39_core_golden.py <reference root>")
+    main(pathlib.Path(sys.argv[1]))
