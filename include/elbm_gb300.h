@@ -377,17 +377,23 @@ int elbm_damp_level(elbm_ctx* ctx, int lvl, int64_t* repaired);
 
 /* Time every variant of the level's step kernel on its current state (reps
  * launches each, the state does not advance) and keep the fastest for
- * elbm_level_step.  chosen and ms_per_variant (room for 8) may be NULL.  The
- * reference has no counterpart (it has one code path per lattice). */
+ * elbm_level_step.  chosen and ms_per_variant (room for ELBM_KERNEL_VARIANTS)
+ * may be NULL.  The reference has no counterpart (it has one code path per
+ * lattice). */
+#define ELBM_KERNEL_VARIANTS 9
 int elbm_autotune(elbm_ctx* ctx, int lvl, int reps, int* chosen, double* ms_per_variant);
 
 /* Use kernel variant v (0: direct loads; 1, 4, 5, 6, 7: direct, registers
  * capped for 4, 5, 6, 8, 7 blocks of 128 threads per SM; 2: rows staged in
  * shared memory by bulk copies, persistent; 3: direct loads, persistent warps
- * taking 32-node chunks from a counter) for
- * the level's FP32 D3Q27 steps, instead of the autotuner's choice.  Variant 2
- * applies to boxes with nx and the plane size multiples of 4 and ny, nz >= 3;
- * other boxes fall back to variant 0.  No counterpart in the reference. */
+ * taking 32-node chunks from a counter; 8: warp-specialised, a producer warp
+ * keeps tensor copies (TMA) of 256-node tiles in flight into a shared-memory
+ * ring while eight consumer warps collide) for the level's FP32 D3Q27 steps,
+ * instead of the autotuner's choice.  Variant 2 applies to boxes with nx and
+ * the plane size multiples of 4 and ny, nz >= 3, other boxes fall back to
+ * variant 0; variant 8 serves FP32 levels whose boxes all have nx a multiple
+ * of 4, and asking for it on another level returns ELBM_E_UNSUPPORTED with
+ * the reason in elbm_last_error_string.  No counterpart in the reference. */
 int elbm_set_kernel_variant(elbm_ctx* ctx, int lvl, int variant);
 
 /* Learned initial guess of alpha (no counterpart in the reference; its

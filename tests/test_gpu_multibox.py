@@ -89,3 +89,50 @@ def test_multibox_rejects_overlap_and_gaps(pkg, built_lib):
     with pytest.raises(cap.ElbmError):
         ctx.set_links(1, 0, _slice_state(st, (0, 0, 0), (15, 23, 23)), ngrow_state=1)
     ctx.close()
+
+
+# boxes whose widths are whole 16-byte rows (nx % 4 == 0), so that the tensor-copy
+# variant serves them: 32-, 64- and 128-node-wide tiles in one launch
+BOXES4 = [((0, 0, 0), (19, 23, 23)), ((20, 0, 0), (27, 11, 23)), ((20, 12, 0), (27, 23, 23)),
+          ((28, 0, 0), (39, 23, 9)), ((28, 0, 10), (39, 23, 23))]
+
+
+@pytest.mark.parametrize("case", ["plate", "sphere"])
+def test_multibox_tensor_copy_variant(pkg, built_lib, case):
+    """The tensor-copy step variant (8) over a level of uneven boxes agrees
+    with the same domain held as one box and stepped by the direct kernel to
+    FP32 rounding, and with itself on one box bit for bit (its bulk nodes read
+    their pulls from the copied tiles, boundary and cross-box links from their
+    words)."""
+    cap = pkg.capi
+    if case == "sphere":
+        st, f0, bp = _sphere(pkg)
+    else:
+        geo = pkg.geometry
+        st = geo.box_state27(40, 24, 24, geo.flat_plate_faces())
+        f0 = geo.perturbed_equilibrium(40, 24, 24, (0.05, 0.0, 0.0), 2e-3, seed=99)
+        bp = geo.d3q27_boundary_params((0.05, 0.0, 0.0), 1e-3)
+
+    def run(boxes, variant):
+        ctx = cap.Context(0)
+        ctx.level_register(0, cap.ELBM_D3Q27, cap.ELBM_STORE_FP32_DEV, [list(lo) + list(hi) for lo, hi in boxes])
+        ctx.set_d3q27_params(0, cap.make_d3q27_params(**bp))
+        for k, (lo, hi) in enumerate(boxes):
+            ctx.set_links(0, k, _slice_state(st, lo, hi), ngrow_state=1)
+            ctx.upload(0, k, np.ascontiguousarray(_box_view(f0, lo, hi)))
+        ctx.set_kernel_variant(0, variant)
+        s = ctx.step(0, 20)
+        out = np.zeros_like(f0)
+        for k, (lo, hi) in enumerate(boxes):
+            _box_view(out, lo, hi)[...] = ctx.download(0, k)
+        ctx.close()
+        return s, out
+
+    one = [((0, 0, 0), (39, 23, 23))]
+    s_multi, f_multi = run(BOXES4, 8)
+    s_one8, f_one8 = run(one, 8)
+    s_one0, f_one0 = run(one, 0)
+    assert s_multi["status"] & 0x10 == 0 and s_one8["status"] & 0x10 == 0
+    assert s_multi["node_updates"] == s_one8["node_updates"] == s_one0["node_updates"]
+    assert np.array_equal(f_multi, f_one8)
+    assert np.max(np.abs(f_one8 - f_one0)) <= 1e-6

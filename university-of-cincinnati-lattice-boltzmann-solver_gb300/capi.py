@@ -20,6 +20,7 @@ ELBM_E_CUDA = -2
 ELBM_E_UNSUPPORTED = -3
 ELBM_E_STATE = -4
 ELBM_E_NUMERIC = -5
+ELBM_KERNEL_VARIANTS = 9  # FP32 D3Q27 step-kernel variants (elbm_autotune's timing array)
 
 ELBM_ST_NAN = 0x1
 ELBM_ST_NEWTON_FALLBACK = 0x2
@@ -447,7 +448,7 @@ class Context:
     def autotune(self, lvl, reps=3):
         """Pick the fastest step-kernel variant for the level; returns (index, ms per variant)."""
         chosen = ct.c_int(0)
-        ms = np.zeros(8)
+        ms = np.zeros(ELBM_KERNEL_VARIANTS)
         self._check(self.lib.elbm_autotune(self.h, lvl, reps, ct.byref(chosen), _ptr(ms)))
         return chosen.value, ms
 

@@ -1,6 +1,8 @@
 // C ABI of libelbm_gb300: level registry, link decoding, host<->device copies
 // and the per-level step driver.  Declarations and reference citations live in
 // include/elbm_gb300.h.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -132,6 +134,12 @@ struct Level {
   DevBuf<int4> boxdim;
   DevBuf<float> alpha;      // per node (record_alpha)
   DevBuf<unsigned long long> work;  // chunk counter of the persistent step variant
+  // tensor-copy step variant (FP32): 2 x nbox tensor maps (buffer 0's boxes, then buffer 1's),
+  // the boxes' tilings and the level's tile count; empty when the level is not eligible
+  DevBuf<uint8_t> ws_maps;
+  DevBuf<WsBox> ws_boxes;
+  int64_t ws_ntiles = 0;
+  std::string ws_why;  // why the level has no tensor-copy tables (empty: it has them)
   DevBuf<uint32_t> defer_list;      // FP32: strongly non-equilibrium nodes of the step, finished apart
   DevBuf<unsigned long long> defer_count;
   // negative-population repair: (node * 27 + population) list, its count, repaired values
@@ -602,6 +610,91 @@ int step39(elbm_ctx* c, Level& lv, int nsteps) {
 
 }  // namespace
 
+namespace {
+
+// Tensor maps and tilings of the tensor-copy step variant (csrc/d3q27_step.cu,
+// d3q27_fp32_ws_kernel) for a D3Q27 FP32 level.  Per box and population
+// buffer a 4-D map (x, y, z, population) over the box's nodes, with a copy
+// box of (TX + 8) x TY x 1 x 1 floats: TX = 32, 64 or 128 by the box's width
+// (the narrowest that holds a row), TY = 256 / TX.  Levels with a box whose
+// rows are not whole 16-byte units (nx % 4 != 0), or whose maps the driver
+// does not accept, leave the tables empty and step with the other variants.
+int build_ws_tables(elbm_ctx* c, Level& lv) {
+  lv.ws_maps.reset();
+  lv.ws_boxes.reset();
+  lv.ws_ntiles = 0;
+  lv.ws_why.clear();
+  for (auto& b : lv.boxes)
+    if (b->nx % 4 != 0) {
+      lv.ws_why = "a box's rows are not whole 16-byte units (nx % 4 != 0)";
+      return ELBM_OK;
+    }
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    // the driver's tensor-map encoder, through the runtime (no link-time dependency on libcuda)
+    for (unsigned ver : {12000u, (unsigned)CUDA_VERSION}) {
+      void* fn = nullptr;
+      cudaDriverEntryPointQueryResult q{};
+      const cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, ver, cudaEnableDefault, &q);
+      if (e == cudaSuccess && q == cudaDriverEntryPointSuccess && fn) {
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+        break;
+      }
+      char why[160];
+      snprintf(why, sizeof why, "cuTensorMapEncodeTiled not available (runtime error %d, query result %d)", (int)e,
+               (int)q);
+      lv.ws_why = why;
+    }
+    if (!encode) return ELBM_OK;
+    lv.ws_why.clear();
+  }
+  const int nbox = (int)lv.boxes.size();
+  std::vector<WsBox> wb(nbox);
+  std::vector<CUtensorMap> maps(2 * (size_t)nbox);
+  int64_t tiles = 0;
+  for (int k = 0; k < nbox; ++k) {
+    const Box& b = *lv.boxes[k];
+    const int txl = b.nx <= 32 ? 5 : (b.nx <= 64 ? 6 : 7);
+    const int TX = 1 << txl, TY = kWsTileNodes / TX;
+    WsBox& w = wb[k];
+    w.base = b.base;
+    w.tile0 = tiles;
+    w.nx = b.nx;
+    w.ny = b.ny;
+    w.nz = b.nz;
+    w.tx_log2 = txl;
+    w.tiles_x = (b.nx + TX - 1) / TX;
+    w.tiles_y = (b.ny + TY - 1) / TY;
+    tiles += (int64_t)w.tiles_x * w.tiles_y * b.nz;
+    for (int buf = 0; buf < 2; ++buf) {
+      const cuuint64_t dims[4] = {(cuuint64_t)b.nx, (cuuint64_t)b.ny, (cuuint64_t)b.nz, (cuuint64_t)Q27};
+      const cuuint64_t strides[3] = {(cuuint64_t)b.nx * 4, (cuuint64_t)b.nx * b.ny * 4, (cuuint64_t)lv.plane * 4};
+      const cuuint32_t box[4] = {(cuuint32_t)(TX + 8), (cuuint32_t)TY, 1, 1};
+      const cuuint32_t estr[4] = {1, 1, 1, 1};
+      void* base = lv.pop[buf].p + (size_t)b.base * sizeof(float);
+      const CUresult r = encode(&maps[(size_t)buf * nbox + k], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides,
+                                box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (r != CUDA_SUCCESS) {
+        char why[160];
+        snprintf(why, sizeof why, "the driver rejected the tensor map of box %d (CUresult %d)", k, (int)r);
+        lv.ws_why = why;
+        return ELBM_OK;
+      }
+    }
+  }
+  static_assert(sizeof(CUtensorMap) == 128, "tensor map size");
+  CUDA_TRY(lv.ws_maps.alloc(maps.size() * sizeof(CUtensorMap)), "tensor maps");
+  CUDA_TRY(cudaMemcpy(lv.ws_maps.p, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice),
+           "tensor maps");
+  CUDA_TRY(lv.ws_boxes.alloc(nbox), "tile boxes");
+  CUDA_TRY(cudaMemcpy(lv.ws_boxes.p, wb.data(), nbox * sizeof(WsBox), cudaMemcpyHostToDevice), "tile boxes");
+  lv.ws_ntiles = tiles;
+  return ELBM_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 int elbm_create(int device, elbm_ctx** out) {
@@ -710,6 +803,8 @@ int elbm_level_register(elbm_ctx* c, int lvl, int lattice, int storage, int nbox
     CUDA_TRY(cudaMemcpy(lv.boxdim.p, bd.data(), bd.size() * sizeof(int4), cudaMemcpyHostToDevice), "box dims");
   }
   CUDA_TRY(lv.eq.alloc(kEqTables * Q27 * sizeof(double)), "eq tables");
+  if (lattice == ELBM_D3Q27 && storage == ELBM_STORE_FP32_DEV)
+    if (const int rc = build_ws_tables(c, lv)) return rc;
   lv.registered = true;
   return ELBM_OK;
 }
@@ -968,6 +1063,11 @@ Step27Args level_args27(elbm_ctx* c, Level& lv) {
   a.defer_list = lv.defer_list.p;
   a.defer_count = lv.defer_count.p;
   a.defer_cap = (long long)lv.defer_list.n;
+  if (lv.ws_maps.p) {
+    a.ws_maps = lv.ws_maps.p + (size_t)lv.cur * lv.boxes.size() * sizeof(CUtensorMap);
+    a.ws_boxes = lv.ws_boxes.p;
+    a.ws_ntiles = lv.ws_ntiles;
+  }
   return a;
 }
 
@@ -1028,6 +1128,8 @@ int elbm_level_step(elbm_ctx* c, int lvl, int nsteps, elbm_stats* out) {
   return finish_stats(c, out);
 }
 
+static_assert(kFp32Variants == ELBM_KERNEL_VARIANTS, "variant count of the C ABI");
+
 int elbm_autotune(elbm_ctx* c, int lvl, int reps, int* chosen, double* ms_per_variant) {
   Level* lv = get_level(c, lvl);
   if (!lv || reps < 1) return fail(c, ELBM_E_ARG, "unknown level or reps < 1");
@@ -1040,6 +1142,10 @@ int elbm_autotune(elbm_ctx* c, int lvl, int reps, int* chosen, double* ms_per_va
   float best = INFINITY;
   int best_v = 0;
   for (int v = 0; v < kFp32Variants; ++v) {
+    if (v == kVariantTma && !lv->ws_maps.p) {
+      if (ms_per_variant) ms_per_variant[v] = INFINITY;  // not available for this level
+      continue;
+    }
     CUDA_TRY(cudaEventRecord(c->ev0, c->stream), "event");
     for (int r = 0; r < reps + 1; ++r) {
       if (r == 1) CUDA_TRY(cudaEventRecord(c->ev0, c->stream), "event");
@@ -1071,6 +1177,9 @@ int elbm_set_kernel_variant(elbm_ctx* c, int lvl, int variant) {
   if (!c) return ELBM_E_ARG;
   Level* lv = get_level(c, lvl);
   if (!lv || variant < 0 || variant >= kFp32Variants) return fail(c, ELBM_E_ARG, "unknown level or variant");
+  if (variant == kVariantTma && !lv->ws_maps.p)
+    return fail(c, ELBM_E_UNSUPPORTED, "the tensor-copy step variant does not serve this level: %s",
+                lv->ws_why.empty() ? "not a D3Q27 level with FP32 deviation storage" : lv->ws_why.c_str());
   lv->variant = variant;
   return ELBM_OK;
 }

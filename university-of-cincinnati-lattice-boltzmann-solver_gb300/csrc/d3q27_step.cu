@@ -148,6 +148,34 @@ __device__ __forceinline__ void warp_stats(DevStats* st, bool active, unsigned i
   }
 }
 
+// Per-thread statistics of the nodes a persistent thread updates, added to the
+// level's counters once at the end (a warp's atomics per node would all hit
+// the same few addresses).
+struct StatAcc {
+  unsigned nodes = 0, iters = 0, exact = 0, fb = 0, flags = 0, over = 0;
+  double dH = 0.0;
+};
+
+__device__ __forceinline__ void flush_stats(DevStats* st, const StatAcc& s) {
+  const unsigned m = 0xffffffffu;
+  const unsigned nodes = __reduce_add_sync(m, s.nodes), iters = __reduce_add_sync(m, s.iters);
+  const unsigned exact = __reduce_add_sync(m, s.exact), fb = __reduce_add_sync(m, s.fb);
+  const unsigned over = __reduce_add_sync(m, s.over), fl = __reduce_or_sync(m, s.flags);
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(s.dH);
+  const unsigned hi = __reduce_max_sync(m, (unsigned)(bits >> 32));
+  const unsigned lo = __reduce_max_sync(m, ((unsigned)(bits >> 32) == hi) ? (unsigned)bits : 0u);
+  if ((threadIdx.x & 31) == 0) {
+    if (nodes) atomicAdd(&st->node_updates, (unsigned long long)nodes);
+    if (iters) atomicAdd(&st->newton_iters, (unsigned long long)iters);
+    if (exact) atomicAdd(&st->exact_nodes, (unsigned long long)exact);
+    if (fb) atomicAdd(&st->fallbacks, (unsigned long long)fb);
+    if (fl) atomicOr(&st->status, fl);
+    if (over) atomicAdd(&st->dh_over, (unsigned long long)over);
+    const unsigned long long mx = ((unsigned long long)hi << 32) | lo;
+    if (mx) atomicMax(&st->max_dH_bits, mx);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Entropy difference in the conservation-consistent form (see the oracle):
 //   G(alpha) = H(f + alpha Delta) - H(f) = sum_i f_i psi(y_i, alpha),
@@ -864,10 +892,10 @@ __device__ __forceinline__ void node_prepare(const float (&d)[Q], bool want_y, f
 
 // Alpha solve (from delta0 with at most series_it series steps when
 // series_it > 0, the learned guess), relaxation, store and statistics.
-template <bool CHECK, int MODE>
+template <bool CHECK, int MODE, bool ACC = false>
 __device__ __forceinline__ void node_finish(const Step27Args& a, int64_t n, float (&d)[Q], const float2 (&D2)[14],
                                             const float2 (&y2)[14], float ymax, bool bad, float delta0,
-                                            int series_it) {
+                                            int series_it, StatAcc* acc = nullptr) {
   float* __restrict__ dst = static_cast<float*>(a.dst);
   AlphaOut al{0.f, 0.f, 0u, false, false};
   double dH = 0.0;
@@ -936,7 +964,17 @@ __device__ __forceinline__ void node_finish(const Step27Args& a, int64_t n, floa
   }
   store_dst(dst, a.plane, n, d);
   if (a.alpha_out) a.alpha_out[n] = 2.0f + al.delta;
-  warp_stats(a.stats, true, al.iters, al.large, al.fallback, flags, dH);
+  if constexpr (ACC) {
+    acc->nodes += 1u;
+    acc->iters += al.iters;
+    acc->exact += al.large ? 1u : 0u;
+    acc->fb += al.fallback ? 1u : 0u;
+    acc->flags |= flags;
+    acc->over += (flags & 0x8u) ? 1u : 0u;
+    acc->dH = fmax(acc->dH, dH);
+  } else {
+    warp_stats(a.stats, true, al.iters, al.large, al.fallback, flags, dH);
+  }
   if (MODE == 1) {
     const unsigned mk = __activemask();
     const unsigned nm = __popc(__ballot_sync(mk, guess_miss));
@@ -945,8 +983,8 @@ __device__ __forceinline__ void node_finish(const Step27Args& a, int64_t n, floa
 }
 
 // Everything after the gather: moments, equilibrium, alpha, relaxation, store.
-template <bool CHECK, int MODE>
-__device__ __forceinline__ void node_update(const Step27Args& a, int64_t n, float (&d)[Q]) {
+template <bool CHECK, int MODE, bool ACC = false>
+__device__ __forceinline__ void node_update(const Step27Args& a, int64_t n, float (&d)[Q], StatAcc* acc = nullptr) {
   float2 D2[14], y2[14];
   float ymax;
   bool bad;
@@ -982,7 +1020,7 @@ __device__ __forceinline__ void node_update(const Step27Args& a, int64_t n, floa
     delta0 = ymax * mlp_forward(x);
     series_it = 2;
   }
-  node_finish<CHECK, MODE>(a, n, d, D2, y2, ymax, bad, delta0, series_it);
+  node_finish<CHECK, MODE, ACC>(a, n, d, D2, y2, ymax, bad, delta0, series_it, acc);
 }
 
 // Direct variant: one thread per node, the 27 pulls are plain global loads.
@@ -1155,6 +1193,184 @@ __global__ void __launch_bounds__(128, 3) d3q27_fp32_staged_kernel(const Step27A
     for (int64_t k = it; k < it + kStages; ++k)
       if (blockIdx.x + k * gridDim.x < ntiles) mbar_wait(smem_addr(&bars[k % kStages]), (uint32_t)((k / kStages) & 1));
   }
+}
+
+// ---------------------------------------------------------------------------
+// Warp-specialised tensor-copy variant.  A persistent CTA of one producer warp
+// and kWsConsumers consumer warps walks 256-node tiles (TX x TY nodes of one z
+// plane, TX in {32, 64, 128} by box width).  The producer's elected lane
+// issues, per tile, one 4-D tensor copy (cp.async.bulk.tensor) per population
+// j: the box (x0 - 4 .. x0 + TX + 4, y0 - cy_j .. y0 - cy_j + TY, z - cz_j, j)
+// of the source buffer into a stage of a kWsStages-deep shared-memory ring,
+// completing on the stage's `full` mbarrier.  The x start is rounded to a
+// 16-byte boundary (x0 - 4) and the x shift -cx_j is taken in shared memory;
+// y and z shifts are tensor coordinates, so halo rows outside the box come as
+// zero fill (only boundary nodes would pull from there, and they use their
+// link words).  Each consumer thread owns one node of the tile: it reads its
+// 27 pulls from the stage at compile-time offsets, releases the stage (one
+// arrive per warp on `empty`), then collides and stores.  Stages are refilled
+// as soon as every consumer warp has read them, so copies of the next tiles
+// stay in flight while the current one computes, independently of how many
+// warps the register budget leaves per SM.  Every mbarrier wait is bounded:
+// a wait that gives up sets ELBM_ST_COPY_TIMEOUT, and the producer waits
+// (bounded) for its copies still in flight before the CTA exits.
+// ---------------------------------------------------------------------------
+constexpr int kWsConsumers = kWsTileNodes / 32;
+constexpr int kWsThreads = 32 * (kWsConsumers + 1);
+constexpr int kWsStages = 3;
+// floats per population in a stage: the largest TY (TX + 8) over the tile shapes
+// (TX = 32: 8 x 40 = 320); 1,280 bytes keeps every copy's destination 128-byte aligned
+constexpr int kWsPopStride = 320;
+constexpr int kWsStageFloats = Q * kWsPopStride;
+
+struct WsSmem {
+  float stage[kWsStages][kWsStageFloats];
+  unsigned long long full[kWsStages];
+  unsigned long long empty[kWsStages];
+};
+
+// Box of a tile: the last box whose first tile is <= tile (binary search; one box: none).
+__device__ __forceinline__ int ws_find_box(const Step27Args& a, int64_t tile) {
+  int lo = 0, hi = a.nbox - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&a.ws_boxes[mid].tile0) <= tile) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+struct WsTile {
+  int box, tx_log2, x0, y0, z;
+  int nx, ny;
+  int64_t base;
+};
+
+// Tile coordinates (32-bit arithmetic: a level holds fewer than 2^31 nodes, so fewer tiles).
+__device__ __forceinline__ WsTile ws_tile(const Step27Args& a, int tile) {
+  WsTile t;
+  t.box = (a.nbox > 1) ? ws_find_box(a, tile) : 0;
+  const WsBox* b = a.ws_boxes + t.box;
+  const unsigned lt = (unsigned)(tile - (int)__ldg(&b->tile0));
+  const unsigned tiles_x = (unsigned)__ldg(&b->tiles_x), tiles_y = (unsigned)__ldg(&b->tiles_y);
+  t.tx_log2 = __ldg(&b->tx_log2);
+  const unsigned row = lt / tiles_x;
+  const unsigned zz = row / tiles_y;
+  t.x0 = (int)(lt - row * tiles_x) << t.tx_log2;
+  t.y0 = (int)(row - zz * tiles_y) * (kWsTileNodes >> t.tx_log2);
+  t.z = (int)zz;
+  t.nx = __ldg(&b->nx);
+  t.ny = __ldg(&b->ny);
+  t.base = __ldg(&b->base);
+  return t;
+}
+
+// The node a consumer thread (ct = 0 .. 255) owns in a tile, and its type byte.
+__device__ __forceinline__ uint8_t ws_node(const Step27Args& a, const WsTile& t, int ct, int& r, int& xl,
+                                           int64_t& n) {
+  const int TX = 1 << t.tx_log2;
+  r = ct >> t.tx_log2;
+  xl = ct & (TX - 1);
+  const int x = t.x0 + xl, y = t.y0 + r;
+  n = t.base + ((int64_t)t.z * t.ny + y) * t.nx + x;
+  return (x < t.nx && y < t.ny) ? __ldg(a.ntype + n) : (uint8_t)NT_SKIP;
+}
+
+__device__ __forceinline__ void ws_tma_load(uint32_t dst, const void* map, int x, int y, int z, int j, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(j), "r"(bar)
+      : "memory");
+}
+
+template <bool CHECK>
+__global__ void __launch_bounds__(kWsThreads, 2) d3q27_fp32_ws_kernel(const Step27Args a) {
+  extern __shared__ __align__(1024) unsigned char ws_raw[];
+  WsSmem& S = *reinterpret_cast<WsSmem*>(ws_raw);
+  const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31);
+  const int ntiles = (int)a.ws_ntiles;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kWsStages; ++s) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&S.full[s])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&S.empty[s])), "r"(kWsConsumers)
+                   : "memory");
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+
+  if (warp == 0) {
+    // ---- producer: one lane issues the copies ----
+    if (lane != 0) return;
+    int it = 0;
+    bool failed = false;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+      const int s = it % kWsStages;
+      const uint32_t ph = (uint32_t)((it / kWsStages) & 1);
+      // the stage's previous tile must have been read by every consumer warp
+      if (it >= kWsStages && !mbar_wait(smem_addr(&S.empty[s]), ph ^ 1u)) {
+        failed = true;
+        break;
+      }
+      const WsTile t = ws_tile(a, tile);
+      const int TX = 1 << t.tx_log2, TY = kWsTileNodes >> t.tx_log2;
+      const unsigned bytes = (unsigned)(Q * TY * (TX + 8) * 4);
+      const uint32_t bar = smem_addr(&S.full[s]);
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+      const void* map = static_cast<const unsigned char*>(a.ws_maps) + (size_t)t.box * 128;
+      const uint32_t dst = smem_addr(&S.stage[s][0]);
+#pragma unroll
+      for (int j = 0; j < Q; ++j)
+        ws_tma_load(dst + (uint32_t)(j * kWsPopStride * 4), map, t.x0 - 4, t.y0 - cy27(j), t.z - cz27(j), j, bar);
+    }
+    if (failed) atomicOr(&a.stats->status, (unsigned)ELBM_ST_COPY_TIMEOUT);
+    // the copies of the last tiles of every stage must land before the CTA's shared memory is released
+    for (int k = (it > kWsStages ? it - kWsStages : 0); k < it; ++k)
+      mbar_wait(smem_addr(&S.full[k % kWsStages]), (uint32_t)((k / kWsStages) & 1));
+    return;
+  }
+
+  // ---- consumers: one node per thread; the next tile's type byte is loaded while this one computes ----
+  const int ct = (warp - 1) * 32 + lane;  // 0 .. 255
+  const float* __restrict__ src = static_cast<const float*>(a.src);
+  StatAcc acc;
+  int it = 0;
+  int tile = blockIdx.x;
+  WsTile t = ws_tile(a, tile);
+  int r, xl;
+  int64_t n;
+  uint8_t nt = ws_node(a, t, ct, r, xl, n);
+  while (tile < ntiles) {
+    const int s = it % kWsStages;
+    const uint32_t ph = (uint32_t)((it / kWsStages) & 1);
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(smem_addr(&S.full[s]), ph));
+    if (!ok) {
+      if (lane == 0) atomicOr(&a.stats->status, (unsigned)ELBM_ST_COPY_TIMEOUT);
+      break;
+    }
+    float d[Q];
+    if (nt == NT_BULK) {
+      const float* p = &S.stage[s][r * ((1 << t.tx_log2) + 8) + xl + 4];
+#pragma unroll
+      for (int j = 0; j < Q; ++j) d[j] = p[j * kWsPopStride - cx27(j)];
+    } else if (nt == NT_BOUNDARY) {
+      gather(a, src, n, nt, d);
+    }
+    __syncwarp();
+    if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&S.empty[s])) : "memory");
+    const int64_t n_cur = n;
+    const uint8_t nt_cur = nt;
+    tile += gridDim.x;
+    ++it;
+    if (tile < ntiles) {
+      t = ws_tile(a, tile);
+      nt = ws_node(a, t, ct, r, xl, n);
+    }
+    if (nt_cur != NT_SKIP) node_update<CHECK, 0, true>(a, n_cur, d, &acc);
+  }
+  __syncwarp();
+  flush_stats(a.stats, acc);
 }
 
 }  // namespace
@@ -1365,6 +1581,23 @@ void launch_d3q27_fp32_main(const Step27Args& a, cudaStream_t s) {
     const int64_t ntiles = (a.N + 127) / 128;
     const int64_t grid = std::min<int64_t>(ntiles, (int64_t)sms * bps);
     d3q27_fp32_learned_tc_kernel<<<(unsigned)grid, 128, sizeof(MlpTcSmem), s>>>(a);
+    return;
+  }
+  if (a.variant == kVariantTma && a.ws_maps && a.alpha_mode != 2 && !a.harvest) {
+    static int bps = -1, sms = 0;
+    const size_t smem = sizeof(WsSmem);
+    if (bps < 0) {
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      cudaFuncSetAttribute(d3q27_fp32_ws_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaFuncSetAttribute(d3q27_fp32_ws_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, d3q27_fp32_ws_kernel<false>, kWsThreads, smem);
+      if (bps < 1) bps = 1;
+    }
+    const int64_t grid = std::min<int64_t>(a.ws_ntiles, (int64_t)sms * bps);
+    if (a.check_dH) d3q27_fp32_ws_kernel<true><<<(unsigned)grid, kWsThreads, smem, s>>>(a);
+    else d3q27_fp32_ws_kernel<false><<<(unsigned)grid, kWsThreads, smem, s>>>(a);
     return;
   }
   if (a.variant == 3 && !a.check_dH && !a.harvest) {

@@ -26,6 +26,20 @@ struct DevStats {
   unsigned int pad;
 };
 
+// One box of a level as the tensor-copy (TMA) step variant walks it: tiles of
+// TX x TY nodes (TX = 1 << tx_log2 in {32, 64, 128}, TY = 256 / TX) in x, y,
+// one z plane each; tiles numbered box after box, x fastest.
+struct WsBox {
+  int64_t base;   // level index of the box's node (0, 0, 0)
+  int64_t tile0;  // first tile of the box
+  int nx, ny, nz;
+  int tx_log2;
+  int tiles_x, tiles_y;
+};
+// Nodes per tile of the tensor-copy variant and the widest tile it uses.
+constexpr int kWsTileNodes = 256;
+constexpr int kWsMaxTileX = 128;
+
 // Arguments of one fused D3Q27 step on a single box (valid region, no ghosts).
 struct Step27Args {
   const void* src;  // post-collision populations of the previous step, Q planes
@@ -63,6 +77,11 @@ struct Step27Args {
   DevStats* stats;
   const float* mlp;       // learned-alpha weights, FP32 (ELBM_ALPHA_LEARNED)
   int variant;            // kernel variant chosen by the autotuner
+  // tensor-copy variant: one CUtensorMap per box over the source buffer (4-D: x, y, z,
+  // population), the boxes' tilings and the level's tile count (nullptr: not eligible)
+  const void* ws_maps;
+  const WsBox* ws_boxes;
+  int64_t ws_ntiles;
   // harvesting of (populations, alpha) records for training (nullptr: off)
   float* harvest;
   unsigned long long* harvest_count;
@@ -71,8 +90,10 @@ struct Step27Args {
 };
 
 // 0: direct; 1, 4, 5, 6, 7: direct with registers capped for 4, 5, 6, 8, 7 blocks of 128 threads
-// per SM; 2: bulk-copy staged; 3: persistent warps taking chunks from a counter (4 blocks per SM)
-constexpr int kFp32Variants = 8;
+// per SM; 2: bulk-copy staged; 3: persistent warps taking chunks from a counter (4 blocks per SM);
+// 8: warp-specialised, tensor copies (TMA) of 256-node tiles into a shared-memory ring
+constexpr int kFp32Variants = 9;
+constexpr int kVariantTma = 8;
 // Bytes allocated before and after each population buffer (never written):
 // room for the staged kernel's row-segment copies that start 4 floats before
 // a plane or run up to a tile past its end.
