@@ -130,6 +130,8 @@ struct Level {
   DevBuf<uint16_t> words;   // Q per boundary record
   DevBuf<uint8_t> qfrac;    // Q per boundary record, FP64 or FP32 like the populations
   DevBuf<int32_t> xsrc;     // Q per boundary record
+  DevBuf<int32_t> bnode;    // level node index of every boundary record
+  int64_t nrec = 0;         // boundary records of the level
   DevBuf<int32_t> chunk_box;
   DevBuf<int4> boxdim;
   DevBuf<float> alpha;      // per node (record_alpha)
@@ -930,11 +932,15 @@ int elbm_set_links(elbm_ctx* c, int lvl, int box, const int32_t* state, int ngro
   std::vector<uint16_t> lw;
   std::vector<double> lq;
   std::vector<int32_t> lx;
+  std::vector<int32_t> lbn;
   int32_t rec = 0;
   for (auto& bp : lv->boxes) {
     const Box& bb = *bp;
     std::memcpy(&lnt[bb.base], bb.h_ntype.data(), bb.N);
-    for (size_t k = 0; k < bb.h_bnodes.size(); ++k) lbi[bb.base + bb.h_bnodes[k]] = rec++;
+    for (size_t k = 0; k < bb.h_bnodes.size(); ++k) {
+      lbi[bb.base + bb.h_bnodes[k]] = rec++;
+      lbn.push_back((int32_t)(bb.base + bb.h_bnodes[k]));
+    }
     lw.insert(lw.end(), bb.h_words.begin(), bb.h_words.end());
     lq.insert(lq.end(), bb.h_qfrac.begin(), bb.h_qfrac.end());
     lx.insert(lx.end(), bb.h_xsrc.begin(), bb.h_xsrc.end());
@@ -945,6 +951,10 @@ int elbm_set_links(elbm_ctx* c, int lvl, int box, const int32_t* state, int ngro
   CUDA_TRY(lv->words.alloc(std::max<size_t>(lw.size(), 1)), "link words");
   if (!lw.empty())
     CUDA_TRY(cudaMemcpy(lv->words.p, lw.data(), lw.size() * sizeof(uint16_t), cudaMemcpyHostToDevice), "words");
+  CUDA_TRY(lv->bnode.alloc(std::max<size_t>(lbn.size(), 1)), "boundary nodes");
+  if (!lbn.empty())
+    CUDA_TRY(cudaMemcpy(lv->bnode.p, lbn.data(), lbn.size() * sizeof(int32_t), cudaMemcpyHostToDevice), "bnodes");
+  lv->nrec = (int64_t)lbn.size();
   CUDA_TRY(lv->xsrc.alloc(std::max<size_t>(lx.size(), 1)), "cross-box sources");
   if (!lx.empty())
     CUDA_TRY(cudaMemcpy(lv->xsrc.p, lx.data(), lx.size() * sizeof(int32_t), cudaMemcpyHostToDevice), "cross-box");
@@ -1063,6 +1073,8 @@ Step27Args level_args27(elbm_ctx* c, Level& lv) {
   a.defer_list = lv.defer_list.p;
   a.defer_count = lv.defer_count.p;
   a.defer_cap = (long long)lv.defer_list.n;
+  a.bnode = lv.bnode.p;
+  a.nbnd = lv.nrec;
   if (lv.ws_maps.p) {
     a.ws_maps = lv.ws_maps.p + (size_t)lv.cur * lv.boxes.size() * sizeof(CUtensorMap);
     a.ws_boxes = lv.ws_boxes.p;

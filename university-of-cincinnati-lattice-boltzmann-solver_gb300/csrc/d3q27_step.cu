@@ -63,9 +63,10 @@ __device__ __forceinline__ void box_strides(const Step27Args& a, int64_t n, int&
 }
 
 // Gather the 27 streamed populations of node n (pull), bulk or boundary.
+// rec: the node's boundary record when the caller knows it (-1: look it up).
 template <typename T>
 __device__ __forceinline__ void gather(const Step27Args& a, const T* __restrict__ src, int64_t n, uint8_t t,
-                                       T (&f)[Q]) {
+                                       T (&f)[Q], int32_t rec = -1) {
   int nx;
   int64_t nxy;
   box_strides(a, n, nx, nxy);
@@ -73,7 +74,7 @@ __device__ __forceinline__ void gather(const Step27Args& a, const T* __restrict_
 #pragma unroll
     for (int j = 0; j < Q; ++j) f[j] = load_src(src, a.plane, j, n - nbr_offset(j, nx, nxy));
   } else {
-    const int32_t b = __ldg(a.bidx + n);
+    const int32_t b = rec >= 0 ? rec : __ldg(a.bidx + n);
     const uint16_t* __restrict__ wp = a.words + (int64_t)b * Q;
     const T* __restrict__ eq = static_cast<const T*>(a.eq);
 #pragma unroll
@@ -113,13 +114,27 @@ __device__ __forceinline__ void gather(const Step27Args& a, const T* __restrict_
   }
 }
 
+// The 27 pulls of a bulk node (all interior links of its own box).
+// One base pointer per thread; with one box per level the 27 offsets
+// j plane - (c_j . strides) are the same for every thread of the launch.
+template <typename T>
+__device__ __forceinline__ void gather_bulk(const Step27Args& a, const T* __restrict__ src, int64_t n, T (&f)[Q]) {
+  int nx;
+  int64_t nxy;
+  box_strides(a, n, nx, nxy);
+  const T* __restrict__ p = src + n;
+#pragma unroll
+  for (int j = 0; j < Q; ++j) f[j] = __ldg(p + ((int64_t)j * a.plane - nbr_offset(j, nx, nxy)));
+}
+
 // Streaming (evict-first) stores: the new populations are not read again before
 // the next step, and a level larger than L2 would only push out the lines that
 // neighbouring warps' pulls still share (+0.9% on the 512x256x256 level).
 template <typename T>
 __device__ __forceinline__ void store_dst(T* __restrict__ dst, int64_t plane, int64_t n, const T (&f)[Q]) {
+  T* __restrict__ p = dst + n;
 #pragma unroll
-  for (int j = 0; j < Q; ++j) __stcs(dst + (int64_t)j * plane + n, f[j]);
+  for (int j = 0; j < Q; ++j) __stcs(p + (int64_t)j * plane, f[j]);
 }
 
 __device__ __forceinline__ void warp_stats(DevStats* st, bool active, unsigned iters, bool exact, bool fb,
@@ -151,16 +166,20 @@ __device__ __forceinline__ void warp_stats(DevStats* st, bool active, unsigned i
 // Per-thread statistics of the nodes a persistent thread updates, added to the
 // level's counters once at the end (a warp's atomics per node would all hit
 // the same few addresses).
+// Counts are packed two to a word (a thread of a persistent launch updates at
+// most 2^31 / 65,536 < 2^16 nodes of a level).
 struct StatAcc {
-  unsigned nodes = 0, iters = 0, exact = 0, fb = 0, flags = 0, over = 0;
+  unsigned nodes_exact = 0;  // nodes (low half), exact-path nodes (high half)
+  unsigned fb_over = 0;      // Newton fallbacks (low half), |dH| above tolerance (high half)
+  unsigned iters = 0, flags = 0;
   double dH = 0.0;
 };
 
 __device__ __forceinline__ void flush_stats(DevStats* st, const StatAcc& s) {
   const unsigned m = 0xffffffffu;
-  const unsigned nodes = __reduce_add_sync(m, s.nodes), iters = __reduce_add_sync(m, s.iters);
-  const unsigned exact = __reduce_add_sync(m, s.exact), fb = __reduce_add_sync(m, s.fb);
-  const unsigned over = __reduce_add_sync(m, s.over), fl = __reduce_or_sync(m, s.flags);
+  const unsigned nodes = __reduce_add_sync(m, s.nodes_exact & 0xffffu), iters = __reduce_add_sync(m, s.iters);
+  const unsigned exact = __reduce_add_sync(m, s.nodes_exact >> 16), fb = __reduce_add_sync(m, s.fb_over & 0xffffu);
+  const unsigned over = __reduce_add_sync(m, s.fb_over >> 16), fl = __reduce_or_sync(m, s.flags);
   const unsigned long long bits = (unsigned long long)__double_as_longlong(s.dH);
   const unsigned hi = __reduce_max_sync(m, (unsigned)(bits >> 32));
   const unsigned lo = __reduce_max_sync(m, ((unsigned)(bits >> 32) == hi) ? (unsigned)bits : 0u);
@@ -818,24 +837,33 @@ __device__ __forceinline__ AlphaOut alpha_solve32(const float2 (&D2)[14], const 
   return alpha_fallback(P, max_it, tol_dH, r.iters);
 }
 
-// MINB: minimum resident blocks per SM requested from the register allocator
-// (0: none).  Both variants are built; the level's autotuner picks one.
-// MODE 0: Newton from alpha = 2; 1: learned guess + at most two Newton steps,
-// Newton from 2 as the fallback; 2: Newton and harvesting of training records.
-// Moments, entropic equilibrium and Delta = f^eq - f of one node from its
-// deviations d (pairs D2); with want_y, also y = Delta / f (pairs y2) and
-// ymax = max |y|.  bad: rho or u not finite.
-__device__ __forceinline__ void node_prepare(const float (&d)[Q], bool want_y, float2 (&D2)[14], float2 (&y2)[14],
-                                             float& ymax, bool& bad) {
-  // moments of the deviations: rho = 1 + sum d, j = sum c d (sum c w = 0)
-  float dr = 0.f, jx = 0.f, jy = 0.f, jz = 0.f;
+// Moments and the factors of the entropic equilibrium of one node (from its
+// deviations d): Delta_i follows from them with three operations.
+struct NodeEq {
+  float dr, rp1;     // rho - 1, rho
+  float e0[3];       // per-axis factor minus one, x axis, c = -1, 0, +1
+  float qyz[3][3];   // (y, z) part of prod(1 + e) - 1
+  bool bad;          // rho or u not finite
+};
+
+__device__ __forceinline__ void node_eq(const float (&d)[Q], NodeEq& q) {
+  // moments of the deviations: rho = 1 + sum d, j = sum c d (sum c w = 0), each as two
+  // interleaved partial sums on the paired FP32 pipe (shorter dependency chains)
+  float2 r2 = make_float2(0.f, 0.f), x2 = r2, y2 = r2, z2 = r2;
 #pragma unroll
-  for (int i = 0; i < Q; ++i) {
-    dr += d[i];
-    if (cx27(i)) jx += cx27(i) * d[i];
-    if (cy27(i)) jy += cy27(i) * d[i];
-    if (cz27(i)) jz += cz27(i) * d[i];
+  for (int q2 = 0; q2 < 14; ++q2) {
+    const int i0 = 2 * q2, i1 = 2 * q2 + 1;
+    const float b = (i1 < Q) ? d[i1] : 0.f;
+    const float2 v = make_float2(d[i0], b);
+    r2 = __fadd2_rn(r2, v);
+    if (cx27(i0) || (i1 < Q && cx27(i1)))
+      x2 = __ffma2_rn(make_float2((float)cx27(i0), i1 < Q ? (float)cx27(i1) : 0.f), v, x2);
+    if (cy27(i0) || (i1 < Q && cy27(i1)))
+      y2 = __ffma2_rn(make_float2((float)cy27(i0), i1 < Q ? (float)cy27(i1) : 0.f), v, y2);
+    if (cz27(i0) || (i1 < Q && cz27(i1)))
+      z2 = __ffma2_rn(make_float2((float)cz27(i0), i1 < Q ? (float)cz27(i1) : 0.f), v, z2);
   }
+  const float dr = r2.x + r2.y, jx = x2.x + x2.y, jy = y2.x + y2.y, jz = z2.x + z2.y;
   const float rho = 1.0f + dr;
   const float inv_rho = __fdividef(1.0f, rho);
   const float u[3] = {jx * inv_rho, jy * inv_rho, jz * inv_rho};
@@ -853,38 +881,56 @@ __device__ __forceinline__ void node_prepare(const float (&d)[Q], bool want_y, f
     e[k][0] = __fdividef(-sm1 - zm1, 1.0f + zm1);
   }
   // P_i = prod(1 + e) - 1 = A + (1 + A)(B + (1 + B) C), with the (y, z) part shared
-  float qyz[3][3];
 #pragma unroll
   for (int b = 0; b < 3; ++b)
 #pragma unroll
-    for (int c = 0; c < 3; ++c) qyz[b][c] = fmaf(1.0f + e[1][b], e[2][c], e[1][b]);
-  // Delta_i = f^eq_i - f_i in deviation form: w_i [P (1 + dr) + dr] - d_i, kept in pairs
-  const float rp1 = 1.0f + dr;
+    for (int c = 0; c < 3; ++c) q.qyz[b][c] = fmaf(1.0f + e[1][b], e[2][c], e[1][b]);
 #pragma unroll
-  for (int q = 0; q < 14; ++q) {
-    float v[2];
+  for (int c = 0; c < 3; ++c) q.e0[c] = e[0][c];
+  q.dr = dr;
+  q.rp1 = 1.0f + dr;
+  q.bad = !isfinite(rho) || !isfinite(u[0]) || !isfinite(u[1]) || !isfinite(u[2]);
+}
+
+// Delta_i = f^eq_i - f_i in deviation form, w_i [P (1 + dr) + dr] - d_i, for the
+// pair (2q, 2q + 1) (the 28th lane is 0).
+__device__ __forceinline__ float2 delta_pair(const NodeEq& e, const float (&d)[Q], int q) {
+  float v[2];
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int i = 2 * q + h;
-      if (i < Q) {
-        const float A = e[0][cx27(i) + 1];
-        const float P = fmaf(1.0f + A, qyz[cy27(i) + 1][cz27(i) + 1], A);
-        v[h] = fmaf((float)w27(i), fmaf(P, rp1, dr), -d[i]);
-      } else {
-        v[h] = 0.f;
-      }
+  for (int h = 0; h < 2; ++h) {
+    const int i = 2 * q + h;
+    if (i < Q) {
+      const float A = e.e0[cx27(i) + 1];
+      const float P = fmaf(1.0f + A, e.qyz[cy27(i) + 1][cz27(i) + 1], A);
+      v[h] = fmaf((float)w27(i), fmaf(P, e.rp1, e.dr), -d[i]);
+    } else {
+      v[h] = 0.f;
     }
-    D2[q] = make_float2(v[0], v[1]);
   }
-  bad = !isfinite(rho) || !isfinite(u[0]) || !isfinite(u[1]) || !isfinite(u[2]);
+  return make_float2(v[0], v[1]);
+}
+
+// f = w + d for the pair (2q, 2q + 1) (the 28th lane is 1).
+__device__ __forceinline__ float2 f_pair(const float (&d)[Q], int q) {
+  return make_float2((float)w27(2 * q) + d[2 * q], (2 * q + 1 < Q) ? (float)w27(2 * q + 1) + d[2 * q + 1] : 1.0f);
+}
+
+// Moments, entropic equilibrium and Delta = f^eq - f of one node from its
+// deviations d (pairs D2); with want_y, also y = Delta / f (pairs y2) and
+// ymax = max |y|.  bad: rho or u not finite.
+__device__ __forceinline__ void node_prepare(const float (&d)[Q], bool want_y, float2 (&D2)[14], float2 (&y2)[14],
+                                             float& ymax, bool& bad) {
+  NodeEq e;
+  node_eq(d, e);
+#pragma unroll
+  for (int q = 0; q < 14; ++q) D2[q] = delta_pair(e, d, q);
+  bad = e.bad;
   ymax = 0.f;
   if (want_y) {
 #pragma unroll
     for (int q = 0; q < 14; ++q) {
-      const int i0 = 2 * q, i1 = 2 * q + 1;
-      const float fa = (float)w27(i0) + d[i0];
-      const float fb = (i1 < Q) ? (float)w27(i1) + d[i1] : 1.0f;
-      y2[q] = make_float2(__fdividef(D2[q].x, fa), __fdividef(D2[q].y, fb));
+      const float2 f2 = f_pair(d, q);
+      y2[q] = make_float2(__fdividef(D2[q].x, f2.x), __fdividef(D2[q].y, f2.y));
       ymax = fmaxf(ymax, fmaxf(fabsf(y2[q].x), fabsf(y2[q].y)));
     }
   }
@@ -965,13 +1011,11 @@ __device__ __forceinline__ void node_finish(const Step27Args& a, int64_t n, floa
   store_dst(dst, a.plane, n, d);
   if (a.alpha_out) a.alpha_out[n] = 2.0f + al.delta;
   if constexpr (ACC) {
-    acc->nodes += 1u;
+    acc->nodes_exact += 1u + (al.large ? 0x10000u : 0u);
+    acc->fb_over += (al.fallback ? 1u : 0u) + ((flags & 0x8u) ? 0x10000u : 0u);
     acc->iters += al.iters;
-    acc->exact += al.large ? 1u : 0u;
-    acc->fb += al.fallback ? 1u : 0u;
     acc->flags |= flags;
-    acc->over += (flags & 0x8u) ? 1u : 0u;
-    acc->dH = fmax(acc->dH, dH);
+    if (CHECK) acc->dH = fmax(acc->dH, dH);
   } else {
     warp_stats(a.stats, true, al.iters, al.large, al.fallback, flags, dH);
   }
@@ -983,8 +1027,155 @@ __device__ __forceinline__ void node_finish(const Step27Args& a, int64_t n, floa
 }
 
 // Everything after the gather: moments, equilibrium, alpha, relaxation, store.
+// The out-of-line solvers on a node given by its deviations alone (Delta and
+// y formed again, exactly as node_prepare forms them).
+__device__ __noinline__ AlphaOut alpha_solve_from_d(NodePops& P, int max_it, float polish_thr, float tol_dH,
+                                                    bool series_failed, unsigned iters) {
+  float ymax;
+  bool bad;
+  node_prepare(P.d, true, P.D2, P.y2, ymax, bad);
+  if (series_failed) return alpha_fallback(P, max_it, tol_dH, iters);
+  return alpha_solve_large<kSeriesK>(P, max_it, polish_thr, tol_dH, true, 0.f, -1);
+}
+
+// The Newton-alpha update of one node with little live state: the
+// equilibrium factors (NodeEq) stay, while each pair of Delta and y is formed,
+// added into the power sums and dropped; the relaxation forms Delta again
+// (the same operations, so the same values).  Nodes with some |y| > kYSmall go
+// to the out-of-line solver, or, with a deferred-node list, to the second
+// kernel.
+template <bool CHECK, bool ACC>
+__device__ __forceinline__ void node_update_newton(const Step27Args& a, int64_t n, float (&d)[Q], StatAcc* acc) {
+  constexpr int K = kSeriesK;
+  NodeEq e;
+  node_eq(d, e);
+  AlphaOut al{0.f, 0.f, 0u, false, false};
+  if (a.alpha_mode != 0) {
+    float ymax = 0.f;
+    float2 S2[K + 1];
+#pragma unroll
+    for (int k = 0; k <= K; ++k) S2[k] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int q = 0; q < 14; ++q) {
+      const float2 D = delta_pair(e, d, q), f2 = f_pair(d, q);
+      const float2 y = make_float2(__fdividef(D.x, f2.x), __fdividef(D.y, f2.y));
+      ymax = fmaxf(ymax, fmaxf(fabsf(y.x), fabsf(y.y)));
+      float2 p = __fmul2_rn(D, y);  // f y^2
+      S2[2] = __fadd2_rn(S2[2], p);
+#pragma unroll
+      for (int k = 3; k <= K; ++k) {
+        p = __fmul2_rn(p, y);
+        S2[k] = __fadd2_rn(S2[k], p);
+      }
+    }
+    if (a.defer_on) {
+      // a node whose populations leave the series range takes the out-of-line solver, which would
+      // hold its whole warp: list it for the second kernel instead (warp-aggregated slots)
+      const bool defer = ymax > kYSmall;
+      const unsigned mk = __activemask();
+      const unsigned dm = __ballot_sync(mk, defer);
+      if (dm) {
+        const int lane = (int)(threadIdx.x & 31), leader = __ffs(dm) - 1;
+        unsigned long long base = 0;
+        if (lane == leader) base = atomicAdd(a.defer_count, (unsigned long long)__popc(dm));
+        base = __shfl_sync(mk, base, leader);
+        if (defer) {
+          const unsigned long long slot = base + __popc(dm & ((1u << lane) - 1u));
+          if ((long long)slot < a.defer_cap) {
+            a.defer_list[slot] = (uint32_t)n;
+            return;
+          }
+        }
+      }
+    }
+    const float pthr = (float)(a.tol_dH * 1e6), tdh = (float)a.tol_dH;
+    bool need_pops = ymax > kYSmall, series_failed = false;
+    if (!need_pops) {
+      float S[K + 1];
+#pragma unroll
+      for (int k = 0; k <= K; ++k) S[k] = S2[k].x + S2[k].y;
+      if (S[2] > 1e-30f) {  // else at equilibrium: alpha = 2
+        float delta = 0.f;
+        if (series_newton<K>(S, a.max_newton, delta, al.iters)) al.delta = delta;
+        else need_pops = series_failed = true;
+      }
+    }
+    if (need_pops) {
+      NodePops P;
+#pragma unroll
+      for (int i = 0; i < Q; ++i) P.d[i] = d[i];
+      al = alpha_solve_from_d(P, a.max_newton, pthr, tdh, series_failed, al.iters);
+    }
+  }
+  double dH = 0.0;
+  if (CHECK && a.alpha_mode != 0) {
+    // |H(f + alpha Delta) - H(f)| in FP64 (conservation-consistent form) from the FP32 populations
+    const double al64 = 2.0 + (double)al.delta + (double)al.delta_lo;
+    double g = 0.0;
+#pragma unroll
+    for (int q = 0; q < 14; ++q) {
+      const float2 D = delta_pair(e, d, q), f2 = f_pair(d, q);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        if (2 * q + h < Q) {
+          const double f64 = (double)(h ? f2.y : f2.x);
+          const double y64 = (double)(h ? D.y : D.x) / f64;
+          g += f64 * (phi64(al64 * y64) - al64 * y64 * log1p(y64));
+        }
+      }
+    }
+    dH = fabs(g);
+  }
+  unsigned flags = 0;
+  if (e.bad) flags |= 0x1u;
+  if (al.fallback) flags |= 0x2u;
+  if (CHECK && dH > a.tol_dH) flags |= 0x8u;
+  const float ab = (2.0f + al.delta) * (float)a.beta;
+  const float2 ab2 = make_float2(ab, ab);
+  // d += alpha beta Delta (Delta formed again)
+#pragma unroll
+  for (int q = 0; q < 14; ++q) {
+    const float2 D = delta_pair(e, d, q);
+    if (2 * q + 1 < Q) {
+      const float2 r = __ffma2_rn(ab2, D, make_float2(d[2 * q], d[2 * q + 1]));
+      d[2 * q] = r.x;
+      d[2 * q + 1] = r.y;
+    } else {
+      d[2 * q] = fmaf(ab, D.x, d[2 * q]);
+    }
+  }
+  // f = w + d < 0, compared without forming the sum (same outcome without flush-to-zero)
+  bool neg = false;
+#pragma unroll
+  for (int i = 0; i < Q; ++i) neg |= d[i] < -(float)w27(i);
+  if (neg) flags |= 0x4u;
+  if (neg && a.neg_list) {
+#pragma unroll
+    for (int i = 0; i < Q; ++i)
+      if (d[i] < -(float)w27(i)) {
+        const unsigned long long slot = atomicAdd(a.neg_count, 1ull);
+        if ((long long)slot < a.neg_cap) a.neg_list[slot] = (unsigned long long)n * Q + i;
+      }
+  }
+  store_dst(static_cast<float*>(a.dst), a.plane, n, d);
+  if (a.alpha_out) a.alpha_out[n] = 2.0f + al.delta;
+  if constexpr (ACC) {
+    acc->nodes_exact += 1u + (al.large ? 0x10000u : 0u);
+    acc->fb_over += (al.fallback ? 1u : 0u) + ((flags & 0x8u) ? 0x10000u : 0u);
+    acc->iters += al.iters;
+    acc->flags |= flags;
+    if (CHECK) acc->dH = fmax(acc->dH, dH);
+  } else {
+    warp_stats(a.stats, true, al.iters, al.large, al.fallback, flags, dH);
+  }
+}
+
 template <bool CHECK, int MODE, bool ACC = false>
 __device__ __forceinline__ void node_update(const Step27Args& a, int64_t n, float (&d)[Q], StatAcc* acc = nullptr) {
+  if constexpr (MODE == 0) {
+    node_update_newton<CHECK, ACC>(a, n, d, acc);
+    return;
+  }
   float2 D2[14], y2[14];
   float ymax;
   bool bad;
@@ -1023,15 +1214,19 @@ __device__ __forceinline__ void node_update(const Step27Args& a, int64_t n, floa
   node_finish<CHECK, MODE, ACC>(a, n, d, D2, y2, ymax, bad, delta0, series_it, acc);
 }
 
+// MINB: minimum resident blocks per SM requested from the register allocator
+// (0: none).  Both variants are built; the level's autotuner picks one.
+// MODE 0: Newton from alpha = 2; 1: learned guess + at most two Newton steps,
+// Newton from 2 as the fallback; 2: Newton and harvesting of training records.
 // Direct variant: one thread per node, the 27 pulls are plain global loads.
 template <bool CHECK, int MINB, int MODE = 0>
 __global__ void __launch_bounds__(128, MINB) d3q27_fp32_kernel(const Step27Args a) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= a.N) return;
-  const uint8_t t = __ldg(a.ntype + n);
-  if (t == NT_SKIP) return;
+  // bulk nodes only: the boundary nodes are the boundary kernel's
+  if (__ldg(a.ntype + n) != NT_BULK) return;
   float d[Q];
-  gather(a, static_cast<const float*>(a.src), n, t, d);
+  gather_bulk(a, static_cast<const float*>(a.src), n, d);
   node_update<CHECK, MODE>(a, n, d);
 }
 
@@ -1053,6 +1248,22 @@ __global__ void __launch_bounds__(128) d3q27_fp32_deferred_kernel(const Step27Ar
   }
 }
 
+// The boundary nodes of a step (the records' nodes), one thread each: their
+// pulls follow the link words; the update is the bulk nodes' (nodes far from
+// equilibrium are solved in place).
+template <bool CHECK, int MODE>
+__global__ void __launch_bounds__(128) d3q27_fp32_boundary_kernel(const Step27Args a) {
+  Step27Args b = a;
+  b.defer_on = 0;
+  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < a.nbnd;
+       r += (long long)gridDim.x * blockDim.x) {
+    const int64_t n = __ldg(a.bnode + r);
+    float d[Q];
+    gather(b, static_cast<const float*>(b.src), n, (uint8_t)NT_BOUNDARY, d, (int32_t)r);
+    node_update<CHECK, MODE>(b, n, d);
+  }
+}
+
 // Persistent variant: a fixed grid (every SM full) whose warps take chunks of
 // 32 consecutive nodes from a global counter, in order, so that no block waits
 // for its slowest warp before the SM can start new work and the chunks in
@@ -1068,10 +1279,9 @@ __global__ void __launch_bounds__(128, MINB) d3q27_fp32_persistent_kernel(const 
     if ((int64_t)c >= nchunks) break;
     const int64_t n = (int64_t)c * 32 + lane;
     if (n >= a.N) continue;
-    const uint8_t t = __ldg(a.ntype + n);
-    if (t == NT_SKIP) continue;
+    if (__ldg(a.ntype + n) != NT_BULK) continue;  // the boundary kernel updates the others
     float d[Q];
-    gather(a, static_cast<const float*>(a.src), n, t, d);
+    gather_bulk(a, static_cast<const float*>(a.src), n, d);
     node_update<CHECK, MODE>(a, n, d);
   }
 }
@@ -1088,8 +1298,9 @@ __global__ void __launch_bounds__(128, MINB) d3q27_fp32_persistent_kernel(const 
 constexpr int kTileX = 128, kHalo = 4, kSegLen = kTileX + 2 * kHalo, kStages = 2;
 constexpr int kStageFloats = Q * kSegLen;
 constexpr unsigned kStageBytes = kStageFloats * 4;
-// Bounded mbarrier waits: each poll suspends for at most ~1 us (time hint), and
-// a wait gives up after 2^20 polls or 2 s of the global timer, whichever first.
+// Bounded mbarrier waits: each poll may suspend the thread for a short,
+// hardware-chosen time, and a wait gives up after 2^20 polls or 2 s of the
+// global timer, whichever first.
 constexpr int kSpinLimit = 1 << 20;
 constexpr unsigned long long kWaitLimitNs = 2000000000ull;
 
@@ -1106,9 +1317,9 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
   for (int i = 0; i < kSpinLimit; ++i) {
     uint32_t done;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done)
-        : "r"(bar), "r"(parity), "r"(1000u)
+        : "r"(bar), "r"(parity)
         : "memory");
     if (done) return true;
     if ((i & 255) == 255 && global_ns() - t0 > kWaitLimitNs) return false;
@@ -1176,15 +1387,13 @@ __global__ void __launch_bounds__(128, 3) d3q27_fp32_staged_kernel(const Step27A
       const float* stg = sm + s * kStageFloats + kHalo + threadIdx.x;
 #pragma unroll
       for (int j = 0; j < Q; ++j) d[j] = stg[j * kSegLen - cx27(j)];
-    } else if (t == NT_BOUNDARY) {
-      gather(a, src, n, t, d);
     }
     __syncthreads();  // every read of stage s is done: refill it
     if (threadIdx.x == 0) {
       const int64_t next = tile + (int64_t)kStages * gridDim.x;
       if (next < ntiles) issue_tile(a, src, next, tiles_x, sm + s * kStageFloats, smem_addr(&bars[s]));
     }
-    if (t != NT_SKIP) node_update<CHECK, MODE>(a, n, d);
+    if (t == NT_BULK) node_update<CHECK, MODE>(a, n, d);  // the boundary kernel updates the others
   }
   if (failed && threadIdx.x == 0) {
     // report, then wait (bounded) for this block's copies still in flight before the
@@ -1196,45 +1405,49 @@ __global__ void __launch_bounds__(128, 3) d3q27_fp32_staged_kernel(const Step27A
 }
 
 // ---------------------------------------------------------------------------
-// Warp-specialised tensor-copy variant.  A persistent CTA of one producer warp
-// and kWsConsumers consumer warps walks 256-node tiles (TX x TY nodes of one z
-// plane, TX in {32, 64, 128} by box width).  The producer's elected lane
-// issues, per tile, one 4-D tensor copy (cp.async.bulk.tensor) per population
-// j: the box (x0 - 4 .. x0 + TX + 4, y0 - cy_j .. y0 - cy_j + TY, z - cz_j, j)
-// of the source buffer into a stage of a kWsStages-deep shared-memory ring,
-// completing on the stage's `full` mbarrier.  The x start is rounded to a
-// 16-byte boundary (x0 - 4) and the x shift -cx_j is taken in shared memory;
-// y and z shifts are tensor coordinates, so halo rows outside the box come as
-// zero fill (only boundary nodes would pull from there, and they use their
-// link words).  Each consumer thread owns one node of the tile: it reads its
-// 27 pulls from the stage at compile-time offsets, releases the stage (one
-// arrive per warp on `empty`), then collides and stores.  Stages are refilled
-// as soon as every consumer warp has read them, so copies of the next tiles
-// stay in flight while the current one computes, independently of how many
-// warps the register budget leaves per SM.  Every mbarrier wait is bounded:
-// a wait that gives up sets ELBM_ST_COPY_TIMEOUT, and the producer waits
-// (bounded) for its copies still in flight before the CTA exits.
+// Tensor-copy variant.  A persistent CTA of eight warps walks 256-node tiles
+// (TX x TY nodes of one z plane, TX in {32, 64, 128} by box width), one node
+// per thread.  Per tile, one 4-D tensor copy (cp.async.bulk.tensor) per
+// population j brings the box (x0 - 4 .. x0 + TX + 4, y0 - cy_j .. y0 - cy_j
+// + TY, z - cz_j, j) of the source buffer into a stage of a kWsStages-deep
+// shared-memory ring, completing on the stage's `full` mbarrier.  The x start
+// is rounded to a 16-byte boundary (x0 - 4) and the x shift -cx_j is taken in
+// shared memory; y and z shifts are tensor coordinates, so halo rows outside
+// the box come as zero fill (only boundary nodes would pull from there, and
+// they use their link words).  Each thread reads its 27 pulls from the stage
+// at compile-time offsets and its warp releases the stage (one arrive on
+// `empty`); one thread then refills the stage with the tile kWsStages ahead
+// once all eight warps have released it, so copies of the next tiles are in
+// flight while the current one computes.  The issuing thread is one of the
+// consumers (no producer warp): eight warps per CTA and two CTAs per SM leave
+// 128 registers per thread.  Every mbarrier wait is bounded: a wait that gives
+// up sets ELBM_ST_COPY_TIMEOUT, and the issuing thread waits (bounded) for its
+// copies still in flight before the CTA exits.
 // ---------------------------------------------------------------------------
-constexpr int kWsConsumers = kWsTileNodes / 32;
-constexpr int kWsThreads = 32 * (kWsConsumers + 1);
+constexpr int kWsWarps = kWsTileNodes / 32;
+constexpr int kWsThreads = 32 * kWsWarps;
 constexpr int kWsStages = 3;
 // floats per population in a stage: the largest TY (TX + 8) over the tile shapes
 // (TX = 32: 8 x 40 = 320); 1,280 bytes keeps every copy's destination 128-byte aligned
 constexpr int kWsPopStride = 320;
 constexpr int kWsStageFloats = Q * kWsPopStride;
 
+// Levels of up to kWsSmemBoxes boxes keep their tilings in shared memory.
+constexpr int kWsSmemBoxes = 64;
+
 struct WsSmem {
   float stage[kWsStages][kWsStageFloats];
   unsigned long long full[kWsStages];
   unsigned long long empty[kWsStages];
+  WsBox boxes[kWsSmemBoxes];
 };
 
 // Box of a tile: the last box whose first tile is <= tile (binary search; one box: none).
-__device__ __forceinline__ int ws_find_box(const Step27Args& a, int64_t tile) {
-  int lo = 0, hi = a.nbox - 1;
+__device__ __forceinline__ int ws_find_box(const WsBox* boxes, int nbox, int64_t tile) {
+  int lo = 0, hi = nbox - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if (__ldg(&a.ws_boxes[mid].tile0) <= tile) lo = mid;
+    if (boxes[mid].tile0 <= tile) lo = mid;
     else hi = mid - 1;
   }
   return lo;
@@ -1246,22 +1459,23 @@ struct WsTile {
   int64_t base;
 };
 
-// Tile coordinates (32-bit arithmetic: a level holds fewer than 2^31 nodes, so fewer tiles).
-__device__ __forceinline__ WsTile ws_tile(const Step27Args& a, int tile) {
+// Tile coordinates (32-bit arithmetic: a level holds fewer than 2^31 nodes, so
+// fewer tiles); `boxes` is the level's table (shared memory or global).
+__device__ __forceinline__ WsTile ws_tile(const Step27Args& a, const WsBox* boxes, int tile) {
   WsTile t;
-  t.box = (a.nbox > 1) ? ws_find_box(a, tile) : 0;
-  const WsBox* b = a.ws_boxes + t.box;
-  const unsigned lt = (unsigned)(tile - (int)__ldg(&b->tile0));
-  const unsigned tiles_x = (unsigned)__ldg(&b->tiles_x), tiles_y = (unsigned)__ldg(&b->tiles_y);
-  t.tx_log2 = __ldg(&b->tx_log2);
+  t.box = (a.nbox > 1) ? ws_find_box(boxes, a.nbox, tile) : 0;
+  const WsBox& b = boxes[t.box];
+  const unsigned lt = (unsigned)(tile - (int)b.tile0);
+  const unsigned tiles_x = (unsigned)b.tiles_x, tiles_y = (unsigned)b.tiles_y;
+  t.tx_log2 = b.tx_log2;
   const unsigned row = lt / tiles_x;
   const unsigned zz = row / tiles_y;
   t.x0 = (int)(lt - row * tiles_x) << t.tx_log2;
   t.y0 = (int)(row - zz * tiles_y) * (kWsTileNodes >> t.tx_log2);
   t.z = (int)zz;
-  t.nx = __ldg(&b->nx);
-  t.ny = __ldg(&b->ny);
-  t.base = __ldg(&b->base);
+  t.nx = b.nx;
+  t.ny = b.ny;
+  t.base = b.base;
   return t;
 }
 
@@ -1284,93 +1498,104 @@ __device__ __forceinline__ void ws_tma_load(uint32_t dst, const void* map, int x
       : "memory");
 }
 
+// The issuing thread's copies of one tile into stage s.
+__device__ __forceinline__ void ws_issue(const Step27Args& a, WsSmem& S, const WsBox* boxes, int tile, int s) {
+  const WsTile t = ws_tile(a, boxes, tile);
+  const int TX = 1 << t.tx_log2, TY = kWsTileNodes >> t.tx_log2;
+  const unsigned bytes = (unsigned)(Q * TY * (TX + 8) * 4);
+  const uint32_t bar = smem_addr(&S.full[s]);
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+  const void* map = static_cast<const unsigned char*>(a.ws_maps) + (size_t)t.box * 128;
+  const uint32_t dst = smem_addr(&S.stage[s][0]);
+#pragma unroll
+  for (int j = 0; j < Q; ++j)
+    ws_tma_load(dst + (uint32_t)(j * kWsPopStride * 4), map, t.x0 - 4, t.y0 - cy27(j), t.z - cz27(j), j, bar);
+}
+
 template <bool CHECK>
 __global__ void __launch_bounds__(kWsThreads, 2) d3q27_fp32_ws_kernel(const Step27Args a) {
   extern __shared__ __align__(1024) unsigned char ws_raw[];
   WsSmem& S = *reinterpret_cast<WsSmem*>(ws_raw);
-  const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31);
+  const int lane = (int)(threadIdx.x & 31);
+  const bool issuer = threadIdx.x == 0;
   const int ntiles = (int)a.ws_ntiles;
-  if (threadIdx.x == 0) {
+  // this CTA's tiles: blockIdx.x + k gridDim.x, k = 0 .. mine - 1
+  const int mine = ((int)blockIdx.x < ntiles) ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  const bool smem_boxes = a.nbox <= kWsSmemBoxes;
+  if (smem_boxes)
+    for (int k = (int)threadIdx.x; k < a.nbox; k += (int)blockDim.x) S.boxes[k] = a.ws_boxes[k];
+  const WsBox* boxes = smem_boxes ? S.boxes : a.ws_boxes;
+  __syncthreads();
+  if (issuer) {
     for (int s = 0; s < kWsStages; ++s) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&S.full[s])) : "memory");
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&S.empty[s])), "r"(kWsConsumers)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&S.empty[s])), "r"(kWsWarps)
                    : "memory");
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    for (int k = 0; k < kWsStages && k < mine; ++k)
+      ws_issue(a, S, boxes, (int)blockIdx.x + k * (int)gridDim.x, k);
   }
   __syncthreads();
 
-  if (warp == 0) {
-    // ---- producer: one lane issues the copies ----
-    if (lane != 0) return;
-    int it = 0;
-    bool failed = false;
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
-      const int s = it % kWsStages;
-      const uint32_t ph = (uint32_t)((it / kWsStages) & 1);
-      // the stage's previous tile must have been read by every consumer warp
-      if (it >= kWsStages && !mbar_wait(smem_addr(&S.empty[s]), ph ^ 1u)) {
-        failed = true;
-        break;
-      }
-      const WsTile t = ws_tile(a, tile);
-      const int TX = 1 << t.tx_log2, TY = kWsTileNodes >> t.tx_log2;
-      const unsigned bytes = (unsigned)(Q * TY * (TX + 8) * 4);
-      const uint32_t bar = smem_addr(&S.full[s]);
-      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-      const void* map = static_cast<const unsigned char*>(a.ws_maps) + (size_t)t.box * 128;
-      const uint32_t dst = smem_addr(&S.stage[s][0]);
-#pragma unroll
-      for (int j = 0; j < Q; ++j)
-        ws_tma_load(dst + (uint32_t)(j * kWsPopStride * 4), map, t.x0 - 4, t.y0 - cy27(j), t.z - cz27(j), j, bar);
-    }
-    if (failed) atomicOr(&a.stats->status, (unsigned)ELBM_ST_COPY_TIMEOUT);
-    // the copies of the last tiles of every stage must land before the CTA's shared memory is released
-    for (int k = (it > kWsStages ? it - kWsStages : 0); k < it; ++k)
-      mbar_wait(smem_addr(&S.full[k % kWsStages]), (uint32_t)((k / kWsStages) & 1));
-    return;
-  }
-
-  // ---- consumers: one node per thread; the next tile's type byte is loaded while this one computes ----
-  const int ct = (warp - 1) * 32 + lane;  // 0 .. 255
-  const float* __restrict__ src = static_cast<const float*>(a.src);
+  const int ct = (int)threadIdx.x;  // 0 .. 255: the node of the tile
   StatAcc acc;
-  int it = 0;
+  int issued = (mine < kWsStages) ? mine : kWsStages;
+  bool failed = false;
   int tile = blockIdx.x;
-  WsTile t = ws_tile(a, tile);
   int r, xl;
   int64_t n;
-  uint8_t nt = ws_node(a, t, ct, r, xl, n);
-  while (tile < ntiles) {
+  // the type byte of this thread's node in the next tile is loaded while the current one computes
+  uint8_t nt_next = ws_node(a, ws_tile(a, boxes, tile), ct, r, xl, n);
+  for (int it = 0; it < mine; ++it, tile += gridDim.x) {
     const int s = it % kWsStages;
     const uint32_t ph = (uint32_t)((it / kWsStages) & 1);
-    const bool ok = __all_sync(0xffffffffu, mbar_wait(smem_addr(&S.full[s]), ph));
-    if (!ok) {
-      if (lane == 0) atomicOr(&a.stats->status, (unsigned)ELBM_ST_COPY_TIMEOUT);
+    const WsTile t = ws_tile(a, boxes, tile);
+    const int TX = 1 << t.tx_log2;
+    r = ct >> t.tx_log2;
+    xl = ct & (TX - 1);
+    n = t.base + ((int64_t)t.z * t.ny + t.y0 + r) * t.nx + t.x0 + xl;
+    const uint8_t nt = nt_next;
+    if (!__all_sync(0xffffffffu, mbar_wait(smem_addr(&S.full[s]), ph))) {
+      failed = true;
       break;
     }
     float d[Q];
     if (nt == NT_BULK) {
-      const float* p = &S.stage[s][r * ((1 << t.tx_log2) + 8) + xl + 4];
+      const float* p = &S.stage[s][r * (TX + 8) + xl + 4];
 #pragma unroll
       for (int j = 0; j < Q; ++j) d[j] = p[j * kWsPopStride - cx27(j)];
-    } else if (nt == NT_BOUNDARY) {
-      gather(a, src, n, nt, d);
     }
     __syncwarp();
     if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&S.empty[s])) : "memory");
-    const int64_t n_cur = n;
-    const uint8_t nt_cur = nt;
-    tile += gridDim.x;
-    ++it;
-    if (tile < ntiles) {
-      t = ws_tile(a, tile);
-      nt = ws_node(a, t, ct, r, xl, n);
+    if (issuer && it + kWsStages < mine) {
+      // every warp has read this tile's stage: refill it with the tile kWsStages ahead
+      if (mbar_wait(smem_addr(&S.empty[s]), ph)) {
+        ws_issue(a, S, boxes, (int)blockIdx.x + (it + kWsStages) * (int)gridDim.x, s);
+        ++issued;
+      } else {
+        failed = true;
+      }
     }
-    if (nt_cur != NT_SKIP) node_update<CHECK, 0, true>(a, n_cur, d, &acc);
+    if (__any_sync(0xffffffffu, failed)) {
+      failed = true;
+      break;
+    }
+    if (it + 1 < mine) {
+      int r2, xl2;
+      int64_t n2;
+      nt_next = ws_node(a, ws_tile(a, boxes, tile + (int)gridDim.x), ct, r2, xl2, n2);
+    }
+    if (nt == NT_BULK) node_update<CHECK, 0, true>(a, n, d, &acc);  // the boundary kernel updates the others
   }
   __syncwarp();
   flush_stats(a.stats, acc);
+  if (failed && lane == 0) atomicOr(&a.stats->status, (unsigned)ELBM_ST_COPY_TIMEOUT);
+  if (issuer) {
+    // the copies of the last issued tiles must land before the CTA's shared memory is released
+    for (int k = (issued > kWsStages ? issued - kWsStages : 0); k < issued; ++k)
+      mbar_wait(smem_addr(&S.full[k % kWsStages]), (uint32_t)((k / kWsStages) & 1));
+  }
 }
 
 }  // namespace
@@ -1543,29 +1768,39 @@ void launch_staged(const Step27Args& a, cudaStream_t s) {
   d3q27_fp32_staged_kernel<CHECK, MODE><<<(unsigned)grid, 128, smem, s>>>(a);
 }
 
-void launch_d3q27_fp32_main(const Step27Args& a, cudaStream_t s);
+// Returns whether the launched kernel updated every node (the learned-alpha
+// tensor-core kernel); the other step kernels update the bulk nodes only.
+bool launch_d3q27_fp32_main(const Step27Args& a, cudaStream_t s);
 
-// Step kernel, then (with a list) the listed nodes.
+// Step kernel (bulk nodes), boundary kernel, then (with a list) the listed nodes.
 void launch_d3q27_fp32(const Step27Args& a0, cudaStream_t s) {
   Step27Args a = a0;
   const bool defer = a.defer_list && a.alpha_mode == 1;  // Newton alpha (the learned guess keeps its own path)
   a.defer_on = defer ? 1 : 0;
   if (defer) cudaMemsetAsync(a.defer_count, 0, sizeof(unsigned long long), s);
-  launch_d3q27_fp32_main(a, s);
-  if (!defer) return;
+  const bool all_nodes = launch_d3q27_fp32_main(a, s);
   static int sms = 0;
   if (sms == 0) {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   }
+  if (!all_nodes && a.nbnd > 0) {
+    const long long bg = std::min<long long>((a.nbnd + 127) / 128, (long long)sms * 8);
+    if (a.check_dH && a.alpha_mode == 2) d3q27_fp32_boundary_kernel<true, 1><<<(unsigned)bg, 128, 0, s>>>(a);
+    else if (a.check_dH) d3q27_fp32_boundary_kernel<true, 0><<<(unsigned)bg, 128, 0, s>>>(a);
+    else if (a.harvest) d3q27_fp32_boundary_kernel<false, 2><<<(unsigned)bg, 128, 0, s>>>(a);
+    else if (a.alpha_mode == 2) d3q27_fp32_boundary_kernel<false, 1><<<(unsigned)bg, 128, 0, s>>>(a);
+    else d3q27_fp32_boundary_kernel<false, 0><<<(unsigned)bg, 128, 0, s>>>(a);
+  }
+  if (!defer) return;
   const long long grid = std::min<long long>((a.defer_cap + 127) / 128, (long long)sms * 8);
   if (a.check_dH) d3q27_fp32_deferred_kernel<true, 0><<<(unsigned)grid, 128, 0, s>>>(a);
   else if (a.harvest) d3q27_fp32_deferred_kernel<false, 2><<<(unsigned)grid, 128, 0, s>>>(a);
   else d3q27_fp32_deferred_kernel<false, 0><<<(unsigned)grid, 128, 0, s>>>(a);
 }
 
-void launch_d3q27_fp32_main(const Step27Args& a, cudaStream_t s) {
+bool launch_d3q27_fp32_main(const Step27Args& a, cudaStream_t s) {
   const int threads = 128;
   const int64_t blocks = (a.N + threads - 1) / threads;
   if (a.alpha_mode == 2 && !a.check_dH && !a.harvest && a.mlp) {
@@ -1581,7 +1816,7 @@ void launch_d3q27_fp32_main(const Step27Args& a, cudaStream_t s) {
     const int64_t ntiles = (a.N + 127) / 128;
     const int64_t grid = std::min<int64_t>(ntiles, (int64_t)sms * bps);
     d3q27_fp32_learned_tc_kernel<<<(unsigned)grid, 128, sizeof(MlpTcSmem), s>>>(a);
-    return;
+    return true;
   }
   if (a.variant == kVariantTma && a.ws_maps && a.alpha_mode != 2 && !a.harvest) {
     static int bps = -1, sms = 0;
@@ -1598,7 +1833,7 @@ void launch_d3q27_fp32_main(const Step27Args& a, cudaStream_t s) {
     const int64_t grid = std::min<int64_t>(a.ws_ntiles, (int64_t)sms * bps);
     if (a.check_dH) d3q27_fp32_ws_kernel<true><<<(unsigned)grid, kWsThreads, smem, s>>>(a);
     else d3q27_fp32_ws_kernel<false><<<(unsigned)grid, kWsThreads, smem, s>>>(a);
-    return;
+    return false;
   }
   if (a.variant == 3 && !a.check_dH && !a.harvest) {
     static int bps = -1, sms = 0;
@@ -1613,12 +1848,12 @@ void launch_d3q27_fp32_main(const Step27Args& a, cudaStream_t s) {
     cudaMemsetAsync(a.work_counter, 0, sizeof(unsigned long long), s);
     if (a.alpha_mode == 2) d3q27_fp32_persistent_kernel<false, 4, 1><<<(unsigned)grid, threads, 0, s>>>(a);
     else d3q27_fp32_persistent_kernel<false, 4, 0><<<(unsigned)grid, threads, 0, s>>>(a);
-    return;
+    return false;
   }
   if (a.variant == 2 && !a.check_dH && !a.harvest && staged_eligible(a)) {
     if (a.alpha_mode == 2) launch_staged<false, 1>(a, s);
     else launch_staged<false, 0>(a, s);
-    return;
+    return false;
   }
   if (a.check_dH) {
     if (a.alpha_mode == 2) d3q27_fp32_kernel<true, 0, 1><<<(unsigned)blocks, threads, 0, s>>>(a);
@@ -1641,6 +1876,7 @@ void launch_d3q27_fp32_main(const Step27Args& a, cudaStream_t s) {
   } else {
     d3q27_fp32_kernel<false, 0, 0><<<(unsigned)blocks, threads, 0, s>>>(a);
   }
+  return false;
 }
 
 }  // namespace elbm

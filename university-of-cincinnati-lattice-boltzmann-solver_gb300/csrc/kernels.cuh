@@ -82,6 +82,10 @@ struct Step27Args {
   const void* ws_maps;
   const WsBox* ws_boxes;
   int64_t ws_ntiles;
+  // boundary nodes: level node index of every boundary record (the FP32 step kernels update the
+  // bulk nodes, a second kernel these)
+  const int32_t* bnode;
+  int64_t nbnd;
   // harvesting of (populations, alpha) records for training (nullptr: off)
   float* harvest;
   unsigned long long* harvest_count;

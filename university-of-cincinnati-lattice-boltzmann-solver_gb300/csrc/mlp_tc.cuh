@@ -89,9 +89,9 @@ __device__ __forceinline__ bool tc_wait(unsigned long long* bar, uint32_t parity
   for (int i = 0; i < (1 << 20); ++i) {
     uint32_t done;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done)
-        : "r"(tc_smem(bar)), "r"(parity), "r"(1000u)
+        : "r"(tc_smem(bar)), "r"(parity)
         : "memory");
     if (done) return true;
     if ((i & 255) == 255) {
