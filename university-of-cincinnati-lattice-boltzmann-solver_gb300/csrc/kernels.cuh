@@ -86,6 +86,8 @@ struct Step27Args {
   // bulk nodes, a second kernel these)
   const int32_t* bnode;
   int64_t nbnd;
+  // resolved sources of the boundary records' pulls, Q x nbnd (nullptr: decode the link words)
+  const uint32_t* rsrc;
   // harvesting of (populations, alpha) records for training (nullptr: off)
   float* harvest;
   unsigned long long* harvest_count;
