@@ -116,9 +116,10 @@ static double entropy_diff(const double* f, const double* d, const double* L1, d
   return g;
 }
 
-/* Entropic alpha by Newton from alpha = 2 on G(alpha) = 0 (non-trivial root).
- * Returns alpha; *iters = iterations; *fallback = 1 when the solve failed and
- * alpha fell back to 2 (clipped into the positivity bracket). */
+/* Entropic alpha by Newton from alpha = 2 on G(alpha) = 0 (non-trivial root),
+ * safeguarded to the bracket (1, amax) of positive populations.  Returns alpha;
+ * *iters = iterations; *fallback = 1 when the solve failed and alpha fell back
+ * to 2 (clipped into the positivity bracket). */
 double o27_alpha_newton(const double f[Q], const double d[Q], double tol, int max_it, int* iters, int* fallback) {
   double L1[Q];
   double s2 = 0.0, amax = INFINITY;
@@ -145,10 +146,13 @@ double o27_alpha_newton(const double f[Q], const double d[Q], double tol, int ma
     *iters = it + 1;
     if (!(gp > 0.0)) break;
     const double step = g / gp;
-    const double next = alpha - step;
-    if (!(next > 1.0) || !(next < amax)) break;
+    double next = alpha - step;
+    /* a Newton step that leaves the bracket (1, amax) is replaced by halving the way to its end */
+    const int clipped = !(next > 1.0) || !(next < amax);
+    if (!(next > 1.0)) next = 0.5 * (alpha + 1.0);
+    else if (!(next < amax)) next = 0.5 * (alpha + amax);
     alpha = next;
-    if (fabs(step) <= tol) {
+    if (!clipped && fabs(step) <= tol) {
       ok = 1;
       break;
     }

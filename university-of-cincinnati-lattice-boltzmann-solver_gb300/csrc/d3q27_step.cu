@@ -281,10 +281,13 @@ __device__ double alpha_newton64(const double (&f)[Q], const double (&d)[Q], dou
     iters = it + 1;
     if (!(gp > 0.0)) break;
     const double step = g / gp;
-    const double next = alpha - step;
-    if (!(next > 1.0) || !(next < amax)) break;
+    double next = alpha - step;
+    // a Newton step that leaves the bracket (1, amax) is replaced by halving the way to its end
+    const bool clipped = !(next > 1.0) || !(next < amax);
+    if (!(next > 1.0)) next = 0.5 * (alpha + 1.0);
+    else if (!(next < amax)) next = 0.5 * (alpha + amax);
     alpha = next;
-    if (fabs(step) <= tol) {
+    if (!clipped && fabs(step) <= tol) {
       ok = true;
       break;
     }
