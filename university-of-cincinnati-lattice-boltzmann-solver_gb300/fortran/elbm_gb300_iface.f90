@@ -14,7 +14,10 @@ module elbm_gb300_iface
   private
 
   integer(c_int), parameter, public :: ELBM_OK = 0, ELBM_E_ARG = -1, ELBM_E_CUDA = -2, &
-    ELBM_E_UNSUPPORTED = -3, ELBM_E_STATE = -4
+    ELBM_E_UNSUPPORTED = -3, ELBM_E_STATE = -4, ELBM_E_NUMERIC = -5
+  integer(c_int), parameter, public :: ELBM_ST_NAN = 1, ELBM_ST_NEWTON_FALLBACK = 2, ELBM_ST_NEG_POP = 4, &
+    ELBM_ST_DH_TOL = 8, ELBM_ST_COPY_TIMEOUT = 16
+  integer(c_int), parameter, public :: ELBM_KERNEL_VARIANTS = 9, ELBM_MLP_PARAMS = 6017, ELBM_MLP_RECORD = 29
   integer(c_int), parameter, public :: ELBM_D3Q27 = 27, ELBM_D3Q39 = 39
   integer(c_int), parameter, public :: ELBM_STORE_FP64 = 0, ELBM_STORE_FP32_DEV = 1
   integer(c_int), parameter, public :: ELBM_ALPHA_FIXED2 = 0, ELBM_ALPHA_NEWTON = 1, ELBM_ALPHA_LEARNED = 2
@@ -65,7 +68,8 @@ module elbm_gb300_iface
     elbm_alpha_mlp_train, elbm_set_alpha_mlp, elbm_interlevel_setup, elbm_fill_fine_ghosts, &
     elbm_average_down, elbm_amr_run, elbm_damp_level, elbm_set_links39, elbm_upload_macro39, &
     elbm_init_level39, elbm_d3q39_equilibrium, elbm_checkpoint_write, elbm_checkpoint_read, elbm_ggm_tags, elbm_ggm_tags_pgs, &
-    elbm_write_plot3d, elbm_mic_sample, elbm_mark_triangles_gpu
+    elbm_write_plot3d, elbm_mic_sample, elbm_mark_triangles_gpu, elbm_last_error_string, &
+    elbm_alpha_mlp_grad, elbm_alpha_mlp_infer, elbm_links39_tables, elbm_error_message
 
   interface
     integer(c_int) function elbm_create(device, ctx) bind(c, name="elbm_create")
@@ -243,11 +247,11 @@ module elbm_gb300_iface
       real(c_double), intent(in) :: fout(*)
     end function
     integer(c_int) function elbm_autotune(ctx, lvl, reps, chosen, ms_per_variant) bind(c, name="elbm_autotune")
-      import :: c_int, c_ptr, c_double
+      import :: c_int, c_ptr, c_double, ELBM_KERNEL_VARIANTS
       type(c_ptr), value :: ctx
       integer(c_int), value :: lvl, reps
       integer(c_int), intent(out) :: chosen
-      real(c_double), intent(out) :: ms_per_variant(8)
+      real(c_double), intent(out) :: ms_per_variant(ELBM_KERNEL_VARIANTS)
     end function
     integer(c_int) function elbm_set_kernel_variant(ctx, lvl, variant) bind(c, name="elbm_set_kernel_variant")
       import :: c_int, c_ptr
@@ -315,7 +319,63 @@ module elbm_gb300_iface
       integer(c_int32_t), intent(in) :: state(*)      ! mfstate(lvl)%dataptr(mfi), 39 comps
       type(elbm_d3q39_bc), intent(in) :: bc
     end function
+    ! The message of the last error on the context (a NUL-terminated C string owned by the
+    ! library, valid until the next call on the context); elbm_error_message copies it.
+    type(c_ptr) function elbm_last_error_string(ctx) bind(c, name="elbm_last_error_string")
+      import :: c_ptr
+      type(c_ptr), value :: ctx
+    end function
+    integer(c_int) function elbm_alpha_mlp_grad(ctx, weights, records, n, grad, loss) &
+        bind(c, name="elbm_alpha_mlp_grad")
+      import :: c_int, c_ptr, c_float, c_int64_t, c_double
+      type(c_ptr), value :: ctx
+      real(c_float), intent(in) :: weights(6017), records(29, *)
+      integer(c_int64_t), value :: n
+      real(c_float), intent(out) :: grad(6017)
+      real(c_double), intent(out) :: loss
+    end function
+    integer(c_int) function elbm_alpha_mlp_infer(ctx, weights, x, n, out, status) &
+        bind(c, name="elbm_alpha_mlp_infer")
+      import :: c_int, c_ptr, c_float, c_int64_t, c_int32_t
+      type(c_ptr), value :: ctx
+      real(c_float), intent(in) :: weights(6017), x(27, *)
+      integer(c_int64_t), value :: n
+      real(c_float), intent(out) :: out(*)
+      integer(c_int32_t), intent(out) :: status
+    end function
+    integer(c_int) function elbm_links39_tables(nx, ny, nz, state, ngrow_state, periodic, shifted, &
+        primary_flow_dir, inlet_type, outlet_type, ntype, rec_node, words, capacity, nrec) &
+        bind(c, name="elbm_links39_tables")
+      import :: c_int, c_int32_t, c_int8_t, c_int64_t
+      integer(c_int), value :: nx, ny, nz, ngrow_state, periodic, shifted, primary_flow_dir
+      integer(c_int32_t), intent(in) :: state(*), inlet_type(8), outlet_type(8)
+      integer(c_int8_t), intent(out) :: ntype(*)
+      integer(c_int32_t), intent(out) :: rec_node(*), words(39, *)   ! words: uint32 link words
+      integer(c_int64_t), value :: capacity
+      integer(c_int64_t), intent(out) :: nrec
+    end function
   end interface
+
+contains
+
+  ! The last error message of a context as a Fortran string (the C string copied up to its NUL,
+  ! blank-padded or cut to len(msg)), for the reference's error_out
+  ! (general/background_calcs/error_out.f95:12-14) to print before it stops.
+  subroutine elbm_error_message(ctx, msg)
+    type(c_ptr), value :: ctx
+    character(len=*), intent(out) :: msg
+    character(kind=c_char), pointer :: cs(:)
+    type(c_ptr) :: p
+    integer :: i
+    msg = ' '
+    p = elbm_last_error_string(ctx)
+    if (.not. c_associated(p)) return
+    call c_f_pointer(p, cs, [len(msg)])
+    do i = 1, len(msg)
+      if (cs(i) == c_null_char) exit
+      msg(i:i) = cs(i)
+    end do
+  end subroutine
 end module elbm_gb300_iface
 
 ! Example body of the reference's per-level collide-stream call with the
