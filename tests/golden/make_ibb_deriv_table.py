@@ -2,14 +2,17 @@
 (card 1 x, 2 y, 3 z), the derivative form the reference's
 first_order_shifted_vel_cond_unknown and first_order_shifted_temp_cond_unknown
 (derivatives/modules/derivatives.f95) select: the wall form dudx_ibb with its
-up-wind flag, or the local difference dudx_local.  Run from the repository
-root where the reference sources sit at /root/reference."""
+up-wind flag, or the local difference dudx_local.
+
+Run: python make_ibb_deriv_table.py <reference root>   (writes ibb_deriv_table.json here)"""
 import json
 import pathlib
 import re
 import sys
 
-SRC = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/derivatives/modules/derivatives.f95")
+if len(sys.argv) != 2:
+    sys.exit("usage: make_ibb_deriv_table.py <reference root>")
+SRC = pathlib.Path(sys.argv[1]) / "derivatives" / "modules" / "derivatives.f95"
 
 
 def table(lines, fname):

@@ -2,14 +2,17 @@
 D3Q39 inviscid links (boundary_conditions/inviscid_edge.f95): for each
 direction (1-based) the ordered IF chain of its SELECT CASE branch, each entry
 the state components that must equal -11, the reflected direction and the
-displacement (loc_cx, loc_cy, loc_cz) of the node that receives it.  Run
-from the repository root where the reference sources sit at /root/reference."""
+displacement (loc_cx, loc_cy, loc_cz) of the node that receives it.
+
+Run: python make_inviscid_table.py <reference root>   (writes inviscid_table.json here)"""
 import json
 import pathlib
 import re
 import sys
 
-SRC = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/boundary_conditions/inviscid_edge.f95")
+if len(sys.argv) != 2:
+    sys.exit("usage: make_inviscid_table.py <reference root>")
+SRC = pathlib.Path(sys.argv[1]) / "boundary_conditions" / "inviscid_edge.f95"
 cases, case, cond, cur = {}, None, [], None
 for raw in SRC.read_text().split("\n"):
     line = raw.split("!")[0].strip()

@@ -183,6 +183,8 @@ def generate(ref_root: pathlib.Path) -> str:
 
 
 if __name__ == "__main__":
-    root = pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_ibb39_table.py <reference root>")
+    root = pathlib.Path(sys.argv[1])
     (HERE / "ibb39_table.h").write_text(generate(root))
     print("wrote", HERE / "ibb39_table.h")
