@@ -48,6 +48,8 @@ DRAM_BYTES_PER_NODE_NCU = 233
 KERNELS_PER_STEP = 2  # the step kernel and the listed-node kernel
 BYTES_PER_NODE_FP64 = 432
 BYTES_PER_NODE_D3Q39 = 1456  # f, g: 39 x 8 B read + written each; 13 multipliers x 8 B read + written
+NU_WEDGE = 2e-4  # lattice kinematic viscosity of the D3Q39 wedge case
+BYTES_PER_NODE_D3Q39_FP32 = 832  # f, g: 39 x 4 B read + written each; 13 multipliers x 8 B read + written
 
 
 def dist_env():
@@ -187,24 +189,29 @@ def cpu_baseline_sample(pkg, budget_s=15.0):
             "sample": f"{sx}x{sy}x{sz} sub-box of the workload, {steps} FP64 Newton-alpha steps, {dt:.1f} s"}
 
 
-def d3q39_wedge_leg(pkg, local_rank, steps=3):
-    """The compressible D3Q39 wedge case at its full size (384x192x48, Mach 1.5, shifted
-    lattice, 10-degree wedge with interpolated wall links, FP64): MLUPS of the fused
-    level step from CUDA events, after one untimed step."""
+def d3q39_wedge_leg(pkg, local_rank, fp32=False, steps=3, size=(384, 48, 192)):
+    """The compressible D3Q39 wedge case at its full size (384x48x192: 48-node span
+    between inviscid side walls, 192 high; Mach 1.5, shifted lattice, 10-degree
+    wedge with interpolated wall links; FP64 populations, or FP32
+    deviation storage of f and g with FP64 multipliers and arithmetic), each step
+    followed by the negative-population repair as the reference's loop runs it
+    (damp_it): MLUPS of the step and repair kernels from CUDA events, after one
+    untimed step.  `size` scales the box (the
+    wedge spans x from nx/4 to 25nx/32 at any size) for small profiling runs."""
     s39, cap = pkg.d3q39_setup, pkg.capi
-    c = s39.wedge_case_consts()
-    nx, ny, nz, periodic = 384, 192, 48, 2
-    faces = {"x-": -101, "x+": -201, "z-": -10, "z+": -1000, "y-": 0, "y+": 0}
+    c = s39.wedge_case_consts(nu_lattice=NU_WEDGE)
+    (nx, ny, nz), periodic = size, 0
     t0 = time.perf_counter()
     ctx = cap.Context(local_rank)
-    params = cap.make_d3q39_params(c, timestep=0, periodic=periodic, damp=0)
+    params = cap.make_d3q39_params(c, timestep=0, periodic=periodic, damp=1)
     lm0 = s39.freestream_start_lm(c)
     _, f, g = ctx.d3q39_equilibrium(params, 1.0, c.mach, 0.0, 0.0, c.temperature, lm0)  # freestream equilibria
-    st = s39.wedge_state39(nx, ny, nz, 96.0, 300.0, 10.0, faces, periodic=periodic)
+    st = s39.wedge_case_state(nx, ny, nz)
     shape = (nz, ny, nx)
     bc = cap.make_d3q39_bc([1] * 8, [6] + [1] * 7, f, g, [f] * 8, [g] * 8, [f] * 8, [g] * 8,
                            (c.mach, 0.0, 0.0, c.temperature))
-    ctx.level_register(0, cap.ELBM_D3Q39, cap.ELBM_STORE_FP64, [[0, 0, 0, nx - 1, ny - 1, nz - 1]])
+    storage = cap.ELBM_STORE_FP32_DEV if fp32 else cap.ELBM_STORE_FP64
+    ctx.level_register(0, cap.ELBM_D3Q39, storage, [[0, 0, 0, nx - 1, ny - 1, nz - 1]])
     ctx.set_d3q39_params(0, params)
     ctx.set_links39(0, 0, st, bc)
     setup_s = time.perf_counter() - t0
@@ -215,11 +222,45 @@ def d3q39_wedge_leg(pkg, local_rank, steps=3):
     s = ctx.step(0, steps)
     ctx.close()
     walls = int(((st[0] >= 0) & (st[1:] <= -1001).any(axis=0)).sum())
-    return {"workload": "D3Q39 Mach 1.5 wedge 384x192x48, FP64, shifted lattice", "steps": steps,
+    name = "FP32 deviation storage, FP64 arithmetic" if fp32 else "FP64"
+    return {"workload": f"D3Q39 Mach 1.5 wedge {nx}x{ny}x{nz}, {name}, shifted lattice", "steps": steps,
             "mlups": s["node_updates"] / (s["kernel_ms"] / 1e3) / 1e6, "ms_per_step": s["kernel_ms"] / steps,
             "wall_nodes": walls, "fallbacks": s["fallbacks"], "status": s["status"],
             "lm_iters_per_node": s["newton_iters"] / max(1, s["node_updates"]), "setup_s": setup_s,
-            "algorithmic_bytes_per_node": BYTES_PER_NODE_D3Q39}
+            "algorithmic_bytes_per_node": BYTES_PER_NODE_D3Q39_FP32 if fp32 else BYTES_PER_NODE_D3Q39}
+
+
+def d3q39_cpu_sample(pkg, seconds=10.0):
+    """The oracle's D3Q39 link step with the negative-population repair on a
+    96x12x48 wedge of the same shape (inlet, outlet, floor, freestream top,
+    inviscid side walls, a 10-degree wedge with interpolated wall links), every
+    node starting at the Mach 1.5 freestream:
+    steps until about `seconds` have passed (at least two)."""
+    from oracle import oracle39 as o39
+
+    s39 = pkg.d3q39_setup
+    c = s39.wedge_case_consts(nu_lattice=NU_WEDGE)
+    k = o39.consts(c)
+    nx, ny, nz = 96, 12, 48
+    st = s39.wedge_case_state(nx, ny, nz)
+    lm, f, g, _ = o39.init_node(k, 1.0, c.mach, 0.0, 0.0, c.temperature, s39.freestream_start_lm(c))
+    lev = o39.Level39(nx, ny, nz)
+    lev.fout[...] = np.asarray(f)[:, None, None, None]
+    lev.gout[...] = np.asarray(g)[:, None, None, None]
+    lev.lm[...] = np.asarray(lm)[:, None, None, None]
+    lev.rho[...], lev.u[...], lev.temp[...] = 1.0, c.mach, c.temperature
+    b = o39.bc([1] * 8, [6] + [1] * 7, f, g, [f] * 8, [g] * 8, [f] * 8, [g] * 8, (c.mach, 0.0, 0.0, c.temperature))
+    pf, pg = lev.fout.copy(), lev.gout.copy()
+    nodes, steps = 0, 0
+    t0 = time.perf_counter()
+    while steps < 2 or time.perf_counter() - t0 < seconds:
+        nodes += o39.step_links_damp(k, lev, steps, st, 0, b, pf, pg, (0, 0, 0), (nx - 1, ny - 1, nz - 1))["nodes"]
+        steps += 1
+    dt = time.perf_counter() - t0
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": nodes / dt / 1e6, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{nx}x{ny}x{nz} wedge, {steps} FP64 link steps of the oracle (collision on OpenMP "
+                      f"threads, streaming and wall targets on one), {dt:.1f} s"}
 
 
 def learned_alpha_leg(pkg, ctx, args, bp, local_rank):
@@ -281,6 +322,8 @@ def main():
                     help="alpha of the timed path (fixed2 = LBGK limit, to separate the alpha solve's cost)")
     ap.add_argument("--variant", type=int, default=None, choices=list(range(9)),
                     help="step-kernel variant instead of the autotuner's choice")
+    ap.add_argument("--d3q39-only", default=None, metavar="NXxNYxNZ",
+                    help="run only the D3Q39 wedge legs (FP64 and FP32 storage) at this size and print them")
     ap.add_argument("--profile", action="store_true",
                     help="timed steps only: no validation, end-to-end, FP64 or CPU legs (for ncu captures)")
     args = ap.parse_args()
@@ -305,6 +348,13 @@ def main():
     import __graft_entry__ as ge
 
     ge.build() if rank == 0 or world == 1 else None
+    if args.d3q39_only:
+        pkg = ge.load_package()
+        size = tuple(int(v) for v in args.d3q39_only.lower().split("x"))
+        legs = [d3q39_wedge_leg(pkg, local_rank, fp32=f, steps=args.steps, size=size) for f in (False, True)]
+        if rank == 0:
+            print(json.dumps({"d3q39_wedge": legs[0], "d3q39_wedge_fp32": legs[1]}), flush=True)
+        return
     if pg:
         pg.barrier()
     pkg = ge.load_package()
@@ -407,9 +457,12 @@ def main():
         fp64 = s64["node_updates"] / (s64["kernel_ms"] / 1e3) / 1e6
         c64.close()
 
-    wedge = None
+    wedge = wedge32 = None
     if not args.no_d3q39:
         wedge = d3q39_wedge_leg(pkg, local_rank)
+        wedge32 = d3q39_wedge_leg(pkg, local_rank, fp32=True)
+        if rank == 0 and world == 1 and not args.no_cpu_baseline:
+            wedge["cpu_baseline"] = d3q39_cpu_sample(pkg)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -446,6 +499,7 @@ def main():
                            "newton_iters_per_node": vst["newton_iters"] / max(1, vst["node_updates"])},
             "plain_fp64_newton_mlups": fp64,
             "d3q39_wedge": wedge,
+            "d3q39_wedge_fp32": wedge32,
             "learned_alpha": learned,
             "cpu_baseline": cpu,
         }

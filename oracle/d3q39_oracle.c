@@ -1134,7 +1134,8 @@ int o39_step_links(const o39_consts* k, o39_level* s, int step, o39_stats* st, c
             int32_t codes[Q];
             for (int q2 = 0; q2 < Q; ++q2) codes[q2] = q2 == 0 ? s0 : state[(int64_t)q2 * N + n];
             int j = 0, d[3];
-            if (!o39_inviscid(i, codes, &j, d)) { rc = -4; break; }
+            /* no branch of inviscid_edge.f95 applies: the reference writes nothing for this link */
+            if (!o39_inviscid(i, codes, &j, d)) continue;
             /* a reflection that lands outside the box leaves it, like a push across a face */
             const int64_t r2 = nb39(x + d[0], y + d[1], z + d[2], nx, ny, nz, periodic);
             if (r2 >= 0) {

@@ -47,8 +47,12 @@ def test_d3q27_checkpoint_restart_bitwise(pkg, built_lib, tmp_path, storage):
     assert np.array_equal(got, ref)
 
 
-def test_d3q39_checkpoint_restart_bitwise(pkg, built_lib, tmp_path):
+@pytest.mark.parametrize("storage", ["fp64", "fp32"])
+def test_d3q39_checkpoint_restart_bitwise(pkg, built_lib, tmp_path, storage):
+    """FP32 storage carries the per-direction reference of its deviations in the
+    checkpoint."""
     s39, cap = pkg.d3q39_setup, pkg.capi
+    store = cap.ELBM_STORE_FP32_DEV if storage == "fp32" else cap.ELBM_STORE_FP64
     c = s39.wedge_case_consts(v_inf_ms=0.8 * math.sqrt(1.4 * s39.GAS_CONST_R * 288.15), use_shifted=True)
     nx, ny, nz, periodic = 24, 6, 12, 2
     faces = {"x-": -101, "x+": -201, "z-": -10, "z+": -1000, "y-": 0, "y+": 0}
@@ -63,7 +67,7 @@ def test_d3q39_checkpoint_restart_bitwise(pkg, built_lib, tmp_path):
     def make():
         ctx = cap.Context(0)
         _, f, g = ctx.d3q39_equilibrium(params, 1.0, c.mach, 0.0, 0.0, c.temperature, lm0)
-        ctx.level_register(0, cap.ELBM_D3Q39, cap.ELBM_STORE_FP64, [[0, 0, 0, nx - 1, ny - 1, nz - 1]])
+        ctx.level_register(0, cap.ELBM_D3Q39, store, [[0, 0, 0, nx - 1, ny - 1, nz - 1]])
         ctx.set_d3q39_params(0, params)
         ctx.set_links39(0, 0, st, cap.make_d3q39_bc([1] * 8, [6] + [1] * 7, f, g, [f] * 8, [g] * 8, [f] * 8,
                                                      [g] * 8, (c.mach, 0.0, 0.0, c.temperature)))

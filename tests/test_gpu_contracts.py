@@ -1,0 +1,189 @@
+"""Long-horizon accuracy of the FP32 deviation storage against the FP64 path on
+the same GPU (the FP64 path is the one pinned to the oracle), on the learned-
+alpha boundary layer and the flow past a sphere, plus the D3Q39 wedge run well
+past its start-up ramps.
+
+- boundary layer (u = 0.06, nu = 2e-5, +-5e-3 noise, flat-plate faces) on a
+  128x64x64 sub-box of the 512x256x256 case, 1000 steps.  At Re ~ 2e5 on 64
+  nodes the flow is chaotic: the FP64 path started from the FP32-rounded
+  initial state leaves its own trajectory by O(1) within 1000 steps, so the
+  FP32 path is held node by node to that measured spread, and the box-averaged
+  velocity profiles are reported; a check-mode window then shows that every
+  node whose entropy condition has a root inside the positivity bracket meets
+  |H(f + alpha Delta) - H(f)| <= 1e-10 (the rare nodes without one fall back
+  to alpha = 2 and are counted);
+- sphere 256x128x128 (r = 16 icosphere, interpolated wall links), 2000 steps:
+  rho within 1e-4 and the rms of u within 1e-4 of the inlet speed; the largest
+  u difference within 1e-3 (FP32 rounding of every step accumulates; the FP64
+  path from an FP32-rounded start stays within 1e-7, so this is not chaos);
+- D3Q39 384x48x192 Mach 1.5 wedge (48-node span between inviscid side walls,
+  the negative-population repair after every step), 300 steps (three times the start-up ramp),
+  FP64 and FP32 deviation storage of f and g (multipliers, alpha and all
+  arithmetic FP64): finite fields, no multiplier solve capped, no fallbacks,
+  and the FP32 path's errors in rho, u, T and alpha against the FP64 path.
+
+Each test prints one line "CONTRACT {json}" with the measured max / rms errors."""
+import json
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _ctx(pkg, storage, st, f0, bp, record_alpha=True):
+    cap = pkg.capi
+    nz, ny, nx = st.shape[1:]
+    ctx = cap.Context(0)
+    ctx.level_register(0, cap.ELBM_D3Q27, storage, [[0, 0, 0, nx - 1, ny - 1, nz - 1]])
+    ctx.set_d3q27_params(0, cap.make_d3q27_params(**dict(bp, record_alpha=int(record_alpha))))
+    ctx.set_links(0, 0, st)
+    ctx.upload(0, 0, f0)
+    return ctx
+
+
+def _errors(lat, f64, f32, a64, a32, u_scale, fluid):
+    f64, f32, a64, a32 = f64[:, fluid], f32[:, fluid], a64[fluid], a32[fluid]
+    r64, u64 = lat.moments27(f64)
+    r32, u32 = lat.moments27(f32)
+    er = np.abs(r32 - r64) / r64
+    eu = np.abs(u32 - u64).max(axis=-1) / u_scale
+    ea = np.abs(a32 - a64)
+    return {"rho_max": float(er.max()), "rho_rms": float(np.sqrt(np.mean(er ** 2))),
+            "u_max": float(eu.max()), "u_rms": float(np.sqrt(np.mean(eu ** 2))),
+            "alpha_max": float(ea.max()), "alpha_rms": float(np.sqrt(np.mean(ea ** 2)))}
+
+
+def _run(pkg, storage, st, f0, bp, steps, fluid, check=False):
+    """steps steps; returns the populations and alpha, the fallback
+    fraction, and (check) the statistics of a 5-step check-mode window."""
+    cap = pkg.capi
+    ctx = _ctx(pkg, storage, st, f0, bp)
+    s = ctx.step(0, steps)
+    assert s["status"] & 1 == 0, s
+    f = ctx.download(0)
+    a = ctx.download_alpha(0)
+    chk = None
+    if check:
+        ctx.set_d3q27_params(0, cap.make_d3q27_params(**dict(bp, check_dH=1)))
+        chk = ctx.step(0, 5)
+    ctx.close()
+    return f, a, s["fallbacks"] / s["node_updates"], chk
+
+
+def _fp32_rounded(lat, f0):
+    """The state as FP32 deviations would hold it: w + float32(f - w)."""
+    w = lat.W.reshape((27,) + (1,) * (f0.ndim - 1))
+    return w + (f0 - w).astype(np.float32).astype(np.float64)
+
+
+def test_boundary_layer_fp32_vs_fp64_1000_steps(pkg, built_lib):
+    geo, lat, cap = pkg.geometry, pkg.lattice, pkg.capi
+    nx, ny, nz, u_in = 128, 64, 64, 0.06
+    st = geo.box_state27(nx, ny, nz, geo.flat_plate_faces())
+    f0 = geo.perturbed_equilibrium(nx, ny, nz, (u_in, 0.0, 0.0), 5e-3, seed=1239)
+    bp = geo.d3q27_boundary_params((u_in, 0.0, 0.0), 2e-5)
+    fluid = st[0] >= 0
+    steps = 1000
+    f64, a64, fb64, _ = _run(pkg, cap.ELBM_STORE_FP64, st, f0, bp, steps, fluid)
+    f32, a32, fb32, chk = _run(pkg, cap.ELBM_STORE_FP32_DEV, st, f0, bp, steps, fluid, check=True)
+    p64, pa64, _, _ = _run(pkg, cap.ELBM_STORE_FP64, st, _fp32_rounded(lat, f0), bp, steps, fluid)
+    e = _errors(lat, f64, f32, a64, a32, u_in, fluid)
+    sens = _errors(lat, f64, p64, a64, pa64, u_in, fluid)
+    # the box-averaged streamwise velocity profile u(z)
+    _, u64 = lat.moments27(f64)
+    _, u32 = lat.moments27(f32)
+    prof = float(np.max(np.abs(u32[..., 0].mean(axis=(1, 2)) - u64[..., 0].mean(axis=(1, 2)))) / u_in)
+    e.update(case="boundary layer 128x64x64, 1000 steps", max_abs_dH=chk["max_abs_dH"], dh_over=chk["dh_over_tol"],
+             check_window_fallbacks=chk["fallbacks"], fallback_fraction_fp64=fb64, fallback_fraction_fp32=fb32,
+             mean_u_profile_max=prof,
+             fp64_from_fp32_rounded_start={k: v for k, v in sens.items() if k.startswith(("rho", "u"))})
+    print("CONTRACT " + json.dumps(e))
+    assert np.isfinite(f32[:, fluid]).all()
+    # Re = 0.06 x 64 / 2e-5 ~ 2e5 on this machine: the FP64 path's own difference from an FP32-rounded
+    # start bounds what can be asked of the FP32 path node by node
+    assert e["rho_max"] <= max(1e-4, 3 * sens["rho_max"]) and e["u_max"] <= max(1e-4, 3 * sens["u_max"])
+    assert fb64 <= 1e-5 and fb32 <= 1e-5
+    # every node whose entropy condition has a root inside the positivity bracket meets the tolerance;
+    # the others (counted as fallbacks) have none to find
+    assert chk["dh_over_tol"] <= chk["fallbacks"]
+
+
+def test_sphere_fp32_vs_fp64_2000_steps(pkg, built_lib):
+    geo, lat, cap = pkg.geometry, pkg.lattice, pkg.capi
+    nx, ny, nz, u_in = 256, 128, 128, 0.08
+    st = geo.box_state27(nx, ny, nz, geo.sphere_faces())
+    cap.mark_triangles(st, (0.0, 0.0, 0.0), 1.0, geo.icosphere(4, 16.0, (64.0, 64.0, 64.0)))
+    f0 = geo.perturbed_equilibrium(nx, ny, nz, (u_in, 0.0, 0.0), 1e-3, seed=1236)
+    solid = st[0] == -1001
+    f0[:, solid] = lat.W[:, None]
+    bp = geo.d3q27_boundary_params((u_in, 0.0, 0.0), 5e-4)
+    fluid = ~solid
+    steps = 2000
+    f64, a64, fb64, _ = _run(pkg, cap.ELBM_STORE_FP64, st, f0, bp, steps, fluid)
+    f32, a32, fb32, chk = _run(pkg, cap.ELBM_STORE_FP32_DEV, st, f0, bp, steps, fluid, check=True)
+    # the flow's own sensitivity: the FP64 path from the initial state rounded as FP32 storage rounds it
+    p64, pa64, _, _ = _run(pkg, cap.ELBM_STORE_FP64, st, _fp32_rounded(lat, f0), bp, steps, fluid)
+    e = _errors(lat, f64, f32, a64, a32, u_in, fluid)
+    sens = _errors(lat, f64, p64, a64, pa64, u_in, fluid)
+    e.update(case="sphere 256x128x128, 2000 steps", max_abs_dH=chk["max_abs_dH"], dh_over=chk["dh_over_tol"],
+             fallback_fraction_fp64=fb64, fallback_fraction_fp32=fb32,
+             fp64_from_fp32_rounded_start={k: v for k, v in sens.items() if k.startswith(("rho", "u"))})
+    print("CONTRACT " + json.dumps(e))
+    assert np.isfinite(f32[:, fluid]).all()
+    # rho and the rms of u within 1e-4; the largest u difference, where FP32 rounding of every step
+    # accumulates over 2000 steps (measured 3.6e-4 of the inlet speed), within 1e-3
+    assert e["rho_max"] <= 1e-4 and e["u_rms"] <= 1e-4 and e["u_max"] <= 1e-3
+    assert chk["dh_over_tol"] == 0 and chk["max_abs_dH"] <= 1e-10
+
+
+def _wedge(pkg, storage, steps):
+    from oracle import oracle39 as o39
+
+    setup39, cap = pkg.d3q39_setup, pkg.capi
+    c = setup39.wedge_case_consts(nu_lattice=2e-4)
+    k = o39.consts(c)
+    lm0 = setup39.freestream_start_lm(c)
+    _, f, g, _ = o39.init_node(k, 1.0, c.mach, 0.0, 0.0, c.temperature, lm0)
+    nx, ny, nz, periodic = 384, 48, 192, 0
+    st = setup39.wedge_case_state(nx, ny, nz)
+    shape = (nz, ny, nx)
+    bc = cap.make_d3q39_bc([1] * 8, [6] + [1] * 7, f, g, [f] * 8, [g] * 8, [f] * 8, [g] * 8,
+                           (c.mach, 0.0, 0.0, c.temperature))
+    ctx = cap.Context(0)
+    ctx.level_register(0, cap.ELBM_D3Q39, storage, [[0, 0, 0, nx - 1, ny - 1, nz - 1]])
+    ctx.set_d3q39_params(0, cap.make_d3q39_params(c, timestep=0, periodic=periodic, damp=1))
+    ctx.set_links39(0, 0, st, bc)
+    ctx.init_level39(0, 0, np.stack([np.full(shape, 1.0), np.full(shape, c.mach), np.zeros(shape),
+                                     np.zeros(shape), np.full(shape, c.temperature)]), lm0)
+    s = ctx.step(0, steps)
+    out = ctx.download39(0)
+    ctx.close()
+    fluid = st[0] >= 0
+    assert s["node_updates"] == steps * fluid.sum() and s["fallbacks"] == 0 and s["status"] & 1 == 0
+    assert np.isfinite(out["fout"][:, fluid]).all() and np.isfinite(out["gout"][:, fluid]).all()
+    return c, out, fluid, s
+
+
+def test_d3q39_wedge_fp32_vs_fp64_300_steps(pkg, built_lib):
+    """The D3Q39 wedge (384x48x192, Mach 1.5) with FP32 deviation storage of f and g
+    (FP64 multipliers, alpha and arithmetic) against the FP64 path, 300 steps (three
+    times the start-up ramp): the errors in rho, u, T and alpha at the fluid nodes."""
+    cap = pkg.capi
+    steps = 300
+    c, o64, fluid, s64 = _wedge(pkg, cap.ELBM_STORE_FP64, steps)
+    _, o32, _, s32 = _wedge(pkg, cap.ELBM_STORE_FP32_DEV, steps)
+    m64, m32 = o64["macro"][:, fluid], o32["macro"][:, fluid]
+    rel = {"rho": np.abs(m32[0] - m64[0]) / m64[0],
+           "u": np.sqrt(((m32[1:4] - m64[1:4]) ** 2).sum(axis=0)) / c.mach,
+           "T": np.abs(m32[4] - m64[4]) / m64[4],
+           "alpha": np.abs(o32["alpha"][fluid] - o64["alpha"][fluid])}
+    e = {"case": f"D3Q39 wedge 384x48x192 FP32 vs FP64, {steps} steps",
+         "lm_iters_per_node_fp64": s64["newton_iters"] / s64["node_updates"],
+         "lm_iters_per_node_fp32": s32["newton_iters"] / s32["node_updates"],
+         "rho_min": float(m64[0].min()), "rho_max": float(m64[0].max())}
+    for k, v in rel.items():
+        e[k + "_max"], e[k + "_rms"] = float(v.max()), float(np.sqrt(np.mean(v ** 2)))
+    print("CONTRACT " + json.dumps(e))
+    assert e["rho_max"] <= 1e-3 and e["u_max"] <= 1e-3 and e["T_max"] <= 1e-3
+    assert e["rho_rms"] <= 1e-4 and e["u_rms"] <= 1e-4 and e["T_rms"] <= 1e-4

@@ -61,6 +61,36 @@ def test_d3q39_periodic_parity(pkg, o39, built_lib, start_step, steps):
     ctx.close()
 
 
+def test_d3q39_fp32_storage_periodic(pkg, o39, built_lib):
+    """FP32 deviation storage of f and g (the multipliers, alpha and every operation
+    stay FP64) against the oracle's FP64 step on the periodic box: each stored
+    population is rounded once per step to a float deviation from the box's
+    per-direction mean, so f and g stay within 1e-6 relative over 6 steps; the
+    rounding error of the initial state alone is under 1e-7."""
+    setup39, cap = pkg.d3q39_setup, pkg.capi
+    c = setup39.wedge_case_consts()
+    k = o39.consts(c)
+    nx, ny, nz, steps = 10, 6, 5, 6
+    lev = _init(o39, setup39, c, k, nx, ny, nz, noise=0.01, seed=11)
+    ctx = cap.Context(0)
+    ctx.level_register(0, cap.ELBM_D3Q39, cap.ELBM_STORE_FP32_DEV, [[0, 0, 0, nx - 1, ny - 1, nz - 1]])
+    ctx.set_d3q39_params(0, cap.make_d3q39_params(c, timestep=0))
+    ctx.upload39(0, 0, lev.fout, lev.gout, lev.lm, lev.w_vel)
+    start = ctx.download39(0)
+    for name, ref in (("fout", lev.fout), ("gout", lev.gout)):
+        assert np.max(np.abs(start[name] - ref) / np.abs(ref)) <= 1e-7, name
+    st = ctx.step(0, steps)
+    out = ctx.download39(0)
+    ctx.close()
+    for s in range(steps):
+        o39.step_periodic(k, lev, s)
+    assert st["fallbacks"] == 0 and st["node_updates"] == steps * nx * ny * nz
+    for name, ref in (("fout", lev.fout), ("gout", lev.gout)):
+        rel = np.max(np.abs(out[name] - ref) / np.abs(ref))
+        print(f"FP32 storage {name}: {rel:.3e}")
+        assert rel <= 1e-6, (name, rel)
+
+
 @pytest.mark.parametrize("shifted,outlet_type,side", [(0, 6, 0), (1, 6, 0), (1, 2, 0), (0, 1, -11), (1, 6, -11)])
 def test_d3q39_link_codes_parity(pkg, o39, built_lib, shifted, outlet_type, side):
     """A D3Q39 box with an inlet, an outlet, a bounce-back wall, a freestream
@@ -115,7 +145,7 @@ def test_d3q39_link_codes_parity(pkg, o39, built_lib, shifted, outlet_type, side
     ctx.close()
 
 
-def _wall_case(pkg, o39, seed, outlet_type, nx=16, ny=6, nz=8, mach=1.5, wedge=False, shifted=True):
+def _wall_case(pkg, o39, seed, outlet_type, nx=16, ny=6, nz=8, mach=1.5, wedge=False, shifted=True, sidewalls=False):
     """Shifted D3Q39 box (Mach 1.5 along +x): inlet at x-, outlet at x+, a
     bounce-back floor, a freestream top, periodic in y, and a solid block on
     the floor whose fluid neighbours carry interpolated wall links with random
@@ -131,7 +161,12 @@ def _wall_case(pkg, o39, seed, outlet_type, nx=16, ny=6, nz=8, mach=1.5, wedge=F
     faces = {"x-": -101, "x+": -201, "z-": -10, "z+": -1000, "y-": 0, "y+": 0}
     periodic = 2
     rng = np.random.default_rng(seed)
-    if wedge:
+    if wedge and sidewalls:
+        # the wedge case's faces (inviscid side walls): behind the back face the side-wall nodes have
+        # inviscid links whose axis links are wall links, which no branch of inviscid_edge.f95 covers
+        faces, periodic = s39.WEDGE_FACES, 0
+        st = s39.wedge_state39(nx, ny, nz, 5.0, 12.0, 20.0, faces, periodic=periodic, priority=s39.WEDGE_PRIORITY)
+    elif wedge:
         # a 20-degree wedge across the span from x = 5 to x = 12, wall distances from the geometry
         st = s39.wedge_state39(nx, ny, nz, 5.0, 12.0, 20.0, faces, periodic=periodic)
     else:
@@ -164,9 +199,11 @@ def _wall_case(pkg, o39, seed, outlet_type, nx=16, ny=6, nz=8, mach=1.5, wedge=F
     return c, k, st, lev, periodic, o39.bc(*args), pkg.capi.make_d3q39_bc(*args)
 
 
-@pytest.mark.parametrize("seed,outlet_type,mach,warm,steps,wedge", [(3, 6, 1.5, 0, 5, False), (4, 1, 0.8, 0, 8, False),
-                                                                   (5, 6, 0.8, 97, 6, False), (6, 6, 1.5, 0, 5, True)])
-def test_d3q39_wall_links_parity(pkg, o39, built_lib, seed, outlet_type, mach, warm, steps, wedge):
+@pytest.mark.parametrize("seed,outlet_type,mach,warm,steps,wedge,sidewalls",
+                         [(3, 6, 1.5, 0, 5, False, False), (4, 1, 0.8, 0, 8, False, False),
+                          (5, 6, 0.8, 97, 6, False, False), (6, 6, 1.5, 0, 5, True, False),
+                          (9, 6, 1.5, 0, 6, True, True)])
+def test_d3q39_wall_links_parity(pkg, o39, built_lib, seed, outlet_type, mach, warm, steps, wedge, sidewalls):
     """Interpolated wall links on the shifted lattice (target_finder, the target
     Newton solve, shifted_ibb) next to the other boundary codes: the GPU step
     against the oracle's push loop, 1e-12 relative.  Steps 0..4 (start-up
@@ -178,10 +215,12 @@ def test_d3q39_wall_links_parity(pkg, o39, built_lib, seed, outlet_type, mach, w
     Newton stops at |delta| <= 1e-7, the closed-form alpha cancels where it is
     small): the oracle fed its own state with 1-ulp noise moves by ~1e-12 per
     step at the wall nodes.  That late run is held to 20 times the oracle's own
-    spread under such noise (and never looser than 1e-9)."""
+    spread under such noise (and never looser than 1e-9).  The last case has the
+    wedge case's inviscid side walls, including links no branch of the
+    reference's inviscid table covers (nothing written for them)."""
     cap = pkg.capi
     c, k, st, lev, periodic, b, cb = _wall_case(pkg, o39, seed, outlet_type, mach=mach, wedge=wedge,
-                                                nx=20 if wedge else 16, nz=10 if wedge else 8)
+                                                nx=20 if wedge else 16, nz=10 if wedge else 8, sidewalls=sidewalls)
     nz, ny, nx = lev.shape
     prev_f, prev_g = lev.fout.copy(), lev.gout.copy()
     for step in range(warm):

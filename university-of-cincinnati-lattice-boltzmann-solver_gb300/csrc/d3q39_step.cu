@@ -238,7 +238,31 @@ __device__ double alpha39(const D3Q39Dev& k, const double (&fi)[Q], const double
   return na;
 }
 
-__global__ void __launch_bounds__(64) d3q39_fp64_kernel(const Step39Args a) {
+// Population loads and stores of either storage: FP64 as is, FP32 as float
+// deviations from the box's per-direction reference (ref[j] for f, ref[39 + j] for g).
+template <bool F32>
+__device__ __forceinline__ double ld_f39(const Step39Args& a, int pop, int64_t s) {
+  if constexpr (F32) return (double)a.fsrc32[(int64_t)pop * a.plane + s] + a.ref[pop];
+  else return a.fsrc[(int64_t)pop * a.plane + s];
+}
+template <bool F32>
+__device__ __forceinline__ double ld_g39(const Step39Args& a, int pop, int64_t s) {
+  if constexpr (F32) return (double)a.gsrc32[(int64_t)pop * a.plane + s] + a.ref[Q + pop];
+  else return a.gsrc[(int64_t)pop * a.plane + s];
+}
+template <bool F32>
+__device__ __forceinline__ void st_fg39(const Step39Args& a, int i, int64_t n, double f, double g) {
+  if constexpr (F32) {
+    a.fdst32[(int64_t)i * a.plane + n] = (float)(f - a.ref[i]);
+    a.gdst32[(int64_t)i * a.plane + n] = (float)(g - a.ref[Q + i]);
+  } else {
+    a.fdst[(int64_t)i * a.plane + n] = f;
+    a.gdst[(int64_t)i * a.plane + n] = g;
+  }
+}
+
+template <bool F32>
+__global__ void __launch_bounds__(64) d3q39_step_kernel(const Step39Args a) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= a.N) return;
   const D3Q39Dev& k = a.k;
@@ -254,8 +278,8 @@ __global__ void __launch_bounds__(64) d3q39_fp64_kernel(const Step39Args a) {
       sy = (sy % a.ny + a.ny) % a.ny;
       sz = (sz % a.nz + a.nz) % a.nz;
       const int64_t s = ((int64_t)sz * a.ny + sy) * a.nx + sx;
-      f[j] = a.fsrc[(int64_t)j * a.plane + s];
-      g[j] = a.gsrc[(int64_t)j * a.plane + s];
+      f[j] = ld_f39<F32>(a, j, s);
+      g[j] = ld_g39<F32>(a, j, s);
     }
   } else {
     // boundary record: what the push loop leaves in each post-streaming slot
@@ -271,8 +295,8 @@ __global__ void __launch_bounds__(64) d3q39_fp64_kernel(const Step39Args a) {
         sy = (sy % a.ny + a.ny) % a.ny;
         sz = (sz % a.nz + a.nz) % a.nz;
         const int64_t s = ((int64_t)sz * a.ny + sy) * a.nx + sx;
-        f[j] = a.fsrc[(int64_t)pop * a.plane + s];
-        g[j] = a.gsrc[(int64_t)pop * a.plane + s];
+        f[j] = ld_f39<F32>(a, pop, s);
+        g[j] = ld_g39<F32>(a, pop, s);
       } else if (kind == L39_EQ) {
         const int table = (int)((w >> 8) & 31u);
         f[j] = a.eqf[table * Q + pop];
@@ -379,8 +403,7 @@ __global__ void __launch_bounds__(64) d3q39_fp64_kernel(const Step39Args a) {
     const double ch = q_lead * (c39.cx[i] * q1 + c39.cy[i] * q2 + c39.cz[i] * q3);
     const double fo = f[i] + alpha * b1 * (fd[i] - qb) + b2 * qb;
     const double go = g[i] + alpha * b1 * (gd[i] - ch) + b2 * ch;
-    a.fdst[(int64_t)i * a.plane + n] = fo;
-    a.gdst[(int64_t)i * a.plane + n] = go;
+    st_fg39<F32>(a, i, n, fo, go);
     neg |= fo < 0.0;
   }
   for (int r = 0; r < NL; ++r) a.lm[(int64_t)r * a.plane + n] = lm[r];
@@ -638,6 +661,7 @@ __device__ __noinline__ void unshifted_ibb39(const D3Q39Dev& k, int d, int code_
 }
 
 // Value of a post-streaming slot described by a link word (PULL / EQ / STALE).
+template <bool F32>
 __device__ __forceinline__ void slot39(const Step39Args& a, uint32_t w, int64_t b, int j, int x, int y, int z,
                                        double& f, double& g) {
   const uint32_t kind = w & 3u;
@@ -649,8 +673,8 @@ __device__ __forceinline__ void slot39(const Step39Args& a, uint32_t w, int64_t 
     sy = (sy % a.ny + a.ny) % a.ny;
     sz = (sz % a.nz + a.nz) % a.nz;
     const int64_t s = ((int64_t)sz * a.ny + sy) * a.nx + sx;
-    f = a.fsrc[(int64_t)pop * a.plane + s];
-    g = a.gsrc[(int64_t)pop * a.plane + s];
+    f = ld_f39<F32>(a, pop, s);
+    g = ld_g39<F32>(a, pop, s);
   } else if (kind == L39_EQ) {
     const int table = (int)((w >> 8) & 31u);
     f = a.eqf[table * Q + pop];
@@ -668,6 +692,7 @@ __device__ __forceinline__ void slot39(const Step39Args& a, uint32_t w, int64_t 
 // 1055-1082) and, for every wall link, shifted_ibb or the unshifted closure.
 // Reads the previous step's macroscopic planes, multipliers and post-collision
 // populations before the step kernel overwrites them (same stream).
+template <bool F32>
 __global__ void __launch_bounds__(64) d3q39_wall_kernel(const Step39Args a) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= a.nwall) return;
@@ -709,7 +734,7 @@ __global__ void __launch_bounds__(64) d3q39_wall_kernel(const Step39Args a) {
       }
       const int s = R.code[c39.opp[j]] < -1000 ? c39.erp[j] : j;
       double fs, gs;
-      slot39(a, R.snap[s], b, s, x, y, z, fs, gs);
+      slot39<F32>(a, R.snap[s], b, s, x, y, z, fs, gs);
       r_ = r_ + fs;
     }
     rho_t = r_;
@@ -929,7 +954,8 @@ __global__ void d3q39_average_down_kernel(const Box39View* __restrict__ fbs, con
 void launch_d3q39_fp64(const Step39Args& a, cudaStream_t s) {
   const int threads = 64;
   const int64_t blocks = (a.N + threads - 1) / threads;
-  d3q39_fp64_kernel<<<(unsigned)blocks, threads, 0, s>>>(a);
+  if (a.fsrc32) d3q39_step_kernel<true><<<(unsigned)blocks, threads, 0, s>>>(a);
+  else d3q39_step_kernel<false><<<(unsigned)blocks, threads, 0, s>>>(a);
 }
 
 // damp_it.f95:64-177, fout part, on a box with link codes (see the oracle's
@@ -941,8 +967,12 @@ void launch_d3q39_fp64(const Step39Args& a, cudaStream_t s) {
 // direction in z, y, x order, so a neighbour that comes earlier in that order
 // and is itself negative is read repaired: damp39_value follows such chains
 // (up to kDampChain links; longer chains read the unrepaired value).
+// FP32 storage (src32 set): float deviations from ref, repaired values
+// rounded back the same way and untouched ones copied as stored.
 struct Damp39 {
   const double* src;
+  const float* src32;
+  const double* ref;
   const unsigned long long* dmask;
   const double* eq;
   int nx, ny, nz, periodic, shifted;
@@ -961,8 +991,12 @@ __device__ int64_t damp39_node(const Damp39& P, int x, int y, int z) {
   return ((int64_t)z * P.ny + y) * P.nx + x;
 }
 
+__device__ __forceinline__ double damp39_ld(const Damp39& P, int i, int64_t m) {
+  return P.src32 ? (double)P.src32[(int64_t)i * P.plane + m] + P.ref[i] : P.src[(int64_t)i * P.plane + m];
+}
+
 __device__ double damp39_value(const Damp39& P, int i, int64_t n, int depth) {
-  const double v = P.src[(int64_t)i * P.plane + n];
+  const double v = damp39_ld(P, i, n);
   if (!(v < 0.0)) return v;
   const int x = (int)(n % P.nx), y = (int)((n / P.nx) % P.ny), z = (int)(n / ((int64_t)P.nx * P.ny));
   const int cx = c39.cx[i], cy = c39.cy[i], cz = c39.cz[i];
@@ -970,7 +1004,7 @@ __device__ double damp39_value(const Damp39& P, int i, int64_t n, int depth) {
   auto read = [&](int64_t m) -> double {
     if (m < 0) return P.eq[i];
     if (m < n && depth > 0) return damp39_value(P, i, m, depth - 1);  // already repaired in the sweep
-    return P.src[(int64_t)i * P.plane + m];
+    return damp39_ld(P, i, m);
   };
   const double fp = read(mp), fm = read(mm);
   const unsigned long long msk = P.dmask ? P.dmask[n] : ~0ull;  // no link codes: every link interior
@@ -1009,24 +1043,30 @@ __device__ double damp39_value(const Damp39& P, int i, int64_t n, int depth) {
   return out;
 }
 
-__global__ void d3q39_damp_links_kernel(const Damp39 P, double* __restrict__ dst, DevStats* stats) {
+__global__ void d3q39_damp_links_kernel(const Damp39 P, void* __restrict__ dst, DevStats* stats) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y;
   if (n >= (int64_t)P.nx * P.ny * P.nz) return;
-  const double v = P.src[(int64_t)i * P.plane + n];
-  double out = v;
+  const int64_t e = (int64_t)i * P.plane + n;
+  const double v = damp39_ld(P, i, n);
   if (v < 0.0) {
-    out = damp39_value(P, i, n, kDampChain);
+    const double out = damp39_value(P, i, n, kDampChain);
     atomicAdd(&stats->exact_nodes, 1ull);
+    if (P.src32) static_cast<float*>(dst)[e] = (float)(out - P.ref[i]);
+    else static_cast<double*>(dst)[e] = out;
+  } else if (P.src32) {
+    static_cast<float*>(dst)[e] = P.src32[e];
+  } else {
+    static_cast<double*>(dst)[e] = P.src[e];
   }
-  dst[(int64_t)i * P.plane + n] = out;
 }
 
-void launch_d3q39_damp_links(const double* src, double* dst, const unsigned long long* dmask, int nx, int ny, int nz,
-                             int64_t plane, int periodic, int shifted, const int* lo, const int* hi, const double* eq,
-                             DevStats* stats, cudaStream_t s) {
+void launch_d3q39_damp_links(const void* src, void* dst, const double* ref, const unsigned long long* dmask, int nx,
+                             int ny, int nz, int64_t plane, int periodic, int shifted, const int* lo, const int* hi,
+                             const double* eq, DevStats* stats, cudaStream_t s) {
   const int64_t N = (int64_t)nx * ny * nz;
-  Damp39 P{src, dmask, eq, nx, ny, nz, periodic, shifted, plane, make_int3(lo[0], lo[1], lo[2]),
+  Damp39 P{ref ? nullptr : static_cast<const double*>(src), ref ? static_cast<const float*>(src) : nullptr, ref,
+           dmask, eq, nx, ny, nz, periodic, shifted, plane, make_int3(lo[0], lo[1], lo[2]),
            make_int3(hi[0], hi[1], hi[2])};
   dim3 grid((unsigned)((N + 255) / 256), 39);
   d3q39_damp_links_kernel<<<grid, 256, 0, s>>>(P, dst, stats);
@@ -1040,7 +1080,9 @@ void launch_d3q39_init(const Step39Args& a, const double* lm0, unsigned long lon
 void launch_d3q39_walls(const Step39Args& a, cudaStream_t s) {
   if (a.nwall <= 0) return;
   const int threads = 64;
-  d3q39_wall_kernel<<<(unsigned)((a.nwall + threads - 1) / threads), threads, 0, s>>>(a);
+  const unsigned blocks = (unsigned)((a.nwall + threads - 1) / threads);
+  if (a.fsrc32) d3q39_wall_kernel<true><<<blocks, threads, 0, s>>>(a);
+  else d3q39_wall_kernel<false><<<blocks, threads, 0, s>>>(a);
 }
 
 void launch_d3q39_explode(const Box39View* coarse, const Box39View& fine, const int32_t* ghost, const int32_t* src,

@@ -72,6 +72,13 @@ struct Step39Args {
   const int32_t* recwall;     // per boundary record: its wall record or -1
   double* wallf;              // 39 per wall record: the wall values of f, then g, of this step
   double* wallg;
+  // FP32 storage (fsrc32 set): f and g held as float deviations from a per-direction reference
+  // (ref: 39 values for f, then 39 for g); the step computes in FP64 as with FP64 storage
+  const float* fsrc32;
+  const float* gsrc32;
+  float* fdst32;
+  float* gdst32;
+  const double* ref;
 };
 
 // Link words of D3Q39 boundary records.
@@ -112,8 +119,9 @@ void launch_d3q39_average_down(const Box39View* fine, const Box39View& coarse, c
 void launch_ggm_pgs(const double* macro, int64_t plane, int nx, int ny, int nz, const uint16_t* mask,
                     const double* ggm, double sensitivity, int reach, uint8_t* tags, cudaStream_t s);
 // dmask nullptr: a box without link codes (every link interior)
-void launch_d3q39_damp_links(const double* src, double* dst, const unsigned long long* dmask, int nx, int ny, int nz,
-                             int64_t plane, int periodic, int shifted, const int* lo, const int* hi, const double* eq,
-                             DevStats* stats, cudaStream_t s);
+// src, dst: FP64 planes, or (ref set) float deviations from ref
+void launch_d3q39_damp_links(const void* src, void* dst, const double* ref, const unsigned long long* dmask, int nx,
+                             int ny, int nz, int64_t plane, int periodic, int shifted, const int* lo, const int* hi,
+                             const double* eq, DevStats* stats, cudaStream_t s);
 
 }  // namespace elbm

@@ -218,10 +218,9 @@ int decode_links39(const int32_t* st, int ngs, int nx, int ny, int nz, int perio
             int32_t codes[Q39];
             for (int q = 0; q < Q39; ++q) codes[q] = code(q, x, y, z);
             int j = 0, d[3];
-            if (!inviscid39(L0, i, codes, j, d)) {
-              why = "an inviscid link whose unit and speed-2 axis links carry no -11 (the reference leaves it unset)";
-              return ELBM_E_UNSUPPORTED;
-            }
+            // no branch of inviscid_edge.f95 applies (no unit or speed-2 axis link of the direction is
+            // -11, e.g. where a wall link took one): the reference writes nothing for this link
+            if (!inviscid39(L0, i, codes, j, d)) continue;
             const int64_t r = node_at(x + d[0], y + d[1], z + d[2]);
             if (r >= 0) emit(r, j, kpos + 1, fo[i]);
             continue;
