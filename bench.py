@@ -189,6 +189,68 @@ def cpu_baseline_sample(pkg, budget_s=15.0):
             "sample": f"{sx}x{sy}x{sz} sub-box of the workload, {steps} FP64 Newton-alpha steps, {dt:.1f} s"}
 
 
+def d3q27_config_legs(pkg, local_rank, cpu=True, budget_s=10.0):
+    """The two smaller D3Q27 configurations on one GPU: the 64^3 flat-plate
+    boundary layer (FP64, Newton alpha, nu = 1e-3, u = 0.05, +-1e-3 noise, 200
+    steps; the reference's own CPU-runnable case, with the oracle timed on the
+    same box's host cores for a bounded number of its steps) and the
+    256x128x128 sphere (5,120 triangles, r = 16, u = 0.08, nu = 5e-4) in FP64 and
+    in FP32 deviation storage, 20 steps each after one untimed step."""
+    geo, cap = pkg.geometry, pkg.capi
+    out = {}
+    n = 64
+    st = geo.box_state27(n, n, n, geo.flat_plate_faces())
+    f0 = geo.perturbed_equilibrium(n, n, n, (0.05, 0.0, 0.0), 1e-3, seed=SEED)
+    bp = geo.d3q27_boundary_params((0.05, 0.0, 0.0), 1e-3)
+    ctx = cap.Context(local_rank)
+    ctx.level_register(0, cap.ELBM_D3Q27, cap.ELBM_STORE_FP64, [[0, 0, 0, n - 1, n - 1, n - 1]])
+    ctx.set_d3q27_params(0, cap.make_d3q27_params(**bp))
+    ctx.set_links(0, 0, st)
+    ctx.upload(0, 0, f0)
+    s = ctx.step(0, 200)
+    ctx.close()
+    leg = {"workload": "D3Q27 flat plate 64^3, FP64, Newton alpha, 200 steps",
+           "mlups": s["node_updates"] / (s["kernel_ms"] / 1e3) / 1e6, "fallbacks": s["fallbacks"],
+           "status": s["status"], "bytes_per_node": 432}
+    if cpu:
+        from oracle import oracle as orc
+
+        p = orc.params(bp["nu"], bp["fs_feq"], bp["inl_feq"], bp["outl_feq"], bp["outlet_type"])
+        f = f0.copy()
+        t0 = time.perf_counter()
+        steps = nodes = 0
+        while steps < 2 or (time.perf_counter() - t0 < budget_s and steps < 200):
+            f, _, _, so = orc.step27(st, f, p)
+            nodes += so["fluid_nodes"]
+            steps += 1
+        dt = time.perf_counter() - t0
+        leg["cpu_baseline"] = {"value": nodes / dt / 1e6, "unit": UNIT,
+                               "cores": int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1)), "kind": "port",
+                               "sample": f"the same 64^3 case, {steps} FP64 Newton-alpha steps, {dt:.1f} s"}
+    out["flat_plate_64"] = leg
+    nx, ny, nz = 256, 128, 128
+    st = geo.box_state27(nx, ny, nz, geo.sphere_faces())
+    cap.mark_triangles(st, (0.0, 0.0, 0.0), 1.0, geo.icosphere(4, 16.0, (64.0, 64.0, 64.0)))
+    f0 = geo.perturbed_equilibrium(nx, ny, nz, (0.08, 0.0, 0.0), 1e-3, seed=SEED)
+    f0[:, st[0] == -1001] = pkg.lattice.W[:, None]
+    bp = geo.d3q27_boundary_params((0.08, 0.0, 0.0), 5e-4)
+    for name, storage, bpn in (("fp64", cap.ELBM_STORE_FP64, 432), ("fp32", cap.ELBM_STORE_FP32_DEV, 216)):
+        ctx = cap.Context(local_rank)
+        ctx.level_register(0, cap.ELBM_D3Q27, storage, [[0, 0, 0, nx - 1, ny - 1, nz - 1]])
+        ctx.set_d3q27_params(0, cap.make_d3q27_params(**bp))
+        ctx.set_links(0, 0, st)
+        ctx.upload(0, 0, f0)
+        if storage == cap.ELBM_STORE_FP32_DEV:
+            ctx.autotune(0)
+        ctx.step(0, 1, want_stats=False)
+        s = ctx.step(0, 20)
+        ctx.close()
+        out["sphere_" + name] = {"workload": f"D3Q27 sphere 256x128x128, {name.upper()}, Newton alpha",
+                                 "mlups": s["node_updates"] / (s["kernel_ms"] / 1e3) / 1e6,
+                                 "fallbacks": s["fallbacks"], "status": s["status"], "bytes_per_node": bpn}
+    return out
+
+
 def d3q39_wedge_leg(pkg, local_rank, fp32=False, steps=3, size=(384, 48, 192)):
     """The compressible D3Q39 wedge case at its full size (384x48x192: 48-node span
     between inviscid side walls, 192 high; Mach 1.5, shifted lattice, 10-degree
@@ -263,6 +325,37 @@ def d3q39_cpu_sample(pkg, seconds=10.0):
                       f"threads, streaming and wall targets on one), {dt:.1f} s"}
 
 
+def amr_sphere_leg(pkg, local_rank, coarse_steps=500):
+    """The 3-level AMR case around the sphere (geometry.amr_sphere_hierarchy:
+    128x64x64 level 0, 24 and 96 boxes on levels 1 and 2, FP32 deviation
+    storage), each level on the variant its autotuner picked, coarse_steps
+    coarse steps through elbm_amr_run (the graph captured by one untimed
+    two-cycle run first): node updates of all levels over the graph replays'
+    device time, then each level stepped alone for its own MLUPS."""
+    geo, cap = pkg.geometry, pkg.capi
+    t0 = time.perf_counter()
+    H = geo.amr_sphere_hierarchy()
+    ctx = cap.Context(local_rank)
+    geo.register_amr_hierarchy(ctx, H, cap.ELBM_STORE_FP32_DEV)
+    variants = [ctx.autotune(l)[0] for l in range(len(H))]
+    setup_s = time.perf_counter() - t0
+    ctx.amr_run(len(H), 2)
+    s = ctx.amr_run(len(H), coarse_steps)
+    levels = []
+    for l, L in enumerate(H):
+        sl = ctx.step(l, 4)
+        valid = int(((L["state"][0] >= 0) & (L["state"][0] != geo.AMR_GHOST)).sum())
+        levels.append({"level": l, "boxes": L["nvalid"], "ghost_slab_boxes": len(L["boxes"]) - L["nvalid"],
+                       "valid_fluid_nodes": valid, "variant": int(variants[l]),
+                       "mlups_alone": sl["node_updates"] / (sl["kernel_ms"] / 1e3) / 1e6})
+    ctx.close()
+    return {"workload": "D3Q27 3-level AMR around the sphere, 24 + 96 fine boxes, FP32 deviation storage",
+            "coarse_steps": coarse_steps, "node_updates": s["node_updates"],
+            "mlups": s["node_updates"] / (s["kernel_ms"] / 1e3) / 1e6,
+            "graph_ms_per_coarse_step": s["kernel_ms"] / coarse_steps, "fallbacks": s["fallbacks"],
+            "status": s["status"], "levels": levels, "setup_s": setup_s}
+
+
 def learned_alpha_leg(pkg, ctx, args, bp, local_rank):
     """Harvest, train, and time the learned-alpha path; returns a summary dict."""
 
@@ -317,10 +410,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-d3q39", action="store_true", help="skip the D3Q39 wedge leg")
+    ap.add_argument("--no-amr", action="store_true", help="skip the 3-level AMR leg")
+    ap.add_argument("--amr-only", type=int, default=None, metavar="COARSE_STEPS",
+                    help="run only the 3-level AMR leg for this many coarse steps and print it")
     ap.add_argument("--size", default=None, help="NXxNYxNZ override (profiling runs on a smaller box)")
     ap.add_argument("--alpha", default="newton", choices=["newton", "fixed2"],
                     help="alpha of the timed path (fixed2 = LBGK limit, to separate the alpha solve's cost)")
-    ap.add_argument("--variant", type=int, default=None, choices=list(range(9)),
+    ap.add_argument("--variant", type=int, default=None, choices=list(range(10)),
                     help="step-kernel variant instead of the autotuner's choice")
     ap.add_argument("--d3q39-only", default=None, metavar="NXxNYxNZ",
                     help="run only the D3Q39 wedge legs (FP64 and FP32 storage) at this size and print them")
@@ -331,7 +427,7 @@ def main():
         global NX, NY, NZ
         NX, NY, NZ = (int(v) for v in args.size.lower().split("x"))
     if args.profile:
-        args.no_cpu_baseline = args.no_fp64 = args.no_d3q39 = True
+        args.no_cpu_baseline = args.no_fp64 = args.no_d3q39 = args.no_amr = True
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
@@ -348,6 +444,11 @@ def main():
     import __graft_entry__ as ge
 
     ge.build() if rank == 0 or world == 1 else None
+    if args.amr_only:
+        leg = amr_sphere_leg(ge.load_package(), local_rank, coarse_steps=args.amr_only)
+        if rank == 0:
+            print(json.dumps({"amr_sphere": leg}), flush=True)
+        return
     if args.d3q39_only:
         pkg = ge.load_package()
         size = tuple(int(v) for v in args.d3q39_only.lower().split("x"))
@@ -464,6 +565,14 @@ def main():
         if rank == 0 and world == 1 and not args.no_cpu_baseline:
             wedge["cpu_baseline"] = d3q39_cpu_sample(pkg)
 
+    amr = None
+    if not args.no_amr:
+        amr = amr_sphere_leg(pkg, local_rank)
+
+    small = None
+    if not args.no_fp64:
+        small = d3q27_config_legs(pkg, local_rank, cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline_sample(pkg)
@@ -500,6 +609,8 @@ def main():
             "plain_fp64_newton_mlups": fp64,
             "d3q39_wedge": wedge,
             "d3q39_wedge_fp32": wedge32,
+            "amr_sphere": amr,
+            "d3q27_configs": small,
             "learned_alpha": learned,
             "cpu_baseline": cpu,
         }

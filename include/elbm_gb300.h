@@ -125,7 +125,12 @@ const char* elbm_last_error_string(const elbm_ctx* ctx);
  * from_scratch (amr/modules/amr_processes.f95:383-476).  lo_hi holds 6 ints per
  * box (lo x,y,z, hi x,y,z, inclusive).  ngrow is the ghost width of the
  * population FABs the host will pass (nghosts_mid in the reference,
- * general/background_calcs/directions_and_weights.f95:355-362). */
+ * general/background_calcs/directions_and_weights.f95:355-362).  Boxes must
+ * not overlap.  A D3Q39 level of several boxes is held as one array over
+ * their bounding box (links reach across box faces in place); its links,
+ * populations, fields and initial state are complete once every box has been
+ * given (elbm_set_links39, elbm_upload_level39 / elbm_upload_macro39,
+ * elbm_init_level39). */
 int elbm_level_register(elbm_ctx* ctx, int lvl, int lattice, int storage, int nbox, const int32_t* lo_hi,
                         int ngrow);
 
@@ -380,7 +385,7 @@ int elbm_damp_level(elbm_ctx* ctx, int lvl, int64_t* repaired);
  * elbm_level_step.  chosen and ms_per_variant (room for ELBM_KERNEL_VARIANTS)
  * may be NULL.  The reference has no counterpart (it has one code path per
  * lattice). */
-#define ELBM_KERNEL_VARIANTS 9
+#define ELBM_KERNEL_VARIANTS 10
 int elbm_autotune(elbm_ctx* ctx, int lvl, int reps, int* chosen, double* ms_per_variant);
 
 /* Use kernel variant v (0: direct loads; 1, 4, 5, 6, 7: direct, registers
@@ -388,12 +393,15 @@ int elbm_autotune(elbm_ctx* ctx, int lvl, int reps, int* chosen, double* ms_per_
  * shared memory by bulk copies, persistent; 3: direct loads, persistent warps
  * taking 32-node chunks from a counter; 8: warp-specialised, a producer warp
  * keeps tensor copies (TMA) of 256-node tiles in flight into a shared-memory
- * ring while eight consumer warps collide) for the level's FP32 D3Q27 steps,
+ * ring while eight consumer warps collide; 9: direct loads at 27 offsets
+ * computed once per launch, for one-box levels whose 27 population planes
+ * stay below 2^31 elements) for the level's FP32 D3Q27 steps,
  * instead of the autotuner's choice.  Variant 2 applies to boxes with nx and
  * the plane size multiples of 4 and ny, nz >= 3, other boxes fall back to
  * variant 0; variant 8 serves FP32 levels whose boxes all have nx a multiple
- * of 4, and asking for it on another level returns ELBM_E_UNSUPPORTED with
- * the reason in elbm_last_error_string.  No counterpart in the reference. */
+ * of 4, and asking for it (or for 9 on a level it does not serve) on another
+ * level returns ELBM_E_UNSUPPORTED with the reason in elbm_last_error_string.
+ * No counterpart in the reference. */
 int elbm_set_kernel_variant(elbm_ctx* ctx, int lvl, int variant);
 
 /* Learned initial guess of alpha (no counterpart in the reference; its

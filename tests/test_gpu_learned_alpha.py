@@ -75,3 +75,59 @@ def test_learned_alpha_pipeline(pkg, built_lib):
           f"{s3['guess_misses'] / s3['node_updates']:.2e}")
     assert s3["guess_misses"] <= 0.02 * s3["node_updates"]
     ctx.close()
+
+
+def test_learned_alpha_budget(pkg, built_lib):
+    """What the learned guess could save against what the network costs, measured
+    on one state of the boundary layer (256x128x64): the step with alpha = 2 (no
+    alpha solve), with Newton from alpha = 2 and with the learned guess on the
+    tensor cores.  The whole alpha solve costs t_newton - t_fixed per node; a
+    guess still needs the power sums and at least one certified Newton step, so
+    it can save at most that.  The network (27-64-64-1, 11.8 kFLOP per node on the
+    tensor cores, and per node 128 bias + GELU evaluations and a 64-term dot
+    product on the FP32 pipe) costs more than the whole alpha solve: the learned
+    step is slower than Newton by more than the alpha solve costs, and the guess
+    saves almost no iterations (Newton converges in two from alpha = 2)."""
+    cap = pkg.capi
+    ctx, st, f0, bp = _level(pkg, cap.ELBM_ALPHA_NEWTON)
+    ctx.set_d3q27_params(0, cap.make_d3q27_params(**bp))
+    ctx.set_links(0, 0, st)
+    ctx.upload(0, 0, f0)
+    rec = ctx.alpha_harvest(0, nsteps=30, stride=3, capacity=1 << 20)
+    w, _ = ctx.alpha_mlp_train(rec, mlp_ref.init(0).astype(np.float32), epochs=8, batch=4096, lr=2e-3, seed=3)
+    ctx.close()
+    n = (256, 128, 64)
+    c0, st0, f1, bp0 = _level(pkg, cap.ELBM_ALPHA_NEWTON, n=n)
+    c0.set_d3q27_params(0, cap.make_d3q27_params(**bp0))
+    c0.set_links(0, 0, st0)
+    c0.upload(0, 0, f1)
+    c0.step(0, 20, want_stats=False)  # develop the non-equilibrium parts
+    f_mid = c0.download(0)
+    c0.close()
+    res = {}
+    for mode in (cap.ELBM_ALPHA_FIXED2, cap.ELBM_ALPHA_NEWTON, cap.ELBM_ALPHA_LEARNED):
+        c2, st2, _, bp2 = _level(pkg, mode, n=n)
+        if mode == cap.ELBM_ALPHA_LEARNED:
+            c2.set_alpha_mlp(0, w)
+        c2.set_d3q27_params(0, cap.make_d3q27_params(**bp2))
+        c2.set_links(0, 0, st2)
+        best = None
+        for _ in range(3):
+            c2.upload(0, 0, f_mid)
+            s = c2.step(0, 4)
+            if best is None or s["kernel_ms"] < best["kernel_ms"]:
+                best = s
+        res[mode] = best
+        c2.close()
+    ns = {m: 1e6 * s["kernel_ms"] / s["node_updates"] for m, s in res.items()}
+    it = {m: s["newton_iters"] / s["node_updates"] for m, s in res.items()}
+    t_alpha = ns[cap.ELBM_ALPHA_NEWTON] - ns[cap.ELBM_ALPHA_FIXED2]
+    t_net = ns[cap.ELBM_ALPHA_LEARNED] - ns[cap.ELBM_ALPHA_NEWTON]
+    print(f"BUDGET ns/node: alpha=2 {ns[cap.ELBM_ALPHA_FIXED2]:.4f}, Newton {ns[cap.ELBM_ALPHA_NEWTON]:.4f} "
+          f"({it[cap.ELBM_ALPHA_NEWTON]:.3f} iterations), learned {ns[cap.ELBM_ALPHA_LEARNED]:.4f} "
+          f"({it[cap.ELBM_ALPHA_LEARNED]:.3f} iterations); whole alpha solve {t_alpha:.4f}, network net {t_net:.4f}")
+    assert res[cap.ELBM_ALPHA_LEARNED]["fallbacks"] <= 1e-5 * res[cap.ELBM_ALPHA_LEARNED]["node_updates"]
+    # the guess saves less than a tenth of an iteration per node
+    assert it[cap.ELBM_ALPHA_NEWTON] - it[cap.ELBM_ALPHA_LEARNED] < 0.1
+    # the network costs more than the whole alpha solve it could at best replace
+    assert t_net > t_alpha

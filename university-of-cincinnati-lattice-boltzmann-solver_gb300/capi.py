@@ -20,7 +20,7 @@ ELBM_E_CUDA = -2
 ELBM_E_UNSUPPORTED = -3
 ELBM_E_STATE = -4
 ELBM_E_NUMERIC = -5
-ELBM_KERNEL_VARIANTS = 9  # FP32 D3Q27 step-kernel variants (elbm_autotune's timing array)
+ELBM_KERNEL_VARIANTS = 10  # FP32 D3Q27 step-kernel variants (elbm_autotune's timing array)
 
 ELBM_ST_NAN = 0x1
 ELBM_ST_NEWTON_FALLBACK = 0x2

@@ -19,6 +19,7 @@
 #include "links39.h"
 #include "mlp.cuh"
 #include <algorithm>
+#include <array>
 #include <random>
 #include "lattice.cuh"
 
@@ -124,6 +125,16 @@ struct Level {
   int variant = 0;  // FP32 D3Q27 kernel variant picked by elbm_autotune
   DevBuf<uint8_t> eq;  // kEqTables x Q, FP64 or FP32 deviations
   DevBuf<double> eq39f, eq39g;  // D3Q39 boundary equilibria of f and g, kEqTables x 39
+  // A D3Q39 level of several boxes is held as one internal box (the sheet) over their bounding
+  // box, so that links, wall targets and the repair reach across box faces in place: sub39 holds
+  // the caller's boxes (lo, hi); a box's state waits here until every box has one (then the sheet's
+  // state is assembled and decoded once), and the per-box calls that complete the sheet's
+  // populations, fields and initial state are counted
+  std::vector<std::array<int32_t, 6>> sub39;
+  std::vector<std::vector<int32_t>> sub39_state;
+  std::vector<int> sub39_ngrow;
+  std::vector<uint8_t> sub39_have_pops, sub39_have_macro, sub39_have_init;
+  elbm_d3q39_bc sub39_bc{};
   double fs39[4] = {0, 0, 0, 0};  // D3Q39 freestream u, v, w, T (interpolated wall links)
   // D3Q27: every box of the level in one set of arrays (one launch per step)
   int64_t plane = 0;        // nodes per population plane: the boxes, each padded to whole 32-node chunks
@@ -388,6 +399,72 @@ cudaError_t packed_to_fab(const T* dev, T* host, const Box& b, int ngrow, int nc
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
+}
+
+// The same copies for a sub-box of a box: the caller's box of a multi-box D3Q39
+// level inside the internal sheet, at offset off, of size n (nodes per axis).
+template <typename T>
+cudaError_t sub_copy(T* host, T* dev, const Box& b, const int (&off)[3], const int (&n)[3], int ngrow, int ncomp,
+                     int64_t plane, bool to_dev, cudaStream_t s) {
+  const int fx = n[0] + 2 * ngrow, fy = n[1] + 2 * ngrow, fz = n[2] + 2 * ngrow;
+  for (int q = 0; q < ncomp; ++q) {
+    cudaPitchedPtr hp = make_cudaPitchedPtr((void*)(host + (int64_t)q * fx * fy * fz), fx * sizeof(T), fx, fy);
+    cudaPitchedPtr dp = make_cudaPitchedPtr((void*)(dev + (int64_t)q * plane), b.nx * sizeof(T), b.nx, b.ny);
+    const cudaPos hpos = make_cudaPos(ngrow * sizeof(T), ngrow, ngrow);
+    const cudaPos dpos = make_cudaPos(off[0] * sizeof(T), off[1], off[2]);
+    cudaMemcpy3DParms p{};
+    p.srcPtr = to_dev ? hp : dp;
+    p.srcPos = to_dev ? hpos : dpos;
+    p.dstPtr = to_dev ? dp : hp;
+    p.dstPos = to_dev ? dpos : hpos;
+    p.extent = make_cudaExtent(n[0] * sizeof(T), n[1], n[2]);
+    p.kind = to_dev ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+    const cudaError_t e = cudaMemcpy3DAsync(&p, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// The caller's box k of a D3Q39 level: the internal box holding it, the box's
+// offset in it and its size.  A single-box level is its own sheet.
+struct Sub39 {
+  Box* b = nullptr;
+  int off[3] = {0, 0, 0};
+  int n[3] = {0, 0, 0};
+  bool whole = true;  // the caller's box is the whole internal box
+};
+
+Sub39 get_sub39(elbm_ctx* c, int lvl, int box, Level** lv_out) {
+  Sub39 r;
+  Level* lv = get_level(c, lvl);
+  if (!lv || lv->lattice != ELBM_D3Q39 || lv->boxes.empty()) return r;
+  if (lv_out) *lv_out = lv;
+  if (lv->sub39.empty()) {
+    if (box < 0 || box >= (int)lv->boxes.size()) return r;
+    r.b = lv->boxes[box].get();
+    r.n[0] = r.b->nx;
+    r.n[1] = r.b->ny;
+    r.n[2] = r.b->nz;
+    return r;
+  }
+  if (box < 0 || box >= (int)lv->sub39.size()) return r;
+  r.b = lv->boxes[0].get();
+  r.whole = false;
+  for (int a = 0; a < 3; ++a) {
+    r.off[a] = lv->sub39[box][a] - r.b->lo[a];
+    r.n[a] = lv->sub39[box][3 + a] - lv->sub39[box][a] + 1;
+  }
+  return r;
+}
+
+// Host-to-device (or back) copy of ncomp component planes of the caller's box.
+template <typename T>
+cudaError_t sub39_copy(const Sub39& u, T* host, T* dev, int ngrow, int ncomp, int64_t plane, bool to_dev,
+                       cudaStream_t s) {
+  if (u.whole)
+    return to_dev ? fab_to_packed((const T*)host, dev, *u.b, ngrow, ncomp, plane, s)
+                  : packed_to_fab((const T*)dev, host, *u.b, ngrow, ncomp, plane, s);
+  return sub_copy(host, dev, *u.b, u.off, u.n, ngrow, ncomp, plane, to_dev, s);
 }
 
 // Pull-form decoding of one population's link (see include/elbm_gb300.h and
@@ -816,8 +893,6 @@ int elbm_level_register(elbm_ctx* c, int lvl, int lattice, int storage, int nbox
   if (lattice != ELBM_D3Q27 && lattice != ELBM_D3Q39) return fail(c, ELBM_E_UNSUPPORTED, "lattice %d", lattice);
   if (storage != ELBM_STORE_FP64 && storage != ELBM_STORE_FP32_DEV) return fail(c, ELBM_E_ARG, "bad storage %d", storage);
   if (nbox < 1) return fail(c, ELBM_E_ARG, "nbox=%d", nbox);
-  if (lattice == ELBM_D3Q39 && nbox != 1)
-    return fail(c, ELBM_E_UNSUPPORTED, "D3Q39 levels hold one periodic box (nbox=%d)", nbox);
   if (!lo_hi || ngrow < 0) return fail(c, ELBM_E_ARG, "null lo_hi or negative ngrow");
   for (int k = 0; k < nbox; ++k)
     for (int m = 0; m < k; ++m) {
@@ -826,6 +901,27 @@ int elbm_level_register(elbm_ctx* c, int lvl, int lattice, int storage, int nbox
         overlap &= lo_hi[6 * k + a] <= lo_hi[6 * m + 3 + a] && lo_hi[6 * m + a] <= lo_hi[6 * k + 3 + a];
       if (overlap) return fail(c, ELBM_E_ARG, "boxes %d and %d overlap", m, k);
     }
+  if (lattice == ELBM_D3Q39 && nbox > 1) {
+    // one internal box over the boxes' bounding box (nodes outside every box stay inactive)
+    int32_t bb[6] = {lo_hi[0], lo_hi[1], lo_hi[2], lo_hi[3], lo_hi[4], lo_hi[5]};
+    for (int k = 1; k < nbox; ++k)
+      for (int a = 0; a < 3; ++a) {
+        if (lo_hi[6 * k + 3 + a] < lo_hi[6 * k + a]) return fail(c, ELBM_E_ARG, "empty box %d", k);
+        bb[a] = std::min(bb[a], lo_hi[6 * k + a]);
+        bb[3 + a] = std::max(bb[3 + a], lo_hi[6 * k + 3 + a]);
+      }
+    if (const int rc = elbm_level_register(c, lvl, lattice, storage, 1, bb, ngrow)) return rc;
+    Level& lv = c->levels[lvl];
+    for (int k = 0; k < nbox; ++k)
+      lv.sub39.push_back({lo_hi[6 * k], lo_hi[6 * k + 1], lo_hi[6 * k + 2], lo_hi[6 * k + 3], lo_hi[6 * k + 4],
+                          lo_hi[6 * k + 5]});
+    lv.sub39_state.assign(nbox, {});
+    lv.sub39_ngrow.assign(nbox, 0);
+    lv.sub39_have_pops.assign(nbox, 0);
+    lv.sub39_have_macro.assign(nbox, 0);
+    lv.sub39_have_init.assign(nbox, 0);
+    return ELBM_OK;
+  }
   CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
   if ((int)c->levels.size() <= lvl) c->levels.resize(lvl + 1);
   Level& lv = c->levels[lvl];
@@ -1153,6 +1249,13 @@ int elbm_download_alpha(elbm_ctx* c, int lvl, int box, double* alpha) {
 }
 
 // The arguments of one D3Q27 step over every box of a level.
+// The offset variant serves one-box levels whose 27 planes stay below 2^31 elements.
+bool off_variant_ok(const Level& lv) {
+  if (lv.boxes.size() != 1) return false;
+  const Box& b = *lv.boxes[0];
+  return (int64_t)Q27 * lv.plane + (int64_t)b.nx * b.ny + b.nx + 1 < ((int64_t)1 << 31);
+}
+
 Step27Args level_args27(elbm_ctx* c, Level& lv) {
   const elbm_d3q27_params& p = lv.p27;
   Step27Args a{};
@@ -1188,6 +1291,12 @@ Step27Args level_args27(elbm_ctx* c, Level& lv) {
   a.bnode = lv.bnode.p;
   a.nbnd = lv.nrec;
   a.rsrc = lv.rsrc.p;
+  if (off_variant_ok(lv)) {
+    const Box& b = *lv.boxes[0];
+    a.pull_off_ok = 1;
+    for (int j = 0; j < Q27; ++j)
+      a.pull_off[j] = (int32_t)((int64_t)j * lv.plane - (cx27(j) + (int64_t)cy27(j) * b.nx + (int64_t)cz27(j) * b.nx * b.ny));
+  }
   if (lv.ws_maps.p) {
     a.ws_maps = lv.ws_maps.p + (size_t)lv.cur * lv.boxes.size() * sizeof(CUtensorMap);
     a.ws_boxes = lv.ws_boxes.p;
@@ -1267,7 +1376,7 @@ int elbm_autotune(elbm_ctx* c, int lvl, int reps, int* chosen, double* ms_per_va
   float best = INFINITY;
   int best_v = 0;
   for (int v = 0; v < kFp32Variants; ++v) {
-    if (v == kVariantTma && !lv->ws_maps.p) {
+    if ((v == kVariantTma && !lv->ws_maps.p) || (v == kVariantOff && !off_variant_ok(*lv))) {
       if (ms_per_variant) ms_per_variant[v] = INFINITY;  // not available for this level
       continue;
     }
@@ -1305,6 +1414,8 @@ int elbm_set_kernel_variant(elbm_ctx* c, int lvl, int variant) {
   if (variant == kVariantTma && !lv->ws_maps.p)
     return fail(c, ELBM_E_UNSUPPORTED, "the tensor-copy step variant does not serve this level: %s",
                 lv->ws_why.empty() ? "not a D3Q27 level with FP32 deviation storage" : lv->ws_why.c_str());
+  if (variant == kVariantOff && !off_variant_ok(*lv))
+    return fail(c, ELBM_E_UNSUPPORTED, "the offset step variant serves one-box levels below 2^31 elements per 27 planes");
   lv->variant = variant;
   return ELBM_OK;
 }
@@ -1874,12 +1985,63 @@ int elbm_set_d3q39_params(elbm_ctx* c, int lvl, const elbm_d3q39_params* p) {
   return ELBM_OK;
 }
 
+namespace {
+int set_links39_sheet(elbm_ctx* c, int lvl, Level* lv, Box* b, const int32_t* state, int ngrow_state,
+                      const elbm_d3q39_bc* bc);
+}
+
 int elbm_set_links39(elbm_ctx* c, int lvl, int box, const int32_t* state, int ngrow_state, const elbm_d3q39_bc* bc) {
   Level* lv = nullptr;
-  Box* b = get_box(c, lvl, box, &lv);
-  if (!b || !state || !bc || ngrow_state < 0) return fail(c, ELBM_E_ARG, "unknown level/box or null state/bc");
-  if (lv->lattice != ELBM_D3Q39) return fail(c, ELBM_E_ARG, "not a D3Q39 level");
+  const Sub39 u = get_sub39(c, lvl, box, &lv);
+  Box* b = u.b;
+  if (!b || !state || !bc || ngrow_state < 0)
+    return fail(c, ELBM_E_ARG, "unknown level/box, not a D3Q39 level, or null state/bc");
   if (!lv->params_set) return fail(c, ELBM_E_STATE, "set the level parameters before the links");
+  if (u.whole) return set_links39_sheet(c, lvl, lv, b, state, ngrow_state, bc);
+  // one box of a multi-box level: keep its state until every box has one, then decode the sheet
+  const int g = ngrow_state;
+  const int fx = u.n[0] + 2 * g, fy = u.n[1] + 2 * g, fz = u.n[2] + 2 * g;
+  lv->sub39_state[box].assign(state, state + (size_t)39 * fx * fy * fz);
+  lv->sub39_ngrow[box] = g;
+  lv->sub39_bc = *bc;
+  for (const auto& v : lv->sub39_state)
+    if (v.empty()) return ELBM_OK;
+  // the sheet's state: every box's valid nodes; a node outside every box takes the first code a
+  // box's ghost layers give it (a coarse-fine ghost, a face code), else it stays inactive (-1)
+  const int64_t N = b->N;
+  std::vector<int32_t> sheet((size_t)39 * N, 0);
+  std::vector<uint8_t> set(N, 0);
+  for (int64_t n = 0; n < N; ++n) sheet[n] = -1;
+  for (int pass = 0; pass < 2; ++pass)
+    for (size_t k = 0; k < lv->sub39.size(); ++k) {
+      const auto& bx = lv->sub39[k];
+      const int gk = lv->sub39_ngrow[k];
+      const int nx = bx[3] - bx[0] + 1, ny = bx[4] - bx[1] + 1, nz = bx[5] - bx[2] + 1;
+      const int ex = nx + 2 * gk, ey = ny + 2 * gk, ez = nz + 2 * gk;
+      const int64_t fplane = (int64_t)ex * ey * ez;
+      const int32_t* st = lv->sub39_state[k].data();
+      for (int z = -gk; z < nz + gk; ++z)
+        for (int y = -gk; y < ny + gk; ++y)
+          for (int x = -gk; x < nx + gk; ++x) {
+            const bool valid = x >= 0 && x < nx && y >= 0 && y < ny && z >= 0 && z < nz;
+            if (valid != (pass == 0)) continue;
+            const int X = bx[0] + x - b->lo[0], Y = bx[1] + y - b->lo[1], Z = bx[2] + z - b->lo[2];
+            if (X < 0 || X >= b->nx || Y < 0 || Y >= b->ny || Z < 0 || Z >= b->nz) continue;
+            const int64_t n = ((int64_t)Z * b->ny + Y) * b->nx + X;
+            if (set[n]) continue;
+            const int64_t src = ((int64_t)(z + gk) * ey + (y + gk)) * ex + (x + gk);
+            for (int q = 0; q < 39; ++q) sheet[(size_t)q * N + n] = st[(size_t)q * fplane + src];
+            set[n] = valid ? 1 : 2;
+          }
+    }
+  return set_links39_sheet(c, lvl, lv, b, sheet.data(), 0, bc);
+}
+
+namespace {
+// Decode the link codes of an internal box (a single-box level's box, or a multi-box level's sheet)
+// and upload its tables.
+int set_links39_sheet(elbm_ctx* c, int lvl, Level* lv, Box* b, const int32_t* state, int ngrow_state,
+                      const elbm_d3q39_bc* bc) {
   Links39 L;
   std::string why;
   const int rc = decode_links39(state, ngrow_state, b->nx, b->ny, b->nz, lv->p39.periodic, lv->p39.shifted,
@@ -1960,14 +2122,59 @@ int elbm_set_links39(elbm_ctx* c, int lvl, int box, const int32_t* state, int ng
   CUDA_TRY(cudaGetLastError(), "stale init");
   return ELBM_OK;
 }
+}  // namespace
 
 int elbm_upload_level39(elbm_ctx* c, int lvl, int box, const double* fout, const double* gout, const double* lm,
                         const double* w_vel) {
   Level* lv = nullptr;
-  Box* b = get_box(c, lvl, box, &lv);
-  if (!b || !fout || !gout || !lm || !w_vel) return fail(c, ELBM_E_ARG, "unknown level/box or null data");
-  if (lv->lattice != ELBM_D3Q39) return fail(c, ELBM_E_ARG, "not a D3Q39 level");
+  const Sub39 u = get_sub39(c, lvl, box, &lv);
+  Box* b = u.b;
+  if (!b || !fout || !gout || !lm || !w_vel)
+    return fail(c, ELBM_E_ARG, "unknown level/box, not a D3Q39 level, or null data");
   CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  if (!u.whole) {
+    // one box of a multi-box level: its part of the sheet; the sheet is complete (both buffers,
+    // the FP32 conversion, the slots that keep last step's values) once every box has arrived
+    const int g = lv->ngrow;
+    const bool f32 = lv->storage == ELBM_STORE_FP32_DEV;
+    if (f32) {
+      if (!b->stage39.p) {
+        CUDA_TRY(b->stage39.alloc((size_t)b->plane * 78), "FP64 staging");
+        CUDA_TRY(cudaMemsetAsync(b->stage39.p, 0, b->stage39.n * sizeof(double), c->stream), "staging");
+      }
+      CUDA_TRY(sub39_copy(u, const_cast<double*>(fout), b->stage39.p, g, 39, b->plane, true, c->stream), "upload f");
+      CUDA_TRY(sub39_copy(u, const_cast<double*>(gout), b->stage39.p + b->plane * 39, g, 39, b->plane, true,
+                          c->stream), "upload g");
+    } else {
+      for (int s2 = 0; s2 < 2; ++s2) {
+        CUDA_TRY(sub39_copy(u, const_cast<double*>(fout), (double*)b->buf[s2].p, g, 39, b->plane, true, c->stream),
+                 "upload f");
+        CUDA_TRY(sub39_copy(u, const_cast<double*>(gout), (double*)b->gbuf[s2].p, g, 39, b->plane, true, c->stream),
+                 "upload g");
+      }
+    }
+    CUDA_TRY(sub39_copy(u, const_cast<double*>(lm), b->lm.p, g, 13, b->plane, true, c->stream), "upload lm");
+    CUDA_TRY(sub39_copy(u, const_cast<double*>(w_vel), b->w_vel.p, g, 1, b->plane, true, c->stream), "upload w");
+    lv->sub39_have_pops[box] = 1;
+    b->macro_set = false;
+    std::fill(lv->sub39_have_macro.begin(), lv->sub39_have_macro.end(), 0);
+    if (std::all_of(lv->sub39_have_pops.begin(), lv->sub39_have_pops.end(), [](uint8_t v) { return v; })) {
+      if (f32) {
+        CUDA_TRY(stage39_to_fp32(*b, c->stream), "FP32 conversion");
+        CUDA_TRY(cudaMemcpyAsync(b->buf[1].p, b->buf[0].p, b->buf[0].n, cudaMemcpyDeviceToDevice, c->stream),
+                 "copy f");
+        CUDA_TRY(cudaMemcpyAsync(b->gbuf[1].p, b->gbuf[0].p, b->gbuf[0].n, cudaMemcpyDeviceToDevice, c->stream),
+                 "copy g");
+        b->cur = b->gcur = 0;
+      }
+      CUDA_TRY(cudaMemsetAsync(b->alpha64.p, 0, b->alpha64.n * sizeof(double), c->stream), "alpha");
+      if (b->links39) launch_stale39_init(*b, c->stream);
+      CUDA_TRY(cudaGetLastError(), "stale init");
+      b->data_set = true;
+    }
+    CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+    return ELBM_OK;
+  }
   if (lv->storage == ELBM_STORE_FP32_DEV) {
     if (!b->stage39.p) CUDA_TRY(b->stage39.alloc((size_t)b->plane * 78), "FP64 staging");
     CUDA_TRY(fab_to_packed(fout, b->stage39.p, *b, lv->ngrow, 39, b->plane, c->stream), "upload f");
@@ -2216,12 +2423,19 @@ int elbm_write_plot3d(elbm_ctx* c, int lvl, const char* grid_path, const char* d
 
 int elbm_mic_sample(elbm_ctx* c, int lvl, int box, int nmic, const int32_t* nodes, const double* weights,
                     double* out) {
-  Level* lv = nullptr;
-  Box* b = get_box(c, lvl, box, &lv);
+  Level* lv = get_level(c, lvl);
+  if (lv && lv->lattice != ELBM_D3Q39) return fail(c, ELBM_E_UNSUPPORTED, "microphones read the D3Q39 fields");
+  const Sub39 u = get_sub39(c, lvl, box, &lv);
+  Box* b = u.b;
   if (!b || nmic < 0 || (nmic > 0 && (!nodes || !weights || !out))) return fail(c, ELBM_E_ARG, "bad arguments");
-  if (lv->lattice != ELBM_D3Q39) return fail(c, ELBM_E_UNSUPPORTED, "microphones read the D3Q39 fields");
-  for (int k = 0; k < 8 * nmic; ++k)
-    if (nodes[k] < 0 || nodes[k] >= b->N) return fail(c, ELBM_E_ARG, "microphone node outside the box");
+  const int64_t nbox = (int64_t)u.n[0] * u.n[1] * u.n[2];
+  std::vector<int32_t> sn((size_t)8 * nmic);
+  for (int k = 0; k < 8 * nmic; ++k) {
+    if (nodes[k] < 0 || nodes[k] >= nbox) return fail(c, ELBM_E_ARG, "microphone node outside the box");
+    // the node in the internal box (the sheet of a multi-box level)
+    const int x = nodes[k] % u.n[0], y = (nodes[k] / u.n[0]) % u.n[1], z = nodes[k] / (u.n[0] * u.n[1]);
+    sn[k] = (int32_t)(((int64_t)(z + u.off[2]) * b->ny + (y + u.off[1])) * b->nx + (x + u.off[0]));
+  }
   if (nmic == 0) return ELBM_OK;
   CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
   DevBuf<int32_t> dn;
@@ -2229,7 +2443,7 @@ int elbm_mic_sample(elbm_ctx* c, int lvl, int box, int nmic, const int32_t* node
   CUDA_TRY(dn.alloc((size_t)8 * nmic), "mic nodes");
   CUDA_TRY(dw.alloc((size_t)8 * nmic), "mic weights");
   CUDA_TRY(dout.alloc((size_t)6 * nmic), "mic values");
-  CUDA_TRY(cudaMemcpyAsync(dn.p, nodes, (size_t)8 * nmic * 4, cudaMemcpyHostToDevice, c->stream), "mic nodes");
+  CUDA_TRY(cudaMemcpyAsync(dn.p, sn.data(), (size_t)8 * nmic * 4, cudaMemcpyHostToDevice, c->stream), "mic nodes");
   CUDA_TRY(cudaMemcpyAsync(dw.p, weights, (size_t)8 * nmic * 8, cudaMemcpyHostToDevice, c->stream), "mic weights");
   launch_mic_sample(b->macro.p, b->plane, nmic, dn.p, dw.p, dout.p, c->stream);
   CUDA_TRY(cudaGetLastError(), "mic launch");
@@ -2245,10 +2459,11 @@ int elbm_ggm_tags(elbm_ctx* c, int lvl, int box, int variable, int scheme, doubl
 
 int elbm_ggm_tags_pgs(elbm_ctx* c, int lvl, int box, int variable, int scheme, double limit, double pgs_sensitivity,
                       int pgs_reach, uint8_t* tags, double* ggm, int64_t* ntagged) {
-  Level* lv = nullptr;
-  Box* b = get_box(c, lvl, box, &lv);
+  Level* lv = get_level(c, lvl);
+  if (lv && lv->lattice != ELBM_D3Q39) return fail(c, ELBM_E_UNSUPPORTED, "GGM tagging reads the D3Q39 fields");
+  const Sub39 u = get_sub39(c, lvl, box, &lv);
+  Box* b = u.b;
   if (!b || !tags) return fail(c, ELBM_E_ARG, "unknown level/box or null tags");
-  if (lv->lattice != ELBM_D3Q39) return fail(c, ELBM_E_UNSUPPORTED, "GGM tagging reads the D3Q39 fields");
   if (variable < 1 || variable > 8 || scheme < 0 || scheme > 2) return fail(c, ELBM_E_ARG, "bad variable or scheme");
   if (!b->data_set) return fail(c, ELBM_E_STATE, "no state");
   CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
@@ -2276,6 +2491,17 @@ int elbm_ggm_tags_pgs(elbm_ctx* c, int lvl, int box, int variable, int scheme, d
     CUDA_TRY(cudaGetLastError(), "pgs launch");
   }
   unsigned long long h = 0;
+  if (!u.whole) {
+    // one box of a multi-box level: the differences ran over the sheet (across box faces in place);
+    // the box's part of the tags and ggm
+    CUDA_TRY(sub_copy(tags, tg.p, *b, u.off, u.n, 0, 1, b->plane, false, c->stream), "tags");
+    if (ggm) CUDA_TRY(sub_copy(ggm, gg.p, *b, u.off, u.n, 0, 1, b->plane, false, c->stream), "ggm");
+    CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+    const int64_t nbox = (int64_t)u.n[0] * u.n[1] * u.n[2];
+    for (int64_t k = 0; k < nbox; ++k) h += tags[k] != 0;
+    if (ntagged) *ntagged = (int64_t)h;
+    return ELBM_OK;
+  }
   CUDA_TRY(cudaMemcpyAsync(tags, tg.p, b->N, cudaMemcpyDeviceToHost, c->stream), "tags");
   if (ggm) CUDA_TRY(cudaMemcpyAsync(ggm, gg.p, b->N * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "ggm");
   CUDA_TRY(cudaMemcpyAsync(&h, cnt.p, sizeof h, cudaMemcpyDeviceToHost, c->stream), "count");
@@ -2291,12 +2517,26 @@ int elbm_ggm_tags_pgs(elbm_ctx* c, int lvl, int box, int variable, int scheme, d
 int elbm_init_level39(elbm_ctx* c, int lvl, int box, const double* macro, const double* lm_start,
                       int64_t* capped) {
   Level* lv = nullptr;
-  Box* b = get_box(c, lvl, box, &lv);
-  if (!b || !macro || !lm_start) return fail(c, ELBM_E_ARG, "unknown level/box or null data");
-  if (lv->lattice != ELBM_D3Q39) return fail(c, ELBM_E_ARG, "not a D3Q39 level");
+  const Sub39 u = get_sub39(c, lvl, box, &lv);
+  Box* b = u.b;
+  if (!b || !macro || !lm_start) return fail(c, ELBM_E_ARG, "unknown level/box, not a D3Q39 level, or null data");
   if (!lv->params_set) return fail(c, ELBM_E_STATE, "set the level parameters first");
   CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
-  CUDA_TRY(fab_to_packed(macro, b->macro.p, *b, lv->ngrow, 5, b->plane, c->stream), "upload macro");
+  CUDA_TRY(sub39_copy(u, const_cast<double*>(macro), b->macro.p, lv->ngrow, 5, b->plane, true, c->stream),
+           "upload macro");
+  if (capped) *capped = 0;
+  if (!u.whole) {
+    // one box of a multi-box level: the sheet's initial state is solved once every box's fields
+    // have arrived (with the last call's start multipliers; its count covers the whole sheet)
+    lv->sub39_have_init[box] = 1;
+    if (!std::all_of(lv->sub39_have_init.begin(), lv->sub39_have_init.end(), [](uint8_t v) { return v; })) {
+      CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+      return ELBM_OK;
+    }
+    std::fill(lv->sub39_have_init.begin(), lv->sub39_have_init.end(), 0);
+    std::fill(lv->sub39_have_pops.begin(), lv->sub39_have_pops.end(), 1);
+    std::fill(lv->sub39_have_macro.begin(), lv->sub39_have_macro.end(), 1);
+  }
   DevBuf<double> lm0;
   DevBuf<unsigned long long> cnt;
   CUDA_TRY(lm0.alloc(13), "start multipliers");
@@ -2379,23 +2619,29 @@ int elbm_d3q39_equilibrium(elbm_ctx* c, const elbm_d3q39_params* p, const double
 
 int elbm_upload_macro39(elbm_ctx* c, int lvl, int box, const double* macro) {
   Level* lv = nullptr;
-  Box* b = get_box(c, lvl, box, &lv);
-  if (!b || !macro) return fail(c, ELBM_E_ARG, "unknown level/box or null data");
-  if (lv->lattice != ELBM_D3Q39) return fail(c, ELBM_E_ARG, "not a D3Q39 level");
+  const Sub39 u = get_sub39(c, lvl, box, &lv);
+  Box* b = u.b;
+  if (!b || !macro) return fail(c, ELBM_E_ARG, "unknown level/box, not a D3Q39 level, or null data");
   if (!b->data_set) return fail(c, ELBM_E_STATE, "upload the populations (elbm_upload_level39) first");
   CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
-  CUDA_TRY(fab_to_packed(macro, b->macro.p, *b, lv->ngrow, 5, b->plane, c->stream), "upload macro");
+  CUDA_TRY(sub39_copy(u, const_cast<double*>(macro), b->macro.p, lv->ngrow, 5, b->plane, true, c->stream),
+           "upload macro");
   CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
-  b->macro_set = true;
+  if (!u.whole) {
+    lv->sub39_have_macro[box] = 1;
+    b->macro_set = std::all_of(lv->sub39_have_macro.begin(), lv->sub39_have_macro.end(), [](uint8_t v) { return v; });
+  } else {
+    b->macro_set = true;
+  }
   return ELBM_OK;
 }
 
 int elbm_download_level39(elbm_ctx* c, int lvl, int box, double* fout, double* gout, double* lm, double* w_vel,
                           double* alpha, double* macro) {
   Level* lv = nullptr;
-  Box* b = get_box(c, lvl, box, &lv);
-  if (!b) return fail(c, ELBM_E_ARG, "unknown level/box");
-  if (lv->lattice != ELBM_D3Q39) return fail(c, ELBM_E_ARG, "not a D3Q39 level");
+  const Sub39 u = get_sub39(c, lvl, box, &lv);
+  Box* b = u.b;
+  if (!b) return fail(c, ELBM_E_ARG, "unknown level/box or not a D3Q39 level");
   if (!b->data_set) return fail(c, ELBM_E_STATE, "no populations uploaded");
   CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
   const int g = lv->ngrow;
@@ -2407,16 +2653,16 @@ int elbm_download_level39(elbm_ctx* c, int lvl, int box, double* fout, double* g
     from_dev39_kernel<<<grid, 256, 0, c->stream>>>((const float*)b->gbuf[b->gcur].p, b->stage39.p + b->plane * 39,
                                                   b->N, b->plane, b->ref39.p + 39);
     CUDA_TRY(cudaGetLastError(), "FP32 conversion");
-    if (fout) CUDA_TRY(packed_to_fab(b->stage39.p, fout, *b, g, 39, b->plane, c->stream), "f");
-    if (gout) CUDA_TRY(packed_to_fab(b->stage39.p + b->plane * 39, gout, *b, g, 39, b->plane, c->stream), "g");
+    if (fout) CUDA_TRY(sub39_copy(u, fout, b->stage39.p, g, 39, b->plane, false, c->stream), "f");
+    if (gout) CUDA_TRY(sub39_copy(u, gout, b->stage39.p + b->plane * 39, g, 39, b->plane, false, c->stream), "g");
   } else {
-    if (fout) CUDA_TRY(packed_to_fab((const double*)b->buf[b->cur].p, fout, *b, g, 39, b->plane, c->stream), "f");
-    if (gout) CUDA_TRY(packed_to_fab((const double*)b->gbuf[b->gcur].p, gout, *b, g, 39, b->plane, c->stream), "g");
+    if (fout) CUDA_TRY(sub39_copy(u, fout, (double*)b->buf[b->cur].p, g, 39, b->plane, false, c->stream), "f");
+    if (gout) CUDA_TRY(sub39_copy(u, gout, (double*)b->gbuf[b->gcur].p, g, 39, b->plane, false, c->stream), "g");
   }
-  if (lm) CUDA_TRY(packed_to_fab((const double*)b->lm.p, lm, *b, g, 13, b->plane, c->stream), "lm");
-  if (w_vel) CUDA_TRY(packed_to_fab((const double*)b->w_vel.p, w_vel, *b, g, 1, b->plane, c->stream), "w");
-  if (alpha) CUDA_TRY(packed_to_fab((const double*)b->alpha64.p, alpha, *b, g, 1, b->plane, c->stream), "alpha");
-  if (macro) CUDA_TRY(packed_to_fab((const double*)b->macro.p, macro, *b, g, 5, b->plane, c->stream), "macro");
+  if (lm) CUDA_TRY(sub39_copy(u, lm, b->lm.p, g, 13, b->plane, false, c->stream), "lm");
+  if (w_vel) CUDA_TRY(sub39_copy(u, w_vel, b->w_vel.p, g, 1, b->plane, false, c->stream), "w");
+  if (alpha) CUDA_TRY(sub39_copy(u, alpha, b->alpha64.p, g, 1, b->plane, false, c->stream), "alpha");
+  if (macro) CUDA_TRY(sub39_copy(u, macro, b->macro.p, g, 5, b->plane, false, c->stream), "macro");
   CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
   return ELBM_OK;
 }

@@ -93,13 +93,19 @@ struct Step27Args {
   unsigned long long* harvest_count;
   long long harvest_cap;
   int harvest_stride;
+  // one-box levels whose 27 planes stay below 2^31 elements: the element offset of each pull,
+  // population j of node n at n + pull_off[j] (the offset variant reads them as kernel parameters)
+  int pull_off_ok;
+  int32_t pull_off[27];
 };
 
 // 0: direct; 1, 4, 5, 6, 7: direct with registers capped for 4, 5, 6, 8, 7 blocks of 128 threads
 // per SM; 2: bulk-copy staged; 3: persistent warps taking chunks from a counter (4 blocks per SM);
-// 8: warp-specialised, tensor copies (TMA) of 256-node tiles into a shared-memory ring
-constexpr int kFp32Variants = 9;
+// 8: warp-specialised, tensor copies (TMA) of 256-node tiles into a shared-memory ring;
+// 9: direct, the 27 pull offsets of a one-box level precomputed (kernel parameters)
+constexpr int kFp32Variants = 10;
 constexpr int kVariantTma = 8;
+constexpr int kVariantOff = 9;
 // Bytes allocated before and after each population buffer (never written):
 // room for the staged kernel's row-segment copies that start 4 floats before
 // a plane or run up to a tile past its end.

@@ -17,7 +17,7 @@ module elbm_gb300_iface
     ELBM_E_UNSUPPORTED = -3, ELBM_E_STATE = -4, ELBM_E_NUMERIC = -5
   integer(c_int), parameter, public :: ELBM_ST_NAN = 1, ELBM_ST_NEWTON_FALLBACK = 2, ELBM_ST_NEG_POP = 4, &
     ELBM_ST_DH_TOL = 8, ELBM_ST_COPY_TIMEOUT = 16
-  integer(c_int), parameter, public :: ELBM_KERNEL_VARIANTS = 9, ELBM_MLP_PARAMS = 6017, ELBM_MLP_RECORD = 29
+  integer(c_int), parameter, public :: ELBM_KERNEL_VARIANTS = 10, ELBM_MLP_PARAMS = 6017, ELBM_MLP_RECORD = 29
   integer(c_int), parameter, public :: ELBM_D3Q27 = 27, ELBM_D3Q39 = 39
   integer(c_int), parameter, public :: ELBM_STORE_FP64 = 0, ELBM_STORE_FP32_DEV = 1
   integer(c_int), parameter, public :: ELBM_ALPHA_FIXED2 = 0, ELBM_ALPHA_NEWTON = 1, ELBM_ALPHA_LEARNED = 2

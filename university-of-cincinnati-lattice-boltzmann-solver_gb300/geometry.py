@@ -144,6 +144,119 @@ def sphere_state27(nx: int, ny: int, nz: int, radius: float, center, subdivision
     return st
 
 
+def slice_state27(st: np.ndarray, lo, hi, g: int = 1) -> np.ndarray:
+    """The state FAB of box [lo, hi] (inclusive, indices into st) with g ghost
+    layers, as AMReX's fill_boundary gives it; outside st: not fluid (-1)."""
+    q, nz, ny, nx = st.shape
+    out = np.full((q, hi[2] - lo[2] + 1 + 2 * g, hi[1] - lo[1] + 1 + 2 * g, hi[0] - lo[0] + 1 + 2 * g), -1, np.int32)
+    src = [slice(max(lo[a] - g, 0), min(hi[a] + g, n - 1) + 1) for a, n in enumerate((nx, ny, nz))]
+    dst = [slice(sl.start - (lo[a] - g), sl.stop - (lo[a] - g)) for a, sl in enumerate(src)]
+    out[:, dst[2], dst[1], dst[0]] = st[:, src[2], src[1], src[0]]
+    return out
+
+
+def _segments(rng, total: int, count: int, edges) -> list:
+    """count lengths drawn from edges that sum to total (rejection sampling)."""
+    for _ in range(1000000):
+        seg = rng.choice(edges, count)
+        if int(seg.sum()) == total:
+            return [int(v) for v in seg]
+    raise ValueError(f"no {count} lengths from {edges} sum to {total}")
+
+
+AMR_GHOST = 10000000  # node type of a fine level's ghost nodes (filled from the coarser level)
+
+
+def amr_sphere_hierarchy(seed: int = 2024, shell: int = 2, edges=(16, 24, 32, 40, 48)):
+    """The 3-level AMR case around the sphere of the 256x128x128 case, at ratio 2:
+    level 0 is that domain at half resolution (128x64x64, sphere of radius 8 at
+    (32, 32, 32)); level 1 holds 24 boxes and level 2 holds 96 boxes with seeded
+    edge lengths from `edges` (multiples of 8) that tile a block around the
+    sphere and its wake (level 1: x [16, 128), y [16, 112), z [24, 104) in its own
+    index space, split 4 x 3 x 2; level 2: x [88, 232), y [72, 184), z [72, 184),
+    split 6 x 4 x 4), so that the refinement covers the shell of radius 10..28
+    (level-0 units) on the sphere's sides and its near wake.  Each fine level is
+    framed by `shell` ghost layers (node type AMR_GHOST, filled from the coarser
+    level), held in six slab boxes; a level-2 box's ghost nodes lie over valid
+    level-1 nodes.  Returns a list over levels of dicts: 'boxes' (inclusive
+    (lo, hi) in the level's index space, valid boxes first), 'nvalid', 'origin'
+    and 'state' (the level-wide state array from origin, sphere wall links
+    marked) and 'scale' (2^level)."""
+    from .capi import mark_triangles
+
+    rng = np.random.default_rng(seed)
+    tri = icosphere(4, 8.0, (32.0, 32.0, 32.0))
+    levels = []
+    st0 = box_state27(128, 64, 64, sphere_faces())
+    mark_triangles(st0, (0.0, 0.0, 0.0), 1.0, tri)
+    levels.append({"boxes": [((0, 0, 0), (127, 63, 63))], "nvalid": 1, "origin": (0, 0, 0), "state": st0, "scale": 1})
+    regions = {1: (((16, 128), (16, 112), (24, 104)), (4, 3, 2)), 2: (((88, 232), (72, 184), (72, 184)), (6, 4, 4))}
+    for lvl in (1, 2):
+        (rx, ry, rz), counts = regions[lvl]
+        r = (rx, ry, rz)
+        cuts = []
+        for a in range(3):
+            seg = _segments(rng, r[a][1] - r[a][0], counts[a], edges)
+            cuts.append(np.concatenate([[r[a][0]], r[a][0] + np.cumsum(seg)]))
+        boxes = []
+        for k in range(counts[2]):
+            for j in range(counts[1]):
+                for i in range(counts[0]):
+                    lo = (int(cuts[0][i]), int(cuts[1][j]), int(cuts[2][k]))
+                    hi = (int(cuts[0][i + 1]) - 1, int(cuts[1][j + 1]) - 1, int(cuts[2][k + 1]) - 1)
+                    boxes.append((lo, hi))
+        a0, b0 = [v[0] for v in r], [v[1] for v in r]
+        s = shell
+        # the ghost frame as six disjoint slabs (z faces over the full frame, then y, then x)
+        slabs = [((a0[0] - s, a0[1] - s, a0[2] - s), (b0[0] + s - 1, b0[1] + s - 1, a0[2] - 1)),
+                 ((a0[0] - s, a0[1] - s, b0[2]), (b0[0] + s - 1, b0[1] + s - 1, b0[2] + s - 1)),
+                 ((a0[0] - s, a0[1] - s, a0[2]), (b0[0] + s - 1, a0[1] - 1, b0[2] - 1)),
+                 ((a0[0] - s, b0[1], a0[2]), (b0[0] + s - 1, b0[1] + s - 1, b0[2] - 1)),
+                 ((a0[0] - s, a0[1], a0[2]), (a0[0] - 1, b0[1] - 1, b0[2] - 1)),
+                 ((b0[0], a0[1], a0[2]), (b0[0] + s - 1, b0[1] - 1, b0[2] - 1))]
+        origin = tuple(v - s for v in a0)
+        dims = [b0[a] - a0[a] + 2 * s for a in range(3)]
+        st = np.zeros((Q27, dims[2], dims[1], dims[0]), np.int32)
+        ghost = np.ones((dims[2], dims[1], dims[0]), bool)
+        ghost[s:-s, s:-s, s:-s] = False
+        st[0][ghost] = AMR_GHOST
+        scale = 2 ** lvl
+        mark_triangles(st, tuple(o / scale for o in origin), 1.0 / scale, tri)
+        levels.append({"boxes": boxes + slabs, "nvalid": len(boxes), "origin": origin, "state": st, "scale": scale})
+    return levels
+
+
+def register_amr_hierarchy(ctx, levels, storage, u_in=(0.08, 0.0, 0.0), nu_level1: float = 5e-4,
+                           noise: float = 1e-3, seed: int = 77) -> list:
+    """Register the levels of amr_sphere_hierarchy on a context: boxes, D3Q27
+    parameters (the viscosity of the 256x128x128 case, 5e-4, on level 1; a
+    level's lattice viscosity doubles with each refinement at fixed physical
+    viscosity under acoustic scaling), per-box state slices with one ghost
+    layer, populations at the equilibrium of u_in with seeded noise (solid nodes
+    at w), and the coarse-fine maps.  Returns the level-wide initial
+    populations."""
+    from .capi import ELBM_D3Q27, make_d3q27_params
+
+    f_all = []
+    for lvl, L in enumerate(levels):
+        st, o = L["state"], L["origin"]
+        ctx.level_register(lvl, ELBM_D3Q27, storage, [list(lo) + list(hi) for lo, hi in L["boxes"]])
+        bp = d3q27_boundary_params(u_in, nu_level1 * 2.0 ** (lvl - 1))
+        ctx.set_d3q27_params(lvl, make_d3q27_params(**bp))
+        nz, ny, nx = st.shape[1:]
+        f = perturbed_equilibrium(nx, ny, nz, u_in, noise, seed=seed + lvl)
+        f[:, st[0] == -1001] = W[:, None]
+        for k, (lo, hi) in enumerate(L["boxes"]):
+            rl = [lo[a] - o[a] for a in range(3)]
+            rh = [hi[a] - o[a] for a in range(3)]
+            ctx.set_links(lvl, k, slice_state27(st, rl, rh, 1), ngrow_state=1)
+            ctx.upload(lvl, k, np.ascontiguousarray(f[:, rl[2]:rh[2] + 1, rl[1]:rh[1] + 1, rl[0]:rh[0] + 1]))
+        f_all.append(f)
+    for lvl in range(1, len(levels)):
+        ctx.interlevel_setup(lvl)
+    return f_all
+
+
 __all__ = [
     "icosphere",
     "sphere_faces",
@@ -153,6 +266,10 @@ __all__ = [
     "perturbed_equilibrium",
     "d3q27_boundary_params",
     "inlet_code",
+    "slice_state27",
+    "amr_sphere_hierarchy",
+    "register_amr_hierarchy",
+    "AMR_GHOST",
     "outlet_code",
     "CODE_BOUNCEBACK",
     "CODE_INVISCID",
