@@ -192,11 +192,13 @@ def test_sphere_ibb_fp32_vs_oracle(pkg, orc, built_lib):
 @pytest.mark.parametrize("shape,variant", [((128, 20, 16), 2), ((200, 12, 10), 2), ((200, 12, 10), 3),
                                            ((64, 32, 32), 1), ((64, 32, 32), 5), ((64, 32, 32), 6),
                                            ((64, 32, 32), 7), ((64, 32, 32), 8), ((200, 12, 10), 8),
-                                           ((40, 20, 16), 8), ((24, 20, 16), 8), ((260, 6, 5), 8)])
+                                           ((40, 20, 16), 8), ((24, 20, 16), 8), ((260, 6, 5), 8),
+                                           ((64, 32, 32), 9), ((200, 12, 10), 9)])
 def test_kernel_variants_match_direct(pkg, built_lib, shape, variant):
     """Every step-kernel variant (1, 5, 6, 7: register-capped, 2: bulk-copy
     staged, 3: persistent warps, 8: warp-specialised tensor copies, with
-    128-, 64- and 32-wide tiles and partial tiles in x and y) computes the
+    128-, 64- and 32-wide tiles and partial tiles in x and y, 9: pull offsets
+    as kernel parameters) computes the
     same step as the direct kernel (variant 0): same node updates,
     populations equal to FP32 rounding, no copy timeouts."""
     nx, ny, nz = shape
