@@ -44,8 +44,8 @@ SEED = 1234 + 5
 BYTES_PER_NODE_FP32 = 216  # 27 x 4 B read + 27 x 4 B written
 # DRAM bytes (read + written) per node of the step kernel, from an ncu capture of a
 # 256x128x128 launch of the same workload (traffic grows in proportion to the nodes)
-DRAM_BYTES_PER_NODE_NCU = 233
-KERNELS_PER_STEP = 2  # the step kernel and the listed-node kernel
+DRAM_BYTES_PER_NODE_NCU = 203  # the bulk-node step kernel, per node of the level (ncu, 256x128x128 launch)
+KERNELS_PER_STEP = 3  # the bulk-node step kernel, the boundary-node kernel and the listed-node kernel
 BYTES_PER_NODE_FP64 = 432
 BYTES_PER_NODE_D3Q39 = 1456  # f, g: 39 x 8 B read + written each; 13 multipliers x 8 B read + written
 NU_WEDGE = 2e-4  # lattice kinematic viscosity of the D3Q39 wedge case
