@@ -4,14 +4,14 @@ alpha boundary layer and the flow past a sphere, plus the D3Q39 wedge run well
 past its start-up ramps.
 
 - boundary layer (u = 0.06, nu = 2e-5, +-5e-3 noise, flat-plate faces) on a
-  128x64x64 sub-box of the 512x256x256 case, 1000 steps.  At Re ~ 2e5 on 64
-  nodes the flow is chaotic: the FP64 path started from the FP32-rounded
-  initial state leaves its own trajectory by O(1) within 1000 steps, so the
-  FP32 path is held node by node to that measured spread, and the box-averaged
-  velocity profiles are reported; a check-mode window then shows that every
-  node whose entropy condition has a root inside the positivity bracket meets
-  |H(f + alpha Delta) - H(f)| <= 1e-10 (the rare nodes without one fall back
-  to alpha = 2 and are counted);
+  128x64x64 sub-box of the 512x256x256 case, 1000 steps: rho and u within
+  1e-4 of the FP64 path in rms; the largest differences (rho 1.6e-4, u 2.3e-3
+  of the inlet speed) sit at the plate's leading edge, where some nodes'
+  entropy condition has no root inside the positivity bracket (alpha = 2,
+  counted, in both paths); reported beside them: the errors away from the
+  leading edge and the FP64 path's own difference from an FP32-rounded start;
+  a check-mode window then shows that every node whose entropy condition has
+  a root meets |H(f + alpha Delta) - H(f)| <= 1e-10;
 - sphere 256x128x128 (r = 16 icosphere, interpolated wall links), 2000 steps:
   rho within 1e-4 and the rms of u within 1e-4 of the inlet speed; the largest
   u difference within 1e-3 (FP32 rounding of every step accumulates; the FP64
@@ -96,15 +96,21 @@ def test_boundary_layer_fp32_vs_fp64_1000_steps(pkg, built_lib):
     _, u64 = lat.moments27(f64)
     _, u32 = lat.moments27(f32)
     prof = float(np.max(np.abs(u32[..., 0].mean(axis=(1, 2)) - u64[..., 0].mean(axis=(1, 2)))) / u_in)
+    # the same away from the plate's leading edge (x >= 8)
+    away = fluid.copy()
+    away[:, :, :8] = False
+    e_away = _errors(lat, f64, f32, a64, a32, u_in, away)
     e.update(case="boundary layer 128x64x64, 1000 steps", max_abs_dH=chk["max_abs_dH"], dh_over=chk["dh_over_tol"],
              check_window_fallbacks=chk["fallbacks"], fallback_fraction_fp64=fb64, fallback_fraction_fp32=fb32,
-             mean_u_profile_max=prof,
+             mean_u_profile_max=prof, away_from_leading_edge={k: v for k, v in e_away.items() if k.endswith("max")},
              fp64_from_fp32_rounded_start={k: v for k, v in sens.items() if k.startswith(("rho", "u"))})
     print("CONTRACT " + json.dumps(e))
     assert np.isfinite(f32[:, fluid]).all()
-    # Re = 0.06 x 64 / 2e-5 ~ 2e5 on this machine: the FP64 path's own difference from an FP32-rounded
-    # start bounds what can be asked of the FP32 path node by node
-    assert e["rho_max"] <= max(1e-4, 3 * sens["rho_max"]) and e["u_max"] <= max(1e-4, 3 * sens["u_max"])
+    # rho and u within 1e-4 of the FP64 path in rms; the largest differences sit at the plate's
+    # leading edge (inlet meets wall), where some nodes' entropy condition has no root in the
+    # positivity bracket in either path (alpha = 2 there, counted): measured rho 1.6e-4, u 2.3e-3
+    assert e["rho_rms"] <= 1e-4 and e["u_rms"] <= 1e-4
+    assert e["rho_max"] <= 1e-3 and e["u_max"] <= 1e-2
     assert fb64 <= 1e-5 and fb32 <= 1e-5
     # every node whose entropy condition has a root inside the positivity bracket meets the tolerance;
     # the others (counted as fallbacks) have none to find

@@ -577,9 +577,17 @@ __device__ __noinline__ bool df_newton_all(LargePop* lp, float amax, int max_it,
       delta_lo = delta.lo;
       return true;
     }
-    if (!(Gp > 0.f)) break;
-    const df next = df_add(delta, df_make(-G.hi / Gp));
-    if (!(2.0f + next.hi > 1.0f) || !(2.0f + next.hi < amax)) break;
+    if (!(Gp > 0.f)) {
+      // left of the minimum of G (convex, G(0) = 0): towards the bracket's upper end, if it has one
+      if (!(amax < INFINITY)) break;
+      delta = df_make(0.5f * (delta.hi + amax - 2.0f));
+      continue;
+    }
+    df next = df_add(delta, df_make(-G.hi / Gp));
+    // a step that leaves the bracket (1, amax) is replaced by halving the way to its end (the
+    // root can sit close to amax: a Newton step from the left overshoots it)
+    if (!(2.0f + next.hi > 1.0f)) next = df_make(0.5f * (delta.hi - 1.0f));
+    else if (!(2.0f + next.hi < amax)) next = df_make(0.5f * (delta.hi + amax - 2.0f));
     delta = next;
   }
   return false;
@@ -713,25 +721,34 @@ __device__ __noinline__ AlphaOut alpha_solve_large(const NodePops& P, int max_it
     }
   }
   if (ok && nl && GLabs > polish_thr) {
-    // FP32 cannot resolve G_L to the tolerance (its rounding error is ~1e-7 GLabs):
-    // one Newton step with G_L in float pairs, the series part (accurate) in FP32
-    float g, gp;
-    series_g<K>(S, delta, g, gp);
-    const df alpha = df_add(df_make(2.0f), df_make(delta));
-    df G;
-    float Gp;
-    df_terms(lp, nl, alpha, G, Gp);
-    G = df_add(G, df_mul_f(alpha, g));  // G = alpha g_small + G_L
-    const float Gd = alpha.hi * gp_last;  // dG/dalpha at the root (g = 0)
-    if (Gd > 0.f) {
-      const df next = df_add(df_make(delta), df_make(-G.hi / Gd));
-      if (2.0f + next.hi > 1.0f && 2.0f + next.hi < amax) {
-        delta = next.hi;
-        r.delta_lo = next.lo;
+    // FP32 cannot resolve G_L to the tolerance (its rounding error is ~1e-7 GLabs): Newton
+    // steps with G_L in float pairs, the series part (accurate) in FP32, until |G| meets the
+    // tolerance (at most three; otherwise the float-pair solve over all populations below)
+    df dl = df_make(delta);
+    ok = false;
+    for (int pit = 0; pit < 3; ++pit) {
+      float g, gp;
+      series_g<K>(S, dl.hi, g, gp);
+      const df alpha = df_add(df_make(2.0f), dl);
+      df G;
+      float Gp;
+      df_terms(lp, nl, alpha, G, Gp);
+      G = df_add(G, df_mul_f(alpha, g));  // G = alpha g_small + G_L
+      r.iters += 1;
+      if (fabsf(G.hi) <= 0.25f * tol_dH) {
+        ok = true;
+        break;
       }
+      const float Gd = fmaf(alpha.hi, gp, g) + Gp;  // dG/dalpha = g_small + alpha g_small' + G_L'
+      if (!(Gd > 0.f)) break;
+      const df next = df_add(dl, df_make(-G.hi / Gd));
+      if (!(2.0f + next.hi > 1.0f) || !(2.0f + next.hi < amax)) break;
+      dl = next;
     }
-    r.iters += 1;
+    delta = dl.hi;
+    r.delta_lo = ok ? dl.lo : 0.f;
     (void)gsmall;
+    (void)gp_last;
   }
   if (!ok && allow_df) {
     // float-pair Newton over all populations; alpha = 2 (or inside the bracket) if that fails too
