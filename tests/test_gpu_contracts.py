@@ -5,13 +5,13 @@ past its start-up ramps.
 
 - boundary layer (u = 0.06, nu = 2e-5, +-5e-3 noise, flat-plate faces) on a
   128x64x64 sub-box of the 512x256x256 case, 1000 steps: rho and u within
-  1e-4 of the FP64 path in rms; the largest differences (rho 1.6e-4, u 2.3e-3
-  of the inlet speed) sit at the plate's leading edge, where some nodes'
-  entropy condition has no root inside the positivity bracket (alpha = 2,
-  counted, in both paths); reported beside them: the errors away from the
-  leading edge and the FP64 path's own difference from an FP32-rounded start;
-  a check-mode window then shows that every node whose entropy condition has
-  a root meets |H(f + alpha Delta) - H(f)| <= 1e-10;
+  1e-4 of the FP64 path in rms; the largest differences at isolated nodes
+  (rho 1.6e-4, u 2.3e-3 of the inlet speed) are reported with the node where
+  the velocity one sits, beside the FP64 path's own difference from an
+  FP32-rounded start (1.8e-7, 1.7e-5); a check-mode window then shows that
+  every node whose entropy condition has a root inside the positivity
+  bracket meets |H(f + alpha Delta) - H(f)| <= 1e-10 (the rare nodes without
+  one take alpha = 2 in both paths and are counted);
 - sphere 256x128x128 (r = 16 icosphere, interpolated wall links), 2000 steps:
   rho within 1e-4 and the rms of u within 1e-4 of the inlet speed; the largest
   u difference within 1e-3 (FP32 rounding of every step accumulates; the FP64
@@ -96,19 +96,19 @@ def test_boundary_layer_fp32_vs_fp64_1000_steps(pkg, built_lib):
     _, u64 = lat.moments27(f64)
     _, u32 = lat.moments27(f32)
     prof = float(np.max(np.abs(u32[..., 0].mean(axis=(1, 2)) - u64[..., 0].mean(axis=(1, 2)))) / u_in)
-    # the same away from the plate's leading edge (x >= 8)
-    away = fluid.copy()
-    away[:, :, :8] = False
-    e_away = _errors(lat, f64, f32, a64, a32, u_in, away)
+    # where the largest velocity difference sits
+    _, u64n = lat.moments27(f64)
+    _, u32n = lat.moments27(f32)
+    du = np.where(fluid, np.abs(u32n - u64n).max(axis=-1), 0.0)
+    where = [int(v) for v in np.unravel_index(int(np.argmax(du)), du.shape)]
     e.update(case="boundary layer 128x64x64, 1000 steps", max_abs_dH=chk["max_abs_dH"], dh_over=chk["dh_over_tol"],
              check_window_fallbacks=chk["fallbacks"], fallback_fraction_fp64=fb64, fallback_fraction_fp32=fb32,
-             mean_u_profile_max=prof, away_from_leading_edge={k: v for k, v in e_away.items() if k.endswith("max")},
+             mean_u_profile_max=prof, u_max_at_zyx=where,
              fp64_from_fp32_rounded_start={k: v for k, v in sens.items() if k.startswith(("rho", "u"))})
     print("CONTRACT " + json.dumps(e))
     assert np.isfinite(f32[:, fluid]).all()
-    # rho and u within 1e-4 of the FP64 path in rms; the largest differences sit at the plate's
-    # leading edge (inlet meets wall), where some nodes' entropy condition has no root in the
-    # positivity bracket in either path (alpha = 2 there, counted): measured rho 1.6e-4, u 2.3e-3
+    # rho and u within 1e-4 of the FP64 path in rms; the largest differences are isolated nodes
+    # (measured rho 1.6e-4, u 2.3e-3 of the inlet speed; rms 8.9e-6 and 9.4e-5)
     assert e["rho_rms"] <= 1e-4 and e["u_rms"] <= 1e-4
     assert e["rho_max"] <= 1e-3 and e["u_max"] <= 1e-2
     assert fb64 <= 1e-5 and fb32 <= 1e-5
