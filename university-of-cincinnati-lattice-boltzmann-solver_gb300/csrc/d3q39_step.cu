@@ -18,6 +18,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <utility>
 
 #include "kernels39.cuh"
 
@@ -114,7 +115,82 @@ __device__ double lu_update39(double* J, const double (&target)[NL], double (&lm
   return md;
 }
 
+// The lattice tables at compile time for the two velocity sets the step runs
+// most (LAT 1: unshifted; LAT 2: shifted along +x, primary flow direction 1;
+// LAT 0: the tables in constant memory, any set).  With the integers known
+// as template arguments, the zero terms of the Jacobian (53-62% of its 3,549
+// products) and of the exponents drop out at compile time and the +-1 terms
+// become additions: the same fused operations on the non-zero terms in the
+// same order, so the same results, with about half the FP64 work of the
+// multiplier Newton.
+__host__ __device__ constexpr int cx39u(int i) {
+  const int t[39] = {0, 1, 0, 0, -1, 0, 0, 1, -1, -1, 1, 1, -1, -1, 1, 2, 0, 0, -2, 0,
+                     0, 2, 2, 0, -2, -2, 2, 2, -2, -2, 0, 0, 0, 3, 0, 0, -3, 0, 0};
+  return t[i];
+}
+__host__ __device__ constexpr int cy39u(int i) {
+  const int t[39] = {0, 0, 1, 0, 0, -1, 0, 1, 1, -1, -1, 1, 1, -1, -1, 0, 2, 0, 0, -2,
+                     0, 2, 0, 2, 2, -2, -2, 0, 0, 0, 2, -2, -2, 0, 3, 0, 0, -3, 0};
+  return t[i];
+}
+__host__ __device__ constexpr int cz39u(int i) {
+  const int t[39] = {0, 0, 0, 1, 0, 0, -1, 1, 1, 1, 1, -1, -1, -1, -1, 0, 0, 2, 0, 0,
+                     -2, 0, 2, 2, 0, 0, 0, -2, -2, 2, -2, -2, 2, 0, 0, 3, 0, 0, -3};
+  return t[i];
+}
+template <int LAT>
+__host__ __device__ constexpr int phi39c(int r, int i) {
+  const int x = cx39u(i) + (LAT == 2 ? 1 : 0), y = cy39u(i), z = cz39u(i);
+  const int c2 = x * x + y * y + z * z;
+  const int m[13] = {1, x, y, z, x * x, y * y, z * z, x * y, x * z, y * z, x * c2, y * c2, z * c2};
+  return m[r];
+}
+
+// s += V * x as one fused operation, nothing for V = 0
+template <int V>
+__device__ __forceinline__ void fma39(double& s, double x) {
+  if constexpr (V != 0) s = fma((double)V, x, s);
+}
+
+// the exponent of fieq39 for direction I: lm[0] + sum_r phi_r lm[r], left to right
+template <int LAT, int I, int... R>
+__device__ __forceinline__ double expo39(const double (&lm)[NL], std::integer_sequence<int, R...>) {
+  double a = lm[0];
+  (fma39<phi39c<LAT>(R + 1, I)>(a, lm[R + 1]), ...);
+  return a;
+}
+template <int LAT, int... I>
+__device__ __forceinline__ void fieq39_all(double rho, const double (&lm)[NL], double (&fe)[Q],
+                                           std::integer_sequence<int, I...>) {
+  ((fe[I] = rho * exp(expo39<LAT, I>(lm, std::make_integer_sequence<int, NL - 1>{}))), ...);
+}
+
+// Jacobian entry (R, C): sum_i phi_R phi_C fieq_i over the directions in order
+template <int LAT, int R, int C, int... I>
+__device__ __forceinline__ double jac39(const double (&fe)[Q], std::integer_sequence<int, I...>) {
+  double s = 0.0;
+  (fma39<phi39c<LAT>(R, I) * phi39c<LAT>(C, I)>(s, fe[I]), ...);
+  return s;
+}
+template <int LAT, int R, int C>
+__device__ __forceinline__ void jac39_cell(double* J, const double (&fe)[Q]) {
+  if constexpr (C >= R) {
+    const double s = jac39<LAT, R, C>(fe, std::make_integer_sequence<int, Q>{});
+    J[R * NL + C] = s;
+    J[C * NL + R] = s;
+  }
+}
+template <int LAT, int R, int... C>
+__device__ __forceinline__ void jac39_row(double* J, const double (&fe)[Q], std::integer_sequence<int, C...>) {
+  (jac39_cell<LAT, R, C>(J, fe), ...);
+}
+template <int LAT, int... R>
+__device__ __forceinline__ void jac39_all(double* J, const double (&fe)[Q], std::integer_sequence<int, R...>) {
+  (jac39_row<LAT, R>(J, fe, std::make_integer_sequence<int, NL>{}), ...);
+}
+
 // calculate_lagrangian_mults.f95:696-1097; returns iterations (negative at the cap).
+template <int LAT = 0>
 __device__ int lagrange39(int max_it, double rho, double u, double v, double w, double temp, const double (&P)[6],
                           double (&lm)[NL], double (&fieq)[Q]) {
   const double vel_mag = u * u + v * v + w * w;
@@ -128,15 +204,20 @@ __device__ int lagrange39(int max_it, double rho, double u, double v, double w, 
   while (max_diff > 1.0e-7) {
     if (it >= max_it) return -it;
     ++it;
-    for (int i = 0; i < Q; ++i) fieq[i] = fieq39(rho, lm, i);
-    int k = 0;
-    for (int r = 0; r < NL; ++r)
-      for (int c = r; c < NL; ++c, ++k) {
-        double s = 0.0;
-        for (int i = 0; i < Q; ++i) s += c39d.pp[k][i] * fieq[i];
-        J[r * NL + c] = s;
-        J[c * NL + r] = s;
-      }
+    if constexpr (LAT == 0) {
+      for (int i = 0; i < Q; ++i) fieq[i] = fieq39(rho, lm, i);
+      int k = 0;
+      for (int r = 0; r < NL; ++r)
+        for (int c = r; c < NL; ++c, ++k) {
+          double s = 0.0;
+          for (int i = 0; i < Q; ++i) s += c39d.pp[k][i] * fieq[i];
+          J[r * NL + c] = s;
+          J[c * NL + r] = s;
+        }
+    } else {
+      fieq39_all<LAT>(rho, lm, fieq, std::make_integer_sequence<int, Q>{});
+      jac39_all<LAT>(J, fieq, std::make_integer_sequence<int, NL>{});
+    }
     max_diff = lu_update39(J, target, lm);
   }
   return it;
@@ -261,7 +342,7 @@ __device__ __forceinline__ void st_fg39(const Step39Args& a, int i, int64_t n, d
   }
 }
 
-template <bool F32>
+template <bool F32, int LAT>
 __global__ void __launch_bounds__(64) d3q39_step_kernel(const Step39Args a) {
   const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= a.N) return;
@@ -337,7 +418,7 @@ __global__ void __launch_bounds__(64) d3q39_step_kernel(const Step39Args a) {
   const double P[6] = {rho * (temp + u * u), rho * (temp + v * v), rho * (temp + w_old * w_old),
                        rho * u * v,          rho * u * w,          rho * v * w};
   double fe[Q];
-  int it = lagrange39(k.max_lm_iters, rho, u, v, w, temp, P, lm, fe);
+  int it = lagrange39<LAT>(k.max_lm_iters, rho, u, v, w, temp, P, lm, fe);
   unsigned flags = 0;
   if (it < 0) {
     flags |= 0x2u;
@@ -350,8 +431,9 @@ __global__ void __launch_bounds__(64) d3q39_step_kernel(const Step39Args a) {
   // collision.f95:153-300 with the final multipliers
   const double lead = 2.0 * k.const_vol - 3;
   double gd[Q];
+  if constexpr (LAT != 0) fieq39_all<LAT>(rho, lm, fe, std::make_integer_sequence<int, Q>{});
   for (int i = 0; i < Q; ++i) {
-    fe[i] = fieq39(rho, lm, i);
+    if constexpr (LAT == 0) fe[i] = fieq39(rho, lm, i);
     fd[i] = fe[i] - f[i];
     gd[i] = lead * temp * fe[i] - g[i];
   }
@@ -954,8 +1036,18 @@ __global__ void d3q39_average_down_kernel(const Box39View* __restrict__ fbs, con
 void launch_d3q39_fp64(const Step39Args& a, cudaStream_t s) {
   const int threads = 64;
   const int64_t blocks = (a.N + threads - 1) / threads;
-  if (a.fsrc32) d3q39_step_kernel<true><<<(unsigned)blocks, threads, 0, s>>>(a);
-  else d3q39_step_kernel<false><<<(unsigned)blocks, threads, 0, s>>>(a);
+  // the compile-time tables of the unshifted set and of the set shifted along +x
+  const int lat = !a.k.shifted ? 1 : (a.k.primary_flow_dir == 1 ? 2 : 0);
+  const unsigned g = (unsigned)blocks;
+  if (a.fsrc32) {
+    if (lat == 1) d3q39_step_kernel<true, 1><<<g, threads, 0, s>>>(a);
+    else if (lat == 2) d3q39_step_kernel<true, 2><<<g, threads, 0, s>>>(a);
+    else d3q39_step_kernel<true, 0><<<g, threads, 0, s>>>(a);
+  } else {
+    if (lat == 1) d3q39_step_kernel<false, 1><<<g, threads, 0, s>>>(a);
+    else if (lat == 2) d3q39_step_kernel<false, 2><<<g, threads, 0, s>>>(a);
+    else d3q39_step_kernel<false, 0><<<g, threads, 0, s>>>(a);
+  }
 }
 
 // damp_it.f95:64-177, fout part, on a box with link codes (see the oracle's
