@@ -300,6 +300,22 @@ int elbm_mark_triangles(int nx, int ny, int nz, const double* origin, double dx,
  * meet one +x ray; elbm_mark_triangles handles those). */
 int elbm_mark_triangles_gpu(elbm_ctx* ctx, int nx, int ny, int nz, const double* origin, double dx, int ntri,
                             const double* tri, int32_t* state);
+/* The D3Q39 codes of a box from a closed triangulated surface (the same set-up
+ * for the D3Q39 lattices: lbgrid/shifted_state_directions.f95:54-68 on the
+ * shifted lattice, state_directions.f95:696 on the unshifted one, with the
+ * crossing of inter_bb_setup.f95 / linkwise.f95:45-57).  state is
+ * (39, nz, ny, nx), updated in place: solid nodes (odd count of +x ray
+ * crossings) get node type -1001 and -666 on their links; link i of a fluid
+ * node gets -1001 - floor(t 1e9) when the node x - c_i (shifted lattice, c the
+ * shifted velocities of primary_flow_dir) or x + c_i (unshifted) is solid, t
+ * the nearest crossing of the segment towards it (1 when none is found);
+ * periodic (bits x, y, z) wraps that neighbour.  elbm_mark_triangles39 runs on
+ * the host, elbm_mark_triangles39_gpu on the context's device with the same
+ * codes bit for bit. */
+int elbm_mark_triangles39(int nx, int ny, int nz, const double* origin, double dx, int ntri, const double* tri,
+                          int shifted, int primary_flow_dir, int periodic, int32_t* state);
+int elbm_mark_triangles39_gpu(elbm_ctx* ctx, int nx, int ny, int nz, const double* origin, double dx, int ntri,
+                              const double* tri, int shifted, int primary_flow_dir, int periodic, int32_t* state);
 
 /* Copy one box's post-collision populations (fout FAB, FP64, Q comps) to / from the device. */
 int elbm_upload_level(elbm_ctx* ctx, int lvl, int box, const double* fout);

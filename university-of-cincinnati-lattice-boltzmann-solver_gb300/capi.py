@@ -183,6 +183,10 @@ SIGNATURES = {
                                      _vp, _vp, ct.c_int64, _vp]),
     "elbm_mark_triangles": (_c_int, [_c_int, _c_int, _c_int, _vp, _c_double, _c_int, _vp, _vp]),
     "elbm_mark_triangles_gpu": (_c_int, [_vp, _c_int, _c_int, _c_int, _vp, _c_double, _c_int, _vp, _vp]),
+    "elbm_mark_triangles39": (_c_int, [_c_int, _c_int, _c_int, _vp, _c_double, _c_int, _vp, _c_int, _c_int, _c_int,
+                                       _vp]),
+    "elbm_mark_triangles39_gpu": (_c_int, [_vp, _c_int, _c_int, _c_int, _vp, _c_double, _c_int, _vp, _c_int, _c_int,
+                                           _c_int, _vp]),
     "elbm_alpha_harvest": (_c_int, [_vp, _c_int, _c_int, _c_int, _vp, ct.c_int64, _vp]),
     "elbm_alpha_mlp_infer": (_c_int, [_vp, _vp, _vp, ct.c_int64, _vp, _vp]),
     "elbm_alpha_mlp_grad": (_c_int, [_vp, _vp, _vp, ct.c_int64, _vp, _vp]),
@@ -280,6 +284,21 @@ def mark_triangles(state: np.ndarray, origin, dx: float, tri: np.ndarray) -> Non
     rc = lib.elbm_mark_triangles(nx, ny, nz, _ptr(o), dx, t.shape[0], _ptr(t), _ptr(state))
     if rc != ELBM_OK:
         raise ElbmError(rc, "elbm_mark_triangles failed")
+
+
+def mark_triangles39(state: np.ndarray, origin, dx: float, tri: np.ndarray, shifted: int = 1,
+                     primary_flow_dir: int = 1, periodic: int = 0) -> None:
+    """D3Q39 solid nodes and wall links of a closed triangulated surface in a state
+    array (39, nz, ny, nx), in place (host code, no GPU needed)."""
+    lib = load()
+    assert state.dtype == np.int32 and state.flags.c_contiguous and state.shape[0] == 39
+    _, nz, ny, nx = state.shape
+    o = np.ascontiguousarray(origin, np.float64)
+    t = np.ascontiguousarray(tri, np.float64).reshape(-1, 9)
+    rc = lib.elbm_mark_triangles39(nx, ny, nz, _ptr(o), dx, t.shape[0], _ptr(t), shifted, primary_flow_dir, periodic,
+                                   _ptr(state))
+    if rc != ELBM_OK:
+        raise ElbmError(rc, "elbm_mark_triangles39 failed")
 
 
 class Context:
@@ -405,6 +424,16 @@ class Context:
         t = np.ascontiguousarray(tri, np.float64)
         self._check(self.lib.elbm_mark_triangles_gpu(self.h, nx, ny, nz, _ptr(o), dx, t.shape[0], _ptr(t),
                                                      _ptr(state)))
+
+    def mark_triangles39(self, state: np.ndarray, origin, dx: float, tri: np.ndarray, shifted: int = 1,
+                         primary_flow_dir: int = 1, periodic: int = 0) -> None:
+        """elbm_mark_triangles39 on this context's device (state (39, nz, ny, nx) int32, updated in place)."""
+        assert state.dtype == np.int32 and state.flags.c_contiguous and state.shape[0] == 39
+        nz, ny, nx = state.shape[1:]
+        o = np.ascontiguousarray(origin, np.float64)
+        t = np.ascontiguousarray(tri, np.float64).reshape(-1, 9)
+        self._check(self.lib.elbm_mark_triangles39_gpu(self.h, nx, ny, nz, _ptr(o), dx, t.shape[0], _ptr(t), shifted,
+                                                       primary_flow_dir, periodic, _ptr(state)))
 
     def checkpoint_write(self, lvl, path):
         self._check(self.lib.elbm_checkpoint_write(self.h, lvl, str(path).encode()))

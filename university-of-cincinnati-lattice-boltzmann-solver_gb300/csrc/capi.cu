@@ -2353,6 +2353,19 @@ int elbm_mark_triangles_gpu(elbm_ctx* c, int nx, int ny, int nz, const double* o
   return ELBM_OK;
 }
 
+int elbm_mark_triangles39_gpu(elbm_ctx* c, int nx, int ny, int nz, const double* origin, double dx, int ntri,
+                              const double* tri, int shifted, int primary_flow_dir, int periodic, int32_t* state) {
+  if (!c || nx < 1 || ny < 1 || nz < 1 || !origin || !(dx > 0.0) || ntri < 1 || !tri || !state || periodic < 0 ||
+      periodic > 7 || primary_flow_dir < 1 || primary_flow_dir > 6)
+    return fail(c, ELBM_E_ARG, "bad arguments");
+  CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
+  std::string why;
+  const int rc = mark_triangles39_device(nx, ny, nz, origin, dx, ntri, tri, shifted, primary_flow_dir, periodic,
+                                         state, c->stream, why);
+  if (rc) return fail(c, rc, "%s", why.c_str());
+  return ELBM_OK;
+}
+
 int elbm_write_plot3d(elbm_ctx* c, int lvl, const char* grid_path, const char* data_path, const double* origin,
                       double dx, const elbm_plot3d_header* hdr) {
   Level* lv = get_level(c, lvl);

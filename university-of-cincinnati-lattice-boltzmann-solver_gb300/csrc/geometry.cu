@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/elbm_gb300.h"
+#include "kernels39.cuh"
 #include "lattice.cuh"
 
 namespace {
@@ -96,7 +97,7 @@ struct TriGrid {
   std::vector<int32_t> start, tris;  // per cell: tris[start[c] .. start[c + 1])
 };
 
-void build_tri_grid(int ntri, const double* tri, double dx, TriGrid& G) {
+void build_tri_grid(int ntri, const double* tri, double dx, TriGrid& G, double reach = 1.0) {
   G.T.resize(ntri);
   for (int c = 0; c < 3; ++c) {
     G.glo[c] = INFINITY;
@@ -118,7 +119,8 @@ void build_tri_grid(int ntri, const double* tri, double dx, TriGrid& G) {
       G.ghi[c] = std::max(G.ghi[c], t.hi[c]);
     }
   }
-  G.cell = 2.0 * dx;
+  // cells of 2 dx (D3Q27 links are at most sqrt(3) dx long) or of the longest D3Q39 link
+  G.cell = std::max(2.0, reach) * dx;
   for (int c = 0; c < 3; ++c) G.gn[c] = std::max(1, (int)std::ceil((G.ghi[c] - G.glo[c]) / G.cell) + 1);
   const size_t ncell = (size_t)G.gn[0] * G.gn[1] * G.gn[2];
   std::vector<std::vector<int32_t>> lists(ncell);
@@ -166,6 +168,112 @@ __host__ __device__ int32_t wall_code(const Tri* T, const int32_t* start, const 
   const double len = sqrt((double)(c[0] * c[0] + c[1] * c[1] + c[2] * c[2])) * dx;
   const double dist = tbest * len;
   return -1001 - (int32_t)floor(dist / len * 1e9);
+}
+
+// The nearest crossing t in (0, 1] of the segment p0 -> p0 + c dx with the
+// triangles of the cells around p0 (cells at least as long as the segment),
+// 1 when none is found (a link that ends in a solid node without a recorded
+// crossing), as the wall code -1001 - floor(t 1e9) (linkwise.f95:56).
+__host__ __device__ int32_t seg_code(const Tri* T, const int32_t* start, const int32_t* tris, const double* glo,
+                                     double cell, const int* gn, const double p0[3], const int c[3], double dx) {
+  const int gc[3] = {(int)floor((p0[0] - glo[0]) / cell), (int)floor((p0[1] - glo[1]) / cell),
+                     (int)floor((p0[2] - glo[2]) / cell)};
+  const double p1[3] = {p0[0] + c[0] * dx, p0[1] + c[1] * dx, p0[2] + c[2] * dx};
+  double tbest = INFINITY;
+  for (int d2 = -1; d2 <= 1; ++d2)
+    for (int d1 = -1; d1 <= 1; ++d1)
+      for (int d0 = -1; d0 <= 1; ++d0) {
+        const int g0 = gc[0] + d0, g1 = gc[1] + d1, g2 = gc[2] + d2;
+        if (g0 < 0 || g1 < 0 || g2 < 0 || g0 >= gn[0] || g1 >= gn[1] || g2 >= gn[2]) continue;
+        const size_t cc = ((size_t)g2 * gn[1] + g1) * gn[0] + g0;
+        for (int32_t e = start[cc]; e < start[cc + 1]; ++e) {
+          const double tt = seg_tri(T[tris[e]], p0, p1);
+          if (tt > 0.0 && tt < tbest) tbest = tt;
+        }
+      }
+  if (tbest == INFINITY) tbest = 1.0;
+  return -1001 - (int32_t)floor(tbest * 1e9);
+}
+
+// The D3Q39 link vectors of a level and the rule that makes link i a wall
+// link: on the shifted lattice (shifted_state_directions.f95:54-68) when the
+// upstream node x - c_i is solid, the crossing searched from x towards it; on
+// the unshifted lattice (state_directions.f95:696) when the downstream node
+// x + c_i is solid, searched towards it.  seg[i] is the searched segment's
+// direction, +-c_i.
+struct Links39Geo {
+  int seg[39][3];
+  int periodic;
+};
+
+Links39Geo links39_geo(int shifted, int pfd, int periodic) {
+  elbm::Lattice39 L;
+  elbm::build_lattice39(shifted, pfd, L);
+  Links39Geo G{};
+  const int sgn = shifted ? -1 : 1;
+  for (int i = 0; i < 39; ++i) {
+    G.seg[i][0] = sgn * L.cx[i];
+    G.seg[i][1] = sgn * L.cy[i];
+    G.seg[i][2] = sgn * L.cz[i];
+  }
+  G.periodic = periodic;
+  return G;
+}
+
+// Index of (i, j, k) with periodic wrap, -1 outside the box on a non-periodic axis.
+__host__ __device__ int64_t geo_node(int i, int j, int k, int nx, int ny, int nz, int periodic) {
+  if (periodic & 1) i = ((i % nx) + nx) % nx;
+  else if (i < 0 || i >= nx) return -1;
+  if (periodic & 2) j = ((j % ny) + ny) % ny;
+  else if (j < 0 || j >= ny) return -1;
+  if (periodic & 4) k = ((k % nz) + nz) % nz;
+  else if (k < 0 || k >= nz) return -1;
+  return ((int64_t)k * ny + j) * nx + i;
+}
+
+// The D3Q39 codes of node n: a solid node gets node type -1001 and -666 on its
+// links; a fluid node's links whose searched neighbour is solid get wall codes.
+__host__ __device__ void links39_node(const Tri* T, const int32_t* start, const int32_t* tris, const double* glo,
+                                      double cell, const int* gn, int nx, int ny, int nz, const double* origin,
+                                      double dx, const Links39Geo& G, const uint8_t* solid, int64_t n,
+                                      int32_t* state) {
+  const int64_t N = (int64_t)nx * ny * nz;
+  if (solid[n]) {
+    state[n] = -1001;
+    for (int q = 1; q < 39; ++q) state[(int64_t)q * N + n] = -666;
+    return;
+  }
+  const int i = (int)(n % nx), j = (int)((n / nx) % ny), k = (int)(n / ((int64_t)nx * ny));
+  const double p0[3] = {origin[0] + i * dx, origin[1] + j * dx, origin[2] + k * dx};
+  for (int q = 1; q < 39; ++q) {
+    const int64_t m = geo_node(i + G.seg[q][0], j + G.seg[q][1], k + G.seg[q][2], nx, ny, nz, G.periodic);
+    if (m < 0 || !solid[m]) continue;
+    state[(int64_t)q * N + n] = seg_code(T, start, tris, glo, cell, gn, p0, G.seg[q], dx);
+  }
+}
+
+// Solid nodes by +x ray casting (host).
+void mark_solid_host(const TriGrid& G, int nx, int ny, int nz, const double* origin, double dx,
+                     std::vector<uint8_t>& solid) {
+  const std::vector<Tri>& T = G.T;
+  const int ntri = (int)T.size();
+  solid.assign((size_t)nx * ny * nz, 0);
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j) {
+      const double y = origin[1] + (j + kRayDy) * dx, z = origin[2] + (k + kRayDz) * dx;
+      if (y < G.glo[1] || y > G.ghi[1] || z < G.glo[2] || z > G.ghi[2]) continue;
+      std::vector<int> cand;
+      for (int t = 0; t < ntri; ++t)
+        if (T[t].lo[1] <= y && y <= T[t].hi[1] && T[t].lo[2] <= z && z <= T[t].hi[2]) cand.push_back(t);
+      if (cand.empty()) continue;
+      for (int i = 0; i < nx; ++i) {
+        const double p[3] = {origin[0] + i * dx, y, z};
+        if (p[0] > G.ghi[0]) break;
+        int cross = 0;
+        for (int t : cand) cross += ray_x_crosses(T[t], p) ? 1 : 0;
+        if (cross & 1) solid[((int64_t)k * ny + j) * nx + i] = 1;
+      }
+    }
 }
 
 // ---- device path ----
@@ -230,9 +338,85 @@ __global__ void mark_links_kernel(const Tri* __restrict__ T, const int32_t* __re
   }
 }
 
+// One thread per node: the D3Q39 codes (links39_node).
+__global__ void mark_links39_kernel(const Tri* __restrict__ T, const int32_t* __restrict__ start,
+                                    const int32_t* __restrict__ tris, int nx, int ny, int nz, double3 origin,
+                                    double dx, double3 glo, double cell, int3 gn, const Links39Geo G,
+                                    const uint8_t* __restrict__ solid, int32_t* __restrict__ state) {
+  const int64_t N = (int64_t)nx * ny * nz;
+  const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const double o[3] = {origin.x, origin.y, origin.z}, g0[3] = {glo.x, glo.y, glo.z};
+  const int gnn[3] = {gn.x, gn.y, gn.z};
+  links39_node(T, start, tris, g0, cell, gnn, nx, ny, nz, o, dx, G, solid, n, state);
+}
+
+// The longest searched D3Q39 segment in lattice units.
+double seg39_reach(const Links39Geo& G) {
+  double r = 0.0;
+  for (int q = 0; q < 39; ++q)
+    r = std::max(r, std::sqrt((double)(G.seg[q][0] * G.seg[q][0] + G.seg[q][1] * G.seg[q][1] + G.seg[q][2] * G.seg[q][2])));
+  return std::ceil(r);
+}
+
 }  // namespace
 
 namespace elbm {
+
+// elbm_mark_triangles39 on the device.
+int mark_triangles39_device(int nx, int ny, int nz, const double* origin, double dx, int ntri, const double* tri,
+                            int shifted, int pfd, int periodic, int32_t* state, cudaStream_t s, std::string& why) {
+  const Links39Geo LG = links39_geo(shifted, pfd, periodic);
+  TriGrid G;
+  build_tri_grid(ntri, tri, dx, G, seg39_reach(LG));
+  const int64_t N = (int64_t)nx * ny * nz;
+  Tri* dT = nullptr;
+  int32_t *dstart = nullptr, *dtris = nullptr, *dstate = nullptr;
+  uint8_t* dsolid = nullptr;
+  int* dover = nullptr;
+  auto release = [&]() {
+    cudaFree(dT);
+    cudaFree(dstart);
+    cudaFree(dtris);
+    cudaFree(dstate);
+    cudaFree(dsolid);
+    cudaFree(dover);
+  };
+  if (cudaMalloc(&dT, sizeof(Tri) * ntri) || cudaMalloc(&dstart, sizeof(int32_t) * G.start.size()) ||
+      cudaMalloc(&dtris, sizeof(int32_t) * std::max<size_t>(G.tris.size(), 1)) ||
+      cudaMalloc(&dstate, sizeof(int32_t) * 39 * N) || cudaMalloc(&dsolid, N) || cudaMalloc(&dover, sizeof(int))) {
+    release();
+    why = "device memory";
+    return ELBM_E_CUDA;
+  }
+  cudaMemcpyAsync(dT, G.T.data(), sizeof(Tri) * ntri, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(dstart, G.start.data(), sizeof(int32_t) * G.start.size(), cudaMemcpyHostToDevice, s);
+  if (!G.tris.empty())
+    cudaMemcpyAsync(dtris, G.tris.data(), sizeof(int32_t) * G.tris.size(), cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(dstate, state, sizeof(int32_t) * 39 * N, cudaMemcpyHostToDevice, s);
+  cudaMemsetAsync(dover, 0, sizeof(int), s);
+  const double3 o = make_double3(origin[0], origin[1], origin[2]);
+  mark_solid_kernel<<<(unsigned)((int64_t)ny * nz), 128, 0, s>>>(
+      dT, ntri, nx, ny, nz, o, dx, make_double3(G.glo[0], G.glo[1], G.glo[2]),
+      make_double3(G.ghi[0], G.ghi[1], G.ghi[2]), dsolid, dover);
+  mark_links39_kernel<<<(unsigned)((N + 127) / 128), 128, 0, s>>>(
+      dT, dstart, dtris, nx, ny, nz, o, dx, make_double3(G.glo[0], G.glo[1], G.glo[2]), G.cell,
+      make_int3(G.gn[0], G.gn[1], G.gn[2]), LG, dsolid, dstate);
+  int over = 0;
+  cudaMemcpyAsync(&over, dover, sizeof(int), cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(state, dstate, sizeof(int32_t) * 39 * N, cudaMemcpyDeviceToHost, s);
+  const cudaError_t e = cudaStreamSynchronize(s);
+  release();
+  if (e != cudaSuccess) {
+    why = cudaGetErrorString(e);
+    return ELBM_E_CUDA;
+  }
+  if (over) {
+    why = "more than 4096 triangles along one +x ray of the lattice; use elbm_mark_triangles39";
+    return ELBM_E_UNSUPPORTED;
+  }
+  return ELBM_OK;
+}
 
 // elbm_mark_triangles on the device (the C-ABI entry takes the context's stream).
 int mark_triangles_device(int nx, int ny, int nz, const double* origin, double dx, int ntri, const double* tri,
@@ -339,5 +523,24 @@ extern "C" int elbm_mark_triangles(int nx, int ny, int nz, const double* origin,
           state[(int64_t)q * N + n] = wall_code(T.data(), G.start.data(), G.tris.data(), glo, G.cell, G.gn, p0, q, dx);
         }
       }
+  return ELBM_OK;
+}
+
+extern "C" int elbm_mark_triangles39(int nx, int ny, int nz, const double* origin, double dx, int ntri,
+                                     const double* tri, int shifted, int primary_flow_dir, int periodic,
+                                     int32_t* state) {
+  using namespace elbm;
+  if (nx < 1 || ny < 1 || nz < 1 || !origin || !(dx > 0.0) || ntri < 1 || !tri || !state || periodic < 0 ||
+      periodic > 7 || primary_flow_dir < 1 || primary_flow_dir > 6)
+    return ELBM_E_ARG;
+  const Links39Geo LG = links39_geo(shifted, primary_flow_dir, periodic);
+  TriGrid G;
+  build_tri_grid(ntri, tri, dx, G, seg39_reach(LG));
+  std::vector<uint8_t> solid;
+  mark_solid_host(G, nx, ny, nz, origin, dx, solid);
+  const int64_t N = (int64_t)nx * ny * nz;
+  for (int64_t n = 0; n < N; ++n)
+    links39_node(G.T.data(), G.start.data(), G.tris.data(), G.glo, G.cell, G.gn, nx, ny, nz, origin, dx, LG,
+                 solid.data(), n, state);
   return ELBM_OK;
 }

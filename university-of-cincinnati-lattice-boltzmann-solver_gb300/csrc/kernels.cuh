@@ -12,6 +12,9 @@ namespace elbm {
 // state is the host array, read and written back.
 int mark_triangles_device(int nx, int ny, int nz, const double* origin, double dx, int ntri, const double* tri,
                           int32_t* state, cudaStream_t s, std::string& why);
+// D3Q39 codes (shifted or unshifted lattice) from a triangulated surface on the device.
+int mark_triangles39_device(int nx, int ny, int nz, const double* origin, double dx, int ntri, const double* tri,
+                            int shifted, int pfd, int periodic, int32_t* state, cudaStream_t s, std::string& why);
 
 // Device-side statistics of one or more steps (accumulated with atomics).
 struct DevStats {

@@ -301,3 +301,22 @@ def wedge_case_state(nx: int = 384, ny: int = 48, nz: int = 192) -> np.ndarray:
     explicit scheme does not keep finite."""
     return wedge_state39(nx, ny, nz, nx / 4, nx * 7 / 8, 10.0, WEDGE_FACES, periodic=0, priority=WEDGE_PRIORITY,
                          x_apex=nx * 9 / 16)
+
+
+def wedge_triangles(x0: float, x_apex: float, x1: float, angle_deg: float, ny: int) -> np.ndarray:
+    """The double-ramp wedge of wedge_state39 (x_apex given) as a closed
+    triangulated prism (8 triangles, (8, 3, 3)): its cross-section in the x-z
+    plane is the triangle under the two ramps, continued below the floor to
+    z = -1, extruded over y from -2 to ny + 1 (beyond the box, so that its end
+    caps meet no link)."""
+    t = math.tan(math.radians(angle_deg))
+    a = (x0 - 1.0 / t, -1.0)
+    b = (x_apex, t * (x_apex - x0))
+    c = (x1 + 1.0 / t, -1.0)
+    y0, y1 = -2.0, ny + 1.0
+    P = lambda q, y: (q[0], y, q[1])
+    tris = [(P(a, y0), P(b, y0), P(c, y0)), (P(a, y1), P(c, y1), P(b, y1))]
+    for p, q in ((a, b), (b, c), (c, a)):
+        tris.append((P(p, y0), P(q, y0), P(q, y1)))
+        tris.append((P(p, y0), P(q, y1), P(p, y1)))
+    return np.asarray(tris, np.float64)

@@ -69,7 +69,8 @@ module elbm_gb300_iface
     elbm_average_down, elbm_amr_run, elbm_damp_level, elbm_set_links39, elbm_upload_macro39, &
     elbm_init_level39, elbm_d3q39_equilibrium, elbm_checkpoint_write, elbm_checkpoint_read, elbm_ggm_tags, elbm_ggm_tags_pgs, &
     elbm_write_plot3d, elbm_mic_sample, elbm_mark_triangles_gpu, elbm_last_error_string, &
-    elbm_alpha_mlp_grad, elbm_alpha_mlp_infer, elbm_links39_tables, elbm_error_message
+    elbm_alpha_mlp_grad, elbm_alpha_mlp_infer, elbm_links39_tables, elbm_error_message, &
+    elbm_mark_triangles39, elbm_mark_triangles39_gpu
 
   interface
     integer(c_int) function elbm_create(device, ctx) bind(c, name="elbm_create")
@@ -166,6 +167,23 @@ module elbm_gb300_iface
       import :: c_int, c_ptr, c_double, c_int32_t
       type(c_ptr), value :: ctx
       integer(c_int), value :: nx, ny, nz, ntri
+      real(c_double), intent(in) :: origin(3), tri(9, *)
+      real(c_double), value :: dx
+      integer(c_int32_t), intent(inout) :: state(*)
+    end function
+    integer(c_int) function elbm_mark_triangles39(nx, ny, nz, origin, dx, ntri, tri, shifted, primary_flow_dir, &
+        periodic, state) bind(c, name="elbm_mark_triangles39")
+      import :: c_int, c_double, c_int32_t
+      integer(c_int), value :: nx, ny, nz, ntri, shifted, primary_flow_dir, periodic
+      real(c_double), intent(in) :: origin(3), tri(9, *)
+      real(c_double), value :: dx
+      integer(c_int32_t), intent(inout) :: state(*)
+    end function
+    integer(c_int) function elbm_mark_triangles39_gpu(ctx, nx, ny, nz, origin, dx, ntri, tri, shifted, &
+        primary_flow_dir, periodic, state) bind(c, name="elbm_mark_triangles39_gpu")
+      import :: c_int, c_ptr, c_double, c_int32_t
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: nx, ny, nz, ntri, shifted, primary_flow_dir, periodic
       real(c_double), intent(in) :: origin(3), tri(9, *)
       real(c_double), value :: dx
       integer(c_int32_t), intent(inout) :: state(*)
