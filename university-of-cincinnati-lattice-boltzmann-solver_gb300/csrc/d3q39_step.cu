@@ -1,5 +1,6 @@
 // Fused D3Q39 compressible ELBM level step (two populations f, g; 13 Lagrange
-// multipliers per node), FP64, one thread per node.
+// multipliers per node), FP64 arithmetic on FP64 or FP32-deviation storage,
+// one thread per node.
 //
 // Replaces, for the reference's D3Q39 lattice, the per-level chain
 //   streaming (looping/timestepping/streaming.f95:266-369, interior links)
