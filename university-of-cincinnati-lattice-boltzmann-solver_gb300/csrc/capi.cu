@@ -951,6 +951,8 @@ int elbm_level_register(elbm_ctx* c, int lvl, int lattice, int storage, int nbox
       CUDA_TRY(b->w_vel.alloc((size_t)b->plane), "w");
       CUDA_TRY(b->alpha64.alloc((size_t)b->plane), "alpha");
       CUDA_TRY(b->macro.alloc((size_t)b->plane * 5), "macro");
+      // defined fields for nodes no upload covers (a multi-box level's uncovered nodes)
+      CUDA_TRY(cudaMemset(b->macro.p, 0, b->macro.n * sizeof(double)), "macro");
       if (storage == ELBM_STORE_FP32_DEV) CUDA_TRY(b->ref39.alloc(78), "FP32 reference");
     }
     lv.boxes.push_back(std::move(b));
