@@ -635,9 +635,22 @@ int decode_link27(const int32_t* st, int64_t fab_plane, int64_t sidx, const int 
 
 int finish_stats(elbm_ctx* c, elbm_stats* out) {
   if (!out) return ELBM_OK;
-  DevStats ds{};
-  CUDA_TRY(cudaMemcpyAsync(&ds, c->stats.p, sizeof ds, cudaMemcpyDeviceToHost, c->stream), "stats");
+  DevStats slots[kStatSlots * kStatStride];
+  CUDA_TRY(cudaMemcpyAsync(slots, c->stats.p, kStatBytes, cudaMemcpyDeviceToHost, c->stream), "stats");
   CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
+  // the slots added up (maxima and flags combined)
+  DevStats ds{};
+  for (int k = 0; k < kStatSlots; ++k) {
+    const DevStats& s = slots[k * kStatStride];
+    ds.node_updates += s.node_updates;
+    ds.newton_iters += s.newton_iters;
+    ds.exact_nodes += s.exact_nodes;
+    ds.fallbacks += s.fallbacks;
+    ds.max_dH_bits = std::max(ds.max_dH_bits, s.max_dH_bits);
+    ds.dh_over += s.dh_over;
+    ds.guess_misses += s.guess_misses;
+    ds.status |= s.status;
+  }
   float ms = 0.f;
   CUDA_TRY(cudaEventElapsedTime(&ms, c->ev0, c->ev1), "elapsed");
   std::memset(out, 0, sizeof *out);
@@ -865,7 +878,8 @@ int elbm_create(int device, elbm_ctx** out) {
   if (e != cudaSuccess) return ELBM_E_CUDA;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return ELBM_E_CUDA;
   if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) return ELBM_E_CUDA;
-  if (c->stats.alloc(1) != cudaSuccess) return ELBM_E_CUDA;
+  if (c->stats.alloc((size_t)kStatSlots * kStatStride) != cudaSuccess) return ELBM_E_CUDA;
+  if (cudaMemset(c->stats.p, 0, kStatBytes) != cudaSuccess) return ELBM_E_CUDA;
   // reserve the allocation-free upload's staging buffer on this device now (csrc/noalloc.cu)
   if (noalloc_setup(device) != cudaSuccess) return ELBM_E_CUDA;
   *out = c.release();
@@ -1341,7 +1355,7 @@ int elbm_level_step(elbm_ctx* c, int lvl, int nsteps, elbm_stats* out) {
   if (nsteps < 0) return fail(c, ELBM_E_ARG, "negative step count");
   if (!lv->params_set) return fail(c, ELBM_E_STATE, "level parameters not set");
   CUDA_TRY(cudaSetDevice(c->device), "cudaSetDevice");
-  CUDA_TRY(cudaMemsetAsync(c->stats.p, 0, sizeof(DevStats), c->stream), "stats reset");
+  CUDA_TRY(cudaMemsetAsync(c->stats.p, 0, kStatBytes, c->stream), "stats reset");
   if (lv->lattice == ELBM_D3Q39) {
     const int rc = step39(c, *lv, nsteps);
     if (rc) return rc;
@@ -1405,7 +1419,7 @@ int elbm_autotune(elbm_ctx* c, int lvl, int reps, int* chosen, double* ms_per_va
   }
   lv->variant = best_v;
   if (chosen) *chosen = best_v;
-  CUDA_TRY(cudaMemsetAsync(c->stats.p, 0, sizeof(DevStats), c->stream), "stats reset");
+  CUDA_TRY(cudaMemsetAsync(c->stats.p, 0, kStatBytes, c->stream), "stats reset");
   return ELBM_OK;
 }
 
@@ -1452,7 +1466,7 @@ int elbm_alpha_harvest(elbm_ctx* c, int lvl, int nsteps, int stride, float* reco
   CUDA_TRY(buf.alloc((size_t)capacity * kMlpRecord), "harvest buffer");
   CUDA_TRY(cnt.alloc(1), "harvest counter");
   CUDA_TRY(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned long long), c->stream), "memset");
-  CUDA_TRY(cudaMemsetAsync(c->stats.p, 0, sizeof(DevStats), c->stream), "stats reset");
+  CUDA_TRY(cudaMemsetAsync(c->stats.p, 0, kStatBytes, c->stream), "stats reset");
   if (const int rc = ready27(c, *lv)) return rc;
   for (int s = 0; s < nsteps; ++s) {
     Step27Args a = level_args27(c, *lv);
@@ -1924,7 +1938,7 @@ int elbm_amr_run(elbm_ctx* c, int nlev, int ncycles, elbm_stats* out) {
     c->amr_nlev = nlev;
     c->amr_key = key;
   }
-  CUDA_TRY(cudaMemsetAsync(c->stats.p, 0, sizeof(DevStats), c->stream), "stats reset");
+  CUDA_TRY(cudaMemsetAsync(c->stats.p, 0, kStatBytes, c->stream), "stats reset");
   CUDA_TRY(cudaEventRecord(c->ev0, c->stream), "event");
   for (int r = 0; r < ncycles / 2; ++r) CUDA_TRY(cudaGraphLaunch(c->amr_exec, c->stream), "graph launch");
   if (ncycles % 2) enqueue_cycle(c, 0, nlev);  // an odd count: the last cycle by plain launches

@@ -173,6 +173,7 @@ __device__ __forceinline__ void store_dst(T* __restrict__ dst, int64_t plane, in
 
 __device__ __forceinline__ void warp_stats(DevStats* st, bool active, unsigned iters, bool exact, bool fb,
                                            unsigned flags, double dH) {
+  st += (blockIdx.x & (kStatSlots - 1)) * kStatStride;
   const unsigned mask = __activemask();
   const unsigned nover = __popc(__ballot_sync(mask, (flags & 0x8u) != 0));
   const unsigned nact = __popc(__ballot_sync(mask, active));
@@ -210,6 +211,7 @@ struct StatAcc {
 };
 
 __device__ __forceinline__ void flush_stats(DevStats* st, const StatAcc& s) {
+  st += (blockIdx.x & (kStatSlots - 1)) * kStatStride;
   const unsigned m = 0xffffffffu;
   const unsigned nodes = __reduce_add_sync(m, s.nodes_exact & 0xffffu), iters = __reduce_add_sync(m, s.iters);
   const unsigned exact = __reduce_add_sync(m, s.nodes_exact >> 16), fb = __reduce_add_sync(m, s.fb_over & 0xffffu);

@@ -28,6 +28,16 @@ struct DevStats {
   unsigned int status;
   unsigned int pad;
 };
+static_assert(sizeof(DevStats) == 64, "DevStats is half a cache line");
+
+// A context keeps kStatSlots DevStats slots, kStatStride apart (one 128-byte
+// line each).  The D3Q27 step kernels send a warp's updates to the slot of its
+// block (block index mod kStatSlots), so that the atomics of a big level do not
+// all queue at one L2 line; the other kernels use slot 0 and the host adds the
+// slots up.
+constexpr int kStatSlots = 64;
+constexpr int kStatStride = 2;
+constexpr size_t kStatBytes = sizeof(DevStats) * kStatSlots * kStatStride;
 
 // One box of a level as the tensor-copy (TMA) step variant walks it: tiles of
 // TX x TY nodes (TX = 1 << tx_log2 in {32, 64, 128}, TY = 256 / TX) in x, y,
