@@ -130,7 +130,8 @@ const char* elbm_last_error_string(const elbm_ctx* ctx);
  * their bounding box (links reach across box faces in place); its links,
  * populations, fields and initial state are complete once every box has been
  * given (elbm_set_links39, elbm_upload_level39 / elbm_upload_macro39,
- * elbm_init_level39). */
+ * elbm_init_level39).  An upload or initial state given to a box of a complete
+ * level starts over: the level steps again once every box has been given anew. */
 int elbm_level_register(elbm_ctx* ctx, int lvl, int lattice, int storage, int nbox, const int32_t* lo_hi,
                         int ngrow);
 

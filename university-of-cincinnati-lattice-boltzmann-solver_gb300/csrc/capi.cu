@@ -705,7 +705,11 @@ D3Q39Dev dev39(const elbm_d3q39_params& p, const Level& lv) {
 int step39(elbm_ctx* c, Level& lv, int nsteps) {
   const elbm_d3q39_params& p = lv.p39;
   for (auto& bp : lv.boxes) {
-    if (!bp->data_set) return fail(c, ELBM_E_STATE, "populations missing");
+    if (!bp->data_set)
+      return fail(c, ELBM_E_STATE,
+                  lv.sub39.empty() ? "populations missing"
+                                   : "populations missing: a level of several boxes steps once every box has been "
+                                     "uploaded (elbm_upload_level39 or elbm_init_level39)");
     if (!bp->links39 && p.periodic != 7)
       return fail(c, ELBM_E_STATE, "a D3Q39 box that is not periodic on every axis needs elbm_set_links39");
     if (bp->nwall39 > 0 && !bp->macro_set)
@@ -2153,6 +2157,12 @@ int elbm_upload_level39(elbm_ctx* c, int lvl, int box, const double* fout, const
     // the FP32 conversion, the slots that keep last step's values) once every box has arrived
     const int g = lv->ngrow;
     const bool f32 = lv->storage == ELBM_STORE_FP32_DEV;
+    if (b->data_set) {
+      // the level was complete: a new upload starts over, and the level steps again once every
+      // box has arrived (a box not given again would keep a state of another time)
+      std::fill(lv->sub39_have_pops.begin(), lv->sub39_have_pops.end(), 0);
+      b->data_set = false;
+    }
     if (f32) {
       if (!b->stage39.p) {
         CUDA_TRY(b->stage39.alloc((size_t)b->plane * 78), "FP64 staging");
@@ -2556,7 +2566,12 @@ int elbm_init_level39(elbm_ctx* c, int lvl, int box, const double* macro, const 
   if (capped) *capped = 0;
   if (!u.whole) {
     // one box of a multi-box level: the sheet's initial state is solved once every box's fields
-    // have arrived (with the last call's start multipliers; its count covers the whole sheet)
+    // have arrived (with the last call's start multipliers; its count covers the whole sheet);
+    // on a complete level the first call starts over, as an upload does
+    if (b->data_set) {
+      std::fill(lv->sub39_have_pops.begin(), lv->sub39_have_pops.end(), 0);
+      b->data_set = false;
+    }
     lv->sub39_have_init[box] = 1;
     if (!std::all_of(lv->sub39_have_init.begin(), lv->sub39_have_init.end(), [](uint8_t v) { return v; })) {
       CUDA_TRY(cudaStreamSynchronize(c->stream), "sync");
