@@ -277,7 +277,10 @@ void launch_stale39_init(Box& b, cudaStream_t s) {
 
 // FP32 D3Q39 storage: per-plane sums of an FP64 plane set (for the reference), and the
 // conversions between FP64 planes and float deviations from the reference.
-__global__ void plane_sums39_kernel(const double* __restrict__ src, int64_t N, int64_t plane, double* sums) {
+// Per-block partial sums of each of 39 planes (plane j, block k at j * gridDim.x + k); the host
+// adds them in block order, so that the reference (and every FP32 value) is the same run after run.
+__global__ void plane_sums39_kernel(const double* __restrict__ src, int64_t N, int64_t plane,
+                                    double* __restrict__ parts) {
   __shared__ double part[256];
   const int j = blockIdx.y;
   double acc = 0.0;
@@ -289,7 +292,7 @@ __global__ void plane_sums39_kernel(const double* __restrict__ src, int64_t N, i
     if ((int)threadIdx.x < w) part[threadIdx.x] += part[threadIdx.x + w];
     __syncthreads();
   }
-  if (threadIdx.x == 0) atomicAdd(&sums[j], part[0]);
+  if (threadIdx.x == 0) parts[(int64_t)j * gridDim.x + blockIdx.x] = part[0];
 }
 
 __global__ void to_dev39_kernel(const double* __restrict__ src, float* __restrict__ dst, int64_t N, int64_t plane,
@@ -312,15 +315,22 @@ cudaError_t stage39_to_fp32(Box& b, cudaStream_t s) {
   cudaError_t e = cudaSuccess;
   const int64_t half = b.plane * 39;
   if (!b.ref39_set) {
-    if ((e = cudaMemsetAsync(b.ref39.p, 0, 78 * sizeof(double), s)) != cudaSuccess) return e;
     const unsigned gx = (unsigned)std::min<int64_t>((b.N + 255) / 256, 512);
-    plane_sums39_kernel<<<dim3(gx, 39), 256, 0, s>>>(b.stage39.p, b.N, b.plane, b.ref39.p);
-    plane_sums39_kernel<<<dim3(gx, 39), 256, 0, s>>>(b.stage39.p + half, b.N, b.plane, b.ref39.p + 39);
-    std::vector<double> h(78);
-    if ((e = cudaMemcpyAsync(h.data(), b.ref39.p, 78 * sizeof(double), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+    DevBuf<double> parts;
+    if ((e = parts.alloc((size_t)78 * gx)) != cudaSuccess) return e;
+    plane_sums39_kernel<<<dim3(gx, 39), 256, 0, s>>>(b.stage39.p, b.N, b.plane, parts.p);
+    plane_sums39_kernel<<<dim3(gx, 39), 256, 0, s>>>(b.stage39.p + half, b.N, b.plane, parts.p + (size_t)39 * gx);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    std::vector<double> hp((size_t)78 * gx), h(78);
+    if ((e = cudaMemcpyAsync(hp.data(), parts.p, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, s)) !=
+        cudaSuccess)
       return e;
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
-    for (auto& v : h) v /= (double)b.N;
+    for (int j = 0; j < 78; ++j) {
+      double acc = 0.0;
+      for (unsigned k = 0; k < gx; ++k) acc += hp[(size_t)j * gx + k];
+      h[j] = acc / (double)b.N;
+    }
     if ((e = cudaMemcpyAsync(b.ref39.p, h.data(), 78 * sizeof(double), cudaMemcpyHostToDevice, s)) != cudaSuccess)
       return e;
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
