@@ -158,7 +158,9 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"D3Q27 boundary layer {NX}x{NY}x{NZ} (sampled {sx}x{sy}x{sz})", "alpha": "newton",
-                   "storage": "fp64"},
+                   "storage": "fp64",
+                   "arm": "the reference has no D3Q27 step to run: this arm times the FP64 CPU restatement of "
+                          "the method (the oracle port) on the host cores, a stated baseline"},
         "cpu_baseline": {"value": mlups, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{sx}x{sy}x{sz} sub-box of the workload, {args.steps} steps, OpenMP"},
         "e2e": {"value": mlups, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
