@@ -227,6 +227,14 @@ def _ptr(a: np.ndarray):
     return a.ctypes.data_as(_vp)
 
 
+def _at_least(a: np.ndarray, need: int, name: str) -> np.ndarray:
+    """a, if it holds at least need values: the library reads (or writes) exactly need
+    values through the pointer, so a shorter array would be overrun."""
+    if a.size < need:
+        raise ValueError(f"{name}: {a.size} values given, the call reads or writes {need}")
+    return a
+
+
 def make_d3q27_params(nu, tol_alpha=1e-12, tol_dH=1e-10, max_newton=30, alpha_mode=ELBM_ALPHA_NEWTON, check_dH=0,
                       record_alpha=0, outlet_type=(1,) * 8, fs_feq=None, inl_feq=None, outl_feq=None,
                       damp=0) -> D3Q27Params:
@@ -339,6 +347,22 @@ class Context:
         self._check(self.lib.elbm_level_register(self.h, lvl, lattice, storage, lo_hi.shape[0], _ptr(lo_hi), ngrow))
         self._boxes[lvl] = (lo_hi.copy(), ngrow, lattice)
 
+    def _fab_values(self, lvl, box, ncomp, ngrow=None):
+        """Values of an ncomp-component FAB of a registered box (ghost width ngrow,
+        default the level's), or None when the level or box is unknown here (the
+        library reports that)."""
+        if lvl not in self._boxes or not (0 <= box < self._boxes[lvl][0].shape[0]):
+            return None
+        lo_hi, g0, _ = self._boxes[lvl]
+        g = g0 if ngrow is None else ngrow
+        n = lo_hi[box, 3:] - lo_hi[box, :3] + 1 + 2 * g
+        return int(ncomp) * int(n[0]) * int(n[1]) * int(n[2])
+
+    def _fab(self, lvl, box, ncomp, arr, name, dtype=np.float64, ngrow=None):
+        a = np.ascontiguousarray(arr, dtype)
+        need = self._fab_values(lvl, box, ncomp, ngrow)
+        return a if need is None else _at_least(a, need, name)
+
     def box_shape(self, lvl, box=0, ghosts=True):
         lo_hi, ngrow, _ = self._boxes[lvl]
         g = ngrow if ghosts else 0
@@ -350,17 +374,23 @@ class Context:
         self._check(self.lib.elbm_set_d3q27_params(self.h, lvl, ct.byref(params)))
 
     def set_links(self, lvl, box, state: np.ndarray, ngrow_state=0):
-        st = np.ascontiguousarray(state, np.int32)
+        st = self._fab(lvl, box, 27, state, "state", np.int32, ngrow_state)
         self._check(self.lib.elbm_set_links(self.h, lvl, box, _ptr(st), ngrow_state))
 
     def upload(self, lvl, box, f: np.ndarray):
-        fa = np.ascontiguousarray(f, np.float64)
+        fa = self._fab(lvl, box, 27, f, "fout")
         self._check(self.lib.elbm_upload_level(self.h, lvl, box, _ptr(fa)))
 
     def download(self, lvl, box=0, out: np.ndarray | None = None) -> np.ndarray:
         q = self._boxes[lvl][2]
         if out is None:
             out = np.zeros((q,) + self.box_shape(lvl, box), np.float64)
+        elif out.dtype != np.float64 or not out.flags.c_contiguous:
+            raise ValueError("out: a C-contiguous float64 array is written in place")
+        else:
+            need = self._fab_values(lvl, box, q)
+            if need is not None:
+                _at_least(out, need, "out")
         self._check(self.lib.elbm_download_level(self.h, lvl, box, _ptr(out)))
         return out
 
@@ -381,11 +411,12 @@ class Context:
         self._check(self.lib.elbm_set_d3q39_params(self.h, lvl, ct.byref(params)))
 
     def set_links39(self, lvl, box, state: np.ndarray, bc: D3Q39Bc, ngrow_state=0):
-        st = np.ascontiguousarray(state, np.int32)
+        st = self._fab(lvl, box, 39, state, "state", np.int32, ngrow_state)
         self._check(self.lib.elbm_set_links39(self.h, lvl, box, _ptr(st), ngrow_state, ct.byref(bc)))
 
     def upload39(self, lvl, box, fout, gout, lm, w_vel):
-        arrs = [np.ascontiguousarray(a, np.float64) for a in (fout, gout, lm, w_vel)]
+        arrs = [self._fab(lvl, box, q, a, nm) for q, a, nm in ((39, fout, "fout"), (39, gout, "gout"), (13, lm, "lm"),
+                                                                (1, w_vel, "w_vel"))]
         self._check(self.lib.elbm_upload_level39(self.h, lvl, box, *map(_ptr, arrs)))
 
     def ggm_tags(self, lvl, box, variable, scheme, limit, pgs_sensitivity=None, pgs_reach=-1):
@@ -444,8 +475,8 @@ class Context:
     def init_level39(self, lvl, box, macro, lm_start):
         """Equilibrium initial state of a D3Q39 box from rho, u, v, w, T (5, nz, ny, nx) on the
         device; returns the number of nodes whose multiplier Newton hit the cap."""
-        m = np.ascontiguousarray(macro, np.float64)
-        l0 = np.ascontiguousarray(lm_start, np.float64)
+        m = self._fab(lvl, box, 5, macro, "macro")
+        l0 = _at_least(np.ascontiguousarray(lm_start, np.float64), 13, "lm_start")
         capped = ct.c_int64(0)
         self._check(self.lib.elbm_init_level39(self.h, lvl, box, _ptr(m), _ptr(l0), ct.byref(capped)))
         return capped.value
@@ -453,7 +484,7 @@ class Context:
     def d3q39_equilibrium(self, params, rho, u, v, w, T, lm_start):
         """(lm, fieq, gieq) of one state: the multiplier Newton from lm_start."""
         m = np.array([rho, u, v, w, T], np.float64)
-        lm = np.ascontiguousarray(lm_start, np.float64).copy()
+        lm = _at_least(np.ascontiguousarray(lm_start, np.float64).copy(), 13, "lm_start")
         f = np.zeros(39)
         g = np.zeros(39)
         self._check(self.lib.elbm_d3q39_equilibrium(self.h, ct.byref(params), _ptr(m), _ptr(lm), _ptr(f), _ptr(g)))
@@ -461,7 +492,7 @@ class Context:
 
     def upload_macro39(self, lvl, box, macro):
         """rho, u, v, w, T (5, nz, ny, nx) the next step starts from (after upload39)."""
-        m = np.ascontiguousarray(macro, np.float64)
+        m = self._fab(lvl, box, 5, macro, "macro")
         self._check(self.lib.elbm_upload_macro39(self.h, lvl, box, _ptr(m)))
 
     def download39(self, lvl, box=0):
@@ -516,31 +547,31 @@ class Context:
 
     def alpha_mlp_infer(self, weights, x):
         """Tensor-core network outputs for feature rows x (n, 27); returns (out, status)."""
-        w = np.ascontiguousarray(weights, np.float32)
-        xs = np.ascontiguousarray(x, np.float32)
+        w = _at_least(np.ascontiguousarray(weights, np.float32), MLP_PARAMS, "weights")
+        xs = np.ascontiguousarray(x, np.float32).reshape(-1, 27)
         out = np.zeros(xs.shape[0], np.float32)
         st = ct.c_uint32(0)
         self._check(self.lib.elbm_alpha_mlp_infer(self.h, _ptr(w), _ptr(xs), xs.shape[0], _ptr(out), ct.byref(st)))
         return out, st.value
 
     def alpha_mlp_grad(self, weights, records):
-        w = np.ascontiguousarray(weights, np.float32)
-        r = np.ascontiguousarray(records, np.float32)
+        w = _at_least(np.ascontiguousarray(weights, np.float32), MLP_PARAMS, "weights")
+        r = np.ascontiguousarray(records, np.float32).reshape(-1, MLP_RECORD)
         g = np.zeros(MLP_PARAMS, np.float32)
         loss = ct.c_double(0)
         self._check(self.lib.elbm_alpha_mlp_grad(self.h, _ptr(w), _ptr(r), r.shape[0], _ptr(g), ct.byref(loss)))
         return g, loss.value
 
     def alpha_mlp_train(self, records, weights, epochs=4, batch=4096, lr=1e-3, seed=0):
-        w = np.ascontiguousarray(weights, np.float32).copy()
-        r = np.ascontiguousarray(records, np.float32)
+        w = _at_least(np.ascontiguousarray(weights, np.float32).copy(), MLP_PARAMS, "weights")
+        r = np.ascontiguousarray(records, np.float32).reshape(-1, MLP_RECORD)
         hist = np.zeros(epochs)
         self._check(self.lib.elbm_alpha_mlp_train(self.h, _ptr(r), r.shape[0], epochs, batch, lr, seed, _ptr(w),
                                                   _ptr(hist)))
         return w, hist
 
     def set_alpha_mlp(self, lvl, weights):
-        w = np.ascontiguousarray(weights, np.float32)
+        w = _at_least(np.ascontiguousarray(weights, np.float32), MLP_PARAMS, "weights")
         self._check(self.lib.elbm_set_alpha_mlp(self.h, lvl, _ptr(w)))
 
     def sync(self):
