@@ -392,6 +392,39 @@ static void collide_node39(const o39_consts* k, const o39_lattice* Lp, const dou
   }
 }
 
+/* calculate_flow_variables.f95:192-228 for one node: rho, u, v, w and the
+ * temperature from f and g, then the six pressure-tensor targets of the
+ * multiplier solve.  The zz target reads the node's stored w (the previous
+ * step's, w_old: w_vel(a,b,c,1) at :225, while the new w sits in dummy_w);
+ * xz and yz read the new one.  out: rho, u, v, w, T, P_xx, P_yy, P_zz,
+ * P_xy, P_xz, P_yz. */
+static void flow_vars39(const o39_consts* k, const o39_lattice* L, const double* f, const double* g, double w_old,
+                        double* out) {
+  double rs = 0, us = 0, vs = 0, ws = 0, es = 0;
+  for (int i = 0; i < Q; ++i) {
+    rs = rs + f[i];
+    us = us + L->rcx[i] * f[i];
+    vs = vs + L->rcy[i] * f[i];
+    es = es + L->cmag[i] * f[i] + g[i];
+  }
+  const double rho = rs, u = us / rs, v = vs / rs;
+  for (int i = 0; i < Q; ++i) ws = ws + L->rcz[i] * f[i];
+  const double w = ws / rs;
+  const double vmag = u * u + v * v + w * w;
+  const double temp = (es - rho * vmag) / (2 * k->const_vol * rho);
+  out[0] = rho;
+  out[1] = u;
+  out[2] = v;
+  out[3] = w;
+  out[4] = temp;
+  out[5] = rho * (temp + u * u);
+  out[6] = rho * (temp + v * v);
+  out[7] = rho * (temp + w_old * w_old);
+  out[8] = rho * u * v;
+  out[9] = rho * u * w;
+  out[10] = rho * v * w;
+}
+
 static void collide39(const o39_consts* k, const o39_lattice* Lp, o39_level* s, const double* fi, const double* gi,
                       int step, const int32_t* state, int64_t* lm_iters_out, int64_t* capped_out, int64_t* not2_out) {
   const o39_lattice L = *Lp;
@@ -414,21 +447,10 @@ static void collide39(const o39_consts* k, const o39_lattice* Lp, o39_level* s, 
       if (wall)
         for (int r = 0; r < NLM; ++r) lm[r] = k->su_lm[r];
     }
-    double rs = 0, us = 0, vs = 0, ws = 0, es = 0;
-    for (int i = 0; i < Q; ++i) {
-      rs = rs + f[i];
-      us = us + L.rcx[i] * f[i];
-      vs = vs + L.rcy[i] * f[i];
-      es = es + L.cmag[i] * f[i] + g[i];
-    }
-    const double rho = rs, u = us / rs, v = vs / rs;
-    for (int i = 0; i < Q; ++i) ws = ws + L.rcz[i] * f[i];
-    const double w = ws / rs;
-    const double w_old = s->w_vel[n];
-    const double vmag = u * u + v * v + w * w;
-    const double temp = (es - rho * vmag) / (2 * k->const_vol * rho);
-    const double P[6] = {rho * (temp + u * u), rho * (temp + v * v), rho * (temp + w_old * w_old),
-                         rho * u * v,          rho * u * w,          rho * v * w};
+    double fv[11];
+    flow_vars39(k, &L, f, g, s->w_vel[n], fv);
+    const double rho = fv[0], u = fv[1], v = fv[2], w = fv[3], temp = fv[4];
+    const double* P = fv + 5;
     int it = o39_lagrange(&L, k->max_lm_iters, rho, u, v, w, temp, P, lm, fieq_a);
     if (it < 0) {
       capped++;
@@ -1383,6 +1405,17 @@ void o39_little_q_bar_api(const o39_consts* k, const double* gd, double u, doubl
   o39_lattice L;
   o39_lattice_init(&L, k->shifted, k->primary_flow_dir);
   little_q_bar(&L, k, gd, u, v, w, T, step, out);
+}
+
+/* rho, u, v, w, T and the six pressure-tensor targets of one node (flow_vars39),
+ * then the pressure press = rho (T + |u|^2 / 2) (calculate_flow_variables.f95:221):
+ * out has 12 values. */
+void o39_flow_vars_api(const o39_consts* k, const double* f, const double* g, double w_old, double* out) {
+  o39_lattice L;
+  o39_lattice_init(&L, k->shifted, k->primary_flow_dir);
+  flow_vars39(k, &L, f, g, w_old, out);
+  const double vmag = out[1] * out[1] + out[2] * out[2] + out[3] * out[3];
+  out[11] = out[0] * (out[4] + vmag / 2.0);
 }
 
 void o39_collide_node_api(const o39_consts* k, const double* f, const double* g, const double* lm, double rho,

@@ -272,12 +272,22 @@ def _pieces():
         L.o39_little_q_bar_api.argtypes = [ct.POINTER(O39Consts), vp, d, d, d, d, i, vp]
         L.o39_collide_node_api.restype = None
         L.o39_collide_node_api.argtypes = [ct.POINTER(O39Consts), vp, vp, vp, d, d, d, d, d, d, i, vp, vp]
+        L.o39_flow_vars_api.restype = None
+        L.o39_flow_vars_api.argtypes = [ct.POINTER(O39Consts), vp, vp, d, vp]
         L._o39_pieces = True
     return L
 
 
 def _a(x):
     return np.ascontiguousarray(x, np.float64)
+
+
+def flow_vars(k: O39Consts, f, g, w_old):
+    """rho, u, v, w, T, P_xx, P_yy, P_zz, P_xy, P_xz, P_yz, press of one node from
+    f and g (calculate_flow_variables.f95:192-228; P_zz reads the stored w_old)."""
+    out = np.zeros(12)
+    _pieces().o39_flow_vars_api(ct.byref(k), _p(_a(f)), _p(_a(g)), float(w_old), _p(out))
+    return out
 
 
 def fieq(shifted, pfd, rho, lm):

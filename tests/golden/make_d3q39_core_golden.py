@@ -8,6 +8,8 @@ Fortran statements (tests/golden/f95_subset.py interprets them in float64):
   LU update             looping/timestepping/lagrangian_multipliers/lu_decomp.f95 (both index quirks)
   closed-form alpha     looping/timestepping/calculate_alpha.f95
   heat-flux corrections looping/timestepping/component_subroutines/find_q_bar.f95, find_little_q_bar.f95
+  flow variables        looping/timestepping/calculate_flow_variables.f95:192-228 (moments of f and g,
+                        temperature, pressure and the six pressure-tensor targets; P_zz reads the stored w)
   collision of a node   looping/timestepping/collision.f95 (the body of the per-node loop)
   transport             utilities/modules/quick_calcs.f95, amr_processes.f95 beta_1/2_calculator,
                         epsilon_calculator
@@ -170,6 +172,33 @@ class Reference:
         self.interp.call("find_little_q_bar", [F.FArray(np.asarray(gd, np.float64)), u, v, w, T, ch, F.FInt(0)])
         return ch.a.tolist()
 
+    def flow_vars(self, root, f, g, w_old):
+        """calculate_flow_variables.f95's statements for one node (a = b = c = 1) from the
+        sums of f and g (:192) to the last pressure-tensor target (:228), just before the
+        multiplier solve; w_old is the node's stored w, which the P_zz target reads."""
+        lines = F.logical_lines((root / "looping/timestepping/calculate_flow_variables.f95").read_text())
+        i0 = next(k for k, (no, s) in enumerate(lines) if re.match(r"^rho_sum\s*=", s))
+        body, _ = F.parse_block(lines, i0, r"^if\s*\(timestep\(lvl\)")
+        local = {}
+        scope = self.interp.scope_for(local)
+        for no, s in lines[:i0]:
+            if re.match(r"^(real|integer)\b", s) and "intent" not in s:
+                self.interp.declare(s, local, scope, set())
+
+        def node_arr(vals):
+            a = np.asarray(vals, np.float64).reshape(1, 1, 1, -1)
+            return F.FArray(a.copy(), [1, 1, 1, 1])
+
+        nan = [float("nan")]
+        local.update(a=F.FInt(1), b=F.FInt(1), c=F.FInt(1), lvl=F.FInt(0), fi=node_arr(f), gi=node_arr(g),
+                     rho=node_arr(nan), u_vel=node_arr(nan), v_vel=node_arr(nan), w_vel=node_arr([w_old]),
+                     temp=node_arr(nan), press=node_arr(nan))
+        self.interp.run(body, local, scope)
+        one = lambda name: float(local[name].a.ravel()[0])  # noqa: E731
+        return [one("rho"), one("u_vel"), one("v_vel"), float(local["dummy_w"]), one("temp"),
+                float(local["new_pxx"]), float(local["new_pyy"]), float(local["new_pzz"]), float(local["new_pxy"]),
+                float(local["new_pxz"]), float(local["new_pyz"]), one("press")]
+
     def collide(self, root, f, g, lm, rho, u, v, w, T, alpha):
         """The body of collision.f95's per-node loop for one node (a = b = c = 1)."""
         lines = F.logical_lines((root / "looping/timestepping/collision.f95").read_text())
@@ -218,6 +247,7 @@ def case_consts(s39, shifted: bool):
 def main(root: pathlib.Path) -> None:
     s39 = _setup_module()
     rng = np.random.default_rng(20241204)
+    rng_w = np.random.default_rng(20241205)  # the stored (previous-step) w of the flow-variable cases
     out = {"lattices": {}}
     for shifted in (True, False):
         c = case_consts(s39, shifted)
@@ -243,6 +273,8 @@ def main(root: pathlib.Path) -> None:
             g = (lead * T * np.asarray(fe) * (1.0 + rng.uniform(-0.03, 0.03, 39))).tolist()
             fd = (np.asarray(fe) - np.asarray(f)).tolist()
             gd = (lead * T * np.asarray(fe) - np.asarray(g)).tolist()
+            w_old = float(w + rng_w.uniform(-0.05, 0.05))
+            flow = {"w_old": w_old, "out": ref.flow_vars(root, f, g, w_old)}
             steps = {}
             for step in (3, c.startup_timesteps + 7):
                 ref.set_step(step)
@@ -253,7 +285,7 @@ def main(root: pathlib.Path) -> None:
             lat["cases"].append({
                 "rho": rho, "u": u, "v": v, "w": w, "T": T, "P": P, "lm0": list(lm_start),
                 "lm": lm, "fieq": fe, "iterations": len(lus), "expo0": expo0, "lu": lus[:2],
-                "f": f, "g": g, "fd": fd, "gd": gd, "steps": steps})
+                "f": f, "g": g, "fd": fd, "gd": gd, "flow": flow, "steps": steps})
         out["lattices"]["shifted" if shifted else "unshifted"] = lat
     # lu_decomp on dense, diagonally dominant matrices, where both index quirks change the result at O(1)
     recs = []

@@ -6,7 +6,9 @@ unshifted one hand-expanded in calculate_lagrangian_mults.f95:341-695, the
 shifted one generic, :696-1097), the LU update with its two index quirks
 (lu_decomp.f95:105, :441), the whole multiplier solve, the closed-form alpha
 (calculate_alpha.f95), the heat-flux corrections (find_q_bar.f95,
-find_little_q_bar.f95) and the two-population collision of a node
+find_little_q_bar.f95), the flow variables of a node
+(calculate_flow_variables.f95:192-228, with the pressure-tensor target P_zz
+read from the stored w) and the two-population collision of a node
 (collision.f95), inside and after the start-up ramps.
 
 The oracle sums in its own order (generic loops where the reference spells
@@ -119,6 +121,21 @@ def test_alpha_heat_flux_and_collision(o39, name):
             assert ok, f"fout step {step}: {err}"
             ok, err = _close(go, ref["gout"])
             assert ok, f"gout step {step}: {err}"
+
+
+@pytest.mark.parametrize("name", LATTICES)
+def test_flow_variables(o39, name):
+    """rho, u, v, w, T, the six pressure-tensor targets and the pressure from f and g:
+    the same sums in the same order as the reference's statements, so bit for bit;
+    P_zz takes the stored w, the new w enters P_xz and P_yz."""
+    lat = DATA["lattices"][name]
+    k = _consts(o39, lat)
+    for c in lat["cases"]:
+        fl = c["flow"]
+        out = o39.flow_vars(k, c["f"], c["g"], fl["w_old"])
+        assert out.tolist() == fl["out"], (out.tolist(), fl["out"])
+        rho, u, v, w, T = out[:5]
+        assert out[7] == rho * (T + fl["w_old"] ** 2) and out[7] != rho * (T + w * w)
 
 
 def test_lu_update_dense_bitwise_with_quirks(o39):
