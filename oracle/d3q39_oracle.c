@@ -1407,6 +1407,15 @@ void o39_little_q_bar_api(const o39_consts* k, const double* gd, double u, doubl
   little_q_bar(&L, k, gd, u, v, w, T, step, out);
 }
 
+/* The fout repair of one box without periodic axes (damp39_links), in place;
+ * returns the number of negative populations met. */
+int64_t o39_damp_api(const o39_consts* k, double* fo, const int32_t* state, int nx, int ny, int nz, const int* lo,
+                     const int* hi, const double* fs_fieq) {
+  o39_lattice L;
+  o39_lattice_init(&L, k->shifted, k->primary_flow_dir);
+  return damp39_links(k, &L, fo, state, nx, ny, nz, 0, lo, hi, fs_fieq);
+}
+
 /* rho, u, v, w, T and the six pressure-tensor targets of one node (flow_vars39),
  * then the pressure press = rho (T + |u|^2 / 2) (calculate_flow_variables.f95:221):
  * out has 12 values. */

@@ -274,12 +274,26 @@ def _pieces():
         L.o39_collide_node_api.argtypes = [ct.POINTER(O39Consts), vp, vp, vp, d, d, d, d, d, d, i, vp, vp]
         L.o39_flow_vars_api.restype = None
         L.o39_flow_vars_api.argtypes = [ct.POINTER(O39Consts), vp, vp, d, vp]
+        L.o39_damp_api.restype = ct.c_int64
+        L.o39_damp_api.argtypes = [ct.POINTER(O39Consts), vp, vp, i, i, i, vp, vp, vp]
         L._o39_pieces = True
     return L
 
 
 def _a(x):
     return np.ascontiguousarray(x, np.float64)
+
+
+def damp(k: O39Consts, fout, state, lo, hi, fs_fieq):
+    """The fout repair of a box without periodic axes (damp_it.f95:64-177): fout and
+    state (39, nz, ny, nx); lo, hi the box in the level's index space; outside the box
+    fout is fs_fieq and the node type -666.  Returns (repaired fout, count)."""
+    f = _a(fout).copy()
+    st = np.ascontiguousarray(state, np.int32)
+    nz, ny, nx = f.shape[1:]
+    lo_a, hi_a = np.asarray(lo, np.int32), np.asarray(hi, np.int32)
+    n = _pieces().o39_damp_api(ct.byref(k), _p(f), _p(st), nx, ny, nz, _p(lo_a), _p(hi_a), _p(_a(fs_fieq)))
+    return f, int(n)
 
 
 def flow_vars(k: O39Consts, f, g, w_old):

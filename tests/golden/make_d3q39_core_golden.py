@@ -11,6 +11,8 @@ Fortran statements (tests/golden/f95_subset.py interprets them in float64):
   flow variables        looping/timestepping/calculate_flow_variables.f95:192-228 (moments of f and g,
                         temperature, pressure and the six pressure-tensor targets; P_zz reads the stored w)
   collision of a node   looping/timestepping/collision.f95 (the body of the per-node loop)
+  fout repair           looping/timestepping/damp_it.f95 (the reach and the in-place sweep of one box,
+                        written to d3q39_damp_golden.json)
   transport             utilities/modules/quick_calcs.f95, amr_processes.f95 beta_1/2_calculator,
                         epsilon_calculator
 
@@ -35,6 +37,7 @@ import numpy as np
 
 HERE = pathlib.Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE))
+import damp39_inputs  # noqa: E402
 import f95_subset as F  # noqa: E402
 
 PKG = HERE.parents[1] / "university-of-cincinnati-lattice-boltzmann-solver_gb300"
@@ -199,6 +202,51 @@ class Reference:
                 float(local["new_pxx"]), float(local["new_pyy"]), float(local["new_pzz"]), float(local["new_pxy"]),
                 float(local["new_pxz"]), float(local["new_pyz"]), one("press")]
 
+    def damp(self, root, fout, gout, state, fs_f, fs_g, lo, hi, ng=8):
+        """damp_it.f95 on one box at level 0: its reach, then its in-place sweep (direction
+        outermost) over the box and `reach` ghost layers.  fout, gout, state: (39, nz, ny, nx)
+        of the box; their FABs get ng ghost layers holding fs_f, fs_g (the freestream
+        equilibria, positive) and the node code -666 in every component (outside an
+        external-flow domain); fi and gi are positive everywhere, so the sweep's parts for
+        them leave them alone.  The
+        box's bounds, a derived type there, are passed as the arrays fux_lo, fux_hi.
+        nghosts_mid is 8: directions_and_weights.f95 sets it (:355-362) before it sets
+        shifted (:479), so the module's initial .false. picks the unshifted value."""
+        lines = [(no, s.replace("fux%lo(", "fux_lo(").replace("fux%hi(", "fux_hi("))
+                 for no, s in F.logical_lines((root / "looping/timestepping/damp_it.f95").read_text())]
+        k_reach = next(k for k, (no, s) in enumerate(lines) if s == "if (.not. shifted) then")
+        k_loop = next(k for k, (no, s) in enumerate(lines) if re.match(r"^do\s+i\s*=\s*1\s*,\s*dir$", s))
+        reach_if, _ = F.parse_stmt(lines, k_reach)
+        loop, _ = F.parse_stmt(lines, k_loop)
+        nz, ny, nx = fout.shape[1:]
+
+        def fab_of(pop, fs):
+            fab = np.empty((nx + 2 * ng, ny + 2 * ng, nz + 2 * ng, 39))
+            fab[...] = np.asarray(fs)[None, None, None, :]
+            fab[ng:ng + nx, ng:ng + ny, ng:ng + nz, :] = np.transpose(pop, (3, 2, 1, 0))
+            return fab
+
+        ffab, gfab = fab_of(fout, fs_f), fab_of(gout, fs_g)
+        sfab = np.full((nx + 2 * ng, ny + 2 * ng, nz + 2 * ng, 39), -666, np.int64)
+        sfab[ng:ng + nx, ng:ng + ny, ng:ng + nz, :] = np.transpose(state, (3, 2, 1, 0))
+        lb = [lo[0] - ng, lo[1] - ng, lo[2] - ng, 1]
+        local = {}
+        scope = self.interp.scope_for(local)
+        self.interp.declare("integer :: a,b,c,i,reach", local, scope, set())
+        self.g["nghosts_mid"] = F.FInt(8)
+        # the sweep also repairs fi (the post-streaming populations, which the next streaming
+        # overwrites except in slots no rule writes); positive here, so that part does nothing
+        local.update(lvl=F.FInt(0), fout=F.FArray(ffab, lb), gout=F.FArray(gfab, lb), state=F.FArray(sfab, lb),
+                     fi=F.FArray(np.ones_like(ffab), lb), gi=F.FArray(np.ones_like(gfab), lb),
+                     fux_lo=F.FArray(np.array(lo, np.int64), [1]), fux_hi=F.FArray(np.array(hi, np.int64), [1]))
+        self.interp.run([reach_if, loop], local, scope)
+
+        def valid(name):
+            out = local[name].a[ng:ng + nx, ng:ng + ny, ng:ng + nz, :]
+            return np.ascontiguousarray(np.transpose(out, (3, 2, 1, 0)))
+
+        return valid("fout"), valid("gout"), int(local["reach"])
+
     def collide(self, root, f, g, lm, rho, u, v, w, T, alpha):
         """The body of collision.f95's per-node loop for one node (a = b = c = 1)."""
         lines = F.logical_lines((root / "looping/timestepping/collision.f95").read_text())
@@ -249,6 +297,7 @@ def main(root: pathlib.Path) -> None:
     rng = np.random.default_rng(20241204)
     rng_w = np.random.default_rng(20241205)  # the stored (previous-step) w of the flow-variable cases
     out = {"lattices": {}}
+    damp_out = {}
     for shifted in (True, False):
         c = case_consts(s39, shifted)
         ref = Reference(root, c, shifted)
@@ -287,6 +336,20 @@ def main(root: pathlib.Path) -> None:
                 "lm": lm, "fieq": fe, "iterations": len(lus), "expo0": expo0, "lu": lus[:2],
                 "f": f, "g": g, "fd": fd, "gd": gd, "flow": flow, "steps": steps})
         out["lattices"]["shifted" if shifted else "unshifted"] = lat
+        # the fout repair of a box with link codes
+        def changes(before, after):
+            k = np.flatnonzero(after.ravel() != before.ravel())
+            return [[int(j), float(after.ravel()[j])] for j in k]
+
+        for name, (sh, *_) in damp39_inputs.CASES.items():
+            if sh != shifted:
+                continue
+            fo, go, st, fs_f, fs_g = damp39_inputs.case(name)
+            lo, hi = damp39_inputs.bounds(name)
+            rf, rg, reach = ref.damp(root, fo, go, st, fs_f, fs_g, lo, hi)
+            damp_out[name] = {"consts": lat["consts"], "lo": list(lo), "hi": list(hi), "reach": reach,
+                              "negative_f": int((fo < 0).sum()), "negative_g": int((go < 0).sum()),
+                              "changed_f": changes(fo, rf), "changed_g": changes(go, rg)}
     # lu_decomp on dense, diagonally dominant matrices, where both index quirks change the result at O(1)
     recs = []
     for k in range(4):
@@ -302,6 +365,7 @@ def main(root: pathlib.Path) -> None:
                      "lm_out": [lm[n] for n in LM_NAMES], "max_diff": md["v"]})
     out["lu_dense"] = recs
     (HERE / "d3q39_core_golden.json").write_text(json.dumps(out))
+    (HERE / "d3q39_damp_golden.json").write_text(json.dumps(damp_out))
 
 
 if __name__ == "__main__":

@@ -8,8 +8,9 @@ shifted one generic, :696-1097), the LU update with its two index quirks
 (calculate_alpha.f95), the heat-flux corrections (find_q_bar.f95,
 find_little_q_bar.f95), the flow variables of a node
 (calculate_flow_variables.f95:192-228, with the pressure-tensor target P_zz
-read from the stored w) and the two-population collision of a node
-(collision.f95), inside and after the start-up ramps.
+read from the stored w), the two-population collision of a node
+(collision.f95), inside and after the start-up ramps, and the negative-
+population repair's sweep over a box (damp_it.f95, d3q39_damp_golden.json).
 
 The oracle sums in its own order (generic loops where the reference spells
 terms out), so the bar is 1e-13 relative to each quantity's scale; the LU
@@ -23,6 +24,7 @@ import pytest
 GOLDEN = pathlib.Path(__file__).resolve().parent / "golden" / "d3q39_core_golden.json"
 DATA = json.loads(GOLDEN.read_text())
 LATTICES = sorted(DATA["lattices"])
+DAMP = json.loads((GOLDEN.parent / "d3q39_damp_golden.json").read_text())
 
 
 @pytest.fixture(scope="module")
@@ -136,6 +138,34 @@ def test_flow_variables(o39, name):
         assert out.tolist() == fl["out"], (out.tolist(), fl["out"])
         rho, u, v, w, T = out[:5]
         assert out[7] == rho * (T + fl["w_old"] ** 2) and out[7] != rho * (T + w * w)
+
+
+@pytest.mark.parametrize("name", sorted(DAMP))
+def test_damp_sweep(o39, name):
+    """damp_it.f95's in-place sweep over a box with link codes, fout and gout (the same
+    rules on each), against the reference's statements: every population bit for bit,
+    the repaired ones and the negative ones no rule changes (shifted lattice: link and
+    upstream node type both below -500 away from the band) alike."""
+    import sys
+
+    sys.path.insert(0, str(GOLDEN.parent))
+    import damp39_inputs as D
+
+    ref = DAMP[name]
+    k = o39.O39Consts()
+    for n, v in ref["consts"].items():
+        setattr(k, n, v)
+    fo, go, st, fs_f, fs_g = D.case(name)
+    lo, hi = D.bounds(name)
+    assert list(lo) == ref["lo"] and list(hi) == ref["hi"]
+    for pop, fs, key, nneg in ((fo, fs_f, "changed_f", "negative_f"), (go, fs_g, "changed_g", "negative_g")):
+        assert int((pop < 0).sum()) == ref[nneg]
+        out, count = o39.damp(k, pop, st, lo, hi, fs)
+        want = pop.ravel().copy()
+        for j, v in ref[key]:
+            want[j] = v
+        assert count == ref[nneg]
+        assert np.array_equal(out.ravel(), want), (key, int((out.ravel() != want).sum()))
 
 
 def test_lu_update_dense_bitwise_with_quirks(o39):
