@@ -260,11 +260,12 @@ typedef struct {
  * push nor collide; state >= 0 must be fluid (outside 200..298 and
  * 1000..50999); nodes outside the box on a non-periodic axis count as null
  * nodes (-666), as lbgrid/fluid_or_solid.f95:69-119 marks them for an
- * external flow.  With damp = 1 the fout part of damp_it.f95 follows every
- * step with the rules for boundary links (unshifted: interior links select
- * the neighbours; shifted: the band near the box's high faces and the node
- * types >= -500); its fi part, which only matters for slots no rule writes,
- * is not applied. */
+ * external flow.  With damp = 1 the fout and gout parts of damp_it.f95
+ * follow every step with the rules for boundary links (unshifted: interior
+ * links select the neighbours; shifted: the band near the box's high faces
+ * and the node types >= -500; outside the box each set's freestream
+ * equilibrium); its fi and gi parts, which only matter for slots no rule
+ * writes, are not applied. */
 int elbm_set_links39(elbm_ctx* ctx, int lvl, int box, const int32_t* state, int ngrow_state,
                      const elbm_d3q39_bc* bc);
 

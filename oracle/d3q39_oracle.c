@@ -505,11 +505,13 @@ int o39_step_periodic(const o39_consts* k, o39_level* s, int step, o39_stats* st
         }
   int64_t lm_iters = 0, capped = 0, not2 = 0;
   collide39(k, &L, s, fi, gi, step, NULL, &lm_iters, &capped, &not2);
-  /* damp_it.f95:64-177, fout part (damp39_links with every link interior; the box at the origin) */
+  /* damp_it.f95:64-177, fout and gout parts (damp39_links with every link interior; the box at the
+   * origin; the same rules on each population set) */
   int32_t* zst = (int32_t*)calloc((size_t)Q * N, sizeof(int32_t));
   if (!zst) return -100;
   const int lo[3] = {0, 0, 0}, hi[3] = {nx - 1, ny - 1, nz - 1};
-  const int64_t damped = damp39_links(k, &L, s->fout, zst, nx, ny, nz, 7, lo, hi, NULL);
+  const int64_t damped = damp39_links(k, &L, s->fout, zst, nx, ny, nz, 7, lo, hi, NULL) +
+                         damp39_links(k, &L, s->gout, zst, nx, ny, nz, 7, lo, hi, NULL);
   free(zst);
   st->nodes = N;
   st->lm_iters = lm_iters;
@@ -816,7 +818,8 @@ static int64_t nb39(int x, int y, int z, int nx, int ny, int nz, int periodic) {
   return idx3(x, y, z, nx, ny);
 }
 
-/* damp_it.f95:64-177, fout part, on a box with link codes, in the reference's
+/* damp_it.f95:64-177 on one population set (fout or gout: the reference applies
+ * the same rules to each) of a box with link codes, in the reference's
  * in-place sweep (direction outermost, then z, y, x).  lo, hi: the box in the
  * level's index space.  Unshifted lattice: the neighbours x +- c_i enter when
  * the links i / opp(i) of the node are interior (state >= 0).  Shifted: nodes
@@ -825,7 +828,7 @@ static int64_t nb39(int x, int y, int z, int nx, int ny, int nz, int periodic) {
  * included) take (fout(x + c_i) + |fout|) / 2 when link i is >= -500;
  * elsewhere the link and the node type of x - c_i (>= -500) select the
  * neighbours, and a population with neither keeps its value.  Outside the box
- * on a non-periodic axis a node type is -666 and fout the freestream
+ * on a non-periodic axis a node type is -666 and the population the freestream
  * equilibrium (the initial value of the nodes outside an external-flow domain,
  * multilevel_initialization.f90:185-268, which never collide).  nghosts_mid is
  * 8 for D3Q39: directions_and_weights.f95:355-362 sets it before the same
@@ -1360,7 +1363,10 @@ int o39_step_links_damp(const o39_consts* k, o39_level* s, int step, o39_stats* 
   if (rc) return rc;
   o39_lattice L;
   o39_lattice_init(&L, k->shifted, k->primary_flow_dir);
-  st->damped = damp39_links(k, &L, s->fout, state, s->nx, s->ny, s->nz, periodic, lo, hi, bc->fs_fieq);
+  /* damp_it.f95:64-177: the fout part, then the gout part (the same rules; outside the box g's
+   * freestream equilibrium) */
+  st->damped = damp39_links(k, &L, s->fout, state, s->nx, s->ny, s->nz, periodic, lo, hi, bc->fs_fieq) +
+               damp39_links(k, &L, s->gout, state, s->nx, s->ny, s->nz, periodic, lo, hi, bc->fs_gieq);
   return 0;
 }
 

@@ -350,7 +350,7 @@ def test_d3q39_initial_state_on_device(pkg, o39, built_lib):
 
 @pytest.mark.parametrize("shifted", [0, 1])
 def test_d3q39_repair_with_link_codes(pkg, o39, built_lib, shifted):
-    """The fout part of damp_it.f95 after the step on a box with link codes (inlet, outlet,
+    """The fout and gout parts of damp_it.f95 after the step on a box with link codes (inlet, outlet,
     bounce-back floor, freestream top, periodic span), past the start-up ramps: a few
     populations are inflated so that the over-relaxed collision drives isolated neighbours
     negative; GPU against the oracle's in-place sweep, 1e-12 relative."""

@@ -1103,12 +1103,13 @@ void launch_d3q39_fp64(const Step39Args& a, cudaStream_t s) {
   }
 }
 
-// damp_it.f95:64-177, fout part, on a box with link codes (see the oracle's
+// damp_it.f95:64-177 on one population set (fout, or gout: the reference
+// applies the same rules to each) of a box with link codes (see the oracle's
 // damp39_links for the rules).  dmask per node: bit i link i interior
 // (unshifted: state >= 0; shifted: >= -500), bit 63 node type >= -500.
-// Outside the box on a non-periodic axis a node type is -666 and fout the
-// freestream equilibrium eq[i] (the initial value of the nodes outside an
-// external-flow domain).  The reference repairs in place, direction by
+// Outside the box on a non-periodic axis a node type is -666 and the
+// population the set's freestream equilibrium eq[i] (the initial value of the
+// nodes outside an external-flow domain).  The reference repairs in place, direction by
 // direction in z, y, x order, so a neighbour that comes earlier in that order
 // and is itself negative is read repaired: damp39_value follows such chains
 // (up to kDampChain links; longer chains read the unrepaired value).
