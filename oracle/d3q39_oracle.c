@@ -964,6 +964,51 @@ void o39_ibb39_unshifted_terms(int d, const double* D, double u, double v, doubl
   *gpoly = ibb39_poly(ibb39_g_terms, ibb39_g_off[d], ibb39_g_off[d + 1], D, u, v, w, T, b1, b2, cv);
 }
 
+/* target_finder.f95:23-135 for one node.  code: the node's 39 link codes;
+ * up, vp, wp, Tp: u, v, w, T at x + c_j (the caller's u_pass ... temp_pass;
+ * only the entries the rules read are used); fi: the node's post-streaming
+ * slots as the push loop has left them; fs_temp: the freestream temperature
+ * (`temperature`).  out: rho, u, v, w, T targets.  Unshifted lattice: per
+ * wall link j the node across (u_pass(opp(j))) when link opp(j) is fluid,
+ * else the node itself (u_pass(1)) with the wall at fs_temp; shifted: u_pass(j)
+ * when link erp(j) is -666, else u_pass(5).  rho sums the slots j, or erp(j)
+ * (opp(j) on the unshifted lattice) where link opp(j) is a wall. */
+static void target_finder39(const o39_consts* k, const o39_lattice* L, const int32_t* code, const double* up,
+                            const double* vp, const double* wp, const double* Tp, const double* fi, double fs_temp,
+                            double* out) {
+  int count = 0;
+  double r_ = 0, u_ = 0, v_ = 0, w_ = 0, T_ = 0;
+  for (int j = 0; j < Q; ++j) {
+    const int32_t cj = code[j];
+    if (cj <= -1001 && !k->shifted) {
+      const double d = fabs(((double)cj + 1001.0) / 1.0e9);
+      count++;
+      const int o = L->opp[j];
+      const int fluid = code[o] >= 0;
+      const int m = fluid ? o : 0;
+      u_ = u_ + (d * up[m]) / (d + 1.0);
+      v_ = v_ + (d * vp[m]) / (d + 1.0);
+      w_ = w_ + (d * wp[m]) / (d + 1.0);
+      T_ = T_ + (d * Tp[m] + (fluid ? Tp[m] : fs_temp)) / (d + 1.0);
+    } else if (cj <= -1001) {
+      const double d = fabs(((double)cj + 1001.0) / 1.0e9);
+      count++;
+      const int src = code[erp39(j)] == -666 ? j : 4;
+      u_ = u_ + (d * up[src]) / (d + 1.0);
+      v_ = v_ + (d * vp[src]) / (d + 1.0);
+      w_ = w_ + (d * wp[src]) / (d + 1.0);
+      T_ = T_ + (d * Tp[src] + Tp[src]) / (d + 1.0);
+    }
+    if (code[L->opp[j]] < -1000) r_ = r_ + fi[erp39(j)];
+    else r_ = r_ + fi[j];
+  }
+  out[0] = r_;
+  out[1] = u_ / count;
+  out[2] = v_ / count;
+  out[3] = w_ / count;
+  out[4] = T_ / count;
+}
+
 /* Wall link i of fluid node n at (x, y, z) during the push loop: the value
  * shifted_ibb writes into fi(x, i) and gi(x, i).  fi, gi are the post-streaming
  * arrays as the loop has left them so far (target_finder reads them).  Node
@@ -982,43 +1027,31 @@ static int ibb_link39(const o39_consts* k, const o39_lattice* L, const o39_level
   double rho_t, ut, vt, wt, Tt, lm_t[NLM];
   if (adjacent) {
     if (first) {
-      /* target_finder.f95:89-140 */
-      int count = 0;
-      double r_ = 0, u_ = 0, v_ = 0, w_ = 0, T_ = 0;
+      /* target_finder.f95:23-135 on what streaming.f95:773-778 passes it: the fields at x + c_j
+       * (gathered here only for the entries the rules read; a read that leaves the box fails) */
+      int32_t code[Q];
+      double up[Q], vp[Q], wp[Q], Tp[Q], fin[Q], tg[5];
       for (int j = 0; j < Q; ++j) {
-        const int32_t cj = CODE39(j);
-        if (cj <= -1001 && !k->shifted) {
-          /* target_finder.f95:36-58: the node across (x + c_opp(j)) when that link is fluid, else the node itself
-           * with the wall at the freestream temperature */
-          const double d = fabs(((double)cj + 1001.0) / 1.0e9);
-          count++;
-          const int o = L->opp[j];
-          const int fluid = CODE39(o) >= 0;
-          const int64_t m = fluid ? nb39(x + L->cx[o], y + L->cy[o], z + L->cz[o], nx, ny, nz, periodic) : n;
-          if (m < 0) return -2;
-          u_ = u_ + (d * s->u[m]) / (d + 1.0);
-          v_ = v_ + (d * s->v[m]) / (d + 1.0);
-          w_ = w_ + (d * s->w_vel[m]) / (d + 1.0);
-          T_ = T_ + (d * s->temp[m] + (fluid ? s->temp[m] : bc->fs_temp)) / (d + 1.0);
-        } else if (cj <= -1001) {
-          const double d = fabs(((double)cj + 1001.0) / 1.0e9);
-          count++;
-          const int src = CODE39(erp39(j)) == -666 ? j : 4;
-          const int64_t m = nb39(x + L->cx[src], y + L->cy[src], z + L->cz[src], nx, ny, nz, periodic);
-          if (m < 0) return -2;
-          u_ = u_ + (d * s->u[m]) / (d + 1.0);
-          v_ = v_ + (d * s->v[m]) / (d + 1.0);
-          w_ = w_ + (d * s->w_vel[m]) / (d + 1.0);
-          T_ = T_ + (d * s->temp[m] + s->temp[m]) / (d + 1.0);
-        }
-        if (CODE39(L->opp[j]) < -1000) r_ = r_ + fi[(int64_t)erp39(j) * N + n];
-        else r_ = r_ + fi[(int64_t)j * N + n];
+        code[j] = CODE39(j);
+        fin[j] = fi[(int64_t)j * N + n];
+        up[j] = vp[j] = wp[j] = Tp[j] = NAN;
       }
-      rho_t = r_;
-      ut = u_ / count;
-      vt = v_ / count;
-      wt = w_ / count;
-      Tt = T_ / count;
+      for (int j = 0; j < Q; ++j) {
+        if (code[j] > -1001) continue;
+        const int p = !k->shifted ? (code[L->opp[j]] >= 0 ? L->opp[j] : 0) : (code[erp39(j)] == -666 ? j : 4);
+        const int64_t m = nb39(x + L->cx[p], y + L->cy[p], z + L->cz[p], nx, ny, nz, periodic);
+        if (m < 0) return -2;
+        up[p] = s->u[m];
+        vp[p] = s->v[m];
+        wp[p] = s->w_vel[m];
+        Tp[p] = s->temp[m];
+      }
+      target_finder39(k, L, code, up, vp, wp, Tp, fin, bc->fs_temp, tg);
+      rho_t = tg[0];
+      ut = tg[1];
+      vt = tg[2];
+      wt = tg[3];
+      Tt = tg[4];
       /* streaming.f95:788-850: warm start from the node's multipliers (the start-up set for timestep <= 4) */
       for (int r = 0; r < NLM; ++r) lm_t[r] = (step <= 4 && k->shifted) ? k->su_lm[r] : s->lm[(int64_t)r * N + n];
       const double P[6] = {rho_t * Tt + rho_t * (ut * ut), rho_t * Tt + rho_t * (vt * vt),
@@ -1411,6 +1444,14 @@ void o39_little_q_bar_api(const o39_consts* k, const double* gd, double u, doubl
   o39_lattice L;
   o39_lattice_init(&L, k->shifted, k->primary_flow_dir);
   little_q_bar(&L, k, gd, u, v, w, T, step, out);
+}
+
+/* target_finder39 on given inputs (39 codes, fields at x + c_j, slots); out: 5 targets. */
+void o39_target_finder_api(const o39_consts* k, const int32_t* code, const double* up, const double* vp,
+                           const double* wp, const double* Tp, const double* fi, double fs_temp, double* out) {
+  o39_lattice L;
+  o39_lattice_init(&L, k->shifted, k->primary_flow_dir);
+  target_finder39(k, &L, code, up, vp, wp, Tp, fi, fs_temp, out);
 }
 
 /* The fout repair of one box without periodic axes (damp39_links), in place;

@@ -274,6 +274,8 @@ def _pieces():
         L.o39_collide_node_api.argtypes = [ct.POINTER(O39Consts), vp, vp, vp, d, d, d, d, d, d, i, vp, vp]
         L.o39_flow_vars_api.restype = None
         L.o39_flow_vars_api.argtypes = [ct.POINTER(O39Consts), vp, vp, d, vp]
+        L.o39_target_finder_api.restype = None
+        L.o39_target_finder_api.argtypes = [ct.POINTER(O39Consts), vp, vp, vp, vp, vp, vp, d, vp]
         L.o39_damp_api.restype = ct.c_int64
         L.o39_damp_api.argtypes = [ct.POINTER(O39Consts), vp, vp, i, i, i, vp, vp, vp]
         L._o39_pieces = True
@@ -282,6 +284,16 @@ def _pieces():
 
 def _a(x):
     return np.ascontiguousarray(x, np.float64)
+
+
+def target_finder(k: O39Consts, code, u, v, w, T, fi, fs_temp):
+    """rho, u, v, w, T targets of a wall node (target_finder.f95): its 39 link codes, the
+    fields at x + c_j, its post-streaming slots and the freestream temperature."""
+    out = np.zeros(5)
+    cd = np.ascontiguousarray(code, np.int32)
+    _pieces().o39_target_finder_api(ct.byref(k), _p(cd), _p(_a(u)), _p(_a(v)), _p(_a(w)), _p(_a(T)), _p(_a(fi)),
+                                    float(fs_temp), _p(out))
+    return out
 
 
 def damp(k: O39Consts, fout, state, lo, hi, fs_fieq):

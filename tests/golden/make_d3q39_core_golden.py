@@ -11,6 +11,7 @@ Fortran statements (tests/golden/f95_subset.py interprets them in float64):
   flow variables        looping/timestepping/calculate_flow_variables.f95:192-228 (moments of f and g,
                         temperature, pressure and the six pressure-tensor targets; P_zz reads the stored w)
   collision of a node   looping/timestepping/collision.f95 (the body of the per-node loop)
+  wall targets          boundary_conditions/interpolative_bc/target_finder.f95 (both lattices)
   fout repair           looping/timestepping/damp_it.f95 (the reach and the in-place sweep of one box,
                         written to d3q39_damp_golden.json)
   transport             utilities/modules/quick_calcs.f95, amr_processes.f95 beta_1/2_calculator,
@@ -91,10 +92,12 @@ class Reference:
                  R / "looping/timestepping/component_subroutines/find_q_bar.f95",
                  R / "looping/timestepping/component_subroutines/find_little_q_bar.f95",
                  R / "utilities/modules/quick_calcs.f95",
-                 R / "general/background_calcs/directions_and_weights.f95"]
+                 R / "general/background_calcs/directions_and_weights.f95",
+                 R / "boundary_conditions/interpolative_bc/target_finder.f95"]
         wanted = {"fieq_comp_39", "fieq_comp_39_shifted", "beta_1_calculator", "beta_2_calculator",
                   "epsilon_calculator", "calculate_lagrangian_mults", "lu_decomp", "calculate_alpha", "find_q_bar",
-                  "find_little_q_bar", "quick_sutherlands", "quick_therm_cond", "directions_and_weights"}
+                  "find_little_q_bar", "quick_sutherlands", "quick_therm_cond", "directions_and_weights",
+                  "target_finder"}
         self.procs = {}
         for p in files:
             self.procs.update(F.parse_units(F.logical_lines(p.read_text()), only=wanted))
@@ -104,6 +107,7 @@ class Reference:
         g = {"dp": F.FInt(8), "sp": F.FInt(4)}
         _module_values(R / "general/modules/precise.f95", g)
         _module_values(R / "general/modules/constants.f95", g)
+        _module_values(R / "linking/modules/linkwise.f95", g)  # erp, the unshifted opposites
         # case values of the modules (constants, timing, amr_info_holder, grid_data, namelists)
         g.update(dimensions=F.FInt(3), primary_flow_dir=F.FInt(c.primary_flow_dir), gama=c.gama, t_ref=c.t_ref,
                  rho_ref=c.rho_ref, p_ref=c.p_ref, mu_ref=c.mu_ref, kappa_ref=c.kappa_ref, gas_const_r=c.gas_const_R,
@@ -112,6 +116,7 @@ class Reference:
                  beta_2_scaling=c.beta_2_scaling, startup_timesteps=F.FInt(c.startup_timesteps),
                  self=F.FInt(0), amr_max_lvl=F.FInt(0), mach=(1.5 if shifted else 0.5), use_shifted=bool(shifted),
                  shifted=bool(shifted), turbulent=True,
+                 temperature=c.temperature,
                  dt=F.FArray(np.array([c.dt]), [0]), elbm_epsilon=F.FArray(np.array([c.elbm_epsilon]), [0]),
                  timestep=F.FArray(np.array([0], np.int64), [0]))
         g["__int_arrays"] = _int_arrays(R / "linking/modules/linkwise.f95") | {"opp"}
@@ -201,6 +206,16 @@ class Reference:
         return [one("rho"), one("u_vel"), one("v_vel"), float(local["dummy_w"]), one("temp"),
                 float(local["new_pxx"]), float(local["new_pyy"]), float(local["new_pzz"]), float(local["new_pxy"]),
                 float(local["new_pxz"]), float(local["new_pyz"]), one("press")]
+
+    def targets(self, code, up, vp, wp, Tp, fi):
+        """target_finder.f95 for one node (a = b = c = 1): its 39 link codes, u, v, w, T at
+        x + c_j, and its post-streaming slots; returns rho, u, v, w, T targets."""
+        out = {n: float("nan") for n in ("r", "u", "v", "w", "t")}
+        node = lambda vals, dt=np.float64: F.FArray(np.asarray(vals, dt).reshape(1, 1, 1, 39), [1, 1, 1, 1])  # noqa: E731
+        vec = lambda vals: F.FArray(np.asarray(vals, np.float64).copy())  # noqa: E731
+        self.interp.call("target_finder", [node(code, np.int64), vec(up), vec(vp), vec(wp), vec(Tp), node(fi)] +
+                         [F.Ref(out, n) for n in ("r", "u", "v", "w", "t")] + [F.FInt(1), F.FInt(1), F.FInt(1)])
+        return [out[n] for n in ("r", "u", "v", "w", "t")]
 
     def damp(self, root, fout, gout, state, fs_f, fs_g, lo, hi, ng=8):
         """damp_it.f95 on one box at level 0: its reach, then its in-place sweep (direction
@@ -304,6 +319,22 @@ def main(root: pathlib.Path) -> None:
         lat = {"consts": {k: getattr(c, k) for k in CONST_FIELDS}, "su_lm": list(c.su_lm),
                "tables": ref.tables(), "cases": []}
         lat["consts"]["shifted"] = int(shifted)
+        # target_finder on seeded nodes: wall links (packed distances) among interior, null and
+        # boundary links, the fields at x + c_j and the node's slots
+        rng_t = np.random.RandomState(4242 + int(shifted))
+        tcases = []
+        for _ in range(8):
+            code = rng_t.choice([0, 0, 3, -10, -666, -1000], 39).astype(np.int64)
+            walls = rng_t.random_sample(39) < 0.3
+            walls[rng_t.randint(1, 39)] = True
+            code[walls] = -1001 - np.floor(rng_t.uniform(0.02, 0.98, int(walls.sum())) * 1e9).astype(np.int64)
+            up, vp, wp = (c.mach * rng_t.uniform(-1.2, 1.2, 39) for _ in range(3))
+            Tp = c.temperature * rng_t.uniform(0.8, 1.2, 39)
+            fi_n = rng_t.uniform(0.001, 0.2, 39)
+            tcases.append({"code": code.tolist(), "u": up.tolist(), "v": vp.tolist(), "w": wp.tolist(), "T": Tp.tolist(),
+                           "fi": fi_n.tolist(), "fs_temp": c.temperature,
+                           "out": ref.targets(code, up, vp, wp, Tp, fi_n)})
+        lat["targets"] = tcases
         lm_start = s39.freestream_start_lm(c)
         for k in range(3):
             rho = float(rng.uniform(0.92, 1.08))

@@ -8,7 +8,8 @@ shifted one generic, :696-1097), the LU update with its two index quirks
 (calculate_alpha.f95), the heat-flux corrections (find_q_bar.f95,
 find_little_q_bar.f95), the flow variables of a node
 (calculate_flow_variables.f95:192-228, with the pressure-tensor target P_zz
-read from the stored w), the two-population collision of a node
+read from the stored w), the wall targets (target_finder.f95), the
+two-population collision of a node
 (collision.f95), inside and after the start-up ramps, and the negative-
 population repair's sweep over a box (damp_it.f95, d3q39_damp_golden.json).
 
@@ -138,6 +139,19 @@ def test_flow_variables(o39, name):
         assert out.tolist() == fl["out"], (out.tolist(), fl["out"])
         rho, u, v, w, T = out[:5]
         assert out[7] == rho * (T + fl["w_old"] ** 2) and out[7] != rho * (T + w * w)
+
+
+@pytest.mark.parametrize("name", LATTICES)
+def test_wall_targets(o39, name):
+    """target_finder.f95's rho, u, v, w, T targets of a wall node from its link codes,
+    the fields at x + c_j and its slots (unshifted: the node across a fluid opposite
+    link, else the node itself at the freestream temperature; shifted: x + c_j beside
+    a null link, else direction 5), bit for bit."""
+    lat = DATA["lattices"][name]
+    k = _consts(o39, lat)
+    for c in lat["targets"]:
+        out = o39.target_finder(k, c["code"], c["u"], c["v"], c["w"], c["T"], c["fi"], c["fs_temp"])
+        assert out.tolist() == c["out"], (out.tolist(), c["out"])
 
 
 @pytest.mark.parametrize("name", sorted(DAMP))
