@@ -752,8 +752,12 @@ static void shifted_ibb39(const o39_consts* k, const o39_lattice* L, int i, int 
  * component is -11 the component reflects (displacement 0 for speed-1
  * diagonals, -c/2 for speed-2 ones); else, for speed-2 diagonals, if the
  * speed-2 link along it is -11 it reflects with displacement +c/2; else it
- * keeps its value and displacement c.  Axis directions reflect whatever the
- * other links are (displacement 0, c/2, -2c/3 for speeds 1, 2, 3).  Two
+ * keeps its value and displacement c.  Axis directions always reflect; the
+ * displacement is 0 for speed 1; for speed 2, -c/2 when the unit link along
+ * the axis is -11, else +c/2; for speed 3, +2c/3 when the unit and the speed-2
+ * links along it are both -11, 0 when only the speed-2 one is, else -2c/3.
+ * On the shifted lattice the routine then adds the shift (the primary flow
+ * direction's unit vector) to the displacement; the caller does that.  Two
  * entries of the reference's table differ from this rule and are kept:
  * direction 9 (1-based) with x and y (x and z) reflecting goes to 12 (11),
  * and direction 27 with only y reflecting is displaced by the opposite y.
@@ -771,7 +775,12 @@ int o39_inviscid(int i, const int32_t* code, int* j, int* d) {
   if (nz == 1) {
     for (int a = 0; a < 3; ++a) {
       r[a] = -c[a];
-      d[a] = sp == 1 ? 0 : sp == 2 ? c[a] / 2 : -(2 * c[a]) / 3;
+      d[a] = 0;
+      if (c[a] == 0) continue;
+      const int neg = c[a] < 0;
+      const int unit = code[1 + a + 3 * neg] == -11, two = code[15 + a + 3 * neg] == -11;
+      if (sp == 2) d[a] = unit ? -c[a] / 2 : c[a] / 2;
+      else if (sp == 3) d[a] = (unit && two) ? (2 * c[a]) / 3 : two ? 0 : -(2 * c[a]) / 3;
     }
   } else {
     int any = 0;
@@ -1194,6 +1203,11 @@ int o39_step_links(const o39_consts* k, o39_level* s, int step, o39_stats* st, c
             int j = 0, d[3];
             /* no branch of inviscid_edge.f95 applies: the reference writes nothing for this link */
             if (!o39_inviscid(i, codes, &j, d)) continue;
+            if (k->shifted) {
+              /* inviscid_edge.f95:1230-1243: the shifted lattice adds the shift to the displacement */
+              const int pf = k->primary_flow_dir, sgn = pf <= 3 ? 1 : -1;
+              d[(pf - 1) % 3] += sgn;
+            }
             /* a reflection that lands outside the box leaves it, like a push across a face */
             const int64_t r2 = nb39(x + d[0], y + d[1], z + d[2], nx, ny, nz, periodic);
             if (r2 >= 0) {

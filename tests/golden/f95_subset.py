@@ -740,10 +740,11 @@ class Interp:
         dummies = {pyname(a) for a in p.args}
         present = set()
         refs = {}
+        entry = {}
         for a, v in zip(p.args, actuals):
             if isinstance(v, Ref):
                 refs[pyname(a)] = v
-                local[pyname(a)] = v.get()
+                local[pyname(a)] = entry[pyname(a)] = v.get()
             else:
                 local[pyname(a)] = v
             present.add(pyname(a))
@@ -763,8 +764,14 @@ class Interp:
             self.run(p.body, local, scope)
         except _Return:
             pass
+        # copy-out of the arguments the procedure assigned: an argument passed by reference that
+        # the procedure leaves alone does not write (two dummies may name one actual element, as
+        # outlet_bc's fout_outl and fout_opp do on the shifted lattice, where opp(i) = i)
         for a, r in refs.items():
-            r.set(local[a])
+            new, old = local[a], entry[a]
+            if new is old or (not isinstance(new, FArray) and type(new) is type(old) and new == old):
+                continue
+            r.set(new)
         if p.kind == "function":
             return local[pyname(p.result)]
         return None

@@ -12,6 +12,10 @@ Fortran statements (tests/golden/f95_subset.py interprets them in float64):
                         temperature, pressure and the six pressure-tensor targets; P_zz reads the stored w)
   collision of a node   looping/timestepping/collision.f95 (the body of the per-node loop)
   wall targets          boundary_conditions/interpolative_bc/target_finder.f95 (both lattices)
+  push loop             looping/timestepping/streaming.f95:263-1161 with the boundary routines it calls
+                        (bc_switchboard, bounceback, inlet_bc, outlet_bc and its variants,
+                        freestream_edge_bc, inviscid_edge) on boxes of push39_inputs: digests of the
+                        post-streaming fi, gi of the fluid nodes, written to d3q39_push_golden.json
   fout repair           looping/timestepping/damp_it.f95 (the reach and the in-place sweep of one box,
                         written to d3q39_damp_golden.json)
   transport             utilities/modules/quick_calcs.f95, amr_processes.f95 beta_1/2_calculator,
@@ -39,6 +43,7 @@ import numpy as np
 HERE = pathlib.Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE))
 import damp39_inputs  # noqa: E402
+import push39_inputs  # noqa: E402
 import f95_subset as F  # noqa: E402
 
 PKG = HERE.parents[1] / "university-of-cincinnati-lattice-boltzmann-solver_gb300"
@@ -93,11 +98,18 @@ class Reference:
                  R / "looping/timestepping/component_subroutines/find_little_q_bar.f95",
                  R / "utilities/modules/quick_calcs.f95",
                  R / "general/background_calcs/directions_and_weights.f95",
-                 R / "boundary_conditions/interpolative_bc/target_finder.f95"]
+                 R / "boundary_conditions/interpolative_bc/target_finder.f95"] + \
+                [R / "boundary_conditions" / f for f in ("bc_switchboard.f95", "bounceback.f95", "inlet_bc.f95",
+                                                          "outlet_bc.f95", "rho_v_bc.f95", "press_temp_bc.f95",
+                                                          "v_temp_bc.f95", "freestream_bc.f95", "null_bc.f95",
+                                                          "freestream_edge_bc.f95", "pure_outflow_bc.f95",
+                                                          "inviscid_edge.f95")]
         wanted = {"fieq_comp_39", "fieq_comp_39_shifted", "beta_1_calculator", "beta_2_calculator",
                   "epsilon_calculator", "calculate_lagrangian_mults", "lu_decomp", "calculate_alpha", "find_q_bar",
                   "find_little_q_bar", "quick_sutherlands", "quick_therm_cond", "directions_and_weights",
-                  "target_finder"}
+                  "target_finder", "bc_switchboard", "bounceback", "inlet_bc", "outlet_bc", "rho_v_bc",
+                  "press_temp_bc", "v_temp_bc", "freestream_bc", "null_bc", "freestream_edge_bc", "pure_outflow_bc",
+                  "inviscid_edge"}
         self.procs = {}
         for p in files:
             self.procs.update(F.parse_units(F.logical_lines(p.read_text()), only=wanted))
@@ -206,6 +218,76 @@ class Reference:
         return [one("rho"), one("u_vel"), one("v_vel"), float(local["dummy_w"]), one("temp"),
                 float(local["new_pxx"]), float(local["new_pyy"]), float(local["new_pzz"]), float(local["new_pxy"]),
                 float(local["new_pxz"]), float(local["new_pyz"]), one("press")]
+
+    def push(self, root, cs, G=8):
+        """streaming.f95's push loop (:263-1161) over one box at level 0, for a case of
+        push39_inputs (boundary links, no interpolated wall links).  The box's FABs get G
+        ghost layers: on a periodic axis the periodic images (as fill_boundary leaves
+        them), on the others nodes whose every code is -666 (outside an external-flow
+        domain).  Two statements are rewritten for the interpreter, neither changing what
+        runs: `go to 1000` (the shifted lattice's rest-direction push onto a fluid node)
+        becomes the two assignments labelled 1000 followed by `cycle` (after the SELECT
+        nothing but a diagnostic print remains in the loop body), and the box bounds
+        wax%lo, wax%hi become the arrays wax_lo, wax_hi.  fi, gi start from the previous
+        step's post-streaming values (what slots no rule writes keep).  Returns the
+        post-streaming fi, gi of the box, (39, nz, ny, nx)."""
+        text = (root / "looping/timestepping/streaming.f95").read_text()
+        label_line = next(no for no, s in enumerate(text.splitlines(), 1) if re.match(r"^\s*1000\s+fi\(", s))
+        raw = F.logical_lines(text)  # (statement labels are dropped there)
+        k_goto = next(k for k, (no, s) in enumerate(raw) if re.match(r"^go\s*to\s+1000$", s))
+        k_lab = next(k for k, (no, s) in enumerate(raw) if no == label_line)
+        lab_f, lab_g = raw[k_lab][1], raw[k_lab + 1][1]
+        assert lab_f.startswith("fi(a+cx(i)") and lab_g.startswith("gi(a+cx(i)"), (lab_f, lab_g)
+        lines = []
+        for k, (no, s) in enumerate(raw):
+            s = s.replace("wax%lo(", "wax_lo(").replace("wax%hi(", "wax_hi(")
+            lines += [(no, lab_f), (no, lab_g), (no, "cycle")] if k == k_goto else [(no, s)]
+        k_reach = next(k for k, (no, s) in enumerate(lines) if s == "if (.not. shifted) then")
+        k_pt = next(k for k, (no, s) in enumerate(lines) if s == "node_pt = 0")
+        k_loop = next(k for k in range(k_pt, len(lines)) if re.match(r"^do\s+i\s*=\s*1\s*,\s*dir$", lines[k][1]))
+        reach_if, _ = F.parse_stmt(lines, k_reach)
+        loop, _ = F.parse_stmt(lines, k_loop)
+        st = cs["state"]
+        q, nz, ny, nx = st.shape
+        per_y = bool(cs["periodic"] & 2)
+
+        def fab(arr, fill, dtype):
+            out = np.full((nx + 2 * G, ny + 2 * G, nz + 2 * G, 39), fill, dtype)
+            t = np.transpose(arr, (3, 2, 1, 0))
+            out[G:G + nx, G:G + ny, G:G + nz, :] = t
+            if per_y:
+                for yf in list(range(G)) + list(range(G + ny, ny + 2 * G)):
+                    out[G:G + nx, yf, G:G + nz, :] = t[:, (yf - G) % ny, :, :]
+            return out
+
+        lb = [-G, -G, -G, 1]
+        g = self.g
+        g["inlet_type"] = F.FArray(np.array([cs["inlet_type"], cs["inlet_type"]], np.int64), [1, 1])
+        g["outlet_type"] = F.FArray(np.array([cs["outlet_type"], cs["outlet_type"]], np.int64), [1, 1])
+        g["inl_fieq"] = F.FArray(np.array([cs["fi"]] * 8).T.copy(), [1, 1])
+        g["inl_gieq"] = F.FArray(np.array([cs["gi"]] * 8).T.copy(), [1, 1])
+        g["outl_fieq"] = F.FArray(np.array([cs["fo"]] * 8).T.copy(), [1, 1])
+        g["outl_gieq"] = F.FArray(np.array([cs["go"]] * 8).T.copy(), [1, 1])
+        g["fs_fieq"] = F.FArray(np.asarray(cs["ff"], np.float64).copy(), [1])
+        g["fs_gieq"] = F.FArray(np.asarray(cs["gf"], np.float64).copy(), [1])
+        local = {}
+        scope = self.interp.scope_for(local)
+        self.interp.declare("integer :: a,b,c,i,j,reach,loc_cx,loc_cy,loc_cz", local, scope, set())
+        local.update(lvl=F.FInt(0), dummy_fout=0.0, dummy_gout=0.0,
+                     wax_lo=F.FArray(np.array([0, 0, 0], np.int64), [1]),
+                     wax_hi=F.FArray(np.array([nx - 1, ny - 1, nz - 1], np.int64), [1]),
+                     state=F.FArray(fab(st, -666, np.int64), lb),
+                     fout=F.FArray(fab(cs["fout"], 0.0, np.float64), lb),
+                     gout=F.FArray(fab(cs["gout"], 0.0, np.float64), lb),
+                     fi=F.FArray(fab(cs["prev_f"], 0.0, np.float64), lb),
+                     gi=F.FArray(fab(cs["prev_g"], 0.0, np.float64), lb),
+                     node_pt=F.FArray(np.zeros((nx + 2 * G, ny + 2 * G, nz + 2 * G, 1), np.int64), lb))
+        self.interp.run([reach_if, loop], local, scope)
+
+        def valid(name):
+            return np.ascontiguousarray(np.transpose(local[name].a[G:G + nx, G:G + ny, G:G + nz, :], (3, 2, 1, 0)))
+
+        return valid("fi"), valid("gi"), int(local["reach"])
 
     def targets(self, code, up, vp, wp, Tp, fi):
         """target_finder.f95 for one node (a = b = c = 1): its 39 link codes, u, v, w, T at
@@ -397,6 +479,18 @@ def main(root: pathlib.Path) -> None:
     out["lu_dense"] = recs
     (HERE / "d3q39_core_golden.json").write_text(json.dumps(out))
     (HERE / "d3q39_damp_golden.json").write_text(json.dumps(damp_out))
+    push_out = {}
+    for name, (sh, *_) in push39_inputs.CASES.items():
+        c = case_consts(s39, bool(sh))
+        ref = Reference(root, c, bool(sh))
+        cs = push39_inputs.case(name, s39)
+        fi, gi, reach = ref.push(root, cs)
+        fluid = cs["state"][0] >= 0
+        push_out[name] = {"consts": {k: getattr(c, k) for k in CONST_FIELDS}, "reach": reach,
+                          "fluid_nodes": int(fluid.sum()), "fi": push39_inputs.digest(fi[:, fluid]),
+                          "gi": push39_inputs.digest(gi[:, fluid])}
+        push_out[name]["consts"]["shifted"] = int(sh)
+    (HERE / "d3q39_push_golden.json").write_text(json.dumps(push_out, indent=0))
 
 
 if __name__ == "__main__":

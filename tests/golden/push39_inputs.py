@@ -1,0 +1,57 @@
+"""Seeded inputs of the D3Q39 push-loop cases (streaming.f95 with boundary
+links, no interpolated wall links), shared by the golden generator and the
+test: a 14 x 6 x 7 box with an inlet (-101) at x-, an outlet (-201, of the
+case's type) at x+, a bounce-back floor (-10), a freestream top (-1000), and
+either a periodic span or inviscid side walls (-11); two solid nodes whose
+fluid neighbours bounce back towards them (-10) and one null link (-666).
+Populations, the previous step's post-streaming values and the boundary
+equilibria are seeded positive numbers: the push loop only moves, swaps and
+copies them.  The legacy RandomState stream is frozen across numpy versions."""
+import numpy as np
+
+NX, NY, NZ = 14, 6, 7
+# name: (shifted lattice, outlet type, side-face code (0: periodic span), seed).  A
+# shifted box with a periodic span is left out: there the reference's pushes across
+# the periodic face come from ghost images swept before the face's first layer, so an
+# outlet link at the face writes its slot after them, while the library's single array
+# lets the wrapped node push later in the sweep (a documented difference at the
+# corners where an outlet face meets a periodic one).
+CASES = {"unshifted_outflow": (0, 6, 0, 11), "unshifted_rho_v": (0, 1, 0, 12), "unshifted_inviscid": (0, 6, -11, 15),
+         "shifted_inviscid": (1, 1, -11, 16), "shifted_inviscid_press_temp": (1, 2, -11, 17)}
+
+
+def case(name: str, s39):
+    """dict of the case: state (39, nz, ny, nx), fout, gout, prev_f, prev_g, the
+    equilibrium tables ff, gf (freestream), fi, gi (inlets), fo, go (outlets),
+    inlet and outlet types, periodic flags, shifted.  s39: the package's
+    d3q39_setup (box_state39, lattice39)."""
+    shifted, outlet_type, side, seed = CASES[name]
+    periodic = 2 if side == 0 else 0
+    faces = {"x-": -101, "x+": -201, "z-": -10, "z+": -1000, "y-": side, "y+": side}
+    prio = ("x-", "x+", "z-", "z+", "y-", "y+") if side == 0 else ("y-", "y+", "x-", "x+", "z-", "z+")
+    st = s39.box_state39(NX, NY, NZ, faces, shifted, 1, periodic=periodic, priority=prio)
+    st[0, 3, 2:4, 5:7] = -1
+    cx, cy, cz, _ = s39.lattice39(shifted, 1)
+    for i in range(1, 39):
+        for z in range(NZ):
+            for y in range(NY):
+                for x in range(NX):
+                    if st[0, z, y, x] < 0:
+                        continue
+                    tx, ty, tz = x + cx[i], (y + cy[i]) % NY, z + cz[i]
+                    if 0 <= tx < NX and 0 <= tz < NZ and st[0, tz, ty, tx] < 0:
+                        st[i, z, y, x] = -10
+    st[5, 1, 1, 1] = -666
+    rs = np.random.RandomState(seed)
+    pops = [0.01 + 0.1 * rs.random_sample((39, NZ, NY, NX)) for _ in range(4)]
+    tabs = [0.01 + 0.1 * rs.random_sample(39) for _ in range(6)]
+    return {"state": st, "fout": pops[0], "gout": pops[1], "prev_f": pops[2], "prev_g": pops[3],
+            "ff": tabs[0], "gf": tabs[1], "fi": tabs[2], "gi": tabs[3], "fo": tabs[4], "go": tabs[5],
+            "inlet_type": [1] * 8, "outlet_type": [outlet_type] + [1] * 7, "periodic": periodic,
+            "shifted": shifted}
+
+
+def digest(a: np.ndarray) -> str:
+    import hashlib
+
+    return hashlib.sha256(np.ascontiguousarray(a, np.float64).tobytes()).hexdigest()

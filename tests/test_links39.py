@@ -103,7 +103,7 @@ def test_pull_tables_match_push_loop(pkg, built_lib, shifted, outlet_type, side)
         assert np.array_equal(G[:, fluid], prev_g[:, fluid]), step
 
 
-@pytest.mark.parametrize("shifted", [1, 0])
+@pytest.mark.parametrize("shifted", [1, 0, "wedge"])
 def test_wall_link_slots_match_push_loop(pkg, built_lib, shifted):
     """Interpolated wall links on the shifted and the unshifted lattice: every
     slot the tables do not mark as a wall value matches the oracle's push loop
@@ -111,16 +111,25 @@ def test_wall_link_slots_match_push_loop(pkg, built_lib, shifted):
     the shifted lattice those slots are exactly the wall links (opp(i) = i);
     on the unshifted one slot opp(i) of wall link i, unless a later rule of the
     loop writes it (a bounce-back of link opp(i) through a face writes slot i
-    from the fout(x, i) the closure rewrote in place)."""
+    from the fout(x, i) the closure rewrote in place).  "wedge": the shifted
+    lattice's double-ramp wedge between inviscid side walls (the inviscid
+    reflections next to the walls, the wall links of the ramp)."""
     s39, cap = pkg.d3q39_setup, pkg.capi
+    wedge = shifted == "wedge"
+    shifted = 1 if wedge else shifted
     c, k, lm0, (ff, gf, fi, gi, fo, go) = _case(pkg, shifted)
-    nx, ny, nz, periodic = 14, 6, 7, 2
-    faces = {"x-": -101, "x+": -201, "z-": -10, "z+": -1000, "y-": 0, "y+": 0}
-    st = s39.box_state39(nx, ny, nz, faces, shifted, 1, periodic=periodic)
-    solid = np.zeros((nz, ny, nx), bool)
-    solid[0:2, 1:4, 5:8] = True
     rng = np.random.default_rng(9)
-    s39.wall_links39(st, solid, rng.uniform(0.05, 0.95, (39, nz, ny, nx)), shifted, 1, periodic=periodic)
+    if wedge:
+        nx, ny, nz, periodic = 20, 6, 10, 0
+        st = s39.wedge_state39(nx, ny, nz, 5.0, 12.0, 20.0, s39.WEDGE_FACES, periodic=0,
+                               priority=s39.WEDGE_PRIORITY)
+    else:
+        nx, ny, nz, periodic = 14, 6, 7, 2
+        faces = {"x-": -101, "x+": -201, "z-": -10, "z+": -1000, "y-": 0, "y+": 0}
+        st = s39.box_state39(nx, ny, nz, faces, shifted, 1, periodic=periodic)
+        solid = np.zeros((nz, ny, nx), bool)
+        solid[0:2, 1:4, 5:8] = True
+        s39.wall_links39(st, solid, rng.uniform(0.05, 0.95, (39, nz, ny, nx)), shifted, 1, periodic=periodic)
     opp = s39.lattice39(shifted, 1)[3]
     inl_t, out_t = [1] * 8, [6] + [1] * 7
     fs = (c.mach, 0.0, 0.0, c.temperature)

@@ -127,35 +127,35 @@ def test_wall_derivative_rule_matches_reference_table(o39):
 
 def test_inviscid_rule_matches_reference_table(o39):
     """The oracle's specular-reflection rule for D3Q39 inviscid links against
-    the reference's table (tests/golden/inviscid_table.json, written by
-    tests/golden/make_inviscid_table.py from inviscid_edge.f95): for every
-    direction and every combination of its unit and speed-2 axis links being
-    -11, the first branch of the reference's IF chain that applies gives the
-    reflected direction and the displacement."""
-    import itertools
+    inviscid_edge.f95 itself (tests/golden/inviscid_table.json, written by
+    tests/golden/make_inviscid_table.py, which runs the routine through the
+    f95_subset interpreter): for every direction and every combination of the
+    state components its branch consults being -11, the reflected direction
+    and the displacement, or no write where no branch applies; on the shifted
+    lattice (primary flow along +x) the routine adds the shift to the
+    displacement."""
     import json
     import pathlib
 
     table = json.loads((pathlib.Path(__file__).parent / "golden" / "inviscid_table.json").read_text())
-    assert len(table) == 38
     checked = 0
-    for key, branches in table.items():
-        i = int(key) - 1
-        comps = sorted({c for b in branches for c in b["cond"]})
-        for r in range(len(comps) + 1):
-            for walls in itertools.combinations(comps, r):
+    for lattice, shift in (("unshifted", (0, 0, 0)), ("shifted", (1, 0, 0))):
+        assert len(table[lattice]) == 38
+        for key, entries in table[lattice].items():
+            i = int(key) - 1
+            for e in entries:
                 codes = np.zeros(39, np.int32)
                 codes[i] = -11
-                for c in walls:
+                for c in e["walls"]:
                     codes[c - 1] = -11
-                want = next((b for b in branches if set(b["cond"]) <= set(walls)), None)
                 ok, j, d = o39.inviscid(i, codes)
-                if want is None:
-                    assert not ok, (key, walls)
+                if e["dir"] is None:
+                    assert not ok, (lattice, key, e)
                 else:
-                    assert ok and j + 1 == want["dir"] and list(d) == want["loc"], (key, walls, j + 1, d, want)
+                    got = [d[a] + shift[a] for a in range(3)]
+                    assert ok and j + 1 == e["dir"] and got == e["loc"], (lattice, key, e, j + 1, got)
                 checked += 1
-    assert checked == 274
+    assert checked == 2 * 298
 
 
 @pytest.mark.parametrize("shifted", [0, 1])

@@ -11,7 +11,9 @@ find_little_q_bar.f95), the flow variables of a node
 read from the stored w), the wall targets (target_finder.f95), the
 two-population collision of a node
 (collision.f95), inside and after the start-up ramps, and the negative-
-population repair's sweep over a box (damp_it.f95, d3q39_damp_golden.json).
+population repair's sweep over a box (damp_it.f95, d3q39_damp_golden.json),
+and the push loop of streaming.f95 with its boundary routines
+(d3q39_push_golden.json).
 
 The oracle sums in its own order (generic loops where the reference spells
 terms out), so the bar is 1e-13 relative to each quantity's scale; the LU
@@ -26,6 +28,7 @@ GOLDEN = pathlib.Path(__file__).resolve().parent / "golden" / "d3q39_core_golden
 DATA = json.loads(GOLDEN.read_text())
 LATTICES = sorted(DATA["lattices"])
 DAMP = json.loads((GOLDEN.parent / "d3q39_damp_golden.json").read_text())
+PUSH = json.loads((GOLDEN.parent / "d3q39_push_golden.json").read_text())
 
 
 @pytest.fixture(scope="module")
@@ -152,6 +155,37 @@ def test_wall_targets(o39, name):
     for c in lat["targets"]:
         out = o39.target_finder(k, c["code"], c["u"], c["v"], c["w"], c["T"], c["fi"], c["fs_temp"])
         assert out.tolist() == c["out"], (out.tolist(), c["out"])
+
+
+@pytest.mark.parametrize("name", sorted(PUSH))
+def test_push_loop(o39, pkg, name):
+    """The oracle's push loop (o39_step_links) against streaming.f95's own sweep with
+    the boundary routines it calls, on boxes with inlet, outlet, bounce-back,
+    freestream, inviscid and null links: the post-streaming fi and gi of every fluid
+    node bit for bit (sha-256 digests of the reference's arrays; slots no rule writes
+    keep the previous step's values on both sides)."""
+    import sys
+
+    sys.path.insert(0, str(GOLDEN.parent))
+    import push39_inputs as P
+
+    ref = PUSH[name]
+    k = o39.O39Consts()
+    for n, v in ref["consts"].items():
+        setattr(k, n, v)
+    k.max_lm_iters = 200
+    cs = P.case(name, pkg.d3q39_setup)
+    lev = o39.Level39(P.NX, P.NY, P.NZ)
+    lev.fout[...] = cs["fout"]
+    lev.gout[...] = cs["gout"]
+    pf, pg = cs["prev_f"].copy(), cs["prev_g"].copy()
+    b = o39.bc(cs["inlet_type"], cs["outlet_type"], cs["ff"], cs["gf"], [cs["fi"]] * 8, [cs["gi"]] * 8,
+               [cs["fo"]] * 8, [cs["go"]] * 8)
+    o39.step_links(k, lev, 0, cs["state"], cs["periodic"], b, pf, pg)
+    fluid = cs["state"][0] >= 0
+    assert int(fluid.sum()) == ref["fluid_nodes"]
+    assert P.digest(pf[:, fluid]) == ref["fi"]
+    assert P.digest(pg[:, fluid]) == ref["gi"]
 
 
 @pytest.mark.parametrize("name", sorted(DAMP))

@@ -46,8 +46,12 @@ struct Sym {
 // the unit link along it being -11 reflects it (displacement 0 for speed-1
 // diagonals, -c/2 for speed-2 ones), else for speed-2 diagonals the speed-2
 // link being -11 reflects it (displacement +c/2), else it keeps c.  Axis
-// directions always reflect (displacement 0, c/2, -2c/3 for speeds 1, 2, 3).
-// The reference's table departs from this in two entries, kept here:
+// directions always reflect: displacement 0 for speed 1; for speed 2, -c/2
+// when the unit link along the axis is -11, else +c/2; for speed 3, +2c/3
+// when the unit and the speed-2 links along it are both -11, 0 when only the
+// speed-2 one is, else -2c/3.  On the shifted lattice the routine then adds
+// the shift (the primary flow direction's unit vector, :1230-1243); the
+// caller does that.  The reference's table departs from this in two entries, kept here:
 // direction 9 (1-based) with x and y (x and z) reflecting goes to 12 (11), and
 // direction 27 with only y reflecting is displaced by the opposite y.
 bool inviscid39(const Lattice39& U, int i, const int32_t* code, int& j, int (&d)[3]) {
@@ -59,7 +63,12 @@ bool inviscid39(const Lattice39& U, int i, const int32_t* code, int& j, int (&d)
   if (nz == 1) {
     for (int a = 0; a < 3; ++a) {
       r[a] = -c[a];
-      d[a] = sp == 1 ? 0 : sp == 2 ? c[a] / 2 : -(2 * c[a]) / 3;
+      d[a] = 0;
+      if (c[a] == 0) continue;
+      const int side = c[a] < 0 ? 3 : 0;
+      const bool unit = code[1 + a + side] == -11, two = code[15 + a + side] == -11;
+      if (sp == 2) d[a] = unit ? -c[a] / 2 : c[a] / 2;
+      else if (sp == 3) d[a] = (unit && two) ? (2 * c[a]) / 3 : two ? 0 : -(2 * c[a]) / 3;
     }
   } else {
     for (int a = 0; a < 3; ++a) {
@@ -221,6 +230,7 @@ int decode_links39(const int32_t* st, int ngs, int nx, int ny, int nz, int perio
             // no branch of inviscid_edge.f95 applies (no unit or speed-2 axis link of the direction is
             // -11, e.g. where a wall link took one): the reference writes nothing for this link
             if (!inviscid39(L0, i, codes, j, d)) continue;
+            if (shifted) d[(pfd - 1) % 3] += pfd <= 3 ? 1 : -1;  // the shift, inviscid_edge.f95:1230-1243
             const int64_t r = node_at(x + d[0], y + d[1], z + d[2]);
             if (r >= 0) emit(r, j, kpos + 1, fo[i]);
             continue;
