@@ -56,7 +56,7 @@ def pull39(words_kind, lev_f, lev_g, ntype, rec, words, prev_f, prev_g, eqf, eqg
 
 
 @pytest.mark.parametrize("shifted,outlet_type,side", [(0, 6, 0), (0, 1, 0), (1, 6, 0), (1, 2, 0), (0, 6, -11),
-                                                      (1, 1, -11)])
+                                                      (1, 1, -11), (1, 6, -11), (0, 2, -11)])
 def test_pull_tables_match_push_loop(pkg, built_lib, shifted, outlet_type, side):
     """side 0: periodic in y; -11 / -12: inviscid side walls (specular reflection), which take the
     links that also cross another face (so every inviscid link has an inviscid axis link)."""
