@@ -1460,6 +1460,17 @@ void o39_little_q_bar_api(const o39_consts* k, const double* gd, double u, doubl
   little_q_bar(&L, k, gd, u, v, w, T, step, out);
 }
 
+/* shifted_ibb39 on given inputs: wall link i (0-based), the closure direction's equilibria,
+ * rho, the (u, v, w, T) targets, the seven-point stencil's fields and node types; out: fout, gout. */
+void o39_shifted_ibb_api(const o39_consts* k, int i, int step, double fieq, double gieq, double rho, const double* tgt,
+                         const double* ul, const double* vl, const double* wl, const double* Tl, const int* sp,
+                         double* out) {
+  o39_lattice L;
+  o39_lattice_init(&L, k->shifted, k->primary_flow_dir);
+  shifted_ibb39(k, &L, i, step, fieq, gieq, rho, tgt[0], tgt[1], tgt[2], tgt[3], ul, vl, wl, Tl, sp, &out[0],
+                &out[1]);
+}
+
 /* target_finder39 on given inputs (39 codes, fields at x + c_j, slots); out: 5 targets. */
 void o39_target_finder_api(const o39_consts* k, const int32_t* code, const double* up, const double* vp,
                            const double* wp, const double* Tp, const double* fi, double fs_temp, double* out) {

@@ -274,6 +274,8 @@ def _pieces():
         L.o39_collide_node_api.argtypes = [ct.POINTER(O39Consts), vp, vp, vp, d, d, d, d, d, d, i, vp, vp]
         L.o39_flow_vars_api.restype = None
         L.o39_flow_vars_api.argtypes = [ct.POINTER(O39Consts), vp, vp, d, vp]
+        L.o39_shifted_ibb_api.restype = None
+        L.o39_shifted_ibb_api.argtypes = [ct.POINTER(O39Consts), i, i, d, d, d, vp, vp, vp, vp, vp, vp, vp]
         L.o39_target_finder_api.restype = None
         L.o39_target_finder_api.argtypes = [ct.POINTER(O39Consts), vp, vp, vp, vp, vp, vp, d, vp]
         L.o39_damp_api.restype = ct.c_int64
@@ -284,6 +286,17 @@ def _pieces():
 
 def _a(x):
     return np.ascontiguousarray(x, np.float64)
+
+
+def shifted_ibb(k: O39Consts, i, step, fieq, gieq, rho, tgt, u, v, w, T, sp):
+    """(fout, gout) of shifted_ibb.f95 for wall link i (0-based): the closure direction's
+    equilibria, rho, the (u, v, w, T) targets, the seven-point stencil's fields and node
+    types (rest, +x, +y, +z, -x, -y, -z)."""
+    out = np.zeros(2)
+    spa = np.ascontiguousarray(sp, np.int32)
+    _pieces().o39_shifted_ibb_api(ct.byref(k), int(i), int(step), float(fieq), float(gieq), float(rho),
+                                  _p(_a(tgt)), _p(_a(u)), _p(_a(v)), _p(_a(w)), _p(_a(T)), _p(spa), _p(out))
+    return out
 
 
 def target_finder(k: O39Consts, code, u, v, w, T, fi, fs_temp):

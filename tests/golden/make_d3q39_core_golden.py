@@ -12,6 +12,8 @@ Fortran statements (tests/golden/f95_subset.py interprets them in float64):
                         temperature, pressure and the six pressure-tensor targets; P_zz reads the stored w)
   collision of a node   looping/timestepping/collision.f95 (the body of the per-node loop)
   wall targets          boundary_conditions/interpolative_bc/target_finder.f95 (both lattices)
+  shifted wall closure  boundary_conditions/interpolative_bc/shifted_ibb.f95 with the wall and local
+                        derivatives of derivatives/modules/derivatives.f95
   push loop             looping/timestepping/streaming.f95:263-1161 with the boundary routines it calls
                         (bc_switchboard, bounceback, inlet_bc, outlet_bc and its variants,
                         freestream_edge_bc, inviscid_edge) on boxes of push39_inputs: digests of the
@@ -113,6 +115,11 @@ class Reference:
         self.procs = {}
         for p in files:
             self.procs.update(F.parse_units(F.logical_lines(p.read_text()), only=wanted))
+        # the wall-derivative functions of the derivatives module (shifted_ibb's stencil)
+        self.procs.update(F.parse_units(F.logical_lines((R / "derivatives/modules/derivatives.f95").read_text())))
+        if shifted:
+            self.procs.update(F.parse_units(F.logical_lines(
+                (R / "boundary_conditions/interpolative_bc/shifted_ibb.f95").read_text()), only={"shifted_ibb"}))
         missing = wanted - set(self.procs)
         if missing:
             raise RuntimeError(f"reference routines not found: {sorted(missing)}")
@@ -289,6 +296,21 @@ class Reference:
 
         return valid("fi"), valid("gi"), int(local["reach"])
 
+    def shifted_ibb(self, i, code_i, fieq_opp, gieq_opp, rho, tgt, ul, vl, wl, Tl, sp):
+        """shifted_ibb.f95 for wall link i (1-based) of a node: its code of direction i, the
+        equilibria of the closure's direction, rho, the (u, v, w, T) targets, the seven-point
+        stencil's u, v, w, T and node types; returns (fout, gout)."""
+        v = {"fo": float("nan"), "go": float("nan")}
+        node = F.FArray(np.full((1, 1, 1, 39), -1, np.int64), [1, 1, 1, 1])
+        node.set((1, 1, 1, i), code_i)
+        vec = lambda vals, dt=np.float64: F.FArray(np.asarray(vals, dt).copy())  # noqa: E731
+        nan = float("nan")
+        self.interp.call("shifted_ibb", [F.Ref(v, "fo"), nan, nan, nan, float(fieq_opp), nan, nan, F.Ref(v, "go"),
+                                         nan, nan, nan, float(gieq_opp)] + [float(x) for x in tgt] +
+                         [F.FInt(i), F.FInt(0), node, float(rho), vec(ul), vec(vl), vec(wl), vec(Tl),
+                          vec(sp, np.int64), F.FInt(0), F.FInt(1), F.FInt(1), F.FInt(1)])
+        return v["fo"], v["go"]
+
     def targets(self, code, up, vp, wp, Tp, fi):
         """target_finder.f95 for one node (a = b = c = 1): its 39 link codes, u, v, w, T at
         x + c_j, and its post-streaming slots; returns rho, u, v, w, T targets."""
@@ -417,6 +439,28 @@ def main(root: pathlib.Path) -> None:
                            "fi": fi_n.tolist(), "fs_temp": c.temperature,
                            "out": ref.targets(code, up, vp, wp, Tp, fi_n)})
         lat["targets"] = tcases
+        if shifted:
+            # shifted_ibb on seeded wall links: stencil node types interior, solid (-1001) or
+            # null (-666), before and after the start-up ramps
+            rng_s = np.random.RandomState(5151)
+            scases = []
+            for n_case in range(16):
+                i = int(rng_s.randint(1, 40))
+                code_i = int(-1001 - np.floor(rng_s.uniform(0.02, 0.98) * 1e9))
+                sp = [0] + rng_s.choice([0, 0, 0, -1001, -666, -1001 - 400000000], 6).tolist()
+                tgt = [c.mach * rng_s.uniform(0.0, 1.0), c.mach * rng_s.uniform(-0.2, 0.2),
+                       c.mach * rng_s.uniform(-0.2, 0.2), c.temperature * rng_s.uniform(0.9, 1.3)]
+                ul, vl, wl = (c.mach * rng_s.uniform(-0.3, 1.2, 7) for _ in range(3))
+                Tl = c.temperature * rng_s.uniform(0.8, 1.4, 7)
+                rho = float(rng_s.uniform(0.8, 1.3))
+                fe, ge = float(rng_s.uniform(0.001, 0.1)), float(rng_s.uniform(0.001, 0.1))
+                step = 3 if n_case % 2 == 0 else c.startup_timesteps + 11
+                ref.set_step(step)
+                fo, go = ref.shifted_ibb(i, code_i, fe, ge, rho, tgt, ul, vl, wl, Tl, sp)
+                scases.append({"i": i, "code": code_i, "fieq": fe, "gieq": ge, "rho": rho, "tgt": tgt,
+                               "u": ul.tolist(), "v": vl.tolist(), "w": wl.tolist(), "T": Tl.tolist(), "sp": sp,
+                               "step": step, "fout": fo, "gout": go})
+            lat["shifted_ibb"] = scases
         lm_start = s39.freestream_start_lm(c)
         for k in range(3):
             rho = float(rng.uniform(0.92, 1.08))

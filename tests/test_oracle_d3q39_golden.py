@@ -8,7 +8,8 @@ shifted one generic, :696-1097), the LU update with its two index quirks
 (calculate_alpha.f95), the heat-flux corrections (find_q_bar.f95,
 find_little_q_bar.f95), the flow variables of a node
 (calculate_flow_variables.f95:192-228, with the pressure-tensor target P_zz
-read from the stored w), the wall targets (target_finder.f95), the
+read from the stored w), the wall targets (target_finder.f95), the shifted
+lattice's wall closure (shifted_ibb.f95 with the derivatives module), the
 two-population collision of a node
 (collision.f95), inside and after the start-up ramps, and the negative-
 population repair's sweep over a box (damp_it.f95, d3q39_damp_golden.json),
@@ -155,6 +156,19 @@ def test_wall_targets(o39, name):
     for c in lat["targets"]:
         out = o39.target_finder(k, c["code"], c["u"], c["v"], c["w"], c["T"], c["fi"], c["fs_temp"])
         assert out.tolist() == c["out"], (out.tolist(), c["out"])
+
+
+def test_shifted_wall_closure(o39):
+    """shifted_ibb.f95 (the Grad-type closure of a wall link on the shifted lattice, with
+    the derivatives module's one-sided wall and local stencil derivatives) against the
+    oracle's shifted_ibb39: fout and gout bit for bit, before and after the start-up
+    ramps, with interior, solid and null stencil nodes."""
+    lat = DATA["lattices"]["shifted"]
+    k = _consts(o39, lat)
+    for c in lat["shifted_ibb"]:
+        out = o39.shifted_ibb(k, c["i"] - 1, c["step"], c["fieq"], c["gieq"], c["rho"], c["tgt"], c["u"], c["v"],
+                              c["w"], c["T"], c["sp"])
+        assert out.tolist() == [c["fout"], c["gout"]], (c["i"], c["step"], out.tolist(), c["fout"], c["gout"])
 
 
 @pytest.mark.parametrize("name", sorted(PUSH))
