@@ -152,6 +152,19 @@ class FArray:
     def __neg__(self):
         return FArray(-self.a)
 
+    # elementwise comparisons (for ANY / ALL over sections)
+    def __lt__(self, o):
+        return self._bin(o, np.less)
+
+    def __le__(self, o):
+        return self._bin(o, np.less_equal)
+
+    def __gt__(self, o):
+        return self._bin(o, np.greater)
+
+    def __ge__(self, o):
+        return self._bin(o, np.greater_equal)
+
 
 def _S(lo, hi):
     return slice(lo, hi)
@@ -237,6 +250,7 @@ INTRINSICS = {
     "selected_real_kind": lambda p=6, r=37: FInt(8 if p > 6 or r > 37 else 4),
     "selected_int_kind": lambda r=9: FInt(8 if r > 9 else 4),
     "kind": lambda x: FInt(8),
+    "any": lambda x: bool(np.any(_val(x))), "all": lambda x: bool(np.all(_val(x))),
 }
 
 PY_RESERVED = {"lambda", "in", "is", "if", "else", "for", "while", "and", "or", "not", "def", "class", "return",
@@ -700,6 +714,23 @@ class Interp:
             name, dims = m.group(1), m.group(3) or (dim_attr.group(1) if dim_attr else None)
             pname = pyname(name)
             if pname in dummies:
+                # an explicit-shape dummy array takes its declared shape and bounds over the actual's
+                # elements (sequence association: a section a(i,j,k,1:n) passed to b(i:i,j:j,k:k,1:n))
+                act = local.get(pname)
+                if dims is not None and isinstance(act, FArray) and not re.fullmatch(r"[:,\s*]*", dims):
+                    shape, lbs = [], []
+                    for d in split_top(dims):
+                        if ":" in d:
+                            lo, hi = d.split(":")
+                            lo_v = int(self.ev(lo, scope)) if lo.strip() else 1
+                            hi_v = int(self.ev(hi, scope))
+                        else:
+                            lo_v, hi_v = 1, int(self.ev(d, scope))
+                        shape.append(hi_v - lo_v + 1)
+                        lbs.append(lo_v)
+                    if int(np.prod(shape)) == act.a.size and (tuple(shape) != act.a.shape or tuple(lbs) != act.lb):
+                        data = act.a if tuple(shape) == act.a.shape else act.a.reshape(shape, order="F")
+                        local[pname] = FArray(data, lbs)
                 continue
             if dims is not None and not re.fullmatch(r"[:,\s]*", dims):
                 shape, lbs = [], []

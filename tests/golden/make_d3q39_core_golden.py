@@ -16,8 +16,10 @@ Fortran statements (tests/golden/f95_subset.py interprets them in float64):
                         derivatives of derivatives/modules/derivatives.f95
   push loop             looping/timestepping/streaming.f95:263-1161 with the boundary routines it calls
                         (bc_switchboard, bounceback, inlet_bc, outlet_bc and its variants,
-                        freestream_edge_bc, inviscid_edge) on boxes of push39_inputs: digests of the
-                        post-streaming fi, gi of the fluid nodes, written to d3q39_push_golden.json
+                        freestream_edge_bc, inviscid_edge; on the wall cases also target_finder, the target
+                        multiplier solve and shifted_ibb) on boxes of push39_inputs: digests of the
+                        post-streaming fi, gi of the fluid nodes (the wall-link slots, whose closure sums
+                        the oracle orders its own way, as values), written to d3q39_push_golden.json
   fout repair           looping/timestepping/damp_it.f95 (the reach and the in-place sweep of one box,
                         written to d3q39_damp_golden.json)
   transport             utilities/modules/quick_calcs.f95, amr_processes.f95 beta_1/2_calculator,
@@ -160,7 +162,7 @@ class Reference:
             if len(self.lu_log) > 200:
                 raise RuntimeError("multiplier solve did not converge in 200 iterations")
 
-        self.procs["lu_decomp"] = lu_hook
+        self.procs["lu_decomp"] = self._lu_hook = lu_hook
 
     def set_step(self, step: int):
         self.g["timestep"].set((0,), step)
@@ -250,9 +252,11 @@ class Reference:
             s = s.replace("wax%lo(", "wax_lo(").replace("wax%hi(", "wax_hi(")
             lines += [(no, lab_f), (no, lab_g), (no, "cycle")] if k == k_goto else [(no, s)]
         k_reach = next(k for k, (no, s) in enumerate(lines) if s == "if (.not. shifted) then")
+        k_kg = next(k for k, (no, s) in enumerate(lines) if s.startswith("k_gieq = "))
         k_pt = next(k for k, (no, s) in enumerate(lines) if s == "node_pt = 0")
         k_loop = next(k for k in range(k_pt, len(lines)) if re.match(r"^do\s+i\s*=\s*1\s*,\s*dir$", lines[k][1]))
         reach_if, _ = F.parse_stmt(lines, k_reach)
+        kg_stmt, _ = F.parse_stmt(lines, k_kg)
         loop, _ = F.parse_stmt(lines, k_loop)
         st = cs["state"]
         q, nz, ny, nx = st.shape
@@ -279,7 +283,34 @@ class Reference:
         g["fs_gieq"] = F.FArray(np.asarray(cs["gf"], np.float64).copy(), [1])
         local = {}
         scope = self.interp.scope_for(local)
-        self.interp.declare("integer :: a,b,c,i,j,reach,loc_cx,loc_cy,loc_cz", local, scope, set())
+        self.interp.declare("integer :: a,b,c,i,j,reach,loc_cx,loc_cy,loc_cz,fine,state_pass(7)", local, scope,
+                            set())
+        self.interp.declare("real(kind=dp) :: loc_fieq,loc_gieq,loc_fieq_opp,loc_gieq_opp,k_gieq,pass_fieq(dir),"
+                            "pxx_temp,pyy_temp,pzz_temp,pxy_temp,pxz_temp,pyz_temp", local, scope, set())
+        for nm in ("u_local", "v_local", "w_local", "temp_local"):
+            local[nm] = F.FArray(np.zeros(7))
+        for nm in ("u_pass", "v_pass", "w_pass", "temp_pass"):
+            local[nm] = F.FArray(np.zeros(39))
+        if "fields" in cs:
+            # the fields, multipliers and the per-node target scratch FABs the wall branch reads and writes
+            def fab1(arr3):
+                out = np.zeros((nx + 2 * G, ny + 2 * G, nz + 2 * G, 1))
+                out[G:G + nx, G:G + ny, G:G + nz, 0] = np.transpose(arr3, (2, 1, 0))
+                return F.FArray(out, lb)
+            for nm, arr in zip(("rho", "u_vel", "v_vel", "w_vel", "temp"), cs["fields"]):
+                local[nm] = fab1(arr)
+            for r, nm in enumerate(LM_NAMES):
+                local[nm] = fab1(cs["lm"][r])
+                local[nm + "_temp"] = fab1(np.zeros((nz, ny, nx)))
+            for nm in ("rho_tgt_temp", "u_tgt_temp", "v_tgt_temp", "w_tgt_temp", "temp_tgt_temp"):
+                local[nm] = fab1(np.zeros((nz, ny, nx)))
+            fs = cs["fs_uvwT"]
+            g.update(fs_u=fs[0], fs_v=fs[1], fs_w=fs[2], temperature=fs[3])
+            for nm, v in zip(("su_chi", "su_zeta_x", "su_zeta_y", "su_zeta_z", "su_pixx", "su_piyy", "su_pizz",
+                              "su_pixy", "su_pixz", "su_piyz", "su_lambda_x", "su_lambda_y", "su_lambda_z"),
+                             cs["su_lm"]):
+                g[nm] = float(v)
+            self.set_step(cs.get("step", 0))
         local.update(lvl=F.FInt(0), dummy_fout=0.0, dummy_gout=0.0,
                      wax_lo=F.FArray(np.array([0, 0, 0], np.int64), [1]),
                      wax_hi=F.FArray(np.array([nx - 1, ny - 1, nz - 1], np.int64), [1]),
@@ -289,7 +320,12 @@ class Reference:
                      fi=F.FArray(fab(cs["prev_f"], 0.0, np.float64), lb),
                      gi=F.FArray(fab(cs["prev_g"], 0.0, np.float64), lb),
                      node_pt=F.FArray(np.zeros((nx + 2 * G, ny + 2 * G, nz + 2 * G, 1), np.int64), lb))
-        self.interp.run([reach_if, loop], local, scope)
+        local["fine"] = F.FInt(0)
+        self.procs["lu_decomp"] = self.real_lu  # (the recording wrapper caps its log at 200 updates)
+        try:
+            self.interp.run([reach_if, kg_stmt, loop], local, scope)
+        finally:
+            self.procs["lu_decomp"] = self._lu_hook
 
         def valid(name):
             return np.ascontiguousarray(np.transpose(local[name].a[G:G + nx, G:G + ny, G:G + nz, :], (3, 2, 1, 0)))
@@ -534,6 +570,20 @@ def main(root: pathlib.Path) -> None:
                           "fluid_nodes": int(fluid.sum()), "fi": push39_inputs.digest(fi[:, fluid]),
                           "gi": push39_inputs.digest(gi[:, fluid])}
         push_out[name]["consts"]["shifted"] = int(sh)
+    for name in push39_inputs.WALL_CASES:
+        c = s39.wedge_case_consts()
+        ref = Reference(root, c, True)
+        cs = push39_inputs.wall_case(name, s39)
+        fi, gi, reach = ref.push(root, cs)
+        fluid = cs["state"][0] >= 0
+        wall = (cs["state"] <= -1001) & fluid[None]
+        wall[0] = False
+        other = fluid[None] & ~wall
+        push_out[name] = {"consts": {k: getattr(c, k) for k in CONST_FIELDS}, "reach": reach,
+                          "fluid_nodes": int(fluid.sum()), "wall_slots": int(wall.sum()),
+                          "fi": push39_inputs.digest(fi[other]), "gi": push39_inputs.digest(gi[other]),
+                          "fi_wall": fi[wall].tolist(), "gi_wall": gi[wall].tolist()}
+        push_out[name]["consts"]["shifted"] = 1
     (HERE / "d3q39_push_golden.json").write_text(json.dumps(push_out, indent=0))
 
 

@@ -55,3 +55,39 @@ def digest(a: np.ndarray) -> str:
     import hashlib
 
     return hashlib.sha256(np.ascontiguousarray(a, np.float64).tobytes()).hexdigest()
+
+
+# wall cases: the shifted lattice's double-ramp wedge between inviscid side walls (inlet,
+# outlet of type 6, bounce-back floor, freestream top, the ramp's interpolated wall links),
+# at the start (timestep 0: the start-up multipliers seed the target solves) and past the
+# start-up (the node's own multipliers seed them)
+WALL_CASES = {"wedge_start": (0, 21), "wedge_late": (150, 22)}
+# side faces of the wall cases: bounce-back, so that no inviscid link meets a wall link (where
+# the reference's inviscid_edge assigns no direction and the push writes into the slot of a
+# stale direction variable, which the library does not reproduce)
+WALL_FACES = {"x-": -101, "x+": -201, "z-": -10, "z+": -1000, "y-": -10, "y+": -10}
+WNX, WNY, WNZ = 20, 6, 10
+
+
+def wall_case(name: str, s39):
+    """The push-loop case dict (see case) plus the fields rho, u, v, w, T near the
+    freestream, every node's multipliers at the freestream solution, the start-up
+    multipliers, the freestream (u, v, w, T) and the step."""
+    step, seed = WALL_CASES[name]
+    c = s39.wedge_case_consts()
+    st = s39.wedge_state39(WNX, WNY, WNZ, 5.0, 12.0, 20.0, WALL_FACES, periodic=0, priority=s39.WEDGE_PRIORITY)
+    rs = np.random.RandomState(seed)
+    shape = (39, WNZ, WNY, WNX)
+    pops = [0.01 + 0.1 * rs.random_sample(shape) for _ in range(4)]
+    tabs = [0.01 + 0.1 * rs.random_sample(39) for _ in range(6)]
+    n3 = (WNZ, WNY, WNX)
+    fields = [1.0 + 0.02 * rs.uniform(-1, 1, n3), c.mach * (1 + 0.05 * rs.uniform(-1, 1, n3)),
+              0.02 * c.mach * rs.uniform(-1, 1, n3), 0.02 * c.mach * rs.uniform(-1, 1, n3),
+              c.temperature * (1 + 0.03 * rs.uniform(-1, 1, n3))]
+    lm0 = np.asarray(s39.freestream_start_lm(c), np.float64)
+    lm = np.broadcast_to(lm0[:, None, None, None], (13,) + n3).copy()
+    return {"state": st, "fout": pops[0], "gout": pops[1], "prev_f": pops[2], "prev_g": pops[3],
+            "ff": tabs[0], "gf": tabs[1], "fi": tabs[2], "gi": tabs[3], "fo": tabs[4], "go": tabs[5],
+            "inlet_type": [1] * 8, "outlet_type": [6] + [1] * 7, "periodic": 0, "shifted": 1,
+            "fields": fields, "lm": lm, "su_lm": list(c.su_lm), "fs_uvwT": (c.mach, 0.0, 0.0, c.temperature),
+            "step": step}

@@ -171,7 +171,41 @@ def test_shifted_wall_closure(o39):
         assert out.tolist() == [c["fout"], c["gout"]], (c["i"], c["step"], out.tolist(), c["fout"], c["gout"])
 
 
-@pytest.mark.parametrize("name", sorted(PUSH))
+@pytest.mark.parametrize("name", sorted(n for n in PUSH if "fi_wall" in PUSH[n]))
+def test_push_loop_with_wall_links(o39, pkg, name):
+    """The push loop over the shifted lattice's double-ramp wedge with interpolated wall
+    links (target_finder at each wall node's first wall link, the target multiplier
+    solve from the start-up multipliers at timestep 0 or the node's own ones later, the
+    seven-point stencil and shifted_ibb), against streaming.f95 run through the
+    interpreter: every slot but the wall-link ones bit for bit; the wall-link slots,
+    whose multiplier and closure sums the oracle orders its own way, within 1e-13."""
+    import sys
+
+    sys.path.insert(0, str(GOLDEN.parent))
+    import push39_inputs as P
+
+    ref = PUSH[name]
+    k = o39.consts(pkg.d3q39_setup.wedge_case_consts())
+    cs = P.wall_case(name, pkg.d3q39_setup)
+    lev = o39.Level39(P.WNX, P.WNY, P.WNZ)
+    lev.fout[...], lev.gout[...], lev.lm[...] = cs["fout"], cs["gout"], cs["lm"]
+    lev.rho[...], lev.u[...], lev.v[...], lev.w_vel[...], lev.temp[...] = cs["fields"]
+    pf, pg = cs["prev_f"].copy(), cs["prev_g"].copy()
+    b = o39.bc(cs["inlet_type"], cs["outlet_type"], cs["ff"], cs["gf"], [cs["fi"]] * 8, [cs["gi"]] * 8,
+               [cs["fo"]] * 8, [cs["go"]] * 8, cs["fs_uvwT"])
+    o39.step_links(k, lev, cs["step"], cs["state"], 0, b, pf, pg)
+    fluid = cs["state"][0] >= 0
+    wall = (cs["state"] <= -1001) & fluid[None]
+    wall[0] = False
+    assert int(fluid.sum()) == ref["fluid_nodes"] and int(wall.sum()) == ref["wall_slots"]
+    other = fluid[None] & ~wall
+    assert P.digest(pf[other]) == ref["fi"] and P.digest(pg[other]) == ref["gi"]
+    for got, key in ((pf[wall], "fi_wall"), (pg[wall], "gi_wall")):
+        want = np.array(ref[key])
+        assert np.max(np.abs(got - want) / np.abs(want)) <= 1e-13, key
+
+
+@pytest.mark.parametrize("name", sorted(n for n in PUSH if "fi_wall" not in PUSH[n]))
 def test_push_loop(o39, pkg, name):
     """The oracle's push loop (o39_step_links) against streaming.f95's own sweep with
     the boundary routines it calls, on boxes with inlet, outlet, bounce-back,
