@@ -119,9 +119,10 @@ class Reference:
             self.procs.update(F.parse_units(F.logical_lines(p.read_text()), only=wanted))
         # the wall-derivative functions of the derivatives module (shifted_ibb's stencil)
         self.procs.update(F.parse_units(F.logical_lines((R / "derivatives/modules/derivatives.f95").read_text())))
-        if shifted:
-            self.procs.update(F.parse_units(F.logical_lines(
-                (R / "boundary_conditions/interpolative_bc/shifted_ibb.f95").read_text()), only={"shifted_ibb"}))
+        ibb = ("shifted_ibb", "shifted_ibb.f95") if shifted else \
+            ("interpolative_bounceback_bc", "interpolative_bounceback_bc.f95")
+        self.procs.update(F.parse_units(F.logical_lines(
+            (R / "boundary_conditions/interpolative_bc" / ibb[1]).read_text()), only={ibb[0]}))
         missing = wanted - set(self.procs)
         if missing:
             raise RuntimeError(f"reference routines not found: {sorted(missing)}")
@@ -570,20 +571,26 @@ def main(root: pathlib.Path) -> None:
                           "fluid_nodes": int(fluid.sum()), "fi": push39_inputs.digest(fi[:, fluid]),
                           "gi": push39_inputs.digest(gi[:, fluid])}
         push_out[name]["consts"]["shifted"] = int(sh)
-    for name in push39_inputs.WALL_CASES:
-        c = s39.wedge_case_consts()
-        ref = Reference(root, c, True)
-        cs = push39_inputs.wall_case(name, s39)
+    wall_cases = [(name, s39.wedge_case_consts(), push39_inputs.wall_case(name, s39))
+                  for name in push39_inputs.WALL_CASES]
+    wall_cases.append(("unshifted_walls",) + push39_inputs.unshifted_wall_case(s39))
+    for name, c, cs in wall_cases:
+        sh = bool(cs["shifted"])
+        ref = Reference(root, c, sh)
         fi, gi, reach = ref.push(root, cs)
         fluid = cs["state"][0] >= 0
         wall = (cs["state"] <= -1001) & fluid[None]
         wall[0] = False
+        # the slots a wall closure's value can reach: slot opp(i) of wall link i, and slot i where a
+        # later bounce-back of link opp(i) writes it from the rewritten fout(x, i)
+        opp = s39.lattice39(int(sh), 1)[3]
+        wall = wall | wall[opp]
         other = fluid[None] & ~wall
         push_out[name] = {"consts": {k: getattr(c, k) for k in CONST_FIELDS}, "reach": reach,
                           "fluid_nodes": int(fluid.sum()), "wall_slots": int(wall.sum()),
                           "fi": push39_inputs.digest(fi[other]), "gi": push39_inputs.digest(gi[other]),
                           "fi_wall": fi[wall].tolist(), "gi_wall": gi[wall].tolist()}
-        push_out[name]["consts"]["shifted"] = 1
+        push_out[name]["consts"]["shifted"] = int(sh)
     (HERE / "d3q39_push_golden.json").write_text(json.dumps(push_out, indent=0))
 
 

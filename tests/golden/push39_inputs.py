@@ -69,6 +69,36 @@ WALL_FACES = {"x-": -101, "x+": -201, "z-": -10, "z+": -1000, "y-": -10, "y+": -
 WNX, WNY, WNZ = 20, 6, 10
 
 
+def unshifted_wall_case(s39, seed=23, step=150):
+    """An unshifted box (Mach 0.5) with an inlet, an outlet of type 6, bounce-back floor
+    and side faces, a freestream top and a solid block whose fluid neighbours carry
+    interpolated wall links of seeded fractions; fields near the freestream, every
+    node's multipliers at the freestream solution."""
+    import math
+
+    c = s39.wedge_case_consts(v_inf_ms=0.5 * math.sqrt(1.4 * s39.GAS_CONST_R * 288.15), use_shifted=False)
+    faces = {"x-": -101, "x+": -201, "z-": -10, "z+": -1000, "y-": -10, "y+": -10}
+    st = s39.box_state39(WNX, WNY, WNZ, faces, 0, 1, periodic=0)
+    solid = np.zeros((WNZ, WNY, WNX), bool)
+    solid[0:3, 2:4, 8:11] = True
+    rs = np.random.RandomState(seed)
+    s39.wall_links39(st, solid, rs.uniform(0.05, 0.95, (39, WNZ, WNY, WNX)), 0, 1, periodic=0)
+    shape = (39, WNZ, WNY, WNX)
+    pops = [0.01 + 0.1 * rs.random_sample(shape) for _ in range(4)]
+    tabs = [0.01 + 0.1 * rs.random_sample(39) for _ in range(6)]
+    n3 = (WNZ, WNY, WNX)
+    fields = [1.0 + 0.02 * rs.uniform(-1, 1, n3), c.mach * (1 + 0.05 * rs.uniform(-1, 1, n3)),
+              0.02 * c.mach * rs.uniform(-1, 1, n3), 0.02 * c.mach * rs.uniform(-1, 1, n3),
+              c.temperature * (1 + 0.03 * rs.uniform(-1, 1, n3))]
+    lm0 = np.asarray(s39.freestream_start_lm(c), np.float64)
+    lm = np.broadcast_to(lm0[:, None, None, None], (13,) + n3).copy()
+    return c, {"state": st, "fout": pops[0], "gout": pops[1], "prev_f": pops[2], "prev_g": pops[3],
+               "ff": tabs[0], "gf": tabs[1], "fi": tabs[2], "gi": tabs[3], "fo": tabs[4], "go": tabs[5],
+               "inlet_type": [1] * 8, "outlet_type": [6] + [1] * 7, "periodic": 0, "shifted": 0,
+               "fields": fields, "lm": lm, "su_lm": list(c.su_lm), "fs_uvwT": (c.mach, 0.0, 0.0, c.temperature),
+               "step": step}
+
+
 def wall_case(name: str, s39):
     """The push-loop case dict (see case) plus the fields rho, u, v, w, T near the
     freestream, every node's multipliers at the freestream solution, the start-up

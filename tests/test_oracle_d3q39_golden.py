@@ -173,20 +173,25 @@ def test_shifted_wall_closure(o39):
 
 @pytest.mark.parametrize("name", sorted(n for n in PUSH if "fi_wall" in PUSH[n]))
 def test_push_loop_with_wall_links(o39, pkg, name):
-    """The push loop over the shifted lattice's double-ramp wedge with interpolated wall
-    links (target_finder at each wall node's first wall link, the target multiplier
-    solve from the start-up multipliers at timestep 0 or the node's own ones later, the
-    seven-point stencil and shifted_ibb), against streaming.f95 run through the
-    interpreter: every slot but the wall-link ones bit for bit; the wall-link slots,
-    whose multiplier and closure sums the oracle orders its own way, within 1e-13."""
+    """The push loop with interpolated wall links against streaming.f95 run through the
+    interpreter: the shifted lattice's double-ramp wedge (target_finder at each wall
+    node's first wall link, the target multiplier solve from the start-up multipliers at
+    timestep 0 or the node's own ones later, the seven-point stencil and shifted_ibb) and
+    an unshifted box with a solid block (interpolative_bounceback_bc's 38 closures):
+    every slot a wall closure cannot reach bit for bit; those it can (slots i and opp(i)
+    of wall link i), whose multiplier and closure sums the oracle orders its own way,
+    within 1e-13."""
     import sys
 
     sys.path.insert(0, str(GOLDEN.parent))
     import push39_inputs as P
 
     ref = PUSH[name]
-    k = o39.consts(pkg.d3q39_setup.wedge_case_consts())
-    cs = P.wall_case(name, pkg.d3q39_setup)
+    if name == "unshifted_walls":
+        c, cs = P.unshifted_wall_case(pkg.d3q39_setup)
+    else:
+        c, cs = pkg.d3q39_setup.wedge_case_consts(), P.wall_case(name, pkg.d3q39_setup)
+    k = o39.consts(c)
     lev = o39.Level39(P.WNX, P.WNY, P.WNZ)
     lev.fout[...], lev.gout[...], lev.lm[...] = cs["fout"], cs["gout"], cs["lm"]
     lev.rho[...], lev.u[...], lev.v[...], lev.w_vel[...], lev.temp[...] = cs["fields"]
@@ -197,6 +202,7 @@ def test_push_loop_with_wall_links(o39, pkg, name):
     fluid = cs["state"][0] >= 0
     wall = (cs["state"] <= -1001) & fluid[None]
     wall[0] = False
+    wall = wall | wall[pkg.d3q39_setup.lattice39(cs["shifted"], 1)[3]]
     assert int(fluid.sum()) == ref["fluid_nodes"] and int(wall.sum()) == ref["wall_slots"]
     other = fluid[None] & ~wall
     assert P.digest(pf[other]) == ref["fi"] and P.digest(pg[other]) == ref["gi"]
