@@ -20,6 +20,9 @@ Fortran statements (tests/golden/f95_subset.py interprets them in float64):
                         multiplier solve and shifted_ibb) on boxes of push39_inputs: digests of the
                         post-streaming fi, gi of the fluid nodes (the wall-link slots, whose closure sums
                         the oracle orders its own way, as values), written to d3q39_push_golden.json
+  explosion of a node   looping/timestepping/interlevel/interlevel_interpolation.f95 (the per-node block
+                        after the interpolation: coarse equilibrium for negative or NaN pairs, moments,
+                        multiplier solve, alpha)
   fout repair           looping/timestepping/damp_it.f95 (the reach and the in-place sweep of one box,
                         written to d3q39_damp_golden.json)
   transport             utilities/modules/quick_calcs.f95, amr_processes.f95 beta_1/2_calculator,
@@ -333,6 +336,42 @@ class Reference:
 
         return valid("fi"), valid("gi"), int(local["reach"])
 
+    def explode(self, root, f, g, crs_lm, crs_rho, crs_temp, step):
+        """interlevel_interpolation.f95's per-node block for one fine ghost node (state
+        1e7..1.1e9): the coarse multipliers, the interpolated f and g (each negative or NaN
+        pair replaced by the coarse equilibrium), the moments, the multiplier solve from the
+        coarse multipliers and alpha.  Returns f, g, the 13 multipliers, rho, u, v, w, T, alpha."""
+        lines = F.logical_lines((root / "looping/timestepping/interlevel/interlevel_interpolation.f95").read_text())
+        k_if = next(k for k, (no, s) in enumerate(lines)
+                    if re.match(r"^if \(state\(a,b,c,1\) >=\s*10000000 \.and\.", s))
+        block, _ = F.parse_stmt(lines, k_if)
+        local = {}
+        scope = self.interp.scope_for(local)
+        self.interp.declare("integer :: a,b,c,i,lvl", local, scope, set())
+        self.interp.declare("real(kind=dp) :: rho_sum,u_sum,v_sum,w_sum,energy_sum,v_mag,pxx,pyy,pzz,pxy,pxz,pyz,"
+                            "mu_c,mu_f,kappa_c,kappa_f,old_fi(dir),fieq_skip(dir),loc_fi_diff(dir)", local, scope,
+                            set())
+        node = lambda vals, dt=np.float64: F.FArray(np.asarray(vals, dt).reshape(1, 1, 1, -1).copy(), [1, 1, 1, 1])  # noqa: E731
+        one = lambda v: node([v])  # noqa: E731
+        nan = float("nan")
+        local.update(a=F.FInt(1), b=F.FInt(1), c=F.FInt(1), lvl=F.FInt(0), valid_interp_nodes=False,
+                     state=node([10000001] * 39, np.int64), fi=node(np.full(39, nan)), gi=node(np.full(39, nan)),
+                     crs_fi=node(f), crs_gi=node(g), crs_rho=one(crs_rho), crs_temp=one(crs_temp),
+                     rho=one(crs_rho), u_vel=one(nan), v_vel=one(nan), w_vel=one(nan), temp=one(crs_temp),
+                     alpha=one(nan))
+        for r, nm in enumerate(LM_NAMES):
+            local["crs_" + nm] = one(crs_lm[r])
+            local[nm] = one(nan)
+        self.set_step(step)
+        self.procs["lu_decomp"] = self.real_lu
+        try:
+            self.interp.run([block], local, scope)
+        finally:
+            self.procs["lu_decomp"] = self._lu_hook
+        v = lambda nm: local[nm].a.ravel().tolist()  # noqa: E731
+        return {"f": v("fi"), "g": v("gi"), "lm": [local[nm].a.ravel()[0] for nm in LM_NAMES],
+                "m5": [v(nm)[0] for nm in ("rho", "u_vel", "v_vel", "w_vel", "temp")], "alpha": v("alpha")[0]}
+
     def shifted_ibb(self, i, code_i, fieq_opp, gieq_opp, rho, tgt, ul, vl, wl, Tl, sp):
         """shifted_ibb.f95 for wall link i (1-based) of a node: its code of direction i, the
         equilibria of the closure's direction, rho, the (u, v, w, T) targets, the seven-point
@@ -476,6 +515,29 @@ def main(root: pathlib.Path) -> None:
                            "fi": fi_n.tolist(), "fs_temp": c.temperature,
                            "out": ref.targets(code, up, vp, wp, Tp, fi_n)})
         lat["targets"] = tcases
+        # interlevel_interpolation.f95's per-node explosion on seeded interpolants (some with a
+        # negative f and a NaN g, which take the coarse equilibrium)
+        rng_e = np.random.RandomState(99 + int(shifted))
+        lm_fs = s39.freestream_start_lm(c)
+        ecases = []
+        for n_case in range(6):
+            rho0, u0 = 1.0 + 0.02 * rng_e.uniform(-1, 1), c.mach * (1 + 0.05 * rng_e.uniform(-1, 1))
+            T0 = c.temperature * (1 + 0.02 * rng_e.uniform(-1, 1))
+            P0 = [rho0 * (T0 + u0 * u0), rho0 * T0 + 1e-4, rho0 * T0 - 1e-4, 1e-4, -1e-4, 0.0]
+            lm_c, fe, _ = ref.lagrange(rho0, u0, 0.01, -0.01, T0, P0, lm_fs)
+            lead = 2.0 * c.const_vol - 3
+            f = np.asarray(fe) * (1 + 0.03 * rng_e.uniform(-1, 1, 39))
+            g = lead * T0 * np.asarray(fe) * (1 + 0.03 * rng_e.uniform(-1, 1, 39))
+            if n_case >= 3:
+                f[rng_e.randint(0, 39)] = -0.01
+                g[rng_e.randint(0, 39)] = float("nan")
+            crs_rho, crs_T = rho0 * (1 + 0.01 * rng_e.uniform(-1, 1)), T0 * (1 + 0.01 * rng_e.uniform(-1, 1))
+            step = 3 if n_case % 2 == 0 else c.startup_timesteps + 30
+            r = ref.explode(root, f, g, lm_c, crs_rho, crs_T, step)
+            ecases.append({"f": [x if math.isfinite(x) else None for x in f.tolist()],
+                           "g": [x if math.isfinite(x) else None for x in g.tolist()], "lm": list(lm_c),
+                           "rho": crs_rho, "T": crs_T, "step": step, "out": r})
+        lat["explode"] = ecases
         if shifted:
             # shifted_ibb on seeded wall links: stencil node types interior, solid (-1001) or
             # null (-666), before and after the start-up ramps
