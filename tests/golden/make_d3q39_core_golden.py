@@ -23,6 +23,8 @@ Fortran statements (tests/golden/f95_subset.py interprets them in float64):
   explosion of a node   looping/timestepping/interlevel/interlevel_interpolation.f95 (the per-node block
                         after the interpolation: coarse equilibrium for negative or NaN pairs, moments,
                         multiplier solve, alpha)
+  GGM derivative        derivatives/modules/derivatives.f95:589-700 (derivative_windage_secondord and
+                        _firstord: central, upwind and downwind schemes)
   fout repair           looping/timestepping/damp_it.f95 (the reach and the in-place sweep of one box,
                         written to d3q39_damp_golden.json)
   transport             utilities/modules/quick_calcs.f95, amr_processes.f95 beta_1/2_calculator,
@@ -620,6 +622,19 @@ def main(root: pathlib.Path) -> None:
         recs.append({"jacobian": J.ravel().tolist(), "moments": moments, "lm_in": lm_in,
                      "lm_out": [lm[n] for n in LM_NAMES], "max_diff": md["v"]})
     out["lu_dense"] = recs
+    # derivative_windage_secondord (the GGM derivative), every combination of its four link
+    # states, the three schemes and both wind signs
+    wrec = []
+    for scheme in range(3):
+        up, down, cen = scheme == 1, scheme == 2, scheme == 0
+        for bits in range(16):
+            for wind in (0.37, -0.29):
+                q = [float(x) for x in rng.uniform(-1.0, 1.0, 5)]
+                st5 = [0] + [0 if (bits >> b) & 1 else -10 for b in range(4)]
+                dq = ref.interp.call("derivative_windage_secondord",
+                                     [F.FArray(np.array(q)), F.FArray(np.array(st5, np.int64)), wind, up, down, cen])
+                wrec.append({"scheme": scheme, "q": q, "state": st5, "wind": wind, "dq": float(dq)})
+    out["windage"] = wrec
     (HERE / "d3q39_core_golden.json").write_text(json.dumps(out))
     (HERE / "d3q39_damp_golden.json").write_text(json.dumps(damp_out))
     push_out = {}

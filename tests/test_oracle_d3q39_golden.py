@@ -294,6 +294,21 @@ def test_damp_sweep(o39, name):
         assert np.array_equal(out.ravel(), want), (key, int((out.ravel() != want).sum()))
 
 
+def test_ggm_derivative():
+    """The GGM restatement's derivative (oracle/ggm.py windage2) against
+    derivative_windage_secondord / _firstord of derivatives.f95 run through the
+    interpreter: every combination of the four link states, the central, upwind and
+    downwind schemes and both wind signs, bit for bit (the central form's sign and the
+    upwind forms' use of the minus-side values on the plus side included)."""
+    from oracle import ggm as og
+
+    assert len(DATA["windage"]) == 96
+    for r in DATA["windage"]:
+        s = r["state"]
+        got = og.windage2(r["q"], (s[1] >= 0, s[2] >= 0, s[3] >= 0, s[4] >= 0), r["wind"], r["scheme"])
+        assert got == r["dq"], r
+
+
 def test_lu_update_dense_bitwise_with_quirks(o39):
     """lu_decomp on dense matrices: the oracle matches bit for bit, and the
     golden results differ from a plain LU solve at O(1e-3) or more, so the
