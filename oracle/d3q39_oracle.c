@@ -17,9 +17,17 @@
  *   heat-flux corrections     component_subroutines/find_q_bar.f95:33-220, find_little_q_bar.f95:23-52
  *   transport / relaxation    utilities/modules/quick_calcs.f95:24-215, amr_processes.f95:1751-1814
  *   streaming (interior push) looping/timestepping/streaming.f95:266-369
- *   negative-population repair looping/timestepping/damp_it.f95:64-177 (fout part)
+ *   negative-population repair looping/timestepping/damp_it.f95:64-177 (fout and gout parts)
+ *   push loop with boundary links and wall links: streaming.f95:263-1161, target_finder.f95,
+ *                             shifted_ibb.f95, interpolative_bounceback_bc.f95, inviscid_edge.f95
+ *   fine-ghost explosion      looping/timestepping/interlevel/interlevel_interpolation.f95:364-440
  * The reference loops the Newton until max_diff <= 1e-7 with no cap; this
  * restatement adds a cap (counted, never hit in the tests).
+ *
+ * Pinned: tests/golden/make_d3q39_core_golden.py runs the reference's own
+ * statements through the f95_subset interpreter and tests/test_oracle_d3q39_golden.py
+ * holds these functions to the results (bit for bit where the operation order is the
+ * reference's).
  */
 #include <math.h>
 #include <stdint.h>
