@@ -26,7 +26,7 @@ Fortran statements (tests/golden/f95_subset.py interprets them in float64):
   GGM derivative        derivatives/modules/derivatives.f95:589-700 (derivative_windage_secondord and
                         _firstord: central, upwind and downwind schemes)
   fout repair           looping/timestepping/damp_it.f95 (the reach and the in-place sweep of one box,
-                        written to d3q39_damp_golden.json)
+                        fout and gout parts, written to d3q39_damp_golden.json)
   transport             utilities/modules/quick_calcs.f95, amr_processes.f95 beta_1/2_calculator,
                         epsilon_calculator
 
@@ -36,7 +36,14 @@ relaxation ramps) come from the package's host set-up of the wedge case (d3q39_s
 restates basic_fluids_calcs / viscosity_and_timing; they are inputs here and are stored with the
 case.
 
-Run: python make_d3q39_core_golden.py <reference root>   (writes d3q39_core_golden.json)
+Two statements of streaming.f95 are rewritten for the interpreter without changing what runs
+(see Reference.push), and three facts of the reference's set-up are stated rather than run:
+directions_and_weights sets nghosts_mid before it sets `shifted`, so the module's initial .false.
+gives nghosts_mid = 8; the periodic span and AMReX's ghost images are left out of the push boxes
+(their sweep order is a documented difference); the fi and gi parts of damp_it see positive values.
+
+Run: python make_d3q39_core_golden.py <reference root>
+     (writes d3q39_core_golden.json, d3q39_damp_golden.json and d3q39_push_golden.json)
 """
 from __future__ import annotations
 
