@@ -25,6 +25,8 @@ Fortran statements (tests/golden/f95_subset.py interprets them in float64):
                         multiplier solve, alpha)
   GGM derivative        derivatives/modules/derivatives.f95:589-700 (derivative_windage_secondord and
                         _firstord: central, upwind and downwind schemes)
+  predictive splitting  GGM/PGS/predictive_splitter.f95 (the loop over a box of pgs_inputs; ghost
+                        layers of node type -666, which no scan counts)
   fout repair           looping/timestepping/damp_it.f95 (the reach and the in-place sweep of one box,
                         fout and gout parts, written to d3q39_damp_golden.json)
   transport             utilities/modules/quick_calcs.f95, amr_processes.f95 beta_1/2_calculator,
@@ -59,6 +61,7 @@ import numpy as np
 HERE = pathlib.Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE))
 import damp39_inputs  # noqa: E402
+import pgs_inputs  # noqa: E402
 import push39_inputs  # noqa: E402
 import f95_subset as F  # noqa: E402
 
@@ -381,6 +384,36 @@ class Reference:
         return {"f": v("fi"), "g": v("gi"), "lm": [local[nm].a.ravel()[0] for nm in LM_NAMES],
                 "m5": [v(nm)[0] for nm in ("rho", "u_vel", "v_vel", "w_vel", "temp")], "alpha": v("alpha")[0]}
 
+    def pgs(self, root, ggm, u, v, w, s0, sensitivity, max_scan, G=8):
+        """GGM/PGS/predictive_splitter.f95's loop over one box (tux_lo = 0): ggm, u, v, w and
+        the node types s0 (nz, ny, nx) of the box; its FABs get G ghost layers of node type -666
+        (which no scan counts) and ggm 0.  Returns the tags (nz, ny, nx), 1 where set."""
+        lines = F.logical_lines((root / "GGM/PGS/predictive_splitter.f95").read_text())
+        k_loop = next(k for k, (no, s) in enumerate(lines) if re.match(r"^do c = tux_lo\(3\),tux_hi\(3\)$", s))
+        loop, _ = F.parse_stmt(lines, k_loop)
+        nz, ny, nx = s0.shape
+
+        def fab(arr, fill, dtype=np.float64, comps=1):
+            out = np.full((nx + 2 * G, ny + 2 * G, nz + 2 * G, comps), fill, dtype)
+            out[G:G + nx, G:G + ny, G:G + nz, 0] = np.transpose(arr, (2, 1, 0))
+            return F.FArray(out, [-G, -G, -G, 1])
+
+        local = {}
+        scope = self.interp.scope_for(local)
+        self.interp.declare("integer :: a,b,c,x,y,z,v,reach(6)", local, scope, set())
+        self.interp.declare("logical :: x_upwind,y_upwind,z_upwind,u_dominant,v_dominant,w_dominant,victory",
+                            local, scope, set())
+        tags = np.full((nx, ny, nz), "0", object)
+        st = fab(s0, -666, np.int64, 39)
+        local.update(g=F.FInt(1), settag="1", cleartag="0", pgs_limit=2 * sensitivity, pgs_upper=3 * sensitivity,
+                     tux_lo=F.FArray(np.array([0, 0, 0], np.int64)),
+                     tux_hi=F.FArray(np.array([nx - 1, ny - 1, nz - 1], np.int64)),
+                     tagarr=F.FArray(tags, [0, 0, 0]), state=st, ggm=fab(ggm, 0.0),
+                     u_vel=fab(u, 0.0), v_vel=fab(v, 0.0), w_vel=fab(w, 0.0))
+        self.g.update(pgs_max_scan=F.FInt(max_scan), ggm_sensitivity=sensitivity, nghosts=F.FInt(G))
+        self.interp.run([loop], local, scope)
+        return np.transpose(tags == "1", (2, 1, 0)).astype(np.uint8)
+
     def shifted_ibb(self, i, code_i, fieq_opp, gieq_opp, rho, tgt, ul, vl, wl, Tl, sp):
         """shifted_ibb.f95 for wall link i (1-based) of a node: its code of direction i, the
         equilibria of the closure's direction, rho, the (u, v, w, T) targets, the seven-point
@@ -642,6 +675,10 @@ def main(root: pathlib.Path) -> None:
                                      [F.FArray(np.array(q)), F.FArray(np.array(st5, np.int64)), wind, up, down, cen])
                 wrec.append({"scheme": scheme, "q": q, "state": st5, "wind": wind, "dq": float(dq)})
     out["windage"] = wrec
+    # predictive splitting over a box
+    ggm, u, v, w, s0 = pgs_inputs.case()
+    tags = ref.pgs(root, ggm, u, v, w, s0, pgs_inputs.SENSITIVITY, pgs_inputs.MAX_SCAN)
+    out["pgs"] = {"tagged": np.flatnonzero(tags.ravel()).tolist()}
     (HERE / "d3q39_core_golden.json").write_text(json.dumps(out))
     (HERE / "d3q39_damp_golden.json").write_text(json.dumps(damp_out))
     push_out = {}

@@ -309,6 +309,25 @@ def test_ggm_derivative():
         assert got == r["dq"], r
 
 
+def test_predictive_splitting():
+    """oracle/ggm.py's predictive splitting against predictive_splitter.f95's loop run
+    through the interpreter on a seeded box (dominant-velocity scans upstream and
+    downstream, the isotropic scans, solid nodes): the same tags."""
+    import sys
+
+    sys.path.insert(0, str(GOLDEN.parent))
+    import pgs_inputs as P
+    from oracle import ggm as og
+
+    ggm, u, v, w, s0 = P.case()
+    macro = np.stack([np.ones_like(u), u, v, w, np.ones_like(u)])
+    state = np.zeros((39,) + s0.shape, np.int32)
+    state[0] = s0
+    tags = np.zeros(s0.shape, np.uint8)
+    og.pgs_tags(tags, ggm, macro, state, P.SENSITIVITY, P.MAX_SCAN)
+    assert np.flatnonzero(tags.ravel()).tolist() == DATA["pgs"]["tagged"]
+
+
 def test_lu_update_dense_bitwise_with_quirks(o39):
     """lu_decomp on dense matrices: the oracle matches bit for bit, and the
     golden results differ from a plain LU solve at O(1e-3) or more, so the
