@@ -25,6 +25,7 @@ Fortran statements (tests/golden/f95_subset.py interprets them in float64):
                         multiplier solve, alpha)
   GGM derivative        derivatives/modules/derivatives.f95:589-700 (derivative_windage_secondord and
                         _firstord: central, upwind and downwind schemes)
+  gradient tags         GGM/derivatives/calculate_grad_mag.f95, calculate_gradgrad_mag.f95 (three schemes)
   predictive splitting  GGM/PGS/predictive_splitter.f95 (the loop over a box of pgs_inputs; ghost
                         layers of node type -666, which no scan counts)
   fout repair           looping/timestepping/damp_it.f95 (the reach and the in-place sweep of one box,
@@ -384,6 +385,47 @@ class Reference:
         return {"f": v("fi"), "g": v("gi"), "lm": [local[nm].a.ravel()[0] for nm in LM_NAMES],
                 "m5": [v(nm)[0] for nm in ("rho", "u_vel", "v_vel", "w_vel", "temp")], "alpha": v("alpha")[0]}
 
+    def ggm_box(self, root, q, u, v, w, state, scheme, limit, q_fs, G=8):
+        """calculate_grad_mag.f95's and calculate_gradgrad_mag.f95's loops over one box (tux_lo
+        = 0; PGS off): q (the variable), u, v, w and the 39 link codes of the box; its FABs get G
+        ghost layers holding q_fs, zero velocities and node type -666.  scheme 0 central,
+        1 upwind, 2 downwind.  Returns gm, ggm and the tags (nz, ny, nx) of the box."""
+        out = {}
+        for fname in ("calculate_grad_mag.f95", "calculate_gradgrad_mag.f95"):
+            lines = F.logical_lines((root / "GGM/derivatives" / fname).read_text())
+            k = next(k for k, (no, s) in enumerate(lines) if re.match(r"^do c = tux_lo\(3\)", s))
+            out[fname] = F.parse_stmt(lines, k)[0]
+            if fname.startswith("calculate_grad_mag"):
+                k_r = next(k for k, (no, s) in enumerate(lines) if s.startswith("reach = "))
+                out["reach"] = F.parse_stmt(lines, k_r)[0]
+        nz, ny, nx = q.shape
+
+        def fab(arr, fill, dtype=np.float64, comps=1):
+            o = np.full((nx + 2 * G, ny + 2 * G, nz + 2 * G, comps), fill, dtype)
+            t = np.transpose(arr, tuple(range(arr.ndim))[::-1])
+            o[G:G + nx, G:G + ny, G:G + nz, :] = t.reshape(nx, ny, nz, comps)
+            return F.FArray(o, [-G, -G, -G, 1])
+
+        local = {}
+        scope = self.interp.scope_for(local)
+        self.interp.declare("integer :: a,b,c,reach", local, scope, set())
+        self.interp.declare("real(kind=dp) :: x_der,y_der,z_der", local, scope, set())
+        tags = np.full((nx, ny, nz), "0", object)
+        local.update(g=F.FInt(1), lvl=F.FInt(0), settag="1", cleartag="0",
+                     tux_lo=F.FArray(np.array([0, 0, 0], np.int64)),
+                     tux_hi=F.FArray(np.array([nx - 1, ny - 1, nz - 1], np.int64)),
+                     tagarr=F.FArray(tags, [0, 0, 0]), state=fab(state, -666, np.int64, 39),
+                     holder=fab(q, q_fs), gm=fab(np.zeros_like(q), 0.0), ggm=fab(np.zeros_like(q), 0.0),
+                     u_vel=fab(u, 0.0), v_vel=fab(v, 0.0), w_vel=fab(w, 0.0))
+        self.g.update(upwind=scheme == 1, downwind=scheme == 2, central=scheme == 0, nghosts=F.FInt(6),
+                      ggm_tag_limit=F.FArray(np.array([limit]), [0]), use_pgs=False)
+        self.interp.run([out["reach"], out["calculate_grad_mag.f95"], out["calculate_gradgrad_mag.f95"]], local, scope)
+
+        def valid(nm):
+            return np.ascontiguousarray(np.transpose(local[nm].a[G:G + nx, G:G + ny, G:G + nz, 0], (2, 1, 0)))
+
+        return valid("gm"), valid("ggm"), np.transpose(tags == "1", (2, 1, 0)).astype(np.uint8)
+
     def pgs(self, root, ggm, u, v, w, s0, sensitivity, max_scan, G=8):
         """GGM/PGS/predictive_splitter.f95's loop over one box (tux_lo = 0): ggm, u, v, w and
         the node types s0 (nz, ny, nx) of the box; its FABs get G ghost layers of node type -666
@@ -679,6 +721,19 @@ def main(root: pathlib.Path) -> None:
     ggm, u, v, w, s0 = pgs_inputs.case()
     tags = ref.pgs(root, ggm, u, v, w, s0, pgs_inputs.SENSITIVITY, pgs_inputs.MAX_SCAN)
     out["pgs"] = {"tagged": np.flatnonzero(tags.ravel()).tolist()}
+    # the gradient magnitudes and the tags of calculate_grad_mag / calculate_gradgrad_mag: gm at
+    # every node of the box, ggm and the tags where the +-2 stencil stays inside it (the ghost
+    # nodes' gm, which the reference computes from the ghost layers, is left out)
+    gcases = []
+    for scheme in range(3):
+        rho, u, v, w, state, rho_fs = pgs_inputs.ggm_case(scheme)
+        gm, ggm, gtags = ref.ggm_box(root, rho, u, v, w, state, scheme, 0.05, rho_fs)
+        inner = np.zeros(rho.shape, bool)
+        inner[2:-2, 2:-2, 2:-2] = True
+        gcases.append({"scheme": scheme, "limit": 0.05, "gm": push39_inputs.digest(gm),
+                       "ggm_inner": push39_inputs.digest(ggm[inner]),
+                       "tagged_inner": np.flatnonzero(gtags[inner]).tolist()})
+    out["ggm"] = gcases
     (HERE / "d3q39_core_golden.json").write_text(json.dumps(out))
     (HERE / "d3q39_damp_golden.json").write_text(json.dumps(damp_out))
     push_out = {}

@@ -21,3 +21,16 @@ def case():
     w[dom == 2] *= 20
     s0 = np.where(rs.uniform(0, 1, shape) < 0.1, -1001, 0)
     return ggm, u, v, w, s0
+
+
+def ggm_case(scheme: int):
+    """rho (the tagged variable), u, v, w, the 39 link codes (10% of the links boundary
+    codes, 10% of the nodes solid or null) and the freestream rho of the gradient case."""
+    rs = np.random.RandomState(300 + scheme)
+    shape = (NZ, NY, NX)
+    rho = 1.0 + 0.05 * rs.uniform(-1, 1, shape) + 0.2 * (rs.uniform(0, 1, shape) < 0.05)
+    u, v, w = (rs.uniform(-1, 1, shape) for _ in range(3))
+    state = np.where(rs.uniform(0, 1, (39,) + shape) < 0.1, -10, 0).astype(np.int32)
+    node = rs.uniform(0, 1, shape)
+    state[0] = np.where(node < 0.05, -1001, np.where(node < 0.1, -666, 0))
+    return rho, u, v, w, state, 1.0

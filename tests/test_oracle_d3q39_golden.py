@@ -309,6 +309,29 @@ def test_ggm_derivative():
         assert got == r["dq"], r
 
 
+def test_ggm_gradients():
+    """oracle/ggm.py's gradient magnitudes and tags against calculate_grad_mag.f95 and
+    calculate_gradgrad_mag.f95 run through the interpreter on seeded boxes (boundary
+    links, solid and null nodes; central, upwind and downwind schemes): gm at every node
+    and ggm and the tags where the +-2 stencil stays inside the box, bit for bit."""
+    import sys
+
+    sys.path.insert(0, str(GOLDEN.parent))
+    import pgs_inputs as P
+    import push39_inputs as Q
+    from oracle import ggm as og
+
+    for ref in DATA["ggm"]:
+        rho, u, v, w, state, rho_fs = P.ggm_case(ref["scheme"])
+        macro = np.stack([rho, u, v, w, np.ones_like(rho)])
+        tags, ggm, gm = og.ggm_tags(macro, state, 0, 1, ref["scheme"], ref["limit"], (rho_fs, 0.0, 0.0, 0.0, 1.0))
+        inner = np.zeros(rho.shape, bool)
+        inner[2:-2, 2:-2, 2:-2] = True
+        assert Q.digest(gm) == ref["gm"]
+        assert Q.digest(ggm[inner]) == ref["ggm_inner"]
+        assert np.flatnonzero(tags[inner]).tolist() == ref["tagged_inner"]
+
+
 def test_predictive_splitting():
     """oracle/ggm.py's predictive splitting against predictive_splitter.f95's loop run
     through the interpreter on a seeded box (dominant-velocity scans upstream and
