@@ -11,7 +11,15 @@ block and logical IF; DO (counted, WHILE, bare) with EXIT / CYCLE; SELECT
 CASE (values, ranges, DEFAULT); CALL with by-reference arguments; RETURN;
 ALLOCATE / DEALLOCATE; array constructors (/ ... /); intrinsics (ABS, SQRT,
 EXP, LOG, MAX, MIN, SUM, REAL, DBLE, INT, NINT, FLOOR, MOD, ISNAN, SIGN,
-MAXVAL, MINVAL, SIZE, PRESENT).  WRITE, PRINT, FORMAT and USE are no-ops.
+MAXVAL, MINVAL, SIZE, PRESENT, ANY, ALL) and elementwise comparisons of
+array sections.  WRITE, PRINT, FORMAT and USE are no-ops; statement labels
+are dropped (a caller rewrites the one GO TO it meets).
+
+Arguments are passed as by reference: scalars and array elements are copied
+in and written back only when the procedure assigned them (two dummies may
+name one actual element, as outlet_bc's do on the shifted lattice), whole
+arrays are shared, and an explicit-shape dummy array takes its declared
+shape and bounds over the actual's elements (sequence association).
 
 Arithmetic follows Fortran where the routines depend on it: integer / integer
 truncates toward zero, and a real literal without a D exponent is a default
