@@ -235,7 +235,7 @@ def inviscid(i, codes):
 
 def step_links_damp(k: O39Consts, lev: Level39, step: int, state: np.ndarray, periodic: int, b: O39Bc,
                     fi_prev: np.ndarray, gi_prev: np.ndarray, lo, hi):
-    """step_links, then the fout part of damp_it on the box (lo, hi: its index-space corners)."""
+    """step_links, then the fout and gout parts of damp_it on the box (lo, hi: its index-space corners)."""
     L = lib()
     if not getattr(L, "_o39_damp_ready", False):
         L.o39_step_links_damp.restype = ct.c_int
