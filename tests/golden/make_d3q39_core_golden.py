@@ -599,6 +599,21 @@ def main(root: pathlib.Path) -> None:
                            "fi": fi_n.tolist(), "fs_temp": c.temperature,
                            "out": ref.targets(code, up, vp, wp, Tp, fi_n)})
         lat["targets"] = tcases
+        # calculate_alpha across its branches: deviations from equilibrium scaled from tiny (alpha =
+        # 2 below the chi_3 threshold) to large (the quadratic root clamped to [alpha_sum_min, 2.125])
+        rng_a = np.random.RandomState(6060 + int(shifted))
+        lm_fs = s39.freestream_start_lm(c)
+        _, fe_a, _ = ref.lagrange(1.0, c.mach, 0.0, 0.0, c.temperature,
+                                  [c.temperature + c.mach ** 2, c.temperature, c.temperature, 0.0, 0.0, 0.0], lm_fs)
+        acases = []
+        for scale in (1e-12, 1e-6, 1e-3, 0.02, 0.1, 0.3, 0.6, 0.9):
+            for step in (3, c.startup_timesteps + 5):
+                fd = np.asarray(fe_a) * scale * rng_a.uniform(-1, 1, 39)
+                f = (np.asarray(fe_a) - fd).tolist()
+                ref.set_step(step)
+                a = ref.alpha(f, fd.tolist(), c.temperature)
+                acases.append({"f": f, "fd": fd.tolist(), "T": c.temperature, "step": step, "alpha": a})
+        lat["alpha_branches"] = acases
         # interlevel_interpolation.f95's per-node explosion on seeded interpolants (some with a
         # negative f and a NaN g, which take the coarse equilibrium)
         rng_e = np.random.RandomState(99 + int(shifted))

@@ -147,6 +147,21 @@ def test_flow_variables(o39, name):
 
 
 @pytest.mark.parametrize("name", LATTICES)
+def test_alpha_branches(o39, name):
+    """calculate_alpha.f95 on deviations from equilibrium scaled from 1e-12 to 0.9 of the
+    populations, before and after the start-up ramp: the alpha = 2 branch below the chi_3
+    threshold, the quadratic root and its clamps, within 1e-12."""
+    lat = DATA["lattices"][name]
+    k = _consts(o39, lat)
+    seen = set()
+    for c in lat["alpha_branches"]:
+        a = o39.alpha(k, np.array(c["f"]), np.array(c["fd"]), c["T"], c["step"])
+        assert abs(a - c["alpha"]) <= 1e-12, (a, c["alpha"], c["step"])
+        seen.add(round(c["alpha"], 12) == 2.0)
+    assert seen == {True, False}
+
+
+@pytest.mark.parametrize("name", LATTICES)
 def test_wall_targets(o39, name):
     """target_finder.f95's rho, u, v, w, T targets of a wall node from its link codes,
     the fields at x + c_j and its slots (unshifted: the node across a fluid opposite
