@@ -106,7 +106,8 @@ typedef struct {
 typedef struct {
   int64_t node_updates;     /* fluid nodes advanced, summed over steps */
   int64_t newton_iters;     /* total Newton iterations (scalar or per-population) */
-  int64_t exact_path_nodes; /* FP32 path: nodes with some |Delta_i/f_i| > 0.1 (solved out of line) */
+  int64_t exact_path_nodes; /* D3Q27 FP32 path: nodes with some |Delta_i/f_i| > 0.1 (solved out of line);
+                               D3Q39 with damp = 1: negative f and g populations the repair met */
   int64_t fallbacks;        /* alpha solves that fell back */
   uint32_t status;          /* ELBM_ST_* flags */
   uint32_t pad;
