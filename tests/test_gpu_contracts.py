@@ -18,7 +18,7 @@ past its start-up ramps.
   path from an FP32-rounded start stays within 1e-7, so this is not chaos);
 - D3Q39 384x48x192 Mach 1.5 wedge (48-node span between inviscid side walls,
   lattice viscosity 2e-4, the negative-population repair after every step),
-  300 steps (three times the start-up ramp), FP64 and FP32 deviation storage
+  150 steps (one and a half times the start-up ramp), FP64 and FP32 deviation storage
   of f and g (multipliers, alpha and all arithmetic FP64): finite fields, no
   multiplier solve capped, no fallbacks, and the FP32 path's errors in rho, u,
   T and alpha against the FP64 path beside the FP64 path's own spread from
@@ -186,16 +186,20 @@ def _wedge_errors(c, a, b, fluid):
     return e
 
 
-def test_d3q39_wedge_fp32_vs_fp64_300_steps(pkg, built_lib):
+def test_d3q39_wedge_fp32_vs_fp64_150_steps(pkg, built_lib):
     """The D3Q39 wedge (384x48x192, Mach 1.5) with FP32 deviation storage of f and g
-    (FP64 multipliers, alpha and arithmetic) against the FP64 path, 300 steps (three
-    times the start-up ramp): the errors in rho, u, T and alpha at the fluid nodes.
+    (FP64 multipliers, alpha and arithmetic) against the FP64 path, 150 steps (past the
+    start-up ramp): the errors in rho, u, T and alpha at the fluid nodes.  With the
+    reference's inviscid reflections and the repair of f and g, the oracle's FP64 step of
+    this case stays finite with no multiplier solve capped through step 200 and goes
+    non-finite between steps 200 and 250 (lattice viscosity 2e-4 is near the limit), so
+    the comparison stops well before that.
     The flow's own sensitivity is measured the same way: the FP64 path from an
     initial state whose fields carry 1-ulp noise.  Past the start-up the shocks
     and the outflow corner amplify any rounding, so the FP32 path is held to three
     times that spread (rms and max), and never looser than 1e-4."""
     cap = pkg.capi
-    steps = 300
+    steps = 150
     c, o64, fluid, s64 = _wedge(pkg, cap.ELBM_STORE_FP64, steps)
     _, o32, _, s32 = _wedge(pkg, cap.ELBM_STORE_FP32_DEV, steps)
     _, p64, _, _ = _wedge(pkg, cap.ELBM_STORE_FP64, steps, perturb=2.2e-16)
